@@ -1,0 +1,38 @@
+"""GB300 (sm_103a) backend for ImageFiltering.jl's FIR and rank-filter path.
+
+Python mirror of the reference API over the C ABI in include/ifx_gb300.h:
+
+    imfilter, imfilter_ (imfilter!), imgradients, mapwindow, mapwindow_
+    (mapwindow!), padarray, Pad, Fill, Kernel, KernelFactors, centered,
+    Algorithm (with the new tag Algorithm.GB300)
+
+Arrays use Julia's memory order (Fortran-ordered numpy arrays on the host,
+``DeviceArray`` for device-resident data).  Every result is computed by the
+CUDA kernels of ``_build/libifx_gb300.so``; there is no CPU fallback, and the
+functions raise if the library is missing.
+"""
+from . import _abi
+from ._abi import (ArgumentError, DimensionMismatch, ErrorException, CudaError, OutOfMemory,
+                   Unsupported, launch_count)
+from .arrays import DeviceArray, N0f8Array, n0f8
+from .borders import Fill, Inner, NA, Pad, borderinstance, padarray
+from .filtering import Algorithm, factorkernel, filter_type, imfilter, imfilter_, imgradients
+from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD, centered,
+                      iscopy, kernelfactors)
+from .rank import extrema, mapwindow, mapwindow_, maximum, median, median_, minimum
+
+OffsetArray = OffsetKernel
+
+
+def library_path() -> str:
+    return _abi.LIB_PATH
+
+
+__all__ = [
+    "imfilter", "imfilter_", "imgradients", "mapwindow", "mapwindow_", "padarray", "Pad", "Fill",
+    "Inner", "NA", "Kernel", "KernelFactors", "centered", "kernelfactors", "Algorithm",
+    "OffsetArray", "OffsetKernel", "ReshapedOneD", "LaplacianKernel", "DeviceArray", "N0f8Array",
+    "n0f8", "median", "median_", "extrema", "minimum", "maximum", "filter_type", "factorkernel",
+    "iscopy", "borderinstance", "ArgumentError", "DimensionMismatch", "ErrorException",
+    "CudaError", "OutOfMemory", "Unsupported", "launch_count", "library_path",
+]

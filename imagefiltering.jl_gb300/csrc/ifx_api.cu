@@ -1,0 +1,883 @@
+// ifx_api.cu -- the C ABI (include/ifx_gb300.h): argument validation with the
+// reference's error classes, host<->device staging, scratch management and
+// dispatch to the sm_103a kernels.  No CPU compute path exists: every result
+// is produced by a kernel of this library.
+#include "ifx_internal.h"
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace ifx {
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+size_t sep2d_smem_bytes(int kx, int ky, int x_first, int f64);
+size_t dense2d_smem_bytes(int kw, int kh, int f64);
+
+static thread_local std::string t_err;
+
+static int fail(int code, const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    static const char *cls[] = {"", "ArgumentError: ", "DimensionMismatch: ", "ErrorException: ",
+                                "CUDA error: ", "OutOfMemory: ", "Timeout: ", "Unsupported: "};
+    t_err = std::string(code >= 0 && code <= 7 ? cls[code] : "") + buf;
+    return code;
+}
+
+#define IFX_CUDA(call)                                                                         \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) return fail(IFX_ERR_CUDA, "%s (%s:%d)", cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                \
+    } while (0)
+
+static size_t elsize(int t)
+{
+    switch (t) {
+    case IFX_F32: return 4;
+    case IFX_F64: return 8;
+    case IFX_N0F8:
+    case IFX_U8: return 1;
+    case IFX_I16: return 2;
+    default: return 0;
+    }
+}
+static bool is8(int t) { return t == IFX_N0F8 || t == IFX_U8; }
+
+// ------------------------------------------------------------------ context
+struct Slot {
+    void *ptr = nullptr;
+    size_t cap = 0;
+};
+
+} // namespace ifx
+
+struct ifx_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    ifx::Slot slots[24];
+};
+
+namespace ifx {
+
+enum { kSlotIn = 0, kSlotOut = 1, kSlotTmp = 12 };
+
+static int slot_get(ifx_context *c, int i, size_t bytes, void **out)
+{
+    Slot &s = c->slots[i];
+    if (s.cap < bytes) {
+        if (s.ptr) {
+            IFX_CUDA(cudaDeviceSynchronize());
+            IFX_CUDA(cudaFree(s.ptr));
+            s.ptr = nullptr;
+            s.cap = 0;
+        }
+        size_t want = bytes < 256 ? 256 : bytes;
+        cudaError_t e = cudaMalloc(&s.ptr, want);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            s.ptr = nullptr;
+            return fail(IFX_ERR_NOMEM, "device allocation of %zu bytes failed", want);
+        }
+        s.cap = want;
+    }
+    *out = s.ptr;
+    return IFX_OK;
+}
+
+// ------------------------------------------------------------------ arrays
+static long long numel(const ifx_array_t &a)
+{
+    long long n = 1;
+    for (int d = 0; d < a.ndim; ++d) n *= a.size[d];
+    return n;
+}
+
+static int check_array(const ifx_array_t *a, const char *name, int values_per_elem = 1)
+{
+    if (!a) return fail(IFX_ERR_ARGUMENT, "%s is NULL", name);
+    if (a->ndim < 1 || a->ndim > IFX_MAX_DIMS)
+        return fail(IFX_ERR_ARGUMENT, "%s: ndims %d not in 1..%d", name, a->ndim, IFX_MAX_DIMS);
+    if (elsize(a->eltype) == 0) return fail(IFX_ERR_ARGUMENT, "%s: unknown eltype %d", name, a->eltype);
+    long long s = 1;
+    for (int d = 0; d < a->ndim; ++d) {
+        if (a->size[d] < 0) return fail(IFX_ERR_ARGUMENT, "%s: negative size", name);
+        if (a->size[d] > (1LL << 30))
+            return fail(IFX_ERR_UNSUPPORTED, "%s: axis %d longer than 2^30", name, d);
+        if (a->size[d] > 1 && a->stride[d] != s)
+            return fail(IFX_ERR_ARGUMENT, "%s: only dense column-major arrays are supported "
+                        "(axis %d stride %lld, expected %lld)", name, d, (long long)a->stride[d], s);
+        s *= a->size[d];
+    }
+    (void)values_per_elem;
+    if (s > 0 && !a->data) return fail(IFX_ERR_ARGUMENT, "%s: data is NULL", name);
+    return IFX_OK;
+}
+
+static int check_same_axes(const ifx_array_t &out, const ifx_array_t &img)
+{
+    if (out.ndim != img.ndim)
+        return fail(IFX_ERR_DIMENSION, "output has %d dimensions, input %d", out.ndim, img.ndim);
+    for (int d = 0; d < img.ndim; ++d)
+        if (out.size[d] != img.size[d] || out.first[d] != img.first[d])
+            return fail(IFX_ERR_DIMENSION, "output indices disagree with the input's on axis %d "
+                        "(%lld:%lld vs %lld:%lld)", d + 1, (long long)out.first[d],
+                        (long long)(out.first[d] + out.size[d] - 1), (long long)img.first[d],
+                        (long long)(img.first[d] + img.size[d] - 1));
+    return IFX_OK;
+}
+
+static bool is_device_ptr(const void *p)
+{
+    if (!p) return false;
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, p);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+// Staging of one call's arrays: host arrays are copied to scratch slots.
+struct Call {
+    ifx_context *ctx;
+    cudaStream_t s;
+    bool host = false;                  // any host array -> synchronous call
+    struct Back { void *host; void *dev; size_t bytes; };
+    std::vector<Back> back;
+    int next_slot = kSlotIn;
+
+    int input(const ifx_array_t &a, const void **dptr, size_t bytes_override = 0)
+    {
+        const size_t bytes = bytes_override ? bytes_override : (size_t)numel(a) * elsize(a.eltype);
+        if (bytes == 0 || is_device_ptr(a.data)) {
+            *dptr = a.data;
+            return IFX_OK;
+        }
+        host = true;
+        void *d;
+        int rc = slot_get(ctx, next_slot++, bytes, &d);
+        if (rc) return rc;
+        IFX_CUDA(cudaMemcpyAsync(d, a.data, bytes, cudaMemcpyHostToDevice, s));
+        *dptr = d;
+        return IFX_OK;
+    }
+    int output(const ifx_array_t &a, void **dptr, size_t bytes_override = 0)
+    {
+        const size_t bytes = bytes_override ? bytes_override : (size_t)numel(a) * elsize(a.eltype);
+        if (bytes == 0 || is_device_ptr(a.data)) {
+            *dptr = a.data;
+            return IFX_OK;
+        }
+        host = true;
+        void *d;
+        int rc = slot_get(ctx, next_slot++, bytes, &d);
+        if (rc) return rc;
+        back.push_back({a.data, d, bytes});
+        *dptr = d;
+        return IFX_OK;
+    }
+    int finish()
+    {
+        IFX_CUDA(cudaGetLastError());
+        for (auto &b : back) IFX_CUDA(cudaMemcpyAsync(b.host, b.dev, b.bytes, cudaMemcpyDeviceToHost, s));
+        if (host) IFX_CUDA(cudaStreamSynchronize(s));
+        return IFX_OK;
+    }
+};
+
+static int begin(ifx_context *ctx, void *stream, Call &c)
+{
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    IFX_CUDA(cudaSetDevice(ctx->device));
+    c.ctx = ctx;
+    c.s = stream ? (cudaStream_t)stream : ctx->stream;
+    return IFX_OK;
+}
+
+// ------------------------------------------------------------------ borders
+static int check_border(const ifx_border_t *b)
+{
+    if (!b) return fail(IFX_ERR_ARGUMENT, "border is NULL");
+    if (b->style < IFX_REPLICATE || b->style > IFX_FILL)
+        return fail(IFX_ERR_ARGUMENT, "border style %d not a recognized border", b->style);
+    return IFX_OK;
+}
+
+// The reference builds every padindex table, so reflect on a length-1 axis is
+// a DivideError (src/border.jl:581-586: period 2n-2 == 0).
+static int check_reflect(const ifx_border_t *b, const ifx_array_t &img)
+{
+    if (b->style != IFX_REFLECT) return IFX_OK;
+    for (int d = 0; d < img.ndim; ++d)
+        if (img.size[d] == 1)
+            return fail(IFX_ERR_ERROR, "DivideError: integer division error (reflect padding of a "
+                        "length-1 axis %d)", d + 1);
+    return IFX_OK;
+}
+
+// Padding needed per axis (src/border.jl:614-621, 637-641) against an explicit
+// Pad/Fill (src/imfilter.jl:604-615 raises DimensionMismatch when too small).
+static int check_padding(const ifx_border_t *b, const ifx_array_t &img, const long long *pfirst,
+                         const long long *plast)
+{
+    if (!b->explicit_pad) return IFX_OK;
+    for (int d = 0; d < img.ndim; ++d) {
+        long long need_lo = pfirst[d] < 0 ? -pfirst[d] : 0;
+        long long need_hi = plast[d] > 0 ? plast[d] : 0;
+        if (b->lo[d] < need_lo || b->hi[d] < need_hi)
+            return fail(IFX_ERR_DIMENSION, "requested indices and kernel indices %lld:%lld do not "
+                        "agree with indices of padded input (axis %d padded by %lld,%lld)",
+                        pfirst[d], plast[d], d + 1, (long long)b->lo[d], (long long)b->hi[d]);
+    }
+    return IFX_OK;
+}
+
+// Fill value in the element domain of type t (8-bit: the code).
+static int fill_for(const ifx_border_t *b, int t, double *out)
+{
+    double v = b->style == IFX_FILL ? b->fill_value : 0.0;
+    if (is8(t)) {
+        double code = t == IFX_N0F8 ? v * 255.0 : v;
+        double r = std::nearbyint(code);
+        if (!(r >= 0.0 && r <= 255.0) || std::fabs(r - code) > 1e-6)
+            return fail(IFX_ERR_ARGUMENT, "Cannot convert elements of border=Fill(%g) to the 8-bit "
+                        "image eltype", v);
+        *out = r;
+        return IFX_OK;
+    }
+    *out = v;
+    return IFX_OK;
+}
+
+// Fill converted as BorderArray does (to the image eltype, src/borderarray.jl:
+// 11-20), then expressed in the destination's domain: the 8-bit code for 8-bit
+// destinations, the numeric value otherwise.
+static int image_fill(const ifx_border_t *b, int img_type, int dst_type, double *out)
+{
+    double v;
+    int rc = fill_for(b, img_type, &v);
+    if (rc) return rc;
+    if (is8(img_type) && !is8(dst_type)) v = img_type == IFX_N0F8 ? v / 255.0 : v;
+    *out = v;
+    return IFX_OK;
+}
+
+static Box image_box(const ifx_array_t &a)
+{
+    int lo[IFX_MAXD] = {0, 0, 0, 0}, sz[IFX_MAXD];
+    for (int d = 0; d < IFX_MAXD; ++d) sz[d] = d < a.ndim ? (int)a.size[d] : 1;
+    return make_box(a.ndim, lo, sz);
+}
+
+// ------------------------------------------------------------------ cascade
+struct Fac { int axis, first, len; const double *w; };
+
+static bool is_copy(const ifx_factor_t &f)
+{
+    return f.length == 1 && f.first == 0 && f.weights[0] == 1.0;
+}
+
+// Cascade over device arrays.  img/out are device pointers.
+static int run_cascade(Call &c, const ifx_array_t &imgd, const void *img, const ifx_array_t &outd,
+                       void *out, const std::vector<Fac> &facs, const ifx_border_t *border,
+                       int tmp_slot_base)
+{
+    const int nd = imgd.ndim;
+    const int ct = imgd.eltype == IFX_F64 ? IFX_F64 : IFX_F32;   // compute type
+    const size_t cs = elsize(ct);
+    double fill;
+    int rc = image_fill(border, imgd.eltype, ct, &fill);
+    if (rc) return rc;
+    int n[IFX_MAXD];
+    for (int d = 0; d < IFX_MAXD; ++d) n[d] = d < nd ? (int)imgd.size[d] : 1;
+
+    if (facs.empty()) {   // all copies: convert into out
+        PadBoxArgs pa{img, imgd.eltype, out, outd.eltype, nd, {n[0], n[1], n[2], n[3]},
+                      image_box(imgd), IFX_REPLICATE, 0.0};
+        IFX_CUDA(launch_pad_box(pa, c.s));
+        return IFX_OK;
+    }
+
+    // fast path: 1-D / 2-D with at most one factor per axis -> fused tile kernel
+    bool fused = nd <= 2 && facs.size() <= 2 &&
+                 !(facs.size() == 2 && facs[0].axis == facs[1].axis);
+    if (fused) {
+        static const double one = 1.0;
+        Fac fx{0, 0, 1, &one}, fy{1, 0, 1, &one};
+        int x_first = 1;
+        for (size_t i = 0; i < facs.size(); ++i) (facs[i].axis == 0 ? fx : fy) = facs[i];
+        if (facs.size() == 2) x_first = facs[0].axis == 0;
+        else x_first = facs[0].axis == 0 ? 1 : 0;
+        if (sep2d_smem_bytes(fx.len, fy.len, x_first, ct == IFX_F64) > 200 * 1024) fused = false;
+        if (fused) {
+            Sep2dArgs a{img, imgd.eltype, out, outd.eltype, n[0], nd > 1 ? n[1] : 1,
+                        fx.first, fx.len, fy.first, fy.len, fx.w, fy.w, x_first,
+                        border->style, fill, ct == IFX_F64};
+            IFX_CUDA(launch_sep2d(a, c.s));
+            return IFX_OK;
+        }
+    }
+
+    // generic: materialise the padded box in the compute type, then passes
+    long long pfirst[IFX_MAXD] = {0, 0, 0, 0}, plast[IFX_MAXD] = {0, 0, 0, 0};
+    for (auto &f : facs) {
+        pfirst[f.axis] += f.first;
+        plast[f.axis] += f.first + f.len - 1;
+    }
+    int blo[IFX_MAXD], bsz[IFX_MAXD];
+    for (int d = 0; d < IFX_MAXD; ++d) {
+        blo[d] = d < nd ? (int)pfirst[d] : 0;
+        bsz[d] = d < nd ? (int)(n[d] + plast[d] - pfirst[d]) : 1;
+    }
+    Box cur = make_box(nd, blo, bsz);
+    void *bufA, *bufB;
+    rc = slot_get(c.ctx, tmp_slot_base, (size_t)cur.count * cs, &bufA);
+    if (rc) return rc;
+    PadBoxArgs pa{img, imgd.eltype, bufA, ct, nd, {n[0], n[1], n[2], n[3]}, cur, border->style, fill};
+    IFX_CUDA(launch_pad_box(pa, c.s));
+    int slo[IFX_MAXD], shi[IFX_MAXD];
+    for (int d = 0; d < IFX_MAXD; ++d) {
+        slo[d] = blo[d];
+        shi[d] = blo[d] + bsz[d] - 1;
+    }
+    const void *src = bufA;
+    int which = 1;
+    for (size_t q = 0; q < facs.size(); ++q) {
+        const Fac &f = facs[q];
+        slo[f.axis] -= f.first;
+        shi[f.axis] -= f.first + f.len - 1;
+        int olo[IFX_MAXD], osz[IFX_MAXD];
+        for (int d = 0; d < IFX_MAXD; ++d) {
+            olo[d] = slo[d];
+            osz[d] = shi[d] - slo[d] + 1;
+        }
+        Box ob = make_box(nd, olo, osz);
+        const bool last = q + 1 == facs.size();
+        void *dst;
+        Box db;
+        int dtype;
+        if (last) {
+            dst = out;
+            db = image_box(imgd);
+            dtype = outd.eltype;
+        } else {
+            rc = slot_get(c.ctx, tmp_slot_base + which, (size_t)ob.count * cs, &bufB);
+            if (rc) return rc;
+            dst = bufB;
+            db = ob;
+            dtype = ct;
+            which = 1 - which;
+        }
+        PassBoxArgs pb{src, cur, dst, db, dtype, ob, f.axis, f.first, f.len, f.w, ct == IFX_F64};
+        IFX_CUDA(launch_pass_box(pb, c.s));
+        src = dst;
+        cur = db;
+    }
+    return IFX_OK;
+}
+
+static int check_filter_types(const ifx_array_t &img, const ifx_array_t &out)
+{
+    if (img.eltype == IFX_I16) return fail(IFX_ERR_UNSUPPORTED, "Int16 images are not supported");
+    if (out.eltype != IFX_F32 && out.eltype != IFX_F64)
+        return fail(IFX_ERR_UNSUPPORTED, "linear filters write Float32 or Float64 outputs");
+    return IFX_OK;
+}
+
+} // namespace ifx
+
+using namespace ifx;
+
+// =========================================================================
+// C ABI
+// =========================================================================
+extern "C" {
+
+int ifx_abi_version(void) { return IFX_ABI_VERSION; }
+
+const char *ifx_last_error(void) { return t_err.c_str(); }
+
+uint64_t ifx_launch_count(void) { return g_launches.load(); }
+
+int ifx_create(ifx_context_t **ctx, int device)
+{
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "ctx is NULL");
+    *ctx = nullptr;
+    int ndev = 0;
+    IFX_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(IFX_ERR_ARGUMENT, "device %d out of range", device);
+    IFX_CUDA(cudaSetDevice(device));
+    auto *c = new ifx_context();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(IFX_ERR_CUDA, "%s", cudaGetErrorString(e));
+    }
+    *ctx = c;
+    return IFX_OK;
+}
+
+int ifx_destroy(ifx_context_t *ctx)
+{
+    if (!ctx) return IFX_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &s : ctx->slots)
+        if (s.ptr) cudaFree(s.ptr);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return IFX_OK;
+}
+
+int ifx_synchronize(ifx_context_t *ctx, void *stream)
+{
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    IFX_CUDA(cudaSetDevice(ctx->device));
+    IFX_CUDA(cudaStreamSynchronize(stream ? (cudaStream_t)stream : ctx->stream));
+    return IFX_OK;
+}
+
+int ifx_padarray(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                 const ifx_border_t *border, void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
+        return rc;
+    if (!border->explicit_pad)
+        return fail(IFX_ERR_ARGUMENT, "border lacks the proper padding sizes for an array with %d "
+                    "dimensions", img->ndim);
+    if (out->ndim != img->ndim) return fail(IFX_ERR_DIMENSION, "output dimensionality differs");
+    for (int d = 0; d < img->ndim; ++d) {
+        if (border->lo[d] < 0 || border->hi[d] < 0)
+            return fail(IFX_ERR_ARGUMENT, "negative padding");
+        if (out->size[d] != img->size[d] + border->lo[d] + border->hi[d])
+            return fail(IFX_ERR_DIMENSION, "output size on axis %d must be lo+n+hi", d + 1);
+    }
+    if (is8(out->eltype) != is8(img->eltype) && is8(out->eltype))
+        return fail(IFX_ERR_UNSUPPORTED, "padarray to an 8-bit eltype from a float eltype");
+    if (out->eltype == IFX_I16 || img->eltype == IFX_I16)
+        return fail(IFX_ERR_UNSUPPORTED, "Int16 arrays");
+    if (numel(*out) == 0) return IFX_OK;
+    if (numel(*img) == 0) return fail(IFX_ERR_ERROR, "cannot pad an empty array");
+    if ((rc = check_reflect(border, *img))) return rc;
+    double fill;
+    if ((rc = image_fill(border, img->eltype, out->eltype, &fill))) return rc;
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *dout;
+    if ((rc = c.input(*img, &din)) || (rc = c.output(*out, &dout))) return rc;
+    int lo[IFX_MAXD], sz[IFX_MAXD], n[IFX_MAXD];
+    for (int d = 0; d < IFX_MAXD; ++d) {
+        lo[d] = d < img->ndim ? -(int)border->lo[d] : 0;
+        sz[d] = d < img->ndim ? (int)out->size[d] : 1;
+        n[d] = d < img->ndim ? (int)img->size[d] : 1;
+    }
+    PadBoxArgs pa{din, img->eltype, dout, out->eltype, img->ndim, {n[0], n[1], n[2], n[3]},
+                  make_box(img->ndim, lo, sz), border->style, fill};
+    IFX_CUDA(launch_pad_box(pa, c.s));
+    return c.finish();
+}
+
+static int collect_factors(const ifx_array_t &img, int32_t nf, const ifx_factor_t *factors,
+                           std::vector<Fac> &facs, long long *pfirst, long long *plast)
+{
+    if (nf < 0 || (nf > 0 && !factors)) return fail(IFX_ERR_ARGUMENT, "bad factor list");
+    for (int d = 0; d < IFX_MAXD; ++d) pfirst[d] = plast[d] = 0;
+    for (int i = 0; i < nf; ++i) {
+        const ifx_factor_t &f = factors[i];
+        if (f.axis < 0 || f.axis >= img.ndim)
+            return fail(IFX_ERR_DIMENSION, "factor %d filters axis %d of a %d-dimensional image",
+                        i + 1, f.axis + 1, img.ndim);
+        if (f.length < 1 || f.length > IFX_MAX_TAPS)
+            return fail(IFX_ERR_UNSUPPORTED, "factor %d has %d taps (1..%d supported)", i + 1,
+                        f.length, IFX_MAX_TAPS);
+        if (!f.weights) return fail(IFX_ERR_ARGUMENT, "factor %d has no weights", i + 1);
+        if (f.first < -(1 << 20) || f.first > (1 << 20))
+            return fail(IFX_ERR_UNSUPPORTED, "factor offset out of range");
+        pfirst[f.axis] += f.first;
+        plast[f.axis] += f.first + f.length - 1;
+        if (!is_copy(f)) facs.push_back({f.axis, (int)f.first, f.length, f.weights});
+    }
+    return IFX_OK;
+}
+
+int ifx_imfilter_factored(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                          int32_t nfactors, const ifx_factor_t *factors,
+                          const ifx_border_t *border, void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
+        return rc;
+    if ((rc = check_same_axes(*out, *img)) || (rc = check_filter_types(*img, *out))) return rc;
+    std::vector<Fac> facs;
+    long long pfirst[IFX_MAXD], plast[IFX_MAXD];
+    if ((rc = collect_factors(*img, nfactors, factors, facs, pfirst, plast))) return rc;
+    if (border->explicit_pad && (rc = check_padding(border, *img, pfirst, plast))) return rc;
+    if (numel(*img) == 0) return IFX_OK;
+    if ((rc = check_reflect(border, *img))) return rc;
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *dout;
+    if ((rc = c.input(*img, &din)) || (rc = c.output(*out, &dout))) return rc;
+    if ((rc = run_cascade(c, *img, din, *out, dout, facs, border, kSlotTmp))) return rc;
+    return c.finish();
+}
+
+int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                       const double *kernel, const int64_t *ksize, const int64_t *kfirst,
+                       const ifx_border_t *border, int32_t method, void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
+        return rc;
+    if ((rc = check_same_axes(*out, *img)) || (rc = check_filter_types(*img, *out))) return rc;
+    if (!kernel || !ksize || !kfirst) return fail(IFX_ERR_ARGUMENT, "kernel arrays are NULL");
+    const int nd = img->ndim;
+    long long kn = 1, pfirst[IFX_MAXD] = {0, 0, 0, 0}, plast[IFX_MAXD] = {0, 0, 0, 0};
+    for (int d = 0; d < nd; ++d) {
+        if (ksize[d] < 1) return fail(IFX_ERR_ARGUMENT, "empty kernel");
+        kn *= ksize[d];
+        pfirst[d] = kfirst[d];
+        plast[d] = kfirst[d] + ksize[d] - 1;
+    }
+    if (kn > kMaxDenseTaps)
+        return fail(IFX_ERR_UNSUPPORTED, "dense kernel with %lld taps (at most %d)", kn, kMaxDenseTaps);
+    if (method < 0 || method > 2) return fail(IFX_ERR_ARGUMENT, "method %d", method);
+    if (border->explicit_pad && (rc = check_padding(border, *img, pfirst, plast))) return rc;
+    if (numel(*img) == 0) return IFX_OK;
+    if ((rc = check_reflect(border, *img))) return rc;
+    if (method == 2)
+        return fail(IFX_ERR_UNSUPPORTED, "the tensor-core dense path is not built in this library");
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *dout;
+    if ((rc = c.input(*img, &din)) || (rc = c.output(*out, &dout))) return rc;
+    const int ct = img->eltype == IFX_F64 ? IFX_F64 : IFX_F32;
+    double fill;
+    if ((rc = image_fill(border, img->eltype, ct, &fill))) return rc;
+    int n[IFX_MAXD];
+    for (int d = 0; d < IFX_MAXD; ++d) n[d] = d < nd ? (int)img->size[d] : 1;
+    if (nd <= 2 && dense2d_smem_bytes((int)ksize[0], nd > 1 ? (int)ksize[1] : 1, ct == IFX_F64) <=
+                       200 * 1024) {
+        Dense2dArgs a{din, img->eltype, dout, out->eltype, n[0], nd > 1 ? n[1] : 1,
+                      (int)kfirst[0], (int)ksize[0], nd > 1 ? (int)kfirst[1] : 0,
+                      nd > 1 ? (int)ksize[1] : 1, kernel, border->style, fill, ct == IFX_F64};
+        IFX_CUDA(launch_dense2d(a, c.s));
+        return c.finish();
+    }
+    int blo[IFX_MAXD], bsz[IFX_MAXD];
+    for (int d = 0; d < IFX_MAXD; ++d) {
+        blo[d] = d < nd ? (int)pfirst[d] : 0;
+        bsz[d] = d < nd ? (int)(n[d] + plast[d] - pfirst[d]) : 1;
+    }
+    Box pb = make_box(nd, blo, bsz);
+    void *buf;
+    if ((rc = slot_get(ctx, kSlotTmp, (size_t)pb.count * elsize(ct), &buf))) return rc;
+    PadBoxArgs pa{din, img->eltype, buf, ct, nd, {n[0], n[1], n[2], n[3]}, pb, border->style, fill};
+    IFX_CUDA(launch_pad_box(pa, c.s));
+    DenseBoxArgs da;
+    memset(&da, 0, sizeof da);
+    da.src = buf;
+    da.sbox = pb;
+    da.out = dout;
+    da.out_type = out->eltype;
+    da.obox = image_box(*img);
+    da.nd = nd;
+    for (int d = 0; d < IFX_MAXD; ++d) {
+        da.ksize[d] = d < nd ? (int)ksize[d] : 1;
+        da.kfirst[d] = d < nd ? (int)kfirst[d] : 0;
+    }
+    da.K = kernel;
+    da.compute_f64 = ct == IFX_F64;
+    IFX_CUDA(launch_dense_box(da, c.s));
+    return c.finish();
+}
+
+int ifx_imfilter_laplacian(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                           const int32_t *flags, const ifx_border_t *border, void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
+        return rc;
+    if ((rc = check_same_axes(*out, *img))) return rc;
+    if (!flags) return fail(IFX_ERR_ARGUMENT, "flags is NULL");
+    const int it = img->eltype, ot = out->eltype;
+    const bool ok = (it == IFX_F32 || it == IFX_F64) ? (ot == IFX_F32 || ot == IFX_F64)
+                    : is8(it) ? (ot == IFX_F32 || ot == IFX_F64 || ot == IFX_I16) : false;
+    if (!ok) return fail(IFX_ERR_UNSUPPORTED, "Laplacian from eltype %d to %d", it, ot);
+    long long pf[IFX_MAXD] = {0, 0, 0, 0}, pl[IFX_MAXD] = {0, 0, 0, 0};
+    for (int d = 0; d < img->ndim; ++d) {
+        pf[d] = flags[d] ? -1 : 0;
+        pl[d] = flags[d] ? 1 : 0;
+    }
+    if (border->explicit_pad && (rc = check_padding(border, *img, pf, pl))) return rc;
+    if (numel(*img) == 0) return IFX_OK;
+    if ((rc = check_reflect(border, *img))) return rc;
+    double fill;
+    if ((rc = image_fill(border, it, ot, &fill))) return rc;
+    if (ot == IFX_I16 && fill != std::nearbyint(fill))
+        return fail(IFX_ERR_ARGUMENT, "Cannot convert elements of border=Fill(%g)", fill);
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *dout;
+    if ((rc = c.input(*img, &din)) || (rc = c.output(*out, &dout))) return rc;
+    LaplacianArgs a;
+    memset(&a, 0, sizeof a);
+    a.img = din;
+    a.in_type = it;
+    a.out = dout;
+    a.out_type = ot;
+    a.nd = img->ndim;
+    for (int d = 0; d < IFX_MAXD; ++d) {
+        a.n[d] = d < img->ndim ? (int)img->size[d] : 1;
+        a.flags[d] = d < img->ndim ? (flags[d] != 0) : 0;
+    }
+    a.style = border->style;
+    a.fill = fill;
+    IFX_CUDA(launch_laplacian(a, c.s));
+    return c.finish();
+}
+
+int ifx_imgradients(ifx_context_t *ctx, ifx_array_t *outs, const ifx_array_t *img,
+                    const double *deriv, const double *smooth, int32_t length, int64_t first,
+                    const int32_t *extended, const ifx_border_t *border, void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img")) || (rc = check_border(border))) return rc;
+    if (!outs || !deriv || !smooth || !extended) return fail(IFX_ERR_ARGUMENT, "NULL argument");
+    if (length < 1 || length > IFX_MAX_TAPS) return fail(IFX_ERR_UNSUPPORTED, "gradient length");
+    const int nd = img->ndim;
+    for (int d = 0; d < nd; ++d) {
+        if ((rc = check_array(&outs[d], "outs[d]")) || (rc = check_same_axes(outs[d], *img)) ||
+            (rc = check_filter_types(*img, outs[d])))
+            return rc;
+    }
+    // per-gradient factor lists (gradfactors, src/kernelfactors.jl:598-604)
+    static const double one = 1.0;
+    std::vector<std::vector<ifx_factor_t>> lists(nd);
+    for (int d = 0; d < nd; ++d)
+        for (int e = 0; e < nd; ++e) {
+            ifx_factor_t f;
+            f.axis = e;
+            if (!extended[e]) {
+                f.length = 1;
+                f.first = 0;
+                f.weights = &one;
+            } else {
+                f.length = length;
+                f.first = first;
+                f.weights = e == d ? deriv : smooth;
+            }
+            lists[d].push_back(f);
+        }
+    for (int d = 0; d < nd; ++d) {
+        std::vector<Fac> facs;
+        long long pfirst[IFX_MAXD], plast[IFX_MAXD];
+        if ((rc = collect_factors(*img, nd, lists[d].data(), facs, pfirst, plast))) return rc;
+        if (border->explicit_pad && (rc = check_padding(border, *img, pfirst, plast))) return rc;
+    }
+    if (numel(*img) == 0) return IFX_OK;
+    if ((rc = check_reflect(border, *img))) return rc;
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    if ((rc = c.input(*img, &din))) return rc;
+    for (int d = 0; d < nd; ++d) {
+        void *dout;
+        if ((rc = c.output(outs[d], &dout))) return rc;
+        std::vector<Fac> facs;
+        long long pfirst[IFX_MAXD], plast[IFX_MAXD];
+        collect_factors(*img, nd, lists[d].data(), facs, pfirst, plast);
+        if ((rc = run_cascade(c, *img, din, outs[d], dout, facs, border, kSlotTmp))) return rc;
+    }
+    return c.finish();
+}
+
+// mapwindow's copy_win! builds padindex tables relative to window-intersect-
+// image; with reflect a length-1 intersection is the reference's DivideError.
+static int check_window_reflect(const ifx_border_t *b, const ifx_array_t &img, const int *wf,
+                                const int *wl)
+{
+    if (!b || b->style != IFX_REFLECT) return IFX_OK;
+    bool edges = false;
+    for (int d = 0; d < img.ndim; ++d)
+        if (wf[d] < 0 || wf[d] + wl[d] - 1 > 0) edges = true;
+    if (!edges) return IFX_OK;
+    for (int d = 0; d < img.ndim; ++d) {
+        long long n = img.size[d], a = wf[d], b2 = wf[d] + wl[d] - 1;
+        long long m = n;
+        if (b2 + 1 < m) m = b2 + 1;
+        if (1 - a < m) m = 1 - a;
+        if (wl[d] < m) m = wl[d];
+        if (m <= 1)
+            return fail(IFX_ERR_ERROR, "DivideError: integer division error (reflect window of "
+                        "length 1 on axis %d)", d + 1);
+    }
+    return IFX_OK;
+}
+
+int ifx_mapwindow_median(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                         const int64_t *wfirst, const int64_t *wlen, const ifx_border_t *border,
+                         void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
+        return rc;
+    if ((rc = check_same_axes(*out, *img))) return rc;
+    if (!wfirst || !wlen) return fail(IFX_ERR_ARGUMENT, "window is NULL");
+    const int nd = img->ndim;
+    int wf[IFX_MAXD] = {0, 0, 0, 0}, wl[IFX_MAXD] = {1, 1, 1, 1};
+    long long m = 1;
+    for (int d = 0; d < nd; ++d) {
+        if (wlen[d] < 1) return fail(IFX_ERR_ARGUMENT, "empty window");
+        if (wfirst[d] > 0 || wfirst[d] + wlen[d] - 1 < 0)
+            return fail(IFX_ERR_UNSUPPORTED, "windows must contain offset 0");
+        wf[d] = (int)wfirst[d];
+        wl[d] = (int)wlen[d];
+        m *= wlen[d];
+    }
+    if (m > 256) return fail(IFX_ERR_UNSUPPORTED, "median window of %lld values (at most 256)", m);
+    const int it = img->eltype, ot = out->eltype;
+    if (it == IFX_I16 || ot == IFX_I16) return fail(IFX_ERR_UNSUPPORTED, "Int16 median");
+    if (!is8(it) && is8(ot)) return fail(IFX_ERR_UNSUPPORTED, "float median into 8-bit output");
+    if (numel(*img) == 0) return IFX_OK;
+    if ((rc = check_window_reflect(border, *img, wf, wl))) return rc;
+    double fill;
+    if ((rc = fill_for(border, it, &fill))) return rc;
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *dout;
+    if ((rc = c.input(*img, &din)) || (rc = c.output(*out, &dout))) return rc;
+    MedianArgs a;
+    memset(&a, 0, sizeof a);
+    a.img = din;
+    a.in_type = it;
+    a.out = dout;
+    a.out_type = ot;
+    a.nd = nd;
+    for (int d = 0; d < IFX_MAXD; ++d) {
+        a.n[d] = d < nd ? (int)img->size[d] : 1;
+        a.wfirst[d] = wf[d];
+        a.wlen[d] = wl[d];
+    }
+    a.style = border->style;
+    a.fill = fill;
+    IFX_CUDA(launch_median(a, c.s));
+    return c.finish();
+}
+
+int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                          const int64_t *wfirst, const int64_t *wlen, const ifx_border_t *border,
+                          int32_t which, void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img")) || (rc = check_array(out, "out"))) return rc;
+    if (border && (rc = check_border(border))) return rc;
+    if ((rc = check_same_axes(*out, *img))) return rc;
+    if (which < 0 || which > 2) return fail(IFX_ERR_ARGUMENT, "which must be 0, 1 or 2");
+    if (!wlen) return fail(IFX_ERR_ARGUMENT, "window is NULL");
+    if (out->eltype != img->eltype)
+        return fail(IFX_ERR_ARGUMENT, "extrema output eltype must equal the input eltype");
+    if (img->eltype == IFX_I16) return fail(IFX_ERR_UNSUPPORTED, "Int16 extrema");
+    const int nd = img->ndim;
+    int a0[IFX_MAXD], a1[IFX_MAXD], wf[IFX_MAXD], wl[IFX_MAXD];
+    for (int d = 0; d < nd; ++d) {
+        if (wlen[d] < 1) return fail(IFX_ERR_ARGUMENT, "empty window");
+        if (border) {
+            if (!wfirst) return fail(IFX_ERR_ARGUMENT, "window first is NULL");
+            a0[d] = (int)wfirst[d];
+            a1[d] = (int)(wfirst[d] + wlen[d] - 1);
+            if (a0[d] > 0 || a1[d] < 0) return fail(IFX_ERR_UNSUPPORTED, "windows must contain offset 0");
+        } else {
+            const int w = (int)wlen[d];
+            a0[d] = -(w >> 1);
+            a1[d] = w - 1 - (w >> 1);
+        }
+        wf[d] = a0[d];
+        wl[d] = a1[d] - a0[d] + 1;
+    }
+    if (numel(*img) == 0) return IFX_OK;
+    if ((rc = check_window_reflect(border, *img, wf, wl))) return rc;
+    double fill = 0.0;
+    const int use_fill = border && border->style == IFX_FILL;
+    if (use_fill && (rc = fill_for(border, img->eltype, &fill))) return rc;
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const size_t es = elsize(img->eltype);
+    const size_t N = (size_t)numel(*img);
+    const void *din;
+    void *dout;
+    if ((rc = c.input(*img, &din)) || (rc = c.output(*out, &dout, which == 0 ? 2 * N * es : 0)))
+        return rc;
+    void *planes[4] = {nullptr, nullptr, nullptr, nullptr};
+    if (nd > 1)
+        for (int i = 0; i < (nd > 2 ? 4 : 2); ++i)
+            if ((rc = slot_get(ctx, kSlotTmp + i, N * es, &planes[i]))) return rc;
+    const void *smin = din, *smax = din;
+    for (int d = 0; d < nd; ++d) {
+        const bool last = d == nd - 1;
+        ExtremaPassArgs a;
+        memset(&a, 0, sizeof a);
+        a.src_min = smin;
+        a.src_max = smax;
+        a.type = img->eltype;
+        a.nd = nd;
+        for (int e = 0; e < IFX_MAXD; ++e) a.n[e] = e < nd ? (int)img->size[e] : 1;
+        a.axis = d;
+        a.a0 = a0[d];
+        a.a1 = a1[d];
+        a.use_fill = use_fill;
+        a.fill = fill;
+        a.want_min = which != 2;
+        a.want_max = which != 1;
+        if (last) {
+            a.dst_interleaved = which == 0;
+            a.dst_min = dout;
+            a.dst_max = dout;
+        } else {
+            void *pm = planes[(d & 1) * 2], *px = planes[(d & 1) * 2 + 1];
+            a.dst_min = pm;
+            a.dst_max = px;
+            smin = pm;
+            smax = px;
+        }
+        IFX_CUDA(launch_extrema_pass(a, c.s));
+    }
+    return c.finish();
+}
+
+} // extern "C"

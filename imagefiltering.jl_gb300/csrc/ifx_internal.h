@@ -1,0 +1,100 @@
+// ifx_internal.h -- launch descriptors shared between the C-ABI layer
+// (ifx_api.cu) and the kernel files.  Host-side only types; no torch.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "ifx_common.cuh"
+
+namespace ifx {
+
+constexpr int kMaxDenseTaps = 3600;      // dense kernels passed by value (60x60)
+
+// Weights by value (kernel parameter space is 32 KB on sm_70+ with CUDA 12.1+).
+template <class Tc, int N> struct Weights { Tc w[N]; };
+
+// Generic N-d box pipeline --------------------------------------------------
+struct PadBoxArgs {
+    const void *img; int in_type;          // ifx_eltype of img
+    void *dst; int out_type;               // ifx_eltype of dst (compute type or output eltype)
+    int nd; int n[IFX_MAXD];               // image sizes
+    Box box;                               // dst box in image index space
+    int style; double fill;                // fill already in dst's value domain (code for 8-bit)
+};
+cudaError_t launch_pad_box(const PadBoxArgs &a, cudaStream_t s);
+
+struct PassBoxArgs {
+    const void *src; Box sbox;             // compute-type buffer
+    void *dst; Box dbox; int out_type;     // dst buffer (compute type, or the output eltype)
+    Box obox;                              // region to compute (inside dbox)
+    int axis, kfirst, klen;
+    const double *w;                       // host weights (copied into the launch)
+    int compute_f64;
+};
+cudaError_t launch_pass_box(const PassBoxArgs &a, cudaStream_t s);
+
+// Fused 2-D separable tile kernel -------------------------------------------
+struct Sep2dArgs {
+    const void *img; int in_type;
+    void *out; int out_type;
+    int nx, ny;
+    int fx, kx, fy, ky;                    // x factor: first, taps; y factor: first, taps
+    const double *wx, *wy;                 // host weights
+    int x_first;                           // pass order
+    int style; double fill;                // fill in value domain
+    int compute_f64;
+};
+cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s);
+
+// Dense --------------------------------------------------------------------
+struct Dense2dArgs {
+    const void *img; int in_type;
+    void *out; int out_type;
+    int nx, ny;
+    int fx, kw, fy, kh;                    // K axes: x first/size, y first/size
+    const double *K;                       // column-major kh? no: K[i + kw*j], i along x
+    int style; double fill;
+    int compute_f64;
+};
+cudaError_t launch_dense2d(const Dense2dArgs &a, cudaStream_t s);
+
+struct DenseBoxArgs {                      // N-d dense over a padded compute-type box
+    const void *src; Box sbox;
+    void *out; int out_type; Box obox;     // obox == image box (lo 0)
+    int nd; int ksize[IFX_MAXD]; int kfirst[IFX_MAXD];
+    const double *K;
+    int compute_f64;
+};
+cudaError_t launch_dense_box(const DenseBoxArgs &a, cudaStream_t s);
+
+// Laplacian ---------------------------------------------------------------
+struct LaplacianArgs {
+    const void *img; int in_type;
+    void *out; int out_type;               // also the arithmetic type
+    int nd; int n[IFX_MAXD]; int flags[IFX_MAXD];
+    int style; double fill;                // fill in value domain of the output type
+};
+cudaError_t launch_laplacian(const LaplacianArgs &a, cudaStream_t s);
+
+// Rank filters --------------------------------------------------------------
+struct MedianArgs {
+    const void *img; int in_type;
+    void *out; int out_type;
+    int nd; int n[IFX_MAXD];
+    int wfirst[IFX_MAXD], wlen[IFX_MAXD];
+    int style; double fill;                // fill: code for 8-bit inputs, value otherwise
+};
+cudaError_t launch_median(const MedianArgs &a, cudaStream_t s);
+
+struct ExtremaPassArgs {                   // one separable min/max pass along `axis`
+    const void *src_min, *src_max;         // src (input image for pass 0: both == img)
+    void *dst_min, *dst_max;               // may be the final interleaved output
+    int type;                              // element type of src and dst (F32/F64/U8)
+    int nd; int n[IFX_MAXD];
+    int axis, a0, a1;                      // window offsets a0..a1 along axis
+    int use_fill; double fill;             // Fill border: fill joins windows leaving the image
+    int dst_interleaved;                   // 1: dst_min points to (min,max) pairs
+    int want_min, want_max;
+};
+cudaError_t launch_extrema_pass(const ExtremaPassArgs &a, cudaStream_t s);
+
+} // namespace ifx

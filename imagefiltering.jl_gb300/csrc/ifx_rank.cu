@@ -1,0 +1,351 @@
+// ifx_rank.cu -- rank filters for sm_103a: median (mapwindow(median!, ...))
+// and running min/max (mapwindow(extrema / minimum / maximum, ...)).
+// Both are bit-exact: they select or compare input values, never compute new
+// ones.
+//
+// Median (src/mapwindow.jl:123-131): the ((1+m) div 2)-th smallest of the m
+// window values.  8-bit images take a packed-SIMD path: each thread owns four
+// horizontally adjacent outputs in one 32-bit word and finds the median bit by
+// bit from the most significant: the answer is the largest v with
+// #{window values < v} < rank, and every candidate test is one byte-wise
+// compare (__vcmpltu4) and one byte-wise count update (__vsub4) per window
+// element, for all four pixels at once.
+//
+// Windows at the border follow copy_win! (src/mapwindow.jl:310-333): a Pad
+// style pads relative to window-intersect-image.  For replicate, symmetric and
+// reflect that is the same as mapping through the whole image (the truncated
+// window never needs a second reflection), so the SIMD path gathers a padded
+// tile; circular (which wraps inside the truncated window) and non-8-bit or
+// N-d images use the per-pixel kernel, which applies the window-relative map
+// literally.
+#include "ifx_internal.h"
+#include <cstring>
+
+namespace ifx {
+
+static inline int grid1(long long n, int block)
+{
+    long long g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 152LL * 64) g = 152LL * 64;
+    return (int)g;
+}
+
+template <class T> __device__ __forceinline__ void store_sel(void *out, int out_type, long long i,
+                                                             T v, bool norm);
+template <> __device__ __forceinline__ void store_sel<uint8_t>(void *out, int out_type, long long i,
+                                                               uint8_t v, bool norm)
+{
+    if (out_type == IFX_F32)
+        ((float *)out)[i] = norm ? __fdiv_rn((float)v, 255.0f) : (float)v;
+    else if (out_type == IFX_F64)
+        ((double *)out)[i] = norm ? __ddiv_rn((double)v, 255.0) : (double)v;
+    else
+        ((uint8_t *)out)[i] = v;
+}
+template <> __device__ __forceinline__ void store_sel<float>(void *out, int out_type, long long i,
+                                                             float v, bool)
+{
+    if (out_type == IFX_F64) ((double *)out)[i] = (double)v;
+    else ((float *)out)[i] = v;
+}
+template <> __device__ __forceinline__ void store_sel<double>(void *out, int out_type, long long i,
+                                                              double v, bool)
+{
+    if (out_type == IFX_F32) ((float *)out)[i] = (float)v;
+    else ((double *)out)[i] = v;
+}
+
+// Julia's isless order for floats (NaN after everything); plain < for codes.
+template <class T> __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
+template <> __device__ __forceinline__ bool lt<float>(float a, float b)
+{
+    return isnan(b) ? !isnan(a) : a < b;
+}
+template <> __device__ __forceinline__ bool lt<double>(double a, double b)
+{
+    return isnan(b) ? !isnan(a) : a < b;
+}
+
+// =========================================================================
+// Per-pixel median, any eltype, N-d, window up to kMaxWin values.
+// =========================================================================
+constexpr int kMaxWin = 256;
+
+template <class T>
+__global__ void k_median_px(const T *__restrict__ img, void *out, int out_type, int nd, int4 n4,
+                            int4 wf4, int4 wl4, int style, T fill, bool norm)
+{
+    const int n[4] = {n4.x, n4.y, n4.z, n4.w};
+    const int wf[4] = {wf4.x, wf4.y, wf4.z, wf4.w};
+    const int wl[4] = {wl4.x, wl4.y, wl4.z, wl4.w};
+    const long long total = (long long)n[0] * n[1] * n[2] * n[3];
+    const int m = wl[0] * wl[1] * wl[2] * wl[3];
+    const int rank = (m + 1) / 2;             // 1-based
+    T buf[kMaxWin];
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total;
+         p += (long long)gridDim.x * blockDim.x) {
+        int c[4], ilo[4], ilen[4];
+        long long rem = p;
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            c[d] = (int)(rem % n[d]);
+            rem /= n[d];
+            int of = c[d] + wf[d], ol = of + wl[d] - 1;
+            int a = of > 0 ? of : 0, b = ol < n[d] - 1 ? ol : n[d] - 1;
+            ilo[d] = a;
+            ilen[d] = b - a + 1;
+        }
+        // gather (copy_win!: Pad styles relative to window-intersect-image)
+        int t = 0;
+        for (int l = 0; l < wl[3]; ++l)
+            for (int k = 0; k < wl[2]; ++k)
+                for (int j = 0; j < wl[1]; ++j)
+                    for (int i = 0; i < wl[0]; ++i, ++t) {
+                        const int q[4] = {c[0] + wf[0] + i, c[1] + wf[1] + j, c[2] + wf[2] + k,
+                                          c[3] + wf[3] + l};
+                        long long off = 0, st = 1;
+                        bool outside = false;
+#pragma unroll
+                        for (int d = 0; d < 4; ++d) {
+                            int mm = style == IFX_FILL
+                                         ? (((unsigned)q[d] < (unsigned)n[d]) ? q[d] : -1)
+                                         : map_index_in(q[d], ilo[d], ilen[d], style);
+                            outside |= mm < 0;
+                            off += (long long)mm * st;
+                            st *= n[d];
+                        }
+                        buf[t] = outside ? fill : img[off];
+                    }
+        // selection: the value with #less < rank <= #less + #equal
+        T med = buf[0];
+        for (int a = 0; a < m; ++a) {
+            int less = 0, eq = 0;
+            for (int b = 0; b < m; ++b) {
+                less += lt(buf[b], buf[a]);
+                eq += !lt(buf[b], buf[a]) && !lt(buf[a], buf[b]);
+            }
+            if (less < rank && rank <= less + eq) {
+                med = buf[a];
+                break;
+            }
+        }
+        store_sel<T>(out, out_type, p, med, norm);
+    }
+}
+
+// =========================================================================
+// Packed 8-bit median, 2-D.  CTA tile: TX = 128 outputs wide (32 threads x 4
+// pixels), TY = 8 rows; the padded input tile is gathered into shared memory
+// through the whole-image border map.  W0/W1 > 0 fixes the window at compile
+// time (the words stay in registers); W0 == 0 reads them from shared memory
+// every round.
+// =========================================================================
+constexpr int kMedTX = 128, kMedTY = 8;
+
+__device__ __forceinline__ uint32_t load_word(const uint8_t *row, int col)
+{
+    const int a = col & ~3, sh = col & 3;
+    const uint32_t lo = *reinterpret_cast<const uint32_t *>(row + a);
+    const uint32_t hi = *reinterpret_cast<const uint32_t *>(row + a + 4);
+    return __byte_perm(lo, hi, 0x3210 + 0x1111 * sh);
+}
+
+__device__ __forceinline__ uint32_t count_lt(uint32_t cnt, uint32_t w, uint32_t trial)
+{
+    return __vsub4(cnt, __vcmpltu4(w, trial));
+}
+
+template <int W0, int W1>
+__global__ void __launch_bounds__(256)
+k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, int ny, int f0,
+            int f1, int w0rt, int w1rt, int style, uint8_t fill, bool norm)
+{
+    const int w0 = W0 > 0 ? W0 : w0rt, w1 = W1 > 0 ? W1 : w1rt;
+    extern __shared__ __align__(16) uint8_t tile[];
+    const int CT = ((kMedTX + w0 - 1 + 3) & ~3) + 4;
+    const int RT = kMedTY + w1 - 1;
+    const int tx0 = blockIdx.x * kMedTX, ty0 = blockIdx.y * kMedTY;
+    for (int idx = threadIdx.x; idx < RT * CT; idx += blockDim.x) {
+        const int r = idx / CT, c = idx - r * CT;
+        uint8_t v = 0;
+        if (c < kMedTX + w0 - 1) {
+            const int mx = map_index(tx0 + f0 + c, nx, style);
+            const int my = map_index(ty0 + f1 + r, ny, style);
+            v = (mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx];
+        }
+        tile[idx] = v;
+    }
+    __syncthreads();
+    const int lx = (threadIdx.x & 31) * 4, ly = threadIdx.x >> 5;
+    const int m = w0 * w1;
+    const uint32_t rank4 = 0x01010101u * (uint32_t)((m + 1) / 2);
+    uint32_t res = 0;
+    if (W0 > 0 && W1 > 0) {
+        uint32_t w[(W0 > 0 ? W0 : 1) * (W1 > 0 ? W1 : 1)];
+#pragma unroll
+        for (int j = 0; j < (W1 > 0 ? W1 : 1); ++j)
+#pragma unroll
+            for (int i = 0; i < (W0 > 0 ? W0 : 1); ++i)
+                w[j * W0 + i] = load_word(tile + (size_t)(ly + j) * CT, lx + i);
+#pragma unroll
+        for (int b = 7; b >= 0; --b) {
+            const uint32_t trial = res | (0x01010101u << b);
+            uint32_t cnt = 0;
+#pragma unroll
+            for (int k = 0; k < (W0 > 0 ? W0 : 1) * (W1 > 0 ? W1 : 1); ++k) cnt = count_lt(cnt, w[k], trial);
+            const uint32_t below = __vcmpltu4(cnt, rank4);
+            res = (trial & below) | (res & ~below);
+        }
+    } else {
+        for (int b = 7; b >= 0; --b) {
+            const uint32_t trial = res | (0x01010101u << b);
+            uint32_t cnt = 0;
+            for (int j = 0; j < w1; ++j) {
+                const uint8_t *row = tile + (size_t)(ly + j) * CT;
+                for (int i = 0; i < w0; ++i) cnt = count_lt(cnt, load_word(row, lx + i), trial);
+            }
+            const uint32_t below = __vcmpltu4(cnt, rank4);
+            res = (trial & below) | (res & ~below);
+        }
+    }
+    const int y = ty0 + ly;
+    if (y < ny) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int x = tx0 + lx + q;
+            if (x < nx) store_sel<uint8_t>(out, out_type, (long long)y * nx + x,
+                                           (uint8_t)(res >> (8 * q)), norm);
+        }
+    }
+}
+
+template <class T>
+static cudaError_t median_px_t(const MedianArgs &a, cudaStream_t s)
+{
+    int4 n = make_int4(a.n[0], a.nd > 1 ? a.n[1] : 1, a.nd > 2 ? a.n[2] : 1, a.nd > 3 ? a.n[3] : 1);
+    int4 wf = make_int4(a.wfirst[0], a.nd > 1 ? a.wfirst[1] : 0, a.nd > 2 ? a.wfirst[2] : 0,
+                        a.nd > 3 ? a.wfirst[3] : 0);
+    int4 wl = make_int4(a.wlen[0], a.nd > 1 ? a.wlen[1] : 1, a.nd > 2 ? a.wlen[2] : 1,
+                        a.nd > 3 ? a.wlen[3] : 1);
+    long long total = (long long)n.x * n.y * n.z * n.w;
+    k_median_px<T><<<grid1(total, 128), 128, 0, s>>>((const T *)a.img, a.out, a.out_type, a.nd, n,
+                                                      wf, wl, a.style, (T)a.fill,
+                                                      a.in_type == IFX_N0F8);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <int W0, int W1>
+static cudaError_t median_u8_t(const MedianArgs &a, cudaStream_t s)
+{
+    const int nx = a.n[0], ny = a.nd > 1 ? a.n[1] : 1;
+    const int w0 = a.wlen[0], w1 = a.nd > 1 ? a.wlen[1] : 1;
+    const int CT = ((kMedTX + w0 - 1 + 3) & ~3) + 4;
+    const size_t smem = (size_t)(kMedTY + w1 - 1) * CT;
+    auto kern = k_median_u8<W0, W1>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((nx + kMedTX - 1) / kMedTX, (ny + kMedTY - 1) / kMedTY);
+    kern<<<grid, 256, smem, s>>>((const uint8_t *)a.img, a.out, a.out_type, nx, ny, a.wfirst[0],
+                                 a.nd > 1 ? a.wfirst[1] : 0, w0, w1, a.style, (uint8_t)a.fill,
+                                 a.in_type == IFX_N0F8);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_median(const MedianArgs &a, cudaStream_t s)
+{
+    long long total = 1;
+    for (int d = 0; d < a.nd; ++d) total *= a.n[d];
+    if (total == 0) return cudaSuccess;
+    const bool u8 = a.in_type == IFX_N0F8 || a.in_type == IFX_U8;
+    const int m = a.wlen[0] * (a.nd > 1 ? a.wlen[1] : 1);
+    if (u8 && a.nd <= 2 && a.style != IFX_CIRCULAR && m <= 255) {
+        const int w0 = a.wlen[0], w1 = a.nd > 1 ? a.wlen[1] : 1;
+        if (w0 == 3 && w1 == 3) return median_u8_t<3, 3>(a, s);
+        if (w0 == 5 && w1 == 5) return median_u8_t<5, 5>(a, s);
+        if (w0 == 7 && w1 == 7) return median_u8_t<7, 7>(a, s);
+        return median_u8_t<0, 0>(a, s);
+    }
+    if (u8) return median_px_t<uint8_t>(a, s);
+    if (a.in_type == IFX_F32) return median_px_t<float>(a, s);
+    if (a.in_type == IFX_F64) return median_px_t<double>(a, s);
+    return cudaErrorInvalidValue;
+}
+
+// =========================================================================
+// Separable running min/max.  The min (max) of a box is the min (max) of
+// per-axis mins (maxes), and truncating a box at the image edges is truncating
+// each axis interval, so one pass per axis is exact.  For a Fill border the
+// fill value joins every window that leaves the image along some axis, which
+// the per-axis passes reproduce by adding it in the pass of that axis.
+// One thread per output element; loads coalesce along axis 0.
+// =========================================================================
+template <class T>
+__global__ void k_extrema_pass(const T *__restrict__ smin, const T *__restrict__ smax,
+                               T *__restrict__ dmin, T *__restrict__ dmax, int4 n4, int axis,
+                               int a0, int a1, int use_fill, T fill, int interleaved,
+                               int want_min, int want_max)
+{
+    const int n[4] = {n4.x, n4.y, n4.z, n4.w};
+    const long long total = (long long)n[0] * n[1] * n[2] * n[3];
+    long long st = 1;
+    for (int d = 0; d < axis; ++d) st *= n[d];
+    const int na = n[axis];
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)((p / st) % na);
+        int lo = c + a0, hi = c + a1;
+        const bool leaves = lo < 0 || hi > na - 1;
+        lo = lo < 0 ? 0 : lo;
+        hi = hi > na - 1 ? na - 1 : hi;
+        const long long base = p - (long long)c * st;
+        T mn = fill, mx = fill;
+        bool have = use_fill && leaves;
+        for (int q = lo; q <= hi; ++q) {
+            const long long o = base + (long long)q * st;
+            if (want_min) {
+                const T v = smin[o];
+                mn = (!have || v < mn) ? v : mn;
+            }
+            if (want_max) {
+                const T v = smax[o];
+                mx = (!have || v > mx) ? v : mx;
+            }
+            have = true;
+        }
+        if (interleaved) {
+            dmin[2 * p] = mn;
+            dmin[2 * p + 1] = mx;
+        } else {
+            if (want_min) dmin[p] = mn;
+            if (want_max) dmax[p] = mx;
+        }
+    }
+}
+
+template <class T>
+static cudaError_t extrema_t(const ExtremaPassArgs &a, cudaStream_t s)
+{
+    int4 n = make_int4(a.n[0], a.nd > 1 ? a.n[1] : 1, a.nd > 2 ? a.n[2] : 1, a.nd > 3 ? a.n[3] : 1);
+    long long total = (long long)n.x * n.y * n.z * n.w;
+    k_extrema_pass<T><<<grid1(total, 256), 256, 0, s>>>(
+        (const T *)a.src_min, (const T *)a.src_max, (T *)a.dst_min, (T *)a.dst_max, n, a.axis,
+        a.a0, a.a1, a.use_fill, (T)a.fill, a.dst_interleaved, a.want_min, a.want_max);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_extrema_pass(const ExtremaPassArgs &a, cudaStream_t s)
+{
+    long long total = 1;
+    for (int d = 0; d < a.nd; ++d) total *= a.n[d];
+    if (total == 0) return cudaSuccess;
+    if (a.type == IFX_F32) return extrema_t<float>(a, s);
+    if (a.type == IFX_F64) return extrema_t<double>(a, s);
+    if (a.type == IFX_N0F8 || a.type == IFX_U8) return extrema_t<uint8_t>(a, s);
+    return cudaErrorInvalidValue;
+}
+
+} // namespace ifx

@@ -1,0 +1,177 @@
+/*
+ * ifx_gb300.h -- C ABI of the GB300 (sm_103a) FIR and rank-filter library.
+ *
+ * This is the drop-in boundary for ImageFiltering.jl's FIR / rank-filter path.
+ * A Julia method for a new algorithm tag `Algorithm.GB300 <: Alg` runs the
+ * reference's dispatch steps 1-4 unchanged (output eltype, kernel factoring,
+ * border resolution, output allocation: src/imfilter.jl:1-49, 204-254) and
+ * then `ccall`s one entry point below in place of the padded-copy + CPU loop
+ * backend.  Every entry point names the reference method it replaces
+ * (paths relative to the ImageFiltering.jl v0.7.12 tree).
+ *
+ * Conventions
+ *  - Arrays are column-major with axis 0 = Julia axis 1 (contiguous).  Only
+ *    dense arrays are accepted: stride[0] == 1, stride[d] == stride[d-1]*size[d-1].
+ *  - `data` may be host memory (plain or pinned) or device memory of the
+ *    context's device.  Host arrays are staged through the library's own
+ *    device buffers and the call returns when the result is back in host
+ *    memory.  When every array is device memory the work is only enqueued on
+ *    `stream` (NULL = the context's stream) and the call returns at once.
+ *  - Return value: IFX_OK or an ifx_status; ifx_last_error() gives the
+ *    message of the calling thread's last failure.  Status codes map to the
+ *    reference's exception classes (ArgumentError, DimensionMismatch, error).
+ *  - No C++ exceptions cross this boundary and no torch types appear in it.
+ */
+#ifndef IFX_GB300_H
+#define IFX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IFX_ABI_VERSION 1
+#define IFX_MAX_DIMS 4
+#define IFX_MAX_TAPS 129          /* longest 1-D factor */
+
+typedef enum {
+    IFX_OK = 0,
+    IFX_ERR_ARGUMENT = 1,          /* ArgumentError   (src/border.jl:147-156, 250-256) */
+    IFX_ERR_DIMENSION = 2,         /* DimensionMismatch (src/imfilter.jl:604-615)      */
+    IFX_ERR_ERROR = 3,             /* error(...) / DivideError (src/mapwindow.jl:133-137,
+                                      src/border.jl:581-586 with a length-1 axis)      */
+    IFX_ERR_CUDA = 4,              /* a CUDA runtime call failed                        */
+    IFX_ERR_NOMEM = 5,             /* device or host allocation failed / over the cap   */
+    IFX_ERR_TIMEOUT = 6,           /* a bounded wait ran out                            */
+    IFX_ERR_UNSUPPORTED = 7        /* a case this path does not implement               */
+} ifx_status;
+
+typedef enum {                     /* element types of arrays crossing the ABI          */
+    IFX_F32 = 0,                   /* Float32 / Gray{Float32}                           */
+    IFX_F64 = 1,                   /* Float64 / Gray{Float64}                           */
+    IFX_N0F8 = 2,                  /* N0f8 / Gray{N0f8}: 8-bit code c means c/255       */
+    IFX_U8 = 3,                    /* UInt8: 8-bit code c means c                       */
+    IFX_I16 = 4                    /* Int16 (Laplacian of UInt8, src/imfilter.jl:1139)  */
+} ifx_eltype;
+
+typedef enum {                     /* border styles (src/border.jl:136-248, 465-555)    */
+    IFX_REPLICATE = 0,
+    IFX_CIRCULAR = 1,
+    IFX_SYMMETRIC = 2,             /* dcba|abcd|dcba: edge duplicated (border.jl:574-580) */
+    IFX_REFLECT = 3,               /* dcb|abcd|cba: edge not repeated (border.jl:581-586) */
+    IFX_FILL = 4                   /* Fill(value)                                        */
+} ifx_style;
+
+typedef struct ifx_array {
+    void *data;
+    int32_t eltype;                /* ifx_eltype */
+    int32_t ndim;                  /* 1 .. IFX_MAX_DIMS */
+    int64_t size[IFX_MAX_DIMS];
+    int64_t stride[IFX_MAX_DIMS];  /* in elements */
+    int64_t first[IFX_MAX_DIMS];   /* first index of each axis (1 for Array, any for OffsetArray) */
+} ifx_array_t;
+
+typedef struct ifx_border {
+    int32_t style;                 /* ifx_style */
+    int32_t explicit_pad;          /* 0: Pad{0}/Fill{T,0}, amounts come from the kernel
+                                      (src/border.jl:236-237, 614-621);
+                                      1: Pad{N}/Fill{T,N} with lo/hi below, which must
+                                      cover the kernel (DimensionMismatch otherwise)  */
+    int64_t lo[IFX_MAX_DIMS];
+    int64_t hi[IFX_MAX_DIMS];
+    double fill_value;             /* Fill value, already converted to the image eltype
+                                      (src/borderarray.jl:11-20)                        */
+} ifx_border_t;
+
+typedef struct ifx_factor {        /* one ReshapedOneD factor (src/kernelfactors.jl:52-131) */
+    int32_t axis;                  /* 0-based axis it filters along (Npre)               */
+    int32_t length;                /* taps, 1 .. IFX_MAX_TAPS                            */
+    int64_t first;                 /* kernel index of the first tap (OffsetArray axes)   */
+    const double *weights;         /* host memory, `length` values                       */
+} ifx_factor_t;
+
+typedef struct ifx_context ifx_context_t;
+
+/* ---- context ------------------------------------------------------------- */
+int ifx_abi_version(void);
+int ifx_create(ifx_context_t **ctx, int device);
+int ifx_destroy(ifx_context_t *ctx);
+const char *ifx_last_error(void);
+/* Number of this library's kernel launches made by the calling process so far. */
+uint64_t ifx_launch_count(void);
+int ifx_synchronize(ifx_context_t *ctx, void *stream);
+
+/* ---- a1: border index maps ------------------------------------------------
+ * padarray(T, img, border) (src/border.jl:324-331 -> borderarray.jl:179-196,
+ * index maps src/border.jl:564-596).  out has sizes lo+n+hi per axis and the
+ * output eltype; its first indices are img.first - lo. */
+int ifx_padarray(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                 const ifx_border_t *border, void *stream);
+
+/* ---- a2/a3: separable cascade ---------------------------------------------
+ * imfilter!(r::AbstractResource{GB300}, out, img, kernel::Tuple{ReshapedOneD...},
+ * border) -- replaces the padded copy (src/imfilter.jl:331-341), the cascade
+ * scheduler (385-457, tiled 460-564) and the 1-D loops (671-739).  Results
+ * equal pad-then-cascade: each pass covers the halo that later passes need,
+ * so Fill borders behave as in the reference.  Copy factors are skipped. */
+int ifx_imfilter_factored(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                          int32_t nfactors, const ifx_factor_t *factors,
+                          const ifx_border_t *border, void *stream);
+
+/* ---- a4: dense kernel -------------------------------------------------------
+ * imfilter! with a single dense (non-separable) kernel, the `(dummy, K)` case
+ * after factorkernel (src/imfilter.jl:1159-1184) -> __imfilter_inbounds!
+ * (src/imfilter.jl:624-669).  K is column-major with sizes ksize and first
+ * indices kfirst (host memory).  method: 0 = automatic, 1 = FP32/FP64 CUDA
+ * cores, 2 = tcgen05 tensor cores (BF16 hi/lo split, three products, FP32
+ * accumulation; 2-D Float32 only). */
+int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                       const double *kernel, const int64_t *ksize, const int64_t *kfirst,
+                       const ifx_border_t *border, int32_t method, void *stream);
+
+/* ---- a5: Laplacian stencil --------------------------------------------------
+ * imfilter(img, Kernel.Laplacian(flags), border) (src/specialty.jl:3-17,
+ * src/kernel.jl:341-391).  Exact: the same operation order in the output
+ * eltype (Float32, Float64 or Int16). */
+int ifx_imfilter_laplacian(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                           const int32_t *flags, const ifx_border_t *border, void *stream);
+
+/* ---- a6: imgradients --------------------------------------------------------
+ * imgradients(img, kernelfun, border) for factored gradient kernels
+ * (src/specialty.jl:39-53, gradfactors src/kernelfactors.jl:598-602): output d
+ * is the cascade with `deriv` along axis d and `smooth` along every other
+ * extended axis.  outs holds img.ndim arrays.  extended[d] == 0 gives a copy
+ * factor on axis d (kdim, src/kernelfactors.jl:604). */
+int ifx_imgradients(ifx_context_t *ctx, ifx_array_t *outs, const ifx_array_t *img,
+                    const double *deriv, const double *smooth, int32_t length, int64_t first,
+                    const int32_t *extended, const ifx_border_t *border, void *stream);
+
+/* ---- a8: median -------------------------------------------------------------
+ * mapwindow(median!, img, window; border) (src/mapwindow.jl:75-85, 123-131,
+ * 270-333).  Window offsets wfirst .. wfirst+wlen-1 per axis, odd lengths
+ * only for Dims windows (resolve_window, 133-137: the host checks).  The
+ * selected value is written in out's eltype (8-bit inputs: code/255 for N0f8,
+ * code for UInt8).  Bit-exact. */
+int ifx_mapwindow_median(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                         const int64_t *wfirst, const int64_t *wlen,
+                         const ifx_border_t *border, void *stream);
+
+/* ---- a9: extrema ------------------------------------------------------------
+ * which = 0: extrema -> out holds (min,max) pairs (Tuple{T,T} layout, 2 values
+ *            per element); 1: minimum; 2: maximum.
+ * border == NULL: mapwindow(extrema, A, window::Dims) without keywords, the
+ *   Lemire filter (src/mapwindow.jl:337-338, 388-473): window offsets
+ *   -(w>>1) .. w-1-(w>>1), truncated at the edges, even w allowed (wfirst is
+ *   ignored and may be NULL).
+ * border != NULL: the generic window path with that border (src/mapwindow.jl:
+ *   270-333): Pad styles take values inside window-intersect-image only, Fill
+ *   adds the fill value where the window leaves the image.  Bit-exact. */
+int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
+                          const int64_t *wfirst, const int64_t *wlen,
+                          const ifx_border_t *border, int32_t which, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IFX_GB300_H */

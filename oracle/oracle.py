@@ -1,0 +1,187 @@
+"""Python face of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import this module, and only as the checker.  The product
+(the CUDA library and its host layer) never imports it.
+
+Arrays follow Julia's memory order: numpy arrays in Fortran (column-major)
+order whose axis 0 is Julia's axis 1.  All arithmetic is FP64 unless a routine
+says otherwise.  Each wrapper names the reference lines its C routine restates
+(paths relative to the ImageFiltering.jl v0.7.12 source tree).
+
+``np_padarray`` is an independent numpy cross-check of the border maps: numpy's
+``np.pad`` modes edge / wrap / symmetric / reflect / constant coincide with the
+reference's replicate / circular / symmetric / reflect / Fill (the reference's
+docstrings for symmetric and reflect are swapped relative to its code,
+src/border.jl:107-130 vs 574-586; the code and test/border.jl:67-86 win).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import build as _build
+
+STYLES = {"replicate": 0, "circular": 1, "symmetric": 2, "reflect": 3, "fill": 4}
+_ERRS = {1: "ArgumentError", 2: "DimensionMismatch", 3: "Error", 5: "OutOfMemory"}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(_build.build())
+        i64p = np.ctypeslib.ndpointer(np.int64, flags="C")
+        f64p = np.ctypeslib.ndpointer(np.float64, flags="F")
+        f64c = np.ctypeslib.ndpointer(np.float64, flags="C")
+        i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
+        _lib.ora_padindex.argtypes = [C.c_int, C.c_int64, C.c_int64, C.c_int64, i64p]
+        _lib.ora_padarray.argtypes = [C.c_int, i64p, f64p, C.c_int, C.c_double, i64p, i64p, f64p]
+        _lib.ora_imfilter_cascade.argtypes = [C.c_int, i64p, f64p, C.c_int, i32p, i64p, i64p,
+                                              f64c, C.c_int, C.c_double, f64p]
+        _lib.ora_imfilter_dense.argtypes = [C.c_int, i64p, f64p, i64p, i64p, f64p,
+                                            C.c_int, C.c_double, f64p]
+        for nm in ("ora_laplacian_f64", "ora_laplacian_f32", "ora_laplacian_i64"):
+            getattr(_lib, nm).argtypes = [C.c_int, i64p, f64p, i32p, C.c_int, C.c_double, f64p]
+        _lib.ora_mapwindow_median.argtypes = [C.c_int, i64p, f64p, i64p, i64p, C.c_int,
+                                              C.c_double, f64p]
+        _lib.ora_mapwindow_extrema.argtypes = [C.c_int, i64p, f64p, i64p, i64p, C.c_int,
+                                               C.c_double, f64p, f64p]
+        _lib.ora_extrema_trunc.argtypes = [C.c_int, i64p, f64p, i64p, f64p, f64p]
+        u8p = np.ctypeslib.ndpointer(np.uint8, flags="F")
+        _lib.ora_mapwindow_median_u8_mt.argtypes = [i64p, u8p, i64p, i64p, C.c_int, C.c_double,
+                                                    u8p, C.c_int64, C.c_int64]
+        _lib.ora_set_threads.argtypes = [C.c_int]
+    return _lib
+
+
+def set_threads(n: int) -> None:
+    lib().ora_set_threads(int(n))
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("oracle: %s" % _ERRS.get(rc, "status %d" % rc))
+
+
+def _f64(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+def _dims(a):
+    return np.array(a.shape, dtype=np.int64)
+
+
+def padindex(style, lo, n, hi):
+    """0-based source indices for padded positions -lo .. n-1+hi
+    (src/border.jl:564-596)."""
+    out = np.zeros(max(lo + n + hi, 1), dtype=np.int64)
+    _check(lib().ora_padindex(STYLES[style], lo, n, hi, out))
+    return out[: lo + n + hi]
+
+
+def padarray(img, style, lo, hi, fill=0.0):
+    """padarray(img, Pad(style, lo, hi)) or Fill(fill, lo, hi)
+    (src/border.jl:324-352); returns the padded array (axis d starts at -lo[d])."""
+    a = _f64(img)
+    lo = np.array(lo, dtype=np.int64)
+    hi = np.array(hi, dtype=np.int64)
+    out = np.zeros(tuple(int(x) for x in lo + np.array(a.shape) + hi), dtype=np.float64, order="F")
+    _check(lib().ora_padarray(a.ndim, _dims(a), a, STYLES[style], float(fill), lo, hi, out))
+    return out
+
+
+def imfilter_cascade(img, factors, style, fill=0.0):
+    """imfilter with a tuple of 1-D factors, pad-then-cascade
+    (src/imfilter.jl:331-341, 385-457, 671-739).  ``factors`` is a list of
+    (axis, first_index, weights)."""
+    a = _f64(img)
+    nf = len(factors)
+    axis = np.array([f[0] for f in factors], dtype=np.int32)
+    first = np.array([f[1] for f in factors], dtype=np.int64)
+    klen = np.array([len(f[2]) for f in factors], dtype=np.int64)
+    kdata = np.ascontiguousarray(np.concatenate([np.asarray(f[2], np.float64) for f in factors])
+                                 if nf else np.zeros(1))
+    out = np.zeros(a.shape, dtype=np.float64, order="F")
+    _check(lib().ora_imfilter_cascade(a.ndim, _dims(a), a, nf, axis, first, klen, kdata,
+                                      STYLES[style], float(fill), out))
+    return out
+
+
+def imfilter_dense(img, K, kfirst, style, fill=0.0):
+    """Dense N-d correlation, K[0,...] at index kfirst (src/imfilter.jl:624-669)."""
+    a = _f64(img)
+    k = _f64(K)
+    assert k.ndim == a.ndim
+    out = np.zeros(a.shape, dtype=np.float64, order="F")
+    _check(lib().ora_imfilter_dense(a.ndim, _dims(a), a, _dims(k),
+                                    np.array(kfirst, dtype=np.int64), k,
+                                    STYLES[style], float(fill), out))
+    return out
+
+
+def laplacian(img, flags, style, fill=0.0, arith="f64"):
+    """Laplacian stencil (src/specialty.jl:3-17) computed in the output eltype:
+    arith 'f64', 'f32' (inputs must already be Float32 values) or 'int'."""
+    a = _f64(img)
+    out = np.zeros(a.shape, dtype=np.float64, order="F")
+    fn = {"f64": lib().ora_laplacian_f64, "f32": lib().ora_laplacian_f32,
+          "int": lib().ora_laplacian_i64}[arith]
+    _check(fn(a.ndim, _dims(a), a, np.array(flags, dtype=np.int32), STYLES[style],
+              float(fill), out))
+    return out
+
+
+def mapwindow_median(img, wfirst, wlen, style, fill=0.0):
+    """mapwindow(median!, img, window; border) (src/mapwindow.jl:123-131, 270-333)."""
+    a = _f64(img)
+    out = np.zeros(a.shape, dtype=np.float64, order="F")
+    _check(lib().ora_mapwindow_median(a.ndim, _dims(a), a, np.array(wfirst, np.int64),
+                                      np.array(wlen, np.int64), STYLES[style], float(fill), out))
+    return out
+
+
+def mapwindow_extrema(img, wfirst, wlen, style, fill=0.0):
+    """mapwindow(extrema, img, window; border) through the generic window path
+    (src/mapwindow.jl:75-85, 270-333); returns (min, max)."""
+    a = _f64(img)
+    mn = np.zeros(a.shape, dtype=np.float64, order="F")
+    mx = np.zeros(a.shape, dtype=np.float64, order="F")
+    _check(lib().ora_mapwindow_extrema(a.ndim, _dims(a), a, np.array(wfirst, np.int64),
+                                       np.array(wlen, np.int64), STYLES[style], float(fill),
+                                       mn, mx))
+    return mn, mx
+
+
+def extrema_trunc(img, w):
+    """mapwindow(extrema, A, window::Dims) without keywords -> Lemire filter with
+    windows truncated at the edges (src/mapwindow.jl:337-338, 388-473)."""
+    a = _f64(img)
+    mn = np.zeros(a.shape, dtype=np.float64, order="F")
+    mx = np.zeros(a.shape, dtype=np.float64, order="F")
+    _check(lib().ora_extrema_trunc(a.ndim, _dims(a), a, np.array(w, np.int64), mn, mx))
+    return mn, mx
+
+
+def median_u8_rows(img_u8, wfirst, wlen, style, fill, row0, row1):
+    """Threaded 8-bit median over rows [row0,row1) of a 2-D image (CPU-baseline
+    timing helper; same window semantics as mapwindow_median)."""
+    a = np.asfortranarray(img_u8, dtype=np.uint8)
+    out = np.zeros(a.shape, dtype=np.uint8, order="F")
+    _check(lib().ora_mapwindow_median_u8_mt(_dims(a), a, np.array(wfirst, np.int64),
+                                            np.array(wlen, np.int64), STYLES[style], float(fill),
+                                            out, int(row0), int(row1)))
+    return out
+
+
+_NP_MODES = {"replicate": "edge", "circular": "wrap", "symmetric": "symmetric",
+             "reflect": "reflect"}
+
+
+def np_padarray(img, style, lo, hi, fill=0.0):
+    """Independent numpy restatement of padarray for cross-checking the C maps."""
+    a = np.asarray(img, dtype=np.float64)
+    widths = [(int(l), int(h)) for l, h in zip(lo, hi)]
+    if style == "fill":
+        return np.pad(a, widths, mode="constant", constant_values=fill)
+    return np.pad(a, widths, mode=_NP_MODES[style])

@@ -1,0 +1,59 @@
+"""The GB300 library as a backend for tests/kat_cases.py: every call goes
+through the package's reference-shaped API and the C ABI."""
+import numpy as np
+
+
+class GpuBackend:
+    def __init__(self, ifx, dtype=np.float64):
+        self.ifx = ifx
+        self.dtype = dtype
+
+    def _border(self, style, fill):
+        return self.ifx.Fill(fill) if style == "fill" else self.ifx.Pad(style)
+
+    def _img(self, a):
+        return np.asfortranarray(np.asarray(a, dtype=self.dtype))
+
+    def padarray(self, A, style, lo, hi, fill=0.0):
+        ifx = self.ifx
+        b = ifx.Fill(fill, tuple(lo), tuple(hi)) if style == "fill" else ifx.Pad(style, tuple(lo), tuple(hi))
+        out, _ = ifx.padarray(self._img(A), b)
+        return np.asarray(out, dtype=np.float64)
+
+    def cascade(self, img, factors, style, fill=0.0):
+        ifx = self.ifx
+        img = self._img(img)
+        ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(np.asarray(w, np.float64), (first,)), img.ndim, ax)
+                   for ax, first, w in factors)
+        return np.asarray(ifx.imfilter(img, ks, self._border(style, fill)), dtype=np.float64)
+
+    def dense(self, img, K, kfirst, style, fill=0.0):
+        ifx = self.ifx
+        img = self._img(img)
+        k = ifx.OffsetKernel(np.asarray(K, np.float64), tuple(kfirst))
+        return np.asarray(ifx.imfilter(img, (k,), self._border(style, fill)), dtype=np.float64)
+
+    def laplacian(self, img, flags, style, fill=0.0, arith="f64"):
+        ifx = self.ifx
+        dt = {"f64": np.float64, "f32": np.float32, "int": np.uint8}[arith]
+        a = np.asfortranarray(np.asarray(img, dtype=dt))
+        out = ifx.imfilter(a, ifx.Kernel.Laplacian(tuple(bool(f) for f in flags)),
+                           self._border(style, fill))
+        return np.asarray(out, dtype=np.float64)
+
+    def median(self, img, wf, wl, style, fill=0.0):
+        ifx = self.ifx
+        win = tuple(range(f, f + l) for f, l in zip(wf, wl))
+        return np.asarray(ifx.mapwindow(ifx.median, self._img(img), win, border=self._border(style, fill)),
+                          dtype=np.float64)
+
+    def extrema(self, img, wf, wl, style, fill=0.0):
+        ifx = self.ifx
+        win = tuple(range(f, f + l) for f, l in zip(wf, wl))
+        out = ifx.mapwindow(ifx.extrema, self._img(img), win, border=self._border(style, fill))
+        return np.asarray(out[0], np.float64), np.asarray(out[1], np.float64)
+
+    def extrema_lemire(self, img, w):
+        ifx = self.ifx
+        out = ifx.mapwindow(ifx.extrema, self._img(img), tuple(int(x) for x in w))
+        return np.asarray(out[0], np.float64), np.asarray(out[1], np.float64)

@@ -1,0 +1,420 @@
+"""Known-answer cases of ImageFiltering.jl's own test suite, shared by the
+oracle tests (CPU) and the GPU parity tests.
+
+Each case cites the reference test it restates (paths relative to the
+ImageFiltering.jl v0.7.12 tree).  Literal tables come from
+tests/golden/reference_kats.json (extracted from the reference's test files by
+tests/golden/extract_reference_kats.py); the structural cases (impulse
+responses, edge coefficients, analytic targets) are rebuilt here with the same
+construction as the reference test.
+
+A backend is an object with the methods used below (see OracleBackend and, in
+the GPU tests, GpuBackend).  Arrays are numpy arrays in Julia axis order
+(index [i, j] is Julia's [i+1, j+1]).
+"""
+import json
+import os
+
+import numpy as np
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                     "reference_kats.json")))
+BORDERS = ["replicate", "circular", "symmetric", "reflect", "fill"]
+
+
+def F(a, dtype=np.float64):
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+# ------------------------------------------------------------------- backends
+class OracleBackend:
+    """The CPU oracle, FP64."""
+
+    def __init__(self, O):
+        self.O = O
+
+    def padarray(self, A, style, lo, hi, fill=0.0):
+        return self.O.padarray(A, style, lo, hi, fill)
+
+    def cascade(self, img, factors, style, fill=0.0):
+        return self.O.imfilter_cascade(img, factors, style, fill)
+
+    def dense(self, img, K, kfirst, style, fill=0.0):
+        return self.O.imfilter_dense(img, K, kfirst, style, fill)
+
+    def laplacian(self, img, flags, style, fill=0.0, arith="f64"):
+        return self.O.laplacian(img, flags, style, fill, arith)
+
+    def median(self, img, wf, wl, style, fill=0.0):
+        return self.O.mapwindow_median(img, wf, wl, style, fill)
+
+    def extrema(self, img, wf, wl, style, fill=0.0):
+        return self.O.mapwindow_extrema(img, wf, wl, style, fill)
+
+    def extrema_lemire(self, img, w):
+        return self.O.extrema_trunc(img, w)
+
+
+# ------------------------------------------------------------------- padarray
+def padarray_cases():
+    """test/border.jl:35-206 golden tables."""
+    for k in GOLDEN["padarray"]:
+        A = F(k["A"])
+        b = k["border"]
+        yield k["source"], A, b["style"], b["lo"], b["hi"], b.get("fill", 0), F(k["expected"])
+
+
+def check_padarray(be, dtype=np.float64, unsigned=False):
+    n = 0
+    for src, A, style, lo, hi, fill, exp in padarray_cases():
+        if unsigned and fill < 0:        # Fill(-1) has no UInt8 value
+            continue
+        got = be.padarray(F(A, dtype), style, lo, hi, fill)
+        assert got.shape == exp.shape, src
+        assert np.array_equal(np.asarray(got, np.float64), exp), "%s %s" % (src, style)
+        n += 1
+    assert n >= 19
+
+
+def check_padindex_vs_numpy(be, O):
+    """Border maps against numpy's np.pad on random sizes (test/border.jl:15-23
+    checks BorderArray == padarray the same way)."""
+    rng = np.random.default_rng(7)
+    for _ in range(30):
+        A = F(rng.standard_normal((int(rng.integers(2, 7)), int(rng.integers(2, 7)))))
+        style = ["replicate", "circular", "symmetric", "reflect"][int(rng.integers(0, 4))]
+        lo = [int(x) for x in rng.integers(0, 9, 2)]
+        hi = [int(x) for x in rng.integers(0, 9, 2)]
+        got = be.padarray(A, style, lo, hi)
+        exp = O.np_padarray(A, style, lo, hi)
+        assert np.array_equal(np.asarray(got), exp), (style, lo, hi, A.shape)
+
+
+# ------------------------------------------------------------------- impulses
+KERN = np.array([[0.1, 0.2], [0.4, 0.5]])          # test/2d.jl:55-56, axes (-1:0, 1:2)
+KFIRST = (-1, 1)
+FACTORS = [(0, -1, np.array([0.2, 0.8])), (1, 1, np.array([0.3, 0.6]))]   # test/2d.jl:83
+
+
+def rot180(a):
+    return a[::-1, ::-1]
+
+
+def check_impulse_interior(be):
+    """test/2d.jl:49-79 and 82-100: impulse away from the edges; every border
+    gives target[3:4,2:3] = rot180(kern) (correlation, origin at K[0,0])."""
+    img = np.zeros((5, 7))
+    img[2, 3] = 1
+    img = F(img)
+    target = np.zeros((5, 7))
+    target[2:4, 1:3] = rot180(KERN)
+    kf = np.outer(FACTORS[0][2], FACTORS[1][2])
+    targetf = np.zeros((5, 7))
+    targetf[2:4, 1:3] = rot180(kf)
+    for style in BORDERS:
+        got = be.dense(img, KERN, KFIRST, style)
+        np.testing.assert_allclose(got, target, atol=1e-12, err_msg=style)
+        got = be.cascade(img, FACTORS, style)
+        np.testing.assert_allclose(got, targetf, atol=1e-12, err_msg=style)
+
+
+def target1(style, kern):
+    """test/2d.jl:171-195: impulse at [1,2] where the border matters."""
+    ret = np.zeros((5, 7))
+    x = 1.0
+    if style in ("replicate", "symmetric"):
+        ret[0, 0] = (kern[0, 0] + kern[1, 0]) * x
+        ret[1, 0] = kern[0, 0] * x
+    elif style == "circular":
+        r = rot180(kern) * x                      # a[0:1, -1:0] of an FFTView
+        ret[0, 6], ret[0, 0] = r[0, 0], r[0, 1]
+        ret[1, 6], ret[1, 0] = r[1, 0], r[1, 1]
+    else:                                         # reflect, Fill(0)
+        ret[0, 0] = kern[1, 0] * x
+        ret[1, 0] = kern[0, 0] * x
+    return ret
+
+
+def check_impulse_edge(be):
+    img = np.zeros((5, 7))
+    img[0, 1] = 1
+    img = F(img)
+    kf = np.outer(FACTORS[0][2], FACTORS[1][2])
+    for style in BORDERS:
+        np.testing.assert_allclose(be.dense(img, KERN, KFIRST, style), target1(style, KERN),
+                                   atol=1e-12, err_msg=style)
+        np.testing.assert_allclose(be.cascade(img, FACTORS, style), target1(style, kf),
+                                   atol=1e-12, err_msg=style)
+
+
+# ------------------------------------------------------------------- 1-D cascades
+K1 = (0, -1, np.array([0.25, 0.5, 0.25]))             # test/nd.jl:58
+K2 = (0, 1, np.array([0.5, 0.5]))                      # OffsetArray([0.5,0.5], 1:2)
+KC = (0, 0, np.array([1.0]))                           # centered([1]): a copy kernel
+
+
+def _golden_cascade(name):
+    for k in GOLDEN["cascade_1d"]:
+        if k["name"] == name:
+            return k
+    raise KeyError(name)
+
+
+def check_cascade_1d(be):
+    """test/nd.jl:56-75: cascade trimming and copy kernels on 1:8."""
+    img = F(np.arange(1, 9))
+    A2 = _golden_cascade("A2")
+    a2 = np.array(A2["expected"])                       # axes 0:9
+    a3 = np.array([0.25 * a2[i - 1] + 0.5 * a2[i] + 0.25 * a2[i + 1] for i in range(1, 9)])
+    casc = be.cascade(img, [K1, K2, K1], "replicate")
+    np.testing.assert_allclose(casc, a3, rtol=1e-12)
+    # A1/A2 are the successive Inner filterings of the padded array
+    A0 = be.padarray(img, "replicate", [2], [4])         # axes -1:12
+    a1 = np.array([sum(A0[i + 1 + j - 1] * K1[2][j] for j in range(3)) for i in range(0, 12)])
+    np.testing.assert_allclose(a1, _golden_cascade("A1")["expected"], rtol=1e-12)
+    a2c = np.array([sum(a1[i + 1 + j] * K2[2][j] for j in range(2)) for i in range(10)])
+    np.testing.assert_allclose(a2c, a2, rtol=1e-12)
+    exp = _golden_cascade("k1_on_1to8")["expected"]
+    np.testing.assert_allclose(be.cascade(img, [K1], "replicate"), exp, rtol=1e-12)
+    np.testing.assert_allclose(be.cascade(img, [KC, K1], "replicate"), exp, rtol=1e-12)
+    np.testing.assert_allclose(be.cascade(img, [K1, KC], "replicate"), exp, rtol=1e-12)
+
+
+def check_offset_axes_1d(be):
+    """test/nd.jl:84-93: impulse in the middle, every border."""
+    img = np.zeros(11)
+    img[5] = 1
+    img = F(img)
+    for style in BORDERS:
+        f = be.cascade(img, [K1], style)
+        assert f[4] == f[6] == 0.25 and f[5] == 0.5
+        assert np.all(f[:4] == 0) and np.all(f[7:] == 0)
+
+
+def check_nonfinite(be):
+    """test/nd.jl:95-109: NaN/Inf spread over the 31-tap window only."""
+    rng = np.random.default_rng(11)
+    for x in (np.nan, np.inf, -np.inf):
+        v = F(rng.random(100))
+        i = int(rng.integers(0, 100))
+        w = v.copy()
+        w[i] = x
+        k = [(0, -15, np.ones(31))]
+        vf = be.cascade(v, k, "replicate")
+        wf = be.cascade(w, k, "replicate")
+        around = np.abs(np.arange(100) - i) <= 15
+        assert np.all(np.isnan(wf[around])) if np.isnan(x) else np.all(wf[around] == x)
+        np.testing.assert_allclose(wf[~around], vf[~around], rtol=1e-10)
+
+
+def check_3d_box(be):
+    """test/nd.jl:128-157: 3-D box kernel on ones; Fill(0) gives (2/3)^k at
+    faces, edges and corners; every Pad style gives ones."""
+    img = F(np.ones((10, 10, 10)))
+    K = np.full((3, 3, 3), 1 / 27)
+    for style in ["replicate", "circular", "symmetric", "reflect"]:
+        np.testing.assert_allclose(be.dense(img, K, (-1, -1, -1), style), img, rtol=1e-12)
+    t = np.ones((10, 10, 10))
+    for i in (0, 9):
+        t[:, :, i] = t[:, i, :] = t[i, :, :] = 2 / 3
+    for i in (0, 9):
+        for j in (0, 9):
+            t[:, i, j] = t[i, :, j] = t[i, j, :] = (2 / 3) ** 2
+    for i in (0, 9):
+        for j in (0, 9):
+            for k in (0, 9):
+                t[i, j, k] = (2 / 3) ** 3
+    np.testing.assert_allclose(be.dense(img, K, (-1, -1, -1), "fill"), t, rtol=1e-12)
+
+
+def check_cascade_equals_dense(be):
+    """test/cascade.jl:4-39: a cascade equals the convolved dense kernel for
+    every border."""
+    rng = np.random.default_rng(5)
+    a = F(rng.random(15))
+    c = np.array([1.0, 2, 3, 2, 1])
+    for style in BORDERS:
+        afc = be.cascade(a, [(0, -1, np.ones(3)), (0, -1, np.ones(3))], style)
+        af2 = be.dense(a, c, (-2,), style)
+        np.testing.assert_allclose(afc, af2, rtol=1e-12)
+    a = F(rng.random((15, 15)))
+    kx, ky = (0, -1, np.ones(3)), (1, -1, np.ones(3))
+    kern2 = np.outer(c, c)
+    kern2x = np.outer(c, np.ones(3))
+    kern2y = np.outer(np.ones(3), c)
+    for style in BORDERS:
+        np.testing.assert_allclose(be.cascade(a, [kx, ky, kx, ky], style),
+                                   be.dense(a, kern2, (-2, -2), style), rtol=1e-12)
+        np.testing.assert_allclose(be.cascade(a, [kx, kx, ky, ky], style),
+                                   be.dense(a, kern2, (-2, -2), style), rtol=1e-12)
+        np.testing.assert_allclose(be.cascade(a, [kx, kx, ky], style),
+                                   be.dense(a, kern2x, (-2, -1), style), rtol=1e-12)
+        np.testing.assert_allclose(be.cascade(a, [ky, kx, ky], style),
+                                   be.dense(a, kern2y, (-1, -2), style), rtol=1e-12)
+
+
+def check_fill_interior(be, gauss_factors):
+    """test/2d.jl:241-268 (issue #85): Fill(0) and Fill(10) agree inside and
+    differ at the corner."""
+    A = F(np.ones((8, 8)))
+    r1 = be.cascade(A, gauss_factors, "fill", 0.0)
+    r2 = be.cascade(A, gauss_factors, "fill", 10.0)
+    assert r1[3, 3] == r2[3, 3]
+    assert r1[0, 0] != r2[0, 0]
+
+
+def check_prewitt_band(be):
+    """test/2d.jl:7-25: Prewitt factors on a UInt8 diagonal band."""
+    m = np.zeros((20, 20))
+    for i in range(-2, 3):
+        idx = np.arange(max(0, -i), min(20, 20 - i))
+        m[idx, idx + i] = 255
+    m = F(m)
+    target = np.zeros((20, 20))
+    dv = [42.5, 85, 85, 42.5]
+    for i in range(1, 5):
+        idx = np.arange(0, 20 - i)
+        target[idx, idx + i] = dv[i - 1]
+        target[idx + i, idx] = -dv[i - 1]
+    facs = [(0, -1, np.array([-1.0, 0.0, 1.0]) / 2), (1, -1, np.array([1.0, 1.0, 1.0]) / 3)]
+    mf = be.cascade(m, facs, "replicate")
+    np.testing.assert_allclose(mf[1:19, 1:19], target[1:19, 1:19], rtol=1e-12, atol=1e-9)
+
+
+# ------------------------------------------------------------------- Laplacian
+def check_laplacian(be, arith="f64"):
+    """test/specialty.jl:6-156: impulse goldens and edge coefficients, exact."""
+    def imp(shape, idx):
+        a = np.zeros(shape)
+        a[idx] = 1
+        return F(a)
+    a = imp((5,), 2)
+    assert np.array_equal(be.laplacian(a, [1], "replicate", arith=arith), [0, 1, -2, 1, 0])
+    a = imp((5,), 0)
+    for style, c in (("replicate", -1), ("fill", -2)):
+        assert np.array_equal(be.laplacian(a, [1], style, arith=arith), [c, 1, 0, 0, 0])
+    a = imp((5, 5), (2, 2))
+    exp = np.zeros((5, 5))
+    exp[2, 2] = -4
+    exp[1, 2] = exp[3, 2] = exp[2, 1] = exp[2, 3] = 1
+    assert np.array_equal(be.laplacian(a, [1, 1], "replicate", arith=arith), exp)
+    a = imp((5, 5), (2, 0))
+    for style, c in (("replicate", -3), ("fill", -4)):
+        exp = np.zeros((5, 5))
+        exp[1, 0] = exp[3, 0] = exp[2, 1] = 1
+        exp[2, 0] = c
+        assert np.array_equal(be.laplacian(a, [1, 1], style, arith=arith), exp), style
+    a = imp((5, 5), (4, 4))
+    for style, c in (("replicate", -2), ("fill", -4)):
+        exp = np.zeros((5, 5))
+        exp[3, 4] = exp[4, 3] = 1
+        exp[4, 4] = c
+        assert np.array_equal(be.laplacian(a, [1, 1], style, arith=arith), exp), style
+    # vertical only: Laplacian((true,false))
+    a = imp((5, 5), (2, 2))
+    exp = np.zeros((5, 5))
+    exp[1, 2] = exp[3, 2] = 1
+    exp[2, 2] = -2
+    assert np.array_equal(be.laplacian(a, [1, 0], "replicate", arith=arith), exp)
+    a = imp((5, 5), (2, 0))
+    for style, c in (("replicate", -2), ("fill", -2)):
+        exp = np.zeros((5, 5))
+        exp[1, 0] = exp[3, 0] = 1
+        exp[2, 0] = c
+        assert np.array_equal(be.laplacian(a, [1, 0], style, arith=arith), exp), style
+    a = imp((5, 5), (4, 4))
+    for style, c in (("replicate", -1), ("fill", -2)):
+        exp = np.zeros((5, 5))
+        exp[3, 4] = 1
+        exp[4, 4] = c
+        assert np.array_equal(be.laplacian(a, [1, 0], style, arith=arith), exp), style
+
+
+# ------------------------------------------------------------------- gradients
+SOBEL = (np.array([-1.0, 0.0, 1.0]) / 2, np.array([1.0, 2.0, 1.0]) / 4)
+
+
+def sobel_factors(nd, d, extended=None):
+    ext = extended or [True] * nd
+    fs = []
+    for e in range(nd):
+        if not ext[e]:
+            continue
+        fs.append((e, -1, SOBEL[0] if e == d else SOBEL[1]))
+    return fs
+
+
+def check_gradient_ramps(be):
+    """test/gradient.jl:4-70: linear ramps have constant gradients inside
+    (the reference checks with Inner(); here the interior of a replicate result)."""
+    y = np.arange(1, 6)[:, None] * np.ones((1, 7))
+    x = np.ones((5, 1)) * np.arange(1, 8)[None, :]
+    for img, ey, ex in ((F(y), 1, 0), (F(x), 0, 1)):
+        gy = be.cascade(img, sobel_factors(2, 0), "replicate")
+        gx = be.cascade(img, sobel_factors(2, 1), "replicate")
+        assert np.all(np.abs(gy[1:-1, 1:-1] - ey) < 1e-4)
+        assert np.all(np.abs(gx[1:-1, 1:-1] - ex) < 1e-4)
+    y3 = np.arange(1, 6)[:, None, None] * np.ones((5, 7, 6))
+    x3 = np.arange(1, 8)[None, :, None] * np.ones((5, 7, 6))
+    z3 = np.arange(1, 7)[None, None, :] * np.ones((5, 7, 6))
+    for img, e in ((F(y3), (1, 0, 0)), (F(x3), (0, 1, 0)), (F(z3), (0, 0, 1))):
+        for d in range(3):
+            g = be.cascade(img, sobel_factors(3, d), "replicate")
+            assert np.all(np.abs(g[1:-1, 1:-1, 1:-1] - e[d]) < 1e-4)
+
+
+# ------------------------------------------------------------------- mapwindow
+def check_extrema_lemire_golden(be):
+    """test/mapwindow.jl:17-46: 1-D extrema, windows 1..7 (even included)."""
+    n = 0
+    for k in GOLDEN["extrema_lemire_1d"]:
+        A = F(k["A"])
+        mn, mx = be.extrema_lemire(A, [k["window"]])
+        exp = np.array(k["expected"])
+        assert np.array_equal(mn, exp[:, 0]) and np.array_equal(mx, exp[:, 1]), k["source"]
+        n += 1
+    assert n == 14
+
+
+def groundtruth(f, A, window):
+    """test/mapwindow.jl:5-14: reduce over clamped shifts."""
+    Aex = A.copy()
+    h = [w // 2 + 1 for w in window]
+    for shift in np.ndindex(*window):
+        for I in np.ndindex(*A.shape):
+            J = tuple(min(max(I[d] + shift[d] + 1 - h[d], 0), A.shape[d] - 1) for d in range(A.ndim))
+            Aex[I] = f(Aex[I], A[J])
+    return Aex
+
+
+def check_extrema_nd(be, seed=3):
+    """test/mapwindow.jl:47-73: 2-D and 3-D extrema against the clamp ground truth."""
+    rng = np.random.default_rng(seed)
+    A = rng.random((5, 5)) / 10
+    A[1, 1] = 0.8
+    A[3, 3] = 0.6
+    A = F(A)
+    for w in ((2, 2), (2, 3), (3, 2), (3, 3), (2, 5)):
+        mn, mx = be.extrema_lemire(A, list(w))
+        assert np.array_equal(mx, groundtruth(max, A, w))
+        assert np.array_equal(mn, groundtruth(min, A, w))
+    A = rng.random((5, 5, 5)) / 10
+    A[1, 1, 1] = 0.7
+    A[3, 3, 1] = 0.4
+    A[1, 1, 3] = 0.5
+    A = F(A)
+    for w in ((2, 2, 2), (2, 3, 2), (3, 2, 2), (2, 2, 3), (3, 3, 3), (2, 5, 3)):
+        mn, mx = be.extrema_lemire(A, list(w))
+        assert np.array_equal(mx, groundtruth(max, A, w))
+        assert np.array_equal(mn, groundtruth(min, A, w))
+
+
+def check_median_golden(be):
+    """test/mapwindow.jl:105-124: median goldens (default border replicate)."""
+    n = 0
+    for k in GOLDEN["median"]:
+        A = F(k["A"])
+        got = be.median(A, k["window_first"], k["window_len"], "replicate")
+        assert np.array_equal(got, np.array(k["expected"], dtype=np.float64)), k["source"]
+        n += 1
+    assert n == 6

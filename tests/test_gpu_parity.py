@@ -1,0 +1,392 @@
+"""GB300 kernels against the CPU oracle on seeded random inputs.
+
+Tolerances (stated by the FIR path's contract): linear filters within 1e-5
+normwise relative error (max|gpu - oracle| / max|oracle|) when the image is
+not Float64 (FP32 arithmetic on the GPU against the FP64 oracle), 1e-12 for
+Float64 images (FP64 on the GPU); border maps, Laplacian, median and extrema
+bit-exact.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+STYLES = ["replicate", "circular", "symmetric", "reflect", "fill"]
+RTOL = {"F32": 1e-5, "F64": 1e-12, "N0F8": 1e-5, "U8": 1e-5}
+
+
+def normwise(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    d = np.max(np.abs(a - b)) if a.size else 0.0
+    m = np.max(np.abs(b)) if b.size else 0.0
+    return d / m if m > 0 else d
+
+
+def make_img(rng, shape, kind):
+    if kind == "F32":
+        return np.asfortranarray(rng.random(shape, dtype=np.float32))
+    if kind == "F64":
+        return np.asfortranarray(rng.random(shape))
+    codes = np.asfortranarray(rng.integers(0, 256, shape, dtype=np.uint8))
+    return codes
+
+
+def values(ifx, img, kind):
+    """The numeric values the reference sees (N0f8: c/255)."""
+    if kind == "N0F8":
+        return img.astype(np.float64) / 255.0
+    return img.astype(np.float64)
+
+
+def wrap(ifx, img, kind):
+    return ifx.n0f8(img) if kind == "N0F8" else img
+
+
+def border_of(ifx, style, fill=0.7):
+    return ifx.Fill(fill) if style == "fill" else ifx.Pad(style)
+
+
+def fill_value(kind, fill=0.7):
+    if kind == "U8":
+        return 0.0
+    if kind == "N0F8":
+        return round(fill * 255) / 255.0
+    if kind == "F32":
+        return float(np.float32(fill))
+    return fill
+
+
+# --------------------------------------------------------------------- separable
+@pytest.mark.parametrize("kind", ["F32", "F64", "N0F8", "U8"])
+@pytest.mark.parametrize("style", STYLES)
+def test_separable_2d_random(gpu_ifx, oracle, kind, style):
+    ifx = gpu_ifx
+    rng = np.random.default_rng(hash((kind, style)) % 2 ** 32)
+    for shape in [(67, 45), (130, 7), (3, 200), (64, 64)]:
+        img = make_img(rng, shape, kind)
+        for _ in range(3):
+            lx, ly = int(rng.integers(1, 34)), int(rng.integers(1, 34))
+            fx, fy = int(rng.integers(-lx, 2)), int(rng.integers(-ly, 2))
+            wx, wy = rng.standard_normal(lx), rng.standard_normal(ly)
+            order = [(0, fx, wx), (1, fy, wy)] if rng.random() < 0.5 else [(1, fy, wy), (0, fx, wx)]
+            ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(w, (f,)), 2, ax) for ax, f, w in order)
+            fill = 0.7 if kind != "U8" else 3.0
+            b = ifx.Fill(fill) if style == "fill" else ifx.Pad(style)
+            got = ifx.imfilter(wrap(ifx, img, kind), ks, b)
+            fv = fill_value(kind, fill) if kind != "U8" else 3.0
+            ref = oracle.imfilter_cascade(values(ifx, img, kind), order, style, fv)
+            assert got.dtype == np.float64
+            assert normwise(got, ref) <= RTOL[kind], (shape, order, style)
+
+
+@pytest.mark.parametrize("taps", [9, 17])
+def test_config_512_gaussian_replicate(gpu_ifx, oracle, taps):
+    """512x512 Float32 uniform[0,1) seed 1, KernelFactors.gaussian((2,2)) (9 taps)
+    and gaussian((2,2),(17,17)), Pad(:replicate): Float64 output."""
+    ifx = gpu_ifx
+    img = np.asfortranarray(np.random.default_rng(1).random((512, 512), dtype=np.float32))
+    k = ifx.KernelFactors.gaussian((2, 2), None if taps == 9 else (17, 17))
+    got = ifx.imfilter(img, k, "replicate", ifx.Algorithm.GB300())
+    facs = [(f.axis, f.data.first[0], np.asarray(f.data.data)) for f in k]
+    ref = oracle.imfilter_cascade(img.astype(np.float64), facs, "replicate")
+    assert got.dtype == np.float64
+    assert normwise(got, ref) <= 1e-5
+
+
+@pytest.mark.parametrize("style", STYLES)
+def test_separable_nd_generic(gpu_ifx, oracle, style):
+    """1-D, 3-D, 4-D and repeated-axis cascades (the generic box pipeline)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(99)
+    cases = [((50,), [(0, -3, rng.standard_normal(7))]),
+             ((12, 9, 10), [(0, -2, rng.standard_normal(5)), (1, -1, rng.standard_normal(3)),
+                            (2, -4, rng.standard_normal(9))]),
+             ((6, 5, 4, 7), [(3, -1, rng.standard_normal(3)), (0, 0, rng.standard_normal(2)),
+                             (2, -1, rng.standard_normal(3))]),
+             ((20, 17), [(0, -1, np.ones(3)), (1, -1, np.ones(3)), (0, -1, np.ones(3)),
+                         (1, 0, rng.standard_normal(4))])]
+    for shape, facs in cases:
+        for kind in ("F32", "F64"):
+            img = make_img(rng, shape, kind)
+            ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(w, (f,)), len(shape), ax) for ax, f, w in facs)
+            got = ifx.imfilter(img, ks, border_of(ifx, style))
+            ref = oracle.imfilter_cascade(img.astype(np.float64), facs, style,
+                                          fill_value(kind))
+            assert normwise(got, ref) <= RTOL[kind], (shape, style, kind)
+
+
+def test_separable_3d_volume(gpu_ifx, oracle):
+    """σ=(3,3,1.5) Gaussian (13/13/9 taps), Pad(:symmetric), on a 64^3 volume with
+    1% impulse outliers (the 256^3 workload's shape of input, smaller)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(3)
+    vol = rng.random((64, 64, 64), dtype=np.float32)
+    m = rng.random(vol.shape) < 0.01
+    vol[m] = 1.0
+    vol = np.asfortranarray(vol)
+    k = ifx.KernelFactors.gaussian((3, 3, 1.5))
+    assert [len(f.data) for f in k] == [13, 13, 9]
+    got = ifx.imfilter(vol, k, "symmetric")
+    facs = [(f.axis, f.data.first[0], np.asarray(f.data.data)) for f in k]
+    ref = oracle.imfilter_cascade(vol.astype(np.float64), facs, "symmetric")
+    assert normwise(got, ref) <= 1e-5
+
+
+# --------------------------------------------------------------------- dense
+@pytest.mark.parametrize("ksz,seed", [(5, 20), (15, 21), (31, 22)])
+@pytest.mark.parametrize("style", ["reflect", "fill", "replicate", "circular", "symmetric"])
+def test_dense_2d(gpu_ifx, oracle, ksz, seed, style):
+    """N(0,1) kernels normalised to sum 1 (seeds 20-22, |sum| >= 0.1)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(seed)
+    while True:
+        K = rng.standard_normal((ksz, ksz))
+        if abs(K.sum()) >= 0.1:
+            break
+    K = K / K.sum()
+    img = np.asfortranarray(np.random.default_rng(2).random((301, 257), dtype=np.float32))
+    kern = ifx.centered(K)
+    fk = ifx.factorkernel(kern)
+    assert len(fk) == 2 and ifx.iscopy(fk[0])       # full rank: stays dense
+    b = ifx.Fill(0) if style == "fill" else ifx.Pad(style)
+    got = ifx.imfilter(img, kern, b)
+    ref = oracle.imfilter_dense(img.astype(np.float64), K, kern.first, style, 0.0)
+    assert got.dtype == np.float64
+    assert normwise(got, ref) <= 1e-5
+    got64 = ifx.imfilter(img.astype(np.float64), kern, b)
+    assert normwise(got64, ref) <= 1e-12
+
+
+def test_dense_nd_and_offcenter(gpu_ifx, oracle):
+    ifx = gpu_ifx
+    rng = np.random.default_rng(4)
+    img = np.asfortranarray(rng.random((17, 13, 11)))
+    K = rng.standard_normal((3, 4, 2))
+    for style in STYLES:
+        got = ifx.imfilter(img, (ifx.OffsetKernel(K, (-1, 0, -2)),), border_of(ifx, style))
+        ref = oracle.imfilter_dense(img, K, (-1, 0, -2), style, 0.7)
+        assert normwise(got, ref) <= 1e-12, style
+    img2 = np.asfortranarray(rng.random((40, 33), dtype=np.float32))
+    K2 = rng.standard_normal((4, 6))
+    got = ifx.imfilter(img2, (ifx.OffsetKernel(K2, (1, -7)),), "circular")
+    ref = oracle.imfilter_dense(img2.astype(np.float64), K2, (1, -7), "circular")
+    assert normwise(got, ref) <= 1e-5
+
+
+# --------------------------------------------------------------------- Laplacian
+@pytest.mark.parametrize("kind,arith", [("F32", "f32"), ("F64", "f64"), ("N0F8", "f32"),
+                                        ("U8", "int")])
+@pytest.mark.parametrize("style", STYLES)
+def test_laplacian_exact(gpu_ifx, oracle, kind, arith, style):
+    ifx = gpu_ifx
+    rng = np.random.default_rng(8)
+    for shape, flags in [((37, 29), (True, True)), ((37, 29), (False, True)), ((9, 8, 7), (True, True, True)),
+                         ((40,), (True,))]:
+        img = make_img(rng, shape, kind)
+        fill = 0.0 if kind in ("U8",) else 0.5
+        b = ifx.Fill(fill) if style == "fill" else ifx.Pad(style)
+        got = ifx.imfilter(wrap(ifx, img, kind), ifx.Kernel.Laplacian(flags), b)
+        if kind == "N0F8":
+            vals = (img.astype(np.float32) / np.float32(255)).astype(np.float64)
+            fv = float(np.float32(round(fill * 255) / np.float32(255)))
+        else:
+            vals = img.astype(np.float64)
+            fv = fill if kind != "F32" else float(np.float32(fill))
+        ref = oracle.laplacian(vals, [int(f) for f in flags], style, fv, arith)
+        assert got.dtype == {"F32": np.float32, "F64": np.float64, "N0F8": np.float32,
+                             "U8": np.int16}[kind]
+        assert np.array_equal(np.asarray(got, np.float64), ref), (shape, flags, style)
+
+
+# --------------------------------------------------------------------- gradients
+@pytest.mark.parametrize("name", ["sobel", "prewitt", "scharr", "bickley", "ando3"])
+@pytest.mark.parametrize("style", STYLES)
+def test_imgradients(gpu_ifx, oracle, name, style):
+    ifx = gpu_ifx
+    rng = np.random.default_rng(12)
+    fn = getattr(ifx.KernelFactors, name)
+    k1, k2 = fn.gradient_pair
+    for shape in [(33, 28), (16, 12, 10), (25, 1, 9)]:
+        img = np.asfortranarray(rng.random(shape, dtype=np.float32))
+        if style == "reflect" and 1 in shape:
+            with pytest.raises(ifx.ErrorException):
+                ifx.imgradients(img, fn, ifx.Pad(style))
+            continue
+        gs = ifx.imgradients(img, fn, border_of(ifx, style))
+        assert len(gs) == len(shape)
+        for d, g in enumerate(gs):
+            facs = []
+            for e in range(len(shape)):
+                if shape[e] > 1:
+                    facs.append((e, -1, k1 if e == d else k2))
+            ref = oracle.imfilter_cascade(img.astype(np.float64), facs, style,
+                                          float(np.float32(0.7)))
+            assert g.dtype == np.float64
+            assert normwise(g, ref) <= 1e-5 or np.max(np.abs(g - ref)) < 1e-6, (shape, d)
+
+
+def test_imgradients_ando4_dense_kernels(gpu_ifx, oracle):
+    ifx = gpu_ifx
+    img = np.asfortranarray(np.random.default_rng(5).random((30, 31)))
+    gy, gx = ifx.imgradients(img, ifx.KernelFactors.ando4, "replicate")
+    k1, k2 = ifx.KernelFactors.ando4.gradient_pair
+    ref = oracle.imfilter_cascade(img, [(0, -1, k1), (1, -1, k2)], "replicate")
+    assert normwise(gy, ref) <= 1e-12
+    dy, dx = ifx.imgradients(img, ifx.Kernel.sobel, "reflect")
+    s1, s2 = ifx.KernelFactors.sobel.gradient_pair
+    ref = oracle.imfilter_cascade(img, [(0, -1, s2), (1, -1, s1)], "reflect")
+    assert normwise(dx, ref) <= 1e-12
+
+
+# --------------------------------------------------------------------- median
+@pytest.mark.parametrize("kind", ["N0F8", "U8"])
+@pytest.mark.parametrize("style", STYLES)
+def test_median_u8_exact(gpu_ifx, oracle, kind, style):
+    ifx = gpu_ifx
+    rng = np.random.default_rng(21)
+    for shape in [(130, 37), (9, 300), (5, 6)]:
+        img = make_img(rng, shape, kind)
+        salt = rng.random(shape) < 0.05
+        img[salt] = np.where(rng.random(salt.sum()) < 0.5, 0, 255)
+        for win in [(3, 3), (5, 5), (7, 7), (9, 9), (3, 5), (1, 7)]:
+            fill = 0.2 if kind == "N0F8" else 51
+            b = ifx.Fill(fill) if style == "fill" else ifx.Pad(style)
+            if style == "reflect" and 1 in win:
+                continue
+            got = ifx.mapwindow(ifx.median, wrap(ifx, img, kind), win, border=b)
+            code = round(fill * 255) if kind == "N0F8" else fill
+            ref = oracle.mapwindow_median(img.astype(np.float64), [-(w // 2) for w in win],
+                                          list(win), style, float(code))
+            if kind == "N0F8":
+                assert got.dtype == np.float32
+                exp = (ref.astype(np.float32) / np.float32(255))
+                assert np.array_equal(got, exp), (shape, win, style)
+            else:
+                assert got.dtype == np.float64
+                assert np.array_equal(got, ref), (shape, win, style)
+
+
+@pytest.mark.parametrize("kind", ["F32", "F64"])
+def test_median_float_nd(gpu_ifx, oracle, kind):
+    ifx = gpu_ifx
+    rng = np.random.default_rng(22)
+    for shape, win in [((31, 17), (3, 5)), ((9, 8, 7), (3, 3, 3)), ((50,), (7,))]:
+        img = make_img(rng, shape, kind)
+        for style in STYLES:
+            got = ifx.mapwindow(ifx.median, img, win, border=border_of(ifx, style, 0.25))
+            ref = oracle.mapwindow_median(img.astype(np.float64), [-(w // 2) for w in win],
+                                          list(win), style, fill_value(kind, 0.25))
+            assert np.array_equal(np.asarray(got, np.float64), ref), (shape, style)
+
+
+# --------------------------------------------------------------------- extrema
+@pytest.mark.parametrize("kind", ["U8", "F32", "F64"])
+def test_extrema_exact(gpu_ifx, oracle, kind):
+    ifx = gpu_ifx
+    rng = np.random.default_rng(31)
+    for shape in [(70, 45), (11, 9, 13)]:
+        img = make_img(rng, shape, kind)
+        nd = len(shape)
+        for w in ([7] * nd, [15] * nd, [4] * nd, [2, 5, 3][:nd]):
+            mm = ifx.mapwindow(ifx.extrema, img, tuple(w))              # Lemire path
+            mn, mx = oracle.extrema_trunc(img.astype(np.float64), w)
+            assert np.array_equal(np.asarray(mm[0], np.float64), mn)
+            assert np.array_equal(np.asarray(mm[1], np.float64), mx)
+        for style in STYLES:
+            w = [7] * nd
+            fill = 77 if kind == "U8" else 0.5
+            b = ifx.Fill(fill) if style == "fill" else ifx.Pad(style)
+            mm = ifx.mapwindow(ifx.extrema, img, tuple(w), border=b)
+            mn, mx = oracle.mapwindow_extrema(img.astype(np.float64), [-3] * nd, w, style,
+                                              float(fill) if kind != "F32" else float(np.float32(fill)))
+            assert np.array_equal(np.asarray(mm[0], np.float64), mn), style
+            assert np.array_equal(np.asarray(mm[1], np.float64), mx), style
+            lo = ifx.mapwindow(ifx.minimum, img, tuple(w), border=b)
+            hi = ifx.mapwindow(ifx.maximum, img, tuple(w), border=b)
+            assert np.array_equal(np.asarray(lo, np.float64), mn)
+            assert np.array_equal(np.asarray(hi, np.float64), mx)
+
+
+def test_config_2048_rank_filters(gpu_ifx, oracle):
+    """2048x2048 Gray{N0f8} with 5% salt-and-pepper, median 3x3/5x5 and extrema
+    7x7/15x15, Pad(:symmetric): bit-exact on sampled rows and on all edges."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(4)
+    img = rng.integers(0, 256, (2048, 2048), dtype=np.uint8)
+    r = rng.random(img.shape)
+    img[r < 0.025] = 0
+    img[(r >= 0.025) & (r < 0.05)] = 255
+    img = np.asfortranarray(img)
+    for w in (3, 5):
+        got = ifx.mapwindow(ifx.median, ifx.n0f8(img), (w, w), border="symmetric")
+        codes = np.rint(got.astype(np.float64) * 255).astype(np.uint8)
+        rows = [0, 1, 2, 1000, 2045, 2046, 2047]
+        for y in rows:
+            ref = oracle.median_u8_rows(img, [-(w // 2)] * 2, [w, w], "symmetric", 0.0, y, y + 1)
+            assert np.array_equal(codes[:, y], ref[:, y])
+        exp = got[:, 7]
+        assert np.array_equal(exp, codes[:, 7].astype(np.float32) / np.float32(255))
+    for w in (7, 15):
+        mm = ifx.mapwindow(ifx.extrema, ifx.n0f8(img), (w, w), border="symmetric")
+        sub = np.asfortranarray(img[:, :64])
+        mn, mx = oracle.extrema_trunc(sub.astype(np.float64), [w, w])
+        h = w // 2
+        assert np.array_equal(mm[0][:, : 64 - h].astype(np.float64), mn[:, : 64 - h])
+        assert np.array_equal(mm[1][:, : 64 - h].astype(np.float64), mx[:, : 64 - h])
+
+
+# --------------------------------------------------------------------- full-size properties
+def test_dense_4096_circular_shift_equivariance(gpu_ifx):
+    """4096x4096, 31x31 dense, circular border: filtering commutes with a
+    circular shift (exactly: the same products and sums in the same order)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(2)
+    img = np.asfortranarray(rng.random((4096, 4096), dtype=np.float32))
+    K = rng.standard_normal((31, 31))
+    K /= K.sum()
+    a = ifx.imfilter(img, ifx.centered(K), "circular")
+    b = ifx.imfilter(np.asfortranarray(np.roll(img, (64, 32), axis=(0, 1))), ifx.centered(K), "circular")
+    assert np.array_equal(np.roll(a, (64, 32), axis=(0, 1)), b)
+
+
+def test_linearity_full_size(gpu_ifx):
+    """256^3 volume, σ=(3,3,1.5), symmetric: filtering is linear."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(3)
+    a = np.asfortranarray(rng.random((256, 256, 256), dtype=np.float32))
+    b = np.asfortranarray(rng.random((256, 256, 256), dtype=np.float32))
+    k = ifx.KernelFactors.gaussian((3, 3, 1.5))
+    fa = ifx.imfilter(a, k, "symmetric")
+    fb = ifx.imfilter(b, k, "symmetric")
+    fab = ifx.imfilter(np.asfortranarray(a + b), k, "symmetric")
+    assert normwise(fab, fa + fb) <= 1e-5
+    c = np.asfortranarray(np.full((256, 256, 256), 0.25, dtype=np.float32))
+    fc = ifx.imfilter(c, k, "symmetric")
+    assert np.max(np.abs(fc - 0.25)) < 1e-6
+
+
+# --------------------------------------------------------------------- device arrays
+def test_device_resident_arrays(gpu_ifx, oracle):
+    ifx = gpu_ifx
+    import torch
+    rng = np.random.default_rng(6)
+    img = np.asfortranarray(rng.random((300, 200), dtype=np.float32))
+    d = ifx.DeviceArray.from_host(img)
+    k = ifx.KernelFactors.gaussian((2, 2))
+    out = ifx.imfilter(d, k, "reflect")
+    torch.cuda.synchronize()
+    assert isinstance(out, ifx.DeviceArray)
+    host = ifx.imfilter(img, k, "reflect")
+    assert np.array_equal(out.numpy(), host)
+    u = ifx.DeviceArray.from_host(ifx.n0f8(rng.integers(0, 256, (128, 96), dtype=np.uint8)))
+    med = ifx.mapwindow(ifx.median, u, (5, 5), border="symmetric")
+    torch.cuda.synchronize()
+    assert np.array_equal(med.numpy(), ifx.mapwindow(ifx.median, u.numpy(), (5, 5), border="symmetric"))
+
+
+def test_launch_counter_counts_kernels(gpu_ifx):
+    ifx = gpu_ifx
+    before = ifx.launch_count()
+    ifx.imfilter(np.asfortranarray(np.ones((40, 40), np.float32)), ifx.KernelFactors.gaussian((1, 1)))
+    assert ifx.launch_count() == before + 1          # one fused tile kernel

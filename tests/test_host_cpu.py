@@ -1,0 +1,192 @@
+"""Host-side logic and the C-ABI boundary, without a GPU.
+
+The library must load on a machine without a GPU and export every entry
+point declared in include/ifx_gb300.h; argument validation happens on the
+host before any CUDA call and maps to the reference's exception classes.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib(ifx):
+    import __graft_entry__ as g
+    g._load_builder().build()
+    return ifx._abi.load()
+
+
+def declared_symbols():
+    out = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            out |= set(re.findall(r"^\s*(?:int|const char \*|uint64_t)\s*\**\s*(ifx_\w+)\s*\(", txt, re.M))
+    return out
+
+
+def test_library_exports_every_declared_symbol(lib, ifx):
+    syms = declared_symbols()
+    assert len(syms) >= 13
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(ifx._abi.SYMBOLS) <= syms
+    assert lib.ifx_abi_version() == 1
+
+
+def test_library_is_built_for_sm103a():
+    import subprocess
+    so = os.path.join(ROOT, "imagefiltering.jl_gb300", "_build", "libifx_gb300.so")
+    r = subprocess.run(["cuobjdump", "--list-elf", so], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in r.stdout
+
+
+def _arr(ifx, a, kind):
+    p = a.ctypes.data
+    return ifx._abi.describe(p, kind, a.shape, [s // a.itemsize for s in a.strides])
+
+
+def test_validation_errors_before_any_cuda_call(lib, ifx):
+    A = ifx._abi
+    img = np.zeros((5, 5), order="F")
+    out = np.zeros((5, 5), order="F")
+    ai, ao = _arr(ifx, img, "F64"), _arr(ifx, out, "F64")
+    w = np.array([1.0, 2.0, 1.0])
+    f = (A.IfxFactor * 1)()
+    f[0].axis, f[0].length, f[0].first, f[0].weights = 0, 3, -1, A.dptr(w)
+    # unknown border style -> ArgumentError
+    b = A.border_struct("replicate")
+    b.style = 9
+    assert lib.ifx_imfilter_factored(None, ao, ai, 1, f, b, None) == 1
+    assert "not a recognized border" in lib.ifx_last_error().decode()
+    # factor on a missing axis -> DimensionMismatch
+    f[0].axis = 2
+    assert lib.ifx_imfilter_factored(None, ao, ai, 1, f, A.border_struct("replicate"), None) == 2
+    f[0].axis = 0
+    # explicit padding too small (test/2d.jl:345-350) -> DimensionMismatch
+    b = A.border_struct("fill", [0, 0], [0, 0], 0.0)
+    assert lib.ifx_imfilter_factored(None, ao, ai, 1, f, b, None) == 2
+    # reflect on a length-1 axis -> the reference's DivideError
+    img1 = np.zeros((5, 1), order="F")
+    out1 = np.zeros((5, 1), order="F")
+    rc = lib.ifx_imfilter_factored(None, _arr(ifx, out1, "F64"), _arr(ifx, img1, "F64"), 1, f,
+                                   A.border_struct("reflect"), None)
+    assert rc == 3 and "DivideError" in lib.ifx_last_error().decode()
+    # output axes must match
+    out2 = np.zeros((4, 5), order="F")
+    assert lib.ifx_imfilter_factored(None, _arr(ifx, out2, "F64"), ai, 1, f,
+                                     A.border_struct("replicate"), None) == 2
+    # non column-major input
+    imgc = np.zeros((5, 6))
+    rc = lib.ifx_imfilter_factored(None, _arr(ifx, np.zeros((5, 6), order="F"), "F64"),
+                                   _arr(ifx, imgc, "F64"), 1, f, A.border_struct("replicate"), None)
+    assert rc == 1
+    # Fill value not representable in UInt8 (src/borderarray.jl:11-20)
+    u8 = np.zeros((5, 5), dtype=np.uint8, order="F")
+    rc = lib.ifx_mapwindow_median(None, _arr(ifx, u8, "U8"), _arr(ifx, u8, "U8"),
+                                  (C.c_int64 * 4)(-1, -1), (C.c_int64 * 4)(3, 3),
+                                  A.border_struct("fill", None, None, 0.5), None)
+    assert rc == 1 and "Cannot convert" in lib.ifx_last_error().decode()
+    # a NULL context is reported after validation passes
+    rc = lib.ifx_imfilter_factored(None, ao, ai, 1, f, A.border_struct("replicate"), None)
+    assert rc == 1 and "context" in lib.ifx_last_error().decode()
+
+
+def test_borderinstance(ifx):
+    assert ifx.borderinstance("replicate").style == "replicate"
+    with pytest.raises(ifx.ArgumentError, match="deprecated"):
+        ifx.borderinstance("inner")
+    with pytest.raises(ifx.ArgumentError, match="not a recognized border"):
+        ifx.borderinstance("nonsense")
+    p = ifx.Pad("circular", (1, 2), (3, 4))
+    assert p.lo == (1, 2) and p.hi == (3, 4)
+    assert ifx.Pad(1, 1).lo == (1, 1) and ifx.Pad(1, 1).style == "replicate"
+    assert ifx.Fill(0, (3, 2)).hi == (3, 2)
+
+
+def test_filter_type(ifx):
+    kf = ifx.KernelFactors.gaussian((2, 2))
+    kf32 = ifx.KernelFactors.gaussian((np.float32(2), np.float32(2)))
+    assert ifx.filter_type("F32", kf) == "F64"        # src/imfilter.jl:1133 (survey item 5)
+    assert ifx.filter_type("F32", kf32) == "F32"
+    assert ifx.filter_type("N0F8", kf) == "F64"
+    assert ifx.filter_type("U8", kf) == "F64"
+    L = ifx.Kernel.Laplacian()
+    assert ifx.filter_type("N0F8", L) == "F32"        # src/imfilter.jl:1135
+    assert ifx.filter_type("U8", L) == "I16"          # src/imfilter.jl:1139
+    assert ifx.filter_type("F64", L) == "F64"
+
+
+def test_gaussian_weights(ifx):
+    """test/specialty.jl:168-199."""
+    def cmp(s, xr):
+        c = np.exp(-np.asarray(xr, float) ** 2 / (2 * s ** 2))
+        return c / c.sum()
+    g = ifx.KernelFactors.gaussian(2, 9)
+    assert g.first == (-4,)
+    np.testing.assert_allclose(g.data, cmp(2, range(-4, 5)), rtol=1e-14)
+    k = ifx.KernelFactors.gaussian((2, 3), (9, 7))
+    np.testing.assert_allclose(k[1].data.data, cmp(3, range(-3, 4)), rtol=1e-14)
+    assert len(ifx.KernelFactors.gaussian(2).data) == 9        # 4*ceil(σ)+1 (survey item 4)
+    assert abs(ifx.KernelFactors.gaussian(5).data.sum() - 1) < 1e-14
+    k = ifx.KernelFactors.gaussian((3, 3, 0))
+    assert list(k[2].data.data) == [1.0] and k[2].data.first == (0,)
+    with pytest.raises(ValueError):
+        ifx.KernelFactors.gaussian(2, 8)
+    np.testing.assert_allclose(ifx.Kernel.gaussian((2, 3), (9, 7)).data,
+                               np.outer(cmp(2, range(-4, 5)), cmp(3, range(-3, 4))), rtol=1e-14)
+    with pytest.raises(ValueError):
+        ifx.KernelFactors.box((3, 4, 5))
+
+
+def test_laplacian_and_log_kernels(ifx):
+    """test/specialty.jl:6-20 (dense form of Laplacian) and LoG sizes."""
+    L = ifx.Kernel.Laplacian().dense()
+    assert L.first == (-1, -1)
+    assert np.array_equal(L.data, [[0, 1, 0], [1, -4, 1], [0, 1, 0]])
+    L = ifx.Kernel.Laplacian((True, False)).dense()
+    assert np.array_equal(L.data.reshape(-1), [1, -2, 1]) and L.first == (-1, 0)
+    L = ifx.Kernel.Laplacian([2], 2).dense()
+    assert L.shape == (1, 3) and L.first == (0, -1)
+    k = ifx.Kernel.LoG(2.5)
+    assert k.shape == (23, 23) and k.first == (-11, -11)      # 2*(ceil(8.5σ)>>1)+1
+    np.testing.assert_allclose(ifx.Kernel.laplacian2d(0.5).data,
+                               [[1 / 3, 1 / 3, 1 / 3], [1 / 3, -8 / 3, 1 / 3], [1 / 3, 1 / 3, 1 / 3]])
+
+
+def test_factorkernel_svd(ifx):
+    """src/imfilter.jl:1159-1184: separable 2-D kernels become two factors."""
+    k = ifx.Kernel.gaussian((1, 1), (3, 3))
+    fk = ifx.factorkernel(k)
+    assert len(fk) == 2
+    np.testing.assert_allclose(fk[0].data * fk[1].data, k.data, rtol=1e-12)
+    rng = np.random.default_rng(0)
+    K = ifx.centered(rng.standard_normal((5, 5)))
+    fk = ifx.factorkernel(K)
+    assert len(fk) == 2 and ifx.iscopy(fk[0]) and fk[1] is K
+
+
+def test_resolve_window(ifx):
+    from imagefiltering_gb300 import rank
+    assert rank.resolve_window((3, 5), 2) == ([-1, -2], [3, 5])
+    with pytest.raises(ifx.ErrorException, match="odd"):
+        rank.resolve_window((4, 4), 2)
+    assert rank.resolve_window((4,), 1, allow_even=True) == ([-2], [4])
+    with pytest.raises(ifx.ArgumentError, match="empty window"):
+        rank.resolve_window((), 2)
+    assert rank.resolve_window((range(-2, 1),), 1) == ([-2], [3])
+
+
+def test_no_cpu_algorithms(ifx):
+    img = np.zeros((4, 4), dtype=np.float32, order="F")
+    with pytest.raises(ifx.Unsupported):
+        ifx.imfilter(img, ifx.KernelFactors.gaussian((1, 1)), "replicate", ifx.Algorithm.FIR())
+    with pytest.raises(ifx.Unsupported):
+        ifx.mapwindow(lambda v: v.sum(), img, (3, 3))
