@@ -1,0 +1,424 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FIR / rank-filter path.  Prints ONE JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload stream|dense4096|volume256x8|rank2048|gauss512]
+
+Default workload ("stream"): the mixed serving stream -- 2-D images with one
+side log-uniform in 64..4096 (aspect 1:4..4:1), Float32 or N0f8, op drawn from
+{Gaussian σ~U[0.5,8], Sobel gradient, Laplacian 3x3, median 3x3/5x5}, border
+drawn from the Pad styles (seed 5).  A step is one wave of `--per-step`
+requests of that stream, in stream order; K steps cover K*per_step requests.
+
+  value  Mpixel/s (output pixels of all requests / device time), inputs
+         resident in HBM, through the batched engine when built, else one
+         C-ABI call per request ("plain").
+  e2e    the same metric through the public API with pinned HOST buffers:
+         host->device copies of each request's image and device->host copies
+         of its outputs inside the timed region.
+Under torchrun (N>1) each rank runs the same stream as an independent replica
+(the path does not exchange data); value = all ranks' pixels / max time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+# ----------------------------------------------------------------------------- args
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="stream",
+                   choices=["stream", "dense4096", "volume256x8", "rank2048", "gauss512"])
+    p.add_argument("--per-step", type=int, default=500)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    return p.parse_args()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    import torch
+    torch.cuda.set_device(local)
+    os.environ["IFX_DEVICE"] = str(local)
+    dist.init_process_group("nccl")
+    return rank, ws, dist
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except Exception:
+            rows = []
+        sm, reasons, mx = [], set(), None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- stream
+def stream_calls(ifx, reqs, dev_inputs, out_arena, torch):
+    """One prebuilt C-ABI call per request (device pointers), as a plain caller
+    of the library makes them.  Returns [(op, fn, args, alg_bytes, pixels)]."""
+    import ctypes as C
+    A = ifx._abi
+    ctx = A.context()
+    lib = ctx.lib
+    calls = []
+    off = 0
+    keep = []
+    for r, d_in in zip(reqs, dev_inputs):
+        ai = A.describe(d_in.data_ptr(), r.kind, (r.h, r.w))
+        outs = []
+        for k in r.out_kinds():
+            nbytes = r.pixels * (8 if k == "F64" else 4)
+            outs.append(A.describe(out_arena.data_ptr() + off, k, (r.h, r.w)))
+            off += (nbytes + 255) // 256 * 256
+        b = A.border_struct(r.style)
+        keep += [ai, b] + outs
+        stream = torch.cuda.current_stream().cuda_stream
+        if r.op == "gaussian":
+            g = np.ascontiguousarray(ifx.KernelFactors.gaussian(r.sigma).data, dtype=np.float64)
+            fac = (A.IfxFactor * 2)()
+            for i in range(2):
+                fac[i].axis, fac[i].length, fac[i].first, fac[i].weights = i, g.size, -(g.size // 2), A.dptr(g)
+            keep += [g, fac]
+            calls.append(("gaussian", lib.ifx_imfilter_factored,
+                          (ctx.handle, outs[0], ai, 2, fac, b, stream)))
+        elif r.op == "sobel":
+            d, s = ifx.KernelFactors.sobel.gradient_pair
+            d = np.ascontiguousarray(d)
+            s = np.ascontiguousarray(s)
+            arr = (A.IfxArray * 2)(*outs)
+            ext = (C.c_int32 * 4)(1, 1)
+            keep += [d, s, arr, ext]
+            calls.append(("sobel", lib.ifx_imgradients,
+                          (ctx.handle, arr, ai, A.dptr(d), A.dptr(s), 3, -1, ext, b, stream)))
+        elif r.op == "laplacian":
+            fl = (C.c_int32 * 4)(1, 1)
+            keep.append(fl)
+            calls.append(("laplacian", lib.ifx_imfilter_laplacian, (ctx.handle, outs[0], ai, fl, b, stream)))
+        else:
+            wf = (C.c_int64 * 4)(-(r.win // 2), -(r.win // 2))
+            wl = (C.c_int64 * 4)(r.win, r.win)
+            keep += [wf, wl]
+            calls.append(("median", lib.ifx_mapwindow_median, (ctx.handle, outs[0], ai, wf, wl, b, stream)))
+    return calls, keep, off
+
+
+def alg_bytes(r):
+    return r.in_bytes() + r.out_bytes()
+
+
+def run_stream(args, ifx, torch, rank):
+    from imagefiltering_gb300 import synthetic as S
+    n_req = args.per_step * (args.steps + args.warmup)
+    reqs = S.stream_requests(n_req, seed=5)
+    warm, timed = reqs[: args.per_step * args.warmup], reqs[args.per_step * args.warmup:]
+    dev = torch.device("cuda")
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5 + rank)
+
+    def make_inputs(rs):
+        ins = []
+        for r in rs:
+            if r.kind == "F32":
+                t = torch.rand((r.w, r.h), device=dev, dtype=torch.float32, generator=gen)
+            else:
+                t = torch.randint(0, 256, (r.w, r.h), device=dev, dtype=torch.uint8, generator=gen)
+            ins.append(t)      # (w, h) row-major == (h, w) column-major
+        return ins
+
+    def wave(rs):
+        return [rs[i:i + args.per_step] for i in range(0, len(rs), args.per_step)]
+
+    out_bytes = max(sum((r.out_bytes() + 255 * len(r.out_kinds())) for r in w) for w in wave(timed))
+    out_bytes = max(out_bytes, max(sum(r.out_bytes() + 255 * len(r.out_kinds()) for r in w)
+                                   for w in wave(warm)) if warm else 0)
+    out_arena = torch.empty(out_bytes + 4096, dtype=torch.uint8, device=dev)
+    A = ifx._abi
+
+    def run_waves(rs, record=None):
+        for w in wave(rs):
+            ins = make_inputs(w)
+            calls, keep, _ = stream_calls(ifx, w, ins, out_arena, torch)
+            torch.cuda.synchronize()
+            yield w, ins, calls, keep
+
+    # warm-up
+    for w, ins, calls, keep in run_waves(warm):
+        for op, fn, a in calls:
+            A.check(fn(*a))
+    torch.cuda.synchronize()
+    # prebuild timed waves (inputs resident before timing)
+    prepared = list(run_waves(timed))
+    ev = []
+    launches0 = ifx.launch_count()
+    if WORLD[1] > 1:
+        WORLD[2].barrier()
+    torch.cuda.synchronize()
+    with Clocks(torch.cuda.current_device()) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for w, ins, calls, keep in prepared:
+            for (op, fn, a), r in zip(calls, w):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                rc = fn(*a)
+                e1.record()
+                if rc:
+                    A.check(rc)
+                ev.append((op, r, e0, e1))
+        t1.record()
+        torch.cuda.synchronize()
+    dev_ms = t0.elapsed_time(t1)
+    launches = ifx.launch_count() - launches0
+    per_op = {}
+    for op, r, e0, e1 in ev:
+        d = per_op.setdefault(op, [0.0, 0, 0, 0])
+        d[0] += e0.elapsed_time(e1)
+        d[1] += alg_bytes(r)
+        d[2] += 1
+        d[3] += r.pixels
+    pixels = sum(r.pixels for r in timed)
+    return {"pixels": pixels, "dev_ms": dev_ms, "launches": launches, "per_op": per_op,
+            "clocks": clk.summary(), "reqs": timed}
+
+
+def run_stream_e2e(args, ifx, torch, reqs_all):
+    """Per-request calls with pinned host buffers (H2D + compute + D2H each)."""
+    from imagefiltering_gb300 import synthetic as S
+    reqs = reqs_all[: min(len(reqs_all), 200)]
+    A = ifx._abi
+    pins = []
+    h2d = d2h = 0
+    for r in reqs:
+        img = S.image_for(r)
+        t_in = torch.from_numpy(np.ascontiguousarray(img.T)).pin_memory()
+        outs = [torch.empty((r.w, r.h), dtype=torch.float64 if k == "F64" else torch.float32).pin_memory()
+                for k in r.out_kinds()]
+        pins.append((r, t_in, outs))
+        h2d += r.in_bytes()
+        d2h += r.out_bytes()
+    # one warm call per op
+    def call(r, t_in, outs):
+        ai = A.describe(t_in.data_ptr(), r.kind, (r.h, r.w))
+        descs = [A.describe(o.data_ptr(), k, (r.h, r.w)) for o, k in zip(outs, r.out_kinds())]
+        b = A.border_struct(r.style)
+        ctx = A.context()
+        lib = ctx.lib
+        if r.op == "gaussian":
+            g = np.ascontiguousarray(ifx.KernelFactors.gaussian(r.sigma).data, dtype=np.float64)
+            fac = (A.IfxFactor * 2)()
+            for i in range(2):
+                fac[i].axis, fac[i].length, fac[i].first, fac[i].weights = i, g.size, -(g.size // 2), A.dptr(g)
+            A.check(lib.ifx_imfilter_factored(ctx.handle, descs[0], ai, 2, fac, b, None))
+        elif r.op == "sobel":
+            import ctypes as C
+            d, s = ifx.KernelFactors.sobel.gradient_pair
+            d, s = np.ascontiguousarray(d), np.ascontiguousarray(s)
+            A.check(lib.ifx_imgradients(ctx.handle, (A.IfxArray * 2)(*descs), ai, A.dptr(d), A.dptr(s),
+                                        3, -1, (C.c_int32 * 4)(1, 1), b, None))
+        elif r.op == "laplacian":
+            import ctypes as C
+            A.check(lib.ifx_imfilter_laplacian(ctx.handle, descs[0], ai, (C.c_int32 * 4)(1, 1), b, None))
+        else:
+            import ctypes as C
+            A.check(lib.ifx_mapwindow_median(ctx.handle, descs[0], ai,
+                                             (C.c_int64 * 4)(-(r.win // 2), -(r.win // 2)),
+                                             (C.c_int64 * 4)(r.win, r.win), b, None))
+    for p in pins[:8]:
+        call(*p)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p in pins:
+        call(*p)
+    dt = time.perf_counter() - t0
+    px = sum(r.pixels for r in reqs)
+    return {"value": px / dt / 1e6, "unit": "Mpixel/s", "h2d_bytes_per_step": int(h2d * args.per_step / len(reqs)),
+            "d2h_bytes_per_step": int(d2h * args.per_step / len(reqs)), "requests": len(reqs),
+            "mode": "plain per-request C-ABI calls, pinned host buffers"}
+
+
+def cpu_stream_baseline(args, seconds, threads):
+    """The oracle port (restatement of the reference loops) on a bounded sample
+    of the stream, all host threads for the separable passes."""
+    from oracle import oracle as O
+    from imagefiltering_gb300 import synthetic as S
+    import __graft_entry__ as g
+    ifx = g.load_package()
+    O.set_threads(threads)
+    reqs = S.stream_requests(args.per_step * (args.steps + args.warmup), seed=5)
+    px = 0
+    n = 0
+    t0 = time.perf_counter()
+    for r in reqs:
+        if time.perf_counter() - t0 > seconds:
+            break
+        img = S.image_for(r)
+        vals = img.astype(np.float64) if r.kind == "F32" else img.astype(np.float64) / 255.0
+        if r.op == "gaussian":
+            k = np.asarray(ifx.KernelFactors.gaussian(r.sigma).data, np.float64)
+            O.imfilter_cascade(vals, [(0, -(k.size // 2), k), (1, -(k.size // 2), k)], r.style)
+        elif r.op == "sobel":
+            d, s = ifx.KernelFactors.sobel.gradient_pair
+            O.imfilter_cascade(vals, [(0, -1, d), (1, -1, s)], r.style)
+            O.imfilter_cascade(vals, [(0, -1, s), (1, -1, d)], r.style)
+        elif r.op == "laplacian":
+            O.laplacian(vals.astype(np.float32).astype(np.float64), [1, 1], r.style, arith="f32")
+        else:
+            O.mapwindow_median(vals, [-(r.win // 2)] * 2, [r.win] * 2, r.style)
+        px += r.pixels
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": px / dt / 1e6, "unit": "Mpixel/s", "cores": threads, "kind": "port",
+            "sample": "first %d requests of the stream (%.1f Mpixel), oracle port of the reference loops; "
+                      "separable passes threaded over %d threads, median/Laplacian single-threaded as in "
+                      "the reference" % (n, px / 1e6, threads)}
+
+
+# ----------------------------------------------------------------------------- main
+WORLD = (0, 1, None)
+
+
+def main():
+    global WORLD
+    args = parse()
+    rank, ws, dist = dist_init()
+    WORLD = (rank, ws, dist)
+    threads = os.cpu_count() or 1
+    hbm_peak, bf16_peak, peak_src = peaks()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = cpu_stream_baseline(args, max(2.0, args.cpu_seconds / 5), threads)
+            if i >= args.warmup:
+                vals.append(r["value"])
+        v = float(np.mean(vals))
+        line = {"impl": "reference", "metric": "Mpixel/s, mixed filter stream (served)",
+                "value": v, "unit": "Mpixel/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "mixed stream, seed 5 (bounded CPU sample per step)"},
+                "cpu_baseline": {"value": v, "unit": "Mpixel/s", "cores": threads, "kind": "port",
+                                 "sample": r["sample"]},
+                "e2e": {"value": v, "unit": "Mpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    ifx = g.load_package()
+    ifx._abi.context()
+    res = run_stream(args, ifx, torch, rank)
+    dev_ms = res["dev_ms"]
+    if ws > 1:
+        t = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    pixels_all = res["pixels"] * ws
+    value = pixels_all / (dev_ms / 1e3) / 1e6
+    per_op = res["per_op"]
+    dom = max(per_op.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_bytes, dom_n, dom_px) = dom
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    e2e = run_stream_e2e(args, ifx, torch, res["reqs"])
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_stream_baseline(args, args.cpu_seconds, threads)
+    if rank != 0:
+        return 0
+    line = {
+        "metric": "Mpixel/s at <=1e-5 rel err, mixed filter stream (plain per-call GPU)",
+        "value": value, "unit": "Mpixel/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "mixed 2-D filter stream (seed 5): sides log-U[64,4096], aspect 1:4-4:1, "
+                               "F32/N0f8, Gaussian/Sobel/Laplacian/median3-5, Pad styles",
+                   "requests_per_step": args.per_step, "mode": "plain: one C-ABI call per request, "
+                   "device-resident inputs", "l2": "inputs larger than L2 (each step ~%.1f GB)" %
+                   (sum(alg_bytes(r) for r in res["reqs"]) / args.steps / 1e9),
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "e2e": e2e,
+        "gpu_launches": res["launches"],
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_src,
+                     "traffic": None, "calls": dom_n,
+                     "alg_bytes_per_call": dom_bytes / dom_n},
+        "per_op_ms": {k: round(v[0], 3) for k, v in per_op.items()},
+        "clocks": res["clocks"],
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -158,13 +158,14 @@ cudaError_t launch_pass_box(const PassBoxArgs &a, cudaStream_t s)
 
 // =========================================================================
 // Register-blocked 1-D correlation on shared memory:
-//   acc[i] = sum_{t < k4} w[t] * p[(i+t)*step],  i < NB
-// k4 is the tap count rounded up to 4 (padded weights are zero); the window of
-// NB+4 values slides through registers so each loaded value feeds up to NB
-// multiply-adds.
+//   acc[i] = sum_{t < k} w[t] * p[(i+t)*step],  i < NB
+// The window of NB(+4) values slides through registers so each loaded value
+// feeds up to NB multiply-adds.  Taps go four at a time and the last k mod 4
+// one at a time, so no padded weight ever multiplies data (0*Inf would be NaN).
+// Reads p[0 .. NB+k-2] only.
 // =========================================================================
 template <class Tc, int NB>
-__device__ __forceinline__ void corr_run(const Tc *p, int step, const Tc *w, int k4, Tc *acc)
+__device__ __forceinline__ void corr_run(const Tc *p, int step, const Tc *w, int k, Tc *acc)
 {
     Tc v[NB + 4];
 #pragma unroll
@@ -172,7 +173,8 @@ __device__ __forceinline__ void corr_run(const Tc *p, int step, const Tc *w, int
         v[i] = p[i * step];
         acc[i] = 0;
     }
-    for (int t0 = 0; t0 < k4; t0 += 4) {
+    int t0 = 0;
+    for (; t0 + 4 <= k; t0 += 4) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) v[NB + j] = p[(NB + t0 + j) * step];
 #pragma unroll
@@ -183,6 +185,16 @@ __device__ __forceinline__ void corr_run(const Tc *p, int step, const Tc *w, int
         }
 #pragma unroll
         for (int i = 0; i < NB; ++i) v[i] = v[i + 4];
+    }
+    for (; t0 < k; ++t0) {
+        const Tc wt = w[t0];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) acc[i] = fma(wt, v[i], acc[i]);
+        if (t0 + 1 < k) {
+#pragma unroll
+            for (int i = 0; i < NB - 1; ++i) v[i] = v[i + 1];
+            v[NB - 1] = p[(NB + t0) * step];
+        }
     }
 }
 
@@ -262,7 +274,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         for (int it = tid; it < (TY + ky4) * segs; it += nth) {
             const int r = it / segs, c0 = (it - r * segs) * NB;
             if (r < RT) {
-                corr_run<Tc, NB>(T + (size_t)r * CT + c0, 1, wx, kx4, acc);
+                corr_run<Tc, NB>(T + (size_t)r * CT + c0, 1, wx, kx, acc);
 #pragma unroll
                 for (int i = 0; i < NB; ++i) I[(size_t)r * TX + c0 + i] = acc[i];
             } else {
@@ -275,7 +287,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         const int rsegs = TY / NB;
         for (int it = tid; it < TX * rsegs; it += nth) {
             const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
-            corr_run<Tc, NB>(I + (size_t)r0 * TX + c, TX, wy, ky4, acc);
+            corr_run<Tc, NB>(I + (size_t)r0 * TX + c, TX, wy, ky, acc);
             const int x = tx0 + c;
             if (x < nx) {
 #pragma unroll
@@ -292,7 +304,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         for (int it = tid; it < CI * rsegs; it += nth) {
             const int rs = it / CI, c = it - rs * CI, r0 = rs * NB;
             if (c < CT) {
-                corr_run<Tc, NB>(T + (size_t)r0 * CT + c, CT, wy, ky4, acc);
+                corr_run<Tc, NB>(T + (size_t)r0 * CT + c, CT, wy, ky, acc);
 #pragma unroll
                 for (int i = 0; i < NB; ++i) I[(size_t)(r0 + i) * CI + c] = acc[i];
             } else {
@@ -305,7 +317,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         const int segs = TX / NB;
         for (int it = tid; it < TY * segs; it += nth) {
             const int r = it / segs, c0 = (it - r * segs) * NB;
-            corr_run<Tc, NB>(I + (size_t)r * CI + c0, 1, wx, kx4, acc);
+            corr_run<Tc, NB>(I + (size_t)r * CI + c0, 1, wx, kx, acc);
             const int y = ty0 + r;
             if (y < ny) {
 #pragma unroll
@@ -412,7 +424,7 @@ k_dense2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
 #pragma unroll
         for (int i = 0; i < NB; ++i) acc[i] = 0;
         for (int j = 0; j < kh; ++j) {
-            corr_run<Tc, NB>(T + (size_t)(r + j) * CT + c0, 1, Ks + (size_t)j * kw4, kw4, part);
+            corr_run<Tc, NB>(T + (size_t)(r + j) * CT + c0, 1, Ks + (size_t)j * kw4, kw, part);
 #pragma unroll
             for (int i = 0; i < NB; ++i) acc[i] += part[i];
         }

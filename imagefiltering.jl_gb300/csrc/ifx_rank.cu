@@ -20,6 +20,7 @@
 // literally.
 #include "ifx_internal.h"
 #include <cstring>
+#include <utility>
 
 namespace ifx {
 
@@ -220,6 +221,128 @@ k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, in
     }
 }
 
+// =========================================================================
+// Float median, 2-D, fixed window: a sorting network on order-preserving
+// integer keys.  The network is Batcher's odd-even merge sort for arbitrary n
+// (the iterative formulation: for p = 1,2,4..; k = p,p/2..1; j = k mod p,
+// step 2k; i < min(k, n-j-k); compare (i+j, i+j+k) when both lie in the same
+// 2p block), built at compile time; only the comparators the middle output
+// depends on survive dead-code elimination.  Keys map floats so that unsigned
+// order is Julia's isless order (-0.0 < 0.0, NaN after +Inf), which is what
+// partialsort! uses (src/mapwindow.jl:123-128).
+// =========================================================================
+template <int N> struct Net {
+    int n = 0;
+    short a[640] = {};
+    short b[640] = {};
+};
+
+template <int N> constexpr Net<N> make_net()
+{
+    Net<N> r{};
+    for (int p = 1; p < N; p <<= 1)
+        for (int k = p; k >= 1; k >>= 1)
+            for (int j = k % p; j + k < N; j += 2 * k)
+                for (int i = 0; i < k && i < N - j - k; ++i)
+                    if ((i + j) / (2 * p) == (i + j + k) / (2 * p)) {
+                        r.a[r.n] = (short)(i + j);
+                        r.b[r.n] = (short)(i + j + k);
+                        ++r.n;
+                    }
+    return r;
+}
+
+template <int N> struct NetOf { static constexpr Net<N> net = make_net<N>(); };
+
+template <class T> struct SortKey;
+template <> struct SortKey<float> {
+    using K = uint32_t;
+    static __device__ __forceinline__ K key(float x)
+    {
+        uint32_t b = isnan(x) ? 0x7fffffffu : __float_as_uint(x);
+        return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    }
+    static __device__ __forceinline__ float val(K k)
+    {
+        return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+    }
+};
+template <> struct SortKey<double> {
+    using K = unsigned long long;
+    static __device__ __forceinline__ K key(double x)
+    {
+        unsigned long long b = isnan(x) ? 0x7fffffffffffffffull : (unsigned long long)__double_as_longlong(x);
+        return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+    }
+    static __device__ __forceinline__ double val(K k)
+    {
+        return __longlong_as_double((long long)((k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k));
+    }
+};
+
+template <int N, int I, class K> __device__ __forceinline__ void net_cx(K (&v)[N])
+{
+    constexpr int x = NetOf<N>::net.a[I];
+    constexpr int y = NetOf<N>::net.b[I];
+    const K lo = v[x] < v[y] ? v[x] : v[y];
+    const K hi = v[x] < v[y] ? v[y] : v[x];
+    v[x] = lo;
+    v[y] = hi;
+}
+
+template <int N, class K, size_t... I>
+__device__ __forceinline__ void net_apply(K (&v)[N], std::index_sequence<I...>)
+{
+    (net_cx<N, (int)I, K>(v), ...);
+}
+
+template <int N, class K> __device__ __forceinline__ void net_sort(K (&v)[N])
+{
+    net_apply<N, K>(v, std::make_index_sequence<NetOf<N>::net.n>{});
+}
+
+constexpr int kFmTX = 32, kFmTY = 8;
+
+template <class T, int W0, int W1>
+__global__ void __launch_bounds__(256)
+k_median_float(const T *__restrict__ img, void *out, int out_type, int nx, int ny, int f0, int f1,
+               int style, T fill)
+{
+    using SK = SortKey<T>;
+    using K = typename SK::K;
+    constexpr int CT = kFmTX + W0 - 1, RT = kFmTY + W1 - 1, N = W0 * W1;
+    __shared__ T tile[RT * CT];
+    const int tx0 = blockIdx.x * kFmTX, ty0 = blockIdx.y * kFmTY;
+    for (int idx = threadIdx.x; idx < RT * CT; idx += blockDim.x) {
+        const int r = idx / CT, c = idx - r * CT;
+        const int mx = map_index(tx0 + f0 + c, nx, style);
+        const int my = map_index(ty0 + f1 + r, ny, style);
+        tile[idx] = (mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx];
+    }
+    __syncthreads();
+    const int lx = threadIdx.x % kFmTX, ly = threadIdx.x / kFmTX;
+    K v[N];
+#pragma unroll
+    for (int j = 0; j < W1; ++j)
+#pragma unroll
+        for (int i = 0; i < W0; ++i) v[j * W0 + i] = SK::key(tile[(ly + j) * CT + lx + i]);
+    net_sort<N, K>(v);
+    const int x = tx0 + lx, y = ty0 + ly;
+    if (x < nx && y < ny) store_sel<T>(out, out_type, (long long)y * nx + x, SK::val(v[(N - 1) / 2]), false);
+}
+
+template <class T, int W0, int W1>
+static cudaError_t median_float_t(const MedianArgs &a, cudaStream_t s)
+{
+    const int nx = a.n[0], ny = a.nd > 1 ? a.n[1] : 1;
+    dim3 grid((nx + kFmTX - 1) / kFmTX, (ny + kFmTY - 1) / kFmTY);
+    k_median_float<T, W0, W1><<<grid, kFmTX * kFmTY, 0, s>>>(
+        (const T *)a.img, a.out, a.out_type, nx, ny, a.wfirst[0], a.nd > 1 ? a.wfirst[1] : 0,
+        a.style, (T)a.fill);
+    note_launch();
+    return cudaGetLastError();
+}
+
 template <class T>
 static cudaError_t median_px_t(const MedianArgs &a, cudaStream_t s)
 {
@@ -269,6 +392,14 @@ cudaError_t launch_median(const MedianArgs &a, cudaStream_t s)
         return median_u8_t<0, 0>(a, s);
     }
     if (u8) return median_px_t<uint8_t>(a, s);
+    const bool fast2d = a.nd <= 2 && a.style != IFX_CIRCULAR;
+    if (fast2d && (a.in_type == IFX_F32 || a.in_type == IFX_F64)) {
+        const int w0 = a.wlen[0], w1 = a.nd > 1 ? a.wlen[1] : 1;
+        const bool f32 = a.in_type == IFX_F32;
+        if (w0 == 3 && w1 == 3) return f32 ? median_float_t<float, 3, 3>(a, s) : median_float_t<double, 3, 3>(a, s);
+        if (w0 == 5 && w1 == 5) return f32 ? median_float_t<float, 5, 5>(a, s) : median_float_t<double, 5, 5>(a, s);
+        if (w0 == 7 && w1 == 7) return f32 ? median_float_t<float, 7, 7>(a, s) : median_float_t<double, 7, 7>(a, s);
+    }
     if (a.in_type == IFX_F32) return median_px_t<float>(a, s);
     if (a.in_type == IFX_F64) return median_px_t<double>(a, s);
     return cudaErrorInvalidValue;

@@ -190,3 +190,46 @@ def test_no_cpu_algorithms(ifx):
         ifx.imfilter(img, ifx.KernelFactors.gaussian((1, 1)), "replicate", ifx.Algorithm.FIR())
     with pytest.raises(ifx.Unsupported):
         ifx.mapwindow(lambda v: v.sum(), img, (3, 3))
+
+
+def batcher_network(n):
+    """The comparator list the float-median kernel builds at compile time
+    (csrc/ifx_rank.cu make_net): Batcher's odd-even merge sort for any n."""
+    ops = []
+    p = 1
+    while p < n:
+        k = p
+        while k >= 1:
+            j = k % p
+            while j + k < n:
+                for i in range(min(k, n - j - k)):
+                    if (i + j) // (2 * p) == (i + j + k) // (2 * p):
+                        ops.append((i + j, i + j + k))
+                j += 2 * k
+            k //= 2
+        p *= 2
+    return ops
+
+
+@pytest.mark.parametrize("n", [9, 15, 25])
+def test_median_network_sorts_all_01_inputs(n):
+    """0-1 principle: a comparator network sorts every input iff it sorts
+    every 0-1 input; checked exhaustively with bit-parallel wires."""
+    m = 1 << n
+    idx = np.arange(m, dtype=np.uint64)
+    wires = [((idx >> np.uint64(b)) & np.uint64(1)).astype(bool) for b in range(n)]
+    for a, b in batcher_network(n):
+        wires[a], wires[b] = wires[a] & wires[b], wires[a] | wires[b]
+    for i in range(n - 1):
+        assert not np.any(wires[i] & ~wires[i + 1])
+
+
+def test_median_network_49_random():
+    rng = np.random.default_rng(0)
+    ops = batcher_network(49)
+    for _ in range(2000):
+        v = list(rng.integers(0, 5, 49))
+        for a, b in ops:
+            if v[a] > v[b]:
+                v[a], v[b] = v[b], v[a]
+        assert v == sorted(v)
