@@ -64,10 +64,18 @@ class IfxFactor(C.Structure):
                 ("weights", C.POINTER(C.c_double))]
 
 
+class IfxRequest(C.Structure):
+    _fields_ = [("op", C.c_int32), ("window", C.c_int32), ("img", IfxArray), ("out", IfxArray * 2),
+                ("border", IfxBorder), ("taps", C.c_int32 * 2), ("first", C.c_int64 * 2),
+                ("weights", C.POINTER(C.c_double) * 2)]
+
+
+OP_FACTORED2D, OP_GRADIENTS2D, OP_LAPLACIAN2D, OP_MEDIAN2D = 1, 2, 3, 4
+
 SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "ifx_launch_count",
            "ifx_synchronize", "ifx_padarray", "ifx_imfilter_factored", "ifx_imfilter_dense",
            "ifx_imfilter_laplacian", "ifx_imgradients", "ifx_mapwindow_median",
-           "ifx_mapwindow_extrema"]
+           "ifx_mapwindow_extrema", "ifx_batch_run"]
 
 _lib = None
 _lock = threading.Lock()
@@ -105,6 +113,7 @@ def load(path: str = LIB_PATH):
                                              P(C.c_int64), P(IfxBorder), vp]
         lib.ifx_mapwindow_extrema.argtypes = [vp, P(IfxArray), P(IfxArray), P(C.c_int64),
                                               P(C.c_int64), P(IfxBorder), C.c_int32, vp]
+        lib.ifx_batch_run.argtypes = [vp, P(IfxRequest), C.c_int32, P(C.c_int64), vp]
         for name in SYMBOLS:
             getattr(lib, name)          # every declared entry point must be exported
         _lib = lib

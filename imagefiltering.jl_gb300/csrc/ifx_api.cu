@@ -639,6 +639,8 @@ int ifx_imfilter_laplacian(ifx_context_t *ctx, ifx_array_t *out, const ifx_array
     if ((rc = check_reflect(border, *img))) return rc;
     double fill;
     if ((rc = image_fill(border, it, ot, &fill))) return rc;
+    if (it == IFX_N0F8 && ot == IFX_F32)        // Float32(N0f8): code/255 rounded once in FP32
+        fill = (double)((float)std::nearbyint(fill * 255.0) / 255.0f);
     if (ot == IFX_I16 && fill != std::nearbyint(fill))
         return fail(IFX_ERR_ARGUMENT, "Cannot convert elements of border=Fill(%g)", fill);
     if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
@@ -878,6 +880,90 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
         IFX_CUDA(launch_extrema_pass(a, c.s));
     }
     return c.finish();
+}
+
+int ifx_batch_run(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n, int64_t *tiles,
+                  void *stream)
+{
+    if (n < 0 || (n > 0 && !reqs)) return fail(IFX_ERR_ARGUMENT, "bad request list");
+    if (tiles) *tiles = 0;
+    std::vector<BatchItem> items((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const ifx_request_t &q = reqs[i];
+        BatchItem &it = items[i];
+        int rc;
+        if ((rc = check_array(&q.img, "img")) || (rc = check_border(&q.border))) return rc;
+        if (q.img.ndim != 2) return fail(IFX_ERR_UNSUPPORTED, "request %d: batched requests are 2-D", i);
+        const int et = q.img.eltype;
+        if (et != IFX_F32 && !is8(et))
+            return fail(IFX_ERR_UNSUPPORTED, "request %d: batched images are Float32, N0f8 or UInt8", i);
+        const int nout = q.op == IFX_OP_GRADIENTS2D ? 2 : 1;
+        if (q.op < IFX_OP_FACTORED2D || q.op > IFX_OP_MEDIAN2D)
+            return fail(IFX_ERR_ARGUMENT, "request %d: unknown op %d", i, q.op);
+        for (int o = 0; o < nout; ++o) {
+            if ((rc = check_array(&q.out[o], "out")) || (rc = check_same_axes(q.out[o], q.img))) return rc;
+            const int ot = q.out[o].eltype;
+            if (ot != IFX_F32 && ot != IFX_F64)
+                return fail(IFX_ERR_UNSUPPORTED, "request %d: outputs are Float32 or Float64", i);
+            if (!is_device_ptr(q.out[o].data))
+                return fail(IFX_ERR_ARGUMENT, "request %d: batched outputs must be device memory", i);
+        }
+        if (q.out[0].eltype != (nout == 2 ? q.out[1].eltype : q.out[0].eltype))
+            return fail(IFX_ERR_UNSUPPORTED, "request %d: both gradients need one eltype", i);
+        if (!is_device_ptr(q.img.data))
+            return fail(IFX_ERR_ARGUMENT, "request %d: batched images must be device memory", i);
+        if (q.border.explicit_pad)
+            return fail(IFX_ERR_UNSUPPORTED, "request %d: explicit padding sizes in a batch", i);
+        if ((rc = check_reflect(&q.border, q.img))) return rc;
+        memset(&it, 0, sizeof it);
+        it.op = q.op;
+        it.in_type = et;
+        it.out_type = q.out[0].eltype;
+        it.style = q.border.style;
+        it.nx = (int)q.img.size[0];
+        it.ny = (int)q.img.size[1];
+        it.in = q.img.data;
+        it.out0 = q.out[0].data;
+        it.out1 = nout == 2 ? q.out[1].data : nullptr;
+        double code = 0.0;
+        if ((rc = fill_for(&q.border, et, &code))) return rc;
+        it.fill_code = is8(et) ? (int)code : 0;
+        it.fill = et == IFX_N0F8 ? (double)((float)code / 255.0f) : code;
+        if (et == IFX_F32) it.fill = (double)(float)code;
+        if (q.op == IFX_OP_FACTORED2D) {
+            for (int a = 0; a < 2; ++a)
+                if (q.taps[a] < 1 || q.taps[a] > 33 || !q.weights[a] || q.first[a] < -4096 || q.first[a] > 4096)
+                    return fail(IFX_ERR_UNSUPPORTED, "request %d: batched factors have 1..33 taps", i);
+            it.kx = q.taps[0];
+            it.ky = q.taps[1];
+            it.fx = (int)q.first[0];
+            it.fy = (int)q.first[1];
+            it.wx = q.weights[0];
+            it.wy = q.weights[1];
+        } else if (q.op == IFX_OP_GRADIENTS2D) {
+            if (q.taps[0] != 3 || q.taps[1] != 3 || q.first[0] != -1 || q.first[1] != -1 ||
+                !q.weights[0] || !q.weights[1])
+                return fail(IFX_ERR_UNSUPPORTED, "request %d: batched gradients use 3-tap centred pairs", i);
+            it.kx = it.ky = 3;
+            it.fx = it.fy = -1;
+            it.wx = q.weights[0];
+            it.wy = q.weights[1];
+        } else if (q.op == IFX_OP_LAPLACIAN2D) {
+            if (it.out_type != IFX_F32 || is8(et) && et != IFX_N0F8)
+                return fail(IFX_ERR_UNSUPPORTED, "request %d: batched Laplacian writes Float32", i);
+        } else {
+            if (q.window != 3 && q.window != 5)
+                return fail(IFX_ERR_UNSUPPORTED, "request %d: batched median windows are 3 or 5", i);
+            it.window = q.window;
+        }
+    }
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    IFX_CUDA(cudaSetDevice(ctx->device));
+    long long t = 0;
+    IFX_CUDA(launch_batch(ctx->device, items.data(), n, stream ? (cudaStream_t)stream : ctx->stream, &t));
+    if (tiles) *tiles = t;
+    return IFX_OK;
 }
 
 } // extern "C"

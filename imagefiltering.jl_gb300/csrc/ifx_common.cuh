@@ -68,6 +68,8 @@ template <class Tc> __device__ __forceinline__ Tc to_c(uint8_t v, bool norm)
 template <class To> __device__ __forceinline__ To from_c(float v) { return (To)v; }
 template <class To> __device__ __forceinline__ To from_c(double v) { return (To)v; }
 
+__host__ __device__ __forceinline__ int up4(int k) { return (k + 3) & ~3; }
+
 // Dense N-d box of an index space (lo .. lo+size-1 per axis), column-major.
 struct Box {
     int nd;
@@ -90,6 +92,71 @@ inline Box make_box(int nd, const int *lo, const int *size)
     }
     b.count = s;
     return b;
+}
+
+// =========================================================================
+// Register-blocked 1-D correlation on shared memory:
+//   acc[i] = sum_{t < k} w[t] * p[(i+t)*step],  i < NB
+// The window of NB(+4) values slides through registers so each loaded value
+// feeds up to NB multiply-adds.  Taps go four at a time and the last k mod 4
+// one at a time, so no padded weight ever multiplies data (0*Inf would be NaN).
+// Reads p[0 .. NB+k-2] only.
+// =========================================================================
+template <class Tc, int NB>
+__device__ __forceinline__ void corr_run(const Tc *p, int step, const Tc *w, int k, Tc *acc)
+{
+    Tc v[NB + 4];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        v[i] = p[i * step];
+        acc[i] = 0;
+    }
+    int t0 = 0;
+    for (; t0 + 4 <= k; t0 += 4) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[NB + j] = p[(NB + t0 + j) * step];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const Tc wt = w[t0 + j];
+#pragma unroll
+            for (int i = 0; i < NB; ++i) acc[i] = fma(wt, v[i + j], acc[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < NB; ++i) v[i] = v[i + 4];
+    }
+    for (; t0 < k; ++t0) {
+        const Tc wt = w[t0];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) acc[i] = fma(wt, v[i], acc[i]);
+        if (t0 + 1 < k) {
+#pragma unroll
+            for (int i = 0; i < NB - 1; ++i) v[i] = v[i + 1];
+            v[NB - 1] = p[(NB + t0) * step];
+        }
+    }
+}
+
+// Tile gather with U independent loads in flight per thread: load(idx)
+// returns element idx of the tile (row-major in shared memory).  All U
+// loads of a round are issued before any shared-memory store, so a CTA keeps
+// U*blockDim.x global loads outstanding instead of one per thread.
+template <int U, class T, class F>
+__device__ __forceinline__ void gather_tile(T *dst, int total, F load)
+{
+    const int nth = blockDim.x;
+    for (int base = threadIdx.x; base < total; base += nth * U) {
+        T v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int idx = base + u * nth;
+            v[u] = idx < total ? load(idx) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int idx = base + u * nth;
+            if (idx < total) dst[idx] = v[u];
+        }
+    }
 }
 
 } // namespace ifx

@@ -157,48 +157,6 @@ cudaError_t launch_pass_box(const PassBoxArgs &a, cudaStream_t s)
 }
 
 // =========================================================================
-// Register-blocked 1-D correlation on shared memory:
-//   acc[i] = sum_{t < k} w[t] * p[(i+t)*step],  i < NB
-// The window of NB(+4) values slides through registers so each loaded value
-// feeds up to NB multiply-adds.  Taps go four at a time and the last k mod 4
-// one at a time, so no padded weight ever multiplies data (0*Inf would be NaN).
-// Reads p[0 .. NB+k-2] only.
-// =========================================================================
-template <class Tc, int NB>
-__device__ __forceinline__ void corr_run(const Tc *p, int step, const Tc *w, int k, Tc *acc)
-{
-    Tc v[NB + 4];
-#pragma unroll
-    for (int i = 0; i < NB; ++i) {
-        v[i] = p[i * step];
-        acc[i] = 0;
-    }
-    int t0 = 0;
-    for (; t0 + 4 <= k; t0 += 4) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) v[NB + j] = p[(NB + t0 + j) * step];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const Tc wt = w[t0 + j];
-#pragma unroll
-            for (int i = 0; i < NB; ++i) acc[i] = fma(wt, v[i + j], acc[i]);
-        }
-#pragma unroll
-        for (int i = 0; i < NB; ++i) v[i] = v[i + 4];
-    }
-    for (; t0 < k; ++t0) {
-        const Tc wt = w[t0];
-#pragma unroll
-        for (int i = 0; i < NB; ++i) acc[i] = fma(wt, v[i], acc[i]);
-        if (t0 + 1 < k) {
-#pragma unroll
-            for (int i = 0; i < NB - 1; ++i) v[i] = v[i + 1];
-            v[NB - 1] = p[(NB + t0) * step];
-        }
-    }
-}
-
-// =========================================================================
 // Fused 2-D separable kernel.  One CTA computes a TX x TY output tile:
 //  1. gather the (TX+kx-1) x (TY+ky-1) input tile through the border map,
 //     converting to the compute type (FP32, or FP64 for Float64 images);
@@ -213,7 +171,6 @@ constexpr int kSepNB = 8;
 
 template <class Tc> struct Sep2dW { Tc wx[IFX_MAX_TAPS + 3]; Tc wy[IFX_MAX_TAPS + 3]; };
 
-__host__ __device__ __forceinline__ int up4(int k) { return (k + 3) & ~3; }
 
 template <class Tc>
 static size_t sep2d_smem(int kx, int ky, int x_first)
@@ -255,16 +212,13 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
     Tc *I = T + (size_t)RT * CT;
 
     // 1. gather through the border map
-    for (int idx = tid; idx < RT * CT; idx += nth) {
+    gather_tile<8>(T, RT * CT, [&](int idx) -> Tc {
         const int r = idx / CT, c = idx - r * CT;
-        Tc v = 0;
-        if (r < RV && c < CV) {
-            const int mx = map_index(tx0 + fx + c, nx, style);
-            const int my = map_index(ty0 + fy + r, ny, style);
-            v = (mx < 0 || my < 0) ? fill : cvt<Tc, Tin>(img[(long long)my * nx + mx], norm);
-        }
-        T[idx] = v;
-    }
+        if (r >= RV || c >= CV) return Tc(0);
+        const int mx = map_index(tx0 + fx + c, nx, style);
+        const int my = map_index(ty0 + fy + r, ny, style);
+        return (mx < 0 || my < 0) ? fill : cvt<Tc, Tin>(img[(long long)my * nx + mx], norm);
+    });
     __syncthreads();
 
     Tc acc[NB];
@@ -406,16 +360,13 @@ k_dense2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         Ks[t] = i < kw ? W.w[j * kw + i] : (Tc)0;
     }
     const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
-    for (int idx = tid; idx < RT * CT; idx += nth) {
+    gather_tile<8>(T, RT * CT, [&](int idx) -> Tc {
         const int r = idx / CT, c = idx - r * CT;
-        Tc v = 0;
-        if (c < CV) {
-            const int mx = map_index(tx0 + fx + c, nx, style);
-            const int my = map_index(ty0 + fy + r, ny, style);
-            v = (mx < 0 || my < 0) ? fill : cvt<Tc, Tin>(img[(long long)my * nx + mx], norm);
-        }
-        T[idx] = v;
-    }
+        if (c >= CV) return Tc(0);
+        const int mx = map_index(tx0 + fx + c, nx, style);
+        const int my = map_index(ty0 + fy + r, ny, style);
+        return (mx < 0 || my < 0) ? fill : cvt<Tc, Tin>(img[(long long)my * nx + mx], norm);
+    });
     __syncthreads();
     const int segs = TX / NB;
     for (int it = tid; it < TY * segs; it += nth) {
@@ -593,9 +544,57 @@ __global__ void k_laplacian(const Tin *__restrict__ img, TT *__restrict__ out, i
         out[p] = (TT)tmp;
     }
 }
+// 2-D tile version: the halo-1 tile is gathered once (border map applied),
+// each output reads its 4 neighbours from shared memory; same operation order.
+constexpr int kLapTX = 64, kLapTY = 32;
+
+template <class Tin, class TT>
+__global__ void __launch_bounds__(256)
+k_lap2d(const Tin *__restrict__ img, TT *__restrict__ out, int nx, int ny, int fxl, int fyl,
+        int style, typename LapAcc<TT>::type fill, bool norm)
+{
+    using A = typename LapAcc<TT>::type;
+    constexpr int CT = kLapTX + 2, RT = kLapTY + 2;
+    __shared__ A T[RT * CT];
+    const int tx0 = blockIdx.x * kLapTX, ty0 = blockIdx.y * kLapTY;
+    gather_tile<8>(T, RT * CT, [&](int idx) -> A {
+        const int r = idx / CT, c = idx - r * CT;
+        const int mx = map_index(tx0 - 1 + c, nx, style);
+        const int my = map_index(ty0 - 1 + r, ny, style);
+        return (mx < 0 || my < 0) ? fill : cvt<A, Tin>(img[(long long)my * nx + mx], norm);
+    });
+    __syncthreads();
+    const A n2 = (A)(-2 * (fxl + fyl));
+    for (int it = threadIdx.x; it < kLapTX * kLapTY; it += blockDim.x) {
+        const int r = it / kLapTX, c = it - r * kLapTX;
+        const int x = tx0 + c, y = ty0 + r;
+        if (x >= nx || y >= ny) continue;
+        const A *p = T + (r + 1) * CT + (c + 1);
+        A tmp = lap_mul<A>(n2, p[0]);
+        if (fxl) {
+            tmp = lap_add<A>(tmp, p[1]);
+            tmp = lap_add<A>(tmp, p[-1]);
+        }
+        if (fyl) {
+            tmp = lap_add<A>(tmp, p[CT]);
+            tmp = lap_add<A>(tmp, p[-CT]);
+        }
+        out[(long long)y * nx + x] = (TT)tmp;
+    }
+}
+
 template <class Tin, class TT>
 static cudaError_t laplacian_t(const LaplacianArgs &a, cudaStream_t s)
 {
+    if (a.nd <= 2) {
+        const int nx = a.n[0], ny = a.nd > 1 ? a.n[1] : 1;
+        dim3 grid((nx + kLapTX - 1) / kLapTX, (ny + kLapTY - 1) / kLapTY);
+        k_lap2d<Tin, TT><<<grid, 256, 0, s>>>((const Tin *)a.img, (TT *)a.out, nx, ny, a.flags[0],
+                                              a.nd > 1 ? a.flags[1] : 0, a.style,
+                                              (typename LapAcc<TT>::type)a.fill, a.in_type == IFX_N0F8);
+        note_launch();
+        return cudaGetLastError();
+    }
     int4 n = make_int4(a.n[0], a.nd > 1 ? a.n[1] : 1, a.nd > 2 ? a.n[2] : 1, a.nd > 3 ? a.n[3] : 1);
     int4 f = make_int4(a.flags[0], a.nd > 1 ? a.flags[1] : 0, a.nd > 2 ? a.flags[2] : 0,
                        a.nd > 3 ? a.flags[3] : 0);

@@ -97,4 +97,18 @@ struct ExtremaPassArgs {                   // one separable min/max pass along `
 };
 cudaError_t launch_extrema_pass(const ExtremaPassArgs &a, cudaStream_t s);
 
+// Batched engine -------------------------------------------------------------
+struct BatchItem {                         // one validated 2-D request, device pointers
+    int op, in_type, out_type, style;      // op: 1 factored, 2 gradients, 3 laplacian, 4 median
+    int nx, ny, window;
+    const void *in;
+    void *out0, *out1;
+    double fill;                           // value domain
+    int fill_code;                         // 8-bit images
+    int kx, ky, fx, fy;                    // factored: x/y factors; gradients: deriv/smooth (3, -1)
+    const double *wx, *wy;
+};
+cudaError_t launch_batch(int device, const BatchItem *items, int n, cudaStream_t s, long long *tiles);
+int batch_grid(int device);
+
 } // namespace ifx

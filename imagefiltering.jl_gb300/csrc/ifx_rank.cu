@@ -19,6 +19,7 @@
 // N-d images use the per-pixel kernel, which applies the window-relative map
 // literally.
 #include "ifx_internal.h"
+#include "ifx_select.cuh"
 #include <cstring>
 #include <utility>
 
@@ -144,19 +145,6 @@ __global__ void k_median_px(const T *__restrict__ img, void *out, int out_type, 
 // =========================================================================
 constexpr int kMedTX = 128, kMedTY = 8;
 
-__device__ __forceinline__ uint32_t load_word(const uint8_t *row, int col)
-{
-    const int a = col & ~3, sh = col & 3;
-    const uint32_t lo = *reinterpret_cast<const uint32_t *>(row + a);
-    const uint32_t hi = *reinterpret_cast<const uint32_t *>(row + a + 4);
-    return __byte_perm(lo, hi, 0x3210 + 0x1111 * sh);
-}
-
-__device__ __forceinline__ uint32_t count_lt(uint32_t cnt, uint32_t w, uint32_t trial)
-{
-    return __vsub4(cnt, __vcmpltu4(w, trial));
-}
-
 template <int W0, int W1>
 __global__ void __launch_bounds__(256)
 k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, int ny, int f0,
@@ -167,16 +155,13 @@ k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, in
     const int CT = ((kMedTX + w0 - 1 + 3) & ~3) + 4;
     const int RT = kMedTY + w1 - 1;
     const int tx0 = blockIdx.x * kMedTX, ty0 = blockIdx.y * kMedTY;
-    for (int idx = threadIdx.x; idx < RT * CT; idx += blockDim.x) {
+    gather_tile<8>(tile, RT * CT, [&](int idx) -> uint8_t {
         const int r = idx / CT, c = idx - r * CT;
-        uint8_t v = 0;
-        if (c < kMedTX + w0 - 1) {
-            const int mx = map_index(tx0 + f0 + c, nx, style);
-            const int my = map_index(ty0 + f1 + r, ny, style);
-            v = (mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx];
-        }
-        tile[idx] = v;
-    }
+        if (c >= kMedTX + w0 - 1) return 0;
+        const int mx = map_index(tx0 + f0 + c, nx, style);
+        const int my = map_index(ty0 + f1 + r, ny, style);
+        return (mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx];
+    });
     __syncthreads();
     const int lx = (threadIdx.x & 31) * 4, ly = threadIdx.x >> 5;
     const int m = w0 * w1;
@@ -221,86 +206,6 @@ k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, in
     }
 }
 
-// =========================================================================
-// Float median, 2-D, fixed window: a sorting network on order-preserving
-// integer keys.  The network is Batcher's odd-even merge sort for arbitrary n
-// (the iterative formulation: for p = 1,2,4..; k = p,p/2..1; j = k mod p,
-// step 2k; i < min(k, n-j-k); compare (i+j, i+j+k) when both lie in the same
-// 2p block), built at compile time; only the comparators the middle output
-// depends on survive dead-code elimination.  Keys map floats so that unsigned
-// order is Julia's isless order (-0.0 < 0.0, NaN after +Inf), which is what
-// partialsort! uses (src/mapwindow.jl:123-128).
-// =========================================================================
-template <int N> struct Net {
-    int n = 0;
-    short a[640] = {};
-    short b[640] = {};
-};
-
-template <int N> constexpr Net<N> make_net()
-{
-    Net<N> r{};
-    for (int p = 1; p < N; p <<= 1)
-        for (int k = p; k >= 1; k >>= 1)
-            for (int j = k % p; j + k < N; j += 2 * k)
-                for (int i = 0; i < k && i < N - j - k; ++i)
-                    if ((i + j) / (2 * p) == (i + j + k) / (2 * p)) {
-                        r.a[r.n] = (short)(i + j);
-                        r.b[r.n] = (short)(i + j + k);
-                        ++r.n;
-                    }
-    return r;
-}
-
-template <int N> struct NetOf { static constexpr Net<N> net = make_net<N>(); };
-
-template <class T> struct SortKey;
-template <> struct SortKey<float> {
-    using K = uint32_t;
-    static __device__ __forceinline__ K key(float x)
-    {
-        uint32_t b = isnan(x) ? 0x7fffffffu : __float_as_uint(x);
-        return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-    }
-    static __device__ __forceinline__ float val(K k)
-    {
-        return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
-    }
-};
-template <> struct SortKey<double> {
-    using K = unsigned long long;
-    static __device__ __forceinline__ K key(double x)
-    {
-        unsigned long long b = isnan(x) ? 0x7fffffffffffffffull : (unsigned long long)__double_as_longlong(x);
-        return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
-    }
-    static __device__ __forceinline__ double val(K k)
-    {
-        return __longlong_as_double((long long)((k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k));
-    }
-};
-
-template <int N, int I, class K> __device__ __forceinline__ void net_cx(K (&v)[N])
-{
-    constexpr int x = NetOf<N>::net.a[I];
-    constexpr int y = NetOf<N>::net.b[I];
-    const K lo = v[x] < v[y] ? v[x] : v[y];
-    const K hi = v[x] < v[y] ? v[y] : v[x];
-    v[x] = lo;
-    v[y] = hi;
-}
-
-template <int N, class K, size_t... I>
-__device__ __forceinline__ void net_apply(K (&v)[N], std::index_sequence<I...>)
-{
-    (net_cx<N, (int)I, K>(v), ...);
-}
-
-template <int N, class K> __device__ __forceinline__ void net_sort(K (&v)[N])
-{
-    net_apply<N, K>(v, std::make_index_sequence<NetOf<N>::net.n>{});
-}
-
 constexpr int kFmTX = 32, kFmTY = 8;
 
 template <class T, int W0, int W1>
@@ -313,12 +218,12 @@ k_median_float(const T *__restrict__ img, void *out, int out_type, int nx, int n
     constexpr int CT = kFmTX + W0 - 1, RT = kFmTY + W1 - 1, N = W0 * W1;
     __shared__ T tile[RT * CT];
     const int tx0 = blockIdx.x * kFmTX, ty0 = blockIdx.y * kFmTY;
-    for (int idx = threadIdx.x; idx < RT * CT; idx += blockDim.x) {
+    gather_tile<8>(tile, RT * CT, [&](int idx) -> T {
         const int r = idx / CT, c = idx - r * CT;
         const int mx = map_index(tx0 + f0 + c, nx, style);
         const int my = map_index(ty0 + f1 + r, ny, style);
-        tile[idx] = (mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx];
-    }
+        return (mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx];
+    });
     __syncthreads();
     const int lx = threadIdx.x % kFmTX, ly = threadIdx.x / kFmTX;
     K v[N];

@@ -1,0 +1,104 @@
+// ifx_select.cuh -- exact selection primitives shared by the median kernels
+// and the batched engine: packed 8-bit rank counting and a compile-time
+// sorting network on order-preserving keys.
+#pragma once
+#include <cstdint>
+#include <utility>
+#include "ifx_common.cuh"
+
+namespace ifx {
+
+__device__ __forceinline__ uint32_t load_word(const uint8_t *row, int col)
+{
+    const int a = col & ~3, sh = col & 3;
+    const uint32_t lo = *reinterpret_cast<const uint32_t *>(row + a);
+    const uint32_t hi = *reinterpret_cast<const uint32_t *>(row + a + 4);
+    return __byte_perm(lo, hi, 0x3210 + 0x1111 * sh);
+}
+
+__device__ __forceinline__ uint32_t count_lt(uint32_t cnt, uint32_t w, uint32_t trial)
+{
+    return __vsub4(cnt, __vcmpltu4(w, trial));
+}
+
+// =========================================================================
+// Float median, 2-D, fixed window: a sorting network on order-preserving
+// integer keys.  The network is Batcher's odd-even merge sort for arbitrary n
+// (the iterative formulation: for p = 1,2,4..; k = p,p/2..1; j = k mod p,
+// step 2k; i < min(k, n-j-k); compare (i+j, i+j+k) when both lie in the same
+// 2p block), built at compile time; only the comparators the middle output
+// depends on survive dead-code elimination.  Keys map floats so that unsigned
+// order is Julia's isless order (-0.0 < 0.0, NaN after +Inf), which is what
+// partialsort! uses (src/mapwindow.jl:123-128).
+// =========================================================================
+template <int N> struct Net {
+    int n = 0;
+    short a[640] = {};
+    short b[640] = {};
+};
+
+template <int N> constexpr Net<N> make_net()
+{
+    Net<N> r{};
+    for (int p = 1; p < N; p <<= 1)
+        for (int k = p; k >= 1; k >>= 1)
+            for (int j = k % p; j + k < N; j += 2 * k)
+                for (int i = 0; i < k && i < N - j - k; ++i)
+                    if ((i + j) / (2 * p) == (i + j + k) / (2 * p)) {
+                        r.a[r.n] = (short)(i + j);
+                        r.b[r.n] = (short)(i + j + k);
+                        ++r.n;
+                    }
+    return r;
+}
+
+template <int N> struct NetOf { static constexpr Net<N> net = make_net<N>(); };
+
+template <class T> struct SortKey;
+template <> struct SortKey<float> {
+    using K = uint32_t;
+    static __device__ __forceinline__ K key(float x)
+    {
+        uint32_t b = isnan(x) ? 0x7fffffffu : __float_as_uint(x);
+        return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    }
+    static __device__ __forceinline__ float val(K k)
+    {
+        return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+    }
+};
+template <> struct SortKey<double> {
+    using K = unsigned long long;
+    static __device__ __forceinline__ K key(double x)
+    {
+        unsigned long long b = isnan(x) ? 0x7fffffffffffffffull : (unsigned long long)__double_as_longlong(x);
+        return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+    }
+    static __device__ __forceinline__ double val(K k)
+    {
+        return __longlong_as_double((long long)((k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k));
+    }
+};
+
+template <int N, int I, class K> __device__ __forceinline__ void net_cx(K (&v)[N])
+{
+    constexpr int x = NetOf<N>::net.a[I];
+    constexpr int y = NetOf<N>::net.b[I];
+    const K lo = v[x] < v[y] ? v[x] : v[y];
+    const K hi = v[x] < v[y] ? v[y] : v[x];
+    v[x] = lo;
+    v[y] = hi;
+}
+
+template <int N, class K, size_t... I>
+__device__ __forceinline__ void net_apply(K (&v)[N], std::index_sequence<I...>)
+{
+    (net_cx<N, (int)I, K>(v), ...);
+}
+
+template <int N, class K> __device__ __forceinline__ void net_sort(K (&v)[N])
+{
+    net_apply<N, K>(v, std::make_index_sequence<NetOf<N>::net.n>{});
+}
+
+} // namespace ifx

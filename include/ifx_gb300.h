@@ -171,6 +171,41 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
                           const int64_t *wfirst, const int64_t *wlen,
                           const ifx_border_t *border, int32_t which, void *stream);
 
+/* ---- batched engine: many 2-D requests in one persistent launch --------------
+ * The requests of a batch are cut into output tiles that resident CTAs take
+ * from one device work-queue; a CUDA graph replays the descriptor upload and
+ * the launch.  Every array must be device memory (IFX_ERR_ARGUMENT
+ * otherwise); the work is enqueued on `stream` and the call returns at once.
+ * Results equal the single-request entry points:
+ *   IFX_OP_FACTORED2D  ifx_imfilter_factored with factors (axis 0, axis 1),
+ *                      each at most 33 taps; FP32 arithmetic
+ *   IFX_OP_GRADIENTS2D ifx_imgradients with a 3-tap pair at first index -1
+ *                      (weights[0] = derivative, weights[1] = smoothing)
+ *   IFX_OP_LAPLACIAN2D ifx_imfilter_laplacian, flags (1,1), Float32 output
+ *   IFX_OP_MEDIAN2D    ifx_mapwindow_median, window 3x3 or 5x5
+ * Images are Float32, N0f8 or UInt8; outputs Float32 or Float64. */
+typedef enum {
+    IFX_OP_FACTORED2D = 1,
+    IFX_OP_GRADIENTS2D = 2,
+    IFX_OP_LAPLACIAN2D = 3,
+    IFX_OP_MEDIAN2D = 4
+} ifx_op;
+
+typedef struct ifx_request {
+    int32_t op;                    /* ifx_op */
+    int32_t window;                /* IFX_OP_MEDIAN2D: 3 or 5 */
+    ifx_array_t img;
+    ifx_array_t out[2];            /* out[1] is used by IFX_OP_GRADIENTS2D only */
+    ifx_border_t border;
+    int32_t taps[2];
+    int64_t first[2];
+    const double *weights[2];      /* host memory */
+} ifx_request_t;
+
+/* Runs the batch; *tiles receives the number of tiles (may be NULL). */
+int ifx_batch_run(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n, int64_t *tiles,
+                  void *stream);
+
 #ifdef __cplusplus
 }
 #endif
