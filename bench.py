@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--per-step", type=int, default=500)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--e2e-requests", type=int, default=1000)
+    p.add_argument("--hbm-cap-gb", type=int, default=150)
     return p.parse_args()
 
 
@@ -235,6 +237,8 @@ def run_stream(args, ifx, torch, rank):
     stream = torch.cuda.current_stream().cuda_stream
     tiles = C.c_int64()
 
+    host_s = [0.0]
+
     def timed_region(mode, record_calls):
         ev = []
         if WORLD[1] > 1:
@@ -250,7 +254,9 @@ def run_stream(args, ifx, torch, rank):
                     e0 = torch.cuda.Event(enable_timing=True)
                     e1 = torch.cuda.Event(enable_timing=True)
                     e0.record()
+                    h0 = time.perf_counter()
                     rc = ctx.lib.ifx_batch_run(ctx.handle, arr, len(w), C.byref(tiles), stream)
+                    host_s[0] += time.perf_counter() - h0
                     e1.record()
                     if rc:
                         A.check(rc)
@@ -293,62 +299,131 @@ def run_stream(args, ifx, torch, rank):
         bk[2] += 1
     pixels = sum(r.pixels for r in timed)
     return {"pixels": pixels, "dev_ms": batch_ms, "plain_ms": plain_ms, "launches": launches,
+            "host_ms_per_step": host_s[0] * 1e3 / max(len(timed_p), 1),
             "per_op": per_op, "batch_kernel": bk, "clocks": clocks, "reqs": timed}
 
 
 def run_stream_e2e(args, ifx, torch, reqs_all):
-    """Per-request calls with pinned host buffers (H2D + compute + D2H each)."""
-    from imagefiltering_gb300 import synthetic as S
-    reqs = reqs_all[: min(len(reqs_all), 200)]
+    """Through the serving loop with pinned HOST buffers: every request's image
+    is copied host->device and its outputs device->host inside the timed
+    region.  Throughput: all requests submitted at once.  Latency: Poisson
+    arrivals at half the measured throughput, p50/p99 of submit -> outputs in
+    host memory."""
+    from imagefiltering_gb300.serve import Server
+    reqs = reqs_all[: min(len(reqs_all), args.e2e_requests)]
     A = ifx._abi
-    pins = []
-    h2d = d2h = 0
+    align = 256
+
+    def sz(n):
+        return (n + align - 1) // align * align
+    in_total = sum(sz(r.in_bytes()) for r in reqs)
+    out_total = sum(sz(b) for r in reqs for b in [r.pixels * (8 if k == "F64" else 4) for k in r.out_kinds()])
+    in_arena = torch.empty(in_total, dtype=torch.uint8).pin_memory()
+    out_arena = torch.empty(out_total, dtype=torch.uint8).pin_memory()
+    # synthetic content: uniform [0,1) floats (8-bit images see their bytes as codes)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(55)
+    chunk = 1 << 28
+    for o in range(0, in_total // 4 * 4, chunk):
+        n = min(chunk, in_total // 4 * 4 - o)
+        in_arena[o:o + n].view(torch.float32).copy_(
+            torch.rand(n // 4, device="cuda", generator=g).view(torch.float32).cpu().view(torch.float32))
+    in_np = in_arena.numpy()
+    out_np = out_arena.numpy()
+    items = []
+    io = oo = 0
+    from imagefiltering_gb300 import batch as B
     for r in reqs:
-        img = S.image_for(r)
-        t_in = torch.from_numpy(np.ascontiguousarray(img.T)).pin_memory()
-        outs = [torch.empty((r.w, r.h), dtype=torch.float64 if k == "F64" else torch.float32).pin_memory()
-                for k in r.out_kinds()]
-        pins.append((r, t_in, outs))
-        h2d += r.in_bytes()
-        d2h += r.out_bytes()
-    # one warm call per op
-    def call(r, t_in, outs):
-        ai = A.describe(t_in.data_ptr(), r.kind, (r.h, r.w))
-        descs = [A.describe(o.data_ptr(), k, (r.h, r.w)) for o, k in zip(outs, r.out_kinds())]
-        b = A.border_struct(r.style)
-        ctx = A.context()
-        lib = ctx.lib
-        if r.op == "gaussian":
-            g = np.ascontiguousarray(ifx.KernelFactors.gaussian(r.sigma).data, dtype=np.float64)
-            fac = (A.IfxFactor * 2)()
-            for i in range(2):
-                fac[i].axis, fac[i].length, fac[i].first, fac[i].weights = i, g.size, -(g.size // 2), A.dptr(g)
-            A.check(lib.ifx_imfilter_factored(ctx.handle, descs[0], ai, 2, fac, b, None))
-        elif r.op == "sobel":
-            import ctypes as C
-            d, s = ifx.KernelFactors.sobel.gradient_pair
-            d, s = np.ascontiguousarray(d), np.ascontiguousarray(s)
-            A.check(lib.ifx_imgradients(ctx.handle, (A.IfxArray * 2)(*descs), ai, A.dptr(d), A.dptr(s),
-                                        3, -1, (C.c_int32 * 4)(1, 1), b, None))
-        elif r.op == "laplacian":
-            import ctypes as C
-            A.check(lib.ifx_imfilter_laplacian(ctx.handle, descs[0], ai, (C.c_int32 * 4)(1, 1), b, None))
+        nb = r.in_bytes()
+        if r.kind == "F32":
+            img = in_np[io:io + nb].view(np.float32).reshape((r.h, r.w), order="F")
         else:
-            import ctypes as C
-            A.check(lib.ifx_mapwindow_median(ctx.handle, descs[0], ai,
-                                             (C.c_int64 * 4)(-(r.win // 2), -(r.win // 2)),
-                                             (C.c_int64 * 4)(r.win, r.win), b, None))
-    for p in pins[:8]:
-        call(*p)
-    torch.cuda.synchronize()
+            img = ifx.n0f8(in_np[io:io + nb].reshape((r.h, r.w), order="F"))
+        io += sz(nb)
+        outs = []
+        for k in r.out_kinds():
+            ob = r.pixels * (8 if k == "F64" else 4)
+            outs.append(out_np[oo:oo + ob].view(np.float64 if k == "F64" else np.float32)
+                        .reshape((r.h, r.w), order="F"))
+            oo += sz(ob)
+        bt = B.Batch()
+        q = bt.add(BATCH_OP[r.op](r), img, outs, r.style)
+        items.append((r, q, bt))
+    h2d = sum(r.in_bytes() for r in reqs)
+    d2h = sum(r.out_bytes() for r in reqs)
+    res = {}
+    with Server(hbm_cap_bytes=args.hbm_cap_gb << 30, max_batch=args.per_step, max_inflight=2) as srv:
+        for r, q, bt in items[:50]:                                       # warm-up
+            srv.submit_struct(q)
+        srv.drain()
+        srv.reset_metrics()
+        t0 = time.perf_counter()
+        for r, q, bt in items:
+            srv.submit_struct(q)
+        srv.drain()
+        wall = time.perf_counter() - t0
+        m = srv.metrics()
+        px = sum(r.pixels for r in reqs)
+        res["value"] = px / wall / 1e6
+        res["throughput_p50_ms"] = m["p50_latency_s"] * 1e3
+        res["throughput_p99_ms"] = m["p99_latency_s"] * 1e3
+        res["hbm_peak_gb"] = m["hbm_peak"] / 2 ** 30
+        res["batches"] = m["batches"]
+        # Poisson arrivals at half the measured request rate
+        rate = 0.5 * len(reqs) / wall
+        srv.reset_metrics()
+        rng = np.random.default_rng(5)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(items)))
+        t0 = time.perf_counter()
+        for (r, q, bt), ta in zip(items, arrivals):
+            while time.perf_counter() - t0 < ta:
+                pass
+            srv.submit_struct(q)
+        srv.drain()
+        m = srv.metrics()
+        res["latency"] = {"arrivals": "Poisson", "rate_req_per_s": rate,
+                          "p50_ms": m["p50_latency_s"] * 1e3, "p99_ms": m["p99_latency_s"] * 1e3,
+                          "max_ms": m["max_latency_s"] * 1e3, "requests": m["completed"]}
+    n = len(reqs)
+    res.update({"unit": "Mpixel/s", "h2d_bytes_per_step": int(h2d * args.per_step / n),
+                "d2h_bytes_per_step": int(d2h * args.per_step / n), "requests": n,
+                "mode": "served: ifx_server (continuous batching, HBM cap %d GB) with pinned host "
+                        "buffers" % args.hbm_cap_gb})
+    # plain per-request blocking calls with the same host buffers, for comparison
+    plain = reqs[: min(n, 200)]
     t0 = time.perf_counter()
-    for p in pins:
-        call(*p)
+    for r, q, bt in items[: len(plain)]:
+        call_single(ifx, r, q)
     dt = time.perf_counter() - t0
-    px = sum(r.pixels for r in reqs)
-    return {"value": px / dt / 1e6, "unit": "Mpixel/s", "h2d_bytes_per_step": int(h2d * args.per_step / len(reqs)),
-            "d2h_bytes_per_step": int(d2h * args.per_step / len(reqs)), "requests": len(reqs),
-            "mode": "plain per-request C-ABI calls, pinned host buffers"}
+    res["plain_per_call"] = {"value": sum(r.pixels for r in plain) / dt / 1e6, "unit": "Mpixel/s",
+                             "requests": len(plain),
+                             "mode": "one blocking C-ABI call per request with host buffers"}
+    return res
+
+
+def call_single(ifx, r, q):
+    """The single-request entry point for request `r` with the arrays of `q`."""
+    import ctypes as C
+    A = ifx._abi
+    ctx = A.context()
+    lib = ctx.lib
+    if q.op == A.OP_FACTORED2D:
+        fac = (A.IfxFactor * 2)()
+        for i in range(2):
+            fac[i].axis, fac[i].length, fac[i].first, fac[i].weights = i, q.taps[i], q.first[i], q.weights[i]
+        A.check(lib.ifx_imfilter_factored(ctx.handle, C.byref(q.out[0]), C.byref(q.img), 2, fac,
+                                          C.byref(q.border), None))
+    elif q.op == A.OP_GRADIENTS2D:
+        A.check(lib.ifx_imgradients(ctx.handle, q.out, C.byref(q.img), q.weights[0], q.weights[1], 3, -1,
+                                    (C.c_int32 * 4)(1, 1), C.byref(q.border), None))
+    elif q.op == A.OP_LAPLACIAN2D:
+        A.check(lib.ifx_imfilter_laplacian(ctx.handle, C.byref(q.out[0]), C.byref(q.img),
+                                           (C.c_int32 * 4)(1, 1), C.byref(q.border), None))
+    else:
+        w = q.window
+        A.check(lib.ifx_mapwindow_median(ctx.handle, C.byref(q.out[0]), C.byref(q.img),
+                                         (C.c_int64 * 4)(-(w // 2), -(w // 2)), (C.c_int64 * 4)(w, w),
+                                         C.byref(q.border), None))
 
 
 def cpu_stream_baseline(args, seconds, threads):
@@ -459,6 +534,7 @@ def main():
                       "mode": "one C-ABI call per request (device-resident)",
                       "per_op_ms": {k: round(v[0], 3) for k, v in per_op.items()}},
         "batched_over_plain": value / plain_value,
+        "host_ms_per_step": res["host_ms_per_step"],
         "e2e": e2e,
         "gpu_launches": res["launches"],
         "roofline": {"bound": "hbm", "kernel": "k_batch (persistent tile work-queue)",

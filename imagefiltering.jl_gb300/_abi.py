@@ -72,10 +72,23 @@ class IfxRequest(C.Structure):
 
 OP_FACTORED2D, OP_GRADIENTS2D, OP_LAPLACIAN2D, OP_MEDIAN2D = 1, 2, 3, 4
 
+
+class IfxServerConfig(C.Structure):
+    _fields_ = [("hbm_cap_bytes", C.c_int64), ("max_batch", C.c_int32), ("max_inflight", C.c_int32)]
+
+
+class IfxServerMetrics(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("batches", C.c_uint64), ("pixels", C.c_uint64), ("p50_latency_s", C.c_double),
+                ("p99_latency_s", C.c_double), ("max_latency_s", C.c_double), ("busy_s", C.c_double),
+                ("hbm_in_use", C.c_int64), ("hbm_peak", C.c_int64), ("queue_depth", C.c_int32)]
+
 SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "ifx_launch_count",
            "ifx_synchronize", "ifx_padarray", "ifx_imfilter_factored", "ifx_imfilter_dense",
            "ifx_imfilter_laplacian", "ifx_imgradients", "ifx_mapwindow_median",
-           "ifx_mapwindow_extrema", "ifx_batch_run"]
+           "ifx_mapwindow_extrema", "ifx_batch_run", "ifx_server_create", "ifx_server_submit",
+           "ifx_server_wait", "ifx_server_drain", "ifx_server_metrics", "ifx_server_reset_metrics",
+           "ifx_server_destroy"]
 
 _lib = None
 _lock = threading.Lock()
@@ -114,6 +127,13 @@ def load(path: str = LIB_PATH):
         lib.ifx_mapwindow_extrema.argtypes = [vp, P(IfxArray), P(IfxArray), P(C.c_int64),
                                               P(C.c_int64), P(IfxBorder), C.c_int32, vp]
         lib.ifx_batch_run.argtypes = [vp, P(IfxRequest), C.c_int32, P(C.c_int64), vp]
+        lib.ifx_server_create.argtypes = [vp, P(IfxServerConfig), P(vp)]
+        lib.ifx_server_submit.argtypes = [vp, P(IfxRequest), P(C.c_uint64)]
+        lib.ifx_server_wait.argtypes = [vp, C.c_uint64, C.c_double, P(C.c_int32)]
+        lib.ifx_server_drain.argtypes = [vp, C.c_double]
+        lib.ifx_server_metrics.argtypes = [vp, P(IfxServerMetrics)]
+        lib.ifx_server_reset_metrics.argtypes = [vp]
+        lib.ifx_server_destroy.argtypes = [vp]
         for name in SYMBOLS:
             getattr(lib, name)          # every declared entry point must be exported
         _lib = lib

@@ -398,6 +398,81 @@ static int check_filter_types(const ifx_array_t &img, const ifx_array_t &out)
     return IFX_OK;
 }
 
+// Validation of one batched request (also used by the server, which accepts
+// host arrays and stages them itself).  Fills `it` with the request's own
+// pointers and weights.
+int request_item(const ifx_request_t &q, int i, bool need_device, BatchItem &it)
+{
+    int rc;
+    if ((rc = check_array(&q.img, "img")) || (rc = check_border(&q.border))) return rc;
+    if (q.img.ndim != 2) return fail(IFX_ERR_UNSUPPORTED, "request %d: batched requests are 2-D", i);
+    const int et = q.img.eltype;
+    if (et != IFX_F32 && !is8(et))
+        return fail(IFX_ERR_UNSUPPORTED, "request %d: batched images are Float32, N0f8 or UInt8", i);
+    const int nout = q.op == IFX_OP_GRADIENTS2D ? 2 : 1;
+    if (q.op < IFX_OP_FACTORED2D || q.op > IFX_OP_MEDIAN2D)
+        return fail(IFX_ERR_ARGUMENT, "request %d: unknown op %d", i, q.op);
+    for (int o = 0; o < nout; ++o) {
+        if ((rc = check_array(&q.out[o], "out")) || (rc = check_same_axes(q.out[o], q.img))) return rc;
+        const int ot = q.out[o].eltype;
+        if (ot != IFX_F32 && ot != IFX_F64)
+            return fail(IFX_ERR_UNSUPPORTED, "request %d: outputs are Float32 or Float64", i);
+        if (need_device && !is_device_ptr(q.out[o].data))
+            return fail(IFX_ERR_ARGUMENT, "request %d: batched outputs must be device memory", i);
+    }
+    if (q.out[0].eltype != (nout == 2 ? q.out[1].eltype : q.out[0].eltype))
+        return fail(IFX_ERR_UNSUPPORTED, "request %d: both gradients need one eltype", i);
+    if (need_device && !is_device_ptr(q.img.data))
+        return fail(IFX_ERR_ARGUMENT, "request %d: batched images must be device memory", i);
+    if (q.border.explicit_pad)
+        return fail(IFX_ERR_UNSUPPORTED, "request %d: explicit padding sizes in a batch", i);
+    if ((rc = check_reflect(&q.border, q.img))) return rc;
+    memset(&it, 0, sizeof it);
+    it.op = q.op;
+    it.in_type = et;
+    it.out_type = q.out[0].eltype;
+    it.style = q.border.style;
+    it.nx = (int)q.img.size[0];
+    it.ny = (int)q.img.size[1];
+    it.in = q.img.data;
+    it.out0 = q.out[0].data;
+    it.out1 = nout == 2 ? q.out[1].data : nullptr;
+    double code = 0.0;
+    if ((rc = fill_for(&q.border, et, &code))) return rc;
+    it.fill_code = is8(et) ? (int)code : 0;
+    it.fill = et == IFX_N0F8 ? (double)((float)code / 255.0f) : code;
+    if (et == IFX_F32) it.fill = (double)(float)code;
+    if (q.op == IFX_OP_FACTORED2D) {
+        for (int a = 0; a < 2; ++a)
+            if (q.taps[a] < 1 || q.taps[a] > 33 || !q.weights[a] || q.first[a] < -4096 || q.first[a] > 4096)
+                return fail(IFX_ERR_UNSUPPORTED, "request %d: batched factors have 1..33 taps", i);
+        it.kx = q.taps[0];
+        it.ky = q.taps[1];
+        it.fx = (int)q.first[0];
+        it.fy = (int)q.first[1];
+        it.wx = q.weights[0];
+        it.wy = q.weights[1];
+    } else if (q.op == IFX_OP_GRADIENTS2D) {
+        if (q.taps[0] != 3 || q.taps[1] != 3 || q.first[0] != -1 || q.first[1] != -1 ||
+            !q.weights[0] || !q.weights[1])
+            return fail(IFX_ERR_UNSUPPORTED, "request %d: batched gradients use 3-tap centred pairs", i);
+        it.kx = it.ky = 3;
+        it.fx = it.fy = -1;
+        it.wx = q.weights[0];
+        it.wy = q.weights[1];
+    } else if (q.op == IFX_OP_LAPLACIAN2D) {
+        if (it.out_type != IFX_F32 || (is8(et) && et != IFX_N0F8))
+            return fail(IFX_ERR_UNSUPPORTED, "request %d: batched Laplacian writes Float32", i);
+    } else {
+        if (q.window != 3 && q.window != 5)
+            return fail(IFX_ERR_UNSUPPORTED, "request %d: batched median windows are 3 or 5", i);
+        it.window = q.window;
+    }
+    return IFX_OK;
+}
+
+int set_error(int code, const char *msg) { return fail(code, "%s", msg); }
+
 } // namespace ifx
 
 using namespace ifx;
@@ -889,73 +964,8 @@ int ifx_batch_run(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n, int6
     if (tiles) *tiles = 0;
     std::vector<BatchItem> items((size_t)n);
     for (int i = 0; i < n; ++i) {
-        const ifx_request_t &q = reqs[i];
-        BatchItem &it = items[i];
-        int rc;
-        if ((rc = check_array(&q.img, "img")) || (rc = check_border(&q.border))) return rc;
-        if (q.img.ndim != 2) return fail(IFX_ERR_UNSUPPORTED, "request %d: batched requests are 2-D", i);
-        const int et = q.img.eltype;
-        if (et != IFX_F32 && !is8(et))
-            return fail(IFX_ERR_UNSUPPORTED, "request %d: batched images are Float32, N0f8 or UInt8", i);
-        const int nout = q.op == IFX_OP_GRADIENTS2D ? 2 : 1;
-        if (q.op < IFX_OP_FACTORED2D || q.op > IFX_OP_MEDIAN2D)
-            return fail(IFX_ERR_ARGUMENT, "request %d: unknown op %d", i, q.op);
-        for (int o = 0; o < nout; ++o) {
-            if ((rc = check_array(&q.out[o], "out")) || (rc = check_same_axes(q.out[o], q.img))) return rc;
-            const int ot = q.out[o].eltype;
-            if (ot != IFX_F32 && ot != IFX_F64)
-                return fail(IFX_ERR_UNSUPPORTED, "request %d: outputs are Float32 or Float64", i);
-            if (!is_device_ptr(q.out[o].data))
-                return fail(IFX_ERR_ARGUMENT, "request %d: batched outputs must be device memory", i);
-        }
-        if (q.out[0].eltype != (nout == 2 ? q.out[1].eltype : q.out[0].eltype))
-            return fail(IFX_ERR_UNSUPPORTED, "request %d: both gradients need one eltype", i);
-        if (!is_device_ptr(q.img.data))
-            return fail(IFX_ERR_ARGUMENT, "request %d: batched images must be device memory", i);
-        if (q.border.explicit_pad)
-            return fail(IFX_ERR_UNSUPPORTED, "request %d: explicit padding sizes in a batch", i);
-        if ((rc = check_reflect(&q.border, q.img))) return rc;
-        memset(&it, 0, sizeof it);
-        it.op = q.op;
-        it.in_type = et;
-        it.out_type = q.out[0].eltype;
-        it.style = q.border.style;
-        it.nx = (int)q.img.size[0];
-        it.ny = (int)q.img.size[1];
-        it.in = q.img.data;
-        it.out0 = q.out[0].data;
-        it.out1 = nout == 2 ? q.out[1].data : nullptr;
-        double code = 0.0;
-        if ((rc = fill_for(&q.border, et, &code))) return rc;
-        it.fill_code = is8(et) ? (int)code : 0;
-        it.fill = et == IFX_N0F8 ? (double)((float)code / 255.0f) : code;
-        if (et == IFX_F32) it.fill = (double)(float)code;
-        if (q.op == IFX_OP_FACTORED2D) {
-            for (int a = 0; a < 2; ++a)
-                if (q.taps[a] < 1 || q.taps[a] > 33 || !q.weights[a] || q.first[a] < -4096 || q.first[a] > 4096)
-                    return fail(IFX_ERR_UNSUPPORTED, "request %d: batched factors have 1..33 taps", i);
-            it.kx = q.taps[0];
-            it.ky = q.taps[1];
-            it.fx = (int)q.first[0];
-            it.fy = (int)q.first[1];
-            it.wx = q.weights[0];
-            it.wy = q.weights[1];
-        } else if (q.op == IFX_OP_GRADIENTS2D) {
-            if (q.taps[0] != 3 || q.taps[1] != 3 || q.first[0] != -1 || q.first[1] != -1 ||
-                !q.weights[0] || !q.weights[1])
-                return fail(IFX_ERR_UNSUPPORTED, "request %d: batched gradients use 3-tap centred pairs", i);
-            it.kx = it.ky = 3;
-            it.fx = it.fy = -1;
-            it.wx = q.weights[0];
-            it.wy = q.weights[1];
-        } else if (q.op == IFX_OP_LAPLACIAN2D) {
-            if (it.out_type != IFX_F32 || is8(et) && et != IFX_N0F8)
-                return fail(IFX_ERR_UNSUPPORTED, "request %d: batched Laplacian writes Float32", i);
-        } else {
-            if (q.window != 3 && q.window != 5)
-                return fail(IFX_ERR_UNSUPPORTED, "request %d: batched median windows are 3 or 5", i);
-            it.window = q.window;
-        }
+        int rc = request_item(reqs[i], i, true, items[i]);
+        if (rc) return rc;
     }
     if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
     std::lock_guard<std::mutex> lk(ctx->mu);

@@ -206,6 +206,43 @@ typedef struct ifx_request {
 int ifx_batch_run(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n, int64_t *tiles,
                   void *stream);
 
+/* ---- serving: continuous batching of requests as they arrive ---------------
+ * ifx_server_submit returns at once with a ticket.  An engine thread admits
+ * queued requests in arrival order while the device bytes they need (staged
+ * host images and host outputs; device arrays are used in place and cost
+ * nothing) fit under hbm_cap_bytes, uploads host images on a copy stream,
+ * packs admitted requests into batched launches (at most max_batch each, at
+ * most max_inflight batches on the device at once), copies host outputs back
+ * and frees their device memory.  Requests use the ifx_request_t forms of
+ * ifx_batch_run; the weights are copied at submit.  Latency is measured from
+ * submit to results in place (host outputs copied back). */
+typedef struct ifx_server ifx_server_t;
+
+typedef struct ifx_server_config {
+    int64_t hbm_cap_bytes;         /* device bytes held by admitted requests, at most */
+    int32_t max_batch;             /* requests per batched launch */
+    int32_t max_inflight;          /* batched launches on the device at once */
+} ifx_server_config_t;
+
+typedef struct ifx_server_metrics {
+    uint64_t submitted, completed, failed, batches;
+    uint64_t pixels;               /* pixels of completed requests */
+    double p50_latency_s, p99_latency_s, max_latency_s;
+    double busy_s;                 /* first submit -> last completion */
+    int64_t hbm_in_use, hbm_peak;
+    int32_t queue_depth;           /* submitted, not yet admitted */
+} ifx_server_metrics_t;
+
+int ifx_server_create(ifx_context_t *ctx, const ifx_server_config_t *cfg, ifx_server_t **srv);
+int ifx_server_submit(ifx_server_t *srv, const ifx_request_t *req, uint64_t *ticket);
+/* IFX_ERR_TIMEOUT when the request is not done within timeout_s; *status gets
+ * the request's own status when it is. */
+int ifx_server_wait(ifx_server_t *srv, uint64_t ticket, double timeout_s, int32_t *status);
+int ifx_server_drain(ifx_server_t *srv, double timeout_s);
+int ifx_server_metrics(ifx_server_t *srv, ifx_server_metrics_t *m);
+int ifx_server_reset_metrics(ifx_server_t *srv);
+int ifx_server_destroy(ifx_server_t *srv);
+
 #ifdef __cplusplus
 }
 #endif

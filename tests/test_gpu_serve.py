@@ -1,0 +1,112 @@
+"""The serving loop: continuous batching under an HBM cap, host and device
+arrays, results equal to the single-request API, latency metrics, bounded
+waits (a wait that runs out returns a timeout status, nothing hangs)."""
+import time
+
+import numpy as np
+import pytest
+
+from test_gpu_batch import mixed_requests, reference_call
+
+pytestmark = pytest.mark.gpu
+
+
+def host_outputs(ifx, img, op):
+    from imagefiltering_gb300 import batch as B
+    kinds = B.out_kinds(op)
+    if op[0] == "median":
+        kind = "N0F8" if isinstance(img, ifx.N0f8Array) else ("U8" if img.dtype == np.uint8 else "F32")
+        kinds = [B.MEDIAN_OUT[kind]]
+    return [np.empty(img.shape, dtype=np.float64 if k == "F64" else np.float32, order="F") for k in kinds]
+
+
+def check_outputs(ifx, items, outs):
+    for (img, op, border), got in zip(items, outs):
+        ref = reference_call(ifx, img, op, border)
+        for g, r in zip(got, ref):
+            if op[0] in ("laplacian", "median"):
+                assert np.array_equal(g, r), (op, img.shape)
+            else:
+                d = np.max(np.abs(g - r)) / max(np.max(np.abs(r)), 1e-300)
+                assert d <= 1e-6, (op, img.shape)
+
+
+def test_server_host_arrays_match_single_calls(gpu_ifx):
+    ifx = gpu_ifx
+    from imagefiltering_gb300.serve import Server
+    items = mixed_requests(ifx, seed=3, n=50)
+    with Server(hbm_cap_bytes=1 << 30, max_batch=16) as srv:
+        outs, tickets = [], []
+        for img, op, border in items:
+            o = host_outputs(ifx, img, op)
+            outs.append(o)
+            tickets.append(srv.submit(op, img, o, border))
+        for t in tickets:
+            srv.wait(t, timeout=60)
+        m = srv.metrics()
+    assert m["completed"] == len(items) and m["failed"] == 0
+    assert m["batches"] >= 4                      # max_batch 16 -> several launches
+    assert 0 < m["p50_latency_s"] <= m["p99_latency_s"]
+    check_outputs(ifx, items, outs)
+
+
+def test_server_admission_under_a_small_cap(gpu_ifx):
+    """Total device footprint far above the cap: everything completes and the
+    server never holds more than the cap."""
+    ifx = gpu_ifx
+    from imagefiltering_gb300.serve import Server
+    rng = np.random.default_rng(9)
+    cap = 24 << 20
+    items = []
+    for i in range(40):
+        img = np.asfortranarray(rng.random((512, 512), dtype=np.float32))   # 1 MiB in, 2-4 MiB out
+        items.append((img, ("gaussian", 1.5) if i % 2 else ("median", 5), ifx.Pad("reflect")))
+    with Server(hbm_cap_bytes=cap, max_batch=8) as srv:
+        outs = [host_outputs(ifx, img, op) for img, op, b in items]
+        ts = [srv.submit(op, img, o, b) for (img, op, b), o in zip(items, outs)]
+        srv.drain(timeout=120)
+        m = srv.metrics()
+        for t in ts:
+            srv.wait(t, timeout=1)
+    assert m["completed"] == 40
+    assert m["hbm_peak"] <= cap
+    check_outputs(ifx, items[:6], outs[:6])
+
+
+def test_server_device_arrays_and_arrivals(gpu_ifx):
+    """Device-resident requests arriving while earlier ones run."""
+    ifx = gpu_ifx
+    import torch
+    from imagefiltering_gb300 import batch as B
+    from imagefiltering_gb300.serve import Server
+    items = mixed_requests(ifx, seed=4, n=30)
+    with Server(hbm_cap_bytes=1 << 30, max_batch=4) as srv:
+        douts, ts = [], []
+        for img, op, border in items:
+            d = ifx.DeviceArray.from_host(img)
+            torch.cuda.synchronize()
+            o = B.outputs_for(op, d)
+            douts.append(o)
+            ts.append(srv.submit(op, d, o, border))
+            time.sleep(0.0005)
+        for t in ts:
+            srv.wait(t, timeout=60)
+    check_outputs(ifx, items, [[x.numpy() for x in o] for o in douts])
+
+
+def test_server_bounded_wait_and_oversize(gpu_ifx):
+    ifx = gpu_ifx
+    from imagefiltering_gb300.serve import Server
+    img = np.asfortranarray(np.ones((2048, 2048), np.float32))
+    out = [np.empty((2048, 2048), np.float64, order="F")]
+    with Server(hbm_cap_bytes=8 << 20, max_batch=4) as srv:
+        with pytest.raises(ifx.OutOfMemory):
+            srv.submit(("gaussian", 2.0), img, out)          # needs 48 MiB > cap
+        small = np.asfortranarray(np.ones((64, 64), np.float32))
+        so = [np.empty((64, 64), np.float32, order="F")]
+        t = srv.submit(("median", 3), small, so)
+        try:
+            srv.wait(t, timeout=0.0)                          # may or may not be done yet
+        except TimeoutError:
+            srv.wait(t, timeout=30)
+        assert np.all(so[0] == 1.0)
