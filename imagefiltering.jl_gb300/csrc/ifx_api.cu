@@ -151,6 +151,47 @@ static bool is_device_ptr(const void *p)
     return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
 }
 
+// Device allocations seen by one call, as [base, end) ranges from the driver's
+// cuMemGetAddressRange: arrays inside a known allocation need no further
+// pointer query, and an array must end inside the allocation it starts in.
+typedef int (*PfnAddressRange)(unsigned long long *base, size_t *size, unsigned long long dptr);
+
+static PfnAddressRange address_range_fn()
+{
+    static PfnAddressRange fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PfnAddressRange)p;
+        (void)cudaGetLastError();
+    });
+    return fn;
+}
+
+struct DevRanges {
+    std::vector<std::pair<uintptr_t, uintptr_t>> r;
+    // true when [p, p+bytes) lies in device memory
+    bool holds(const void *p, size_t bytes)
+    {
+        const uintptr_t a = (uintptr_t)p, e = a + (bytes ? bytes : 1);
+        for (auto &x : r)
+            if (a >= x.first && e <= x.second) return true;
+        if (!is_device_ptr(p)) return false;
+        PfnAddressRange fn = address_range_fn();
+        unsigned long long base = 0;
+        size_t size = 0;
+        if (fn && fn(&base, &size, (unsigned long long)a) == 0) {
+            r.push_back({(uintptr_t)base, (uintptr_t)(base + size)});
+            return e <= (uintptr_t)(base + size);
+        }
+        return is_device_ptr((const char *)p + (bytes ? bytes - 1 : 0));
+    }
+};
+
 // Staging of one call's arrays: host arrays are copied to scratch slots.
 struct Call {
     ifx_context *ctx;
@@ -401,7 +442,7 @@ static int check_filter_types(const ifx_array_t &img, const ifx_array_t &out)
 // Validation of one batched request (also used by the server, which accepts
 // host arrays and stages them itself).  Fills `it` with the request's own
 // pointers and weights.
-int request_item(const ifx_request_t &q, int i, bool need_device, BatchItem &it)
+int request_item(const ifx_request_t &q, int i, bool need_device, BatchItem &it, DevRanges *dr)
 {
     int rc;
     if ((rc = check_array(&q.img, "img")) || (rc = check_border(&q.border))) return rc;
@@ -417,12 +458,14 @@ int request_item(const ifx_request_t &q, int i, bool need_device, BatchItem &it)
         const int ot = q.out[o].eltype;
         if (ot != IFX_F32 && ot != IFX_F64)
             return fail(IFX_ERR_UNSUPPORTED, "request %d: outputs are Float32 or Float64", i);
-        if (need_device && !is_device_ptr(q.out[o].data))
+        if (need_device && !(dr ? dr->holds(q.out[o].data, (size_t)numel(q.out[o]) * elsize(ot))
+                                : is_device_ptr(q.out[o].data)))
             return fail(IFX_ERR_ARGUMENT, "request %d: batched outputs must be device memory", i);
     }
     if (q.out[0].eltype != (nout == 2 ? q.out[1].eltype : q.out[0].eltype))
         return fail(IFX_ERR_UNSUPPORTED, "request %d: both gradients need one eltype", i);
-    if (need_device && !is_device_ptr(q.img.data))
+    if (need_device && !(dr ? dr->holds(q.img.data, (size_t)numel(q.img) * elsize(et))
+                            : is_device_ptr(q.img.data)))
         return fail(IFX_ERR_ARGUMENT, "request %d: batched images must be device memory", i);
     if (q.border.explicit_pad)
         return fail(IFX_ERR_UNSUPPORTED, "request %d: explicit padding sizes in a batch", i);
@@ -963,8 +1006,9 @@ int ifx_batch_run(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n, int6
     if (n < 0 || (n > 0 && !reqs)) return fail(IFX_ERR_ARGUMENT, "bad request list");
     if (tiles) *tiles = 0;
     std::vector<BatchItem> items((size_t)n);
+    DevRanges ranges;
     for (int i = 0; i < n; ++i) {
-        int rc = request_item(reqs[i], i, true, items[i]);
+        int rc = request_item(reqs[i], i, true, items[i], &ranges);
         if (rc) return rc;
     }
     if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");

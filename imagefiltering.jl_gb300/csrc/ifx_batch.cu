@@ -55,8 +55,8 @@ enum { BOP_FACTORED = 1, BOP_GRADIENTS = 2, BOP_LAPLACIAN = 3, BOP_MEDIAN = 4 };
 
 // tile shapes (outputs per tile)
 constexpr int kFTX = 64, kFTY = 32;        // factored / gradients / laplacian
-constexpr int kMUX = 128, kMUY = 8;        // 8-bit median (4 pixels per thread)
-constexpr int kMFX = 32, kMFY = 8;         // float median (1 pixel per thread)
+constexpr int kMUX = 128, kMUY = 32;       // 8-bit median (4 pixels per thread, 4 rows)
+constexpr int kMFX = 64, kMFY = 32;        // float median (8 pixels per thread)
 
 __host__ __device__ inline int bt_tile_w(int op, int in_type)
 {
@@ -88,6 +88,37 @@ __device__ __forceinline__ void bt_store(const BReq &R, void *out, int x, int y,
     else ((float *)out)[o] = v;
 }
 
+// Division-free 2-D gather of a tile whose element (r, c) is load(r, c): warps
+// take rows, lanes take columns; each thread issues up to 2 rows x 4 column
+// chunks of loads before storing them, so 8 global loads are in flight.
+template <class T, class F>
+__device__ __forceinline__ void gather2d(T *dst, int rows, int cols, int pitch, F load)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int r0 = warp; r0 < rows; r0 += 2 * nw) {
+        T v[2][4];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int r = r0 + a * nw, c = lane + 32 * b;
+                v[a][b] = (r < rows && c < cols) ? load(r, c) : T(0);
+            }
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int r = r0 + a * nw, c = lane + 32 * b;
+                if (r < rows && c < cols) dst[r * pitch + c] = v[a][b];
+            }
+        for (int c = lane + 128; c < cols; c += 32)          // wide tiles: the rest of the row
+            for (int a = 0; a < 2; ++a) {
+                const int r = r0 + a * nw;
+                if (r < rows) dst[r * pitch + c] = load(r, c);
+            }
+    }
+}
+
 // ---------------------------------------------------------------- factored
 __device__ void bt_factored(const BReq &R, int tx0, int ty0, float *sm)
 {
@@ -99,8 +130,7 @@ __device__ void bt_factored(const BReq &R, int tx0, int ty0, float *sm)
     const int tid = threadIdx.x, nth = blockDim.x;
     if (tid < kx) wx[tid] = R.wx[tid];
     if (tid < ky) wy[tid] = R.wy[tid];
-    gather_tile<8>(T, RT * CT, [&](int idx) -> float {
-        const int r = idx / CT, c = idx - r * CT;
+    gather2d<float>(T, RT, CT, CT, [&](int r, int c) -> float {
         return c < CV ? bt_load(R, tx0 + R.fx + c, ty0 + R.fy + r) : 0.0f;
     });
     __syncthreads();
@@ -134,8 +164,7 @@ __device__ void bt_gradients(const BReq &R, int tx0, int ty0, float *sm)
     constexpr int TX = kFTX, TY = kFTY, NB = 8, CT = TX + 2, RT = TY + 2;
     float *T = sm;
     const int tid = threadIdx.x, nth = blockDim.x;
-    gather_tile<8>(T, RT * CT, [&](int idx) -> float {
-        const int r = idx / CT, c = idx - r * CT;
+    gather2d<float>(T, RT, CT, CT, [&](int r, int c) -> float {
         return bt_load(R, tx0 - 1 + c, ty0 - 1 + r);
     });
     __syncthreads();
@@ -166,8 +195,7 @@ __device__ void bt_laplacian(const BReq &R, int tx0, int ty0, float *sm)
     constexpr int TX = kFTX, TY = kFTY, CT = TX + 2, RT = TY + 2;
     float *T = sm;
     const int tid = threadIdx.x, nth = blockDim.x;
-    gather_tile<8>(T, RT * CT, [&](int idx) -> float {
-        const int r = idx / CT, c = idx - r * CT;
+    gather2d<float>(T, RT, CT, CT, [&](int r, int c) -> float {
         return bt_load(R, tx0 - 1 + c, ty0 - 1 + r);
     });
     __syncthreads();
@@ -200,9 +228,7 @@ template <int W>
 __device__ void bt_median_u8(const BReq &R, int tx0, int ty0, uint8_t *tile)
 {
     constexpr int CT = ((kMUX + W - 1 + 3) & ~3) + 4, RT = kMUY + W - 1, h = W / 2;
-    const int tid = threadIdx.x;
-    gather_tile<8>(tile, RT * CT, [&](int idx) -> uint8_t {
-        const int r = idx / CT, c = idx - r * CT;
+    gather2d<uint8_t>(tile, RT, CT, CT, [&](int r, int c) -> uint8_t {
         if (c >= kMUX + W - 1) return 0;
         const int mx = map_index(tx0 - h + c, R.nx, R.style);
         const int my = map_index(ty0 - h + r, R.ny, R.style);
@@ -210,48 +236,51 @@ __device__ void bt_median_u8(const BReq &R, int tx0, int ty0, uint8_t *tile)
                                   : ((const uint8_t *)R.in)[(long long)my * R.nx + mx];
     });
     __syncthreads();
-    const int lx = (tid & 31) * 4, ly = tid >> 5;
-    const int x0 = tx0 + lx, y = ty0 + ly;
-    uint32_t w[W * W];
-    const bool edge = R.style == IFX_CIRCULAR &&
-                      (x0 < h || x0 + 3 >= R.nx - h || y < h || y >= R.ny - h);
-    if (!edge) {
-#pragma unroll
-        for (int j = 0; j < W; ++j)
-#pragma unroll
-            for (int i = 0; i < W; ++i) w[j * W + i] = load_word(tile + (ly + j) * CT, lx + i);
-    } else {
-        const uint8_t *img = (const uint8_t *)R.in;
-#pragma unroll
-        for (int j = 0; j < W; ++j)
-#pragma unroll
-            for (int i = 0; i < W; ++i) {
-                uint32_t word = 0;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int x = x0 + q < R.nx ? x0 + q : R.nx - 1;
-                    const int yy = y < R.ny ? y : R.ny - 1;
-                    word |= (uint32_t)img[bt_win_index(R, x, yy, i, j, h)] << (8 * q);
-                }
-                w[j * W + i] = word;
-            }
-    }
+    const int tid = threadIdx.x;
+    const int lx = (tid & 31) * 4;
     const uint32_t rank4 = 0x01010101u * (uint32_t)((W * W + 1) / 2);
-    uint32_t res = 0;
-#pragma unroll
-    for (int b = 7; b >= 0; --b) {
-        const uint32_t trial = res | (0x01010101u << b);
-        uint32_t cnt = 0;
-#pragma unroll
-        for (int k = 0; k < W * W; ++k) cnt = count_lt(cnt, w[k], trial);
-        const uint32_t below = __vcmpltu4(cnt, rank4);
-        res = (trial & below) | (res & ~below);
-    }
     const bool norm = R.in_type == IFX_N0F8;
+    for (int ly = tid >> 5; ly < kMUY; ly += blockDim.x >> 5) {
+        const int x0 = tx0 + lx, y = ty0 + ly;
+        if (x0 >= R.nx || y >= R.ny) continue;
+        uint32_t w[W * W];
+        const bool edge = R.style == IFX_CIRCULAR &&
+                          (x0 < h || x0 + 3 >= R.nx - h || y < h || y >= R.ny - h);
+        if (!edge) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const uint8_t code = (uint8_t)(res >> (8 * q));
-        bt_store(R, R.out0, x0 + q, y, norm ? __fdiv_rn((float)code, 255.0f) : (float)code);
+            for (int j = 0; j < W; ++j)
+#pragma unroll
+                for (int i = 0; i < W; ++i) w[j * W + i] = load_word(tile + (ly + j) * CT, lx + i);
+        } else {
+            const uint8_t *img = (const uint8_t *)R.in;
+#pragma unroll
+            for (int j = 0; j < W; ++j)
+#pragma unroll
+                for (int i = 0; i < W; ++i) {
+                    uint32_t word = 0;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int x = x0 + q < R.nx ? x0 + q : R.nx - 1;
+                        word |= (uint32_t)img[bt_win_index(R, x, y, i, j, h)] << (8 * q);
+                    }
+                    w[j * W + i] = word;
+                }
+        }
+        uint32_t res = 0;
+#pragma unroll
+        for (int b = 7; b >= 0; --b) {
+            const uint32_t trial = res | (0x01010101u << b);
+            uint32_t cnt = 0;
+#pragma unroll
+            for (int k = 0; k < W * W; ++k) cnt = count_lt(cnt, w[k], trial);
+            const uint32_t below = __vcmpltu4(cnt, rank4);
+            res = (trial & below) | (res & ~below);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint8_t code = (uint8_t)(res >> (8 * q));
+            bt_store(R, R.out0, x0 + q, y, norm ? __fdiv_rn((float)code, 255.0f) : (float)code);
+        }
     }
 }
 
@@ -260,57 +289,82 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, float *tile)
 {
     using SK = SortKey<float>;
     constexpr int CT = kMFX + W - 1, RT = kMFY + W - 1, h = W / 2, N = W * W;
-    const int tid = threadIdx.x;
-    gather_tile<8>(tile, RT * CT, [&](int idx) -> float {
-        const int r = idx / CT, c = idx - r * CT;
+    gather2d<float>(tile, RT, CT, CT, [&](int r, int c) -> float {
         const int mx = map_index(tx0 - h + c, R.nx, R.style);
         const int my = map_index(ty0 - h + r, R.ny, R.style);
         return (mx < 0 || my < 0) ? R.fill : ((const float *)R.in)[(long long)my * R.nx + mx];
     });
     __syncthreads();
-    const int lx = tid % kMFX, ly = tid / kMFX, x = tx0 + lx, y = ty0 + ly;
-    const bool edge = R.style == IFX_CIRCULAR && (x < h || x >= R.nx - h || y < h || y >= R.ny - h);
-    uint32_t v[N];
-    if (!edge) {
+    for (int p = threadIdx.x; p < kMFX * kMFY; p += blockDim.x) {
+        const int lx = p % kMFX, ly = p / kMFX, x = tx0 + lx, y = ty0 + ly;
+        if (x >= R.nx || y >= R.ny) continue;
+        const bool edge = R.style == IFX_CIRCULAR && (x < h || x >= R.nx - h || y < h || y >= R.ny - h);
+        uint32_t v[N];
+        if (!edge) {
 #pragma unroll
-        for (int j = 0; j < W; ++j)
+            for (int j = 0; j < W; ++j)
 #pragma unroll
-            for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(tile[(ly + j) * CT + lx + i]);
-    } else {
-        const float *img = (const float *)R.in;
-        const int xx = x < R.nx ? x : R.nx - 1, yy = y < R.ny ? y : R.ny - 1;
+                for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(tile[(ly + j) * CT + lx + i]);
+        } else {
+            const float *img = (const float *)R.in;
 #pragma unroll
-        for (int j = 0; j < W; ++j)
+            for (int j = 0; j < W; ++j)
 #pragma unroll
-            for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(img[bt_win_index(R, xx, yy, i, j, h)]);
+                for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(img[bt_win_index(R, x, y, i, j, h)]);
+        }
+        net_sort<N, uint32_t>(v);
+        bt_store(R, R.out0, x, y, SK::val(v[(N - 1) / 2]));
     }
-    net_sort<N, uint32_t>(v);
-    bt_store(R, R.out0, x, y, SK::val(v[(N - 1) / 2]));
 }
 
 // ---------------------------------------------------------------- the kernel
+constexpr int kReqTable = 2048;      // requests whose first tiles are searched in shared memory
+
 __global__ void __launch_bounds__(256)
 k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ long long s_tile;
+    __shared__ int s_base[kReqTable];
+    __shared__ __align__(16) BReq s_req;
     const BHdr *hdr = reinterpret_cast<const BHdr *>(desc);
     const BReq *reqs = reinterpret_cast<const BReq *>(desc + sizeof(BHdr));
     const long long total = hdr->total_tiles;
     const int nreq = hdr->nreq;
+    const int ntab = nreq < kReqTable ? nreq : kReqTable;
+    for (int i = threadIdx.x; i < ntab; i += blockDim.x) s_base[i] = (int)reqs[i].tile_base;
+    long long next = 0;
+    if (threadIdx.x == 0) next = (long long)atomicAdd(counter, 1ULL);
     for (;;) {
-        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(counter, 1ULL);
+        if (threadIdx.x == 0) {
+            s_tile = next;
+            next = (long long)atomicAdd(counter, 1ULL);   // in flight while this tile runs
+        }
         __syncthreads();
         const long long t = s_tile;
-        __syncthreads();
         if (t >= total) break;
-        int lo = 0, hi = nreq - 1;
+        // owning request: binary search over first tiles (shared table, then global)
+        int lo = 0, hi = ntab - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (reqs[mid].tile_base <= t) lo = mid;
+            if (s_base[mid] <= t) lo = mid;
             else hi = mid - 1;
         }
-        const BReq &R = reqs[lo];
+        if (lo == kReqTable - 1 && nreq > kReqTable) {
+            hi = nreq - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (reqs[mid].tile_base <= t) lo = mid;
+                else hi = mid - 1;
+            }
+        }
+        {   // the descriptor, one word per thread
+            const int *src = reinterpret_cast<const int *>(reqs + lo);
+            int *dst = reinterpret_cast<int *>(&s_req);
+            for (int i = threadIdx.x; i < (int)(sizeof(BReq) / 4); i += blockDim.x) dst[i] = src[i];
+        }
+        __syncthreads();
+        const BReq &R = s_req;
         const int local = (int)(t - R.tile_base);
         const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
         const int tw = bt_tile_w(R.op, R.in_type), th = bt_tile_h(R.op, R.in_type);

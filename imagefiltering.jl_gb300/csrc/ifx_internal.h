@@ -111,7 +111,9 @@ struct BatchItem {                         // one validated 2-D request, device 
 cudaError_t launch_batch(int device, const BatchItem *items, int n, cudaStream_t s, long long *tiles);
 int batch_grid(int device);
 // Validates one batched request and fills `it` (the request's own pointers).
-int request_item(const ifx_request_t &q, int index, bool need_device, BatchItem &it);
+struct DevRanges;
+int request_item(const ifx_request_t &q, int index, bool need_device, BatchItem &it,
+                 DevRanges *ranges = nullptr);
 // Sets the calling thread's ifx_last_error() message; returns code.
 int set_error(int code, const char *msg);
 
