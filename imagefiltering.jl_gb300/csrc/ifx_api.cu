@@ -325,7 +325,89 @@ static Box image_box(const ifx_array_t &a)
 }
 
 // ------------------------------------------------------------------ cascade
-struct Fac { int axis, first, len; const double *w; };
+
+// The generic pipeline: the padded box [sum first, n-1+sum last] in the
+// compute type (buffer A), then one pass per factor over the index range the
+// later passes still need, alternating between buffers B and A (the padded
+// box is no longer needed once the first pass has read it); the last pass
+// writes the output.  Every element a pass reads was written before, so the
+// buffers need no initialisation.
+static void generic_cascade_boxes(const ifx_array_t &imgd, const std::vector<Fac> &facs, Box *pad,
+                                  std::vector<Box> *outs)
+{
+    const int nd = imgd.ndim;
+    long long pfirst[IFX_MAXD] = {0, 0, 0, 0}, plast[IFX_MAXD] = {0, 0, 0, 0};
+    for (auto &f : facs) {
+        pfirst[f.axis] += f.first;
+        plast[f.axis] += f.first + f.len - 1;
+    }
+    int blo[IFX_MAXD], bsz[IFX_MAXD], slo[IFX_MAXD], shi[IFX_MAXD];
+    for (int d = 0; d < IFX_MAXD; ++d) {
+        const int n = d < nd ? (int)imgd.size[d] : 1;
+        blo[d] = d < nd ? (int)pfirst[d] : 0;
+        bsz[d] = d < nd ? (int)(n + plast[d] - pfirst[d]) : 1;
+        slo[d] = blo[d];
+        shi[d] = blo[d] + bsz[d] - 1;
+    }
+    *pad = make_box(nd, blo, bsz);
+    outs->clear();
+    for (auto &f : facs) {
+        slo[f.axis] -= f.first;
+        shi[f.axis] -= f.first + f.len - 1;
+        int olo[IFX_MAXD], osz[IFX_MAXD];
+        for (int d = 0; d < IFX_MAXD; ++d) {
+            olo[d] = slo[d];
+            osz[d] = shi[d] - slo[d] + 1;
+        }
+        outs->push_back(make_box(nd, olo, osz));
+    }
+}
+
+// Bytes of buffers A and B the generic pipeline needs.
+void generic_cascade_sizes(const ifx_array_t &imgd, const std::vector<Fac> &facs, size_t *a, size_t *b)
+{
+    const size_t cs = imgd.eltype == IFX_F64 ? 8 : 4;
+    Box pad;
+    std::vector<Box> outs;
+    generic_cascade_boxes(imgd, facs, &pad, &outs);
+    size_t na = (size_t)pad.count * cs, nb = 0;
+    for (size_t q = 0; q + 1 < outs.size(); ++q) {        // intermediate results: B, A, B, ...
+        const size_t bytes = (size_t)outs[q].count * cs;
+        if (q % 2 == 0) nb = bytes > nb ? bytes : nb;
+        else na = bytes > na ? bytes : na;
+    }
+    *a = na;
+    *b = nb;
+}
+
+int generic_cascade_run(cudaStream_t s, const ifx_array_t &imgd, const void *img,
+                        const ifx_array_t &outd, void *out, const std::vector<Fac> &facs, int style,
+                        double fill, void *bufA, void *bufB)
+{
+    const int nd = imgd.ndim;
+    const int ct = imgd.eltype == IFX_F64 ? IFX_F64 : IFX_F32;
+    int n[IFX_MAXD];
+    for (int d = 0; d < IFX_MAXD; ++d) n[d] = d < nd ? (int)imgd.size[d] : 1;
+    Box cur;
+    std::vector<Box> outs;
+    generic_cascade_boxes(imgd, facs, &cur, &outs);
+    PadBoxArgs pa{img, imgd.eltype, bufA, ct, nd, {n[0], n[1], n[2], n[3]}, cur, style, fill};
+    IFX_CUDA(launch_pad_box(pa, s));
+    const void *src = bufA;
+    for (size_t q = 0; q < facs.size(); ++q) {
+        const Fac &f = facs[q];
+        const bool last = q + 1 == facs.size();
+        void *dst = last ? out : (q % 2 == 0 ? bufB : bufA);
+        const Box db = last ? image_box(imgd) : outs[q];
+        PassBoxArgs pb{src, cur, dst, db, last ? outd.eltype : ct, outs[q], f.axis, f.first, f.len, f.w,
+                       ct == IFX_F64};
+        IFX_CUDA(launch_pass_box(pb, s));
+        src = dst;
+        cur = db;
+    }
+    return IFX_OK;
+}
+
 
 static bool is_copy(const ifx_factor_t &f)
 {
@@ -374,61 +456,13 @@ static int run_cascade(Call &c, const ifx_array_t &imgd, const void *img, const 
     }
 
     // generic: materialise the padded box in the compute type, then passes
-    long long pfirst[IFX_MAXD] = {0, 0, 0, 0}, plast[IFX_MAXD] = {0, 0, 0, 0};
-    for (auto &f : facs) {
-        pfirst[f.axis] += f.first;
-        plast[f.axis] += f.first + f.len - 1;
-    }
-    int blo[IFX_MAXD], bsz[IFX_MAXD];
-    for (int d = 0; d < IFX_MAXD; ++d) {
-        blo[d] = d < nd ? (int)pfirst[d] : 0;
-        bsz[d] = d < nd ? (int)(n[d] + plast[d] - pfirst[d]) : 1;
-    }
-    Box cur = make_box(nd, blo, bsz);
-    void *bufA, *bufB;
-    rc = slot_get(c.ctx, tmp_slot_base, (size_t)cur.count * cs, &bufA);
+    size_t need_a = 0, need_b = 0;
+    generic_cascade_sizes(imgd, facs, &need_a, &need_b);
+    void *bufA, *bufB = nullptr;
+    rc = slot_get(c.ctx, tmp_slot_base, need_a, &bufA);
     if (rc) return rc;
-    PadBoxArgs pa{img, imgd.eltype, bufA, ct, nd, {n[0], n[1], n[2], n[3]}, cur, border->style, fill};
-    IFX_CUDA(launch_pad_box(pa, c.s));
-    int slo[IFX_MAXD], shi[IFX_MAXD];
-    for (int d = 0; d < IFX_MAXD; ++d) {
-        slo[d] = blo[d];
-        shi[d] = blo[d] + bsz[d] - 1;
-    }
-    const void *src = bufA;
-    int which = 1;
-    for (size_t q = 0; q < facs.size(); ++q) {
-        const Fac &f = facs[q];
-        slo[f.axis] -= f.first;
-        shi[f.axis] -= f.first + f.len - 1;
-        int olo[IFX_MAXD], osz[IFX_MAXD];
-        for (int d = 0; d < IFX_MAXD; ++d) {
-            olo[d] = slo[d];
-            osz[d] = shi[d] - slo[d] + 1;
-        }
-        Box ob = make_box(nd, olo, osz);
-        const bool last = q + 1 == facs.size();
-        void *dst;
-        Box db;
-        int dtype;
-        if (last) {
-            dst = out;
-            db = image_box(imgd);
-            dtype = outd.eltype;
-        } else {
-            rc = slot_get(c.ctx, tmp_slot_base + which, (size_t)ob.count * cs, &bufB);
-            if (rc) return rc;
-            dst = bufB;
-            db = ob;
-            dtype = ct;
-            which = 1 - which;
-        }
-        PassBoxArgs pb{src, cur, dst, db, dtype, ob, f.axis, f.first, f.len, f.w, ct == IFX_F64};
-        IFX_CUDA(launch_pass_box(pb, c.s));
-        src = dst;
-        cur = db;
-    }
-    return IFX_OK;
+    if (need_b && (rc = slot_get(c.ctx, tmp_slot_base + 1, need_b, &bufB))) return rc;
+    return generic_cascade_run(c.s, imgd, img, outd, out, facs, border->style, fill, bufA, bufB);
 }
 
 static int check_filter_types(const ifx_array_t &img, const ifx_array_t &out)
@@ -515,6 +549,55 @@ int request_item(const ifx_request_t &q, int i, bool need_device, BatchItem &it,
 }
 
 int set_error(int code, const char *msg) { return fail(code, "%s", msg); }
+
+static int collect_factors(const ifx_array_t &img, int32_t nf, const ifx_factor_t *factors,
+                           std::vector<Fac> &facs, long long *pfirst, long long *plast)
+{
+    if (nf < 0 || (nf > 0 && !factors)) return fail(IFX_ERR_ARGUMENT, "bad factor list");
+    for (int d = 0; d < IFX_MAXD; ++d) pfirst[d] = plast[d] = 0;
+    for (int i = 0; i < nf; ++i) {
+        const ifx_factor_t &f = factors[i];
+        if (f.axis < 0 || f.axis >= img.ndim)
+            return fail(IFX_ERR_DIMENSION, "factor %d filters axis %d of a %d-dimensional image",
+                        i + 1, f.axis + 1, img.ndim);
+        if (f.length < 1 || f.length > IFX_MAX_TAPS)
+            return fail(IFX_ERR_UNSUPPORTED, "factor %d has %d taps (1..%d supported)", i + 1,
+                        f.length, IFX_MAX_TAPS);
+        if (!f.weights) return fail(IFX_ERR_ARGUMENT, "factor %d has no weights", i + 1);
+        if (f.first < -(1 << 20) || f.first > (1 << 20))
+            return fail(IFX_ERR_UNSUPPORTED, "factor offset out of range");
+        pfirst[f.axis] += f.first;
+        plast[f.axis] += f.first + f.length - 1;
+        if (!is_copy(f)) facs.push_back({f.axis, (int)f.first, f.length, f.weights});
+    }
+    return IFX_OK;
+}
+
+// Validation of ifx_imfilter_factored's arguments (shared with the
+// fixed-scratch variant): kept factors in `facs`, the fill value in the
+// compute type's domain, *nothing = true when there is no element to write.
+int factored_prepare(const ifx_array_t *out, const ifx_array_t *img, int32_t nfactors,
+                     const ifx_factor_t *factors, const ifx_border_t *border, std::vector<Fac> &facs,
+                     double *fill, bool *nothing)
+{
+    int rc;
+    *nothing = false;
+    if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
+        return rc;
+    if ((rc = check_same_axes(*out, *img)) || (rc = check_filter_types(*img, *out))) return rc;
+    long long pfirst[IFX_MAXD], plast[IFX_MAXD];
+    if ((rc = collect_factors(*img, nfactors, factors, facs, pfirst, plast))) return rc;
+    if (border->explicit_pad && (rc = check_padding(border, *img, pfirst, plast))) return rc;
+    if (numel(*img) == 0) {
+        *nothing = true;
+        return IFX_OK;
+    }
+    if ((rc = check_reflect(border, *img))) return rc;
+    const int ct = img->eltype == IFX_F64 ? IFX_F64 : IFX_F32;
+    return image_fill(border, img->eltype, ct, fill);
+}
+
+bool is_device_array(const void *p) { return is_device_ptr(p); }
 
 } // namespace ifx
 
@@ -614,43 +697,16 @@ int ifx_padarray(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
     return c.finish();
 }
 
-static int collect_factors(const ifx_array_t &img, int32_t nf, const ifx_factor_t *factors,
-                           std::vector<Fac> &facs, long long *pfirst, long long *plast)
-{
-    if (nf < 0 || (nf > 0 && !factors)) return fail(IFX_ERR_ARGUMENT, "bad factor list");
-    for (int d = 0; d < IFX_MAXD; ++d) pfirst[d] = plast[d] = 0;
-    for (int i = 0; i < nf; ++i) {
-        const ifx_factor_t &f = factors[i];
-        if (f.axis < 0 || f.axis >= img.ndim)
-            return fail(IFX_ERR_DIMENSION, "factor %d filters axis %d of a %d-dimensional image",
-                        i + 1, f.axis + 1, img.ndim);
-        if (f.length < 1 || f.length > IFX_MAX_TAPS)
-            return fail(IFX_ERR_UNSUPPORTED, "factor %d has %d taps (1..%d supported)", i + 1,
-                        f.length, IFX_MAX_TAPS);
-        if (!f.weights) return fail(IFX_ERR_ARGUMENT, "factor %d has no weights", i + 1);
-        if (f.first < -(1 << 20) || f.first > (1 << 20))
-            return fail(IFX_ERR_UNSUPPORTED, "factor offset out of range");
-        pfirst[f.axis] += f.first;
-        plast[f.axis] += f.first + f.length - 1;
-        if (!is_copy(f)) facs.push_back({f.axis, (int)f.first, f.length, f.weights});
-    }
-    return IFX_OK;
-}
 
 int ifx_imfilter_factored(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
                           int32_t nfactors, const ifx_factor_t *factors,
                           const ifx_border_t *border, void *stream)
 {
-    int rc;
-    if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
-        return rc;
-    if ((rc = check_same_axes(*out, *img)) || (rc = check_filter_types(*img, *out))) return rc;
     std::vector<Fac> facs;
-    long long pfirst[IFX_MAXD], plast[IFX_MAXD];
-    if ((rc = collect_factors(*img, nfactors, factors, facs, pfirst, plast))) return rc;
-    if (border->explicit_pad && (rc = check_padding(border, *img, pfirst, plast))) return rc;
-    if (numel(*img) == 0) return IFX_OK;
-    if ((rc = check_reflect(border, *img))) return rc;
+    double fill;
+    bool nothing;
+    int rc = factored_prepare(out, img, nfactors, factors, border, facs, &fill, &nothing);
+    if (rc || nothing) return rc;
     if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
     std::lock_guard<std::mutex> lk(ctx->mu);
     Call c;

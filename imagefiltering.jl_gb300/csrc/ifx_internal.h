@@ -3,6 +3,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <vector>
 #include "ifx_common.cuh"
 
 namespace ifx {
@@ -96,6 +97,17 @@ struct ExtremaPassArgs {                   // one separable min/max pass along `
     int want_min, want_max;
 };
 cudaError_t launch_extrema_pass(const ExtremaPassArgs &a, cudaStream_t s);
+
+// Separable cascade, generic pipeline (shared with the fixed-scratch entry) ---
+struct Fac { int axis, first, len; const double *w; };
+int factored_prepare(const ifx_array_t *out, const ifx_array_t *img, int32_t nfactors,
+                     const ifx_factor_t *factors, const ifx_border_t *border, std::vector<Fac> &facs,
+                     double *fill, bool *nothing);
+void generic_cascade_sizes(const ifx_array_t &imgd, const std::vector<Fac> &facs, size_t *a, size_t *b);
+int generic_cascade_run(cudaStream_t s, const ifx_array_t &imgd, const void *img,
+                        const ifx_array_t &outd, void *out, const std::vector<Fac> &facs, int style,
+                        double fill, void *bufA, void *bufB);
+bool is_device_array(const void *p);
 
 // Batched engine -------------------------------------------------------------
 struct BatchItem {                         // one validated 2-D request, device pointers

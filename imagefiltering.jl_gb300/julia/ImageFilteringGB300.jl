@@ -1,0 +1,172 @@
+# ImageFilteringGB300.jl -- the Julia side of the drop-in: a new algorithm tag
+# `GB300 <: ImageFiltering.Algorithm.Alg` whose backend methods `ccall` the
+# C ABI of libifx_gb300.so (include/ifx_gb300.h) instead of padding a copy and
+# running the CPU loops.
+#
+# The reference's dispatch steps 1-4 (output eltype, kernel factoring, border
+# resolution, output allocation; src/imfilter.jl:1-49, 204-254) run unchanged;
+# `default_resource(alg)` wraps the tag in CPU1(GB300()) (src/imfilter.jl:1273)
+# and the methods below, more specific than the reference's
+# `imfilter!(r::AbstractResource, ..., border::BorderSpecAny)`
+# (src/imfilter.jl:321-341), take over before any padding happens.
+#
+# Status: written against ImageFiltering.jl v0.7.12; it cannot be executed in
+# the build environment of this package (no Julia toolchain there).
+module ImageFilteringGB300
+
+using ImageFiltering, ComputationalResources, OffsetArrays, Statistics
+using ImageFiltering: ProcessedKernel, ReshapedOneD, Pad, Fill, NoPad, BorderSpecAny, iscopy
+using ImageFiltering.Algorithm: Alg
+using ImageCore: N0f8, Gray, Normed
+
+export GB300
+
+const libifx = get(ENV, "IFX_GB300_LIB", joinpath(@__DIR__, "..", "_build", "libifx_gb300.so"))
+
+"Filter on a GB300 GPU (sm_103a kernels of libifx_gb300)."
+struct GB300 <: Alg end
+
+# ---------------------------------------------------------------- C structs
+struct IfxArray
+    data::Ptr{Cvoid}
+    eltype::Int32
+    ndim::Int32
+    size::NTuple{4,Int64}
+    stride::NTuple{4,Int64}
+    first::NTuple{4,Int64}
+end
+
+struct IfxBorder
+    style::Int32
+    explicit_pad::Int32
+    lo::NTuple{4,Int64}
+    hi::NTuple{4,Int64}
+    fill_value::Float64
+end
+
+struct IfxFactor
+    axis::Int32
+    length::Int32
+    first::Int64
+    weights::Ptr{Float64}
+end
+
+const IFX_OK = 0
+eltcode(::Type{Float32}) = Int32(0)
+eltcode(::Type{Float64}) = Int32(1)
+eltcode(::Type{<:Union{N0f8,Gray{N0f8}}}) = Int32(2)
+eltcode(::Type{UInt8}) = Int32(3)
+eltcode(::Type{Int16}) = Int32(4)
+eltcode(::Type{Gray{T}}) where {T<:Union{Float32,Float64}} = eltcode(T)
+
+npre(::ReshapedOneD{T,N,Npre}) where {T,N,Npre} = Npre     # the axis a factor filters (0-based)
+
+pad4(t, v) = ntuple(d -> d <= length(t) ? Int64(t[d]) : Int64(v), 4)
+
+function ifxarray(A::AbstractArray{T,N}) where {T,N}
+    N <= 4 || throw(ArgumentError("at most 4 dimensions"))
+    P = parent(A)
+    IfxArray(Ptr{Cvoid}(pointer(P)), eltcode(T), Int32(N), pad4(size(A), 1), pad4(strides(P), 0),
+             pad4(map(first, axes(A)), 1))
+end
+
+const STYLES = Dict(:replicate => 0, :circular => 1, :symmetric => 2, :reflect => 3)
+
+function ifxborder(b::Pad{N}) where {N}
+    IfxBorder(Int32(STYLES[b.style]), Int32(N > 0), pad4(b.lo, 0), pad4(b.hi, 0), 0.0)
+end
+function ifxborder(b::Fill{T,N}, ::Type{E}) where {T,N,E}
+    v = convert(E, b.value)             # BorderArray's conversion (src/borderarray.jl:11-20)
+    IfxBorder(Int32(4), Int32(N > 0), pad4(b.lo, 0), pad4(b.hi, 0), Float64(real(v)))
+end
+ifxborder(b::Pad, ::Type) = ifxborder(b)
+
+# ---------------------------------------------------------------- context
+const CTX = Ref{Ptr{Cvoid}}(C_NULL)
+function context()
+    if CTX[] == C_NULL
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:ifx_create, libifx), Cint, (Ref{Ptr{Cvoid}}, Cint), h, 0))
+        CTX[] = h[]
+    end
+    CTX[]
+end
+
+function check(rc)
+    rc == IFX_OK && return nothing
+    msg = unsafe_string(ccall((:ifx_last_error, libifx), Cstring, ()))
+    rc == 1 && throw(ArgumentError(msg))
+    rc == 2 && throw(DimensionMismatch(msg))
+    error(msg)
+end
+
+# ---------------------------------------------------------------- imfilter!
+# Separable kernels: a tuple of ReshapedOneD (KernelFactors.*) -> ifx_imfilter_factored
+function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
+                                  kernel::Tuple{ReshapedOneD,Vararg{ReshapedOneD}},
+                                  border::Union{Pad,Fill}) where {S,T,N}
+    ws = [collect(Float64, parent(k.data)) for k in kernel]
+    facs = [IfxFactor(Int32(npre(k)), Int32(length(k.data)),
+                      Int64(first(axes(k.data, 1))), pointer(w)) for (k, w) in zip(kernel, ws)]
+    b = ifxborder(border, T)
+    GC.@preserve out img ws facs begin
+        o, i = Ref(ifxarray(out)), Ref(ifxarray(img))
+        check(ccall((:ifx_imfilter_factored, libifx), Cint,
+                    (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Int32, Ptr{IfxFactor}, Ref{IfxBorder}, Ptr{Cvoid}),
+                    context(), o, i, Int32(length(facs)), facs, b, C_NULL))
+    end
+    out
+end
+
+# Dense kernels: the (dummy, K) pair of factorkernel or a 1-tuple -> ifx_imfilter_dense
+function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
+                                  kernel::Tuple{AbstractArray,Vararg{AbstractArray}},
+                                  border::Union{Pad,Fill}) where {S,T,N}
+    ks = filter(k -> !iscopy(k), collect(kernel))
+    length(ks) == 1 || throw(ArgumentError("GB300: one dense kernel per call"))
+    K = ImageFiltering.samedims(out, ks[1])
+    Kd = collect(Float64, parent(K))
+    ksz = pad4(size(K), 1)
+    kf = pad4(map(first, axes(K)), 0)
+    GC.@preserve out img Kd begin
+        check(ccall((:ifx_imfilter_dense, libifx), Cint,
+                    (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Ptr{Float64}, Ref{NTuple{4,Int64}},
+                     Ref{NTuple{4,Int64}}, Ref{IfxBorder}, Int32, Ptr{Cvoid}),
+                    context(), Ref(ifxarray(out)), Ref(ifxarray(img)), Kd, ksz, kf,
+                    ifxborder(border, T), Int32(0), C_NULL))
+    end
+    out
+end
+
+# Laplacian stencil -> ifx_imfilter_laplacian
+function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
+                                  kernel::Tuple{ImageFiltering.Kernel.Laplacian},
+                                  border::Union{Pad,Fill}) where {S,T,N}
+    flags = pad4(map(Int32, kernel[1].flags), 0)
+    GC.@preserve out img begin
+        check(ccall((:ifx_imfilter_laplacian, libifx), Cint,
+                    (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Ref{NTuple{4,Int32}}, Ref{IfxBorder}, Ptr{Cvoid}),
+                    context(), Ref(ifxarray(out)), Ref(ifxarray(img)), map(Int32, flags),
+                    ifxborder(border, T), C_NULL))
+    end
+    out
+end
+
+# ---------------------------------------------------------------- mapwindow
+# mapwindow has no Alg hook; the entry points take the resource first.
+function ImageFiltering.mapwindow(::CPU1{GB300}, ::Union{typeof(median!),typeof(median)}, img::AbstractArray{T,N},
+                                  window::Dims{N}; border="replicate") where {T,N}
+    wf = pad4(map(w -> -(w >> 1), window), 0)
+    wl = pad4(window, 1)
+    out = similar(img, typeof(Statistics.middle(first(img))))
+    b = border isa AbstractString ? ImageFiltering.borderinstance(border) : border
+    GC.@preserve out img begin
+        check(ccall((:ifx_mapwindow_median, libifx), Cint,
+                    (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Ref{NTuple{4,Int64}}, Ref{NTuple{4,Int64}},
+                     Ref{IfxBorder}, Ptr{Cvoid}),
+                    context(), Ref(ifxarray(out)), Ref(ifxarray(img)), wf, wl, ifxborder(b, T), C_NULL))
+    end
+    out
+end
+
+end # module
