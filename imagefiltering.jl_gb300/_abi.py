@@ -88,7 +88,7 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_imfilter_laplacian", "ifx_imgradients", "ifx_mapwindow_median",
            "ifx_mapwindow_extrema", "ifx_batch_run", "ifx_server_create", "ifx_server_submit",
            "ifx_server_wait", "ifx_server_drain", "ifx_server_metrics", "ifx_server_reset_metrics",
-           "ifx_server_destroy"]
+           "ifx_server_destroy", "ifx_noalloc_scratch_bytes", "ifx_imfilter_factored_noalloc"]
 
 _lib = None
 _lock = threading.Lock()
@@ -134,6 +134,9 @@ def load(path: str = LIB_PATH):
         lib.ifx_server_metrics.argtypes = [vp, P(IfxServerMetrics)]
         lib.ifx_server_reset_metrics.argtypes = [vp]
         lib.ifx_server_destroy.argtypes = [vp]
+        lib.ifx_noalloc_scratch_bytes.restype = C.c_uint64
+        lib.ifx_imfilter_factored_noalloc.argtypes = [P(IfxArray), P(IfxArray), C.c_int32, P(IfxFactor),
+                                                      P(IfxBorder), vp]
         for name in SYMBOLS:
             getattr(lib, name)          # every declared entry point must be exported
         _lib = lib

@@ -171,6 +171,25 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
                           const int64_t *wfirst, const int64_t *wlen,
                           const ifx_border_t *border, int32_t which, void *stream);
 
+/* ---- separable cascade without allocation ------------------------------------
+ * No counterpart in the reference: an allocation-free form of
+ * ifx_imfilter_factored for callers that cannot allocate device memory on
+ * the filtering path (a real-time frame loop that must not stall on
+ * cudaMalloc/cudaFree, which can synchronize the device; an application that
+ * reserves its whole device-memory budget at start-up).  Same results and
+ * arguments as ifx_imfilter_factored without the context; arrays must be
+ * device memory of the current device; work is enqueued on `stream`.
+ * Its intermediate buffers live in one fixed device array of
+ * ifx_noalloc_scratch_bytes() bytes (32 MiB) compiled into the library, held
+ * by every GPU that loads the library until exit; a filter needing more is
+ * rejected with IFX_ERR_NOMEM.  The first call on a device looks up that
+ * array's address (make it before any stream capture starts).  All calls share
+ * the array: calls that overlap on the GPU race. */
+uint64_t ifx_noalloc_scratch_bytes(void);
+int ifx_imfilter_factored_noalloc(ifx_array_t *out, const ifx_array_t *img, int32_t nfactors,
+                                  const ifx_factor_t *factors, const ifx_border_t *border,
+                                  void *stream);
+
 /* ---- batched engine: many 2-D requests in one persistent launch --------------
  * The requests of a batch are cut into output tiles that resident CTAs take
  * from one device work-queue; a CUDA graph replays the descriptor upload and
