@@ -227,17 +227,18 @@ def run_stream(args, ifx, torch, rank):
     out_bytes = max(sum(r.out_bytes() + 256 * len(r.out_kinds()) for r in w) for w in waves(reqs))
     out_arena = torch.empty(out_bytes + 4096, dtype=torch.uint8, device=dev)
     prepared = []
+    from imagefiltering_gb300 import batch as B
     for w in waves(reqs):
         ins = make_inputs(w)
         calls, keep, _ = stream_calls(ifx, w, ins, out_arena, torch)
         bt, arr = batch_for_wave(ifx, w, ins, out_arena)
-        prepared.append((w, ins, calls, keep, bt, arr))
+        prepared.append((w, ins, calls, keep, bt, arr, B.Plan(bt)))
     torch.cuda.synchronize()
     warm_p, timed_p = prepared[:args.warmup], prepared[args.warmup:]
     stream = torch.cuda.current_stream().cuda_stream
     tiles = C.c_int64()
 
-    host_s = [0.0]
+    host_s = {"batched": 0.0, "batch_run": 0.0}
 
     def timed_region(mode, record_calls):
         ev = []
@@ -249,14 +250,17 @@ def run_stream(args, ifx, torch, rank):
             t0 = torch.cuda.Event(enable_timing=True)
             t1 = torch.cuda.Event(enable_timing=True)
             t0.record()
-            for w, ins, calls, keep, bt, arr in timed_p:
-                if mode == "batched":
+            for w, ins, calls, keep, bt, arr, plan in timed_p:
+                if mode in ("batched", "batch_run"):
                     e0 = torch.cuda.Event(enable_timing=True)
                     e1 = torch.cuda.Event(enable_timing=True)
                     e0.record()
                     h0 = time.perf_counter()
-                    rc = ctx.lib.ifx_batch_run(ctx.handle, arr, len(w), C.byref(tiles), stream)
-                    host_s[0] += time.perf_counter() - h0
+                    if mode == "batched":
+                        rc = ctx.lib.ifx_batch_plan_launch(plan.handle, C.byref(tiles), stream)
+                    else:
+                        rc = ctx.lib.ifx_batch_run(ctx.handle, arr, len(w), C.byref(tiles), stream)
+                    host_s[mode] += time.perf_counter() - h0
                     e1.record()
                     if rc:
                         A.check(rc)
@@ -278,12 +282,14 @@ def run_stream(args, ifx, torch, rank):
         return t0.elapsed_time(t1), ifx.launch_count() - launches0, ev, clk.summary()
 
     # warm-up both modes
-    for w, ins, calls, keep, bt, arr in warm_p:
+    for w, ins, calls, keep, bt, arr, plan in warm_p:
         for op, fn, a in calls:
             A.check(fn(*a))
         A.check(ctx.lib.ifx_batch_run(ctx.handle, arr, len(w), C.byref(tiles), stream))
+        A.check(ctx.lib.ifx_batch_plan_launch(plan.handle, C.byref(tiles), stream))
     torch.cuda.synchronize()
     plain_ms, _, plain_ev, _ = timed_region("plain", True)
+    run_ms, _, _, _ = timed_region("batch_run", False)
     batch_ms, launches, batch_ev, clocks = timed_region("batched", False)
     per_op = {}
     for op, rs, e0, e1 in plain_ev:
@@ -298,8 +304,9 @@ def run_stream(args, ifx, torch, rank):
         bk[1] += sum(alg_bytes(r) for r in rs)
         bk[2] += 1
     pixels = sum(r.pixels for r in timed)
-    return {"pixels": pixels, "dev_ms": batch_ms, "plain_ms": plain_ms, "launches": launches,
-            "host_ms_per_step": host_s[0] * 1e3 / max(len(timed_p), 1),
+    return {"pixels": pixels, "dev_ms": batch_ms, "plain_ms": plain_ms, "run_ms": run_ms,
+            "launches": launches,
+            "host_ms_per_step": {k: v * 1e3 / max(len(timed_p), 1) for k, v in host_s.items()},
             "per_op": per_op, "batch_kernel": bk, "clocks": clocks, "reqs": timed}
 
 
@@ -525,8 +532,8 @@ def main():
         "config": {"workload": "mixed 2-D filter stream (seed 5): sides log-U[64,4096], aspect 1:4-4:1, "
                                "F32/N0f8, Gaussian/Sobel/Laplacian/median3-5, Pad styles",
                    "requests_per_step": args.per_step,
-                   "mode": "batched: one persistent launch per step over a tile work-queue "
-                           "(CUDA graph), device-resident inputs",
+                   "mode": "batched: one persistent launch per step over a tile work-queue, "
+                           "replayed from a validated plan (CUDA graph), device-resident inputs",
                    "l2": "inputs larger than L2 (each step ~%.1f GB)" %
                    (sum(alg_bytes(r) for r in res["reqs"]) / args.steps / 1e9),
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
@@ -534,6 +541,9 @@ def main():
                       "mode": "one C-ABI call per request (device-resident)",
                       "per_op_ms": {k: round(v[0], 3) for k, v in per_op.items()}},
         "batched_over_plain": value / plain_value,
+        "batch_run_per_call_validation": {
+            "value": res["pixels"] * ws / (res["run_ms"] / 1e3) / 1e6, "unit": "Mpixel/s",
+            "mode": "ifx_batch_run: requests validated on every launch (pointer queries per array)"},
         "host_ms_per_step": res["host_ms_per_step"],
         "e2e": e2e,
         "gpu_launches": res["launches"],

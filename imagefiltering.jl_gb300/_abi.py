@@ -86,7 +86,8 @@ class IfxServerMetrics(C.Structure):
 SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "ifx_launch_count",
            "ifx_synchronize", "ifx_padarray", "ifx_imfilter_factored", "ifx_imfilter_dense",
            "ifx_imfilter_laplacian", "ifx_imgradients", "ifx_mapwindow_median",
-           "ifx_mapwindow_extrema", "ifx_batch_run", "ifx_server_create", "ifx_server_submit",
+           "ifx_mapwindow_extrema", "ifx_batch_run", "ifx_batch_plan_create", "ifx_batch_plan_launch",
+           "ifx_batch_plan_destroy", "ifx_server_create", "ifx_server_submit",
            "ifx_server_wait", "ifx_server_drain", "ifx_server_metrics", "ifx_server_reset_metrics",
            "ifx_server_destroy", "ifx_noalloc_scratch_bytes", "ifx_imfilter_factored_noalloc"]
 
@@ -127,6 +128,9 @@ def load(path: str = LIB_PATH):
         lib.ifx_mapwindow_extrema.argtypes = [vp, P(IfxArray), P(IfxArray), P(C.c_int64),
                                               P(C.c_int64), P(IfxBorder), C.c_int32, vp]
         lib.ifx_batch_run.argtypes = [vp, P(IfxRequest), C.c_int32, P(C.c_int64), vp]
+        lib.ifx_batch_plan_create.argtypes = [vp, P(IfxRequest), C.c_int32, P(vp)]
+        lib.ifx_batch_plan_launch.argtypes = [vp, P(C.c_int64), vp]
+        lib.ifx_batch_plan_destroy.argtypes = [vp]
         lib.ifx_server_create.argtypes = [vp, P(IfxServerConfig), P(vp)]
         lib.ifx_server_submit.argtypes = [vp, P(IfxRequest), P(C.c_uint64)]
         lib.ifx_server_wait.argtypes = [vp, C.c_uint64, C.c_double, P(C.c_int32)]

@@ -98,6 +98,37 @@ class Batch:
         return tiles.value
 
 
+class Plan:
+    """A batch validated once (ifx_batch_plan_create); launch() replays it."""
+
+    def __init__(self, batch):
+        self.batch = batch
+        self.ctx = _abi.context()
+        self._arr = (_abi.IfxRequest * max(1, len(batch.reqs)))(*batch.reqs)
+        h = C.c_void_p()
+        _abi.check(self.ctx.lib.ifx_batch_plan_create(self.ctx.handle, self._arr, len(batch.reqs),
+                                                      C.byref(h)))
+        self.handle = h
+
+    def launch(self, stream=None):
+        tiles = C.c_int64()
+        if stream is None:
+            stream = stream_for(*[k for k in self.batch._keep if isinstance(k, DeviceArray)])
+        _abi.check(self.ctx.lib.ifx_batch_plan_launch(self.handle, C.byref(tiles), stream))
+        return tiles.value
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.ifx_batch_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def outputs_for(op, img):
     """Device outputs with the eltypes the reference returns."""
     kinds = out_kinds(op)

@@ -1076,4 +1076,48 @@ int ifx_batch_run(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n, int6
     return IFX_OK;
 }
 
+struct ifx_batch_plan {
+    int device;
+    void *impl;
+};
+
+int ifx_batch_plan_create(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n,
+                          ifx_batch_plan_t **plan)
+{
+    if (!plan) return fail(IFX_ERR_ARGUMENT, "plan is NULL");
+    *plan = nullptr;
+    if (n < 0 || (n > 0 && !reqs)) return fail(IFX_ERR_ARGUMENT, "bad request list");
+    std::vector<BatchItem> items((size_t)n);
+    DevRanges ranges;
+    for (int i = 0; i < n; ++i) {
+        int rc = request_item(reqs[i], i, true, items[i], &ranges);
+        if (rc) return rc;
+    }
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    IFX_CUDA(cudaSetDevice(ctx->device));
+    void *impl = nullptr;
+    IFX_CUDA(plan_create(ctx->device, items.data(), n, &impl));
+    *plan = new ifx_batch_plan{ctx->device, impl};
+    return IFX_OK;
+}
+
+int ifx_batch_plan_launch(ifx_batch_plan_t *plan, int64_t *tiles, void *stream)
+{
+    if (!plan) return fail(IFX_ERR_ARGUMENT, "plan is NULL");
+    long long t = 0;
+    IFX_CUDA(plan_launch(plan->impl, (cudaStream_t)stream, &t));
+    if (tiles) *tiles = t;
+    return IFX_OK;
+}
+
+int ifx_batch_plan_destroy(ifx_batch_plan_t *plan)
+{
+    if (!plan) return IFX_OK;
+    cudaSetDevice(plan->device);
+    plan_destroy(plan->impl);
+    delete plan;
+    return IFX_OK;
+}
+
 } // extern "C"

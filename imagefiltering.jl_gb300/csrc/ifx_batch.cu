@@ -542,4 +542,75 @@ cudaError_t launch_batch(int device, const BatchItem *items, int n, cudaStream_t
     return cudaEventRecord(S.done, s);
 }
 
+// ---------------------------------------------------------------- plans
+// A validated batch whose descriptors stay in device memory: each launch is one
+// graph replay (counter reset + persistent kernel), with no host-side work.
+struct BatchPlanImpl {
+    int device = 0;
+    unsigned char *dev = nullptr;
+    unsigned long long *counter = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long tiles = 0;
+    int n = 0;
+};
+
+cudaError_t plan_create(int device, const BatchItem *items, int n, void **out)
+{
+    BatchEngine *E;
+    cudaError_t e = engine_for(device, &E);
+    if (e != cudaSuccess) return e;
+    auto *P = new BatchPlanImpl();
+    P->device = device;
+    P->n = n;
+    std::vector<BReq> reqs;
+    P->tiles = batch_describe(items, n, reqs);
+    const size_t bytes = sizeof(BHdr) + (size_t)n * sizeof(BReq);
+    std::vector<unsigned char> host(bytes);
+    BHdr h{n, 0, P->tiles};
+    memcpy(host.data(), &h, sizeof h);
+    if (n) memcpy(host.data() + sizeof(BHdr), reqs.data(), (size_t)n * sizeof(BReq));
+    if ((e = cudaMalloc(&P->dev, bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&P->counter, sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMemcpy(P->dev, host.data(), bytes, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        plan_destroy(P);
+        return e;
+    }
+    std::lock_guard<std::mutex> lk(E->mu);
+    if ((e = cudaStreamBeginCapture(E->capture, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+        plan_destroy(P);
+        return e;
+    }
+    cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), E->capture);
+    k_batch<<<E->grid, 256, kBatchSmem, E->capture>>>(P->dev, P->counter);
+    if ((e = cudaStreamEndCapture(E->capture, &P->graph)) != cudaSuccess ||
+        (e = cudaGraphInstantiate(&P->exec, P->graph, 0)) != cudaSuccess) {
+        plan_destroy(P);
+        return e;
+    }
+    *out = P;
+    return cudaSuccess;
+}
+
+cudaError_t plan_launch(void *plan, cudaStream_t s, long long *tiles)
+{
+    auto *P = (BatchPlanImpl *)plan;
+    if (tiles) *tiles = P->tiles;
+    if (P->tiles == 0) return cudaSuccess;
+    cudaError_t e = cudaGraphLaunch(P->exec, s);
+    if (e == cudaSuccess) note_launch();
+    return e;
+}
+
+void plan_destroy(void *plan)
+{
+    auto *P = (BatchPlanImpl *)plan;
+    if (!P) return;
+    if (P->exec) cudaGraphExecDestroy(P->exec);
+    if (P->graph) cudaGraphDestroy(P->graph);
+    if (P->dev) cudaFree(P->dev);
+    if (P->counter) cudaFree(P->counter);
+    delete P;
+}
+
 } // namespace ifx

@@ -122,6 +122,9 @@ struct BatchItem {                         // one validated 2-D request, device 
 };
 cudaError_t launch_batch(int device, const BatchItem *items, int n, cudaStream_t s, long long *tiles);
 int batch_grid(int device);
+cudaError_t plan_create(int device, const BatchItem *items, int n, void **plan);
+cudaError_t plan_launch(void *plan, cudaStream_t s, long long *tiles);
+void plan_destroy(void *plan);
 // Validates one batched request and fills `it` (the request's own pointers).
 struct DevRanges;
 int request_item(const ifx_request_t &q, int index, bool need_device, BatchItem &it,

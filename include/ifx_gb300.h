@@ -225,6 +225,17 @@ typedef struct ifx_request {
 int ifx_batch_run(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n, int64_t *tiles,
                   void *stream);
 
+/* A batch validated once, with its descriptors kept in device memory, for
+ * workloads that run the same requests (the same arrays, new contents) many
+ * times.  Each launch is one CUDA graph replay on `stream`.  Launches of one
+ * plan must not overlap on the device (they share its tile counter); the
+ * arrays must outlive the plan. */
+typedef struct ifx_batch_plan ifx_batch_plan_t;
+int ifx_batch_plan_create(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n,
+                          ifx_batch_plan_t **plan);
+int ifx_batch_plan_launch(ifx_batch_plan_t *plan, int64_t *tiles, void *stream);
+int ifx_batch_plan_destroy(ifx_batch_plan_t *plan);
+
 /* ---- serving: continuous batching of requests as they arrive ---------------
  * ifx_server_submit returns at once with a ticket.  An engine thread admits
  * queued requests in arrival order while the device bytes they need (staged

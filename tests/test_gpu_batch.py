@@ -139,3 +139,34 @@ def test_batch_rejects_host_memory(gpu_ifx):
     bt.add(("laplacian",), img, [out])
     with pytest.raises(ifx.ArgumentError, match="device memory"):
         bt.run()
+
+
+def test_plan_replays_match_batch_run(gpu_ifx):
+    """A validated plan launched twice gives the batch results both times."""
+    ifx = gpu_ifx
+    import torch
+    from imagefiltering_gb300 import batch as B
+    items = mixed_requests(ifx, seed=5, n=20)
+    bt = B.Batch()
+    outs = []
+    for img, op, border in items:
+        d = ifx.DeviceArray.from_host(img)
+        o = B.outputs_for(op, d)
+        bt.add(op, d, o, border)
+        outs.append(o)
+    torch.cuda.synchronize()
+    bt.run()
+    torch.cuda.synchronize()
+    first = [[x.numpy() for x in o] for o in outs]
+    plan = B.Plan(bt)
+    for _ in range(2):
+        for o in outs:
+            for x in o:
+                x.tensor.zero_()
+        plan.launch()
+        torch.cuda.synchronize()
+        again = [[x.numpy() for x in o] for o in outs]
+        for a, b in zip(first, again):
+            for u, v in zip(a, b):
+                assert np.array_equal(u, v)
+    plan.close()
