@@ -46,6 +46,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--e2e-requests", type=int, default=1000)
     p.add_argument("--hbm-cap-gb", type=int, default=150)
+    p.add_argument("--no-dense", action="store_true")
     return p.parse_args()
 
 
@@ -433,6 +434,70 @@ def call_single(ifx, r, q):
                                          C.byref(q.border), None))
 
 
+def run_dense4096(args, ifx, torch):
+    """Dense non-separable FIR on 4096x4096 Float32 (uniform [0,1), seed 2):
+    N(0,1) kernels normalised to sum 1 (seeds 20-22), 5x5 / 15x15 / 31x31,
+    Pad(:reflect) and Fill(0), on CUDA cores and on tcgen05 tensor cores.
+    Error: normwise against the FP64 oracle on a 384x384 crop interior (pixels
+    whose window lies inside the crop, so the crop border does not matter)."""
+    import ctypes as C
+    from oracle import oracle as O
+    A = ifx._abi
+    ctx = A.context()
+    n = 4096
+    g = torch.Generator(device="cuda")
+    g.manual_seed(2)
+    img_t = torch.rand((n, n), device="cuda", generator=g, dtype=torch.float32)
+    img = ifx.DeviceArray(img_t.t(), "F32")
+    out = ifx.DeviceArray.empty((n, n), "F64")
+    host_img = None
+    res = {}
+    stream = torch.cuda.current_stream().cuda_stream
+    for k, seed in ((5, 20), (15, 21), (31, 22)):
+        rng = np.random.default_rng(seed)
+        while True:
+            K = rng.standard_normal((k, k))
+            if abs(K.sum()) >= 0.1:
+                break
+        K = np.asfortranarray(K / K.sum())
+        ksz = (C.c_int64 * 4)(k, k)
+        kf = (C.c_int64 * 4)(-(k // 2), -(k // 2))
+        for style in ("reflect", "fill"):
+            b = A.border_struct(style)
+            for method, name in ((1, "cuda_cores"), (2, "tensor_cores")):
+                if method == 2 and k < 11:
+                    continue
+                call = lambda: A.check(ctx.lib.ifx_imfilter_dense(
+                    ctx.handle, A.describe(out.ptr(), "F64", (n, n), out.strides()),
+                    A.describe(img.ptr(), "F32", (n, n), img.strides()), A.dptr(K), ksz, kf, b, method,
+                    stream))
+                for _ in range(2):
+                    call()
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                reps = 5
+                e0.record()
+                for _ in range(reps):
+                    call()
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                if host_img is None:
+                    host_img = img.numpy()
+                c0, cn = 1000, 384
+                crop = np.asfortranarray(host_img[c0:c0 + cn, c0:c0 + cn].astype(np.float64))
+                ref = O.imfilter_dense(crop, K, (-(k // 2), -(k // 2)), "replicate")
+                h = k // 2
+                got = out.numpy()[c0:c0 + cn, c0:c0 + cn]
+                inner = (slice(h, cn - h), slice(h, cn - h))
+                err = float(np.max(np.abs(got[inner] - ref[inner])) / np.max(np.abs(ref[inner])))
+                res["%dx%d_%s_%s" % (k, k, style, name)] = {
+                    "ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6,
+                    "tflops": 2 * k * k * n * n / (ms / 1e3) / 1e12, "normwise_err": err}
+    return res
+
+
 def cpu_stream_baseline(args, seconds, threads):
     """The oracle port (restatement of the reference loops) on a bounded sample
     of the stream, all host threads for the separable passes."""
@@ -519,6 +584,7 @@ def main():
     achieved = bk_bytes / (bk_ms / 1e3) / 1e9
     plain_value = res["pixels"] * ws / (res["plain_ms"] / 1e3) / 1e6
     e2e = run_stream_e2e(args, ifx, torch, res["reqs"])
+    dense = run_dense4096(args, ifx, torch) if not args.no_dense else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_stream_baseline(args, args.cpu_seconds, threads)
@@ -552,6 +618,7 @@ def main():
                      "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": None,
                      "launches": bk_n, "alg_bytes_per_launch": bk_bytes / max(bk_n, 1)},
         "clocks": res["clocks"],
+        "dense_4096": dense,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))

@@ -741,8 +741,10 @@ int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *
     if (border->explicit_pad && (rc = check_padding(border, *img, pfirst, plast))) return rc;
     if (numel(*img) == 0) return IFX_OK;
     if ((rc = check_reflect(border, *img))) return rc;
-    if (method == 2)
-        return fail(IFX_ERR_UNSUPPORTED, "the tensor-core dense path is not built in this library");
+    const bool tc_ok = nd <= 2 && dense_tc_supported(img->eltype, (int)ksize[0], nd > 1 ? (int)ksize[1] : 1);
+    if (method == 2 && !tc_ok)
+        return fail(IFX_ERR_UNSUPPORTED, "the tensor-core path takes 2-D Float32/8-bit images and "
+                    "kernels up to 33 wide and 40 tall");
     if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
     std::lock_guard<std::mutex> lk(ctx->mu);
     Call c;
@@ -755,6 +757,16 @@ int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *
     if ((rc = image_fill(border, img->eltype, ct, &fill))) return rc;
     int n[IFX_MAXD];
     for (int d = 0; d < IFX_MAXD; ++d) n[d] = d < nd ? (int)img->size[d] : 1;
+    if (method == 2) {
+        Dense2dArgs a{din, img->eltype, dout, out->eltype, n[0], nd > 1 ? n[1] : 1,
+                      (int)kfirst[0], (int)ksize[0], nd > 1 ? (int)kfirst[1] : 0,
+                      nd > 1 ? (int)ksize[1] : 1, kernel, border->style, fill, 0};
+        IFX_CUDA(launch_dense_tc(a, c.s, ctx->device));
+        if ((rc = c.finish())) return rc;
+        if (c.host && dense_tc_check_error(ctx->device))
+            return fail(IFX_ERR_TIMEOUT, "tensor-core kernel: a bounded wait ran out");
+        return IFX_OK;
+    }
     if (nd <= 2 && dense2d_smem_bytes((int)ksize[0], nd > 1 ? (int)ksize[1] : 1, ct == IFX_F64) <=
                        200 * 1024) {
         Dense2dArgs a{din, img->eltype, dout, out->eltype, n[0], nd > 1 ? n[1] : 1,

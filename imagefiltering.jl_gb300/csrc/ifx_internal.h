@@ -57,6 +57,10 @@ struct Dense2dArgs {
     int compute_f64;
 };
 cudaError_t launch_dense2d(const Dense2dArgs &a, cudaStream_t s);
+// tcgen05 tensor-core path (2-D, kernels up to 33 wide and 40 tall)
+bool dense_tc_supported(int in_type, int kw, int kh);
+cudaError_t launch_dense_tc(const Dense2dArgs &a, cudaStream_t s, int device);
+int dense_tc_check_error(int device);
 
 struct DenseBoxArgs {                      // N-d dense over a padded compute-type box
     const void *src; Box sbox;

@@ -390,3 +390,46 @@ def test_launch_counter_counts_kernels(gpu_ifx):
     before = ifx.launch_count()
     ifx.imfilter(np.asfortranarray(np.ones((40, 40), np.float32)), ifx.KernelFactors.gaussian((1, 1)))
     assert ifx.launch_count() == before + 1          # one fused tile kernel
+
+
+# --------------------------------------------------------------------- dense on tensor cores
+@pytest.mark.parametrize("ksz,seed", [(11, 5), (15, 21), (31, 22)])
+@pytest.mark.parametrize("style", ["reflect", "fill", "circular"])
+def test_dense_tensor_cores(gpu_ifx, oracle, ksz, seed, style):
+    """tcgen05 implicit GEMM (BF16 hi/lo split, three products, FP32 accumulation)
+    within 1e-5 normwise of the FP64 oracle."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(seed)
+    while True:
+        K = rng.standard_normal((ksz, ksz))
+        if abs(K.sum()) >= 0.1:
+            break
+    K = K / K.sum()
+    img = np.asfortranarray(np.random.default_rng(2).random((301, 257), dtype=np.float32))
+    kern = ifx.centered(K)
+    b = ifx.Fill(0) if style == "fill" else ifx.Pad(style)
+    got = ifx.imfilter(img, kern, b, ifx.Algorithm.GB300("tensor_cores"))
+    ref = oracle.imfilter_dense(img.astype(np.float64), K, kern.first, style, 0.0)
+    assert got.dtype == np.float64
+    assert normwise(got, ref) <= 1e-5
+
+
+def test_dense_tensor_cores_shapes(gpu_ifx, oracle):
+    """Rectangular and off-centre kernels, 8-bit input, image edges not multiples
+    of the 128 x 32 tile."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(7)
+    for (kw, kh, f), shape in [((13, 21, (-3, -17)), (517, 130)), ((33, 40, (-16, -20)), (129, 33)),
+                               ((11, 11, (0, 0)), (31, 300))]:
+        K = rng.standard_normal((kw, kh)) / (kw * kh)
+        img = np.asfortranarray(rng.random(shape, dtype=np.float32))
+        k = (ifx.OffsetKernel(K, f),)
+        got = ifx.imfilter(img, k, "symmetric", ifx.Algorithm.GB300("tensor_cores"))
+        ref = oracle.imfilter_dense(img.astype(np.float64), K, f, "symmetric")
+        assert normwise(got, ref) <= 1e-5, (kw, kh, shape)
+    codes = np.asfortranarray(rng.integers(0, 256, (200, 90), dtype=np.uint8))
+    K = rng.standard_normal((15, 15))
+    K /= K.sum()
+    got = ifx.imfilter(ifx.n0f8(codes), ifx.centered(K), "replicate", ifx.Algorithm.GB300("tensor_cores"))
+    ref = oracle.imfilter_dense(codes.astype(np.float64) / 255.0, K, (-7, -7), "replicate")
+    assert normwise(got, ref) <= 1e-5
