@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--e2e-requests", type=int, default=1000)
     p.add_argument("--hbm-cap-gb", type=int, default=150)
     p.add_argument("--no-dense", action="store_true")
+    p.add_argument("--only", default=None, choices=[None, "dense"],
+                   help="run only one secondary section (small device footprint, for profiling)")
     return p.parse_args()
 
 
@@ -571,6 +573,9 @@ def main():
     g.build()
     ifx = g.load_package()
     ifx._abi.context()
+    if args.only == "dense":
+        print(json.dumps({"dense_4096": run_dense4096(args, ifx, torch)}))
+        return 0
     res = run_stream(args, ifx, torch, rank)
     dev_ms = res["dev_ms"]
     if ws > 1:

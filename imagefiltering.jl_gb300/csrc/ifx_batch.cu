@@ -119,6 +119,50 @@ __device__ __forceinline__ void gather2d(T *dst, int rows, int cols, int pitch, 
     }
 }
 
+// N0f8 codes as Float32 (c/255 correctly rounded), one table per CTA.
+__shared__ float s_n0f8[256];
+
+// Gather the (rows x cols) float tile whose element (r, c) is the image value
+// at (ox + c, oy + r) through the border map; columns >= cv are zero.  Tiles
+// whose source box lies inside the image skip the map; the element type
+// branch is taken once per tile.
+__device__ __forceinline__ void bt_gather_f(const BReq &R, float *T, int rows, int cols, int pitch,
+                                            int cv, int ox, int oy)
+{
+    const bool inside = ox >= 0 && oy >= 0 && ox + cv <= R.nx && oy + rows <= R.ny;
+    const int nx = R.nx;
+    if (R.in_type == IFX_F32) {
+        const float *img = (const float *)R.in;
+        if (inside)
+            gather2d<float>(T, rows, cols, pitch, [&](int r, int c) -> float {
+                return c < cv ? img[(long long)(oy + r) * nx + ox + c] : 0.0f;
+            });
+        else
+            gather2d<float>(T, rows, cols, pitch, [&](int r, int c) -> float {
+                if (c >= cv) return 0.0f;
+                const int mx = map_index(ox + c, nx, R.style), my = map_index(oy + r, R.ny, R.style);
+                return (mx < 0 || my < 0) ? R.fill : img[(long long)my * nx + mx];
+            });
+    } else {
+        const uint8_t *img = (const uint8_t *)R.in;
+        const bool norm = R.in_type == IFX_N0F8;
+        if (inside)
+            gather2d<float>(T, rows, cols, pitch, [&](int r, int c) -> float {
+                if (c >= cv) return 0.0f;
+                const uint8_t v = img[(long long)(oy + r) * nx + ox + c];
+                return norm ? s_n0f8[v] : (float)v;
+            });
+        else
+            gather2d<float>(T, rows, cols, pitch, [&](int r, int c) -> float {
+                if (c >= cv) return 0.0f;
+                const int mx = map_index(ox + c, nx, R.style), my = map_index(oy + r, R.ny, R.style);
+                if (mx < 0 || my < 0) return R.fill;
+                const uint8_t v = img[(long long)my * nx + mx];
+                return norm ? s_n0f8[v] : (float)v;
+            });
+    }
+}
+
 // ---------------------------------------------------------------- factored
 __device__ void bt_factored(const BReq &R, int tx0, int ty0, float *sm)
 {
@@ -130,9 +174,7 @@ __device__ void bt_factored(const BReq &R, int tx0, int ty0, float *sm)
     const int tid = threadIdx.x, nth = blockDim.x;
     if (tid < kx) wx[tid] = R.wx[tid];
     if (tid < ky) wy[tid] = R.wy[tid];
-    gather2d<float>(T, RT, CT, CT, [&](int r, int c) -> float {
-        return c < CV ? bt_load(R, tx0 + R.fx + c, ty0 + R.fy + r) : 0.0f;
-    });
+    bt_gather_f(R, T, RT, CT, CT, CV, tx0 + R.fx, ty0 + R.fy);
     __syncthreads();
     float acc[NB];
     const int segs = TX / NB;
@@ -164,9 +206,7 @@ __device__ void bt_gradients(const BReq &R, int tx0, int ty0, float *sm)
     constexpr int TX = kFTX, TY = kFTY, NB = 8, CT = TX + 2, RT = TY + 2;
     float *T = sm;
     const int tid = threadIdx.x, nth = blockDim.x;
-    gather2d<float>(T, RT, CT, CT, [&](int r, int c) -> float {
-        return bt_load(R, tx0 - 1 + c, ty0 - 1 + r);
-    });
+    bt_gather_f(R, T, RT, CT, CT, CT, tx0 - 1, ty0 - 1);
     __syncthreads();
     const float d0 = R.wx[0], d1 = R.wx[1], d2 = R.wx[2];
     const float s0 = R.wy[0], s1 = R.wy[1], s2 = R.wy[2];
@@ -195,9 +235,7 @@ __device__ void bt_laplacian(const BReq &R, int tx0, int ty0, float *sm)
     constexpr int TX = kFTX, TY = kFTY, CT = TX + 2, RT = TY + 2;
     float *T = sm;
     const int tid = threadIdx.x, nth = blockDim.x;
-    gather2d<float>(T, RT, CT, CT, [&](int r, int c) -> float {
-        return bt_load(R, tx0 - 1 + c, ty0 - 1 + r);
-    });
+    bt_gather_f(R, T, RT, CT, CT, CT, tx0 - 1, ty0 - 1);
     __syncthreads();
     for (int it = tid; it < TX * TY; it += nth) {
         const int r = it / TX, c = it - r * TX;
@@ -320,7 +358,7 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, float *tile)
 // ---------------------------------------------------------------- the kernel
 constexpr int kReqTable = 2048;      // requests whose first tiles are searched in shared memory
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -333,6 +371,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter)
     const int nreq = hdr->nreq;
     const int ntab = nreq < kReqTable ? nreq : kReqTable;
     for (int i = threadIdx.x; i < ntab; i += blockDim.x) s_base[i] = (int)reqs[i].tile_base;
+    s_n0f8[threadIdx.x & 255] = __fdiv_rn((float)(threadIdx.x & 255), 255.0f);
     long long next = 0;
     if (threadIdx.x == 0) next = (long long)atomicAdd(counter, 1ULL);
     for (;;) {
