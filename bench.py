@@ -143,7 +143,7 @@ def stream_calls(ifx, reqs, dev_inputs, out_arena, torch):
             off += (nbytes + 255) // 256 * 256
         b = A.border_struct(r.style)
         keep += [ai, b] + outs
-        stream = torch.cuda.current_stream().cuda_stream
+        stream = ifx.arrays.torch_stream()
         if r.op == "gaussian":
             g = np.ascontiguousarray(ifx.KernelFactors.gaussian(r.sigma).data, dtype=np.float64)
             fac = (A.IfxFactor * 2)()
@@ -238,7 +238,7 @@ def run_stream(args, ifx, torch, rank):
         prepared.append((w, ins, calls, keep, bt, arr, B.Plan(bt)))
     torch.cuda.synchronize()
     warm_p, timed_p = prepared[:args.warmup], prepared[args.warmup:]
-    stream = torch.cuda.current_stream().cuda_stream
+    stream = ifx.arrays.torch_stream()
     tiles = C.c_int64()
 
     host_s = {"batched": 0.0, "batch_run": 0.0}
@@ -454,7 +454,7 @@ def run_dense4096(args, ifx, torch):
     out = ifx.DeviceArray.empty((n, n), "F64")
     host_img = None
     res = {}
-    stream = torch.cuda.current_stream().cuda_stream
+    stream = ifx.arrays.torch_stream()
     for k, seed in ((5, 20), (15, 21), (31, 22)):
         rng = np.random.default_rng(seed)
         while True:
@@ -498,6 +498,112 @@ def run_dense4096(args, ifx, torch):
                     "ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6,
                     "tflops": 2 * k * k * n * n / (ms / 1e3) / 1e12, "normwise_err": err}
     return res
+
+
+def _time(torch, fn, reps=5):
+    for _ in range(2):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_sections(args, ifx, torch, hbm_peak):
+    """The other configurations, device-resident, CUDA-event timed:
+    separable Gaussian on 4096^2 Float32 (9 and 17 taps, Float64 and Float32
+    outputs) with its HBM roofline fraction; the 256^3 x 8 volume batch
+    (Gaussian sigma=(3,3,1.5) then Sobel gradients, Pad(:symmetric)); the
+    2048^2 N0f8 rank filters (median 3/5, extrema 7/15, Pad(:symmetric))."""
+    import ctypes as C
+    A = ifx._abi
+    ctx = A.context()
+    stream = ifx.arrays.torch_stream()
+    out = {}
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1)
+
+    def desc(d):
+        return A.describe(d.ptr(), d.kind, d.shape, d.strides())
+
+    def factors(ws):
+        arr = (A.IfxFactor * len(ws))()
+        keep = []
+        for i, (ax, w) in enumerate(ws):
+            w = np.ascontiguousarray(w, dtype=np.float64)
+            keep.append(w)
+            arr[i].axis, arr[i].length, arr[i].first, arr[i].weights = ax, w.size, -(w.size // 2), A.dptr(w)
+        return arr, keep
+
+    n = 4096
+    img = ifx.DeviceArray(torch.rand((n, n), device="cuda", generator=g).t(), "F32")
+    for taps in (9, 17):
+        gk = np.asarray(ifx.KernelFactors.gaussian(2.0, taps).data)
+        arr, keep = factors([(0, gk), (1, gk)])
+        for okind, osz in (("F64", 8), ("F32", 4)):
+            o = ifx.DeviceArray.empty((n, n), okind)
+            b = A.border_struct("replicate")
+            ms = _time(torch, lambda: A.check(ctx.lib.ifx_imfilter_factored(
+                ctx.handle, desc(o), desc(img), 2, arr, C.byref(b), stream)))
+            gbs = n * n * (4 + osz) / (ms / 1e3) / 1e9
+            out["separable_4096_%dtap_%s" % (taps, okind)] = {
+                "ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6, "achieved_gbs": gbs,
+                "hbm_frac": gbs / hbm_peak}
+            del o
+    del img
+    # 256^3 x 8 volumes: Gaussian (3,3,1.5) -> Float64, then Sobel gradients of that
+    nv = 256
+    vols = [ifx.DeviceArray(torch.rand((nv, nv, nv), device="cuda", generator=g).permute(2, 1, 0), "F32")
+            for _ in range(8)]
+    gau = [ifx.DeviceArray.empty((nv, nv, nv), "F64") for _ in range(2)]
+    grads = [ifx.DeviceArray.empty((nv, nv, nv), "F64") for _ in range(3)]
+    kf = ifx.KernelFactors.gaussian((3, 3, 1.5))
+    arr, keep = factors([(f.axis, np.asarray(f.data.data)) for f in kf])
+    d, sm = ifx.KernelFactors.sobel.gradient_pair
+    d = np.ascontiguousarray(d)
+    sm = np.ascontiguousarray(sm)
+    b = A.border_struct("symmetric")
+    ext = (C.c_int32 * 4)(1, 1, 1)
+    gdesc = (A.IfxArray * 3)(*[desc(x) for x in grads])
+
+    def volume_step():
+        for i, v in enumerate(vols):
+            gv = gau[i % 2]
+            A.check(ctx.lib.ifx_imfilter_factored(ctx.handle, desc(gv), desc(v), 3, arr, C.byref(b), stream))
+            A.check(ctx.lib.ifx_imgradients(ctx.handle, gdesc, desc(gv), A.dptr(d), A.dptr(sm), 3, -1, ext,
+                                            C.byref(b), stream))
+    ms = _time(torch, volume_step, reps=2)
+    vox = 8 * nv ** 3
+    out["volume_256x8_gauss_sobel"] = {"ms": round(ms, 3), "mvox_s": vox / (ms / 1e3) / 1e6,
+                                       "note": "Gaussian on Float32 volumes (Float64 out), then "
+                                               "imgradients of the Float64 result in FP64"}
+    del vols, gau, grads
+    # rank filters on 2048^2 N0f8 with 5% salt and pepper
+    m = 2048
+    codes = torch.randint(0, 256, (m, m), device="cuda", generator=g, dtype=torch.uint8)
+    img8 = ifx.DeviceArray(codes.t(), "N0F8")
+    bsym = A.border_struct("symmetric")
+    for w in (3, 5):
+        o = ifx.DeviceArray.empty((m, m), "F32")
+        wf = (C.c_int64 * 4)(-(w // 2), -(w // 2))
+        wl = (C.c_int64 * 4)(w, w)
+        ms = _time(torch, lambda: A.check(ctx.lib.ifx_mapwindow_median(
+            ctx.handle, desc(o), desc(img8), wf, wl, C.byref(bsym), stream)))
+        out["median_2048_%dx%d" % (w, w)] = {"ms": round(ms, 4), "mpix_s": m * m / (ms / 1e3) / 1e6}
+    for w in (7, 15):
+        o = ifx.DeviceArray.empty((2, m, m), "N0F8")
+        wf = (C.c_int64 * 4)(-(w // 2), -(w // 2))
+        wl = (C.c_int64 * 4)(w, w)
+        po = A.describe(o.ptr(), "N0F8", (m, m), (1, m))
+        ms = _time(torch, lambda: A.check(ctx.lib.ifx_mapwindow_extrema(
+            ctx.handle, po, desc(img8), wf, wl, C.byref(bsym), 0, stream)))
+        out["extrema_2048_%dx%d" % (w, w)] = {"ms": round(ms, 4), "mpix_s": m * m / (ms / 1e3) / 1e6}
+    return out
 
 
 def cpu_stream_baseline(args, seconds, threads):
@@ -590,6 +696,7 @@ def main():
     plain_value = res["pixels"] * ws / (res["plain_ms"] / 1e3) / 1e6
     e2e = run_stream_e2e(args, ifx, torch, res["reqs"])
     dense = run_dense4096(args, ifx, torch) if not args.no_dense else None
+    sections = run_sections(args, ifx, torch, hbm_peak) if not args.no_dense else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_stream_baseline(args, args.cpu_seconds, threads)
@@ -624,6 +731,7 @@ def main():
                      "launches": bk_n, "alg_bytes_per_launch": bk_bytes / max(bk_n, 1)},
         "clocks": res["clocks"],
         "dense_4096": dense,
+        "configs": sections,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))

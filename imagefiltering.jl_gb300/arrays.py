@@ -123,6 +123,14 @@ def stream_for(*arrays):
     consumers), else None (the library's own stream, synchronous call)."""
     for a in arrays:
         if isinstance(a, DeviceArray):
-            import torch
-            return torch.cuda.current_stream(a.tensor.device).cuda_stream
+            return torch_stream(a.tensor.device)
     return None
+
+
+def torch_stream(device=None):
+    """torch's current stream as a handle for the C ABI.  torch reports the
+    legacy default stream as 0, which the ABI would read as "the context's
+    own stream" (not ordered with torch's work), so it becomes cudaStreamLegacy."""
+    import torch
+    h = torch.cuda.current_stream(device).cuda_stream
+    return h if h else 1          # 1 == cudaStreamLegacy

@@ -455,6 +455,16 @@ static int run_cascade(Call &c, const ifx_array_t &imgd, const void *img, const 
         }
     }
 
+    // 3-D with one factor per axis in axis order: the fused z-marching kernel
+    if (nd == 3 && ct == IFX_F32 && facs.size() == 3 && facs[0].axis == 0 && facs[1].axis == 1 &&
+        facs[2].axis == 2 &&
+        sep3d_supported(facs[0].len, facs[1].len, facs[2].len, n[0], n[1], n[2], 1)) {
+        Sep3dArgs a{img, imgd.eltype, out, outd.eltype, n[0], n[1], n[2], 1,
+                    facs[0].first, facs[0].len, facs[1].first, facs[1].len, facs[2].first, facs[2].len,
+                    facs[0].w, facs[1].w, facs[2].w, border->style, fill};
+        IFX_CUDA(launch_sep3d(a, c.s));
+        return IFX_OK;
+    }
     // generic: materialise the padded box in the compute type, then passes
     size_t need_a = 0, need_b = 0;
     generic_cascade_sizes(imgd, facs, &need_a, &need_b);

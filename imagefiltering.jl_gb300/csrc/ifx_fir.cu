@@ -325,6 +325,134 @@ cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s)
 }
 
 // =========================================================================
+// Fused 3-D separable kernel (factors along axes 0, 1, 2 in that order), FP32.
+// A CTA owns a TX x TY column of the volume and a chunk of ZC output slices.
+// It sweeps the input slices the chunk needs (ZC + kz - 1 of them): each slice
+// is gathered through the border map with its x/y halo, filtered along x over
+// the halo rows and then along y, and the TX x TY result goes into a ring of
+// kz slices in shared memory; once kz slices are in the ring, the z pass
+// writes one output slice.  The x pass runs over the y halo and the x/y passes
+// over the z halo, as pad-then-cascade does (src/imfilter.jl:385-457).
+// =========================================================================
+constexpr int k3TX = 64, k3TY = 16, k3ZC = 32, k3MaxKz = 17;
+
+struct Sep3dW { float wx[IFX_MAX_TAPS + 3], wy[IFX_MAX_TAPS + 3], wz[k3MaxKz]; };
+
+__host__ __device__ inline size_t sep3d_smem_floats(int kx, int ky, int kz)
+{
+    return (size_t)(k3TY + ky - 1) * (k3TX + up4(kx)) + (size_t)(k3TY + ky - 1) * k3TX +
+           (size_t)kz * k3TY * k3TX + 2 * (IFX_MAX_TAPS + 3) + k3MaxKz;
+}
+
+template <class Tin, class Tout>
+__global__ void __launch_bounds__(256)
+k_sep3d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny, int nz, int fx, int kx,
+        int fy, int ky, int fz, int kz, int style, float fill, bool norm,
+        const __grid_constant__ Sep3dW W)
+{
+    constexpr int TX = k3TX, TY = k3TY, NB = 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *sm = reinterpret_cast<float *>(smem_raw);
+    float *wx = sm, *wy = wx + IFX_MAX_TAPS + 3, *wz = wy + IFX_MAX_TAPS + 3;
+    const int RT = TY + ky - 1, CT = TX + up4(kx), CV = TX + kx - 1;
+    float *T = wz + k3MaxKz;
+    float *I = T + RT * CT;
+    float *ring = I + RT * TX;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    for (int t = tid; t < kx; t += nth) wx[t] = W.wx[t];
+    for (int t = tid; t < ky; t += nth) wy[t] = W.wy[t];
+    for (int t = tid; t < kz; t += nth) wz[t] = W.wz[t];
+    const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
+    const int zc = blockIdx.z % ((nz + k3ZC - 1) / k3ZC), vol = blockIdx.z / ((nz + k3ZC - 1) / k3ZC);
+    const int z0 = zc * k3ZC, z1 = min(nz, z0 + k3ZC);
+    const long long vstride = (long long)nx * ny * nz;
+    const Tin *src = img + vol * vstride;
+    Tout *dst = out + vol * vstride;
+    const long long plane = (long long)nx * ny;
+    const int s_first = z0 + fz, s_last = z1 - 1 + fz + kz - 1;
+    float acc[NB];
+    for (int s = s_first; s <= s_last; ++s) {
+        const int ms = map_index(s, nz, style);
+        __syncthreads();                       // T and I free again
+        gather_tile<8>(T, RT * CT, [&](int idx) -> float {
+            const int r = idx / CT, c = idx - r * CT;
+            if (c >= CV) return 0.0f;
+            const int mx = map_index(tx0 + fx + c, nx, style);
+            const int my = map_index(ty0 + fy + r, ny, style);
+            return (mx < 0 || my < 0 || ms < 0) ? fill
+                   : cvt<float, Tin>(src[(long long)ms * plane + (long long)my * nx + mx], norm);
+        });
+        __syncthreads();
+        const int segs = TX / NB;
+        for (int it = tid; it < RT * segs; it += nth) {
+            const int r = it / segs, c0 = (it - r * segs) * NB;
+            corr_run<float, NB>(T + r * CT + c0, 1, wx, kx, acc);
+#pragma unroll
+            for (int i = 0; i < NB; ++i) I[r * TX + c0 + i] = acc[i];
+        }
+        __syncthreads();
+        float *slot = ring + ((s - s_first) % kz) * (TY * TX);
+        for (int it = tid; it < TX * (TY / NB); it += nth) {
+            const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
+            corr_run<float, NB>(I + r0 * TX + c, TX, wy, ky, acc);
+#pragma unroll
+            for (int i = 0; i < NB; ++i) slot[(r0 + i) * TX + c] = acc[i];
+        }
+        __syncthreads();
+        const int z = s - fz - (kz - 1);       // output slice completed by this input slice
+        if (z >= z0) {
+            for (int it = tid; it < TX * TY; it += nth) {
+                const int r = it / TX, c = it - r * TX;
+                const int x = tx0 + c, y = ty0 + r;
+                float a = 0.0f;
+                for (int t = 0; t < kz; ++t)
+                    a = fmaf(wz[t], ring[((z + fz + t - s_first) % kz) * (TY * TX) + it], a);
+                if (x < nx && y < ny) dst[(long long)z * plane + (long long)y * nx + x] = (Tout)a;
+            }
+        }
+    }
+}
+
+template <class Tin, class Tout>
+static cudaError_t sep3d_t(const Sep3dArgs &a, cudaStream_t s)
+{
+    Sep3dW W;
+    memset(&W, 0, sizeof W);
+    for (int t = 0; t < a.kx; ++t) W.wx[t] = (float)a.wx[t];
+    for (int t = 0; t < a.ky; ++t) W.wy[t] = (float)a.wy[t];
+    for (int t = 0; t < a.kz; ++t) W.wz[t] = (float)a.wz[t];
+    const size_t smem = sep3d_smem_floats(a.kx, a.ky, a.kz) * sizeof(float);
+    auto kern = k_sep3d<Tin, Tout>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int zchunks = (a.nz + k3ZC - 1) / k3ZC;
+    dim3 grid((a.nx + k3TX - 1) / k3TX, (a.ny + k3TY - 1) / k3TY, zchunks * a.nvol);
+    kern<<<grid, 256, smem, s>>>((const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.nz, a.fx, a.kx, a.fy,
+                                 a.ky, a.fz, a.kz, a.style, (float)a.fill, a.in_type == IFX_N0F8, W);
+    note_launch();
+    return cudaGetLastError();
+}
+
+bool sep3d_supported(int kx, int ky, int kz, int nx, int ny, int nz, int nvol)
+{
+    const int zchunks = (nz + k3ZC - 1) / k3ZC;
+    return kz <= k3MaxKz && kx <= 64 && ky <= 64 && (ny + k3TY - 1) / k3TY <= 65535 &&
+           (long long)zchunks * nvol <= 65535 &&
+           sep3d_smem_floats(kx, ky, kz) * sizeof(float) <= 200 * 1024;
+}
+
+cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s)
+{
+    if ((long long)a.nx * a.ny * a.nz == 0 || a.nvol == 0) return cudaSuccess;
+    const int it = a.in_type, ot = a.out_type;
+    if (it == IFX_F32 && ot == IFX_F32) return sep3d_t<float, float>(a, s);
+    if (it == IFX_F32 && ot == IFX_F64) return sep3d_t<float, double>(a, s);
+    if (is8(it) && ot == IFX_F32) return sep3d_t<uint8_t, float>(a, s);
+    if (is8(it) && ot == IFX_F64) return sep3d_t<uint8_t, double>(a, s);
+    return cudaErrorInvalidValue;
+}
+
+// =========================================================================
 // Dense 2-D direct correlation on CUDA cores (src/imfilter.jl:624-669):
 // out[x,y] = sum_{i,j} A[x+fx+i, y+fy+j] K[i,j].  A TX x TY tile plus halo is
 // gathered through the border map; each thread computes 8 consecutive x

@@ -46,6 +46,18 @@ struct Sep2dArgs {
 };
 cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s);
 
+// Fused 3-D separable kernel (factors on axes 0, 1, 2 in that order; FP32) ---
+struct Sep3dArgs {
+    const void *img; int in_type;          // nvol volumes back to back
+    void *out; int out_type;
+    int nx, ny, nz, nvol;
+    int fx, kx, fy, ky, fz, kz;
+    const double *wx, *wy, *wz;
+    int style; double fill;
+};
+bool sep3d_supported(int kx, int ky, int kz, int nx, int ny, int nz, int nvol);
+cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s);
+
 // Dense --------------------------------------------------------------------
 struct Dense2dArgs {
     const void *img; int in_type;

@@ -52,7 +52,7 @@ def _run_both(ifx, img, facs, style, out_kind):
     d_b = ifx.DeviceArray.empty(img.shape, out_kind)
     arr, keep = _factors(ifx, facs)
     b = A.border_struct(style, None, None, 0.25 if style == "fill" else 0.0)
-    stream = torch.cuda.current_stream().cuda_stream
+    stream = ifx.arrays.torch_stream()
     A.check(ctx.lib.ifx_imfilter_factored_noalloc(_desc(ifx, d_a), _desc(ifx, d_in), len(facs), arr,
                                                   C.byref(b), stream))
     A.check(ctx.lib.ifx_imfilter_factored(ctx.handle, _desc(ifx, d_b), _desc(ifx, d_in), len(facs), arr,
