@@ -47,7 +47,9 @@ def parse():
     p.add_argument("--e2e-requests", type=int, default=1000)
     p.add_argument("--hbm-cap-gb", type=int, default=150)
     p.add_argument("--no-dense", action="store_true")
-    p.add_argument("--only", default=None, choices=[None, "dense"],
+    p.add_argument("--dense-ksizes", type=lambda t: [int(v) for v in t.split(",")], default=None,
+                   help="dense section: kernel sizes to run (default 5,11,15,31)")
+    p.add_argument("--only", default=None, choices=[None, "dense", "sections"],
                    help="run only one secondary section (small device footprint, for profiling)")
     return p.parse_args()
 
@@ -438,7 +440,7 @@ def call_single(ifx, r, q):
 
 def run_dense4096(args, ifx, torch):
     """Dense non-separable FIR on 4096x4096 Float32 (uniform [0,1), seed 2):
-    N(0,1) kernels normalised to sum 1 (seeds 20-22), 5x5 / 15x15 / 31x31,
+    N(0,1) kernels normalised to sum 1 (seeds 20-23), 5x5 / 11x11 / 15x15 / 31x31,
     Pad(:reflect) and Fill(0), on CUDA cores and on tcgen05 tensor cores.
     Error: normwise against the FP64 oracle on a 384x384 crop interior (pixels
     whose window lies inside the crop, so the crop border does not matter)."""
@@ -455,7 +457,9 @@ def run_dense4096(args, ifx, torch):
     host_img = None
     res = {}
     stream = ifx.arrays.torch_stream()
-    for k, seed in ((5, 20), (15, 21), (31, 22)):
+    for k, seed in ((5, 20), (11, 23), (15, 21), (31, 22)):
+        if args.dense_ksizes and k not in args.dense_ksizes:
+            continue
         rng = np.random.default_rng(seed)
         while True:
             K = rng.standard_normal((k, k))
@@ -473,18 +477,7 @@ def run_dense4096(args, ifx, torch):
                     ctx.handle, A.describe(out.ptr(), "F64", (n, n), out.strides()),
                     A.describe(img.ptr(), "F32", (n, n), img.strides()), A.dptr(K), ksz, kf, b, method,
                     stream))
-                for _ in range(2):
-                    call()
-                torch.cuda.synchronize()
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                reps = 5
-                e0.record()
-                for _ in range(reps):
-                    call()
-                e1.record()
-                torch.cuda.synchronize()
-                ms = e0.elapsed_time(e1) / reps
+                ms = _time(torch, call)
                 if host_img is None:
                     host_img = img.numpy()
                 c0, cn = 1000, 384
@@ -500,24 +493,35 @@ def run_dense4096(args, ifx, torch):
     return res
 
 
+_FLUSH = []
+
+
 def _time(torch, fn, reps=5):
+    """Mean CUDA-event time of fn() over `reps` runs; L2 is flushed (a 256 MB
+    buffer is overwritten) before every timed run, outside the events."""
+    if not _FLUSH:
+        _FLUSH.append(torch.empty(256 << 20, dtype=torch.uint8, device="cuda"))
     for _ in range(2):
         fn()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
+    total = 0.0
     for _ in range(reps):
+        _FLUSH[0].zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
         fn()
-    e1.record()
-    torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / reps
+        e1.record()
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1)
+    return total / reps
 
 
 def run_sections(args, ifx, torch, hbm_peak):
     """The other configurations, device-resident, CUDA-event timed:
-    separable Gaussian on 4096^2 Float32 (9 and 17 taps, Float64 and Float32
-    outputs) with its HBM roofline fraction; the 256^3 x 8 volume batch
+    separable Gaussian on 4096^2 Float32 and N0f8 (9 and 17 taps, Float64 and
+    Float32 outputs) with its HBM roofline fraction (algorithmic bytes: one
+    read of the image, one write of the output); the 256^3 x 8 volume batch
     (Gaussian sigma=(3,3,1.5) then Sobel gradients, Pad(:symmetric)); the
     2048^2 N0f8 rank filters (median 3/5, extrema 7/15, Pad(:symmetric))."""
     import ctypes as C
@@ -541,21 +545,25 @@ def run_sections(args, ifx, torch, hbm_peak):
         return arr, keep
 
     n = 4096
-    img = ifx.DeviceArray(torch.rand((n, n), device="cuda", generator=g).t(), "F32")
-    for taps in (9, 17):
-        gk = np.asarray(ifx.KernelFactors.gaussian(2.0, taps).data)
-        arr, keep = factors([(0, gk), (1, gk)])
-        for okind, osz in (("F64", 8), ("F32", 4)):
-            o = ifx.DeviceArray.empty((n, n), okind)
-            b = A.border_struct("replicate")
-            ms = _time(torch, lambda: A.check(ctx.lib.ifx_imfilter_factored(
-                ctx.handle, desc(o), desc(img), 2, arr, C.byref(b), stream)))
-            gbs = n * n * (4 + osz) / (ms / 1e3) / 1e9
-            out["separable_4096_%dtap_%s" % (taps, okind)] = {
-                "ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6, "achieved_gbs": gbs,
-                "hbm_frac": gbs / hbm_peak}
-            del o
-    del img
+    imgs = {"F32": ifx.DeviceArray(torch.rand((n, n), device="cuda", generator=g).t(), "F32"),
+            "N0F8": ifx.DeviceArray(torch.randint(0, 256, (n, n), device="cuda", generator=g,
+                                                  dtype=torch.uint8).t(), "N0F8")}
+    for ikind, isz in (("F32", 4), ("N0F8", 1)):
+        img = imgs[ikind]
+        for taps in (9, 17):
+            gk = np.asarray(ifx.KernelFactors.gaussian(2.0, taps).data)
+            arr, keep = factors([(0, gk), (1, gk)])
+            for okind, osz in (("F64", 8), ("F32", 4)):
+                o = ifx.DeviceArray.empty((n, n), okind)
+                b = A.border_struct("replicate")
+                ms = _time(torch, lambda: A.check(ctx.lib.ifx_imfilter_factored(
+                    ctx.handle, desc(o), desc(img), 2, arr, C.byref(b), stream)))
+                gbs = n * n * (isz + osz) / (ms / 1e3) / 1e9
+                out["separable_4096_%s_%dtap_%s" % (ikind, taps, okind)] = {
+                    "ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6, "achieved_gbs": gbs,
+                    "hbm_frac": gbs / hbm_peak}
+                del o
+    del imgs, img
     # 256^3 x 8 volumes: Gaussian (3,3,1.5) -> Float64, then Sobel gradients of that
     nv = 256
     vols = [ifx.DeviceArray(torch.rand((nv, nv, nv), device="cuda", generator=g).permute(2, 1, 0), "F32")
@@ -681,6 +689,9 @@ def main():
     ifx._abi.context()
     if args.only == "dense":
         print(json.dumps({"dense_4096": run_dense4096(args, ifx, torch)}))
+        return 0
+    if args.only == "sections":
+        print(json.dumps({"configs": run_sections(args, ifx, torch, peaks()[0])}))
         return 0
     res = run_stream(args, ifx, torch, rank)
     dev_ms = res["dev_ms"]

@@ -660,6 +660,8 @@ int ifx_synchronize(ifx_context_t *ctx, void *stream)
     if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
     IFX_CUDA(cudaSetDevice(ctx->device));
     IFX_CUDA(cudaStreamSynchronize(stream ? (cudaStream_t)stream : ctx->stream));
+    if (kernel_timeout_take(ctx->device))
+        return fail(IFX_ERR_TIMEOUT, "a kernel's bounded wait for its copies or tensor-core work ran out");
     return IFX_OK;
 }
 
@@ -773,7 +775,7 @@ int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *
                       nd > 1 ? (int)ksize[1] : 1, kernel, border->style, fill, 0};
         IFX_CUDA(launch_dense_tc(a, c.s, ctx->device));
         if ((rc = c.finish())) return rc;
-        if (c.host && dense_tc_check_error(ctx->device))
+        if (c.host && kernel_timeout_take(ctx->device))
             return fail(IFX_ERR_TIMEOUT, "tensor-core kernel: a bounded wait ran out");
         return IFX_OK;
     }

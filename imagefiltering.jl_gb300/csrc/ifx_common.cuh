@@ -68,6 +68,29 @@ template <class Tc> __device__ __forceinline__ Tc to_c(uint8_t v, bool norm)
 template <class To> __device__ __forceinline__ To from_c(float v) { return (To)v; }
 template <class To> __device__ __forceinline__ To from_c(double v) { return (To)v; }
 
+// Float32 -> Float64 widening, exact, in integer operations (the FP64 pipe of
+// this part is narrow, and every Float64 output of an FP32 computation passes
+// through here).  From the IEEE-754 binary32/binary64 formats: a normal
+// number keeps sign and mantissa (shifted up 29 bits) and its exponent is
+// rebiased by 1023 - 127 = 896; zeros keep their sign; subnormals, Inf and
+// NaN take the hardware conversion.
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    if (e == 0u || e == 0xFFu) {
+        if ((b & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+        return (double)f;
+    }
+    const uint32_t hi = (b & 0x80000000u) | (((b >> 3) & 0x0FFFFFFFu) + (896u << 20));
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+// Output store conversion from an FP32 result.
+template <class To> __device__ __forceinline__ To out_cvt(float v) { return (To)v; }
+template <> __device__ __forceinline__ double out_cvt<double>(float v) { return f32_to_f64(v); }
+template <class To> __device__ __forceinline__ To out_cvt(double v) { return (To)v; }
+
 __host__ __device__ __forceinline__ int up4(int k) { return (k + 3) & ~3; }
 
 // Dense N-d box of an index space (lo .. lo+size-1 per axis), column-major.
@@ -111,10 +134,13 @@ __device__ __forceinline__ void corr_run(const Tc *p, int step, const Tc *w, int
         v[i] = p[i * step];
         acc[i] = 0;
     }
+    v[NB + 3] = 0;
     int t0 = 0;
     for (; t0 + 4 <= k; t0 += 4) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) v[NB + j] = p[(NB + t0 + j) * step];
+        for (int j = 0; j < 3; ++j) v[NB + j] = p[(NB + t0 + j) * step];
+        // v[NB+3] first serves the next chunk: not loaded after the last one
+        if (t0 + 4 < k) v[NB + 3] = p[(NB + t0 + 3) * step];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const Tc wt = w[t0 + j];

@@ -24,6 +24,7 @@
 // Waits are bounded: an mbarrier that never completes sets *err, the CTA frees
 // its tensor memory and returns.
 #include "ifx_internal.h"
+#include "ifx_tma.cuh"
 #include <cuda_bf16.h>
 #include <cstring>
 
@@ -31,7 +32,7 @@ namespace ifx {
 
 constexpr int kTcM = 128, kTcN = 32;
 constexpr int kTcMaxKw = 33, kTcMaxKh = 40;
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256, kTcWarps = kTcThreads / 32;
 
 struct TcWeights { float w[kTcMaxKw * kTcMaxKh]; };
 
@@ -76,17 +77,124 @@ struct TcArgs {
     int *err;
 };
 
-__host__ __device__ inline size_t tc_smem_layout(int kh, int Q, int R, size_t *b_off, size_t *a_off,
-                                                 size_t *plane)
+// Shared memory: B hi | B lo | A buffer 0 (hi planes, lo planes) | A buffer 1
+// | epilogue staging (8 warps x 32 rows x 17 floats).
+struct TcLayout {
+    size_t b_bytes;             // one of B hi / B lo
+    size_t plane;               // one A plane: R rows x 16 bytes
+    size_t a_off[2];            // A buffers
+    size_t stage_off;
+    size_t total;
+};
+
+__host__ __device__ inline TcLayout tc_layout(int kh, int Q, int R)
 {
-    const size_t ncm = (size_t)Q + 3;
-    const size_t bbytes = (size_t)kh * ncm * 128;          // one of hi / lo
-    *plane = (size_t)R * 16;
-    *b_off = 0;
-    *a_off = 2 * bbytes;
-    // A hi, A lo, then 16 planes of slack so that no descriptor of this kernel
-    // can address past the allocation
-    return *a_off + (2 * (size_t)Q + 16) * *plane + 64;
+    TcLayout L;
+    L.b_bytes = (size_t)kh * (Q + 3) * 128;
+    L.plane = (size_t)R * 16;
+    L.a_off[0] = 2 * L.b_bytes;
+    L.a_off[1] = L.a_off[0] + 2 * (size_t)Q * L.plane;
+    L.stage_off = L.a_off[1] + 2 * (size_t)Q * L.plane;
+    L.total = L.stage_off + (size_t)kTcWarps * 32 * 17 * sizeof(float) + 128;
+    return L;
+}
+
+template <class Tin>
+__device__ __forceinline__ float tc_in(Tin raw, bool norm)
+{
+    if constexpr (sizeof(Tin) == 1)
+        return norm ? __fdiv_rn((float)raw, 255.0f) : (float)raw;
+    else
+        return (float)raw;
+}
+
+__device__ __forceinline__ uint32_t bf2(float lo_elem, float hi_elem)
+{
+    __nv_bfloat162 p = __floats2bfloat162_rn(lo_elem, hi_elem);
+    return *reinterpret_cast<uint32_t *>(&p);
+}
+
+// Split 8 patch values (x order) into BF16 hi and lo rows of one core-matrix
+// plane; the K index runs in reverse, so row element t holds v[7 - t].
+__device__ __forceinline__ void tc_store_chunk(uint16_t *hi_row, uint16_t *lo_row, const float v[8])
+{
+    float h[8], l[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        h[e] = __bfloat162float(__float2bfloat16_rn(v[e]));
+        l[e] = v[e] - h[e];
+    }
+    uint4 H, Lw;
+    H.x = bf2(h[7], h[6]);
+    H.y = bf2(h[5], h[4]);
+    H.z = bf2(h[3], h[2]);
+    H.w = bf2(h[1], h[0]);
+    Lw.x = bf2(l[7], l[6]);
+    Lw.y = bf2(l[5], l[4]);
+    Lw.z = bf2(l[3], l[2]);
+    Lw.w = bf2(l[1], l[0]);
+    *reinterpret_cast<uint4 *>(hi_row) = H;
+    *reinterpret_cast<uint4 *>(lo_row) = Lw;
+}
+
+// Gather the patch of tile (x0, y0) into A buffer (hi at `Ah`, lo at `Al`):
+// chunk (r, m) is patch row r, columns 8m..8m+7, stored in plane Q-1-m.
+// Columns at or past valid_c stay zero (written once at start-up).
+template <class Tin>
+__device__ __forceinline__ void tc_gather(const TcArgs &a, int x0, int y0, uint16_t *Ah, uint16_t *Al,
+                                          size_t plane_el)
+{
+    const int valid_c = kTcN + a.kw - 1, Mv = (valid_c + 7) >> 3;
+    const int R = a.R, Q = a.Q;
+    const bool norm = a.in_type == IFX_N0F8;
+    const Tin *img = (const Tin *)a.img;
+    const int px0 = x0 + a.fx, py0 = y0 + a.fy;
+    const bool interior = px0 >= 0 && px0 + valid_c <= a.nx && py0 >= 0 && py0 + R <= a.ny;
+    const int nch = R * Mv;
+    for (int base = threadIdx.x; base < nch; base += 2 * kTcThreads) {
+        float v[2][8];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int ch = base + u * kTcThreads;
+            const int r = ch / Mv, m = ch - r * Mv;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[u][e] = 0.0f;
+            if (ch < nch) {
+                const int c0 = 8 * m;
+                if (interior) {
+                    const Tin *rowp = img + (long long)(py0 + r) * a.nx + px0 + c0;
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        if (c0 + e < valid_c) v[u][e] = tc_in<Tin>(rowp[e], norm);
+                } else {
+                    const int my = map_index(py0 + r, a.ny, a.style);
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        if (c0 + e >= valid_c) continue;
+                        const int mx = map_index(px0 + c0 + e, a.nx, a.style);
+                        v[u][e] = (mx < 0 || my < 0) ? a.fill
+                                                     : tc_in<Tin>(img[(long long)my * a.nx + mx], norm);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int ch = base + u * kTcThreads;
+            if (ch >= nch) continue;
+            const int r = ch / Mv, m = ch - r * Mv;
+            const size_t o = (size_t)(Q - 1 - m) * plane_el + (size_t)r * 8;
+            tc_store_chunk(Ah + o, Al + o, v[u]);
+        }
+    }
+}
+
+__device__ __forceinline__ void tc_fence_sync()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
 template <class Tin, class Tout>
@@ -94,27 +202,31 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 k_dense_tc(TcArgs a, const __grid_constant__ TcWeights W)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
     __shared__ int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int kw = a.kw, kh = a.kh, V = a.V, Q = a.Q, R = a.R;
     const int ncm = Q + 3;
-    size_t b_off, a_off, plane;
-    tc_smem_layout(kh, Q, R, &b_off, &a_off, &plane);
-    uint16_t *Bhi = reinterpret_cast<uint16_t *>(sm + b_off);
-    uint16_t *Blo = Bhi + (size_t)kh * ncm * 64;
-    uint16_t *Ahi = reinterpret_cast<uint16_t *>(sm + a_off);
-    uint16_t *Alo = Ahi + (size_t)Q * plane / 2;
+    const TcLayout L = tc_layout(kh, Q, R);
+    const size_t plane_el = L.plane / 2;
+    uint16_t *Bhi = reinterpret_cast<uint16_t *>(sm);
+    uint16_t *Blo = Bhi + L.b_bytes / 2;
+    // A buffer b: hi planes at Ahi(b), lo planes right after them
+    const size_t a_step = L.a_off[1] - L.a_off[0];
+    auto Ahi = [&](int b) { return reinterpret_cast<uint16_t *>(sm + L.a_off[0] + b * a_step); };
+    auto Alo = [&](int b) { return Ahi(b) + (size_t)Q * plane_el; };
+    float *stage = reinterpret_cast<float *>(sm + L.stage_off) + (size_t)warp * 32 * 17;
 
-    // tensor memory: 32 columns hold the 128 x 32 FP32 accumulator
+    // tensor memory: two accumulators of 32 columns (128 lanes x 32 FP32)
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     :: "r"(smem_u32(&tmem_slot)), "r"(32) : "memory");
+                     :: "r"(smem_u32(&tmem_slot)), "r"(64) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar)) : "memory");
+        for (int b = 0; b < 2; ++b)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar[b])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
@@ -129,125 +241,126 @@ k_dense_tc(TcArgs a, const __grid_constant__ TcWeights W)
         Bhi[e] = __bfloat16_as_ushort(hi);
         Blo[e] = __bfloat16_as_ushort(lo);
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    // both A buffers start zero: the columns past the patch are never rewritten
+    {
+        uint4 *z = reinterpret_cast<uint4 *>(sm + L.a_off[0]);
+        const size_t n16 = (L.stage_off - L.a_off[0]) / 16;
+        for (size_t e = tid; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
+    }
     __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
                            ((uint32_t)(kTcM >> 4) << 24);
-    const uint32_t ahi_s = smem_u32(Ahi), alo_s = smem_u32(Alo);
     const uint32_t bhi_s = smem_u32(Bhi), blo_s = smem_u32(Blo);
-    const uint32_t mb = smem_u32(&mbar);
-    const int valid_c = kTcN + kw - 1;
-    uint32_t phase = 0;
+    const uint32_t ps = (uint32_t)L.plane;
+    uint32_t phase = 0;                 // bit b: parity awaited on mbar[b]
 
-    for (int tile = blockIdx.x; tile < a.tiles; tile += gridDim.x) {
+    int tile = blockIdx.x;
+    if (tile < a.tiles) {
         const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
-        const int x0 = tx * kTcN, y0 = ty * kTcM;
-        // A: plane q' row r column t = Pt[r][V-1-(8q'+t)], split into BF16 hi/lo
-        for (int e = tid; e < R * V; e += blockDim.x) {
-            const int r = e / V, c = e - r * V;          // c: patch column (x order)
-            float v = 0.0f;
-            if (c < valid_c) {
-                const int mx = map_index(x0 + a.fx + c, a.nx, a.style);
-                const int my = map_index(y0 + a.fy + r, a.ny, a.style);
-                if (mx < 0 || my < 0) v = a.fill;
-                else {
-                    const Tin raw = ((const Tin *)a.img)[(long long)my * a.nx + mx];
-                    if constexpr (sizeof(Tin) == 1)
-                        v = a.in_type == IFX_N0F8 ? __fdiv_rn((float)raw, 255.0f) : (float)raw;
-                    else
-                        v = (float)raw;
-                }
-            }
-            const int vr = V - 1 - c, q = vr >> 3, t = vr & 7;
-            const size_t o = (size_t)q * (plane / 2) + (size_t)r * 8 + t;
-            const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-            const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
-            Ahi[o] = __bfloat16_as_ushort(hi);
-            Alo[o] = __bfloat16_as_ushort(lo);
-        }
-        // generic-proxy stores -> visible to the tensor core's async proxy
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (tid == 0) {
-            const uint32_t ps = (uint32_t)plane;
-            uint32_t acc = 0;
+        tc_gather<Tin>(a, tx * kTcN, ty * kTcM, Ahi(0), Alo(0), plane_el);
+    }
+    tc_fence_sync();
+    int prev = -1;                      // tile whose accumulator awaits its epilogue
+    for (int k = 0;; ++k, tile += gridDim.x) {
+        const int b = k & 1;
+        const bool have = tile < a.tiles;
+        // 1. issue the MMAs of this tile into accumulator b
+        if (have && tid == 0) {
+            // descriptors advance by adding byte offsets >> 4 to the start-address field
+            const uint64_t dAh = tc_desc(smem_u32(Ahi(b)), ps, 128), dAl = tc_desc(smem_u32(Alo(b)), ps, 128);
+            const uint64_t dBh = tc_desc(bhi_s, 128, 128), dBl = tc_desc(blo_s, 128, 128);
+            const uint32_t dt = tmem + 32u * (uint32_t)b;
+            const uint64_t a_ks = (2u * ps) >> 4;          // next 16 K values: two planes
+            const int ksteps = V / 16;
+            tc_mma(dt, dAh, dBh, idesc, 0);
+            tc_mma(dt, dAh, dBl, idesc, 1);
+            tc_mma(dt, dAl, dBh, idesc, 1);
             for (int i = 0; i < kh; ++i) {
-                for (int s = 0; s < V / 16; ++s) {
-                    const uint32_t aoff = (uint32_t)(2 * s) * ps + 16u * (uint32_t)i;
-                    const uint32_t boff = (uint32_t)((i * ncm + 2 * s) * 128);
-                    const uint64_t da_hi = tc_desc(ahi_s + aoff, ps, 128);
-                    const uint64_t da_lo = tc_desc(alo_s + aoff, ps, 128);
-                    const uint64_t db_hi = tc_desc(bhi_s + boff, 128, 128);
-                    const uint64_t db_lo = tc_desc(blo_s + boff, 128, 128);
-                    tc_mma(tmem, da_hi, db_hi, idesc, acc);
-                    acc = 1;
-                    tc_mma(tmem, da_hi, db_lo, idesc, 1);
-                    tc_mma(tmem, da_lo, db_hi, idesc, 1);
+                uint64_t ah = dAh + (uint64_t)i, al = dAl + (uint64_t)i;       // +16 i bytes
+                uint64_t bh = dBh + (uint64_t)(i * ncm * 8), bl = dBl + (uint64_t)(i * ncm * 8);
+                for (int s = (i == 0); s < ksteps; ++s) {
+                    const uint64_t ds = (uint64_t)s;
+                    tc_mma(dt, ah + ds * a_ks, bh + 16 * ds, idesc, 1);
+                    tc_mma(dt, ah + ds * a_ks, bl + 16 * ds, idesc, 1);
+                    tc_mma(dt, al + ds * a_ks, bh + 16 * ds, idesc, 1);
                 }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         :: "r"(mb) : "memory");
+                         :: "r"(smem_u32(&mbar[b])) : "memory");
         }
-        // bounded wait for the MMAs of this tile
-        bool done = false;
-        for (uint32_t it = 0; it < (1u << 22); ++it) {
-            if (mbar_try_wait(mb, phase)) {
-                done = true;
-                break;
-            }
-        }
-        phase ^= 1;
-        if (!done) {
-            if (lane == 0) atomicExch(a.err, 1);
-            s_abort = 1;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        __syncthreads();
-        if (s_abort) break;
-        // epilogue: warp w reads lanes 32w..32w+31 (rows m), 32 columns (u)
-        uint32_t r[32];
-        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                     "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                     "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                       "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-                       "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]),
-                       "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-                       "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-                       "=r"(r[30]), "=r"(r[31])
-                     : "r"(taddr) : "memory");
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const int y = y0 + 32 * warp + lane;
-        if (y < a.ny) {
-            Tout *orow = (Tout *)a.out + (long long)y * a.nx;
+        // 2. epilogue of the previous tile (accumulator b^1), overlapping this tile's MMAs
+        if (prev >= 0) {
+            const int pb = b ^ 1;
+            bool done = false;
+            for (uint32_t it = 0; it < (1u << 22); ++it)
+                if (mbar_try_wait(smem_u32(&mbar[pb]), (phase >> pb) & 1)) {
+                    done = true;
+                    break;
+                }
+            phase ^= 1u << pb;
+            done = __all_sync(0xffffffffu, done);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (!done) {
+                if (lane == 0) atomicExch(a.err, 1);
+                s_abort = 1;
+            } else {
+                const int q4 = warp & 3, half = warp >> 2;
+                uint32_t r[16];
+                const uint32_t taddr = tmem + ((uint32_t)(32 * q4) << 16) + 32u * (uint32_t)pb +
+                                       16u * (uint32_t)half;
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]),
+                               "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+                               "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                               "=r"(r[15])
+                             : "r"(taddr) : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int u = 0; u < kTcN; ++u) {
-                const int x = x0 + u;
-                if (x < a.nx) orow[x] = (Tout)__uint_as_float(r[u]);
+                for (int u = 0; u < 16; ++u) stage[lane * 17 + u] = __uint_as_float(r[u]);
+                __syncwarp();
+                const int pty = prev / a.tiles_x, ptx = prev - pty * a.tiles_x;
+                const int xo = ptx * kTcN + 16 * half + (lane & 15);
+                const int yb = pty * kTcM + 32 * q4;
+#pragma unroll 4
+                for (int rr = 0; rr < 32; rr += 2) {
+                    const int row = rr + (lane >> 4), y = yb + row;
+                    if (y < a.ny && xo < a.nx)
+                        ((Tout *)a.out)[(long long)y * a.nx + xo] = (Tout)stage[row * 17 + (lane & 15)];
+                }
             }
         }
-        // the next tile's MMAs overwrite the accumulator and the A planes
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // 3. gather the next tile into the other A buffer (its MMAs, two tiles
+        //    back, completed before the epilogue above)
+        const int next = tile + gridDim.x;
+        if (have && next < a.tiles) {
+            const int ty = next / a.tiles_x, tx = next - ty * a.tiles_x;
+            tc_gather<Tin>(a, tx * kTcN, ty * kTcM, Ahi(b ^ 1), Alo(b ^ 1), plane_el);
+        }
+        tc_fence_sync();
+        if (s_abort) {
+            // let this tile's MMAs (if any) drain before the accumulator is freed
+            if (have)
+                for (uint32_t it = 0; it < (1u << 22); ++it)
+                    if (mbar_try_wait(smem_u32(&mbar[b]), (phase >> b) & 1)) break;
+            break;
+        }
+        if (!have) break;
+        prev = tile;
     }
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(32) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(64) : "memory");
 }
-
-static int *g_tc_err[64];
 
 bool dense_tc_supported(int in_type, int kw, int kh)
 {
-    return (in_type == IFX_F32 || in_type == IFX_N0F8 || in_type == IFX_U8) && kw >= 1 &&
-           kw <= kTcMaxKw && kh >= 1 && kh <= kTcMaxKh;
+    if (!((in_type == IFX_F32 || in_type == IFX_N0F8 || in_type == IFX_U8) && kw >= 1 &&
+          kw <= kTcMaxKw && kh >= 1 && kh <= kTcMaxKh))
+        return false;
+    const int V = (kTcN + kw - 1 + 15) / 16 * 16;
+    return tc_layout(kh, V / 8, kTcM + kh - 1).total <= 225 * 1024;   // + static shared
 }
 
 template <class Tin, class Tout>
@@ -272,42 +385,25 @@ static cudaError_t dense_tc_t(const Dense2dArgs &d, cudaStream_t s, int device)
     a.R = kTcM + d.kh - 1;
     a.tiles_x = (d.nx + kTcN - 1) / kTcN;
     a.tiles = a.tiles_x * ((d.ny + kTcM - 1) / kTcM);
-    if (!g_tc_err[device]) {
-        cudaError_t e = cudaMalloc(&g_tc_err[device], sizeof(int));
-        if (e != cudaSuccess) return e;
-        cudaMemset(g_tc_err[device], 0, sizeof(int));
-    }
-    a.err = g_tc_err[device];
+    a.err = tma_error_word(device);
+    if (!a.err) return cudaErrorMemoryAllocation;
     static thread_local TcWeights W;
     for (int t = 0; t < d.kw * d.kh; ++t) W.w[t] = (float)d.K[t];
-    size_t b_off, a_off, plane;
-    const size_t smem = tc_smem_layout(d.kh, a.Q, a.R, &b_off, &a_off, &plane);
+    const size_t smem = tc_layout(d.kh, a.Q, a.R).total;
     auto kern = k_dense_tc<Tin, Tout>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int sms = 0;
+    int sms = 0, per_sm = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const int grid = a.tiles < sms ? a.tiles : sms;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTcThreads, smem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    if (per_sm > 4) per_sm = 4;               // 4 x 64 TMEM columns at most
+    const long long slots = (long long)sms * per_sm;
+    const int grid = a.tiles < slots ? a.tiles : (int)slots;
     kern<<<grid, kTcThreads, smem, s>>>(a, W);
     note_launch();
     return cudaGetLastError();
-}
-
-size_t dense_tc_smem_bytes(int kw, int kh)
-{
-    const int V = (kTcN + kw - 1 + 15) / 16 * 16;
-    size_t b, a, p;
-    return tc_smem_layout(kh, V / 8, kTcM + kh - 1, &b, &a, &p);
-}
-
-// Reads (and clears) the timeout flag of the tensor-core kernel on `device`.
-int dense_tc_check_error(int device)
-{
-    if (device < 0 || device >= 64 || !g_tc_err[device]) return 0;
-    int h = 0;
-    cudaMemcpy(&h, g_tc_err[device], sizeof(int), cudaMemcpyDeviceToHost);
-    if (h) cudaMemset(g_tc_err[device], 0, sizeof(int));
-    return h;
 }
 
 cudaError_t launch_dense_tc(const Dense2dArgs &d, cudaStream_t s, int device)

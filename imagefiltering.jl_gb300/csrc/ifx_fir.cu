@@ -13,6 +13,7 @@
 //  * a pass is the correlation out[i] = sum_j A[i+j] k[j] (src/imfilter.jl:
 //    671-739); dense kernels sum over all taps (src/imfilter.jl:624-669).
 #include "ifx_internal.h"
+#include "ifx_tma.cuh"
 #include <cstdio>
 #include <cstring>
 
@@ -247,7 +248,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
 #pragma unroll
                 for (int i = 0; i < NB; ++i) {
                     const int y = ty0 + r0 + i;
-                    if (y < ny) out[(long long)y * nx + x] = (Tout)acc[i];
+                    if (y < ny) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
                 }
             }
         }
@@ -277,7 +278,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
 #pragma unroll
                 for (int i = 0; i < NB; ++i) {
                     const int x = tx0 + c0 + i;
-                    if (x < nx) out[(long long)y * nx + x] = (Tout)acc[i];
+                    if (x < nx) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
                 }
             }
         }
@@ -303,6 +304,255 @@ static cudaError_t sep2d_t(const Sep2dArgs &a, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// =========================================================================
+// Fused 2-D separable kernel, persistent and fed by the Tensor Memory
+// Accelerator (FP32 compute; Float32 or 8-bit images whose rows meet the copy
+// engine's 16-byte rules).  Each CTA walks tiles blockIdx.x, +gridDim.x, ...
+// and keeps two input buffers: while tile k is filtered, the bulk copy of
+// tile k+1 (TX+kx-1 by TY+ky-1 inputs, x rounded down to the 16-byte
+// boundary) is in flight.  Tiles whose input window leaves the image are
+// gathered through the border map instead (same index arithmetic as
+// k_sep2d).  The passes are those of k_sep2d.
+// =========================================================================
+constexpr int kStTX = 64, kStTY = 64;
+
+__host__ __device__ inline size_t st_round128(size_t b) { return (b + 127) & ~(size_t)127; }
+
+struct SepTmaSmem {
+    size_t raw, w, t, i, total;
+};
+
+__host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int boxw, int elt_bytes)
+{
+    SepTmaSmem L;
+    const int RV = kStTY + ky - 1, CV = kStTX + kx - 1;
+    L.raw = st_round128((size_t)boxw * RV * elt_bytes);
+    L.w = st_round128(2 * (IFX_MAX_TAPS + 3) * sizeof(float) + 256 * sizeof(float));
+    L.t = elt_bytes == 1 ? st_round128((size_t)RV * CV * sizeof(float)) : 0;
+    const size_t ix = (size_t)RV * kStTX, iy = (size_t)kStTY * CV;
+    L.i = st_round128((ix > iy ? ix : iy) * sizeof(float));
+    L.total = 2 * L.raw + L.w + L.t + L.i;
+    return L;
+}
+
+template <class Tin, class Tout>
+__global__ void __launch_bounds__(256)
+k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img, Tout *__restrict__ out,
+            int nx, int ny, int fx, int kx, int fy, int ky, int x_first, int style, float fill, bool norm,
+            int boxw, int tiles_x, int tiles, int *err, const __grid_constant__ Sep2dW<float> W)
+{
+    constexpr int TX = kStTX, TY = kStTY, NB = kSepNB;
+    constexpr int ALIGN = 16 / (int)sizeof(Tin);          // x granularity of a box start
+    extern __shared__ __align__(128) unsigned char st_smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    const int RV = TY + ky - 1, CV = TX + kx - 1;
+    const SepTmaSmem L = sep_tma_smem(kx, ky, boxw, (int)sizeof(Tin));
+    float *wx = reinterpret_cast<float *>(st_smem + 2 * L.raw);
+    float *wy = wx + (IFX_MAX_TAPS + 3);
+    float *lut = wy + (IFX_MAX_TAPS + 3);                   // 8-bit code -> value
+    float *T = reinterpret_cast<float *>(st_smem + 2 * L.raw + L.w);
+    float *I = reinterpret_cast<float *>(st_smem + 2 * L.raw + L.w + L.t);
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const uint32_t box_bytes = (uint32_t)(boxw * RV * (int)sizeof(Tin));
+    for (int t = tid; t < kx; t += nth) wx[t] = W.wx[t];
+    for (int t = tid; t < ky; t += nth) wy[t] = W.wy[t];
+    if (sizeof(Tin) == 1)
+        for (int c = tid; c < 256; c += nth) lut[c] = to_c<float>((uint8_t)c, norm);
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+        tma_prefetch_map(&map);
+    }
+    __syncthreads();
+
+    auto raw = [&](int b) { return reinterpret_cast<Tin *>(st_smem + (size_t)b * L.raw); };
+    auto origin = [&](int t, int &px, int &py) {
+        const int ty = t / tiles_x, tx = t - ty * tiles_x;
+        px = tx * TX + fx;
+        py = ty * TY + fy;
+    };
+    auto interior = [&](int t) {
+        int px, py;
+        origin(t, px, py);
+        return px >= 0 && px + CV <= nx && py >= 0 && py + RV <= ny;
+    };
+    auto issue = [&](int t, int b) {          // thread 0 only
+        int px, py;
+        origin(t, px, py);
+        mbar_expect_tx(&bar[b], box_bytes);
+        tma_load_2d(raw(b), &map, px & ~(ALIGN - 1), py, &bar[b]);
+    };
+
+    uint32_t parity = 0;                      // bit b: phase awaited on bar[b]
+    uint32_t pending = 0;                     // bit b: a copy into raw(b) is in flight
+    int t = blockIdx.x;
+    if (t < tiles && interior(t)) {
+        if (tid == 0) issue(t, 0);
+        pending |= 1u;
+    }
+    for (int k = 0; t < tiles; ++k, t += gridDim.x) {
+        const int b = k & 1;
+        const int tn = t + gridDim.x;
+        if (tn < tiles && interior(tn)) {     // prefetch the next tile into the other buffer
+            if (tid == 0) issue(tn, b ^ 1);
+            pending |= 2u >> b;               // bit b^1
+        }
+        int px, py;
+        origin(t, px, py);
+        const float *P;
+        int SP;
+        if (pending & (1u << b)) {
+            const bool ok = mbar_wait_bounded(&bar[b], (parity >> b) & 1u);
+            parity ^= 1u << b;
+            pending &= ~(1u << b);
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicExch(err, 1);
+                    if (pending & (2u >> b)) mbar_wait_bounded(&bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
+                }
+                return;
+            }
+            const int dx = px & (ALIGN - 1);
+            if (sizeof(Tin) == 4) {
+                P = reinterpret_cast<const float *>(raw(b)) + dx;
+                SP = boxw;
+            } else {
+                const uint8_t *R = reinterpret_cast<const uint8_t *>(raw(b));
+                for (int idx = tid; idx < RV * CV; idx += nth) {
+                    const int r = idx / CV, c = idx - r * CV;
+                    T[idx] = lut[R[r * boxw + dx + c]];
+                }
+                __syncthreads();
+                P = T;
+                SP = CV;
+            }
+        } else {
+            // border tile: gather through the border map
+            float *G = sizeof(Tin) == 4 ? reinterpret_cast<float *>(raw(b)) : T;
+            const int SG = sizeof(Tin) == 4 ? boxw : CV;
+            gather_tile<8>(G, RV * SG, [&](int idx) -> float {
+                const int r = idx / SG, c = idx - r * SG;
+                if (c >= CV) return 0.0f;
+                const int mx = map_index(px + c, nx, style);
+                const int my = map_index(py + r, ny, style);
+                return (mx < 0 || my < 0) ? fill : cvt<float, Tin>(img[(long long)my * nx + mx], norm);
+            });
+            __syncthreads();
+            P = G;
+            SP = SG;
+        }
+
+        const int tx0 = px - fx, ty0 = py - fy;
+        float acc[NB];
+        if (x_first) {
+            const int segs = TX / NB;
+            for (int it = tid; it < RV * segs; it += nth) {
+                const int r = it / segs, c0 = (it - r * segs) * NB;
+                corr_run<float, NB>(P + (size_t)r * SP + c0, 1, wx, kx, acc);
+#pragma unroll
+                for (int i = 0; i < NB; ++i) I[(size_t)r * TX + c0 + i] = acc[i];
+            }
+            __syncthreads();
+            for (int it = tid; it < TX * (TY / NB); it += nth) {
+                const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
+                corr_run<float, NB>(I + (size_t)r0 * TX + c, TX, wy, ky, acc);
+                const int x = tx0 + c;
+                if (x < nx) {
+#pragma unroll
+                    for (int i = 0; i < NB; ++i) {
+                        const int y = ty0 + r0 + i;
+                        if (y < ny) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
+                    }
+                }
+            }
+        } else {
+            for (int it = tid; it < CV * (TY / NB); it += nth) {
+                const int rs = it / CV, c = it - rs * CV, r0 = rs * NB;
+                corr_run<float, NB>(P + (size_t)r0 * SP + c, SP, wy, ky, acc);
+#pragma unroll
+                for (int i = 0; i < NB; ++i) I[(size_t)(r0 + i) * CV + c] = acc[i];
+            }
+            __syncthreads();
+            const int segs = TX / NB;
+            for (int it = tid; it < TY * segs; it += nth) {
+                const int r = it / segs, c0 = (it - r * segs) * NB;
+                corr_run<float, NB>(I + (size_t)r * CV + c0, 1, wx, kx, acc);
+                const int y = ty0 + r;
+                if (y < ny) {
+#pragma unroll
+                    for (int i = 0; i < NB; ++i) {
+                        const int x = tx0 + c0 + i;
+                        if (x < nx) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
+                    }
+                }
+            }
+        }
+        // raw(b), T and I are rewritten by the next rounds (the bulk copy
+        // engine among the writers)
+        fence_proxy_async();
+        __syncthreads();
+    }
+}
+
+template <class Tin, class Tout>
+static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
+{
+    constexpr int ALIGN = 16 / (int)sizeof(Tin);
+    const int CV = kStTX + a.kx - 1, RV = kStTY + a.ky - 1;
+    const int boxw = (CV + ALIGN - 1 + ALIGN - 1) / ALIGN * ALIGN;
+    if (boxw > 256 || RV > 256) return false;
+    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, boxw, (int)sizeof(Tin));
+    if (L.total > 160 * 1024) return false;
+    CUtensorMap map;
+    if (!tma_encode_2d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, (long long)a.nx * (long long)sizeof(Tin),
+                       boxw, RV))
+        return false;
+    int dev = 0;
+    if ((*e = cudaGetDevice(&dev)) != cudaSuccess) return true;
+    int *err = tma_error_word(dev);
+    if (!err) {
+        *e = cudaErrorMemoryAllocation;
+        return true;
+    }
+    Sep2dW<float> W;
+    memset(&W, 0, sizeof W);
+    for (int t = 0; t < a.kx; ++t) W.wx[t] = (float)a.wx[t];
+    for (int t = 0; t < a.ky; ++t) W.wy[t] = (float)a.wy[t];
+    auto kern = k_sep2d_tma<Tin, Tout>;
+    if ((*e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total)) !=
+        cudaSuccess)
+        return true;
+    int sms = 0, per_sm = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, L.total) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const int tiles_x = (a.nx + kStTX - 1) / kStTX;
+    const long long tiles = (long long)tiles_x * ((a.ny + kStTY - 1) / kStTY);
+    if (tiles > (1ll << 30)) return false;
+    const long long slots = (long long)sms * per_sm;
+    const int grid = (int)(tiles < slots ? tiles : slots);
+    kern<<<grid, 256, L.total, s>>>(map, (const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.fx, a.kx, a.fy,
+                                    a.ky, a.x_first, a.style, (float)a.fill, a.in_type == IFX_N0F8, boxw,
+                                    tiles_x, (int)tiles, err, W);
+    note_launch();
+    *e = cudaGetLastError();
+    return true;
+}
+
+// true when the TMA kernel took the call (its launch status in *e); false
+// when it does not apply and k_sep2d runs instead.
+static bool launch_sep2d_tma(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
+{
+    if (a.compute_f64) return false;
+    const int it = a.in_type, ot = a.out_type;
+    if (it == IFX_F32 && ot == IFX_F32) return sep2d_tma_t<float, float>(a, s, e);
+    if (it == IFX_F32 && ot == IFX_F64) return sep2d_tma_t<float, double>(a, s, e);
+    if (is8(it) && ot == IFX_F32) return sep2d_tma_t<uint8_t, float>(a, s, e);
+    if (is8(it) && ot == IFX_F64) return sep2d_tma_t<uint8_t, double>(a, s, e);
+    return false;
+}
+
 size_t sep2d_smem_bytes(int kx, int ky, int x_first, int f64)
 {
     return f64 ? sep2d_smem<double>(kx, ky, x_first) : sep2d_smem<float>(kx, ky, x_first);
@@ -311,6 +561,8 @@ size_t sep2d_smem_bytes(int kx, int ky, int x_first, int f64)
 cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s)
 {
     if (a.nx == 0 || a.ny == 0) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    if (launch_sep2d_tma(a, s, &e)) return e;
     const int it = a.in_type, ot = a.out_type;
     if (!a.compute_f64) {
         if (it == IFX_F32 && ot == IFX_F32) return sep2d_t<float, float, float>(a, s);
@@ -407,7 +659,7 @@ k_sep3d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny, int
                 float a = 0.0f;
                 for (int t = 0; t < kz; ++t)
                     a = fmaf(wz[t], ring[((z + fz + t - s_first) % kz) * (TY * TX) + it], a);
-                if (x < nx && y < ny) dst[(long long)z * plane + (long long)y * nx + x] = (Tout)a;
+                if (x < nx && y < ny) dst[(long long)z * plane + (long long)y * nx + x] = out_cvt<Tout>(a);
             }
         }
     }

@@ -72,7 +72,9 @@ cudaError_t launch_dense2d(const Dense2dArgs &a, cudaStream_t s);
 // tcgen05 tensor-core path (2-D, kernels up to 33 wide and 40 tall)
 bool dense_tc_supported(int in_type, int kw, int kh);
 cudaError_t launch_dense_tc(const Dense2dArgs &a, cudaStream_t s, int device);
-int dense_tc_check_error(int device);
+// Bounded waits that ran out in a kernel launched on `device` since the last
+// call (reads and clears the device's error word).
+int kernel_timeout_take(int device);
 
 struct DenseBoxArgs {                      // N-d dense over a padded compute-type box
     const void *src; Box sbox;

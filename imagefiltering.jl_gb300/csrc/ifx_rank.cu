@@ -14,10 +14,11 @@
 // Windows at the border follow copy_win! (src/mapwindow.jl:310-333): a Pad
 // style pads relative to window-intersect-image.  For replicate, symmetric and
 // reflect that is the same as mapping through the whole image (the truncated
-// window never needs a second reflection), so the SIMD path gathers a padded
-// tile; circular (which wraps inside the truncated window) and non-8-bit or
-// N-d images use the per-pixel kernel, which applies the window-relative map
-// literally.
+// window never needs a second reflection), so the 2-D tile kernels gather a
+// padded tile.  Circular wraps inside the truncated window: the tile kernels
+// read the windows that leave the image straight from the image through the
+// window-relative map (win_index2); N-d images and other window shapes use the
+// per-pixel kernel, which applies the window-relative map literally.
 #include "ifx_internal.h"
 #include "ifx_select.cuh"
 #include <cstring>
@@ -67,6 +68,26 @@ template <> __device__ __forceinline__ bool lt<float>(float a, float b)
 template <> __device__ __forceinline__ bool lt<double>(double a, double b)
 {
     return isnan(b) ? !isnan(a) : a < b;
+}
+
+// Offset in a 2-D image of window element (i, j) of output (x, y) under the
+// window-relative map of copy_win! (window first offsets f0/f1, lengths
+// w0/w1): the Pad style is applied relative to window-intersect-image.
+__device__ __forceinline__ long long win_index2(int x, int y, int i, int j, int f0, int f1, int w0,
+                                                int w1, int nx, int ny, int style)
+{
+    const int ofx = x + f0, olx = ofx + w0 - 1, ofy = y + f1, oly = ofy + w1 - 1;
+    const int ax = ofx > 0 ? ofx : 0, bx = olx < nx - 1 ? olx : nx - 1;
+    const int ay = ofy > 0 ? ofy : 0, by = oly < ny - 1 ? oly : ny - 1;
+    const int mx = map_index_in(ofx + i, ax, bx - ax + 1, style);
+    const int my = map_index_in(ofy + j, ay, by - ay + 1, style);
+    return (long long)my * nx + mx;
+}
+
+// Does the window of output (x, y) leave the image?
+__device__ __forceinline__ bool win_leaves(int x, int y, int f0, int f1, int w0, int w1, int nx, int ny)
+{
+    return x + f0 < 0 || x + f0 + w0 > nx || y + f1 < 0 || y + f1 + w1 > ny;
 }
 
 // =========================================================================
@@ -166,14 +187,28 @@ k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, in
     const int lx = (threadIdx.x & 31) * 4, ly = threadIdx.x >> 5;
     const int m = w0 * w1;
     const uint32_t rank4 = 0x01010101u * (uint32_t)((m + 1) / 2);
+    // circular windows that leave the image are read through the window-relative map
+    const int xw = tx0 + lx, yw = ty0 + ly;
+    const bool edge = style == IFX_CIRCULAR && yw < ny && xw < nx &&
+                      (win_leaves(xw, yw, f0, f1, w0, w1, nx, ny) ||
+                       win_leaves(min(xw + 3, nx - 1), yw, f0, f1, w0, w1, nx, ny));
+    auto word = [&](int j, int i) -> uint32_t {
+        if (!edge) return load_word(tile + (size_t)(ly + j) * CT, lx + i);
+        uint32_t wd = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int x = min(xw + q, nx - 1);
+            wd |= (uint32_t)img[win_index2(x, yw, i, j, f0, f1, w0, w1, nx, ny, style)] << (8 * q);
+        }
+        return wd;
+    };
     uint32_t res = 0;
     if (W0 > 0 && W1 > 0) {
         uint32_t w[(W0 > 0 ? W0 : 1) * (W1 > 0 ? W1 : 1)];
 #pragma unroll
         for (int j = 0; j < (W1 > 0 ? W1 : 1); ++j)
 #pragma unroll
-            for (int i = 0; i < (W0 > 0 ? W0 : 1); ++i)
-                w[j * W0 + i] = load_word(tile + (size_t)(ly + j) * CT, lx + i);
+            for (int i = 0; i < (W0 > 0 ? W0 : 1); ++i) w[j * W0 + i] = word(j, i);
 #pragma unroll
         for (int b = 7; b >= 0; --b) {
             const uint32_t trial = res | (0x01010101u << b);
@@ -187,10 +222,8 @@ k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, in
         for (int b = 7; b >= 0; --b) {
             const uint32_t trial = res | (0x01010101u << b);
             uint32_t cnt = 0;
-            for (int j = 0; j < w1; ++j) {
-                const uint8_t *row = tile + (size_t)(ly + j) * CT;
-                for (int i = 0; i < w0; ++i) cnt = count_lt(cnt, load_word(row, lx + i), trial);
-            }
+            for (int j = 0; j < w1; ++j)
+                for (int i = 0; i < w0; ++i) cnt = count_lt(cnt, word(j, i), trial);
             const uint32_t below = __vcmpltu4(cnt, rank4);
             res = (trial & below) | (res & ~below);
         }
@@ -226,13 +259,17 @@ k_median_float(const T *__restrict__ img, void *out, int out_type, int nx, int n
     });
     __syncthreads();
     const int lx = threadIdx.x % kFmTX, ly = threadIdx.x / kFmTX;
+    const int x = tx0 + lx, y = ty0 + ly;
+    const bool edge = style == IFX_CIRCULAR && x < nx && y < ny &&
+                      win_leaves(x, y, f0, f1, W0, W1, nx, ny);
     K v[N];
 #pragma unroll
     for (int j = 0; j < W1; ++j)
 #pragma unroll
-        for (int i = 0; i < W0; ++i) v[j * W0 + i] = SK::key(tile[(ly + j) * CT + lx + i]);
+        for (int i = 0; i < W0; ++i)
+            v[j * W0 + i] = SK::key(edge ? img[win_index2(x, y, i, j, f0, f1, W0, W1, nx, ny, style)]
+                                         : tile[(ly + j) * CT + lx + i]);
     net_sort<N, K>(v);
-    const int x = tx0 + lx, y = ty0 + ly;
     if (x < nx && y < ny) store_sel<T>(out, out_type, (long long)y * nx + x, SK::val(v[(N - 1) / 2]), false);
 }
 
@@ -289,7 +326,7 @@ cudaError_t launch_median(const MedianArgs &a, cudaStream_t s)
     if (total == 0) return cudaSuccess;
     const bool u8 = a.in_type == IFX_N0F8 || a.in_type == IFX_U8;
     const int m = a.wlen[0] * (a.nd > 1 ? a.wlen[1] : 1);
-    if (u8 && a.nd <= 2 && a.style != IFX_CIRCULAR && m <= 255) {
+    if (u8 && a.nd <= 2 && m <= 255) {
         const int w0 = a.wlen[0], w1 = a.nd > 1 ? a.wlen[1] : 1;
         if (w0 == 3 && w1 == 3) return median_u8_t<3, 3>(a, s);
         if (w0 == 5 && w1 == 5) return median_u8_t<5, 5>(a, s);
@@ -297,7 +334,7 @@ cudaError_t launch_median(const MedianArgs &a, cudaStream_t s)
         return median_u8_t<0, 0>(a, s);
     }
     if (u8) return median_px_t<uint8_t>(a, s);
-    const bool fast2d = a.nd <= 2 && a.style != IFX_CIRCULAR;
+    const bool fast2d = a.nd <= 2;
     if (fast2d && (a.in_type == IFX_F32 || a.in_type == IFX_F64)) {
         const int w0 = a.wlen[0], w1 = a.nd > 1 ? a.wlen[1] : 1;
         const bool f32 = a.in_type == IFX_F32;

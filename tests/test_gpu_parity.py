@@ -6,6 +6,8 @@ not Float64 (FP32 arithmetic on the GPU against the FP64 oracle), 1e-12 for
 Float64 images (FP64 on the GPU); border maps, Laplacian, median and extrema
 bit-exact.
 """
+import zlib
+
 import numpy as np
 import pytest
 
@@ -62,7 +64,7 @@ def fill_value(kind, fill=0.7):
 @pytest.mark.parametrize("style", STYLES)
 def test_separable_2d_random(gpu_ifx, oracle, kind, style):
     ifx = gpu_ifx
-    rng = np.random.default_rng(hash((kind, style)) % 2 ** 32)
+    rng = np.random.default_rng(zlib.crc32((kind + style).encode()))
     for shape in [(67, 45), (130, 7), (3, 200), (64, 64)]:
         img = make_img(rng, shape, kind)
         for _ in range(3):
@@ -78,6 +80,55 @@ def test_separable_2d_random(gpu_ifx, oracle, kind, style):
             ref = oracle.imfilter_cascade(values(ifx, img, kind), order, style, fv)
             assert got.dtype == np.float64
             assert normwise(got, ref) <= RTOL[kind], (shape, order, style)
+
+
+@pytest.mark.parametrize("kind", ["F32", "N0F8", "U8"])
+@pytest.mark.parametrize("style", STYLES)
+def test_separable_2d_tma_tiles(gpu_ifx, oracle, kind, style):
+    """Images whose rows meet the bulk-copy rules (width a multiple of 16), so
+    that the persistent kernel copies interior tiles by TMA and gathers the
+    border tiles: random factor lengths/offsets, both pass orders, Float32 and
+    Float64 outputs, several tiles per CTA on the largest image."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("tma" + kind + style).encode()))
+    for shape in [(256, 200), (1040, 333), (4096, 1100)]:
+        img = make_img(rng, shape, kind)
+        for _ in range(2 if shape[0] < 4096 else 1):
+            lx, ly = int(rng.integers(1, 34)), int(rng.integers(1, 34))
+            fx, fy = int(rng.integers(-lx, 2)), int(rng.integers(-ly, 2))
+            wx, wy = rng.standard_normal(lx), rng.standard_normal(ly)
+            order = [(0, fx, wx), (1, fy, wy)] if rng.random() < 0.5 else [(1, fy, wy), (0, fx, wx)]
+            f32w = rng.random() < 0.5          # Float32 weights keep a Float32 output
+            ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(w.astype(np.float32) if f32w else w, (f,)), 2, ax)
+                       for ax, f, w in order)
+            fill = 0.7 if kind != "U8" else 3.0
+            b = ifx.Fill(fill) if style == "fill" else ifx.Pad(style)
+            got = ifx.imfilter(wrap(ifx, img, kind), ks, b)
+            fv = fill_value(kind, fill) if kind != "U8" else 3.0
+            ref_order = [(ax, f, w.astype(np.float32).astype(np.float64) if f32w else w) for ax, f, w in order]
+            ref = oracle.imfilter_cascade(values(ifx, img, kind), ref_order, style, fv)
+            assert got.dtype == (np.float32 if f32w else np.float64), got.dtype
+            assert normwise(got, ref) <= RTOL[kind], (shape, order, style)
+
+
+def test_float64_widening_exact(gpu_ifx):
+    """Float64 outputs of FP32 arithmetic are widened exactly: zeros,
+    subnormals, the extremes of the normal range, Inf and NaN."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(3)
+    special = np.array([0.0, 1e-40, -1e-40, 1.17549435e-38, -1.17549435e-38, 3.4028235e38 / 2,
+                        -3.4028235e38 / 2, 3.4028235e38, np.inf, -np.inf, np.nan, 1.0, -2.5,
+                        1.4e-45, 123456.789], dtype=np.float32)
+    img = rng.standard_normal((256, 64)).astype(np.float32) * np.float32(1e3)
+    img.flat[: special.size * 37: 37] = special
+    img = np.asfortranarray(img)
+    k = (ifx.ReshapedOneD(ifx.OffsetKernel(np.array([2.0]), (0,)), 2, 0),)
+    for shape_img in (img, np.asfortranarray(img[:, :63])):   # TMA path and plain path
+        got = ifx.imfilter(shape_img, k, "replicate")
+        exp = (shape_img * np.float32(2)).astype(np.float64)
+        assert got.dtype == np.float64
+        assert np.array_equal(got.view(np.uint64)[~np.isnan(exp)], exp.view(np.uint64)[~np.isnan(exp)])
+        assert np.array_equal(np.isnan(got), np.isnan(exp))
 
 
 @pytest.mark.parametrize("taps", [9, 17])
@@ -271,7 +322,8 @@ def test_median_u8_exact(gpu_ifx, oracle, kind, style):
 def test_median_float_nd(gpu_ifx, oracle, kind):
     ifx = gpu_ifx
     rng = np.random.default_rng(22)
-    for shape, win in [((31, 17), (3, 5)), ((9, 8, 7), (3, 3, 3)), ((50,), (7,))]:
+    for shape, win in [((31, 17), (3, 5)), ((9, 8, 7), (3, 3, 3)), ((50,), (7,)),
+                       ((40, 23), (3, 3)), ((40, 23), (5, 5)), ((19, 33), (7, 7)), ((4, 6), (5, 5))]:
         img = make_img(rng, shape, kind)
         for style in STYLES:
             got = ifx.mapwindow(ifx.median, img, win, border=border_of(ifx, style, 0.25))
@@ -433,3 +485,24 @@ def test_dense_tensor_cores_shapes(gpu_ifx, oracle):
     got = ifx.imfilter(ifx.n0f8(codes), ifx.centered(K), "replicate", ifx.Algorithm.GB300("tensor_cores"))
     ref = oracle.imfilter_dense(codes.astype(np.float64) / 255.0, K, (-7, -7), "replicate")
     assert normwise(got, ref) <= 1e-5
+
+
+def test_dense_tensor_cores_many_tiles(gpu_ifx, oracle):
+    """Images with several 128 x 32 tiles per CTA, so that the double-buffered
+    pipeline (gather of tile k+1 and epilogue of tile k-1 around the MMAs of
+    tile k) runs many rounds: against the oracle, and at 4096 x 2048 against
+    the CUDA-core path."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(31)
+    K = rng.standard_normal((15, 15))
+    K /= K.sum()
+    img = np.asfortranarray(rng.random((2049, 1031), dtype=np.float32))
+    got = ifx.imfilter(img, ifx.centered(K), "reflect", ifx.Algorithm.GB300("tensor_cores"))
+    ref = oracle.imfilter_dense(img.astype(np.float64), K, (-7, -7), "reflect")
+    assert normwise(got, ref) <= 1e-5
+    K = rng.standard_normal((31, 31))
+    K /= K.sum()
+    big = np.asfortranarray(rng.random((4096, 2048), dtype=np.float32))
+    tc = ifx.imfilter(big, ifx.centered(K), "circular", ifx.Algorithm.GB300("tensor_cores"))
+    cc = ifx.imfilter(big, ifx.centered(K), "circular", ifx.Algorithm.GB300("cuda_cores"))
+    assert normwise(tc, cc) <= 1e-5
