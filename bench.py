@@ -309,7 +309,22 @@ def run_stream(args, ifx, torch, rank):
         bk[1] += sum(alg_bytes(r) for r in rs)
         bk[2] += 1
     pixels = sum(r.pixels for r in timed)
+    # per filter kind: the first timed wave's requests of one kind as one plan
+    per_op_batched = {}
+    w0, ins0 = timed_p[0][0], timed_p[0][1]
+    for op in sorted(set(r.op for r in w0)):
+        sub = [(r, t) for r, t in zip(w0, ins0) if r.op == op]
+        sbt, _ = batch_for_wave(ifx, [r for r, _ in sub], [t for _, t in sub], out_arena)
+        splan = B.Plan(sbt)
+        ms = _time(torch, lambda: A.check(ctx.lib.ifx_batch_plan_launch(splan.handle, C.byref(tiles),
+                                                                        stream)))
+        by = sum(alg_bytes(r) for r, _ in sub)
+        per_op_batched[op] = {"requests": len(sub), "ms": round(ms, 4), "alg_bytes": by,
+                              "mpix_s": sum(r.pixels for r, _ in sub) / (ms / 1e3) / 1e6,
+                              "achieved_gbs": by / (ms / 1e3) / 1e9}
+        splan.close()
     return {"pixels": pixels, "dev_ms": batch_ms, "plain_ms": plain_ms, "run_ms": run_ms,
+            "per_op_batched": per_op_batched,
             "launches": launches,
             "host_ms_per_step": {k: v * 1e3 / max(len(timed_p), 1) for k, v in host_s.items()},
             "per_op": per_op, "batch_kernel": bk, "clocks": clocks, "reqs": timed}
@@ -730,6 +745,8 @@ def main():
                       "mode": "one C-ABI call per request (device-resident)",
                       "per_op_ms": {k: round(v[0], 3) for k, v in per_op.items()}},
         "batched_over_plain": value / plain_value,
+        "batched_per_kind": {k: dict(v, hbm_frac=v["achieved_gbs"] / hbm_peak)
+                             for k, v in res["per_op_batched"].items()},
         "batch_run_per_call_validation": {
             "value": res["pixels"] * ws / (res["run_ms"] / 1e3) / 1e6, "unit": "Mpixel/s",
             "mode": "ifx_batch_run: requests validated on every launch (pointer queries per array)"},

@@ -162,6 +162,66 @@ __device__ __forceinline__ void corr_run(const Tc *p, int step, const Tc *w, int
     }
 }
 
+// Unrolled forms of corr_run for k <= kCorrKmax taps: the tap loop is
+// unrolled at compile time and left when t reaches k, so every window value
+// has a fixed register and nothing is shifted.
+constexpr int kCorrKmax = 36;
+
+// Column form: acc[i] = sum_{t<k} w[t] p[(i+t)*step], i < NB; reads
+// p[0 .. NB+k-2] only.
+template <int NB>
+__device__ __forceinline__ void corr_col(const float *p, int step, const float *w, int k, float *acc)
+{
+    float v[NB + kCorrKmax - 1];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        v[i] = p[i * step];
+        acc[i] = 0.0f;
+    }
+#pragma unroll
+    for (int t = 0; t < kCorrKmax; ++t) {
+        if (t >= k) break;
+        if (t > 0) v[NB - 1 + t] = p[(NB - 1 + t) * step];
+        const float wt = w[t];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) acc[i] = fmaf(wt, v[i + t], acc[i]);
+    }
+}
+
+// Row form on a 16-byte aligned window, loaded four values at a time:
+// acc[i] = sum_{t<k} w[t] p[i+t], i < NB (NB a multiple of 4); reads
+// p[0 .. 4*ceil((NB+k-1)/4) - 1], up to 3 values past the window.
+template <int NB>
+__device__ __forceinline__ void corr_row4(const float *p, const float *w, int k, float *acc)
+{
+    float v[NB + kCorrKmax + 3];
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+    for (int c = 0; c < NB / 4; ++c) {
+        const float4 f = q[c];
+        v[4 * c] = f.x;
+        v[4 * c + 1] = f.y;
+        v[4 * c + 2] = f.z;
+        v[4 * c + 3] = f.w;
+    }
+#pragma unroll
+    for (int i = 0; i < NB; ++i) acc[i] = 0.0f;
+#pragma unroll
+    for (int t = 0; t < kCorrKmax; ++t) {
+        if (t >= k) break;
+        if (t > 0 && ((NB - 1 + t) & 3) == 0) {
+            const float4 f = q[(NB - 1 + t) >> 2];
+            v[NB - 1 + t] = f.x;
+            v[NB + t] = f.y;
+            v[NB + 1 + t] = f.z;
+            v[NB + 2 + t] = f.w;
+        }
+        const float wt = w[t];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) acc[i] = fmaf(wt, v[i + t], acc[i]);
+    }
+}
+
 // Tile gather with U independent loads in flight per thread: load(idx)
 // returns element idx of the tile (row-major in shared memory).  All U
 // loads of a round are issued before any shared-memory store, so a CTA keeps

@@ -307,31 +307,46 @@ static cudaError_t sep2d_t(const Sep2dArgs &a, cudaStream_t s)
 // =========================================================================
 // Fused 2-D separable kernel, persistent and fed by the Tensor Memory
 // Accelerator (FP32 compute; Float32 or 8-bit images whose rows meet the copy
-// engine's 16-byte rules).  Each CTA walks tiles blockIdx.x, +gridDim.x, ...
-// and keeps two input buffers: while tile k is filtered, the bulk copy of
-// tile k+1 (TX+kx-1 by TY+ky-1 inputs, x rounded down to the 16-byte
-// boundary) is in flight.  Tiles whose input window leaves the image are
-// gathered through the border map instead (same index arithmetic as
-// k_sep2d).  The passes are those of k_sep2d.
+// engine's 16-byte rules; factors of at most kCorrKmax taps).  Each CTA walks
+// tiles blockIdx.x, +gridDim.x, ...  The input buffer of a tile is free once
+// its first pass (or, for 8-bit codes, their conversion to values) has read
+// it: the bulk copy of the next tile (TX+kx-1 by TY+ky-1 inputs) is issued
+// then and lands while the second pass runs.  Tiles whose input window leaves
+// the image are gathered through the border map instead (same index
+// arithmetic as k_sep2d).
+//
+// Shared-memory layout keeps the row passes free of bank conflicts: the tile
+// grid is shifted so that every window starts on a 16-byte boundary,
+// row pitches are 4 mod 8 floats, and each 8-lane phase of a warp reads 4 rows
+// x 2 window starts with 16-byte loads.  The passes are those of k_sep2d
+// (cascade order, pass ranges); outputs of FP32 results widen exactly.
 // =========================================================================
-constexpr int kStTX = 64, kStTY = 64;
+constexpr int kStTX = 64, kStTY = 64, kStNB = 16;
 
 __host__ __device__ inline size_t st_round128(size_t b) { return (b + 127) & ~(size_t)127; }
+// smallest pitch >= n floats that is 4 mod 8
+__host__ __device__ inline int st_pitch(int n) { int p = (n + 3) & ~3; return (p & 7) ? p : p + 4; }
 
 struct SepTmaSmem {
+    int boxw;                   // TMA box width (elements) = row pitch of the input buffer
+    int st, si;                 // pitches of the 8-bit value tile and of the intermediate
     size_t raw, w, t, i, total;
 };
 
-__host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int boxw, int elt_bytes)
+__host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int x_first, int elt_bytes)
 {
     SepTmaSmem L;
     const int RV = kStTY + ky - 1, CV = kStTX + kx - 1;
-    L.raw = st_round128((size_t)boxw * RV * elt_bytes);
+    // Windows start on 16-byte boundaries.  Float32: 3 floats of slack for
+    // the 16-byte loads; 8-bit: codes are converted four at a time.
+    L.boxw = elt_bytes == 4 ? st_pitch(CV + 3) : (CV + 3 + 15) / 16 * 16;
+    L.st = st_pitch(CV + 3);
+    L.si = x_first ? st_pitch(kStTX) : st_pitch(CV + 3);
+    L.raw = st_round128((size_t)L.boxw * RV * elt_bytes);
     L.w = st_round128(2 * (IFX_MAX_TAPS + 3) * sizeof(float) + 256 * sizeof(float));
-    L.t = elt_bytes == 1 ? st_round128((size_t)RV * CV * sizeof(float)) : 0;
-    const size_t ix = (size_t)RV * kStTX, iy = (size_t)kStTY * CV;
-    L.i = st_round128((ix > iy ? ix : iy) * sizeof(float));
-    L.total = 2 * L.raw + L.w + L.t + L.i;
+    L.t = elt_bytes == 1 ? st_round128((size_t)RV * L.st * sizeof(float)) : 0;
+    L.i = st_round128((size_t)(x_first ? RV : kStTY) * L.si * sizeof(float));
+    L.total = L.raw + L.w + L.t + L.i;
     return L;
 }
 
@@ -339,19 +354,21 @@ template <class Tin, class Tout>
 __global__ void __launch_bounds__(256)
 k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img, Tout *__restrict__ out,
             int nx, int ny, int fx, int kx, int fy, int ky, int x_first, int style, float fill, bool norm,
-            int boxw, int tiles_x, int tiles, int *err, const __grid_constant__ Sep2dW<float> W)
+            int shift, int tiles_x, int tiles, int *err, const __grid_constant__ Sep2dW<float> W)
 {
-    constexpr int TX = kStTX, TY = kStTY, NB = kSepNB;
+    constexpr int TX = kStTX, TY = kStTY, NB = kStNB;
     constexpr int ALIGN = 16 / (int)sizeof(Tin);          // x granularity of a box start
     extern __shared__ __align__(128) unsigned char st_smem[];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar;
     const int RV = TY + ky - 1, CV = TX + kx - 1;
-    const SepTmaSmem L = sep_tma_smem(kx, ky, boxw, (int)sizeof(Tin));
-    float *wx = reinterpret_cast<float *>(st_smem + 2 * L.raw);
+    const SepTmaSmem L = sep_tma_smem(kx, ky, x_first, (int)sizeof(Tin));
+    const int boxw = L.boxw;
+    Tin *raw = reinterpret_cast<Tin *>(st_smem);
+    float *wx = reinterpret_cast<float *>(st_smem + L.raw);
     float *wy = wx + (IFX_MAX_TAPS + 3);
     float *lut = wy + (IFX_MAX_TAPS + 3);                   // 8-bit code -> value
-    float *T = reinterpret_cast<float *>(st_smem + 2 * L.raw + L.w);
-    float *I = reinterpret_cast<float *>(st_smem + 2 * L.raw + L.w + L.t);
+    float *T = reinterpret_cast<float *>(st_smem + L.raw + L.w);
+    float *I = reinterpret_cast<float *>(st_smem + L.raw + L.w + L.t);
     const int tid = threadIdx.x, nth = blockDim.x;
     const uint32_t box_bytes = (uint32_t)(boxw * RV * (int)sizeof(Tin));
     for (int t = tid; t < kx; t += nth) wx[t] = W.wx[t];
@@ -359,17 +376,16 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     if (sizeof(Tin) == 1)
         for (int c = tid; c < 256; c += nth) lut[c] = to_c<float>((uint8_t)c, norm);
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        mbar_init(&bar, 1);
         mbar_fence_init();
         tma_prefetch_map(&map);
     }
     __syncthreads();
 
-    auto raw = [&](int b) { return reinterpret_cast<Tin *>(st_smem + (size_t)b * L.raw); };
+    // tile t covers outputs x in [tx*TX - shift, +TX), y in [ty*TY, +TY)
     auto origin = [&](int t, int &px, int &py) {
         const int ty = t / tiles_x, tx = t - ty * tiles_x;
-        px = tx * TX + fx;
+        px = tx * TX - shift + fx;
         py = ty * TY + fy;
     };
     auto interior = [&](int t) {
@@ -377,60 +393,68 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         origin(t, px, py);
         return px >= 0 && px + CV <= nx && py >= 0 && py + RV <= ny;
     };
-    auto issue = [&](int t, int b) {          // thread 0 only
-        int px, py;
-        origin(t, px, py);
-        mbar_expect_tx(&bar[b], box_bytes);
-        tma_load_2d(raw(b), &map, px & ~(ALIGN - 1), py, &bar[b]);
+    // all threads call it (uniform); thread 0 issues the copy of tile t
+    uint32_t parity = 0;
+    bool pending = false;
+    auto prefetch = [&](int t) {
+        if (t < tiles && interior(t)) {
+            if (tid == 0) {
+                int px, py;
+                origin(t, px, py);
+                mbar_expect_tx(&bar, box_bytes);
+                tma_load_2d(raw, &map, px & ~(ALIGN - 1), py, &bar);
+            }
+            pending = true;
+        }
+    };
+    // row-pass item -> (row, window start): a warp covers 16 rows x 2 starts and
+    // each 8-lane phase 4 rows x 2 starts (conflict-free for pitches 4 mod 8)
+    auto row_item = [](int it, int &r, int &c0) {
+        const int lane = it & 31, grp = it >> 5;
+        r = 16 * (grp >> 1) + 4 * (lane >> 3) + ((lane >> 1) & 3);
+        c0 = NB * (2 * (grp & 1) + (lane & 1));
     };
 
-    uint32_t parity = 0;                      // bit b: phase awaited on bar[b]
-    uint32_t pending = 0;                     // bit b: a copy into raw(b) is in flight
     int t = blockIdx.x;
-    if (t < tiles && interior(t)) {
-        if (tid == 0) issue(t, 0);
-        pending |= 1u;
-    }
-    for (int k = 0; t < tiles; ++k, t += gridDim.x) {
-        const int b = k & 1;
+    prefetch(t);
+    for (; t < tiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
-        if (tn < tiles && interior(tn)) {     // prefetch the next tile into the other buffer
-            if (tid == 0) issue(tn, b ^ 1);
-            pending |= 2u >> b;               // bit b^1
-        }
         int px, py;
         origin(t, px, py);
         const float *P;
         int SP;
-        if (pending & (1u << b)) {
-            const bool ok = mbar_wait_bounded(&bar[b], (parity >> b) & 1u);
-            parity ^= 1u << b;
-            pending &= ~(1u << b);
+        if (pending) {
+            const uint32_t ph = parity;
+            const bool ok = mbar_wait_bounded(&bar, ph);
+            parity ^= 1u;
+            pending = false;
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
                     atomicExch(err, 1);
-                    if (pending & (2u >> b)) mbar_wait_bounded(&bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
+                    mbar_wait_bounded(&bar, ph);   // the copy may still land: give it time
                 }
                 return;
             }
-            const int dx = px & (ALIGN - 1);
             if (sizeof(Tin) == 4) {
-                P = reinterpret_cast<const float *>(raw(b)) + dx;
+                P = reinterpret_cast<const float *>(raw);       // window starts aligned
                 SP = boxw;
             } else {
-                const uint8_t *R = reinterpret_cast<const uint8_t *>(raw(b));
-                for (int idx = tid; idx < RV * CV; idx += nth) {
-                    const int r = idx / CV, c = idx - r * CV;
-                    T[idx] = lut[R[r * boxw + dx + c]];
+                // codes -> values, four per thread (the box starts at the window)
+                const int q4 = (CV + 3) >> 2;
+                for (int idx = tid; idx < RV * q4; idx += nth) {
+                    const int r = idx / q4, c = 4 * (idx - r * q4);
+                    const uint32_t w4 = *reinterpret_cast<const uint32_t *>(
+                        reinterpret_cast<const uint8_t *>(raw) + r * boxw + c);
+                    *reinterpret_cast<float4 *>(T + r * L.st + c) =
+                        make_float4(lut[w4 & 0xFF], lut[(w4 >> 8) & 0xFF], lut[(w4 >> 16) & 0xFF], lut[w4 >> 24]);
                 }
-                __syncthreads();
                 P = T;
-                SP = CV;
+                SP = L.st;
             }
         } else {
             // border tile: gather through the border map
-            float *G = sizeof(Tin) == 4 ? reinterpret_cast<float *>(raw(b)) : T;
-            const int SG = sizeof(Tin) == 4 ? boxw : CV;
+            float *G = sizeof(Tin) == 4 ? reinterpret_cast<float *>(raw) : T;
+            const int SG = sizeof(Tin) == 4 ? boxw : L.st;
             gather_tile<8>(G, RV * SG, [&](int idx) -> float {
                 const int r = idx / SG, c = idx - r * SG;
                 if (c >= CV) return 0.0f;
@@ -438,27 +462,36 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 const int my = map_index(py + r, ny, style);
                 return (mx < 0 || my < 0) ? fill : cvt<float, Tin>(img[(long long)my * nx + mx], norm);
             });
-            __syncthreads();
             P = G;
             SP = SG;
         }
+        fence_proxy_async();
+        __syncthreads();
+        if (sizeof(Tin) == 1) prefetch(tn);        // the codes are converted: raw is free
 
         const int tx0 = px - fx, ty0 = py - fy;
         float acc[NB];
         if (x_first) {
-            const int segs = TX / NB;
-            for (int it = tid; it < RV * segs; it += nth) {
-                const int r = it / segs, c0 = (it - r * segs) * NB;
-                corr_run<float, NB>(P + (size_t)r * SP + c0, 1, wx, kx, acc);
+            // x pass over all RV rows -> I (pitch si)
+            for (int it = tid; it < ((RV + 15) & ~15) * (TX / NB); it += nth) {
+                int r, c0;
+                row_item(it, r, c0);
+                if (r >= RV) continue;
+                corr_row4<NB>(P + (size_t)r * SP + c0, wx, kx, acc);
+                float4 *d = reinterpret_cast<float4 *>(I + (size_t)r * L.si + c0);
 #pragma unroll
-                for (int i = 0; i < NB; ++i) I[(size_t)r * TX + c0 + i] = acc[i];
+                for (int q = 0; q < NB / 4; ++q)
+                    d[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
             }
+            fence_proxy_async();
             __syncthreads();
+            if (sizeof(Tin) == 4) prefetch(tn);    // the first pass has read raw
+            // y pass down each column, NB rows per item
             for (int it = tid; it < TX * (TY / NB); it += nth) {
                 const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
-                corr_run<float, NB>(I + (size_t)r0 * TX + c, TX, wy, ky, acc);
+                corr_col<NB>(I + (size_t)r0 * L.si + c, L.si, wy, ky, acc);
                 const int x = tx0 + c;
-                if (x < nx) {
+                if (x >= 0 && x < nx) {
 #pragma unroll
                     for (int i = 0; i < NB; ++i) {
                         const int y = ty0 + r0 + i;
@@ -467,30 +500,32 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 }
             }
         } else {
+            // y pass down each of the CV columns -> I (TY rows, pitch si)
             for (int it = tid; it < CV * (TY / NB); it += nth) {
                 const int rs = it / CV, c = it - rs * CV, r0 = rs * NB;
-                corr_run<float, NB>(P + (size_t)r0 * SP + c, SP, wy, ky, acc);
+                corr_col<NB>(P + (size_t)r0 * SP + c, SP, wy, ky, acc);
 #pragma unroll
-                for (int i = 0; i < NB; ++i) I[(size_t)(r0 + i) * CV + c] = acc[i];
+                for (int i = 0; i < NB; ++i) I[(size_t)(r0 + i) * L.si + c] = acc[i];
             }
+            fence_proxy_async();
             __syncthreads();
-            const int segs = TX / NB;
-            for (int it = tid; it < TY * segs; it += nth) {
-                const int r = it / segs, c0 = (it - r * segs) * NB;
-                corr_run<float, NB>(I + (size_t)r * CV + c0, 1, wx, kx, acc);
+            if (sizeof(Tin) == 4) prefetch(tn);    // the first pass has read raw
+            // x pass along the TY rows
+            for (int it = tid; it < TY * (TX / NB); it += nth) {
+                int r, c0;
+                row_item(it, r, c0);
+                corr_row4<NB>(I + (size_t)r * L.si + c0, wx, kx, acc);
                 const int y = ty0 + r;
                 if (y < ny) {
 #pragma unroll
                     for (int i = 0; i < NB; ++i) {
                         const int x = tx0 + c0 + i;
-                        if (x < nx) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
+                        if (x >= 0 && x < nx) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
                     }
                 }
             }
         }
-        // raw(b), T and I are rewritten by the next rounds (the bulk copy
-        // engine among the writers)
-        fence_proxy_async();
+        // I and T are rewritten by the next round
         __syncthreads();
     }
 }
@@ -498,15 +533,13 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
 template <class Tin, class Tout>
 static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
 {
-    constexpr int ALIGN = 16 / (int)sizeof(Tin);
-    const int CV = kStTX + a.kx - 1, RV = kStTY + a.ky - 1;
-    const int boxw = (CV + ALIGN - 1 + ALIGN - 1) / ALIGN * ALIGN;
-    if (boxw > 256 || RV > 256) return false;
-    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, boxw, (int)sizeof(Tin));
-    if (L.total > 160 * 1024) return false;
+    if (a.kx > kCorrKmax || a.ky > kCorrKmax) return false;
+    const int RV = kStTY + a.ky - 1;
+    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin));
+    if (L.boxw > 256 || RV > 256 || L.total > 160 * 1024) return false;
     CUtensorMap map;
     if (!tma_encode_2d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, (long long)a.nx * (long long)sizeof(Tin),
-                       boxw, RV))
+                       L.boxw, RV))
         return false;
     int dev = 0;
     if ((*e = cudaGetDevice(&dev)) != cudaSuccess) return true;
@@ -527,13 +560,16 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, L.total) != cudaSuccess || per_sm < 1)
         per_sm = 1;
-    const int tiles_x = (a.nx + kStTX - 1) / kStTX;
+    // tiles shift left so that tile windows start on 16-byte boundaries
+    constexpr int ALIGN = 16 / (int)sizeof(Tin);
+    const int shift = ((a.fx % ALIGN) + ALIGN) % ALIGN;
+    const int tiles_x = (a.nx + shift + kStTX - 1) / kStTX;
     const long long tiles = (long long)tiles_x * ((a.ny + kStTY - 1) / kStTY);
     if (tiles > (1ll << 30)) return false;
     const long long slots = (long long)sms * per_sm;
     const int grid = (int)(tiles < slots ? tiles : slots);
     kern<<<grid, 256, L.total, s>>>(map, (const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.fx, a.kx, a.fy,
-                                    a.ky, a.x_first, a.style, (float)a.fill, a.in_type == IFX_N0F8, boxw,
+                                    a.ky, a.x_first, a.style, (float)a.fill, a.in_type == IFX_N0F8, shift,
                                     tiles_x, (int)tiles, err, W);
     note_launch();
     *e = cudaGetLastError();
