@@ -23,6 +23,8 @@
 // tile is gathered.
 #include "ifx_internal.h"
 #include "ifx_select.cuh"
+#include "ifx_tma.cuh"
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -34,7 +36,7 @@ constexpr int kBatchMaxTaps = 36;     // factor taps (<= 33) rounded up to 4
 struct BReq {
     int op, in_type, out_type, style;
     int nx, ny, tiles_x, win;
-    long long tile_base;
+    long long tile_base, tile_end;    // this request's tiles: [tile_base, tile_end)
     const void *in;
     void *out0;
     void *out1;
@@ -67,25 +69,6 @@ __host__ __device__ inline int bt_tile_h(int op, int in_type)
 {
     if (op == BOP_MEDIAN) return (in_type == IFX_F32) ? kMFY : kMUY;
     return kFTY;
-}
-
-__device__ __forceinline__ float bt_load(const BReq &R, int x, int y)
-{
-    const int mx = map_index(x, R.nx, R.style);
-    const int my = map_index(y, R.ny, R.style);
-    if (mx < 0 || my < 0) return R.fill;
-    const long long o = (long long)my * R.nx + mx;
-    if (R.in_type == IFX_F32) return ((const float *)R.in)[o];
-    const uint8_t c = ((const uint8_t *)R.in)[o];
-    return R.in_type == IFX_N0F8 ? __fdiv_rn((float)c, 255.0f) : (float)c;
-}
-
-__device__ __forceinline__ void bt_store(const BReq &R, void *out, int x, int y, float v)
-{
-    if (x >= R.nx || y >= R.ny) return;
-    const long long o = (long long)y * R.nx + x;
-    if (R.out_type == IFX_F64) ((double *)out)[o] = (double)v;
-    else ((float *)out)[o] = v;
 }
 
 // Division-free 2-D gather of a tile whose element (r, c) is load(r, c): warps
@@ -122,107 +105,195 @@ __device__ __forceinline__ void gather2d(T *dst, int rows, int cols, int pitch, 
 // N0f8 codes as Float32 (c/255 correctly rounded), one table per CTA.
 __shared__ float s_n0f8[256];
 
-// Gather the (rows x cols) float tile whose element (r, c) is the image value
-// at (ox + c, oy + r) through the border map; columns >= cv are zero.  Tiles
-// whose source box lies inside the image skip the map; the element type
-// branch is taken once per tile.
-__device__ __forceinline__ void bt_gather_f(const BReq &R, float *T, int rows, int cols, int pitch,
-                                            int cv, int ox, int oy)
+// ---------------------------------------------------------------- staging
+// A tile's input window (rows x cols elements from image position (ox, oy))
+// is staged raw -- Float32 values or 8-bit codes -- in a shared buffer of
+// kStagePitch-byte rows: element (r, c) sits at byte r*kStagePitch + lead[r] +
+// c*elt.  Interior windows arrive by one bulk copy per row (the row's 16-byte
+// aligned superset; lead[r] is the row start's offset in it), issued one tile
+// ahead so the copies land while the previous tile computes.  Windows that
+// leave the image are gathered through the border map (lead 0).
+constexpr int kStageRows = kFTY + 32;                  // factored with 33 taps
+constexpr int kStagePitch = 400;                       // >= 15 + (64 + 32) * 4, multiple of 16
+constexpr int kStageBytes = kStageRows * kStagePitch;
+constexpr int kIPitch = kFTX + 4;                      // factored intermediate (floats)
+
+struct TileGeo {
+    int ox, oy, rows, cols, elt;
+};
+
+__device__ __forceinline__ TileGeo bt_geo(const BReq &R, int tx0, int ty0)
 {
-    const bool inside = ox >= 0 && oy >= 0 && ox + cv <= R.nx && oy + rows <= R.ny;
-    const int nx = R.nx;
-    if (R.in_type == IFX_F32) {
-        const float *img = (const float *)R.in;
-        if (inside)
-            gather2d<float>(T, rows, cols, pitch, [&](int r, int c) -> float {
-                return c < cv ? img[(long long)(oy + r) * nx + ox + c] : 0.0f;
-            });
-        else
-            gather2d<float>(T, rows, cols, pitch, [&](int r, int c) -> float {
-                if (c >= cv) return 0.0f;
-                const int mx = map_index(ox + c, nx, R.style), my = map_index(oy + r, R.ny, R.style);
-                return (mx < 0 || my < 0) ? R.fill : img[(long long)my * nx + mx];
-            });
-    } else {
-        const uint8_t *img = (const uint8_t *)R.in;
-        const bool norm = R.in_type == IFX_N0F8;
-        if (inside)
-            gather2d<float>(T, rows, cols, pitch, [&](int r, int c) -> float {
-                if (c >= cv) return 0.0f;
-                const uint8_t v = img[(long long)(oy + r) * nx + ox + c];
-                return norm ? s_n0f8[v] : (float)v;
-            });
-        else
-            gather2d<float>(T, rows, cols, pitch, [&](int r, int c) -> float {
-                if (c >= cv) return 0.0f;
-                const int mx = map_index(ox + c, nx, R.style), my = map_index(oy + r, R.ny, R.style);
-                if (mx < 0 || my < 0) return R.fill;
-                const uint8_t v = img[(long long)my * nx + mx];
-                return norm ? s_n0f8[v] : (float)v;
-            });
+    const int elt = R.in_type == IFX_F32 ? 4 : 1;
+    switch (R.op) {
+    case BOP_FACTORED: return {tx0 + R.fx, ty0 + R.fy, kFTY + R.ky - 1, kFTX + R.kx - 1, elt};
+    case BOP_GRADIENTS:
+    case BOP_LAPLACIAN: return {tx0 - 1, ty0 - 1, kFTY + 2, kFTX + 2, elt};
+    default: {
+        const int h = R.win / 2;
+        if (elt == 4) return {tx0 - h, ty0 - h, kMFY + R.win - 1, kMFX + R.win - 1, 4};
+        return {tx0 - h, ty0 - h, kMUY + R.win - 1, kMUX + R.win - 1, 1};
+    }
     }
 }
 
+// The window lies in the image and every row's aligned superset lies in the
+// image's bytes (the base is 16-byte aligned).
+__device__ __forceinline__ bool bt_bulk_ok(const BReq &R, const TileGeo &g)
+{
+    if (((uintptr_t)R.in & 15) || g.ox < 0 || g.oy < 0 || g.ox + g.cols > R.nx || g.oy + g.rows > R.ny)
+        return false;
+    const long long last = ((long long)(g.oy + g.rows - 1) * R.nx + g.ox) * g.elt;
+    const long long end = (last & ~15ll) + (((last & 15) + (long long)g.cols * g.elt + 15) & ~15ll);
+    return end <= (long long)R.nx * R.ny * g.elt;
+}
+
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(dst)), "l"((uint64_t)src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+// Warp 0: one bulk copy per row into `st`, all completing on *bar.
+__device__ __forceinline__ void bt_issue_rows(const BReq &R, const TileGeo &g, unsigned char *st,
+                                              unsigned char *lead, uint64_t *bar)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t total = 0;
+    for (int r = lane; r < g.rows; r += 32) {
+        const long long off = ((long long)(g.oy + r) * R.nx + g.ox) * g.elt;
+        const uint32_t ld = (uint32_t)(off & 15);
+        total += (ld + (uint32_t)g.cols * g.elt + 15) & ~15u;
+        lead[r] = (unsigned char)ld;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+    if (lane == 0) mbar_expect_tx(bar, total);
+    __syncwarp();
+    for (int r = lane; r < g.rows; r += 32) {
+        const long long off = ((long long)(g.oy + r) * R.nx + g.ox) * g.elt;
+        const uint32_t ld = (uint32_t)(off & 15);
+        bulk_copy(st + r * kStagePitch, (const unsigned char *)R.in + (off - ld),
+                  (ld + (uint32_t)g.cols * g.elt + 15) & ~15u, bar);
+    }
+}
+
+// All threads: raw window through the border map (lead 0).
+__device__ __forceinline__ void bt_gather_raw(const BReq &R, const TileGeo &g, unsigned char *st,
+                                              unsigned char *lead)
+{
+    for (int r = threadIdx.x; r < g.rows; r += blockDim.x) lead[r] = 0;
+    const int nx = R.nx, ny = R.ny, style = R.style;
+    if (g.elt == 4) {
+        const float *img = (const float *)R.in;
+        gather2d<float>(reinterpret_cast<float *>(st), g.rows, g.cols, kStagePitch / 4,
+                        [&](int r, int c) -> float {
+                            const int mx = map_index(g.ox + c, nx, style), my = map_index(g.oy + r, ny, style);
+                            return (mx < 0 || my < 0) ? R.fill : img[(long long)my * nx + mx];
+                        });
+    } else {
+        const uint8_t *img = (const uint8_t *)R.in;
+        gather2d<uint8_t>(st, g.rows, g.cols, kStagePitch, [&](int r, int c) -> uint8_t {
+            const int mx = map_index(g.ox + c, nx, style), my = map_index(g.oy + r, ny, style);
+            return (mx < 0 || my < 0) ? (uint8_t)R.fill_code : img[(long long)my * nx + mx];
+        });
+    }
+}
+
+// Value of staged element (r, c) in the compute domain.
+struct Staged {
+    const unsigned char *st;
+    const unsigned char *lead;
+    bool f32, norm;
+    __device__ __forceinline__ const unsigned char *row(int r) const { return st + r * kStagePitch + lead[r]; }
+    __device__ __forceinline__ float at(int r, int c) const
+    {
+        if (f32) return reinterpret_cast<const float *>(row(r))[c];
+        const uint8_t v = row(r)[c];
+        return norm ? s_n0f8[v] : (float)v;
+    }
+};
+
+__device__ __forceinline__ void bt_store(const BReq &R, void *out, int x, int y, float v)
+{
+    if (x >= R.nx || y >= R.ny) return;
+    const long long o = (long long)y * R.nx + x;
+    if (R.out_type == IFX_F64) ((double *)out)[o] = f32_to_f64(v);
+    else ((float *)out)[o] = v;
+}
+
 // ---------------------------------------------------------------- factored
-__device__ void bt_factored(const BReq &R, int tx0, int ty0, float *sm)
+// acc[i] = sum_{t<k} w[t] src(i+t), i < NB, the window read through `at`.
+template <int NB, class F>
+__device__ __forceinline__ void corr_fn(F at, const float *w, int k, float *acc)
+{
+    float v[NB + kCorrKmax - 1];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        v[i] = at(i);
+        acc[i] = 0.0f;
+    }
+#pragma unroll
+    for (int t = 0; t < kCorrKmax; ++t) {
+        if (t >= k) break;
+        if (t > 0) v[NB - 1 + t] = at(NB - 1 + t);
+        const float wt = w[t];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) acc[i] = fmaf(wt, v[i + t], acc[i]);
+    }
+}
+
+__device__ void bt_factored(const BReq &R, int tx0, int ty0, const Staged &S, float *I)
 {
     constexpr int TX = kFTX, TY = kFTY, NB = 8;
-    const int kx = R.kx, ky = R.ky, kx4 = up4(kx), ky4 = up4(ky);
-    float *wx = sm, *wy = sm + kBatchMaxTaps, *T = sm + 2 * kBatchMaxTaps;
-    const int RT = TY + ky - 1, CT = TX + kx4, CV = TX + kx - 1;
-    float *I = T + RT * CT;
+    const int kx = R.kx, ky = R.ky, rows = TY + ky - 1;
     const int tid = threadIdx.x, nth = blockDim.x;
-    if (tid < kx) wx[tid] = R.wx[tid];
-    if (tid < ky) wy[tid] = R.wy[tid];
-    bt_gather_f(R, T, RT, CT, CT, CV, tx0 + R.fx, ty0 + R.fy);
-    __syncthreads();
     float acc[NB];
-    const int segs = TX / NB;
-    for (int it = tid; it < RT * segs; it += nth) {
-        const int r = it / segs, c0 = (it - r * segs) * NB;
-        corr_run<float, NB>(T + r * CT + c0, 1, wx, kx, acc);
+    // x pass over all rows (the y halo) -> I
+    for (int it = tid; it < rows * (TX / NB); it += nth) {
+        const int r = it >> 3, c0 = (it & 7) * NB;
+        if (S.f32) {
+            const float *p = reinterpret_cast<const float *>(S.row(r)) + c0;
+            corr_fn<NB>([&](int j) { return p[j]; }, R.wx, kx, acc);
+        } else {
+            const uint8_t *p = S.row(r) + c0;
+            if (S.norm) corr_fn<NB>([&](int j) { return s_n0f8[p[j]]; }, R.wx, kx, acc);
+            else corr_fn<NB>([&](int j) { return (float)p[j]; }, R.wx, kx, acc);
+        }
 #pragma unroll
-        for (int i = 0; i < NB; ++i) I[r * TX + c0 + i] = acc[i];
+        for (int i = 0; i < NB; ++i) I[r * kIPitch + c0 + i] = acc[i];
     }
-    (void)ky4;
     __syncthreads();
+    // y pass down each column
     for (int it = tid; it < TX * (TY / NB); it += nth) {
         const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
-        corr_run<float, NB>(I + r0 * TX + c, TX, wy, ky, acc);
+        corr_col<NB>(I + r0 * kIPitch + c, kIPitch, R.wy, ky, acc);
 #pragma unroll
         for (int i = 0; i < NB; ++i) bt_store(R, R.out0, tx0 + c, ty0 + r0 + i, acc[i]);
     }
 }
 
-__host__ __device__ inline int bt_factored_smem_floats(int kx, int ky)
-{
-    return 2 * kBatchMaxTaps + (kFTY + ky - 1) * (kFTX + up4(kx)) + (kFTY + ky - 1) * kFTX;
-}
-
 // ---------------------------------------------------------------- gradients
-// out0 = smooth_y(deriv_x), out1 = deriv_y(smooth_x) over a halo-1 tile.
-__device__ void bt_gradients(const BReq &R, int tx0, int ty0, float *sm)
+// out0 = smooth_y(deriv_x), out1 = deriv_y(smooth_x) over a halo-1 window.
+__device__ void bt_gradients(const BReq &R, int tx0, int ty0, const Staged &S)
 {
-    constexpr int TX = kFTX, TY = kFTY, NB = 8, CT = TX + 2, RT = TY + 2;
-    float *T = sm;
+    constexpr int TX = kFTX, TY = kFTY, NB = 8;
     const int tid = threadIdx.x, nth = blockDim.x;
-    bt_gather_f(R, T, RT, CT, CT, CT, tx0 - 1, ty0 - 1);
-    __syncthreads();
     const float d0 = R.wx[0], d1 = R.wx[1], d2 = R.wx[2];
     const float s0 = R.wy[0], s1 = R.wy[1], s2 = R.wy[2];
     for (int it = tid; it < TX * (TY / NB); it += nth) {
         const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
-        float D[NB + 2], S[NB + 2];
+        float D[NB + 2], Sm[NB + 2];
 #pragma unroll
         for (int j = 0; j < NB + 2; ++j) {
-            const float *row = T + (r0 + j) * CT + c;
-            D[j] = fmaf(d2, row[2], fmaf(d1, row[1], d0 * row[0]));
-            S[j] = fmaf(s2, row[2], fmaf(s1, row[1], s0 * row[0]));
+            const float a0 = S.at(r0 + j, c), a1 = S.at(r0 + j, c + 1), a2 = S.at(r0 + j, c + 2);
+            D[j] = fmaf(d2, a2, fmaf(d1, a1, d0 * a0));
+            Sm[j] = fmaf(s2, a2, fmaf(s1, a1, s0 * a0));
         }
 #pragma unroll
         for (int i = 0; i < NB; ++i) {
             const float g0 = fmaf(s2, D[i + 2], fmaf(s1, D[i + 1], s0 * D[i]));
-            const float g1 = fmaf(d2, S[i + 2], fmaf(d1, S[i + 1], d0 * S[i]));
+            const float g1 = fmaf(d2, Sm[i + 2], fmaf(d1, Sm[i + 1], d0 * Sm[i]));
             bt_store(R, R.out0, tx0 + c, ty0 + r0 + i, g0);
             bt_store(R, R.out1, tx0 + c, ty0 + r0 + i, g1);
         }
@@ -230,22 +301,30 @@ __device__ void bt_gradients(const BReq &R, int tx0, int ty0, float *sm)
 }
 
 // ---------------------------------------------------------------- laplacian
-__device__ void bt_laplacian(const BReq &R, int tx0, int ty0, float *sm)
+// Kernel.Laplacian((true,true)) in the reference's operation order.
+__device__ void bt_laplacian(const BReq &R, int tx0, int ty0, const Staged &S)
 {
-    constexpr int TX = kFTX, TY = kFTY, CT = TX + 2, RT = TY + 2;
-    float *T = sm;
+    constexpr int TX = kFTX, TY = kFTY, NB = 8;
     const int tid = threadIdx.x, nth = blockDim.x;
-    bt_gather_f(R, T, RT, CT, CT, CT, tx0 - 1, ty0 - 1);
-    __syncthreads();
-    for (int it = tid; it < TX * TY; it += nth) {
-        const int r = it / TX, c = it - r * TX;
-        const float *p = T + (r + 1) * CT + (c + 1);
-        float tmp = __fmul_rn(-4.0f, p[0]);
-        tmp = __fadd_rn(tmp, p[1]);
-        tmp = __fadd_rn(tmp, p[-1]);
-        tmp = __fadd_rn(tmp, p[CT]);
-        tmp = __fadd_rn(tmp, p[-CT]);
-        bt_store(R, R.out0, tx0 + c, ty0 + r, tmp);
+    for (int it = tid; it < TX * (TY / NB); it += nth) {
+        const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
+        float col[NB + 2], lft[NB], rgt[NB];
+#pragma unroll
+        for (int j = 0; j < NB + 2; ++j) col[j] = S.at(r0 + j, c + 1);
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            lft[i] = S.at(r0 + 1 + i, c);
+            rgt[i] = S.at(r0 + 1 + i, c + 2);
+        }
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            float tmp = __fmul_rn(-4.0f, col[i + 1]);
+            tmp = __fadd_rn(tmp, rgt[i]);
+            tmp = __fadd_rn(tmp, lft[i]);
+            tmp = __fadd_rn(tmp, col[i + 2]);
+            tmp = __fadd_rn(tmp, col[i]);
+            bt_store(R, R.out0, tx0 + c, ty0 + r0 + i, tmp);
+        }
     }
 }
 
@@ -263,20 +342,11 @@ __device__ __forceinline__ int bt_win_index(const BReq &R, int x, int y, int i, 
 }
 
 template <int W>
-__device__ void bt_median_u8(const BReq &R, int tx0, int ty0, uint8_t *tile)
+__device__ void bt_median_u8(const BReq &R, int tx0, int ty0, const Staged &S)
 {
-    constexpr int CT = ((kMUX + W - 1 + 3) & ~3) + 4, RT = kMUY + W - 1, h = W / 2;
-    gather2d<uint8_t>(tile, RT, CT, CT, [&](int r, int c) -> uint8_t {
-        if (c >= kMUX + W - 1) return 0;
-        const int mx = map_index(tx0 - h + c, R.nx, R.style);
-        const int my = map_index(ty0 - h + r, R.ny, R.style);
-        return (mx < 0 || my < 0) ? (uint8_t)R.fill_code
-                                  : ((const uint8_t *)R.in)[(long long)my * R.nx + mx];
-    });
-    __syncthreads();
+    constexpr int h = W / 2;
     const int tid = threadIdx.x;
     const int lx = (tid & 31) * 4;
-    const uint32_t rank4 = 0x01010101u * (uint32_t)((W * W + 1) / 2);
     const bool norm = R.in_type == IFX_N0F8;
     for (int ly = tid >> 5; ly < kMUY; ly += blockDim.x >> 5) {
         const int x0 = tx0 + lx, y = ty0 + ly;
@@ -286,9 +356,12 @@ __device__ void bt_median_u8(const BReq &R, int tx0, int ty0, uint8_t *tile)
                           (x0 < h || x0 + 3 >= R.nx - h || y < h || y >= R.ny - h);
         if (!edge) {
 #pragma unroll
-            for (int j = 0; j < W; ++j)
+            for (int j = 0; j < W; ++j) {
+                const unsigned char *base = S.st + (ly + j) * kStagePitch;
+                const int l = S.lead[ly + j];
 #pragma unroll
-                for (int i = 0; i < W; ++i) w[j * W + i] = load_word(tile + (ly + j) * CT, lx + i);
+                for (int i = 0; i < W; ++i) w[j * W + i] = load_word(base, l + lx + i);
+            }
         } else {
             const uint8_t *img = (const uint8_t *)R.in;
 #pragma unroll
@@ -304,35 +377,20 @@ __device__ void bt_median_u8(const BReq &R, int tx0, int ty0, uint8_t *tile)
                     w[j * W + i] = word;
                 }
         }
-        uint32_t res = 0;
-#pragma unroll
-        for (int b = 7; b >= 0; --b) {
-            const uint32_t trial = res | (0x01010101u << b);
-            uint32_t cnt = 0;
-#pragma unroll
-            for (int k = 0; k < W * W; ++k) cnt = count_lt(cnt, w[k], trial);
-            const uint32_t below = __vcmpltu4(cnt, rank4);
-            res = (trial & below) | (res & ~below);
-        }
+        const uint32_t res = median_u8x4<W * W>(w);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const uint8_t code = (uint8_t)(res >> (8 * q));
-            bt_store(R, R.out0, x0 + q, y, norm ? __fdiv_rn((float)code, 255.0f) : (float)code);
+            bt_store(R, R.out0, x0 + q, y, norm ? s_n0f8[code] : (float)code);
         }
     }
 }
 
 template <int W>
-__device__ void bt_median_f32(const BReq &R, int tx0, int ty0, float *tile)
+__device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Staged &S)
 {
     using SK = SortKey<float>;
-    constexpr int CT = kMFX + W - 1, RT = kMFY + W - 1, h = W / 2, N = W * W;
-    gather2d<float>(tile, RT, CT, CT, [&](int r, int c) -> float {
-        const int mx = map_index(tx0 - h + c, R.nx, R.style);
-        const int my = map_index(ty0 - h + r, R.ny, R.style);
-        return (mx < 0 || my < 0) ? R.fill : ((const float *)R.in)[(long long)my * R.nx + mx];
-    });
-    __syncthreads();
+    constexpr int h = W / 2, N = W * W;
     for (int p = threadIdx.x; p < kMFX * kMFY; p += blockDim.x) {
         const int lx = p % kMFX, ly = p / kMFX, x = tx0 + lx, y = ty0 + ly;
         if (x >= R.nx || y >= R.ny) continue;
@@ -340,9 +398,11 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, float *tile)
         uint32_t v[N];
         if (!edge) {
 #pragma unroll
-            for (int j = 0; j < W; ++j)
+            for (int j = 0; j < W; ++j) {
+                const float *rowp = reinterpret_cast<const float *>(S.row(ly + j));
 #pragma unroll
-                for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(tile[(ly + j) * CT + lx + i]);
+                for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(rowp[lx + i]);
+            }
         } else {
             const float *img = (const float *)R.in;
 #pragma unroll
@@ -356,76 +416,131 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, float *tile)
 }
 
 // ---------------------------------------------------------------- the kernel
-constexpr int kReqTable = 2048;      // requests whose first tiles are searched in shared memory
+constexpr int kReqTable = 1024;      // requests whose first tiles are searched in shared memory
 
 __global__ void __launch_bounds__(256, 3)
-k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter)
+k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int *err)
 {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ long long s_tile;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ long long s_tile[2];
     __shared__ int s_base[kReqTable];
-    __shared__ __align__(16) BReq s_req;
+    __shared__ __align__(16) BReq s_req[2];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ unsigned char s_lead[2][kStageRows];
     const BHdr *hdr = reinterpret_cast<const BHdr *>(desc);
     const BReq *reqs = reinterpret_cast<const BReq *>(desc + sizeof(BHdr));
     const long long total = hdr->total_tiles;
     const int nreq = hdr->nreq;
     const int ntab = nreq < kReqTable ? nreq : kReqTable;
-    for (int i = threadIdx.x; i < ntab; i += blockDim.x) s_base[i] = (int)reqs[i].tile_base;
-    s_n0f8[threadIdx.x & 255] = __fdiv_rn((float)(threadIdx.x & 255), 255.0f);
-    long long next = 0;
-    if (threadIdx.x == 0) next = (long long)atomicAdd(counter, 1ULL);
-    for (;;) {
-        if (threadIdx.x == 0) {
-            s_tile = next;
-            next = (long long)atomicAdd(counter, 1ULL);   // in flight while this tile runs
-        }
-        __syncthreads();
-        const long long t = s_tile;
-        if (t >= total) break;
-        // owning request: binary search over first tiles (shared table, then global)
-        int lo = 0, hi = ntab - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_base[mid] <= t) lo = mid;
-            else hi = mid - 1;
-        }
-        if (lo == kReqTable - 1 && nreq > kReqTable) {
-            hi = nreq - 1;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    float *I = reinterpret_cast<float *>(smem + 2 * kStageBytes);
+    for (int i = tid; i < ntab; i += blockDim.x) s_base[i] = (int)reqs[i].tile_base;
+    s_n0f8[tid & 255] = __fdiv_rn((float)(tid & 255), 255.0f);
+    long long ahead = 0;                 // thread 0: the tile after the next one
+    if (tid == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+        mbar_fence_init();
+        s_tile[0] = (long long)atomicAdd(counter, 1ULL);
+        ahead = (long long)atomicAdd(counter, 1ULL);
+    }
+    __syncthreads();
+
+    uint32_t bulk = 0, parity = 0;       // per buffer: copies in flight / phase awaited
+    bool have_req[2] = {false, false};   // s_req[b] holds a descriptor
+    // Looks tile t up, stages its descriptor in s_req[b] and, for an interior
+    // window, issues its row copies into buffer b.  Called by all threads.
+    // Consecutive tiles mostly belong to one request: then the descriptor is
+    // copied from the other buffer instead of searched for and fetched.
+    auto prepare = [&](int b, long long t) {
+        if (t >= total) return;
+        const int *src;
+        if (have_req[b ^ 1] && t >= s_req[b ^ 1].tile_base && t < s_req[b ^ 1].tile_end) {
+            src = reinterpret_cast<const int *>(&s_req[b ^ 1]);
+        } else {
+            int lo = 0, hi = ntab - 1;
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
-                if (reqs[mid].tile_base <= t) lo = mid;
+                if (s_base[mid] <= t) lo = mid;
                 else hi = mid - 1;
             }
+            if (lo == kReqTable - 1 && nreq > kReqTable) {
+                hi = nreq - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (reqs[mid].tile_base <= t) lo = mid;
+                    else hi = mid - 1;
+                }
+            }
+            src = reinterpret_cast<const int *>(reqs + lo);
         }
-        {   // the descriptor, one word per thread
-            const int *src = reinterpret_cast<const int *>(reqs + lo);
-            int *dst = reinterpret_cast<int *>(&s_req);
-            for (int i = threadIdx.x; i < (int)(sizeof(BReq) / 4); i += blockDim.x) dst[i] = src[i];
-        }
+        int *dst = reinterpret_cast<int *>(&s_req[b]);
+        for (int i = tid; i < (int)(sizeof(BReq) / 4); i += blockDim.x) dst[i] = src[i];
+        have_req[b] = true;
         __syncthreads();
-        const BReq &R = s_req;
+        const BReq &R = s_req[b];
         const int local = (int)(t - R.tile_base);
         const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
-        const int tw = bt_tile_w(R.op, R.in_type), th = bt_tile_h(R.op, R.in_type);
-        const int tx0 = bx * tw, ty0 = by * th;
+        const TileGeo g = bt_geo(R, bx * bt_tile_w(R.op, R.in_type), by * bt_tile_h(R.op, R.in_type));
+        if (bt_bulk_ok(R, g)) {
+            if (warp == 0) bt_issue_rows(R, g, smem + b * kStageBytes, s_lead[b], &s_bar[b]);
+            bulk |= 1u << b;
+        }
+    };
+
+    prepare(0, s_tile[0]);
+    for (int k = 0;; ++k) {
+        const int b = k & 1;
+        const long long t = s_tile[b];
+        if (t >= total) break;
+        if (tid == 0) {                        // the counter's latency hides behind a tile
+            s_tile[b ^ 1] = ahead;
+            ahead = (long long)atomicAdd(counter, 1ULL);
+        }
+        __syncthreads();
+        prepare(b ^ 1, s_tile[b ^ 1]);         // its copies land while this tile runs
+
+        const BReq &R = s_req[b];
+        const int local = (int)(t - R.tile_base);
+        const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
+        const int tx0 = bx * bt_tile_w(R.op, R.in_type), ty0 = by * bt_tile_h(R.op, R.in_type);
+        unsigned char *st = smem + b * kStageBytes;
+        if (bulk & (1u << b)) {
+            const bool ok = mbar_wait_bounded(&s_bar[b], (parity >> b) & 1u);
+            parity ^= 1u << b;
+            bulk &= ~(1u << b);
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicExch(err, 1);
+                    if (bulk & (2u >> b)) mbar_wait_bounded(&s_bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
+                }
+                return;
+            }
+        } else {
+            bt_gather_raw(R, bt_geo(R, tx0, ty0), st, s_lead[b]);
+            __syncthreads();
+        }
+        const Staged S{st, s_lead[b], R.in_type == IFX_F32, R.in_type == IFX_N0F8};
         switch (R.op) {
-        case BOP_FACTORED: bt_factored(R, tx0, ty0, reinterpret_cast<float *>(smem)); break;
-        case BOP_GRADIENTS: bt_gradients(R, tx0, ty0, reinterpret_cast<float *>(smem)); break;
-        case BOP_LAPLACIAN: bt_laplacian(R, tx0, ty0, reinterpret_cast<float *>(smem)); break;
+        case BOP_FACTORED: bt_factored(R, tx0, ty0, S, I); break;
+        case BOP_GRADIENTS: bt_gradients(R, tx0, ty0, S); break;
+        case BOP_LAPLACIAN: bt_laplacian(R, tx0, ty0, S); break;
         default:
             if (R.in_type == IFX_F32) {
-                if (R.win == 3) bt_median_f32<3>(R, tx0, ty0, reinterpret_cast<float *>(smem));
-                else bt_median_f32<5>(R, tx0, ty0, reinterpret_cast<float *>(smem));
+                if (R.win == 3) bt_median_f32<3>(R, tx0, ty0, S);
+                else bt_median_f32<5>(R, tx0, ty0, S);
             } else {
-                if (R.win == 3) bt_median_u8<3>(R, tx0, ty0, smem);
-                else bt_median_u8<5>(R, tx0, ty0, smem);
+                if (R.win == 3) bt_median_u8<3>(R, tx0, ty0, S);
+                else bt_median_u8<5>(R, tx0, ty0, S);
             }
         }
+        // buffer b is refilled by the bulk copies of a later tile
+        fence_proxy_async();
         __syncthreads();
     }
 }
 
-constexpr size_t kBatchSmem = (size_t)(2 * kBatchMaxTaps + (kFTY + 32) * (kFTX + 36) + (kFTY + 32) * kFTX) * 4;
+constexpr size_t kBatchSmem = 2 * (size_t)kStageBytes + (size_t)kStageRows * kIPitch * sizeof(float);
 
 // ---------------------------------------------------------------- host side
 struct BatchSlot {
@@ -466,11 +581,13 @@ static cudaError_t slot_build(BatchEngine &E, BatchSlot &S, size_t cap)
     if ((e = cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming)) != cudaSuccess) return e;
     S.cap = cap;
     S.grid = E.grid;
+    int *err = tma_error_word(E.device);     // allocated outside the capture
+    if (!err) return cudaErrorMemoryAllocation;
     // graph: descriptor upload -> counter reset -> persistent kernel
     if ((e = cudaStreamBeginCapture(E.capture, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
     cudaMemcpyAsync(S.dev, S.host, cap, cudaMemcpyHostToDevice, E.capture);
     cudaMemsetAsync(S.counter, 0, sizeof(unsigned long long), E.capture);
-    k_batch<<<E.grid, 256, kBatchSmem, E.capture>>>(S.dev, S.counter);
+    k_batch<<<E.grid, 256, kBatchSmem, E.capture>>>(S.dev, S.counter, err);
     if ((e = cudaStreamEndCapture(E.capture, &S.graph)) != cudaSuccess) return e;
     size_t n = 0;
     if ((e = cudaGraphGetNodes(S.graph, nullptr, &n)) != cudaSuccess) return e;
@@ -516,12 +633,24 @@ int batch_grid(int device)
 }
 
 // Fill `out` from a validated request list; returns the total tile count.
+// The descriptor lists the requests grouped by tile routine (op, element
+// type, window): tiles are handed out in descriptor order, so the CTAs that
+// run at the same time mostly run the same code.  Outputs do not depend on
+// the order.
 long long batch_describe(const BatchItem *items, int n, std::vector<BReq> &out)
 {
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    auto key = [&](int i) {
+        const BatchItem &it = items[i];
+        return (long long)it.op << 40 | (long long)it.in_type << 32 | (long long)it.window << 16 |
+               (long long)(it.kx & 0xFFFF);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key(a) < key(b); });
     out.resize(n);
     long long base = 0;
     for (int i = 0; i < n; ++i) {
-        const BatchItem &it = items[i];
+        const BatchItem &it = items[order[i]];
         BReq &R = out[i];
         memset(&R, 0, sizeof R);
         R.op = it.op;
@@ -547,6 +676,7 @@ long long batch_describe(const BatchItem *items, int n, std::vector<BReq> &out)
         const long long tiles = (long long)R.tiles_x * ((R.ny + th - 1) / th);
         R.tile_base = base;
         base += tiles;
+        R.tile_end = base;
     }
     return base;
 }
@@ -615,13 +745,18 @@ cudaError_t plan_create(int device, const BatchItem *items, int n, void **out)
         plan_destroy(P);
         return e;
     }
+    int *err = tma_error_word(E->device);    // allocated outside the capture
+    if (!err) {
+        plan_destroy(P);
+        return cudaErrorMemoryAllocation;
+    }
     std::lock_guard<std::mutex> lk(E->mu);
     if ((e = cudaStreamBeginCapture(E->capture, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
         plan_destroy(P);
         return e;
     }
     cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), E->capture);
-    k_batch<<<E->grid, 256, kBatchSmem, E->capture>>>(P->dev, P->counter);
+    k_batch<<<E->grid, 256, kBatchSmem, E->capture>>>(P->dev, P->counter, err);
     if ((e = cudaStreamEndCapture(E->capture, &P->graph)) != cudaSuccess ||
         (e = cudaGraphInstantiate(&P->exec, P->graph, 0)) != cudaSuccess) {
         plan_destroy(P);

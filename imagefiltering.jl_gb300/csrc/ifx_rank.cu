@@ -203,21 +203,14 @@ k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, in
         return wd;
     };
     uint32_t res = 0;
-    if (W0 > 0 && W1 > 0) {
-        uint32_t w[(W0 > 0 ? W0 : 1) * (W1 > 0 ? W1 : 1)];
+    if constexpr (W0 > 0 && W1 > 0) {
+        // fixed window: byte-wise selection network (four windows per word)
+        uint32_t w[W0 * W1];
 #pragma unroll
-        for (int j = 0; j < (W1 > 0 ? W1 : 1); ++j)
+        for (int j = 0; j < W1; ++j)
 #pragma unroll
-            for (int i = 0; i < (W0 > 0 ? W0 : 1); ++i) w[j * W0 + i] = word(j, i);
-#pragma unroll
-        for (int b = 7; b >= 0; --b) {
-            const uint32_t trial = res | (0x01010101u << b);
-            uint32_t cnt = 0;
-#pragma unroll
-            for (int k = 0; k < (W0 > 0 ? W0 : 1) * (W1 > 0 ? W1 : 1); ++k) cnt = count_lt(cnt, w[k], trial);
-            const uint32_t below = __vcmpltu4(cnt, rank4);
-            res = (trial & below) | (res & ~below);
-        }
+            for (int i = 0; i < W0; ++i) w[j * W0 + i] = word(j, i);
+        res = median_u8x4<W0 * W1>(w);
     } else {
         for (int b = 7; b >= 0; --b) {
             const uint32_t trial = res | (0x01010101u << b);

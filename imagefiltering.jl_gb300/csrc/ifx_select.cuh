@@ -101,4 +101,31 @@ template <int N, class K> __device__ __forceinline__ void net_sort(K (&v)[N])
     net_apply<N, K>(v, std::make_index_sequence<NetOf<N>::net.n>{});
 }
 
+// The same network on four 8-bit codes per word: each compare-exchange is a
+// byte-wise min and max (__vminu4 / __vmaxu4), so one pass selects the
+// medians of four horizontally adjacent windows.  When only the middle word
+// is used afterwards, the compiler keeps just the comparators (and the min or
+// max halves) it depends on.
+template <int N, int I> __device__ __forceinline__ void net_cx_u8x4(uint32_t (&v)[N])
+{
+    constexpr int x = NetOf<N>::net.a[I];
+    constexpr int y = NetOf<N>::net.b[I];
+    const uint32_t lo = __vminu4(v[x], v[y]);
+    const uint32_t hi = __vmaxu4(v[x], v[y]);
+    v[x] = lo;
+    v[y] = hi;
+}
+
+template <int N, size_t... I>
+__device__ __forceinline__ void net_apply_u8x4(uint32_t (&v)[N], std::index_sequence<I...>)
+{
+    (net_cx_u8x4<N, (int)I>(v), ...);
+}
+
+template <int N> __device__ __forceinline__ uint32_t median_u8x4(uint32_t (&v)[N])
+{
+    net_apply_u8x4<N>(v, std::make_index_sequence<NetOf<N>::net.n>{});
+    return v[(N - 1) / 2];
+}
+
 } // namespace ifx

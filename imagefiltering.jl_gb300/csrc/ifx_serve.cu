@@ -8,8 +8,9 @@
 //   2. while fewer than `max_inflight` batches run, packs admitted requests
 //      into one batched launch (the persistent tile work-queue kernel of
 //      ifx_batch.cu) on the compute stream, which waits for the uploads;
-//   3. when a batch finishes, copies host outputs back on the copy stream and
-//      releases the request's device memory after those copies;
+//   3. when a batch finishes, copies host outputs back on a download stream
+//      (the link's two directions overlap) and releases the request's device
+//      memory after those copies;
 //   4. records submit -> done latency of every request.
 // Requests admitted while other batches run overlap with them on the device:
 // uploads of batch k+1 run on the copy stream during batch k.
@@ -58,7 +59,8 @@ struct ifx_server {
     ifx_context_t *ctx = nullptr;
     int device = 0;
     ifx_server_config_t cfg{};
-    cudaStream_t copy = nullptr, compute = nullptr;
+    cudaStream_t copy = nullptr, compute = nullptr;   // copy: uploads; compute: batches
+    cudaStream_t down = nullptr;                        // downloads and releases
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<std::shared_ptr<ifx::SReq>> incoming;           // submitted, not seen by the engine
@@ -106,18 +108,18 @@ static void finish_batches(ifx_server *S)
         SBatch &b = S->inflight.front();
         if (!b.copies_enqueued) {
             if (cudaEventQuery(b.compute_done) == cudaErrorNotReady) return;
-            cudaStreamWaitEvent(S->copy, b.compute_done, 0);
+            cudaStreamWaitEvent(S->down, b.compute_done, 0);
             for (auto &r : b.reqs)
                 for (int o = 0; o < nouts(r->q); ++o)
                     if (r->host_out[o])
                         cudaMemcpyAsync(r->q.out[o].data, r->d_out[o], r->out_bytes[o],
-                                        cudaMemcpyDeviceToHost, S->copy);
+                                        cudaMemcpyDeviceToHost, S->down);
             for (auto &r : b.reqs) {
-                if (r->host_in && r->d_in) cudaFreeAsync(r->d_in, S->copy);
+                if (r->host_in && r->d_in) cudaFreeAsync(r->d_in, S->down);
                 for (int o = 0; o < 2; ++o)
-                    if (r->host_out[o] && r->d_out[o]) cudaFreeAsync(r->d_out[o], S->copy);
+                    if (r->host_out[o] && r->d_out[o]) cudaFreeAsync(r->d_out[o], S->down);
             }
-            cudaEventRecord(b.copy_done, S->copy);
+            cudaEventRecord(b.copy_done, S->down);
             b.copies_enqueued = true;
         }
         if (cudaEventQuery(b.copy_done) == cudaErrorNotReady) return;
@@ -260,6 +262,7 @@ int ifx_server_create(ifx_context_t *ctx, const ifx_server_config_t *cfg, ifx_se
     S->cfg = *cfg;
     cudaGetDevice(&S->device);
     if (cudaStreamCreateWithFlags(&S->copy, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&S->down, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&S->compute, cudaStreamNonBlocking) != cudaSuccess) {
         delete S;
         return IFX_ERR_CUDA;
@@ -398,8 +401,10 @@ int ifx_server_destroy(ifx_server_t *S)
     S->cv_work.notify_all();
     if (S->engine.joinable()) S->engine.join();
     cudaStreamSynchronize(S->copy);
+    cudaStreamSynchronize(S->down);
     cudaStreamSynchronize(S->compute);
     cudaStreamDestroy(S->copy);
+    cudaStreamDestroy(S->down);
     cudaStreamDestroy(S->compute);
     delete S;
     return IFX_OK;
