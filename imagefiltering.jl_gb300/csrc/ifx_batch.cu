@@ -55,20 +55,22 @@ struct BHdr {
 
 enum { BOP_FACTORED = 1, BOP_GRADIENTS = 2, BOP_LAPLACIAN = 3, BOP_MEDIAN = 4 };
 
-// tile shapes (outputs per tile)
-constexpr int kFTX = 64, kFTY = 32;        // factored / gradients / laplacian
-constexpr int kMUX = 128, kMUY = 32;       // 8-bit median (4 pixels per thread, 4 rows)
-constexpr int kMFX = 64, kMFY = 32;        // float median (8 pixels per thread)
+// tile shapes (outputs per tile); each input window (tile + halo) fits one
+// staging buffer of 64 rows x 400 bytes
+constexpr int kFTX = 64, kFTY = 32;        // factored (halo up to 32 x 32)
+constexpr int kGTX = 64, kGTY = 56;        // gradients / laplacian (halo 2 x 2)
+constexpr int kMUX = 256, kMUY = 56;       // 8-bit median (4 pixels per thread and step)
+constexpr int kMFX = 64, kMFY = 56;        // float median
 
 __host__ __device__ inline int bt_tile_w(int op, int in_type)
 {
     if (op == BOP_MEDIAN) return (in_type == IFX_F32) ? kMFX : kMUX;
-    return kFTX;
+    return op == BOP_FACTORED ? kFTX : kGTX;
 }
 __host__ __device__ inline int bt_tile_h(int op, int in_type)
 {
     if (op == BOP_MEDIAN) return (in_type == IFX_F32) ? kMFY : kMUY;
-    return kFTY;
+    return op == BOP_FACTORED ? kFTY : kGTY;
 }
 
 // Division-free 2-D gather of a tile whose element (r, c) is load(r, c): warps
@@ -128,7 +130,7 @@ __device__ __forceinline__ TileGeo bt_geo(const BReq &R, int tx0, int ty0)
     switch (R.op) {
     case BOP_FACTORED: return {tx0 + R.fx, ty0 + R.fy, kFTY + R.ky - 1, kFTX + R.kx - 1, elt};
     case BOP_GRADIENTS:
-    case BOP_LAPLACIAN: return {tx0 - 1, ty0 - 1, kFTY + 2, kFTX + 2, elt};
+    case BOP_LAPLACIAN: return {tx0 - 1, ty0 - 1, kGTY + 2, kGTX + 2, elt};
     default: {
         const int h = R.win / 2;
         if (elt == 4) return {tx0 - h, ty0 - h, kMFY + R.win - 1, kMFX + R.win - 1, 4};
@@ -200,27 +202,69 @@ __device__ __forceinline__ void bt_gather_raw(const BReq &R, const TileGeo &g, u
     }
 }
 
-// Value of staged element (r, c) in the compute domain.
-struct Staged {
+// Value of staged element (r, c) in the compute domain (the element type is a
+// compile-time parameter of the tile routines; 8-bit codes go through the
+// CTA's code -> value table).
+__shared__ float s_u8f[256];                           // UInt8 code c as Float32
+
+template <class Tin> struct Rows;
+template <> struct Rows<float> {
     const unsigned char *st;
     const unsigned char *lead;
-    bool f32, norm;
-    __device__ __forceinline__ const unsigned char *row(int r) const { return st + r * kStagePitch + lead[r]; }
-    __device__ __forceinline__ float at(int r, int c) const
+    __device__ __forceinline__ Rows(const unsigned char *s, const unsigned char *l, const float *) : st(s), lead(l) {}
+    __device__ __forceinline__ const float *row(int r) const
     {
-        if (f32) return reinterpret_cast<const float *>(row(r))[c];
-        const uint8_t v = row(r)[c];
-        return norm ? s_n0f8[v] : (float)v;
+        return reinterpret_cast<const float *>(st + r * kStagePitch + lead[r]);
     }
+    __device__ __forceinline__ float val(const float *p, int c) const { return p[c]; }
+};
+template <> struct Rows<uint8_t> {
+    const unsigned char *st;
+    const unsigned char *lead;
+    const float *lut;
+    __device__ __forceinline__ Rows(const unsigned char *s, const unsigned char *l, const float *t)
+        : st(s), lead(l), lut(t) {}
+    __device__ __forceinline__ const uint8_t *row(int r) const { return st + r * kStagePitch + lead[r]; }
+    __device__ __forceinline__ float val(const uint8_t *p, int c) const { return lut[p[c]]; }
 };
 
-__device__ __forceinline__ void bt_store(const BReq &R, void *out, int x, int y, float v)
-{
-    if (x >= R.nx || y >= R.ny) return;
-    const long long o = (long long)y * R.nx + x;
-    if (R.out_type == IFX_F64) ((double *)out)[o] = f32_to_f64(v);
-    else ((float *)out)[o] = v;
-}
+// Output rows of a tile: element (x, y) of `out`; `full` tiles skip the bounds tests.
+template <class Tout> struct OutTile {
+    Tout *base;
+    int nx, ny, tx0, ty0;
+    bool full;
+    __device__ __forceinline__ OutTile(const BReq &R, void *out, int x0, int y0, int tw, int th)
+        : base((Tout *)out), nx(R.nx), ny(R.ny), tx0(x0), ty0(y0),
+          full(x0 + tw <= R.nx && y0 + th <= R.ny) {}
+    // NB outputs down column c from row r0
+    template <int NB> __device__ __forceinline__ void col(int c, int r0, const float *v) const
+    {
+        const int x = tx0 + c;
+        Tout *p = base + (long long)(ty0 + r0) * nx + x;
+        if (full) {
+#pragma unroll
+            for (int i = 0; i < NB; ++i) p[(long long)i * nx] = out_cvt<Tout>(v[i]);
+        } else if (x < nx) {
+#pragma unroll
+            for (int i = 0; i < NB; ++i)
+                if (ty0 + r0 + i < ny) p[(long long)i * nx] = out_cvt<Tout>(v[i]);
+        }
+    }
+    // N outputs along row r from column c0
+    template <int N> __device__ __forceinline__ void row(int c0, int r, const float *v) const
+    {
+        const int y = ty0 + r;
+        Tout *p = base + (long long)y * nx + tx0 + c0;
+        if (full) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) p[i] = out_cvt<Tout>(v[i]);
+        } else if (y < ny) {
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+                if (tx0 + c0 + i < nx) p[i] = out_cvt<Tout>(v[i]);
+        }
+    }
+};
 
 // ---------------------------------------------------------------- factored
 // acc[i] = sum_{t<k} w[t] src(i+t), i < NB, the window read through `at`.
@@ -243,7 +287,8 @@ __device__ __forceinline__ void corr_fn(F at, const float *w, int k, float *acc)
     }
 }
 
-__device__ void bt_factored(const BReq &R, int tx0, int ty0, const Staged &S, float *I)
+template <class Tin, class Tout>
+__device__ void bt_factored(const BReq &R, int tx0, int ty0, const Rows<Tin> &S, float *I)
 {
     constexpr int TX = kFTX, TY = kFTY, NB = 8;
     const int kx = R.kx, ky = R.ky, rows = TY + ky - 1;
@@ -252,69 +297,71 @@ __device__ void bt_factored(const BReq &R, int tx0, int ty0, const Staged &S, fl
     // x pass over all rows (the y halo) -> I
     for (int it = tid; it < rows * (TX / NB); it += nth) {
         const int r = it >> 3, c0 = (it & 7) * NB;
-        if (S.f32) {
-            const float *p = reinterpret_cast<const float *>(S.row(r)) + c0;
-            corr_fn<NB>([&](int j) { return p[j]; }, R.wx, kx, acc);
-        } else {
-            const uint8_t *p = S.row(r) + c0;
-            if (S.norm) corr_fn<NB>([&](int j) { return s_n0f8[p[j]]; }, R.wx, kx, acc);
-            else corr_fn<NB>([&](int j) { return (float)p[j]; }, R.wx, kx, acc);
-        }
+        const auto *p = S.row(r) + c0;
+        corr_fn<NB>([&](int j) { return S.val(p, j); }, R.wx, kx, acc);
 #pragma unroll
         for (int i = 0; i < NB; ++i) I[r * kIPitch + c0 + i] = acc[i];
     }
     __syncthreads();
     // y pass down each column
+    const OutTile<Tout> O(R, R.out0, tx0, ty0, TX, TY);
     for (int it = tid; it < TX * (TY / NB); it += nth) {
         const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
         corr_col<NB>(I + r0 * kIPitch + c, kIPitch, R.wy, ky, acc);
-#pragma unroll
-        for (int i = 0; i < NB; ++i) bt_store(R, R.out0, tx0 + c, ty0 + r0 + i, acc[i]);
+        O.template col<NB>(c, r0, acc);
     }
 }
 
 // ---------------------------------------------------------------- gradients
 // out0 = smooth_y(deriv_x), out1 = deriv_y(smooth_x) over a halo-1 window.
-__device__ void bt_gradients(const BReq &R, int tx0, int ty0, const Staged &S)
+template <class Tin, class Tout>
+__device__ void bt_gradients(const BReq &R, int tx0, int ty0, const Rows<Tin> &S)
 {
-    constexpr int TX = kFTX, TY = kFTY, NB = 8;
+    constexpr int TX = kGTX, TY = kGTY, NB = 8;
     const int tid = threadIdx.x, nth = blockDim.x;
     const float d0 = R.wx[0], d1 = R.wx[1], d2 = R.wx[2];
     const float s0 = R.wy[0], s1 = R.wy[1], s2 = R.wy[2];
+    const OutTile<Tout> O0(R, R.out0, tx0, ty0, TX, TY), O1(R, R.out1, tx0, ty0, TX, TY);
     for (int it = tid; it < TX * (TY / NB); it += nth) {
         const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
         float D[NB + 2], Sm[NB + 2];
 #pragma unroll
         for (int j = 0; j < NB + 2; ++j) {
-            const float a0 = S.at(r0 + j, c), a1 = S.at(r0 + j, c + 1), a2 = S.at(r0 + j, c + 2);
+            const auto *p = S.row(r0 + j) + c;
+            const float a0 = S.val(p, 0), a1 = S.val(p, 1), a2 = S.val(p, 2);
             D[j] = fmaf(d2, a2, fmaf(d1, a1, d0 * a0));
             Sm[j] = fmaf(s2, a2, fmaf(s1, a1, s0 * a0));
         }
+        float g0[NB], g1[NB];
 #pragma unroll
         for (int i = 0; i < NB; ++i) {
-            const float g0 = fmaf(s2, D[i + 2], fmaf(s1, D[i + 1], s0 * D[i]));
-            const float g1 = fmaf(d2, Sm[i + 2], fmaf(d1, Sm[i + 1], d0 * Sm[i]));
-            bt_store(R, R.out0, tx0 + c, ty0 + r0 + i, g0);
-            bt_store(R, R.out1, tx0 + c, ty0 + r0 + i, g1);
+            g0[i] = fmaf(s2, D[i + 2], fmaf(s1, D[i + 1], s0 * D[i]));
+            g1[i] = fmaf(d2, Sm[i + 2], fmaf(d1, Sm[i + 1], d0 * Sm[i]));
         }
+        O0.template col<NB>(c, r0, g0);
+        O1.template col<NB>(c, r0, g1);
     }
 }
 
 // ---------------------------------------------------------------- laplacian
 // Kernel.Laplacian((true,true)) in the reference's operation order.
-__device__ void bt_laplacian(const BReq &R, int tx0, int ty0, const Staged &S)
+template <class Tin, class Tout>
+__device__ void bt_laplacian(const BReq &R, int tx0, int ty0, const Rows<Tin> &S)
 {
-    constexpr int TX = kFTX, TY = kFTY, NB = 8;
+    constexpr int TX = kGTX, TY = kGTY, NB = 8;
     const int tid = threadIdx.x, nth = blockDim.x;
+    const OutTile<Tout> O(R, R.out0, tx0, ty0, TX, TY);
     for (int it = tid; it < TX * (TY / NB); it += nth) {
         const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
-        float col[NB + 2], lft[NB], rgt[NB];
+        float col[NB + 2], lft[NB], rgt[NB], res[NB];
 #pragma unroll
-        for (int j = 0; j < NB + 2; ++j) col[j] = S.at(r0 + j, c + 1);
-#pragma unroll
-        for (int i = 0; i < NB; ++i) {
-            lft[i] = S.at(r0 + 1 + i, c);
-            rgt[i] = S.at(r0 + 1 + i, c + 2);
+        for (int j = 0; j < NB + 2; ++j) {
+            const auto *p = S.row(r0 + j) + c;
+            col[j] = S.val(p, 1);
+            if (j >= 1 && j <= NB) {
+                lft[j - 1] = S.val(p, 0);
+                rgt[j - 1] = S.val(p, 2);
+            }
         }
 #pragma unroll
         for (int i = 0; i < NB; ++i) {
@@ -322,9 +369,9 @@ __device__ void bt_laplacian(const BReq &R, int tx0, int ty0, const Staged &S)
             tmp = __fadd_rn(tmp, rgt[i]);
             tmp = __fadd_rn(tmp, lft[i]);
             tmp = __fadd_rn(tmp, col[i + 2]);
-            tmp = __fadd_rn(tmp, col[i]);
-            bt_store(R, R.out0, tx0 + c, ty0 + r0 + i, tmp);
+            res[i] = __fadd_rn(tmp, col[i]);
         }
+        O.template col<NB>(c, r0, res);
     }
 }
 
@@ -341,14 +388,14 @@ __device__ __forceinline__ int bt_win_index(const BReq &R, int x, int y, int i, 
     return my * R.nx + mx;
 }
 
-template <int W>
-__device__ void bt_median_u8(const BReq &R, int tx0, int ty0, const Staged &S)
+template <int W, class Tout>
+__device__ void bt_median_u8(const BReq &R, int tx0, int ty0, const Rows<uint8_t> &S)
 {
     constexpr int h = W / 2;
     const int tid = threadIdx.x;
-    const int lx = (tid & 31) * 4;
-    const bool norm = R.in_type == IFX_N0F8;
-    for (int ly = tid >> 5; ly < kMUY; ly += blockDim.x >> 5) {
+    const OutTile<Tout> O(R, R.out0, tx0, ty0, kMUX, kMUY);
+    for (int step = tid >> 5; step < kMUY * (kMUX / 128); step += blockDim.x >> 5) {
+        const int ly = step % kMUY, lx = (step / kMUY) * 128 + (tid & 31) * 4;
         const int x0 = tx0 + lx, y = ty0 + ly;
         if (x0 >= R.nx || y >= R.ny) continue;
         uint32_t w[W * W];
@@ -378,16 +425,15 @@ __device__ void bt_median_u8(const BReq &R, int tx0, int ty0, const Staged &S)
                 }
         }
         const uint32_t res = median_u8x4<W * W>(w);
+        float v[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint8_t code = (uint8_t)(res >> (8 * q));
-            bt_store(R, R.out0, x0 + q, y, norm ? s_n0f8[code] : (float)code);
-        }
+        for (int q = 0; q < 4; ++q) v[q] = S.lut[(res >> (8 * q)) & 0xFF];
+        O.template row<4>(lx, ly, v);
     }
 }
 
-template <int W>
-__device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Staged &S)
+template <int W, class Tout>
+__device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Rows<float> &S)
 {
     using SK = SortKey<float>;
     constexpr int h = W / 2, N = W * W;
@@ -399,7 +445,7 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Staged &S)
         if (!edge) {
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                const float *rowp = reinterpret_cast<const float *>(S.row(ly + j));
+                const float *rowp = S.row(ly + j);
 #pragma unroll
                 for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(rowp[lx + i]);
             }
@@ -411,7 +457,26 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Staged &S)
                 for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(img[bt_win_index(R, x, y, i, j, h)]);
         }
         net_sort<N, uint32_t>(v);
-        bt_store(R, R.out0, x, y, SK::val(v[(N - 1) / 2]));
+        ((Tout *)R.out0)[(long long)y * R.nx + x] = out_cvt<Tout>(SK::val(v[(N - 1) / 2]));
+    }
+}
+
+// Tile routine for the (element type, output type) pair of the request.
+template <class Tin, class Tout>
+__device__ __forceinline__ void bt_dispatch(const BReq &R, int tx0, int ty0, const Rows<Tin> &S, float *I)
+{
+    switch (R.op) {
+    case BOP_FACTORED: bt_factored<Tin, Tout>(R, tx0, ty0, S, I); break;
+    case BOP_GRADIENTS: bt_gradients<Tin, Tout>(R, tx0, ty0, S); break;
+    case BOP_LAPLACIAN: bt_laplacian<Tin, Tout>(R, tx0, ty0, S); break;
+    default:
+        if constexpr (sizeof(Tin) == 4) {
+            if (R.win == 3) bt_median_f32<3, Tout>(R, tx0, ty0, S);
+            else bt_median_f32<5, Tout>(R, tx0, ty0, S);
+        } else {
+            if (R.win == 3) bt_median_u8<3, Tout>(R, tx0, ty0, S);
+            else bt_median_u8<5, Tout>(R, tx0, ty0, S);
+        }
     }
 }
 
@@ -436,6 +501,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
     float *I = reinterpret_cast<float *>(smem + 2 * kStageBytes);
     for (int i = tid; i < ntab; i += blockDim.x) s_base[i] = (int)reqs[i].tile_base;
     s_n0f8[tid & 255] = __fdiv_rn((float)(tid & 255), 255.0f);
+    s_u8f[tid & 255] = (float)(tid & 255);
     long long ahead = 0;                 // thread 0: the tile after the next one
     if (tid == 0) {
         mbar_init(&s_bar[0], 1);
@@ -520,19 +586,15 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
             bt_gather_raw(R, bt_geo(R, tx0, ty0), st, s_lead[b]);
             __syncthreads();
         }
-        const Staged S{st, s_lead[b], R.in_type == IFX_F32, R.in_type == IFX_N0F8};
-        switch (R.op) {
-        case BOP_FACTORED: bt_factored(R, tx0, ty0, S, I); break;
-        case BOP_GRADIENTS: bt_gradients(R, tx0, ty0, S); break;
-        case BOP_LAPLACIAN: bt_laplacian(R, tx0, ty0, S); break;
-        default:
-            if (R.in_type == IFX_F32) {
-                if (R.win == 3) bt_median_f32<3>(R, tx0, ty0, S);
-                else bt_median_f32<5>(R, tx0, ty0, S);
-            } else {
-                if (R.win == 3) bt_median_u8<3>(R, tx0, ty0, S);
-                else bt_median_u8<5>(R, tx0, ty0, S);
-            }
+        const bool o64 = R.out_type == IFX_F64;
+        if (R.in_type == IFX_F32) {
+            const Rows<float> S(st, s_lead[b], nullptr);
+            if (o64) bt_dispatch<float, double>(R, tx0, ty0, S, I);
+            else bt_dispatch<float, float>(R, tx0, ty0, S, I);
+        } else {
+            const Rows<uint8_t> S(st, s_lead[b], R.in_type == IFX_N0F8 ? s_n0f8 : s_u8f);
+            if (o64) bt_dispatch<uint8_t, double>(R, tx0, ty0, S, I);
+            else bt_dispatch<uint8_t, float>(R, tx0, ty0, S, I);
         }
         // buffer b is refilled by the bulk copies of a later tile
         fence_proxy_async();
