@@ -380,7 +380,7 @@ def run_stream_e2e(args, ifx, torch, reqs_all):
     d2h = sum(r.out_bytes() for r in reqs)
     res = {}
     with Server(hbm_cap_bytes=args.hbm_cap_gb << 30, max_batch=args.per_step, max_inflight=2) as srv:
-        for r, q, bt in items[:50]:                                       # warm-up
+        for r, q, bt in items:              # warm-up pass: the memory pool reaches its size
             srv.submit_struct(q)
         srv.drain()
         srv.reset_metrics()

@@ -437,6 +437,13 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Rows<float>
 {
     using SK = SortKey<float>;
     constexpr int h = W / 2, N = W * W;
+    // staged values -> order-preserving keys, in place, once per element
+    for (int e = threadIdx.x; e < (kMFY + W - 1) * (kMFX + W - 1); e += blockDim.x) {
+        const int r = e / (kMFX + W - 1), c = e - r * (kMFX + W - 1);
+        float *q = const_cast<float *>(S.row(r)) + c;
+        *reinterpret_cast<uint32_t *>(q) = SK::key(*q);
+    }
+    __syncthreads();
     for (int p = threadIdx.x; p < kMFX * kMFY; p += blockDim.x) {
         const int lx = p % kMFX, ly = p / kMFX, x = tx0 + lx, y = ty0 + ly;
         if (x >= R.nx || y >= R.ny) continue;
@@ -445,9 +452,9 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Rows<float>
         if (!edge) {
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                const float *rowp = S.row(ly + j);
+                const uint32_t *rowk = reinterpret_cast<const uint32_t *>(S.row(ly + j));
 #pragma unroll
-                for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(rowp[lx + i]);
+                for (int i = 0; i < W; ++i) v[j * W + i] = rowk[lx + i];
             }
         } else {
             const float *img = (const float *)R.in;

@@ -242,13 +242,13 @@ k_median_float(const T *__restrict__ img, void *out, int out_type, int nx, int n
     using SK = SortKey<T>;
     using K = typename SK::K;
     constexpr int CT = kFmTX + W0 - 1, RT = kFmTY + W1 - 1, N = W0 * W1;
-    __shared__ T tile[RT * CT];
+    __shared__ K tile[RT * CT];                 // order-preserving keys of the window values
     const int tx0 = blockIdx.x * kFmTX, ty0 = blockIdx.y * kFmTY;
-    gather_tile<8>(tile, RT * CT, [&](int idx) -> T {
+    gather_tile<8>(tile, RT * CT, [&](int idx) -> K {
         const int r = idx / CT, c = idx - r * CT;
         const int mx = map_index(tx0 + f0 + c, nx, style);
         const int my = map_index(ty0 + f1 + r, ny, style);
-        return (mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx];
+        return SK::key((mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx]);
     });
     __syncthreads();
     const int lx = threadIdx.x % kFmTX, ly = threadIdx.x / kFmTX;
@@ -260,8 +260,8 @@ k_median_float(const T *__restrict__ img, void *out, int out_type, int nx, int n
     for (int j = 0; j < W1; ++j)
 #pragma unroll
         for (int i = 0; i < W0; ++i)
-            v[j * W0 + i] = SK::key(edge ? img[win_index2(x, y, i, j, f0, f1, W0, W1, nx, ny, style)]
-                                         : tile[(ly + j) * CT + lx + i]);
+            v[j * W0 + i] = edge ? SK::key(img[win_index2(x, y, i, j, f0, f1, W0, W1, nx, ny, style)])
+                                 : tile[(ly + j) * CT + lx + i];
     net_sort<N, K>(v);
     if (x < nx && y < ny) store_sel<T>(out, out_type, (long long)y * nx + x, SK::val(v[(N - 1) / 2]), false);
 }

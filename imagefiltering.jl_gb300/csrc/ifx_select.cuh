@@ -84,8 +84,8 @@ template <int N, int I, class K> __device__ __forceinline__ void net_cx(K (&v)[N
 {
     constexpr int x = NetOf<N>::net.a[I];
     constexpr int y = NetOf<N>::net.b[I];
-    const K lo = v[x] < v[y] ? v[x] : v[y];
-    const K hi = v[x] < v[y] ? v[y] : v[x];
+    const K lo = min(v[x], v[y]);
+    const K hi = max(v[x], v[y]);
     v[x] = lo;
     v[y] = hi;
 }
@@ -101,31 +101,41 @@ template <int N, class K> __device__ __forceinline__ void net_sort(K (&v)[N])
     net_apply<N, K>(v, std::make_index_sequence<NetOf<N>::net.n>{});
 }
 
-// The same network on four 8-bit codes per word: each compare-exchange is a
-// byte-wise min and max (__vminu4 / __vmaxu4), so one pass selects the
-// medians of four horizontally adjacent windows.  When only the middle word
-// is used afterwards, the compiler keeps just the comparators (and the min or
-// max halves) it depends on.
-template <int N, int I> __device__ __forceinline__ void net_cx_u8x4(uint32_t (&v)[N])
+// The same network on packed codes: each word holds two 8-bit codes
+// zero-extended to 16-bit lanes, and each compare-exchange is a lane-wise min
+// and max (__vminu2 / __vmaxu2, single instructions here, where the 8-bit
+// four-lane forms are emulated).  When only the middle word is used
+// afterwards, the compiler keeps just the comparators (and the min or max
+// halves) it depends on.
+template <int N, int I> __device__ __forceinline__ void net_cx_u16x2(uint32_t (&v)[N])
 {
     constexpr int x = NetOf<N>::net.a[I];
     constexpr int y = NetOf<N>::net.b[I];
-    const uint32_t lo = __vminu4(v[x], v[y]);
-    const uint32_t hi = __vmaxu4(v[x], v[y]);
+    const uint32_t lo = __vminu2(v[x], v[y]);
+    const uint32_t hi = __vmaxu2(v[x], v[y]);
     v[x] = lo;
     v[y] = hi;
 }
 
 template <int N, size_t... I>
-__device__ __forceinline__ void net_apply_u8x4(uint32_t (&v)[N], std::index_sequence<I...>)
+__device__ __forceinline__ void net_apply_u16x2(uint32_t (&v)[N], std::index_sequence<I...>)
 {
-    (net_cx_u8x4<N, (int)I>(v), ...);
+    (net_cx_u16x2<N, (int)I>(v), ...);
 }
 
-template <int N> __device__ __forceinline__ uint32_t median_u8x4(uint32_t (&v)[N])
+// Medians of the four byte lanes of w[0..N) (four horizontally adjacent
+// windows), returned packed like the input.
+template <int N> __device__ __forceinline__ uint32_t median_u8x4(const uint32_t (&w)[N])
 {
-    net_apply_u8x4<N>(v, std::make_index_sequence<NetOf<N>::net.n>{});
-    return v[(N - 1) / 2];
+    uint32_t a[N], b[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        a[k] = __byte_perm(w[k], 0u, 0x4140);      // bytes 0, 1 -> 16-bit lanes
+        b[k] = __byte_perm(w[k], 0u, 0x4342);      // bytes 2, 3
+    }
+    net_apply_u16x2<N>(a, std::make_index_sequence<NetOf<N>::net.n>{});
+    net_apply_u16x2<N>(b, std::make_index_sequence<NetOf<N>::net.n>{});
+    return __byte_perm(a[(N - 1) / 2], b[(N - 1) / 2], 0x6420);
 }
 
 } // namespace ifx
