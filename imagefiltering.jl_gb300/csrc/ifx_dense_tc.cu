@@ -57,6 +57,20 @@ __device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t a, uint64_t b, u
                  :: "r"(dtmem), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
 }
 
+// Same MMA with the descriptors given as (low, high) 32-bit words: the issue
+// loop advances only the low words (the start-address field, which never
+// carries into the next field for shared-memory addresses of this kernel).
+__device__ __forceinline__ void tc_mma_w(uint32_t dtmem, uint32_t a_lo, uint32_t a_hi, uint32_t b_lo,
+                                         uint32_t b_hi, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t.reg .b64 da, db;\n\t"
+                 "setp.ne.b32 p, %6, 0;\n\t"
+                 "mov.b64 da, {%1, %2};\n\tmov.b64 db, {%3, %4};\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], da, db, %5, p;\n\t}\n"
+                 :: "r"(dtmem), "r"(a_lo), "r"(a_hi), "r"(b_lo), "r"(b_hi), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity)
 {
     uint32_t ok;
@@ -267,24 +281,34 @@ k_dense_tc(TcArgs a, const __grid_constant__ TcWeights W)
         const bool have = tile < a.tiles;
         // 1. issue the MMAs of this tile into accumulator b
         if (have && tid == 0) {
-            // descriptors advance by adding byte offsets >> 4 to the start-address field
+            // descriptors: the high words are fixed, the low words advance by
+            // byte offsets >> 4 (i rows: +i for A; core matrices: +8 for B)
             const uint64_t dAh = tc_desc(smem_u32(Ahi(b)), ps, 128), dAl = tc_desc(smem_u32(Alo(b)), ps, 128);
             const uint64_t dBh = tc_desc(bhi_s, 128, 128), dBl = tc_desc(blo_s, 128, 128);
+            const uint32_t hAh = (uint32_t)(dAh >> 32), hAl = (uint32_t)(dAl >> 32);
+            const uint32_t hBh = (uint32_t)(dBh >> 32), hBl = (uint32_t)(dBl >> 32);
+            uint32_t ah = (uint32_t)dAh, al = (uint32_t)dAl, bh = (uint32_t)dBh, bl = (uint32_t)dBl;
             const uint32_t dt = tmem + 32u * (uint32_t)b;
-            const uint64_t a_ks = (2u * ps) >> 4;          // next 16 K values: two planes
+            const uint32_t a_ks = (2u * ps) >> 4;          // next 16 K values: two planes
+            const uint32_t b_row = (uint32_t)ncm * 8u;     // next kernel row of B
             const int ksteps = V / 16;
-            tc_mma(dt, dAh, dBh, idesc, 0);
-            tc_mma(dt, dAh, dBl, idesc, 1);
-            tc_mma(dt, dAl, dBh, idesc, 1);
+            uint32_t acc = 0;
             for (int i = 0; i < kh; ++i) {
-                uint64_t ah = dAh + (uint64_t)i, al = dAl + (uint64_t)i;       // +16 i bytes
-                uint64_t bh = dBh + (uint64_t)(i * ncm * 8), bl = dBl + (uint64_t)(i * ncm * 8);
-                for (int s = (i == 0); s < ksteps; ++s) {
-                    const uint64_t ds = (uint64_t)s;
-                    tc_mma(dt, ah + ds * a_ks, bh + 16 * ds, idesc, 1);
-                    tc_mma(dt, ah + ds * a_ks, bl + 16 * ds, idesc, 1);
-                    tc_mma(dt, al + ds * a_ks, bh + 16 * ds, idesc, 1);
+                uint32_t a1 = ah, a2 = al, b1 = bh, b2 = bl;
+                for (int s = 0; s < ksteps; ++s) {
+                    tc_mma_w(dt, a1, hAh, b1, hBh, idesc, acc);
+                    acc = 1;
+                    tc_mma_w(dt, a1, hAh, b2, hBl, idesc, 1);
+                    tc_mma_w(dt, a2, hAl, b1, hBh, idesc, 1);
+                    a1 += a_ks;
+                    a2 += a_ks;
+                    b1 += 16u;
+                    b2 += 16u;
                 }
+                ah += 1u;
+                al += 1u;
+                bh += b_row;
+                bl += b_row;
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                          :: "r"(smem_u32(&mbar[b])) : "memory");
