@@ -769,7 +769,10 @@ int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *
     if ((rc = image_fill(border, img->eltype, ct, &fill))) return rc;
     int n[IFX_MAXD];
     for (int d = 0; d < IFX_MAXD; ++d) n[d] = d < nd ? (int)img->size[d] : 1;
-    if (method == 2) {
+    // automatic: tensor cores for 2-D kernels of 11 x 11 and larger (faster than the
+    // CUDA-core kernel there, within the 1e-5 normwise bound)
+    const bool use_tc = method == 2 || (method == 0 && tc_ok && ksize[0] >= 11 && nd > 1 && ksize[1] >= 11);
+    if (use_tc) {
         Dense2dArgs a{din, img->eltype, dout, out->eltype, n[0], nd > 1 ? n[1] : 1,
                       (int)kfirst[0], (int)ksize[0], nd > 1 ? (int)kfirst[1] : 0,
                       nd > 1 ? (int)ksize[1] : 1, kernel, border->style, fill, 0};
@@ -911,6 +914,28 @@ int ifx_imgradients(ifx_context_t *ctx, ifx_array_t *outs, const ifx_array_t *im
     if ((rc = begin(ctx, stream, c))) return rc;
     const void *din;
     if ((rc = c.input(*img, &din))) return rc;
+    // 3-D, 3-tap pair on every axis, one output eltype: the fused sweep
+    if (nd == 3 && length == 3 && first == -1 && extended[0] && extended[1] && extended[2] &&
+        outs[1].eltype == outs[0].eltype && outs[2].eltype == outs[0].eltype && img->eltype != IFX_I16) {
+        Grad3dArgs g{};
+        g.img = din;
+        g.in_type = img->eltype;
+        for (int d = 0; d < 3; ++d)
+            if ((rc = c.output(outs[d], &g.out[d]))) return rc;
+        g.out_type = outs[0].eltype;
+        g.nx = (int)img->size[0];
+        g.ny = (int)img->size[1];
+        g.nz = (int)img->size[2];
+        for (int t = 0; t < 3; ++t) {
+            g.d[t] = deriv[t];
+            g.s[t] = smooth[t];
+        }
+        g.compute_f64 = img->eltype == IFX_F64;
+        g.style = border->style;
+        if ((rc = image_fill(border, img->eltype, g.compute_f64 ? IFX_F64 : IFX_F32, &g.fill))) return rc;
+        IFX_CUDA(launch_grad3d(g, c.s));
+        return c.finish();
+    }
     for (int d = 0; d < nd; ++d) {
         void *dout;
         if ((rc = c.output(outs[d], &dout))) return rc;

@@ -622,6 +622,14 @@ cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s)
 // writes one output slice.  The x pass runs over the y halo and the x/y passes
 // over the z halo, as pad-then-cascade does (src/imfilter.jl:385-457).
 // =========================================================================
+// Unrolled tap chain when the factor is short enough, the sliding loop otherwise.
+template <int NB>
+__device__ __forceinline__ void corr_any(const float *p, int step, const float *w, int k, float *acc)
+{
+    if (k <= kCorrKmax) corr_col<NB>(p, step, w, k, acc);
+    else corr_run<float, NB>(p, step, w, k, acc);
+}
+
 constexpr int k3TX = 64, k3TY = 16, k3ZC = 32, k3MaxKz = 17;
 
 struct Sep3dW { float wx[IFX_MAX_TAPS + 3], wy[IFX_MAX_TAPS + 3], wz[k3MaxKz]; };
@@ -658,43 +666,76 @@ k_sep3d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny, int
     Tout *dst = out + vol * vstride;
     const long long plane = (long long)nx * ny;
     const int s_first = z0 + fz, s_last = z1 - 1 + fz + kz - 1;
+    // the x/y window of every slice lies inside the image: no border map in x/y
+    const bool inside_xy = tx0 + fx >= 0 && tx0 + fx + CV <= nx && ty0 + fy >= 0 && ty0 + fy + RT <= ny;
+    const int lane = tid & 31, warp = tid >> 5, nw = nth >> 5;
     float acc[NB];
     for (int s = s_first; s <= s_last; ++s) {
         const int ms = map_index(s, nz, style);
         __syncthreads();                       // T and I free again
-        gather_tile<8>(T, RT * CT, [&](int idx) -> float {
-            const int r = idx / CT, c = idx - r * CT;
-            if (c >= CV) return 0.0f;
-            const int mx = map_index(tx0 + fx + c, nx, style);
-            const int my = map_index(ty0 + fy + r, ny, style);
-            return (mx < 0 || my < 0 || ms < 0) ? fill
-                   : cvt<float, Tin>(src[(long long)ms * plane + (long long)my * nx + mx], norm);
-        });
+        // gather: warps take rows, lanes take columns (up to 4 column chunks in flight)
+        if (inside_xy && ms >= 0) {
+            const Tin *sp = src + (long long)ms * plane + (long long)(ty0 + fy) * nx + tx0 + fx;
+            for (int r = warp; r < RT; r += nw) {
+                const Tin *rp = sp + (long long)r * nx;
+                float v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = lane + 32 * q;
+                    v[q] = c < CV ? cvt<float, Tin>(rp[c], norm) : 0.0f;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = lane + 32 * q;
+                    if (c < CT) T[r * CT + c] = v[q];
+                }
+                for (int c = lane + 128; c < CT; c += 32) T[r * CT + c] = c < CV ? cvt<float, Tin>(rp[c], norm) : 0.0f;
+            }
+        } else {
+            for (int r = warp; r < RT; r += nw) {
+                const int my = map_index(ty0 + fy + r, ny, style);
+                for (int c = lane; c < CT; c += 32) {
+                    float v = 0.0f;
+                    if (c < CV) {
+                        const int mx = map_index(tx0 + fx + c, nx, style);
+                        v = (mx < 0 || my < 0 || ms < 0)
+                                ? fill
+                                : cvt<float, Tin>(src[(long long)ms * plane + (long long)my * nx + mx], norm);
+                    }
+                    T[r * CT + c] = v;
+                }
+            }
+        }
         __syncthreads();
         const int segs = TX / NB;
         for (int it = tid; it < RT * segs; it += nth) {
             const int r = it / segs, c0 = (it - r * segs) * NB;
-            corr_run<float, NB>(T + r * CT + c0, 1, wx, kx, acc);
+            corr_any<NB>(T + r * CT + c0, 1, wx, kx, acc);
 #pragma unroll
             for (int i = 0; i < NB; ++i) I[r * TX + c0 + i] = acc[i];
         }
         __syncthreads();
         float *slot = ring + ((s - s_first) % kz) * (TY * TX);
-        for (int it = tid; it < TX * (TY / NB); it += nth) {
-            const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
-            corr_run<float, NB>(I + r0 * TX + c, TX, wy, ky, acc);
+        constexpr int NBY = 4;                 // TX * TY / 4 items: one per thread
+        for (int it = tid; it < TX * (TY / NBY); it += nth) {
+            const int rs = it / TX, c = it - rs * TX, r0 = rs * NBY;
+            corr_any<NBY>(I + r0 * TX + c, TX, wy, ky, acc);
 #pragma unroll
-            for (int i = 0; i < NB; ++i) slot[(r0 + i) * TX + c] = acc[i];
+            for (int i = 0; i < NBY; ++i) slot[(r0 + i) * TX + c] = acc[i];
         }
         __syncthreads();
         const int z = s - fz - (kz - 1);       // output slice completed by this input slice
         if (z >= z0) {
+            const int slot0 = (z + fz - s_first) % kz;     // ring slot of tap 0
             for (int it = tid; it < TX * TY; it += nth) {
                 const int r = it / TX, c = it - r * TX;
                 const int x = tx0 + c, y = ty0 + r;
                 float a = 0.0f;
-                for (int t = 0; t < kz; ++t)
-                    a = fmaf(wz[t], ring[((z + fz + t - s_first) % kz) * (TY * TX) + it], a);
+                int sl = slot0;
+                for (int t = 0; t < kz; ++t) {
+                    a = fmaf(wz[t], ring[sl * (TY * TX) + it], a);
+                    if (++sl == kz) sl = 0;
+                }
                 if (x < nx && y < ny) dst[(long long)z * plane + (long long)y * nx + x] = out_cvt<Tout>(a);
             }
         }
@@ -737,6 +778,114 @@ cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s)
     if (it == IFX_F32 && ot == IFX_F64) return sep3d_t<float, double>(a, s);
     if (is8(it) && ot == IFX_F32) return sep3d_t<uint8_t, float>(a, s);
     if (is8(it) && ot == IFX_F64) return sep3d_t<uint8_t, double>(a, s);
+    return cudaErrorInvalidValue;
+}
+
+// =========================================================================
+// Fused 3-D gradients (imgradients with a 3-tap (derivative, smoothing) pair
+// on all three axes, src/specialty.jl:39-53): gradient d is the cascade of
+// the derivative along axis d and the smoothing along the other axes, in axis
+// order (x, y, z), pad-then-cascade.  The three cascades share their passes:
+// x gives Dx and Sx; y gives SyDx, DySx and SySx; z gives gx = Sz(SyDx),
+// gy = Sz(DySx), gz = Dz(SySx).  A CTA owns a TX x TY column and a chunk of
+// ZC output slices and marches over the chunk's input slices (ZC + 2): each is
+// gathered through the border map with its x/y halo, the x pass runs over the
+// halo rows, the y results go into a ring of three slices, and the z pass
+// writes one output slice of all three gradients.  Every pass sums its three
+// taps in order -1, 0, 1, as the reference's 1-D loop does.
+// =========================================================================
+constexpr int kG3TX = 32, kG3ZC = 32;
+template <class Tc> constexpr int g3ty() { return sizeof(Tc) == 8 ? 8 : 16; }   // static smem < 48 KB
+
+template <class Tc>
+__device__ __forceinline__ Tc tap3(const Tc *w, Tc a, Tc b, Tc c)
+{
+    return fma(w[2], c, fma(w[1], b, w[0] * a));
+}
+
+template <class Tin, class Tc, class Tout>
+__global__ void __launch_bounds__(256)
+k_grad3d(const Tin *__restrict__ img, Tout *__restrict__ gx, Tout *__restrict__ gy, Tout *__restrict__ gz,
+         int nx, int ny, int nz, Tc d0, Tc d1, Tc d2, Tc s0, Tc s1, Tc s2, int style, Tc fill, bool norm)
+{
+    constexpr int TX = kG3TX, TY = g3ty<Tc>(), RT = TY + 2, CT = TX + 2;
+    __shared__ Tc T[RT * CT];                   // input slice tile with x/y halo
+    __shared__ Tc Dx[RT * TX], Sx[RT * TX];     // x pass over the halo rows
+    __shared__ Tc ring[3][3][TY * TX];          // slot, (SyDx, DySx, SySx), pixel
+    const Tc dw[3] = {d0, d1, d2}, sw[3] = {s0, s1, s2};
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
+    const int z0 = blockIdx.z * kG3ZC, z1 = min(nz, z0 + kG3ZC);
+    const long long plane = (long long)nx * ny;
+    for (int sl = z0 - 1; sl <= z1; ++sl) {
+        const int ms = map_index(sl, nz, style);
+        __syncthreads();                        // T, Dx, Sx free again
+        gather_tile<4>(T, RT * CT, [&](int idx) -> Tc {
+            const int r = idx / CT, c = idx - r * CT;
+            const int mx = map_index(tx0 - 1 + c, nx, style);
+            const int my = map_index(ty0 - 1 + r, ny, style);
+            return (mx < 0 || my < 0 || ms < 0) ? fill
+                   : cvt<Tc, Tin>(img[(long long)ms * plane + (long long)my * nx + mx], norm);
+        });
+        __syncthreads();
+        for (int e = tid; e < RT * TX; e += nth) {
+            const int r = e / TX, c = e - r * TX;
+            const Tc *p = T + r * CT + c;
+            Dx[e] = tap3(dw, p[0], p[1], p[2]);
+            Sx[e] = tap3(sw, p[0], p[1], p[2]);
+        }
+        __syncthreads();
+        const int slot = (sl - (z0 - 1)) % 3;
+        for (int e = tid; e < TY * TX; e += nth) {
+            const int r = e / TX, c = e - r * TX;
+            const int i0 = r * TX + c, i1 = i0 + TX, i2 = i1 + TX;
+            ring[slot][0][e] = tap3(sw, Dx[i0], Dx[i1], Dx[i2]);
+            ring[slot][1][e] = tap3(dw, Sx[i0], Sx[i1], Sx[i2]);
+            ring[slot][2][e] = tap3(sw, Sx[i0], Sx[i1], Sx[i2]);
+        }
+        __syncthreads();
+        const int z = sl - 1;                   // output slice completed by this input slice
+        if (z >= z0) {
+            const int a = (z - 1 - (z0 - 1)) % 3, b = (z - (z0 - 1)) % 3, c3 = (z + 1 - (z0 - 1)) % 3;
+            for (int e = tid; e < TY * TX; e += nth) {
+                const int r = e / TX, c = e - r * TX;
+                const int x = tx0 + c, y = ty0 + r;
+                if (x >= nx || y >= ny) continue;
+                const long long o = (long long)z * plane + (long long)y * nx + x;
+                gx[o] = out_cvt<Tout>(tap3(sw, ring[a][0][e], ring[b][0][e], ring[c3][0][e]));
+                gy[o] = out_cvt<Tout>(tap3(sw, ring[a][1][e], ring[b][1][e], ring[c3][1][e]));
+                gz[o] = out_cvt<Tout>(tap3(dw, ring[a][2][e], ring[b][2][e], ring[c3][2][e]));
+            }
+        }
+    }
+}
+
+template <class Tin, class Tc, class Tout>
+static cudaError_t grad3d_t(const Grad3dArgs &a, cudaStream_t s)
+{
+    dim3 grid((a.nx + kG3TX - 1) / kG3TX, (a.ny + g3ty<Tc>() - 1) / g3ty<Tc>(), (a.nz + kG3ZC - 1) / kG3ZC);
+    k_grad3d<Tin, Tc, Tout><<<grid, 256, 0, s>>>(
+        (const Tin *)a.img, (Tout *)a.out[0], (Tout *)a.out[1], (Tout *)a.out[2], a.nx, a.ny, a.nz,
+        (Tc)a.d[0], (Tc)a.d[1], (Tc)a.d[2], (Tc)a.s[0], (Tc)a.s[1], (Tc)a.s[2], a.style, (Tc)a.fill,
+        a.in_type == IFX_N0F8);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grad3d(const Grad3dArgs &a, cudaStream_t s)
+{
+    if ((long long)a.nx * a.ny * a.nz == 0) return cudaSuccess;
+    if ((a.ny + 7) / 8 > 65535 || (a.nz + kG3ZC - 1) / kG3ZC > 65535) return cudaErrorInvalidValue;
+    const int it = a.in_type, ot = a.out_type;
+    if (a.compute_f64) {
+        if (it == IFX_F64 && ot == IFX_F64) return grad3d_t<double, double, double>(a, s);
+        if (it == IFX_F64 && ot == IFX_F32) return grad3d_t<double, double, float>(a, s);
+        return cudaErrorInvalidValue;
+    }
+    if (it == IFX_F32 && ot == IFX_F64) return grad3d_t<float, float, double>(a, s);
+    if (it == IFX_F32 && ot == IFX_F32) return grad3d_t<float, float, float>(a, s);
+    if (is8(it) && ot == IFX_F64) return grad3d_t<uint8_t, float, double>(a, s);
+    if (is8(it) && ot == IFX_F32) return grad3d_t<uint8_t, float, float>(a, s);
     return cudaErrorInvalidValue;
 }
 

@@ -58,6 +58,18 @@ struct Sep3dArgs {
 bool sep3d_supported(int kx, int ky, int kz, int nx, int ny, int nz, int nvol);
 cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s);
 
+// Fused 3-D gradients (3-tap derivative / smoothing pair, all axes extended):
+// the three imgradients outputs from one sweep -----------------------------
+struct Grad3dArgs {
+    const void *img; int in_type;
+    void *out[3]; int out_type;
+    int nx, ny, nz;
+    double d[3], s[3];                     // derivative and smoothing taps (first index -1)
+    int style; double fill;
+    int compute_f64;
+};
+cudaError_t launch_grad3d(const Grad3dArgs &a, cudaStream_t s);
+
 // Dense --------------------------------------------------------------------
 struct Dense2dArgs {
     const void *img; int in_type;

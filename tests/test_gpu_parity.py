@@ -277,6 +277,28 @@ def test_imgradients(gpu_ifx, oracle, name, style):
             assert normwise(g, ref) <= 1e-5 or np.max(np.abs(g - ref)) < 1e-6, (shape, d)
 
 
+@pytest.mark.parametrize("kind", ["F64", "F32", "N0F8"])
+@pytest.mark.parametrize("style", STYLES)
+def test_imgradients_3d_fused(gpu_ifx, oracle, kind, style):
+    """3-D volumes with a 3-tap pair on every axis take the fused sweep (all
+    three gradients at once, z-marching, several z chunks): each gradient equals
+    its own pad-then-cascade (FP64 for Float64 volumes)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("g3" + kind + style).encode()))
+    for shape, name in [((37, 21, 70), "sobel"), ((64, 17, 9), "scharr")]:
+        img = make_img(rng, shape, kind)
+        fn = getattr(ifx.KernelFactors, name)
+        k1, k2 = fn.gradient_pair
+        gs = ifx.imgradients(wrap(ifx, img, kind), fn, border_of(ifx, style, 0.3))
+        assert len(gs) == 3
+        for d, g in enumerate(gs):
+            facs = [(e, -1, k1 if e == d else k2) for e in range(3)]
+            ref = oracle.imfilter_cascade(values(ifx, img, kind), facs, style, fill_value(kind, 0.3))
+            assert g.dtype == np.float64
+            tol = 1e-12 if kind == "F64" else 1e-5
+            assert normwise(g, ref) <= tol or np.max(np.abs(g - ref)) < tol / 10, (shape, d, style)
+
+
 def test_imgradients_ando4_dense_kernels(gpu_ifx, oracle):
     ifx = gpu_ifx
     img = np.asfortranarray(np.random.default_rng(5).random((30, 31)))
@@ -464,6 +486,9 @@ def test_dense_tensor_cores(gpu_ifx, oracle, ksz, seed, style):
     ref = oracle.imfilter_dense(img.astype(np.float64), K, kern.first, style, 0.0)
     assert got.dtype == np.float64
     assert normwise(got, ref) <= 1e-5
+    # the automatic method takes the tensor cores from 11 x 11 up: the same kernel
+    auto = ifx.imfilter(img, kern, b, ifx.Algorithm.GB300())
+    assert np.array_equal(auto, got)
 
 
 def test_dense_tensor_cores_shapes(gpu_ifx, oracle):
