@@ -175,6 +175,11 @@ def stream_calls(ifx, reqs, dev_inputs, out_arena, torch):
     return calls, keep, off
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum over algorithmic bytes for one k_batch
+# launch on a 60-request wave of the same stream (206.356 + 884.533 MB / 1147.791 MB)
+K_BATCH_TRAFFIC_RATIO = (206.356224 + 884.532736) / 1147.791071
+
+
 def alg_bytes(r):
     return r.in_bytes() + r.out_bytes()
 
@@ -770,7 +775,11 @@ def main():
         "gpu_launches": res["launches"],
         "roofline": {"bound": "hbm", "kernel": "k_batch (persistent tile work-queue)",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": None,
+                     "frac": achieved / hbm_peak, "peak_source": peak_src,
+                     "traffic": round(K_BATCH_TRAFFIC_RATIO * bk_bytes / max(bk_n, 1)),
+                     "traffic_source": "DRAM read+write bytes of one k_batch launch, ncu capture of a "
+                                       "60-request wave (profiles/k_batch_mixed_stream.md): %.4f x the "
+                                       "algorithmic bytes, scaled to this launch's" % K_BATCH_TRAFFIC_RATIO,
                      "launches": bk_n, "alg_bytes_per_launch": bk_bytes / max(bk_n, 1)},
         "clocks": res["clocks"],
         "dense_4096": dense,
