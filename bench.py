@@ -777,9 +777,9 @@ def main():
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": peak_src,
                      "traffic": round(K_BATCH_TRAFFIC_RATIO * bk_bytes / max(bk_n, 1)),
-                     "traffic_source": "DRAM read+write bytes of one k_batch launch, ncu capture of a "
-                                       "60-request wave (profiles/k_batch_mixed_stream.md): %.4f x the "
-                                       "algorithmic bytes, scaled to this launch's" % K_BATCH_TRAFFIC_RATIO,
+                     "traffic_source": "DRAM read+write bytes of one k_batch launch in an ncu capture "
+                                       "of a 60-request wave of the same stream: %.4f x the algorithmic "
+                                       "bytes, scaled to this launch's" % K_BATCH_TRAFFIC_RATIO,
                      "launches": bk_n, "alg_bytes_per_launch": bk_bytes / max(bk_n, 1)},
         "clocks": res["clocks"],
         "dense_4096": dense,

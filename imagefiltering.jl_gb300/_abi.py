@@ -89,7 +89,8 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_mapwindow_extrema", "ifx_batch_run", "ifx_batch_plan_create", "ifx_batch_plan_launch",
            "ifx_batch_plan_destroy", "ifx_server_create", "ifx_server_submit",
            "ifx_server_wait", "ifx_server_drain", "ifx_server_metrics", "ifx_server_reset_metrics",
-           "ifx_server_destroy", "ifx_noalloc_scratch_bytes", "ifx_imfilter_factored_noalloc"]
+           "ifx_server_destroy", "ifx_noalloc_scratch_bytes", "ifx_imfilter_factored_noalloc",
+           "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable"]
 
 _lib = None
 _lock = threading.Lock()
@@ -138,6 +139,10 @@ def load(path: str = LIB_PATH):
         lib.ifx_server_metrics.argtypes = [vp, P(IfxServerMetrics)]
         lib.ifx_server_reset_metrics.argtypes = [vp]
         lib.ifx_server_destroy.argtypes = [vp]
+        lib.ifx_na_prepare.argtypes = [vp, P(IfxArray), P(IfxArray), P(IfxArray), C.c_int32,
+                                       P(C.c_int32), vp]
+        lib.ifx_na_divide.argtypes = [vp, P(IfxArray), P(IfxArray), vp]
+        lib.ifx_na_normalize_separable.argtypes = [vp, P(IfxArray), P(IfxArray), vp]
         lib.ifx_noalloc_scratch_bytes.restype = C.c_uint64
         lib.ifx_imfilter_factored_noalloc.argtypes = [P(IfxArray), P(IfxArray), C.c_int32, P(IfxFactor),
                                                       P(IfxBorder), vp]

@@ -53,11 +53,51 @@ class Fill:
 
 
 class Inner:
-    """Inner() -- not part of the GB300 path."""
+    """Inner(), Inner(lo, hi) (src/border.jl:356-386): edges are discarded and
+    only the interior of the result is returned -- the indices where the whole
+    kernel support lies inside the image (Inner()), or inner.(lo, axes(img),
+    hi) for explicit widths.  Results carry their first indices (`first`)."""
+
+    def __init__(self, lo=None, hi=None):
+        if lo is not None and hi is None:
+            hi = lo
+        self.lo = tuple(int(x) for x in lo) if lo is not None else None
+        self.hi = tuple(int(x) for x in hi) if hi is not None else None
+        if self.lo is not None and len(self.lo) != len(self.hi):
+            raise _abi.ArgumentError("Inner: lo and hi need the same number of dimensions")
+
+    def __repr__(self):
+        return "Inner(%s, %s)" % (self.lo, self.hi)
 
 
 class NA:
-    """NA() -- not part of the GB300 path."""
+    """NA(na="isnan") (src/border.jl:388-405): output = (filtered array with
+    Fill(0)) / (filtered ones with Fill(0)); elements for which `na` holds are
+    also outside the image.  The predicate is one of "isnan" (the default),
+    "notfinite" (NA(!isfinite)) or "none" (NA(x -> false)): a Julia closure
+    cannot cross the C ABI."""
+
+    CODES = {"isnan": 0, "notfinite": 1, "none": 2}
+
+    def __init__(self, na="isnan"):
+        if na not in self.CODES:
+            raise _abi.ArgumentError("NA predicate must be one of %s" % sorted(self.CODES))
+        self.na = na
+
+    def __repr__(self):
+        return "NA(%r)" % self.na
+
+
+class NoPad:
+    """NoPad(border=None) (src/border.jl:7-30): the image needs no padding --
+    every index the requested outputs read lies inside it (imfilter_ with
+    `inds`)."""
+
+    def __init__(self, border=None):
+        self.border = border
+
+    def __repr__(self):
+        return "NoPad(%r)" % (self.border,)
 
 
 def borderinstance(border):
@@ -69,8 +109,6 @@ def borderinstance(border):
             raise _abi.ArgumentError("specifying Inner as a string is deprecated, use "
                                      "`imfilter(img, kern, Inner())` instead")
         raise _abi.ArgumentError("%s not a recognized border" % border)
-    if isinstance(border, (Inner, NA)):
-        raise _abi.Unsupported("%s borders are not part of the GB300 path" % type(border).__name__)
     return border
 
 
@@ -101,6 +139,8 @@ def fill_value_for(border, kind):
 def border_struct(border, ndim, kind):
     """The C descriptor of a border for an image of element kind `kind`."""
     border = borderinstance(border)
+    if isinstance(border, (Inner, NA, NoPad)):
+        raise _abi.ArgumentError("%r is not a padding border" % (border,))
     fill = fill_value_for(border, kind)
     if border.lo is not None and (len(border.lo) != ndim or len(border.hi) != ndim):
         raise _abi.ArgumentError("%r lacks the proper padding sizes for an array with %d "

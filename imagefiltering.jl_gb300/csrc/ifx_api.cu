@@ -1169,4 +1169,91 @@ int ifx_batch_plan_destroy(ifx_batch_plan_t *plan)
     return IFX_OK;
 }
 
+// ---------------------------------------------------------------- NA()
+int ifx_na_prepare(ifx_context_t *ctx, ifx_array_t *zeroed, ifx_array_t *valid, const ifx_array_t *img,
+                   int32_t na, int32_t *has_na, void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img")) || (rc = check_array(zeroed, "zeroed")) ||
+        (rc = check_array(valid, "valid")))
+        return rc;
+    if ((rc = check_same_axes(*zeroed, *img)) || (rc = check_same_axes(*valid, *img))) return rc;
+    if (!has_na) return fail(IFX_ERR_ARGUMENT, "has_na is NULL");
+    if (na < IFX_NA_ISNAN || na > IFX_NA_NONE) return fail(IFX_ERR_ARGUMENT, "unknown NA predicate %d", na);
+    if ((zeroed->eltype != IFX_F32 && zeroed->eltype != IFX_F64) ||
+        (valid->eltype != IFX_F32 && valid->eltype != IFX_F64))
+        return fail(IFX_ERR_UNSUPPORTED, "NA filtering works in Float32 or Float64");
+    if (img->eltype == IFX_I16) return fail(IFX_ERR_UNSUPPORTED, "Int16 images are not supported");
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *dz, *dv, *flag;
+    if ((rc = c.input(*img, &din)) || (rc = c.output(*zeroed, &dz)) || (rc = c.output(*valid, &dv))) return rc;
+    if ((rc = slot_get(ctx, 23, sizeof(int), &flag))) return rc;
+    IFX_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), c.s));
+    IFX_CUDA(launch_na_prepare(din, img->eltype, dz, zeroed->eltype, dv, valid->eltype, numel(*img), na,
+                               (int *)flag, c.s));
+    int h = 0;
+    IFX_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+    if ((rc = c.finish())) return rc;
+    IFX_CUDA(cudaStreamSynchronize(c.s));      // has_na is read on the host
+    *has_na = h;
+    return IFX_OK;
+}
+
+int ifx_na_divide(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *den, void *stream)
+{
+    int rc;
+    if ((rc = check_array(out, "out")) || (rc = check_array(den, "den")) || (rc = check_same_axes(*out, *den)))
+        return rc;
+    if ((out->eltype != IFX_F32 && out->eltype != IFX_F64) || (den->eltype != IFX_F32 && den->eltype != IFX_F64))
+        return fail(IFX_ERR_UNSUPPORTED, "NA normalisation works in Float32 or Float64");
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *dd;
+    void *dout;
+    // out is read and written: stage it as an input and copy it back
+    if ((rc = c.input(*out, (const void **)&dout)) || (rc = c.input(*den, &dd))) return rc;
+    if (c.host && !is_device_ptr(out->data)) c.back.push_back({out->data, dout, (size_t)numel(*out) * elsize(out->eltype)});
+    IFX_CUDA(launch_na_divide(dout, out->eltype, dd, den->eltype, numel(*out), c.s));
+    return c.finish();
+}
+
+int ifx_na_normalize_separable(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *sums, void *stream)
+{
+    int rc;
+    if ((rc = check_array(out, "out"))) return rc;
+    if (!sums) return fail(IFX_ERR_ARGUMENT, "sums is NULL");
+    if (out->eltype != IFX_F32 && out->eltype != IFX_F64)
+        return fail(IFX_ERR_UNSUPPORTED, "NA normalisation works in Float32 or Float64");
+    const int nd = out->ndim;
+    for (int d = 0; d < nd; ++d) {
+        if ((rc = check_array(&sums[d], "sums[d]"))) return rc;
+        if (sums[d].eltype != IFX_F64 || sums[d].ndim != 1 || sums[d].size[0] != out->size[d])
+            return fail(IFX_ERR_DIMENSION, "sums[%d] must be a Float64 vector of length %lld", d,
+                        (long long)out->size[d]);
+    }
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    void *dout;
+    if ((rc = c.input(*out, (const void **)&dout))) return rc;
+    if (c.host && !is_device_ptr(out->data)) c.back.push_back({out->data, dout, (size_t)numel(*out) * elsize(out->eltype)});
+    const double *f[IFX_MAXD] = {};
+    long long n[IFX_MAXD] = {};
+    for (int d = 0; d < nd; ++d) {
+        const void *p;
+        if ((rc = c.input(sums[d], &p))) return rc;
+        f[d] = (const double *)p;
+        n[d] = out->size[d];
+    }
+    IFX_CUDA(launch_na_normalize(dout, out->eltype, numel(*out), f, n, nd, c.s));
+    return c.finish();
+}
+
 } // extern "C"

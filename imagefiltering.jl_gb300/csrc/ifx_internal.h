@@ -70,6 +70,13 @@ struct Grad3dArgs {
 };
 cudaError_t launch_grad3d(const Grad3dArgs &a, cudaStream_t s);
 
+// NA() pieces -----------------------------------------------------------------
+cudaError_t launch_na_prepare(const void *img, int it, void *z, int zt, void *v, int vt, long long n, int na,
+                              int *flag, cudaStream_t s);
+cudaError_t launch_na_divide(void *out, int ot, const void *den, int dt, long long n, cudaStream_t s);
+cudaError_t launch_na_normalize(void *out, int ot, long long total, const double *const *f, const long long *n,
+                                int nd, cudaStream_t s);
+
 // Dense --------------------------------------------------------------------
 struct Dense2dArgs {
     const void *img; int in_type;

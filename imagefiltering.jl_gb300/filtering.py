@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _abi
 from .arrays import DeviceArray, alloc_like, host_view, kind_of, ptr_strides, stream_for
-from .borders import border_struct, borderinstance
+from .borders import Fill, Inner, NA, NoPad, border_struct, borderinstance
 from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD,
                       iscopy)
 
@@ -181,8 +181,146 @@ def _desc(a, kind, first=None):
     return _abi.describe(p, kind, a.shape, st, first)
 
 
+# ------------------------------------------------------------------ Inner / NA / NoPad
+def kernel_support(kernel, nd):
+    """calculate_padding / accumulate_padding (src/border.jl:640-652): the
+    lowest and highest offset each axis of the processed kernel reads."""
+    lo, hi = [0] * nd, [0] * nd
+    for k in kernel:
+        if iscopy(k):
+            continue
+        if isinstance(k, LaplacianKernel):
+            for d, f in enumerate(k.flags[:nd]):
+                if f:
+                    lo[d] -= 1
+                    hi[d] += 1
+        elif isinstance(k, ReshapedOneD):
+            n = np.asarray(k.data.data).size
+            lo[k.axis] += k.data.first[0]
+            hi[k.axis] += k.data.first[0] + n - 1
+        else:
+            for d in range(min(k.ndim, nd)):
+                lo[d] += k.first[d]
+                hi[d] += k.first[d] + k.shape[d] - 1
+    return lo, hi
+
+
+class OffsetResult(np.ndarray):
+    """A host result whose axes do not start at 1 (an OffsetArray of the
+    reference): `first` holds each axis' first index."""
+
+    def __array_finalize__(self, obj):
+        self.first = getattr(obj, "first", None)
+
+
+def _region(a, first, inds):
+    """a[inds] where a's axes start at `first` and inds are 1-based ranges (lo, hi)."""
+    return tuple(slice(l - f, h - f + 1) for (l, h), f in zip(inds, first))
+
+
+def _with_first(a, first):
+    if isinstance(a, DeviceArray):
+        t = a.tensor
+        return DeviceArray(t if t.is_contiguous() else t.contiguous(), a.kind, first)
+    r = np.asfortranarray(a).view(OffsetResult)
+    r.first = tuple(first)
+    return r
+
+
+def _check_reads(inds, kernel, img_shape, what):
+    lo, hi = kernel_support(kernel, len(img_shape))
+    for d, ((a, b), n) in enumerate(zip(inds, img_shape)):
+        if a > b:
+            continue
+        if a + lo[d] < 1 or b + hi[d] > n:
+            raise _abi.ArgumentError("BoundsError: %s on axis %d reads indices %d:%d of an axis 1:%d"
+                                     % (what, d + 1, a + lo[d], b + hi[d], n))
+
+
+def _imfilter_inner(img, kernel, border, alg, T, kind):
+    nd = img.ndim
+    if border.lo is None:
+        lo, hi = kernel_support(kernel, nd)
+        inds = [(max(1, 1 - l), min(n, n - h)) for l, h, n in zip(lo, hi, img.shape)]
+    else:
+        if len(border.lo) != nd:
+            raise _abi.DimensionMismatch("dimensionality of img and the border must agree, got %d "
+                                         "and %d" % (nd, len(border.lo)))
+        inds = [(1 + l, n - h) for l, h, n in zip(border.lo, border.hi, img.shape)]
+        _check_reads(inds, kernel, img.shape, "Inner()")
+    # every output in `inds` reads inside the image: the border style is moot
+    full = imfilter(img, kernel, "replicate", alg, T)
+    sl = _region(full, (1,) * nd, inds)
+    part = full.tensor[sl] if isinstance(full, DeviceArray) else full[sl]
+    if isinstance(full, DeviceArray):
+        part = DeviceArray(part, full.kind)
+    return _with_first(part, tuple(a for a, _ in inds))
+
+
+def _separable_factors(kernel, nd):
+    """isseparable (src/imfilter.jl:1218-1219: every factor has one extended
+    dimension) with N factors for N dimensions, as normalize_separable!
+    (1234-1239) needs: factor d's 1-D data (_vec) with its first index, which
+    normalize_separable! pairs with axis d by position."""
+    if len(kernel) != nd:
+        return None
+    out = []
+    for k in kernel:
+        if isinstance(k, ReshapedOneD):
+            out.append((k.data.first[0], np.asarray(k.data.data, dtype=np.float64).reshape(-1)))
+        elif isinstance(k, OffsetKernel):
+            ext = [d for d in range(k.ndim) if k.shape[d] > 1]
+            if len(ext) != 1:
+                return None
+            out.append((k.first[ext[0]], np.asarray(k.data, dtype=np.float64).reshape(-1)))
+        else:
+            return None
+    return out
+
+
+def _imfilter_na(out, img, kernel, border, alg, kind, okind):
+    """_imfilter_na! (src/imfilter.jl:280-318) with imfilter_na_separable! and
+    imfilter_na_inseparable! (1094-1130): the filters are the library's Fill(0)
+    filters, the NA mask and the divisions are ifx_na_* kernels."""
+    if okind not in ("F32", "F64"):
+        raise _abi.Unsupported("NA filtering writes Float32 or Float64 outputs")
+    ctx = _ctx()
+    nd = img.ndim
+    na = border.na if kind in ("F32", "F64") else "none"
+    zeroed = alloc_like(img, img.shape, okind)
+    valid = alloc_like(img, img.shape, okind)
+    has = C.c_int32(0)
+    _abi.check(ctx.lib.ifx_na_prepare(ctx.handle, _desc(zeroed, okind), _desc(valid, okind),
+                                      _desc(img, kind), NA.CODES[na], C.byref(has),
+                                      stream_for(img, zeroed)))
+    seps = _separable_factors(kernel, nd)
+    if seps is not None and not has.value:
+        imfilter_(out, img, kernel, Fill(0), alg)
+        sums, keep = [], []
+        for d, (first, w) in enumerate(seps):
+            ones = alloc_like(img, (img.shape[d],), "F64")
+            if isinstance(ones, DeviceArray):
+                ones.tensor.fill_(1.0)
+            else:
+                ones[...] = 1.0
+            k1 = (ReshapedOneD(OffsetKernel(w, (first,)), 1, 0),)
+            sd = imfilter(ones, k1, Fill(0), alg)
+            keep.append(sd)
+            sums.append(_desc(sd, "F64"))
+        arr = (_abi.IfxArray * nd)(*sums)
+        _abi.check(ctx.lib.ifx_na_normalize_separable(ctx.handle, _desc(out, okind), arr,
+                                                      stream_for(out, img)))
+        return out
+    imfilter_(out, zeroed, kernel, Fill(0), alg)
+    vp = imfilter(valid, kernel, Fill(0), alg)
+    _abi.check(ctx.lib.ifx_na_divide(ctx.handle, _desc(out, okind), _desc(vp, kind_of(vp)),
+                                     stream_for(out, vp)))
+    return out
+
+
 def imfilter(img, kernel, border="replicate", alg=None, T=None):
-    """imfilter([T], img, kernel, [border="replicate"], [alg]) (src/imfilter.jl:1-27)."""
+    """imfilter([T], img, kernel, [border="replicate"], [alg]) (src/imfilter.jl:1-27).
+    With Inner() the result covers only the interior and carries `first`."""
     kind = kind_of(img)
     if not isinstance(img, DeviceArray):
         img = host_view(img, kind)
@@ -190,12 +328,17 @@ def imfilter(img, kernel, border="replicate", alg=None, T=None):
     kernel = factorkernel(kernel)
     if T is None:
         T = filter_type(kind, kernel)
+    border = borderinstance(border)
+    if isinstance(border, Inner):
+        return _imfilter_inner(img, kernel, border, alg, T, kind)
     out = alloc_like(img, img.shape, T)
     return imfilter_(out, img, kernel, border, alg)
 
 
-def imfilter_(out, img, kernel, border="replicate", alg=None):
-    """imfilter!(out, img, kernel, [border], [alg]) (src/imfilter.jl:204-254)."""
+def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
+    """imfilter!(out, img, kernel, [border], [alg]) (src/imfilter.jl:204-254);
+    imfilter!(out, img, kernel, NoPad(), inds) computes only out[inds] (1-based
+    (first, last) per axis), reading only inside img (src/imfilter.jl:367-404)."""
     kind = kind_of(img)
     if not isinstance(img, DeviceArray):
         img = host_view(img, kind)
@@ -203,6 +346,27 @@ def imfilter_(out, img, kernel, border="replicate", alg=None):
     okind = kind_of(out)
     kernel = factorkernel(kernel)
     nd = img.ndim
+    border = borderinstance(border)
+    if inds is not None or isinstance(border, NoPad):
+        if not isinstance(border, NoPad):
+            raise _abi.ErrorException("Invalid border strategy `%r`: only `NoPad()` is supported." % (border,))
+        if inds is None:
+            inds = [(1, n) for n in out.shape]
+        inds = [(int(a), int(b)) for a, b in inds]
+        if len(inds) != nd or any(b > n for (a, b), n in zip(inds, out.shape)):
+            raise _abi.DimensionMismatch("inds must lie within the axes of out")
+        _check_reads(inds, kernel, img.shape, "NoPad()")
+        full = imfilter(img, kernel, "replicate", alg, okind)
+        sl = _region(out, (1,) * nd, inds)
+        if isinstance(out, DeviceArray):
+            out.tensor[sl] = full.tensor[sl]
+        else:
+            out[sl] = full[sl]
+        return out
+    if isinstance(border, NA):
+        return _imfilter_na(out, img, kernel, border, alg, kind, okind)
+    if isinstance(border, Inner):
+        raise _abi.ArgumentError("imfilter! with Inner(): allocate the interior with imfilter")
     b = border_struct(border, nd, kind)
     ai = _desc(img, kind)
     ao = _desc(out, okind)
@@ -251,6 +415,24 @@ def imgradients(img, kernelfun=None, border="replicate"):
         img = host_view(img, kind)
     nd = img.ndim
     extended = [n > 1 for n in img.shape]
+    if isinstance(borderinstance(border), Inner):
+        # each gradient's interior: its kernel reads inside the image there
+        grads = imgradients(img, kernelfun, "replicate")
+        pair = getattr(kernelfun, "gradient_pair", None)
+        if pair is not None:
+            first = 1 - (np.asarray(pair[0]).size + 1) // 2
+            lo = [first if e else 0 for e in extended]
+            hi = [first + np.asarray(pair[0]).size - 1 if e else 0 for e in extended]
+        else:
+            k = _dense_of(kernelfun(tuple(extended), 1), nd)
+            lo, hi = list(k.first), [f + n - 1 for f, n in zip(k.first, k.shape)]
+        inds = [(max(1, 1 - l), min(n, n - h)) for l, h, n in zip(lo, hi, img.shape)]
+        out = []
+        for g in grads:
+            sl = _region(g, (1,) * nd, inds)
+            part = DeviceArray(g.tensor[sl], g.kind) if isinstance(g, DeviceArray) else g[sl]
+            out.append(_with_first(part, tuple(a for a, _ in inds)))
+        return tuple(out)
     if getattr(kernelfun, "dense_of", None):          # Kernel.sobel & co: dense 1-tuples
         outs = []
         for d in range(1, nd + 1):

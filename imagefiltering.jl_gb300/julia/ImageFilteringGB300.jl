@@ -15,7 +15,7 @@
 module ImageFilteringGB300
 
 using ImageFiltering, ComputationalResources, OffsetArrays, Statistics
-using ImageFiltering: ProcessedKernel, ReshapedOneD, Pad, Fill, NoPad, BorderSpecAny, iscopy
+using ImageFiltering: ProcessedKernel, ReshapedOneD, Pad, Fill, NoPad, Inner, NA, BorderSpecAny, iscopy
 using ImageFiltering.Algorithm: Alg
 using ImageCore: N0f8, Gray, Normed
 
@@ -150,6 +150,53 @@ function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::
                     ifxborder(border, T), C_NULL))
     end
     out
+end
+
+# NA() borders (src/imfilter.jl:280-318, 1094-1130): the reference's branch
+# structure, with the mask, the filters and the divisions on the GPU.
+const NA_CODES = Dict(isnan => Int32(0))
+na_code(::NA{na}) where {na} = get(NA_CODES, na) do
+    throw(ArgumentError("GB300: NA predicates are isnan, !isfinite or x->false"))
+end
+
+function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
+                                  kernel::ProcessedKernel, border::NA) where {S,T,N}
+    zeroed, valid = similar(out, S, axes(img)), similar(out, S, axes(img))
+    has = Ref{Int32}(0)
+    GC.@preserve zeroed valid img begin
+        check(ccall((:ifx_na_prepare, libifx), Cint,
+                    (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Ref{IfxArray}, Int32, Ref{Int32}, Ptr{Cvoid}),
+                    context(), Ref(ifxarray(zeroed)), Ref(ifxarray(valid)), Ref(ifxarray(img)),
+                    T <: AbstractFloat ? na_code(border) : Int32(2), has, C_NULL))
+    end
+    fc = Fill(zero(S))
+    if ImageFiltering.isseparable(kernel) && length(kernel) == N && has[] == 0
+        imfilter!(r, out, img, kernel, fc)
+        sums = [imfilter(r, fill(1.0, axes(img, d)), ImageFiltering._vec(kernel[d]), Fill(0.0)) for d in 1:N]
+        descs = [ifxarray(s) for s in sums]
+        GC.@preserve out sums descs begin
+            check(ccall((:ifx_na_normalize_separable, libifx), Cint,
+                        (Ptr{Cvoid}, Ref{IfxArray}, Ptr{IfxArray}, Ptr{Cvoid}),
+                        context(), Ref(ifxarray(out)), descs, C_NULL))
+        end
+    else
+        imfilter!(r, out, zeroed, kernel, fc)
+        vp = imfilter(r, valid, kernel, Fill(zero(S)))
+        GC.@preserve out vp begin
+            check(ccall((:ifx_na_divide, libifx), Cint, (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Ptr{Cvoid}),
+                        context(), Ref(ifxarray(out)), Ref(ifxarray(vp)), C_NULL))
+        end
+    end
+    out
+end
+
+# Inner(): `out` holds the interior (allocate_output, src/border.jl:687-694);
+# its windows read inside `img`, so any padding gives the same values there.
+function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
+                                  kernel::ProcessedKernel, border::Inner) where {S,T,N}
+    full = similar(img, S)
+    imfilter!(r, full, img, kernel, Pad(:replicate))
+    copyto!(out, CartesianIndices(axes(out)), full, CartesianIndices(axes(out)))
 end
 
 # ---------------------------------------------------------------- mapwindow

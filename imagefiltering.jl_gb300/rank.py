@@ -16,7 +16,7 @@ import numpy as np
 
 from . import _abi
 from .arrays import DeviceArray, N0f8Array, alloc_like, host_view, kind_of, ptr_strides, stream_for
-from .borders import border_struct, borderinstance
+from .borders import Inner, border_struct, borderinstance
 
 
 def median(v):
@@ -101,6 +101,8 @@ def mapwindow(f, img, window, border=None, indices=None):
     if not isinstance(img, DeviceArray):
         img = host_view(img, kind)
     name = _fname(f)
+    if isinstance(border, Inner):
+        return _mapwindow_inner(f, img, window, name)
     if name == "extrema":
         shape = (2,) + tuple(img.shape)
         if isinstance(img, DeviceArray):
@@ -114,6 +116,29 @@ def mapwindow(f, img, window, border=None, indices=None):
     else:
         out = alloc_like(img, img.shape, kind)
     return mapwindow_(f, out, img, window, border, indices)
+
+
+def _mapwindow_inner(f, img, window, name):
+    """border=Inner() (default_imginds, src/mapwindow.jl:95-100): only the
+    indices whose whole window lies in the image, with their own axes; a window
+    longer than an axis is a DimensionMismatch.  Those windows read inside the
+    image, so any Pad style gives the same values there."""
+    nd = img.ndim
+    wf, wl = resolve_window(window, nd, allow_even=False)
+    inds = [(1 - f0, n - (f0 + l - 1)) for f0, l, n in zip(wf, wl, img.shape)]
+    if any(a > b for a, b in inds):
+        raise _abi.DimensionMismatch("the window is larger than the array: no interior")
+    full = mapwindow(f, img, window, border="replicate")
+    lead = (slice(None),) if name == "extrema" else ()
+    sl = lead + tuple(slice(a - 1, b) for a, b in inds)
+    first = tuple(a for a, _ in inds)
+    if isinstance(full, DeviceArray):
+        r = DeviceArray(full.tensor[sl].contiguous(), full.kind, first)
+    else:
+        from .filtering import OffsetResult
+        r = np.asfortranarray(full[sl]).view(OffsetResult)
+        r.first = first
+    return r
 
 
 def mapwindow_(f, out, img, window, border=None, indices=None):

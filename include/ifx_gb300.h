@@ -173,6 +173,27 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
                           const int64_t *wfirst, const int64_t *wlen,
                           const ifx_border_t *border, int32_t which, void *stream);
 
+/* ---- NA() borders ---------------------------------------------------------
+ * The non-filter steps of NA filtering (_imfilter_na!, src/imfilter.jl:280-318;
+ * imfilter_na_inseparable! / imfilter_na_separable! 1094-1130;
+ * normalize_separable! / normalize_dims! 1234-1250); the filters are
+ * ifx_imfilter_factored / ifx_imfilter_dense with a Fill(0) border.
+ * ifx_na_prepare: zeroed = img with NA elements set to 0 (in zeroed's eltype,
+ * N0f8 as c/255), valid = 1 where img is not NA and 0 where it is, *has_na =
+ * whether any element is NA; the predicate is isnan, !isfinite or never
+ * (8-bit images have no NA elements).  Synchronous (has_na is read back).
+ * ifx_na_divide: out[I] = out[I] / den[I], the quotient in Float64.
+ * ifx_na_normalize_separable: out[I] = ((out[I] / sums[0][i0]) / sums[1][i1])
+ * ..., in Float64; sums[d] is a Float64 vector of length size[d] (the 1-D
+ * filter of ones along axis d with Fill(0)). */
+#define IFX_NA_ISNAN 0
+#define IFX_NA_NOTFINITE 1
+#define IFX_NA_NONE 2
+int ifx_na_prepare(ifx_context_t *ctx, ifx_array_t *zeroed, ifx_array_t *valid, const ifx_array_t *img,
+                   int32_t na, int32_t *has_na, void *stream);
+int ifx_na_divide(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *den, void *stream);
+int ifx_na_normalize_separable(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *sums, void *stream);
+
 /* ---- separable cascade without allocation ------------------------------------
  * No counterpart in the reference: an allocation-free form of
  * ifx_imfilter_factored for callers that cannot allocate device memory on

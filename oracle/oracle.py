@@ -185,3 +185,50 @@ def np_padarray(img, style, lo, hi, fill=0.0):
     if style == "fill":
         return np.pad(a, widths, mode="constant", constant_values=fill)
     return np.pad(a, widths, mode=_NP_MODES[style])
+
+
+# ------------------------------------------------------------------- NA() and Inner()
+def naflag(img, na="isnan"):
+    """na.(img) for the predicates the GB300 path takes (src/border.jl:388-405)."""
+    a = np.asarray(img)
+    if na == "isnan":
+        return np.isnan(a)
+    if na == "notfinite":
+        return ~np.isfinite(a)
+    return np.zeros(a.shape, dtype=bool)
+
+
+def imfilter_na(img, filt, seps, na="isnan"):
+    """_imfilter_na! (src/imfilter.jl:280-318) in FP64.  `filt(a)` is the filter
+    with a Fill(0) border; `seps` lists (first, weights) of factor d for axis d
+    when the kernel is separable with one factor per dimension (isseparable,
+    1218-1219), else None.  Separable and no NA element: the Fill(0) filter
+    divided by the per-axis filters of ones, in axis order (normalize_dims!,
+    1241-1250); otherwise the filter of the image with NA elements zeroed
+    divided by the filter of the valid-pixel mask (imfilter_na_inseparable!,
+    1110-1121)."""
+    img = np.asfortranarray(np.asarray(img, dtype=np.float64))
+    flag = naflag(img, na)
+    with np.errstate(divide="ignore", invalid="ignore"):     # 0/0 -> NaN, as in Julia
+        return _imfilter_na(img, filt, seps, flag)
+
+
+def _imfilter_na(img, filt, seps, flag):
+    if seps is not None and not flag.any():
+        out = np.asarray(filt(img), dtype=np.float64)
+        for d, (first, w) in enumerate(seps):
+            ones = np.asfortranarray(np.ones(img.shape[d]))
+            sd = imfilter_cascade(ones, [(0, first, np.asarray(w, np.float64))], "fill", 0.0)
+            shape = [1] * img.ndim
+            shape[d] = -1
+            out = out / np.asarray(sd).reshape(shape)
+        return out
+    z = np.asfortranarray(np.where(flag, 0.0, img))
+    v = np.asfortranarray((~flag).astype(np.float64))
+    return np.asarray(filt(z), np.float64) / np.asarray(filt(v), np.float64)
+
+
+def interior(shape, lo, hi):
+    """_interior (src/border.jl:650-655): per axis the 1-based (first, last)
+    where an offset range lo..hi stays inside 1..n."""
+    return [(max(1, 1 - l), min(n, n - h)) for n, l, h in zip(shape, lo, hi)]

@@ -57,3 +57,30 @@ class GpuBackend:
         ifx = self.ifx
         out = ifx.mapwindow(ifx.extrema, self._img(img), tuple(int(x) for x in w))
         return np.asarray(out[0], np.float64), np.asarray(out[1], np.float64)
+
+    def na_cascade(self, img, factors, na="isnan"):
+        ifx = self.ifx
+        img = self._img(img)
+        ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(np.asarray(w, np.float64), (first,)), img.ndim, ax)
+                   for ax, first, w in factors)
+        return np.asarray(ifx.imfilter(img, ks, ifx.NA(na)), dtype=np.float64)
+
+    def na_dense(self, img, K, kfirst, na="isnan"):
+        ifx = self.ifx
+        img = self._img(img)
+        k = ifx.OffsetKernel(np.asarray(K, np.float64), tuple(kfirst))
+        return np.asarray(ifx.imfilter(img, (k,), ifx.NA(na)), dtype=np.float64)
+
+    def inner_dense(self, img, K, kfirst):
+        ifx = self.ifx
+        k = ifx.OffsetKernel(np.asarray(K, np.float64), tuple(kfirst))
+        out = ifx.imfilter(self._img(img), (k,), ifx.Inner())
+        return np.asarray(out, dtype=np.float64), out.first
+
+    def inner_cascade(self, img, factors):
+        ifx = self.ifx
+        img = self._img(img)
+        ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(np.asarray(w, np.float64), (first,)), img.ndim, ax)
+                   for ax, first, w in factors)
+        out = ifx.imfilter(img, ks, ifx.Inner())
+        return np.asarray(out, dtype=np.float64), out.first

@@ -54,6 +54,41 @@ class OracleBackend:
     def extrema_lemire(self, img, w):
         return self.O.extrema_trunc(img, w)
 
+    def na_cascade(self, img, factors, na="isnan"):
+        O = self.O
+        filt = lambda a: O.imfilter_cascade(a, factors, "fill", 0.0)
+        nd = np.asarray(img).ndim
+        seps = [(f, w) for _, f, w in factors] if len(factors) == nd else None
+        return O.imfilter_na(img, filt, seps, na)
+
+    def na_dense(self, img, K, kfirst, na="isnan"):
+        O = self.O
+        K = np.asarray(K, np.float64)
+        filt = lambda a: O.imfilter_dense(a, K, kfirst, "fill", 0.0)
+        ext = [d for d in range(K.ndim) if K.shape[d] > 1]
+        seps = None
+        if np.asarray(img).ndim == 1 and len(ext) == 1:        # a 1-tuple kernel on a vector
+            seps = [(kfirst[0], K.reshape(-1))]
+        return O.imfilter_na(img, filt, seps, na)
+
+    def inner_dense(self, img, K, kfirst):
+        O = self.O
+        K = np.asarray(K, np.float64)
+        inds = O.interior(np.asarray(img).shape, kfirst, [f + n - 1 for f, n in zip(kfirst, K.shape)])
+        full = O.imfilter_dense(img, K, kfirst, "replicate")
+        return full[tuple(slice(a - 1, b) for a, b in inds)], tuple(a for a, _ in inds)
+
+    def inner_cascade(self, img, factors):
+        O = self.O
+        nd = np.asarray(img).ndim
+        lo, hi = [0] * nd, [0] * nd
+        for ax, f, w in factors:
+            lo[ax] += f
+            hi[ax] += f + len(w) - 1
+        inds = O.interior(np.asarray(img).shape, lo, hi)
+        full = O.imfilter_cascade(img, factors, "replicate")
+        return full[tuple(slice(a - 1, b) for a, b in inds)], tuple(a for a, _ in inds)
+
 
 # ------------------------------------------------------------------- padarray
 def padarray_cases():
@@ -418,3 +453,69 @@ def check_median_golden(be):
         assert np.array_equal(got, np.array(k["expected"], dtype=np.float64)), k["source"]
         n += 1
     assert n == 6
+
+
+# ------------------------------------------------------------------- NA() and Inner()
+def check_na_vectors(be):
+    """test/border.jl:272-284 (the NA testset), literal expectations."""
+    # imfilter(1:10, centered([1,1,1].//3), NA()) == [3//2; 2:9; 19//2]
+    got = be.na_dense(F(np.arange(1, 11)), np.full(3, 1 / 3), (-1,))
+    exp = np.concatenate([[1.5], np.arange(2, 10), [9.5]])
+    np.testing.assert_allclose(got, exp, rtol=1e-12)
+    x = F([1, np.nan, np.inf, 0, -np.inf, np.inf, np.nan, np.nan, 1])
+    k, kf = np.array([1.0, 1.0]), (0,)                # OffsetArray([1,1], 0:1)
+    assert np.array_equal(be.na_dense(x, k, kf), [1, np.inf, np.inf, -np.inf, np.nan, np.inf, np.nan, 1, 1],
+                          equal_nan=True)
+    assert np.array_equal(be.na_dense(x, k, kf, "notfinite"), [1, np.nan, 0, 0, np.nan, np.nan, np.nan, 1, 1],
+                          equal_nan=True)
+    assert np.array_equal(be.na_dense(x, k, kf, "none"),
+                          [np.nan, np.nan, np.inf, -np.inf, np.nan, np.nan, np.nan, np.nan, 1], equal_nan=True)
+    # imfilter(1:5, centered([1]), NA()) == 1:5
+    np.testing.assert_array_equal(be.na_dense(F(np.arange(1, 6)), np.array([1.0]), (0,)), np.arange(1, 6))
+
+
+def target1_na(kern):
+    """test/2d.jl:174-181: the NA target of the impulse at [1,2]."""
+    ret = np.zeros((5, 7))
+    ret[0, 0] = kern[1, 0] / (kern[1, 0] + kern[1, 1])
+    ret[1, 0] = kern[0, 0] / kern.sum()
+    ret[:, -1] = np.nan
+    return ret
+
+
+def check_na_impulse(be):
+    """test/2d.jl:192-200 and 216-224: NA() on the edge impulse, dense and
+    factored kernels; NaN outputs (kernel entirely in the padding) compared as
+    zeros, as zerona! does."""
+    img = np.zeros((5, 7))
+    img[0, 1] = 1
+    img = F(img)
+    kf = np.outer(FACTORS[0][2], FACTORS[1][2])
+    zero = lambda a: np.where(np.isnan(a), 0.0, a)
+    t = target1_na(KERN)
+    got = be.na_dense(img, KERN, KFIRST)
+    np.testing.assert_allclose(zero(got), zero(t), atol=1e-12)
+    assert np.array_equal(np.isnan(got), np.isnan(t))
+    t = target1_na(kf)
+    got = be.na_cascade(img, FACTORS)
+    np.testing.assert_allclose(zero(got), zero(t), atol=1e-12)
+    assert np.array_equal(np.isnan(got), np.isnan(t))
+
+
+def check_inner_impulse(be):
+    """test/2d.jl:78-80 and 106-108: Inner() keeps targetimg[2:end, 1:end-2]
+    with axes (2:5, 1:5)."""
+    img = np.zeros((5, 7))
+    img[2, 3] = 1
+    img = F(img)
+    target = np.zeros((5, 7))
+    target[2:4, 1:3] = rot180(KERN)
+    got, first = be.inner_dense(img, KERN, KFIRST)
+    assert tuple(first) == (2, 1) and got.shape == (4, 5)
+    np.testing.assert_allclose(got, target[1:, :-2], atol=1e-12)
+    kf = np.outer(FACTORS[0][2], FACTORS[1][2])
+    target = np.zeros((5, 7))
+    target[2:4, 1:3] = rot180(kf)
+    got, first = be.inner_cascade(img, FACTORS)
+    assert tuple(first) == (2, 1) and got.shape == (4, 5)
+    np.testing.assert_allclose(got, target[1:, :-2], atol=1e-12)

@@ -81,3 +81,15 @@ def test_extrema_nd_groundtruth(be):
 
 def test_median_golden(be):
     K.check_median_golden(be)
+
+
+def test_na_vectors(be):
+    K.check_na_vectors(be)
+
+
+def test_na_impulse(be):
+    K.check_na_impulse(be)
+
+
+def test_inner_impulse(be):
+    K.check_inner_impulse(be)

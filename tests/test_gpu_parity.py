@@ -531,3 +531,98 @@ def test_dense_tensor_cores_many_tiles(gpu_ifx, oracle):
     tc = ifx.imfilter(big, ifx.centered(K), "circular", ifx.Algorithm.GB300("tensor_cores"))
     cc = ifx.imfilter(big, ifx.centered(K), "circular", ifx.Algorithm.GB300("cuda_cores"))
     assert normwise(tc, cc) <= 1e-5
+
+
+# --------------------------------------------------------------------- NA / Inner / NoPad
+@pytest.mark.parametrize("kind", ["F32", "F64", "N0F8"])
+@pytest.mark.parametrize("na", ["isnan", "notfinite", "none"])
+def test_na_border(gpu_ifx, oracle, kind, na):
+    """NA(): separable factors without NA elements (per-axis normalisation),
+    with NaN/Inf elements (masked filters), and a dense kernel -- against the
+    oracle's restatement of _imfilter_na!."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("na" + kind + na).encode()))
+    for shape in [(67, 45), (256, 33)]:
+        img = make_img(rng, shape, kind)
+        vals = values(ifx, img, kind)
+        if kind != "N0F8":
+            bad = rng.random(shape) < 0.05
+            img[bad] = rng.choice(np.array([np.nan, np.inf, -np.inf], dtype=img.dtype), bad.sum())
+            vals = values(ifx, img, kind)
+        fx = (0, -3, rng.random(7) + 0.1)
+        fy = (1, -1, rng.random(4) + 0.1)
+        ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(w, (f,)), 2, ax) for ax, f, w in (fx, fy))
+        got = ifx.imfilter(wrap(ifx, img, kind), ks, ifx.NA(na))
+        filt = lambda a: oracle.imfilter_cascade(a, [fx, fy], "fill", 0.0)
+        onan = na if kind != "N0F8" else "none"
+        ref = oracle.imfilter_na(vals, filt, [(fx[1], fx[2]), (fy[1], fy[2])], onan)
+        assert np.array_equal(np.isnan(got), np.isnan(ref)), (shape, na)
+        fin = np.isfinite(ref)
+        inf = np.isinf(ref)
+        assert np.array_equal(np.asarray(got, np.float64)[inf], ref[inf]), (shape, na)
+        tol = 1e-12 if kind == "F64" else 1e-5
+        assert normwise(np.where(fin, got, 0), np.where(fin, ref, 0)) <= tol, (shape, na)
+        K = rng.random((5, 3)) + 0.05
+        got = ifx.imfilter(wrap(ifx, img, kind), ifx.OffsetKernel(K, (-2, -1)), ifx.NA(na))
+        filt = lambda a: oracle.imfilter_dense(a, K, (-2, -1), "fill", 0.0)
+        ref = oracle.imfilter_na(vals, filt, None, onan)
+        assert np.array_equal(np.isnan(got), np.isnan(ref)), (shape, na, "dense")
+        fin = np.isfinite(ref)
+        assert normwise(np.where(fin, got, 0), np.where(fin, ref, 0)) <= tol, (shape, na, "dense")
+
+
+@pytest.mark.parametrize("kind", ["F32", "N0F8"])
+def test_inner_border(gpu_ifx, oracle, kind):
+    """Inner() and Inner(lo, hi): the interior with its first indices;
+    imgradients and mapwindow with Inner(); a window longer than the array
+    is a DimensionMismatch."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(77)
+    img = make_img(rng, (61, 40), kind)
+    vals = values(ifx, img, kind)
+    facs = [(0, -4, rng.standard_normal(9)), (1, -2, rng.standard_normal(5))]
+    ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(w, (f,)), 2, ax) for ax, f, w in facs)
+    got = ifx.imfilter(wrap(ifx, img, kind), ks, ifx.Inner())
+    assert got.first == (5, 3) and got.shape == (61 - 8, 40 - 4)
+    ref = oracle.imfilter_cascade(vals, facs, "replicate")[4:-4, 2:-2]
+    assert normwise(got, ref) <= 1e-5
+    got = ifx.imfilter(wrap(ifx, img, kind), ks, ifx.Inner((6, 3), (7, 2)))
+    assert got.first == (7, 4) and got.shape == (61 - 13, 40 - 5)
+    ref = oracle.imfilter_cascade(vals, facs, "replicate")[6:-7, 3:-2]
+    assert normwise(got, ref) <= 1e-5
+    with pytest.raises(ifx.ArgumentError):                 # Inner(1, 1) leaves reads outside
+        ifx.imfilter(wrap(ifx, img, kind), ks, ifx.Inner((1, 1), (1, 1)))
+    gy, gx = ifx.imgradients(wrap(ifx, img, kind), ifx.KernelFactors.sobel, ifx.Inner())
+    assert gy.first == (2, 2) and gy.shape == (59, 38)
+    k1, k2 = ifx.KernelFactors.sobel.gradient_pair
+    ref = oracle.imfilter_cascade(vals, [(0, -1, k1), (1, -1, k2)], "replicate")[1:-1, 1:-1]
+    assert normwise(gy, ref) <= 1e-5
+    med = ifx.mapwindow(ifx.median, wrap(ifx, img, kind), (5, 3), border=ifx.Inner())
+    assert med.first == (3, 2) and med.shape == (57, 38)
+    code = img if kind == "N0F8" else vals
+    ref = oracle.mapwindow_median(np.asarray(code, np.float64), [-2, -1], [5, 3], "replicate")[2:-2, 1:-1]
+    exp = (ref.astype(np.float32) / np.float32(255)) if kind == "N0F8" else ref
+    assert np.array_equal(np.asarray(med, np.float64), np.asarray(exp, np.float64))
+    with pytest.raises(ifx.DimensionMismatch):
+        ifx.mapwindow(ifx.median, wrap(ifx, img[:4, :4], kind), (5, 3), border=ifx.Inner())
+
+
+def test_nopad_subregion(gpu_ifx, oracle):
+    """imfilter!(out, img, kernel, NoPad(), inds): only out[inds] is written,
+    reads stay inside img; other borders with inds raise; reads outside raise."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(78)
+    img = np.asfortranarray(rng.random((50, 37)))
+    K = rng.standard_normal((3, 5))
+    k = ifx.OffsetKernel(K, (-1, -2))
+    out = np.asfortranarray(np.full((50, 37), -7.0))
+    ifx.imfilter_(out, img, k, ifx.NoPad(), inds=[(3, 40), (4, 30)])
+    ref = oracle.imfilter_dense(img, K, (-1, -2), "replicate")
+    assert normwise(out[2:40, 3:30], ref[2:40, 3:30]) <= 1e-12
+    mask = np.ones(out.shape, bool)
+    mask[2:40, 3:30] = False
+    assert np.all(out[mask] == -7.0)
+    with pytest.raises(ifx.ErrorException):
+        ifx.imfilter_(out, img, k, ifx.Pad("replicate"), inds=[(3, 40), (4, 30)])
+    with pytest.raises(ifx.ArgumentError):
+        ifx.imfilter_(out, img, k, ifx.NoPad(), inds=[(1, 40), (4, 30)])

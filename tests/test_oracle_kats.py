@@ -122,3 +122,15 @@ def test_fill_cascade_scales_halo(oracle):
             T[i, j] = sum(P[i + t, j] * k1[2][t] for t in range(3))
     exp = np.array([[sum(T[i, j + t] for t in range(3)) for j in range(6)] for i in range(6)])
     np.testing.assert_allclose(out, exp, rtol=0, atol=0)
+
+
+def test_na_vectors(be):
+    K.check_na_vectors(be)
+
+
+def test_na_impulse(be):
+    K.check_na_impulse(be)
+
+
+def test_inner_impulse(be):
+    K.check_inner_impulse(be)
