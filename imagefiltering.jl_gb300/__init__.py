@@ -15,6 +15,7 @@ from . import _abi
 from ._abi import (ArgumentError, DimensionMismatch, ErrorException, CudaError, OutOfMemory,
                    Unsupported, launch_count)
 from .arrays import DeviceArray, N0f8Array, n0f8
+from .blobs import BlobLoG, blob_LoG, findlocalmaxima, findlocalminima, multiLoG
 from .borders import Fill, Inner, NA, NoPad, Pad, borderinstance, padarray
 from .filtering import Algorithm, factorkernel, filter_type, imfilter, imfilter_, imgradients
 from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD, centered,
@@ -30,7 +31,7 @@ def library_path() -> str:
 
 __all__ = [
     "imfilter", "imfilter_", "imgradients", "mapwindow", "mapwindow_", "padarray", "Pad", "Fill",
-    "Inner", "NA", "NoPad", "Kernel", "KernelFactors", "centered", "kernelfactors", "Algorithm",
+    "Inner", "NA", "NoPad", "BlobLoG", "blob_LoG", "multiLoG", "findlocalmaxima", "findlocalminima", "Kernel", "KernelFactors", "centered", "kernelfactors", "Algorithm",
     "OffsetArray", "OffsetKernel", "ReshapedOneD", "LaplacianKernel", "DeviceArray", "N0f8Array",
     "n0f8", "median", "median_", "extrema", "minimum", "maximum", "filter_type", "factorkernel",
     "iscopy", "borderinstance", "ArgumentError", "DimensionMismatch", "ErrorException",

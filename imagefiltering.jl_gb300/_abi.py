@@ -90,7 +90,8 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_batch_plan_destroy", "ifx_server_create", "ifx_server_submit",
            "ifx_server_wait", "ifx_server_drain", "ifx_server_metrics", "ifx_server_reset_metrics",
            "ifx_server_destroy", "ifx_noalloc_scratch_bytes", "ifx_imfilter_factored_noalloc",
-           "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable"]
+           "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable",
+           "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs"]
 
 _lib = None
 _lock = threading.Lock()
@@ -143,6 +144,11 @@ def load(path: str = LIB_PATH):
                                        P(C.c_int32), vp]
         lib.ifx_na_divide.argtypes = [vp, P(IfxArray), P(IfxArray), vp]
         lib.ifx_na_normalize_separable.argtypes = [vp, P(IfxArray), P(IfxArray), vp]
+        lib.ifx_imfilter_factored_sum.argtypes = [vp, P(IfxArray), P(IfxArray), C.c_int32, C.c_int32,
+                                                  P(IfxFactor), C.c_double, P(IfxBorder), vp]
+        lib.ifx_findlocalextrema.argtypes = [vp, P(IfxArray), P(C.c_int32), P(C.c_int32), C.c_int32,
+                                             P(C.c_int64), P(C.c_double), C.c_int64, P(C.c_int64), vp]
+        lib.ifx_maxabs.argtypes = [vp, P(IfxArray), P(C.c_double), vp]
         lib.ifx_noalloc_scratch_bytes.restype = C.c_uint64
         lib.ifx_imfilter_factored_noalloc.argtypes = [P(IfxArray), P(IfxArray), C.c_int32, P(IfxFactor),
                                                       P(IfxBorder), vp]

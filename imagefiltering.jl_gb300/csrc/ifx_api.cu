@@ -445,7 +445,9 @@ static int run_cascade(Call &c, const ifx_array_t &imgd, const void *img, const 
         for (size_t i = 0; i < facs.size(); ++i) (facs[i].axis == 0 ? fx : fy) = facs[i];
         if (facs.size() == 2) x_first = facs[0].axis == 0;
         else x_first = facs[0].axis == 0 ? 1 : 0;
-        if (sep2d_smem_bytes(fx.len, fy.len, x_first, ct == IFX_F64) > 200 * 1024) fused = false;
+        if (fx.len > IFX_MAX_TAPS || fy.len > IFX_MAX_TAPS ||
+            sep2d_smem_bytes(fx.len, fy.len, x_first, ct == IFX_F64) > 200 * 1024)
+            fused = false;
         if (fused) {
             Sep2dArgs a{img, imgd.eltype, out, outd.eltype, n[0], nd > 1 ? n[1] : 1,
                         fx.first, fx.len, fy.first, fy.len, fx.w, fy.w, x_first,
@@ -570,9 +572,9 @@ static int collect_factors(const ifx_array_t &img, int32_t nf, const ifx_factor_
         if (f.axis < 0 || f.axis >= img.ndim)
             return fail(IFX_ERR_DIMENSION, "factor %d filters axis %d of a %d-dimensional image",
                         i + 1, f.axis + 1, img.ndim);
-        if (f.length < 1 || f.length > IFX_MAX_TAPS)
+        if (f.length < 1 || f.length > kMaxFactorTaps)
             return fail(IFX_ERR_UNSUPPORTED, "factor %d has %d taps (1..%d supported)", i + 1,
-                        f.length, IFX_MAX_TAPS);
+                        f.length, kMaxFactorTaps);
         if (!f.weights) return fail(IFX_ERR_ARGUMENT, "factor %d has no weights", i + 1);
         if (f.first < -(1 << 20) || f.first > (1 << 20))
             return fail(IFX_ERR_UNSUPPORTED, "factor offset out of range");
@@ -1166,6 +1168,127 @@ int ifx_batch_plan_destroy(ifx_batch_plan_t *plan)
     cudaSetDevice(plan->device);
     plan_destroy(plan->impl);
     delete plan;
+    return IFX_OK;
+}
+
+// ---------------------------------------------------------------- blob_LoG pieces
+int ifx_imfilter_factored_sum(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, int32_t nterms,
+                              int32_t nfactors, const ifx_factor_t *factors, double scale,
+                              const ifx_border_t *border, void *stream)
+{
+    int rc;
+    if (nterms < 1 || nfactors < 1 || !factors) return fail(IFX_ERR_ARGUMENT, "no terms");
+    if ((rc = check_array(out, "out"))) return rc;
+    if (out->eltype != IFX_F32 && out->eltype != IFX_F64)
+        return fail(IFX_ERR_UNSUPPORTED, "sums of separable terms write Float32 or Float64");
+    std::vector<std::vector<Fac>> terms(nterms);
+    double fill = 0.0;
+    for (int t = 0; t < nterms; ++t) {
+        bool nothing = false;
+        if ((rc = factored_prepare(out, img, nfactors, factors + (size_t)t * nfactors, border, terms[t], &fill,
+                                   &nothing)))
+            return rc;
+        if (nothing) {
+            if (numel(*img) == 0) return IFX_OK;
+            return fail(IFX_ERR_UNSUPPORTED, "term %d is a copy: give it as a 1-tap factor", t);
+        }
+    }
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *dout, *tmp = nullptr;
+    if ((rc = c.input(*img, &din)) || (rc = c.output(*out, &dout))) return rc;
+    const size_t bytes = (size_t)numel(*out) * elsize(out->eltype);
+    if (nterms > 1 && (rc = slot_get(ctx, kSlotTmp + 8, bytes, &tmp))) return rc;
+    for (int t = 0; t < nterms; ++t) {
+        if ((rc = run_cascade(c, *img, din, *out, t == 0 ? dout : tmp, terms[t], border, kSlotTmp))) return rc;
+        if (t > 0) IFX_CUDA(launch_sum_scale(dout, tmp, out->eltype, numel(*out), scale, t == nterms - 1, c.s));
+    }
+    if (nterms == 1 && scale != 1.0) {       // one term: scale it (sum with a zero term)
+        if ((rc = slot_get(ctx, kSlotTmp + 8, bytes, &tmp))) return rc;
+        IFX_CUDA(cudaMemsetAsync(tmp, 0, bytes, c.s));
+        IFX_CUDA(launch_sum_scale(dout, tmp, out->eltype, numel(*out), scale, 1, c.s));
+    }
+    return c.finish();
+}
+
+int ifx_findlocalextrema(ifx_context_t *ctx, const ifx_array_t *img, const int32_t *window, const int32_t *edges,
+                         int32_t minima, int64_t *indices, double *values, int64_t capacity, int64_t *count,
+                         void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img"))) return rc;
+    if (!window || !edges || !count || (capacity > 0 && (!indices || !values)))
+        return fail(IFX_ERR_ARGUMENT, "NULL argument");
+    if (img->eltype == IFX_I16) return fail(IFX_ERR_UNSUPPORTED, "Int16 images are not supported");
+    LeArgs a{};
+    a.eltype = img->eltype;
+    a.nd = img->ndim;
+    a.total = numel(*img);
+    a.minima = minima != 0;
+    for (int d = 0; d < IFX_MAXD; ++d) a.n[d] = 1;
+    for (int d = 0; d < a.nd; ++d) {
+        if (window[d] < 1) return fail(IFX_ERR_ARGUMENT, "window sizes must be positive");
+        a.n[d] = img->size[d];
+        a.half[d] = window[d] >> 1;
+        a.lo[d] = edges[d] ? 0 : 1;                          // clippedinds(R0, !edges)
+        a.hi[d] = (int)(img->size[d] - 1 - (edges[d] ? 0 : 1));
+    }
+    *count = 0;
+    if (a.total == 0) return IFX_OK;
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    if ((rc = c.input(*img, &a.img))) return rc;
+    const long long nb = localextrema_blocks(a.total);
+    void *counts, *total, *didx, *dval;
+    const long long cap = capacity > 0 ? capacity : 1;
+    if ((rc = slot_get(ctx, 19, (size_t)nb * 8, &counts)) || (rc = slot_get(ctx, 20, 16, &total)) ||
+        (rc = slot_get(ctx, 21, (size_t)cap * 8, &didx)) || (rc = slot_get(ctx, 22, (size_t)cap * 8, &dval)))
+        return rc;
+    IFX_CUDA(launch_localextrema(a, (unsigned long long *)counts, (unsigned long long *)total, (long long *)didx,
+                                 (double *)dval, capacity, c.s));
+    unsigned long long found = 0;
+    IFX_CUDA(cudaMemcpyAsync(&found, total, 8, cudaMemcpyDeviceToHost, c.s));
+    IFX_CUDA(cudaStreamSynchronize(c.s));
+    *count = (int64_t)found;
+    const long long k = (long long)found < capacity ? (long long)found : capacity;
+    if (k > 0) {
+        IFX_CUDA(cudaMemcpyAsync(indices, didx, (size_t)k * 8, cudaMemcpyDeviceToHost, c.s));
+        IFX_CUDA(cudaMemcpyAsync(values, dval, (size_t)k * 8, cudaMemcpyDeviceToHost, c.s));
+    }
+    if ((rc = c.finish())) return rc;
+    IFX_CUDA(cudaStreamSynchronize(c.s));
+    return IFX_OK;
+}
+
+int ifx_maxabs(ifx_context_t *ctx, const ifx_array_t *img, double *result, void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img"))) return rc;
+    if (!result) return fail(IFX_ERR_ARGUMENT, "result is NULL");
+    if (img->eltype == IFX_I16) return fail(IFX_ERR_UNSUPPORTED, "Int16 images are not supported");
+    *result = 0.0;
+    if (numel(*img) == 0) return IFX_OK;
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *buf;
+    if ((rc = c.input(*img, &din)) || (rc = slot_get(ctx, 20, 16, &buf))) return rc;
+    IFX_CUDA(cudaMemsetAsync(buf, 0, 16, c.s));
+    IFX_CUDA(launch_maxabs(din, img->eltype, numel(*img), (unsigned long long *)buf, c.s));
+    unsigned long long h[2] = {0, 0};
+    IFX_CUDA(cudaMemcpyAsync(h, buf, 16, cudaMemcpyDeviceToHost, c.s));
+    if ((rc = c.finish())) return rc;
+    IFX_CUDA(cudaStreamSynchronize(c.s));
+    double m;
+    memcpy(&m, &h[0], 8);
+    *result = h[1] ? std::nan("") : m;
     return IFX_OK;
 }
 

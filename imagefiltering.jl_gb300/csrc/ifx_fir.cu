@@ -16,6 +16,7 @@
 #include "ifx_tma.cuh"
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 namespace ifx {
 
@@ -110,8 +111,9 @@ cudaError_t launch_pad_box(const PadBoxArgs &a, cudaStream_t s)
 template <class Tc, class Tout>
 __global__ void k_pass_box(const Tc *__restrict__ src, Box S, Tout *__restrict__ dst, Box D,
                            Box O, int axis, int kfirst, int klen,
-                           const __grid_constant__ Weights<Tc, IFX_MAX_TAPS> W)
+                           const __grid_constant__ Weights<Tc, IFX_MAX_TAPS> W, const Tc *__restrict__ gw)
 {
+    const Tc *w = gw ? gw : W.w;          // factors longer than IFX_MAX_TAPS: weights in device memory
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < O.count;
          p += (long long)gridDim.x * blockDim.x) {
         long long rem = p, so = 0, dof = 0;
@@ -127,7 +129,7 @@ __global__ void k_pass_box(const Tc *__restrict__ src, Box S, Tout *__restrict__
         const long long st = S.stride[axis];
         const Tc *a = src + so + (long long)kfirst * st;
         Tc acc = 0;
-        for (int t = 0; t < klen; ++t) acc = fma(a[t * st], W.w[t], acc);
+        for (int t = 0; t < klen; ++t) acc = fma(a[t * st], w[t], acc);
         dst[dof] = (Tout)acc;
     }
 }
@@ -137,11 +139,24 @@ static cudaError_t pass_box_t(const PassBoxArgs &a, cudaStream_t s)
 {
     Weights<Tc, IFX_MAX_TAPS> W;
     memset(&W, 0, sizeof W);
-    for (int t = 0; t < a.klen; ++t) W.w[t] = (Tc)a.w[t];
+    Tc *gw = nullptr;
+    if (a.klen <= IFX_MAX_TAPS) {
+        for (int t = 0; t < a.klen; ++t) W.w[t] = (Tc)a.w[t];
+    } else {                                  // stream-ordered weight buffer, freed after the pass
+        std::vector<Tc> h(a.klen);
+        for (int t = 0; t < a.klen; ++t) h[t] = (Tc)a.w[t];
+        cudaError_t e = cudaMallocAsync(&gw, sizeof(Tc) * a.klen, s);
+        if (e != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(gw, h.data(), sizeof(Tc) * a.klen, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return e;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;   // h is pageable host memory
+    }
     k_pass_box<Tc, Tout><<<grid_for(a.obox.count, 256), 256, 0, s>>>(
-        (const Tc *)a.src, a.sbox, (Tout *)a.dst, a.dbox, a.obox, a.axis, a.kfirst, a.klen, W);
+        (const Tc *)a.src, a.sbox, (Tout *)a.dst, a.dbox, a.obox, a.axis, a.kfirst, a.klen, W, gw);
     note_launch();
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (gw) cudaFreeAsync(gw, s);
+    return e;
 }
 
 cudaError_t launch_pass_box(const PassBoxArgs &a, cudaStream_t s)

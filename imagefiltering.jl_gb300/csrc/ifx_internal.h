@@ -23,6 +23,11 @@ struct PadBoxArgs {
 };
 cudaError_t launch_pad_box(const PadBoxArgs &a, cudaStream_t s);
 
+// Longest 1-D factor: the fused kernels take up to IFX_MAX_TAPS (weights in
+// the launch parameters), the generic pass kernel up to this many (weights in
+// device memory beyond IFX_MAX_TAPS).
+constexpr int kMaxFactorTaps = 4095;
+
 struct PassBoxArgs {
     const void *src; Box sbox;             // compute-type buffer
     void *dst; Box dbox; int out_type;     // dst buffer (compute type, or the output eltype)
@@ -69,6 +74,25 @@ struct Grad3dArgs {
     int compute_f64;
 };
 cudaError_t launch_grad3d(const Grad3dArgs &a, cudaStream_t s);
+
+// blob_LoG pieces ---------------------------------------------------------------
+struct LeArgs {
+    const void *img;
+    int eltype;
+    int nd;
+    long long n[IFX_MAXD];
+    int half[IFX_MAXD];             // window >> 1
+    int lo[IFX_MAXD], hi[IFX_MAXD]; // candidate range per axis (edges)
+    long long total;
+    int minima;
+};
+
+cudaError_t launch_localextrema(const LeArgs &a, unsigned long long *counts, unsigned long long *total,
+                                long long *idx, double *val, long long capacity, cudaStream_t s);
+long long localextrema_blocks(long long total);
+cudaError_t launch_maxabs(const void *img, int eltype, long long n, unsigned long long *out, cudaStream_t s);
+cudaError_t launch_sum_scale(void *out, const void *term, int eltype, long long n, double scale, int last,
+                             cudaStream_t s);
 
 // NA() pieces -----------------------------------------------------------------
 cudaError_t launch_na_prepare(const void *img, int it, void *z, int zt, void *v, int vt, long long n, int na,

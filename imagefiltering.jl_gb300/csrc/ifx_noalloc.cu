@@ -79,6 +79,10 @@ int ifx_imfilter_factored_noalloc(ifx_array_t *out, const ifx_array_t *img, int3
     bool nothing;
     int rc = factored_prepare(out, img, nfactors, factors, border, facs, &fill, &nothing);
     if (rc || nothing) return rc;
+    for (const Fac &f : facs)
+        if (f.len > IFX_MAX_TAPS)           // longer factors need a device weight buffer
+            return set_error(IFX_ERR_UNSUPPORTED, "the allocation-free entry point takes factors of up to "
+                                                  "129 taps (IFX_MAX_TAPS)");
     if (!is_device_array(img->data) || !is_device_array(out->data))
         return set_error(IFX_ERR_ARGUMENT, "the allocation-free entry point takes device arrays only "
                                            "(host arrays would need staging buffers)");

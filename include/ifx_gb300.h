@@ -33,7 +33,8 @@ extern "C" {
 
 #define IFX_ABI_VERSION 1
 #define IFX_MAX_DIMS 4
-#define IFX_MAX_TAPS 129          /* longest 1-D factor */
+#define IFX_MAX_TAPS 129          /* longest 1-D factor of the fused kernels; the generic
+                                     N-d pipeline takes factors of up to 4095 taps */
 
 typedef enum {
     IFX_OK = 0,
@@ -86,7 +87,7 @@ typedef struct ifx_border {
 
 typedef struct ifx_factor {        /* one ReshapedOneD factor (src/kernelfactors.jl:52-131) */
     int32_t axis;                  /* 0-based axis it filters along (Npre)               */
-    int32_t length;                /* taps, 1 .. IFX_MAX_TAPS                            */
+    int32_t length;                /* taps, 1 .. 4095 (fused kernels up to IFX_MAX_TAPS) */
     int64_t first;                 /* kernel index of the first tap (OffsetArray axes)   */
     const double *weights;         /* host memory, `length` values                       */
 } ifx_factor_t;
@@ -172,6 +173,29 @@ int ifx_mapwindow_median(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t
 int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
                           const int64_t *wfirst, const int64_t *wlen,
                           const ifx_border_t *border, int32_t which, void *stream);
+
+/* ---- blob_LoG pieces --------------------------------------------------------
+ * ifx_imfilter_factored_sum: out = scale * sum over nterms separable terms of
+ * their cascades (term t = factors[t*nfactors .. t*nfactors+nfactors-1], each
+ * like ifx_imfilter_factored), in out's eltype (Float32/Float64).  A
+ * Laplacian of Gaussian is the sum over axes d of the second derivative of
+ * the Gaussian along d times the Gaussian along the others (Kernel.LoG,
+ * src/kernel.jl:325-339); multiLoG (src/extrema.jl:87-98) scales it by -sigma.
+ * ifx_findlocalextrema: findlocalmaxima / findlocalminima
+ * (src/extrema.jl:100-159) on an array of up to 4 dimensions: indices[k] are
+ * the 0-based column-major linear indices of the elements greater (smaller)
+ * than every other element of the window (window[d] >> 1 on each side, parts
+ * outside the array skipped), in column-major order, values[k] their values;
+ * edges[d] == 0 leaves out the first and last index of axis d.  *count is the
+ * number found (only min(count, capacity) are written).  Synchronous.
+ * ifx_maxabs: maximum(abs, img) (NaN if an element is NaN).  Synchronous. */
+int ifx_imfilter_factored_sum(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, int32_t nterms,
+                              int32_t nfactors, const ifx_factor_t *factors, double scale,
+                              const ifx_border_t *border, void *stream);
+int ifx_findlocalextrema(ifx_context_t *ctx, const ifx_array_t *img, const int32_t *window, const int32_t *edges,
+                         int32_t minima, int64_t *indices, double *values, int64_t capacity, int64_t *count,
+                         void *stream);
+int ifx_maxabs(ifx_context_t *ctx, const ifx_array_t *img, double *result, void *stream);
 
 /* ---- NA() borders ---------------------------------------------------------
  * The non-filter steps of NA filtering (_imfilter_na!, src/imfilter.jl:280-318;

@@ -232,3 +232,80 @@ def interior(shape, lo, hi):
     """_interior (src/border.jl:650-655): per axis the 1-based (first, last)
     where an offset range lo..hi stays inside 1..n."""
     return [(max(1, 1 - l), min(n, n - h)) for n, l, h in zip(shape, lo, hi)]
+
+
+# ------------------------------------------------------------------- blob_LoG
+def findlocalextrema(img, window, edges, minima=False):
+    """findlocalextrema (src/extrema.jl:125-159): for every index i left in by
+    the `edges` flags, i is kept when img[i] > img[i+j] (< for minima) for every
+    j != 0 of the window (window >> 1 each side) with i+j inside the array.
+    Returns 1-based index tuples in column-major order."""
+    a = np.asarray(img, dtype=np.float64)
+    nd = a.ndim
+    half = [w >> 1 for w in window]
+    out = []
+    for lin in range(a.size):
+        i = np.unravel_index(lin, a.shape, order="F")
+        if any((not edges[d]) and (i[d] == 0 or i[d] == a.shape[d] - 1) for d in range(nd)):
+            continue
+        v = a[i]
+        ok = True
+        for off in np.ndindex(*[2 * h + 1 for h in half]):
+            j = tuple(o - h for o, h in zip(off, half))
+            if all(x == 0 for x in j):
+                continue
+            k = tuple(x + y for x, y in zip(i, j))
+            if any(x < 0 or x >= n for x, n in zip(k, a.shape)):
+                continue
+            if not ((v < a[k]) if minima else (v > a[k])):
+                ok = False
+                break
+        if ok:
+            out.append(tuple(int(x) + 1 for x in i))
+    return out
+
+
+def log_kernel(sigmas):
+    """Kernel.LoG(σs) (src/kernel.jl:325-339), dense, FP64: half-widths
+    ceil(8.5σ)>>1, C (Σ x_d^2/σ_d^4 - Σ 1/σ_d^2) exp(-Σ x_d^2/2σ_d^2),
+    C = 1/(Π σ (2π)^(N/2)).  Returns (K, first)."""
+    import math
+    N = len(sigmas)
+    ws = [int(math.ceil(8.5 * s)) >> 1 for s in sigmas]
+    s2 = np.array([float(s) ** 2 for s in sigmas])
+    Cn = 1.0 / (float(np.prod(sigmas)) * (2 * math.pi) ** (N / 2))
+    grids = np.meshgrid(*[np.arange(-w, w + 1, dtype=np.float64) for w in ws], indexing="ij")
+    xs = sum(g * g / s for g, s in zip(grids, s2))
+    xs4 = sum(g * g / (s * s) for g, s in zip(grids, s2))
+    K = Cn * (xs4 - float(np.sum(1.0 / s2))) * np.exp(-xs / 2)
+    return np.asfortranarray(K), tuple(-w for w in ws)
+
+
+def multiLoG(img, sigmas, sigma_shape):
+    """multiLoG (src/extrema.jl:87-98): -σ times the dense LoG filter with
+    Pad(:reflect), stacked along a new first axis."""
+    img = np.asfortranarray(np.asarray(img, dtype=np.float64))
+    stack = np.zeros((len(sigmas),) + img.shape, order="F")
+    for i, s in enumerate(sigmas):
+        K, first = log_kernel([s * f for f in sigma_shape])
+        stack[i] = imfilter_dense(img, K, first, "reflect") * (-s)
+    return stack
+
+
+def blob_LoG(img, sigmas, edges, sigma_shape, rthresh=0.001):
+    """blob_LoG (src/extrema.jl:72-85): (location, σ tuple, amplitude) of the
+    local maxima of the multiLoG stack above the threshold."""
+    img = np.asarray(img, dtype=np.float64)
+    N = img.ndim
+    sig = sorted(float(s) for s in sigmas)
+    stack = multiLoG(img, sig, sigma_shape)
+    maxima = findlocalextrema(stack, (3,) * (N + 1), edges)
+    out = []
+    imgmax = float(np.max(np.abs(img))) if img.size else 0.0
+    prod = float(np.prod(sigma_shape))
+    for x in maxima:
+        amp = stack[tuple(k - 1 for k in x)]
+        if rthresh != 0 and not amp > rthresh / (sig[x[0] - 1] ** N * prod) * imgmax:
+            continue
+        out.append((x[1:], tuple(sig[x[0] - 1] * f for f in sigma_shape), amp))
+    return out

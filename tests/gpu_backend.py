@@ -84,3 +84,13 @@ class GpuBackend:
                    for ax, first, w in factors)
         out = ifx.imfilter(img, ks, ifx.Inner())
         return np.asarray(out, dtype=np.float64), out.first
+
+    def localextrema(self, img, window=None, edges=True, minima=False):
+        ifx = self.ifx
+        f = ifx.findlocalminima if minima else ifx.findlocalmaxima
+        return f(self._img(img), window=window, edges=edges)
+
+    def blob_log(self, img, sigmas, edges=None, sigma_shape=None, rthresh=0.001):
+        ifx = self.ifx
+        bl = ifx.blob_LoG(self._img(img), sigmas, edges=edges, sigma_shape=sigma_shape, rthresh=rthresh)
+        return [(b.location, b.sigma, b.amplitude) for b in bl]

@@ -54,6 +54,19 @@ class OracleBackend:
     def extrema_lemire(self, img, w):
         return self.O.extrema_trunc(img, w)
 
+    def localextrema(self, img, window=None, edges=True, minima=False):
+        a = np.asarray(img)
+        window = window or (3,) * a.ndim
+        edges = (edges,) * a.ndim if isinstance(edges, bool) else edges
+        return self.O.findlocalextrema(a, window, edges, minima)
+
+    def blob_log(self, img, sigmas, edges=None, sigma_shape=None, rthresh=0.001):
+        a = np.asarray(img, dtype=np.float64)
+        N = a.ndim
+        edges = (True,) + (False,) * N if edges is None else ((edges,) * (N + 1) if isinstance(edges, bool)
+                                                               else edges)
+        return self.O.blob_LoG(a, sigmas, tuple(edges), tuple(sigma_shape or (1.0,) * N), rthresh)
+
     def na_cascade(self, img, factors, na="isnan"):
         O = self.O
         filt = lambda a: O.imfilter_cascade(a, factors, "fill", 0.0)
@@ -519,3 +532,70 @@ def check_inner_impulse(be):
     got, first = be.inner_cascade(img, FACTORS)
     assert tuple(first) == (2, 1) and got.shape == (4, 5)
     np.testing.assert_allclose(got, target[1:, :-2], atol=1e-12)
+
+
+# ------------------------------------------------------------------- blob_LoG and local extrema
+def check_localextrema(be):
+    """test/extrema.jl:2-12."""
+    A = np.zeros((9, 9))
+    A[[0, 1, 4], 4] = 1
+    assert be.localextrema(A) == [(5, 5)]
+    assert be.localextrema(A, window=(1, 3)) == [(1, 5), (2, 5), (5, 5)]
+    assert be.localextrema(A, window=(1, 3), edges=False) == [(2, 5), (5, 5)]
+    A = np.zeros((9, 9, 9))
+    A[[0, 1, 4], 4, 4] = 1
+    assert be.localextrema(A) == [(5, 5, 5)]
+    assert be.localextrema(A, window=(1, 3, 1)) == [(1, 5, 5), (2, 5, 5), (5, 5, 5)]
+    assert be.localextrema(A, window=(1, 3, 1), edges=False) == [(2, 5, 5), (5, 5, 5)]
+    A = np.zeros((9, 9))
+    A[[0, 1, 4], 4] = -1
+    assert be.localextrema(A, minima=True) == [(5, 5)]
+
+
+def check_blob_log(be):
+    """test/extrema.jl:14-63 (blob_LoG) and the docstring example of blob_LoG
+    (src/extrema.jl:44-52)."""
+    A = np.zeros((9, 9))
+    A[4, 4] = 1
+    blobs = be.blob_log(A, 2.0 ** np.array([0.5, 0, 1]))
+    assert len(blobs) == 1
+    loc, sig, amp = blobs[0]
+    assert abs(amp - 0.3183098861837907) < 1e-12
+    assert tuple(sig) == (1.0, 1.0) and tuple(loc) == (5, 5)
+    assert [tuple(b[0]) for b in be.blob_log(A, [1.0])] == [(5, 5)]
+    assert [tuple(b[0]) for b in be.blob_log(A, [1.0], edges=(True, False, False))] == [(5, 5)]
+    assert be.blob_log(A, [1.0], edges=False) == []
+    A = np.zeros((9, 9))
+    A[0, 4] = 1
+    assert all(b[2] < 1e-16 for b in be.blob_log(A, 2.0 ** np.array([0.5, 0, 1])))
+    blobs = [b for b in be.blob_log(A, 2.0 ** np.array([0.5, 0, 1]), edges=True) if b[2] > 0.1]
+    assert len(blobs) == 1 and tuple(blobs[0][0]) == (1, 5)
+    assert [tuple(b[0]) for b in be.blob_log(A, 2.0 ** np.array([0.5, 0, 1]), edges=(True, True, False))
+            if b[2] > 0.1] == [(1, 5)]
+    assert be.blob_log(A, 2.0 ** np.array([0, 1]), edges=(False, True, False)) == []
+    assert all(b[2] < 1e-16 for b in be.blob_log(A, 2.0 ** np.array([0, 0.5, 1]), edges=(True, False, True)))
+    A = np.zeros((9, 9, 9))
+    A[4, 4, 4] = 1
+    blobs = be.blob_log(A, 2.0 ** np.array([0.5, 0, 1]))
+    assert len(blobs) == 1 and tuple(blobs[0][0]) == (5, 5, 5)
+    A = np.zeros((9, 9, 9))
+    A[4, 3:6, 4] = 1
+    blobs = be.blob_log(A, 2.0 ** np.array([1.0, 0, 0.5]), sigma_shape=(1.0, 3.0, 1.0))
+    assert len(blobs) == 1 and tuple(blobs[0][0]) == (5, 5, 5)
+    A = np.zeros((9, 9, 9))
+    A[0, 0, 3:6] = 1
+    blobs = [b for b in be.blob_log(A, 2.0 ** np.array([0.5, 0, 1]), edges=True, sigma_shape=(1.0, 1.0, 3.0))
+             if b[2] > 0.1]
+    assert len(blobs) == 1 and tuple(blobs[0][0]) == (1, 1, 5)
+    assert be.blob_log(A, 2.0 ** np.array([0, 1]), edges=(False, True, False, False),
+                       sigma_shape=(1.0, 1.0, 3.0)) == []
+    x = np.zeros(12)
+    x[10] = 1.0
+    assert len(be.blob_log(x, [4.0], edges=True, rthresh=0)) > len(be.blob_log(x, [4.0], edges=True))
+    # docstring example
+    x = np.zeros(100)
+    x[19:30] = np.exp(-np.arange(-5, 6) ** 2 / (2 * 4.0 ** 2))
+    x[49:80] = np.exp(-np.arange(-15, 16) ** 2 / (2 * 8.0 ** 2))
+    blobs = be.blob_log(x, 2.0 ** np.arange(1, 7), edges=False)
+    assert [(tuple(b[0]), tuple(b[1])) for b in blobs] == [((25,), (4.0,)), ((65,), (8.0,))]
+    assert abs(blobs[0][2] - 0.10453155018303673) < 1e-12 and abs(blobs[1][2] - 0.046175719034527364) < 1e-12

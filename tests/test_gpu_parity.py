@@ -626,3 +626,48 @@ def test_nopad_subregion(gpu_ifx, oracle):
         ifx.imfilter_(out, img, k, ifx.Pad("replicate"), inds=[(3, 40), (4, 30)])
     with pytest.raises(ifx.ArgumentError):
         ifx.imfilter_(out, img, k, ifx.NoPad(), inds=[(1, 40), (4, 30)])
+
+
+# --------------------------------------------------------------------- blob_LoG
+@pytest.mark.parametrize("kind", ["F64", "F32", "N0F8"])
+def test_findlocalextrema_random(gpu_ifx, oracle, kind):
+    """findlocalmaxima / findlocalminima on random 2-D to 4-D arrays with ties
+    (8-bit values), windows 1..5 and edge flags: the same indices in the same
+    order as the oracle's restatement."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("le" + kind).encode()))
+    for shape, window, edges in [((31, 17), (3, 3), (True, True)), ((12, 9, 7), (3, 1, 5), (False, True, False)),
+                                 ((6, 5, 4, 3), (3, 3, 3, 3), (True, False, True, True))]:
+        img = make_img(rng, shape, kind)
+        vals = values(ifx, img, kind)
+        for minima in (False, True):
+            f = ifx.findlocalminima if minima else ifx.findlocalmaxima
+            got = f(wrap(ifx, img, kind), window=window, edges=edges)
+            assert got == oracle.findlocalextrema(vals, window, edges, minima), (shape, minima)
+
+
+@pytest.mark.parametrize("kind", ["F64", "F32"])
+def test_multilog_and_blobs(gpu_ifx, oracle, kind):
+    """multiLoG (LoG as a sum of separable terms) against the oracle's dense
+    LoG with Pad(:reflect); blob_LoG on an image of Gaussian blobs of several
+    sizes: same locations and scales, amplitudes within the tolerance."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(91)
+    ny, nx = 96, 80
+    yy, xx = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    img = np.zeros((ny, nx))
+    for cy, cx, s in [(20, 18, 2.0), (60, 30, 4.0), (40, 62, 3.0), (80, 70, 1.5)]:
+        img += np.exp(-((yy - cy) ** 2 + (xx - cx) ** 2) / (2 * s * s))
+    img += 0.01 * rng.random((ny, nx))
+    img = np.asfortranarray(img.astype(np.float32 if kind == "F32" else np.float64))
+    sig = [1.0, 1.5, 2.0, 3.0, 4.0]
+    st = ifx.multiLoG(img, sig)
+    ref = oracle.multiLoG(img.astype(np.float64), sig, (1.0, 1.0))
+    assert st.shape == (5, ny, nx)
+    tol = 1e-12 if kind == "F64" else 1e-5
+    assert normwise(np.asarray(st, np.float64), ref) <= tol
+    got = ifx.blob_LoG(img, sig)
+    exp = oracle.blob_LoG(img.astype(np.float64), sig, (True, False, False), (1.0, 1.0))
+    assert [(b.location, b.sigma) for b in got] == [(tuple(l), tuple(s)) for l, s, _ in exp]
+    assert all(abs(b.amplitude - a) <= 1e-5 * max(1.0, abs(a)) for b, (_, _, a) in zip(got, exp))
+    assert len(got) >= 4

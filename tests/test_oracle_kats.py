@@ -134,3 +134,11 @@ def test_na_impulse(be):
 
 def test_inner_impulse(be):
     K.check_inner_impulse(be)
+
+
+def test_localextrema(be):
+    K.check_localextrema(be)
+
+
+def test_blob_log(be):
+    K.check_blob_log(be)
