@@ -91,7 +91,7 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_server_wait", "ifx_server_drain", "ifx_server_metrics", "ifx_server_reset_metrics",
            "ifx_server_destroy", "ifx_noalloc_scratch_bytes", "ifx_imfilter_factored_noalloc",
            "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable",
-           "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs"]
+           "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs", "ifx_imfilter_fft"]
 
 _lib = None
 _lock = threading.Lock()
@@ -149,6 +149,8 @@ def load(path: str = LIB_PATH):
         lib.ifx_findlocalextrema.argtypes = [vp, P(IfxArray), P(C.c_int32), P(C.c_int32), C.c_int32,
                                              P(C.c_int64), P(C.c_double), C.c_int64, P(C.c_int64), vp]
         lib.ifx_maxabs.argtypes = [vp, P(IfxArray), P(C.c_double), vp]
+        lib.ifx_imfilter_fft.argtypes = [vp, P(IfxArray), P(IfxArray), P(C.c_double), P(C.c_int64),
+                                         P(C.c_int64), P(IfxBorder), vp]
         lib.ifx_noalloc_scratch_bytes.restype = C.c_uint64
         lib.ifx_imfilter_factored_noalloc.argtypes = [P(IfxArray), P(IfxArray), C.c_int32, P(IfxFactor),
                                                       P(IfxBorder), vp]

@@ -75,6 +75,21 @@ struct Grad3dArgs {
 };
 cudaError_t launch_grad3d(const Grad3dArgs &a, cudaStream_t s);
 
+// Algorithm.FFT() (cuFFT, loaded at run time) ---------------------------------------
+struct FftArgs {
+    int nd;
+    long long n[IFX_MAXD], P[IFX_MAXD];   // image sizes, padded (FFT) sizes
+    int ksize[IFX_MAXD];
+    long long kn, Ptotal, Pc, total;      // kernel taps, padded elements, spectrum elements, outputs
+    const double *Kdev;                   // kernel on the device, column-major
+    void *padded, *krn, *specA, *specK;   // compute-type work buffers
+    void *out; int out_type;
+    int compute_f64;
+};
+bool fft_available();
+long long fft_size(long long l, long long lk);
+int launch_fft(const FftArgs &f, cudaStream_t s);   // 0 ok, -1 cuFFT, -2 CUDA, -3 no cuFFT
+
 // blob_LoG pieces ---------------------------------------------------------------
 struct LeArgs {
     const void *img;

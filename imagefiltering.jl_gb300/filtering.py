@@ -33,7 +33,8 @@ class Algorithm:
             self.tilesize = tilesize
 
     class FFT(Alg):
-        pass
+        """Correlation through real FFTs on the GPU (cuFFT) over the padfft
+        sizes of the reference (src/imfilter.jl:776-884)."""
 
     class IIR(Alg):
         pass
@@ -44,7 +45,8 @@ class Algorithm:
     class GB300(Alg):
         """Direct (FIR) filtering by the sm_103a kernels of this package.
 
-        ``method``: "auto", "cuda_cores" or "tensor_cores" (dense kernels)."""
+        ``method``: "auto", "cuda_cores" or "tensor_cores" (dense kernels), or
+        "fft" (the same as Algorithm.FFT())."""
 
         def __init__(self, method="auto"):
             self.method = method
@@ -169,7 +171,12 @@ def _ctx():
 
 def _check_alg(alg):
     if alg is None or isinstance(alg, Algorithm.GB300):
-        return alg or Algorithm.GB300()
+        alg = alg or Algorithm.GB300()
+        if alg.method not in _METHOD and alg.method != "fft":
+            raise _abi.ArgumentError("unknown GB300 method %r" % (alg.method,))
+        return Algorithm.FFT() if alg.method == "fft" else alg
+    if isinstance(alg, Algorithm.FFT):
+        return alg
     if isinstance(alg, Algorithm.Alg):
         raise _abi.Unsupported("%s runs on the CPU in the reference; this package implements "
                                "Algorithm.GB300() only" % type(alg).__name__)
@@ -347,6 +354,11 @@ def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
     kernel = factorkernel(kernel)
     nd = img.ndim
     border = borderinstance(border)
+    if isinstance(alg, Algorithm.FFT) and inds is None and isinstance(border, NoPad):
+        # _imfilter_fft! with NoPad (src/imfilter.jl:819-841): the circular
+        # correlation over the unpadded image, which is what a circular
+        # border padded to any larger size gives
+        border = borderinstance("circular")
     if inds is not None or isinstance(border, NoPad):
         if not isinstance(border, NoPad):
             raise _abi.ErrorException("Invalid border strategy `%r`: only `NoPad()` is supported." % (border,))
@@ -372,6 +384,8 @@ def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
     ao = _desc(out, okind)
     ctx = _ctx()
     ks = [k for k in kernel if not iscopy(k)]
+    if isinstance(alg, Algorithm.FFT):
+        return _imfilter_fft(ctx, out, ao, img, ai, ks, b, nd)
     if len(ks) == 1 and isinstance(ks[0], LaplacianKernel):
         L = ks[0]
         if L.N != nd:
@@ -402,6 +416,24 @@ def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
     kf = (C.c_int64 * 4)(*K.first)
     _abi.check(ctx.lib.ifx_imfilter_dense(ctx.handle, ao, ai, _abi.dptr(data), ksz, kf, b,
                                           _METHOD[alg.method], stream_for(img, out)))
+    return out
+
+
+def _imfilter_fft(ctx, out, ao, img, ai, ks, b, nd):
+    """_imfilter_fft! (src/imfilter.jl:819-841): the cascade's composite
+    (kernelconv) correlated with the image padded to the padfft sizes
+    (src/border.jl:239-248)."""
+    if not ks:
+        K = OffsetKernel(np.ones((1,) * nd), (0,) * nd)
+    else:
+        K = _dense_of(ks[0], nd) if len(ks) == 1 else _kernelconv(ks, nd)
+    if K.ndim != nd:
+        raise _abi.DimensionMismatch("kernel has %d dimensions, image %d" % (K.ndim, nd))
+    data = np.asfortranarray(K.data, dtype=np.float64)
+    ksz = (C.c_int64 * 4)(*K.shape)
+    kf = (C.c_int64 * 4)(*K.first)
+    _abi.check(ctx.lib.ifx_imfilter_fft(ctx.handle, ao, ai, _abi.dptr(data), ksz, kf, b,
+                                        stream_for(img, out)))
     return out
 
 

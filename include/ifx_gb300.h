@@ -125,7 +125,11 @@ int ifx_imfilter_factored(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
  * after factorkernel (src/imfilter.jl:1159-1184) -> __imfilter_inbounds!
  * (src/imfilter.jl:624-669).  K is column-major with sizes ksize and first
  * indices kfirst (host memory).  method: 0 = automatic (tensor cores for 2-D
- * kernels of 11 x 11 and larger that they take, CUDA cores otherwise),
+ * kernels of 11 x 11 and larger that they take, CUDA cores otherwise, and the
+ * FFT path of ifx_imfilter_fft when its estimated time is under half the
+ * direct one -- large kernels, Float64 images -- or the kernel has more than
+ * 3600 taps, provided every image element is finite; that check reads one
+ * flag back, so the call waits for its stream then),
  * 1 = FP32/FP64 CUDA cores, 2 = tcgen05 tensor cores (BF16 hi/lo split, three
  * products, FP32 accumulation; 2-D Float32 and 8-bit images, kernels up to
  * 33 wide and 40 tall). */
@@ -173,6 +177,18 @@ int ifx_mapwindow_median(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t
 int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
                           const int64_t *wfirst, const int64_t *wlen,
                           const ifx_border_t *border, int32_t which, void *stream);
+
+/* ---- a4 with Algorithm.FFT() --------------------------------------------------
+ * imfilter! with Algorithm.FFT() (src/imfilter.jl:776-884): each axis of length
+ * l is padded with the border to nextprod([2,3], l + ksize) elements (padfft,
+ * src/border.jl:239-248, 551-555) and the image is correlated with the dense
+ * kernel (sizes ksize, first indices kfirst, column-major, host memory)
+ * through real FFTs in the output's precision (cuFFT, loaded at run time;
+ * IFX_ERR_UNSUPPORTED without it).  Pad/Fill must not carry explicit widths.
+ * The reference selects this algorithm for kernels longer than 30
+ * (filter_algorithm, src/imfilter.jl:1200-1206). */
+int ifx_imfilter_fft(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, const double *kernel,
+                     const int64_t *ksize, const int64_t *kfirst, const ifx_border_t *border, void *stream);
 
 /* ---- blob_LoG pieces --------------------------------------------------------
  * ifx_imfilter_factored_sum: out = scale * sum over nterms separable terms of

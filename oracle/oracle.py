@@ -187,6 +187,46 @@ def np_padarray(img, style, lo, hi, fill=0.0):
     return np.pad(a, widths, mode=_NP_MODES[style])
 
 
+# ------------------------------------------------------------------- Algorithm.FFT()
+def nextprod23(n):
+    """nextprod([2, 3], n): the smallest 2^a 3^b >= n."""
+    best, p2 = None, 1
+    while p2 < 2 * max(n, 1):
+        p = p2
+        while p < 2 * max(n, 1):
+            if p >= n and (best is None or p < best):
+                best = p
+            p *= 3
+        p2 *= 2
+    return best
+
+
+def padfft(lo, hi, n):
+    """padfft (src/border.jl:245-248): the kernel range lo:hi of an axis of
+    length n becomes lo : lo + nextprod([2,3], n + hi - lo + 1) - n; returns
+    the padding widths (before, after)."""
+    P = nextprod23(n + hi - lo + 1)
+    return -lo, lo + P - n
+
+
+def imfilter_fft(img, K, kfirst, style, fill=0.0):
+    """The FFT algorithm (src/imfilter.jl:819-870): pad with the border to the
+    padfft sizes (src/border.jl:239-243, 551-555), place the kernel at the
+    origin of a zero array of the padded size, correlate circularly through
+    real FFTs (filtfft: irfft(rfft(A) .* conj(rfft(krn)))) and keep the
+    image's indices.  FP64 (numpy's pocketfft)."""
+    a = _f64(img)
+    k = _f64(K)
+    assert k.ndim == a.ndim
+    widths = [padfft(f, f + m - 1, n) for f, m, n in zip(kfirst, k.shape, a.shape)]
+    A = padarray(a, style, [w[0] for w in widths], [w[1] for w in widths], fill)
+    krn = np.zeros(A.shape)
+    krn[tuple(slice(0, m) for m in k.shape)] = k
+    ax = list(range(A.ndim))
+    R = np.fft.irfftn(np.fft.rfftn(A) * np.conj(np.fft.rfftn(krn)), s=A.shape, axes=ax)
+    return np.asfortranarray(R[tuple(slice(0, n) for n in a.shape)])
+
+
 # ------------------------------------------------------------------- NA() and Inner()
 def naflag(img, na="isnan"):
     """na.(img) for the predicates the GB300 path takes (src/border.jl:388-405)."""

@@ -33,6 +33,28 @@ class GpuBackend:
         k = ifx.OffsetKernel(np.asarray(K, np.float64), tuple(kfirst))
         return np.asarray(ifx.imfilter(img, (k,), self._border(style, fill)), dtype=np.float64)
 
+    def fft(self, img, K, kfirst, style, fill=0.0):
+        ifx = self.ifx
+        k = ifx.OffsetKernel(np.asarray(K, np.float64), tuple(kfirst))
+        return np.asarray(ifx.imfilter(self._img(img), (k,), self._border(style, fill), ifx.Algorithm.FFT()),
+                          dtype=np.float64)
+
+    def fft_cascade(self, img, factors, style, fill=0.0):
+        ifx = self.ifx
+        img = self._img(img)
+        ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(np.asarray(w, np.float64), (first,)), img.ndim, ax)
+                   for ax, first, w in factors)
+        return np.asarray(ifx.imfilter(img, ks, self._border(style, fill), ifx.Algorithm.FFT()),
+                          dtype=np.float64)
+
+    def fft_nopad(self, img, K, kfirst):
+        ifx = self.ifx
+        img = self._img(img)
+        out = np.asfortranarray(np.zeros(img.shape))
+        k = ifx.OffsetKernel(np.asarray(K, np.float64), tuple(kfirst))
+        ifx.imfilter_(out, img, (k,), ifx.NoPad(), ifx.Algorithm.FFT())
+        return out
+
     def laplacian(self, img, flags, style, fill=0.0, arith="f64"):
         ifx = self.ifx
         dt = {"f64": np.float64, "f32": np.float32, "int": np.uint8}[arith]

@@ -84,6 +84,25 @@ class OracleBackend:
             seps = [(kfirst[0], K.reshape(-1))]
         return O.imfilter_na(img, filt, seps, na)
 
+    def fft(self, img, K, kfirst, style, fill=0.0):
+        return self.O.imfilter_fft(img, K, kfirst, style, fill)
+
+    def fft_cascade(self, img, factors, style, fill=0.0):
+        nd = np.asarray(img).ndim
+        K, first = cascade_kernel(factors, nd)
+        return self.O.imfilter_fft(img, K, first, style, fill)
+
+    def fft_nopad(self, img, K, kfirst):
+        """imfilter!(CPU1(Algorithm.FFT()), out, img, kern, NoPad()): the
+        circular correlation over the unpadded image."""
+        a = np.asarray(img, np.float64)
+        krn = np.zeros(a.shape)
+        for idx in np.ndindex(*np.asarray(K).shape):
+            krn[tuple((i + f) % n for i, f, n in zip(idx, kfirst, a.shape))] = K[idx]
+        ax = list(range(a.ndim))
+        R = np.fft.irfftn(np.fft.rfftn(a) * np.conj(np.fft.rfftn(krn)), s=a.shape, axes=ax)
+        return R
+
     def inner_dense(self, img, K, kfirst):
         O = self.O
         K = np.asarray(K, np.float64)
@@ -101,6 +120,23 @@ class OracleBackend:
         inds = O.interior(np.asarray(img).shape, lo, hi)
         full = O.imfilter_cascade(img, factors, "replicate")
         return full[tuple(slice(a - 1, b) for a, b in inds)], tuple(a for a, _ in inds)
+
+
+def cascade_kernel(factors, nd):
+    """kernelconv of (axis, first, weights) factors: the dense composite and
+    its first indices."""
+    K = np.ones((1,) * nd)
+    first = [0] * nd
+    for ax, f, w in factors:
+        shape = [1] * nd
+        shape[ax] = len(w)
+        b = np.asarray(w, np.float64).reshape(shape)
+        out = np.zeros([sa + sb - 1 for sa, sb in zip(K.shape, b.shape)])
+        for idx in np.ndindex(*b.shape):
+            out[tuple(slice(i, i + s) for i, s in zip(idx, K.shape))] += K * b[idx]
+        K = out
+        first[ax] += f
+    return K, tuple(first)
 
 
 # ------------------------------------------------------------------- padarray
@@ -599,3 +635,78 @@ def check_blob_log(be):
     blobs = be.blob_log(x, 2.0 ** np.arange(1, 7), edges=False)
     assert [(tuple(b[0]), tuple(b[1])) for b in blobs] == [((25,), (4.0,)), ((65,), (8.0,))]
     assert abs(blobs[0][2] - 0.10453155018303673) < 1e-12 and abs(blobs[1][2] - 0.046175719034527364) < 1e-12
+
+
+# ------------------------------------------------------------------- Algorithm.FFT()
+def check_fft_impulses(be):
+    """test/2d.jl:49-79, 82-100, 104-140, 171-195 with Algorithm.FFT(): the
+    impulse targets (interior and at the edge) for the dense kernel, the
+    factored kernel and the rational 3x3 box, every border."""
+    img = np.zeros((5, 7))
+    img[2, 3] = 1
+    img = F(img)
+    target = np.zeros((5, 7))
+    target[2:4, 1:3] = rot180(KERN)
+    kf = np.outer(FACTORS[0][2], FACTORS[1][2])
+    targetf = np.zeros((5, 7))
+    targetf[2:4, 1:3] = rot180(kf)
+    box = [(0, -1, np.full(3, 1 / 3)), (1, -1, np.full(3, 1 / 3))]
+    targetb = np.zeros((5, 7))
+    targetb[1:4, 2:5] = 1 / 9
+    edge = np.zeros((5, 7))
+    edge[0, 1] = 1
+    edge = F(edge)
+    for style in BORDERS:
+        np.testing.assert_allclose(be.fft(img, KERN, KFIRST, style), target, atol=1e-12, err_msg=style)
+        np.testing.assert_allclose(be.fft_cascade(img, FACTORS, style), targetf, atol=1e-12, err_msg=style)
+        np.testing.assert_allclose(be.fft_cascade(img, box, style), targetb, atol=1e-12, err_msg=style)
+        np.testing.assert_allclose(be.fft(edge, KERN, KFIRST, style), target1(style, KERN), atol=1e-12,
+                                   err_msg=style)
+        np.testing.assert_allclose(be.fft_cascade(edge, FACTORS, style), target1(style, kf), atol=1e-12,
+                                   err_msg=style)
+
+
+def check_fft_3d_box(be):
+    """test/nd.jl:128-157 with Algorithm.FFT(): the 3-D box on ones, every
+    Pad style gives ones, Fill(0) gives (2/3)^k at faces, edges and corners."""
+    img = F(np.ones((10, 10, 10)))
+    K = np.full((3, 3, 3), 1 / 27)
+    for style in ["replicate", "circular", "symmetric", "reflect"]:
+        np.testing.assert_allclose(be.fft(img, K, (-1, -1, -1), style), img, rtol=1e-12)
+    t = np.ones((10, 10, 10))
+    for i in (0, 9):
+        t[:, :, i] = t[:, i, :] = t[i, :, :] = 2 / 3
+    for i in (0, 9):
+        for j in (0, 9):
+            t[:, i, j] = t[i, :, j] = t[i, j, :] = (2 / 3) ** 2
+    for i in (0, 9):
+        for j in (0, 9):
+            for k in (0, 9):
+                t[i, j, k] = (2 / 3) ** 3
+    np.testing.assert_allclose(be.fft(img, K, (-1, -1, -1), "fill"), t, rtol=1e-12)
+
+
+def check_fft_nopad(be):
+    """test/nd.jl:77-81: FFT without padding on 1:8 with zero ends equals the
+    replicate FIR result of the 3-tap kernel."""
+    img = np.arange(1, 9, dtype=np.float64)
+    img[0] = img[7] = 0
+    img = F(img)
+    exp = be.cascade(img, [K1], "replicate")
+    np.testing.assert_allclose(be.fft_nopad(img, K1[2], (K1[1],)), exp, rtol=1e-12, atol=1e-14)
+
+
+def check_fft_equals_fir(be, O, tol=1e-12):
+    """Algorithm.FFT() agrees with the direct filter (the reference's tests
+    compare every algorithm to the same target): random off-centre kernels in
+    1-3 dimensions, kernels longer than the image, every border."""
+    rng = np.random.default_rng(17)
+    for shape, ks, first in [((40,), (9,), (-4,)), ((37, 29), (9, 4), (-4, 1)), ((12, 11, 9), (3, 5, 2), (-1, -2, 0)),
+                             ((7, 6), (11, 9), (-5, -4)), ((33, 30), (31, 31), (-15, -15))]:
+        a = F(rng.random(shape))
+        K = rng.standard_normal(ks)
+        for style in BORDERS:
+            ref = O.imfilter_dense(a, K, first, style, 0.3)
+            got = be.fft(a, K, first, style, 0.3)
+            d = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+            assert d <= tol, (shape, ks, style, d)

@@ -101,3 +101,19 @@ def test_localextrema(be):
 
 def test_blob_log(be):
     K.check_blob_log(be)
+
+
+def test_fft_impulses(be):
+    K.check_fft_impulses(be)
+
+
+def test_fft_3d_box(be):
+    K.check_fft_3d_box(be)
+
+
+def test_fft_nopad(be):
+    K.check_fft_nopad(be)
+
+
+def test_fft_equals_fir(be, oracle):
+    K.check_fft_equals_fir(be, oracle)

@@ -671,3 +671,75 @@ def test_multilog_and_blobs(gpu_ifx, oracle, kind):
     assert [(b.location, b.sigma) for b in got] == [(tuple(l), tuple(s)) for l, s, _ in exp]
     assert all(abs(b.amplitude - a) <= 1e-5 * max(1.0, abs(a)) for b, (_, _, a) in zip(got, exp))
     assert len(got) >= 4
+
+
+# --------------------------------------------------------------------- Algorithm.FFT()
+@pytest.mark.parametrize("kind", ["F32", "F64", "N0F8"])
+@pytest.mark.parametrize("style", STYLES)
+def test_fft_matches_fir_oracle(gpu_ifx, oracle, kind, style):
+    """Algorithm.FFT() (cuFFT in the output's precision) against the FP64
+    direct oracle: a 69x69 LoG (σ = 8), an off-centre random 7x5 kernel and a
+    Gaussian cascade (kernelconv), within 1e-5 normwise (1e-12 for Float64)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("fft" + kind + style).encode()))
+    img = make_img(rng, (301, 257), kind)
+    vals = values(ifx, img, kind)
+    fill = fill_value(kind)
+    tol = 1e-12 if kind == "F64" else 1e-5
+    K, first = oracle.log_kernel((8.0, 8.0))
+    cases = [(K, first), (rng.standard_normal((7, 5)), (-3, 1))]
+    for K, first in cases:
+        got = ifx.imfilter(wrap(ifx, img, kind), (ifx.OffsetKernel(K, first),), border_of(ifx, style),
+                           ifx.Algorithm.FFT())
+        ref = oracle.imfilter_dense(vals, K, first, style, fill)
+        assert normwise(got, ref) <= tol, (K.shape, style)
+    g = ifx.KernelFactors.gaussian((3.0, 2.0))
+    got = ifx.imfilter(wrap(ifx, img, kind), g, border_of(ifx, style), ifx.Algorithm.GB300("fft"))
+    fir = ifx.imfilter(wrap(ifx, img, kind), g, border_of(ifx, style))
+    assert normwise(got, fir) <= tol
+
+
+def test_fft_volume_and_limits(gpu_ifx, oracle):
+    ifx = gpu_ifx
+    rng = np.random.default_rng(44)
+    vol = np.asfortranarray(rng.random((40, 33, 21), dtype=np.float32))
+    K = rng.standard_normal((5, 3, 7))
+    got = ifx.imfilter(vol, (ifx.OffsetKernel(K, (-2, -1, -3)),), "symmetric", ifx.Algorithm.FFT())
+    ref = oracle.imfilter_dense(vol.astype(np.float64), K, (-2, -1, -3), "symmetric")
+    assert normwise(got, ref) <= 1e-5
+    v = np.asfortranarray(rng.random(1000))
+    k = rng.standard_normal(61)
+    got = ifx.imfilter(v, (ifx.OffsetKernel(k, (-30,)),), "reflect", ifx.Algorithm.FFT())
+    assert normwise(got, oracle.imfilter_dense(v, k, (-30,), "reflect")) <= 1e-12
+    with pytest.raises(ifx.Unsupported):
+        ifx.imfilter(np.zeros((4, 4, 4, 4)), (ifx.OffsetKernel(np.ones((3, 3, 3, 3)), (-1,) * 4),),
+                     "replicate", ifx.Algorithm.FFT())
+    with pytest.raises(ifx.Unsupported):
+        ifx.imfilter(np.zeros((20, 20)), (ifx.OffsetKernel(np.ones((3, 3)), (-1, -1)),),
+                     ifx.Pad("replicate", (1, 1), (1, 1)), ifx.Algorithm.FFT())
+
+
+def test_dense_auto_takes_fft(gpu_ifx, oracle):
+    """The automatic dense method takes the FFT for Float64 images with large
+    kernels and for kernels over 3600 taps, and the direct kernels when an
+    element is not finite (NaN spreads over the kernel's reach only, as in
+    the reference's FIR fallback)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(55)
+    img = np.asfortranarray(rng.random((300, 260)))
+    K = rng.standard_normal((31, 31))
+    k = (ifx.OffsetKernel(K, (-15, -15)),)
+    ref = oracle.imfilter_dense(img, K, (-15, -15), "reflect")
+    assert normwise(ifx.imfilter(img, k, "reflect"), ref) <= 1e-12
+    K2 = rng.standard_normal((61, 61))
+    img32 = np.asfortranarray(rng.random((200, 180), dtype=np.float32))
+    got = ifx.imfilter(img32, (ifx.OffsetKernel(K2, (-30, -30)),), "replicate")
+    assert normwise(got, oracle.imfilter_dense(img32.astype(np.float64), K2, (-30, -30), "replicate")) <= 1e-5
+    bad = img.copy()
+    bad[150, 100] = np.nan
+    got = ifx.imfilter(bad, k, "reflect")
+    refb = oracle.imfilter_dense(bad, K, (-15, -15), "reflect")
+    assert np.array_equal(np.isnan(got), np.isnan(refb))
+    fin = ~np.isnan(refb)
+    assert np.isnan(refb).sum() == 31 * 31
+    assert normwise(got[fin], refb[fin]) <= 1e-12
