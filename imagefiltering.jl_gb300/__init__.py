@@ -4,7 +4,8 @@ Python mirror of the reference API over the C ABI in include/ifx_gb300.h:
 
     imfilter, imfilter_ (imfilter!), imgradients, mapwindow, mapwindow_
     (mapwindow!), padarray, Pad, Fill, Kernel, KernelFactors, centered,
-    Algorithm (with the new tag Algorithm.GB300)
+    Algorithm (with the new tag Algorithm.GB300), KernelFactors.IIRGaussian /
+    TriggsSdika (recursive filters), NA/Inner/NoPad borders, blob_LoG
 
 Arrays use Julia's memory order (Fortran-ordered numpy arrays on the host,
 ``DeviceArray`` for device-resident data).  Every result is computed by the
@@ -18,8 +19,8 @@ from .arrays import DeviceArray, N0f8Array, n0f8
 from .blobs import BlobLoG, blob_LoG, findlocalmaxima, findlocalminima, multiLoG
 from .borders import Fill, Inner, NA, NoPad, Pad, borderinstance, padarray
 from .filtering import Algorithm, factorkernel, filter_type, imfilter, imfilter_, imgradients
-from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD, centered,
-                      iscopy, kernelfactors)
+from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD, TriggsSdika,
+                      centered, iscopy, kernelfactors)
 from .rank import extrema, mapwindow, mapwindow_, maximum, median, median_, minimum
 
 OffsetArray = OffsetKernel
@@ -32,7 +33,7 @@ def library_path() -> str:
 __all__ = [
     "imfilter", "imfilter_", "imgradients", "mapwindow", "mapwindow_", "padarray", "Pad", "Fill",
     "Inner", "NA", "NoPad", "BlobLoG", "blob_LoG", "multiLoG", "findlocalmaxima", "findlocalminima", "Kernel", "KernelFactors", "centered", "kernelfactors", "Algorithm",
-    "OffsetArray", "OffsetKernel", "ReshapedOneD", "LaplacianKernel", "DeviceArray", "N0f8Array",
+    "OffsetArray", "OffsetKernel", "ReshapedOneD", "LaplacianKernel", "TriggsSdika", "DeviceArray", "N0f8Array",
     "n0f8", "median", "median_", "extrema", "minimum", "maximum", "filter_type", "factorkernel",
     "iscopy", "borderinstance", "ArgumentError", "DimensionMismatch", "ErrorException",
     "CudaError", "OutOfMemory", "Unsupported", "launch_count", "library_path",

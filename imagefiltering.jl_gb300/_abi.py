@@ -64,6 +64,11 @@ class IfxFactor(C.Structure):
                 ("weights", C.POINTER(C.c_double))]
 
 
+class IfxIir(C.Structure):
+    _fields_ = [("axis", C.c_int32), ("coef_f32", C.c_int32), ("a", C.c_double * 3), ("b", C.c_double * 3),
+                ("scale", C.c_double), ("M", C.c_double * 9), ("asum", C.c_double), ("bsum", C.c_double)]
+
+
 class IfxRequest(C.Structure):
     _fields_ = [("op", C.c_int32), ("window", C.c_int32), ("img", IfxArray), ("out", IfxArray * 2),
                 ("border", IfxBorder), ("taps", C.c_int32 * 2), ("first", C.c_int64 * 2),
@@ -91,7 +96,8 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_server_wait", "ifx_server_drain", "ifx_server_metrics", "ifx_server_reset_metrics",
            "ifx_server_destroy", "ifx_noalloc_scratch_bytes", "ifx_imfilter_factored_noalloc",
            "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable",
-           "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs", "ifx_imfilter_fft"]
+           "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs", "ifx_imfilter_fft",
+           "ifx_imfilter_iir"]
 
 _lib = None
 _lock = threading.Lock()
@@ -149,6 +155,7 @@ def load(path: str = LIB_PATH):
         lib.ifx_findlocalextrema.argtypes = [vp, P(IfxArray), P(C.c_int32), P(C.c_int32), C.c_int32,
                                              P(C.c_int64), P(C.c_double), C.c_int64, P(C.c_int64), vp]
         lib.ifx_maxabs.argtypes = [vp, P(IfxArray), P(C.c_double), vp]
+        lib.ifx_imfilter_iir.argtypes = [vp, P(IfxArray), P(IfxArray), C.c_int32, P(IfxIir), P(IfxBorder), vp]
         lib.ifx_imfilter_fft.argtypes = [vp, P(IfxArray), P(IfxArray), P(C.c_double), P(C.c_int64),
                                          P(C.c_int64), P(IfxBorder), vp]
         lib.ifx_noalloc_scratch_bytes.restype = C.c_uint64

@@ -1203,6 +1203,81 @@ int ifx_batch_plan_destroy(ifx_batch_plan_t *plan)
     return IFX_OK;
 }
 
+// ---------------------------------------------------------------- Algorithm.IIR()
+int ifx_imfilter_iir(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, int32_t nfactors,
+                     const ifx_iir_t *factors, const ifx_border_t *border, void *stream)
+{
+    int rc;
+    if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
+        return rc;
+    if ((rc = check_same_axes(*out, *img))) return rc;
+    if (img->eltype == IFX_I16) return fail(IFX_ERR_UNSUPPORTED, "Int16 images are not supported");
+    if (out->eltype != IFX_F32 && out->eltype != IFX_F64)
+        return fail(IFX_ERR_UNSUPPORTED, "IIR filtering writes Float32 or Float64 outputs");
+    if (nfactors < 0 || nfactors > 64 || (nfactors > 0 && !factors))
+        return fail(IFX_ERR_ARGUMENT, "nfactors %d", nfactors);
+    const int nd = img->ndim;
+    for (int f = 0; f < nfactors; ++f) {
+        const int ax = factors[f].axis;
+        if (ax < 0 || ax >= nd)
+            return fail(IFX_ERR_DIMENSION, "cannot have more kernels than dimensions (factor along axis %d of a "
+                        "%d-d image)", ax + 1, nd);
+    }
+    const long long total = numel(*img);
+    if (total == 0) return IFX_OK;
+    for (int f = 0; f < nfactors; ++f) {
+        const int ax = factors[f].axis;
+        if (img->size[ax] <= 3)
+            return fail(IFX_ERR_DIMENSION, "size %lld of img along dimension %d is too small for filtering "
+                        "with IIR kernel of length 3", (long long)img->size[ax], ax + 1);
+    }
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *dout;
+    if ((rc = c.input(*img, &din)) || (rc = c.output(*out, &dout))) return rc;
+    if (nfactors == 0) {                                  // every factor was a copy: convert
+        PadBoxArgs pa{din, img->eltype, dout, out->eltype, nd, {0, 0, 0, 0}, image_box(*img), IFX_REPLICATE, 0.0};
+        for (int d = 0; d < IFX_MAXD; ++d) pa.n[d] = d < nd ? (int)img->size[d] : 1;
+        IFX_CUDA(launch_pad_box(pa, c.s));
+        return c.finish();
+    }
+    long long st[IFX_MAXD];
+    long long s = 1;
+    for (int d = 0; d < IFX_MAXD; ++d) {
+        st[d] = s;
+        s *= d < nd ? img->size[d] : 1;
+    }
+    for (int f = 0; f < nfactors; ++f) {
+        const ifx_iir_t &k = factors[f];
+        IirArgs a;
+        memset(&a, 0, sizeof a);
+        a.src = f == 0 ? din : dout;
+        a.src_type = f == 0 ? img->eltype : out->eltype;
+        a.dst = dout;
+        a.dst_type = out->eltype;
+        a.L = img->size[k.axis];
+        a.inner = st[k.axis];
+        a.lines = total / a.L;
+        for (int j = 0; j < 3; ++j) {
+            a.a[j] = k.a[j];
+            a.b[j] = k.b[j];
+        }
+        for (int j = 0; j < 9; ++j) a.M[j] = k.M[j];
+        a.scale = k.scale;
+        // 1 - sum(a) and 1 - sum(b) in the kernel's float type
+        a.om_a = k.coef_f32 ? (double)(1.0f - (float)k.asum) : 1.0 - k.asum;
+        a.om_b = k.coef_f32 ? (double)(1.0f - (float)k.bsum) : 1.0 - k.bsum;
+        a.edge = border->style == IFX_FILL;
+        a.fill = border->style == IFX_FILL ? border->fill_value : 0.0;
+        a.compute_f64 = out->eltype == IFX_F64 || !k.coef_f32;
+        IFX_CUDA(launch_iir(a, c.s));
+    }
+    return c.finish();
+}
+
 // ---------------------------------------------------------------- Algorithm.FFT()
 // The padfft sizes (src/border.jl:245-248) and the padded box of an FFT
 // filter; 0 or an error code.

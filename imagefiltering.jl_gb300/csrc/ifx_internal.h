@@ -75,6 +75,23 @@ struct Grad3dArgs {
 };
 cudaError_t launch_grad3d(const Grad3dArgs &a, cudaStream_t s);
 
+// Triggs-Sdika IIR passes ------------------------------------------------------------
+// One pass along an axis of a contiguous column-major array: `lines` lines of
+// `L` elements with element stride `inner` (line l = o * inner + p starts at
+// o * inner * L + p).  src may equal dst (in place).  Coefficients hold the
+// values of the kernel's own float type; om_a = 1 - asum and om_b = 1 - bsum
+// are evaluated in that type.  edge 0: boundary values from the lines' end
+// elements (Pad), 1: `fill` (Fill, already in dst's eltype).
+struct IirArgs {
+    const void *src; int src_type;
+    void *dst; int dst_type;
+    long long L, inner, lines;
+    double a[3], b[3], scale, M[9], om_a, om_b;
+    int edge; double fill;
+    int compute_f64;
+};
+cudaError_t launch_iir(const IirArgs &a, cudaStream_t s);
+
 // Algorithm.FFT() (cuFFT, loaded at run time) ---------------------------------------
 struct FftArgs {
     int nd;

@@ -15,7 +15,7 @@ import numpy as np
 from . import _abi
 from .arrays import DeviceArray, alloc_like, host_view, kind_of, ptr_strides, stream_for
 from .borders import Fill, Inner, NA, NoPad, border_struct, borderinstance
-from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD,
+from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD, TriggsSdika,
                       iscopy)
 
 
@@ -96,7 +96,7 @@ def factorkernel(kernel):
     with an SVD (threshold sqrt(eps)); other kernels become 1-tuples."""
     if isinstance(kernel, tuple):
         return kernel
-    if isinstance(kernel, (LaplacianKernel, ReshapedOneD)):
+    if isinstance(kernel, (LaplacianKernel, ReshapedOneD, TriggsSdika)):
         return (kernel,)
     if not isinstance(kernel, OffsetKernel):
         raise _abi.ArgumentError("kernel must be an OffsetKernel (use centered(...))")
@@ -170,6 +170,10 @@ def _ctx():
 
 
 def _check_alg(alg):
+    if isinstance(alg, (Algorithm.IIR, Algorithm.Mixed)):
+        # the recursive filters run on the GPU whatever the tag; FIR factors
+        # of the same call take the direct kernels
+        alg = Algorithm.GB300()
     if alg is None or isinstance(alg, Algorithm.GB300):
         alg = alg or Algorithm.GB300()
         if alg.method not in _METHOD and alg.method != "fft":
@@ -194,7 +198,7 @@ def kernel_support(kernel, nd):
     lowest and highest offset each axis of the processed kernel reads."""
     lo, hi = [0] * nd, [0] * nd
     for k in kernel:
-        if iscopy(k):
+        if iscopy(k) or _is_iir(k):                   # IIR filters have axes 0:0
             continue
         if isinstance(k, LaplacianKernel):
             for d, f in enumerate(k.flags[:nd]):
@@ -246,6 +250,8 @@ def _check_reads(inds, kernel, img_shape, what):
 
 def _imfilter_inner(img, kernel, border, alg, T, kind):
     nd = img.ndim
+    if any(_is_iir(k) for k in kernel):
+        raise _abi.ArgumentError("IIR filters take NA(), Pad or Fill borders, not Inner()")
     if border.lo is None:
         lo, hi = kernel_support(kernel, nd)
         inds = [(max(1, 1 - l), min(n, n - h)) for l, h, n in zip(lo, hi, img.shape)]
@@ -264,6 +270,66 @@ def _imfilter_inner(img, kernel, border, alg, T, kind):
     return _with_first(part, tuple(a for a, _ in inds))
 
 
+def _is_iir(k):
+    return isinstance(k, TriggsSdika) or (isinstance(k, ReshapedOneD) and isinstance(k.data, TriggsSdika))
+
+
+def _iir_factors(kernel, nd):
+    """(factors, bare) for a cascade of Triggs-Sdika filters: factors are
+    (axis, TriggsSdika) without the copies.  A tuple of bare TriggsSdika
+    filters takes the axes in order (_imfilter_inplace_tuple!,
+    src/imfilter.jl:892-953); ReshapedOneD factors their own axes.  None when
+    the cascade holds no IIR filter."""
+    ks = list(kernel)
+    if not any(_is_iir(k) for k in ks):
+        return None
+    if all(isinstance(k, TriggsSdika) for k in ks):
+        if len(ks) > nd:
+            raise _abi.DimensionMismatch("cannot have more kernels than dimensions")
+        facs, bare = list(enumerate(ks)), True
+    else:
+        facs, bare = [], False
+        for k in ks:
+            if iscopy(k):
+                continue
+            if not (isinstance(k, ReshapedOneD) and isinstance(k.data, TriggsSdika)):
+                raise _abi.Unsupported("cascades that mix IIR and FIR filters (Algorithm.Mixed) are not "
+                                       "part of the GB300 path")
+            if k.axis >= nd:
+                raise _abi.DimensionMismatch("factor along axis %d of a %d-d image" % (k.axis + 1, nd))
+            facs.append((k.axis, k.data))
+    return [(ax, t) for ax, t in facs if not iscopy(t)], bare
+
+
+def _imfilter_iir(out, img, facs, border, bare, kind, okind):
+    """Triggs-Sdika cascades (src/imfilter.jl:892-1092) through ifx_imfilter_iir."""
+    if isinstance(border, (Inner, NoPad)):
+        raise _abi.ArgumentError("IIR filters take NA(), Pad or Fill borders, not %r" % (border,))
+    if bare and not isinstance(border, Fill) and border.style != "replicate":
+        raise _abi.ArgumentError('only "replicate" is supported')
+    if okind not in ("F32", "F64"):
+        raise _abi.Unsupported("IIR filtering writes Float32 or Float64 outputs")
+    nd = img.ndim
+    b = border_struct(border, nd, okind)
+    arr = (_abi.IfxIir * max(len(facs), 1))()
+    for i, (ax, t) in enumerate(facs):
+        f = arr[i]
+        f.axis = ax
+        f.coef_f32 = int(t.dtype == np.float32)
+        for j in range(3):
+            f.a[j] = float(t.a[j])
+            f.b[j] = float(t.b[j])
+        for j in range(9):
+            f.M[j] = float(t.M[j // 3, j % 3])
+        f.scale = float(t.scale)
+        f.asum = float(t.asum)
+        f.bsum = float(t.bsum)
+    ctx = _ctx()
+    _abi.check(ctx.lib.ifx_imfilter_iir(ctx.handle, _desc(out, okind), _desc(img, kind), len(facs), arr, b,
+                                        stream_for(img, out)))
+    return out
+
+
 def _separable_factors(kernel, nd):
     """isseparable (src/imfilter.jl:1218-1219: every factor has one extended
     dimension) with N factors for N dimensions, as normalize_separable!
@@ -273,7 +339,9 @@ def _separable_factors(kernel, nd):
         return None
     out = []
     for k in kernel:
-        if isinstance(k, ReshapedOneD):
+        if _is_iir(k):                                # isseparable: any IIR tuple (1218)
+            out.append((None, k if isinstance(k, TriggsSdika) else k.data))
+        elif isinstance(k, ReshapedOneD):
             out.append((k.data.first[0], np.asarray(k.data.data, dtype=np.float64).reshape(-1)))
         elif isinstance(k, OffsetKernel):
             ext = [d for d in range(k.ndim) if k.shape[d] > 1]
@@ -310,7 +378,7 @@ def _imfilter_na(out, img, kernel, border, alg, kind, okind):
                 ones.tensor.fill_(1.0)
             else:
                 ones[...] = 1.0
-            k1 = (ReshapedOneD(OffsetKernel(w, (first,)), 1, 0),)
+            k1 = (w,) if first is None else (ReshapedOneD(OffsetKernel(w, (first,)), 1, 0),)
             sd = imfilter(ones, k1, Fill(0), alg)
             keep.append(sd)
             sums.append(_desc(sd, "F64"))
@@ -349,6 +417,14 @@ def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
     kind = kind_of(img)
     if not isinstance(img, DeviceArray):
         img = host_view(img, kind)
+    if isinstance(kernel, TriggsSdika) and isinstance(border, int) and not isinstance(border, bool):
+        # imfilter!(r, out, img, kernel::TriggsSdika, dim, border) (src/imfilter.jl:922-933):
+        # one pass along dimension `dim` (1-based), any Pad style or Fill
+        dim, border = border, borderinstance("replicate" if alg is None else alg)
+        if not 1 <= dim <= img.ndim:
+            raise _abi.DimensionMismatch("dimension %d of a %d-d image" % (dim, img.ndim))
+        facs = [] if iscopy(kernel) else [(dim - 1, kernel)]
+        return _imfilter_iir(out, img, facs, border, False, kind, kind_of(out))
     alg = _check_alg(alg)
     okind = kind_of(out)
     kernel = factorkernel(kernel)
@@ -359,6 +435,8 @@ def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
         # correlation over the unpadded image, which is what a circular
         # border padded to any larger size gives
         border = borderinstance("circular")
+    if (inds is not None or isinstance(border, NoPad)) and any(_is_iir(k) for k in kernel):
+        raise _abi.Unsupported("IIR filters over a NoPad() subregion are not part of the GB300 path")
     if inds is not None or isinstance(border, NoPad):
         if not isinstance(border, NoPad):
             raise _abi.ErrorException("Invalid border strategy `%r`: only `NoPad()` is supported." % (border,))
@@ -379,6 +457,9 @@ def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
         return _imfilter_na(out, img, kernel, border, alg, kind, okind)
     if isinstance(border, Inner):
         raise _abi.ArgumentError("imfilter! with Inner(): allocate the interior with imfilter")
+    iir = _iir_factors(kernel, nd)
+    if iir is not None:
+        return _imfilter_iir(out, img, iir[0], border, iir[1], kind, okind)
     b = border_struct(border, nd, kind)
     ai = _desc(img, kind)
     ao = _desc(out, okind)

@@ -10,7 +10,10 @@ Representation (Julia -> Python):
     Fortran-ordered numpy array, ``first[d]`` the first index of axis d.
   * ``ReshapedOneD{N,Npre}`` -> ``ReshapedOneD(vec, N, axis=Npre)``.
   * ``Kernel.Laplacian``     -> ``LaplacianKernel(flags)``.
+  * ``KernelFactors.TriggsSdika`` -> ``TriggsSdika(a, b, scale, M)``; a
+    ``ReshapedOneD`` may wrap one (an IIR factor of an N-d cascade).
 """
+import warnings
 import math
 
 import numpy as np
@@ -63,20 +66,80 @@ def centered(a):
 
 
 def iscopy(k) -> bool:
-    """src/imfilter.jl:1252-1255: all axes 0:0 and the value 1."""
+    """src/imfilter.jl:1252-1255: all axes 0:0 and the value 1; a Triggs-Sdika
+    filter with zero coefficients and unit scale (1254)."""
     if isinstance(k, ReshapedOneD):
         return iscopy(k.data)
+    if isinstance(k, TriggsSdika):
+        return all(x == 0 for x in k.a) and all(x == 0 for x in k.b) and k.scale == 1
     if isinstance(k, OffsetKernel):
         return all(n == 1 for n in k.shape) and all(f == 0 for f in k.first) and \
             k.data.reshape(-1)[0] == 1
     return False
 
 
+class TriggsSdika:
+    """KernelFactors.TriggsSdika (src/kernelfactors.jl:462-505): an order-3
+    forward filter ``a``, an order-3 backward filter ``b``, the right-edge
+    matrix ``M`` (3x3) and the final ``scale``, all of one float type.
+
+    ``TriggsSdika(a, b, scale, M)`` takes them as given; ``TriggsSdika(ab,
+    scale)`` is the symmetric filter a = b = ab with M from Triggs & Sdika
+    (2006) (src/kernelfactors.jl:497-505)."""
+
+    def __init__(self, a, b, scale=None, M=None):
+        if M is None:                                 # the symmetric form (ab, scale)
+            if scale is not None:
+                raise TypeError("TriggsSdika(a, b, scale, M) or TriggsSdika(ab, scale)")
+            ab = np.asarray(a)
+            T = ab.dtype.type if ab.dtype in (np.float32, np.float64) else np.float64
+            self.a = ab.astype(T)
+            self.b = ab.astype(T)
+            self.scale = T(b)
+            self.M = self._symmetric_M(self.a)
+        else:
+            aa = np.asarray(a)
+            T = aa.dtype.type if aa.dtype in (np.float32, np.float64) else np.float64
+            self.a = aa.astype(T)
+            self.b = np.asarray(b).astype(T)
+            self.scale = T(scale)
+            self.M = np.asarray(M).astype(T).reshape(3, 3)
+        if self.a.size != 3 or self.b.size != 3:
+            raise ValueError("only order-3 Triggs-Sdika filters are supported")
+        a1, a2, a3 = self.a
+        b1, b2, b3 = self.b
+        self.asum = (a1 + a2) + a3                    # sum(a) in the coefficients' type
+        self.bsum = (b1 + b2) + b3
+
+    @staticmethod
+    def _symmetric_M(a):
+        a1, a2, a3 = a
+        one = type(a1)(1)
+        den = (one + a1 - a2 + a3) * (one - a1 - a2 - a3) * (one + a2 + (a1 - a3) * a3)
+        M = [[-a3 * a1 + one - a3 * a3 - a2, (a3 + a1) * (a2 + a3 * a1), a3 * (a1 + a3 * a2)],
+             [a1 + a3 * a2, -(a2 - one) * (a2 + a3 * a1), -(a3 * a1 + a3 * a3 + a2 - one) * a3],
+             [a3 * a1 + a2 + a1 * a1 - a2 * a2,
+              a1 * a2 + a3 * a2 * a2 - a1 * a3 * a3 - a3 * a3 * a3 - a3 * a2 + a3, a3 * (a1 + a3 * a2)]]
+        return np.array([[m / den for m in row] for row in M], dtype=type(a1))
+
+    @property
+    def dtype(self):
+        return self.a.dtype
+
+    def __repr__(self):
+        return "TriggsSdika(a=%s, b=%s, scale=%r)" % (self.a, self.b, self.scale)
+
+
 class ReshapedOneD:
     """A 1-D factor filtering along ``axis`` of an ``N``-d array
-    (src/kernelfactors.jl:52-131)."""
+    (src/kernelfactors.jl:52-131); ``data`` is a 1-D kernel or a TriggsSdika."""
 
     def __init__(self, data, N, axis):
+        if isinstance(data, TriggsSdika):
+            self.data = data
+            self.N = int(N)
+            self.axis = int(axis)
+            return
         if not isinstance(data, OffsetKernel):
             data = centered(data)
         if data.ndim != 1:
@@ -156,6 +219,36 @@ class KernelFactors:
             x = np.arange(-w, w + 1, dtype=T)
             g = np.exp(-(x * x) / (T(2) * s * s)).astype(T)
         return centered((g / g.sum(dtype=T)).astype(T))
+
+    @staticmethod
+    def IIRGaussian(sigma, T=None, emit_warning=True):
+        """IIRGaussian([T], σ; emit_warning=true) (src/kernelfactors.jl:527-569):
+        the recursive approximation of a Gaussian of Young, van Vliet and van
+        Ginkel (2002) as a symmetric TriggsSdika filter; a tuple of σs gives
+        one ReshapedOneD factor per dimension.  T defaults to σ's float type
+        (Float64 for integers)."""
+        if isinstance(sigma, (tuple, list)):
+            if T is None:
+                T = np.float32 if sigma and all(isinstance(s, np.float32) for s in sigma) else np.float64
+            N = len(sigma)
+            return tuple(ReshapedOneD(KernelFactors.IIRGaussian(s, T, emit_warning), N, d)
+                         for d, s in enumerate(sigma))
+        if T is None:
+            T = _as_f(sigma)
+        T = np.dtype(T).type
+        s = float(sigma)
+        if emit_warning and s < 1 and s != 0:
+            warnings.warn("σ is too small for accuracy")
+        m0, m1, m2 = T(1.16680), T(1.10783), T(1.40586)
+        q = T(1.31564 * (math.sqrt(1 + 0.490811 * s * s) - 1))
+        two, three, four = T(2), T(3), T(4)
+        ascale = (m0 + q) * (m1 * m1 + m2 * m2 + two * m1 * q + q * q)
+        Bb = m0 * (m1 * m1 + m2 * m2) / ascale
+        B = Bb * Bb
+        a1 = q * (two * m0 * m1 + m1 * m1 + m2 * m2 + (two * m0 + four * m1) * q + three * q * q) / ascale
+        a2 = -q * q * (m0 + two * m1 + three * q) / ascale
+        a3 = q * q * q / ascale
+        return TriggsSdika(np.array([a1, a2, a3], dtype=T), B)
 
     @staticmethod
     def box(*sz):

@@ -178,6 +178,33 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
                           const int64_t *wfirst, const int64_t *wlen,
                           const ifx_border_t *border, int32_t which, void *stream);
 
+/* ---- Algorithm.IIR(): Triggs-Sdika recursive filters ---------------------------
+ * One factor per pass, a KernelFactors.TriggsSdika (src/kernelfactors.jl:
+ * 462-505): forward coefficients a, backward coefficients b, the right-edge
+ * matrix M (row-major), scale, and sum(a), sum(b) -- all values of the
+ * kernel's float type (coef_f32 = 1 for Float32 kernels). */
+typedef struct ifx_iir {
+    int32_t axis;                  /* 0-based axis the factor filters along */
+    int32_t coef_f32;              /* 1: Float32 coefficients, 0: Float64   */
+    double a[3], b[3];
+    double scale;
+    double M[9];
+    double asum, bsum;
+} ifx_iir_t;
+
+/* imfilter! with a cascade of Triggs-Sdika factors (src/imfilter.jl:892-900,
+ * 961-1092; ReshapedOneD factors through the cascade of 385-457, whose IIR
+ * padding is empty): each factor filters the previous result along its axis,
+ * over whole lines, in place in `out`.  Arithmetic in promote(eltype(out),
+ * coefficient type), intermediate results rounded to eltype(out), the
+ * reference's operation order.  The border gives the boundary values: Pad
+ * (any style; the padding of an IIR cascade is empty, so the boundary values
+ * are the lines' end elements) or Fill(v) (v converted to eltype(out)).
+ * Lines of 3 or fewer elements are a DimensionMismatch.  out may be img
+ * (same eltype). */
+int ifx_imfilter_iir(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, int32_t nfactors,
+                     const ifx_iir_t *factors, const ifx_border_t *border, void *stream);
+
 /* ---- a4 with Algorithm.FFT() --------------------------------------------------
  * imfilter! with Algorithm.FFT() (src/imfilter.jl:776-884): each axis of length
  * l is padded with the border to nextprod([2,3], l + ksize) elements (padfft,

@@ -21,6 +21,8 @@
  *                       copy_win! with padindex relative to window-intersect-image)
  *   ora_extrema_trunc   src/mapwindow.jl:388-473    (Lemire wedge: min/max over the window
  *                       truncated at the edges; even windows allowed)
+ *   ora_imfilter_iir    src/imfilter.jl:961-1092    (Triggs-Sdika passes with their border
+ *                       initialisation, cascaded along the factors' axes)
  *
  * Arrays are column-major (axis 0 contiguous, i.e. Julia's axis 1), at most
  * ORA_MAXD dimensions, with 0-based indices; Julia's OffsetArray first indices
@@ -711,5 +713,118 @@ int ora_mapwindow_median_u8_mt(const int64_t *n, const uint8_t *img,
         ++launched;
     }
     for (int t = 0; t < launched; ++t) pthread_join(th[t], NULL);
+    return ORA_OK;
+}
+
+/* ------------------------------------------------------------------ IIR
+ * One Triggs-Sdika pass (order 3 forward, order 3 backward) along a line of
+ * length L with element stride st, x -> y (x == y allowed):
+ * _imfilter_dim! (src/imfilter.jl:961-1030) with _leftborder!
+ * (src/imfilter.jl:1033-1045), _rightborder! (1057-1084) and rightΔu
+ * (1087-1092).  ab = a1 a2 a3 b1 b2 b3; M row-major 3x3; edge 0 = Pad
+ * (boundary values are the line's end elements), 1 = Fill(fill).
+ *
+ * Types as in the reference: the arithmetic runs in CT = promote(eltype(out),
+ * coefficient type) (iir_line_f64 / iir_line_f32), every stored result is
+ * rounded to eltype(out) (s32: Float32), sum(a) and sum(b) are taken in the
+ * coefficients' type (c32: Float32).  x and y hold the values as doubles. */
+#define ORA_IIR_LINE(NAME, CT)                                                                        \
+static void NAME(const double *x, double *y, int64_t L, int64_t st, const double *ab, double scale_,  \
+                 const double *M_, int edge, double fill_, int s32, int c32)                          \
+{                                                                                                     \
+    const CT a[3] = {(CT)ab[0], (CT)ab[1], (CT)ab[2]}, b[3] = {(CT)ab[3], (CT)ab[4], (CT)ab[5]};      \
+    CT M[9];                                                                                          \
+    for (int r = 0; r < 9; ++r) M[r] = (CT)M_[r];                                                     \
+    const CT scale = (CT)scale_;                                                                      \
+    const CT om_a = c32 ? (CT)(1.0f - (((float)ab[0] + (float)ab[1]) + (float)ab[2]))                 \
+                        : (CT)(1.0 - ((ab[0] + ab[1]) + ab[2]));                                      \
+    const CT om_b = c32 ? (CT)(1.0f - (((float)ab[3] + (float)ab[4]) + (float)ab[5]))                 \
+                        : (CT)(1.0 - ((ab[3] + ab[4]) + ab[5]));                                      \
+    const CT fill = s32 ? (CT)(float)fill_ : (CT)fill_;                                               \
+    const CT iminus = edge ? fill : (CT)x[0];                                                         \
+    const CT uminus = iminus / om_a;                                                                  \
+    for (int n = 1; n <= 3; ++n) {                 /* the left border */                              \
+        const int64_t i = n - 1;                                                                      \
+        CT tmp = (CT)x[i * st];                                                                       \
+        for (int j = 1; j <= n - 1; ++j) tmp += a[j - 1] * (CT)y[(i - j) * st];                       \
+        for (int j = n; j <= 3; ++j) tmp += a[j - 1] * uminus;                                        \
+        y[i * st] = s32 ? (double)(float)tmp : (double)tmp;                                           \
+    }                                                                                                 \
+    for (int64_t i = 3; i <= L - 2; ++i) {         /* forward, the last point omitted */              \
+        CT tmp = (CT)x[i * st];                                                                       \
+        for (int j = 1; j <= 3; ++j) tmp += a[j - 1] * (CT)y[(i - j) * st];                           \
+        y[i * st] = s32 ? (double)(float)tmp : (double)tmp;                                           \
+    }                                                                                                 \
+    const CT iplus = edge ? fill : (CT)x[(L - 1) * st]; /* read before the last point is written */   \
+    {                                                                                                 \
+        const int64_t i = L - 1;                                                                      \
+        CT tmp = (CT)x[i * st];                                                                       \
+        for (int j = 1; j <= 3; ++j) tmp += a[j - 1] * (CT)y[(i - j) * st];                           \
+        y[i * st] = s32 ? (double)(float)tmp : (double)tmp;                                           \
+    }                                                                                                 \
+    const CT uplus = iplus / om_a;                                                                    \
+    const CT vplus = uplus / om_b;                                                                    \
+    const CT du[3] = {(CT)y[(L - 1) * st] - uplus, (CT)y[(L - 2) * st] - uplus,                       \
+                      (CT)y[(L - 3) * st] - uplus};                                                   \
+    CT vright[3];                                                                                     \
+    for (int r = 0; r < 3; ++r)                                                                       \
+        vright[r] = (M[3 * r] * du[0] + M[3 * r + 1] * du[1] + M[3 * r + 2] * du[2]) + vplus;         \
+    y[(L - 1) * st] = s32 ? (double)(float)vright[0] : (double)vright[0];                             \
+    int n = 1;                                                                                        \
+    for (int64_t i = L - 2; i >= L - 3; --i) {     /* propagate inward from the right edge */         \
+        ++n;                                                                                          \
+        CT tmp = (CT)y[i * st];                                                                       \
+        for (int j = 1; j <= n - 1; ++j) tmp += b[j - 1] * (CT)y[(i + j) * st];                       \
+        for (int j = n; j <= 3; ++j) tmp += b[j - 1] * vright[j - n + 1];                             \
+        y[i * st] = s32 ? (double)(float)tmp : (double)tmp;                                           \
+    }                                                                                                 \
+    for (int64_t i = L - 4; i >= 0; --i) {         /* backward */                                     \
+        CT tmp = (CT)y[i * st];                                                                       \
+        for (int j = 1; j <= 3; ++j) tmp += b[j - 1] * (CT)y[(i + j) * st];                           \
+        y[i * st] = s32 ? (double)(float)tmp : (double)tmp;                                           \
+    }                                                                                                 \
+    for (int64_t i = 0; i < L; ++i) {                                                                 \
+        const CT v = (CT)y[i * st] * scale;                                                           \
+        y[i * st] = s32 ? (double)(float)v : (double)v;                                               \
+    }                                                                                                 \
+}
+ORA_IIR_LINE(iir_line_f64, double)
+ORA_IIR_LINE(iir_line_f32, float)
+
+/* An IIR cascade (src/imfilter.jl:385-457 with the IIR stage of 427-435 and
+ * the zero-width padding of src/border.jl:640-652): every factor filters the
+ * previous stage's result along its axis over the whole array.  nf factors
+ * with axis[f], ab[6f..6f+5], scale[f], M[9f..9f+8].  img holds the values of
+ * the first stage's input already converted to eltype(out).  arith: 0 =
+ * Float64 arithmetic and storage, 1 = Float32 arithmetic and storage,
+ * 2 = Float64 arithmetic with Float32 storage; c32: Float32 coefficients.  A
+ * line of 3 or fewer elements along a filtered axis is a DimensionMismatch
+ * (src/imfilter.jl:971-977). */
+int ora_imfilter_iir(int nd, const int64_t *n, const double *img, int nf, const int32_t *axis,
+                     const double *ab, const double *scale, const double *M, int edge, double fill,
+                     int arith, int c32, double *out)
+{
+    if (nd < 1 || nd > ORA_MAXD) return ORA_EARG;
+    int64_t st[ORA_MAXD];
+    col_strides(nd, n, st);
+    const int64_t total = prod(nd, n);
+    memcpy(out, img, (size_t)total * sizeof(double));
+    const int s32 = arith != 0;
+    for (int f = 0; f < nf; ++f) {
+        const int ax = axis[f];
+        if (ax < 0 || ax >= nd) return ORA_EDIM;
+        const int64_t L = n[ax];
+        if (total == 0) continue;
+        if (L <= 3) return ORA_EDIM;
+        const int64_t inner = st[ax], outer = total / (inner * L);
+        for (int64_t o = 0; o < outer; ++o)
+            for (int64_t p = 0; p < inner; ++p) {
+                double *line = out + o * inner * L + p;
+                if (arith == 1)
+                    iir_line_f32(line, line, L, inner, ab + 6 * f, scale[f], M + 9 * f, edge, fill, s32, c32);
+                else
+                    iir_line_f64(line, line, L, inner, ab + 6 * f, scale[f], M + 9 * f, edge, fill, s32, c32);
+            }
+    }
     return ORA_OK;
 }

@@ -51,6 +51,8 @@ def lib():
         u8p = np.ctypeslib.ndpointer(np.uint8, flags="F")
         _lib.ora_mapwindow_median_u8_mt.argtypes = [i64p, u8p, i64p, i64p, C.c_int, C.c_double,
                                                     u8p, C.c_int64, C.c_int64]
+        _lib.ora_imfilter_iir.argtypes = [C.c_int, i64p, f64p, C.c_int, i32p, f64c, f64c, f64c,
+                                          C.c_int, C.c_double, C.c_int, C.c_int, f64p]
         _lib.ora_set_threads.argtypes = [C.c_int]
     return _lib
 
@@ -187,6 +189,61 @@ def np_padarray(img, style, lo, hi, fill=0.0):
     return np.pad(a, widths, mode=_NP_MODES[style])
 
 
+# ------------------------------------------------------------------- IIR (Triggs-Sdika)
+def triggs_sdika_M(a):
+    """The right-edge matrix of a symmetric Triggs-Sdika filter
+    (TriggsSdika(a, scale), src/kernelfactors.jl:497-505), row-major, in the
+    coefficients' own float type."""
+    a1, a2, a3 = a
+    one = type(a1)(1)
+    den = (one + a1 - a2 + a3) * (one - a1 - a2 - a3) * (one + a2 + (a1 - a3) * a3)
+    M = [[-a3 * a1 + one - a3 * a3 - a2, (a3 + a1) * (a2 + a3 * a1), a3 * (a1 + a3 * a2)],
+         [a1 + a3 * a2, -(a2 - one) * (a2 + a3 * a1), -(a3 * a1 + a3 * a3 + a2 - one) * a3],
+         [a3 * a1 + a2 + a1 * a1 - a2 * a2, a1 * a2 + a3 * a2 * a2 - a1 * a3 * a3 - a3 * a3 * a3 - a3 * a2 + a3,
+          a3 * (a1 + a3 * a2)]]
+    return [[m / den for m in row] for row in M]
+
+
+def iir_gaussian(sigma, T=np.float64):
+    """IIRGaussian(T, σ) (src/kernelfactors.jl:527-545, Young, van Vliet and
+    van Ginkel 2002): (a, b, scale, M) with a == b, every step in T."""
+    T = np.dtype(T).type
+    m0, m1, m2 = T(1.16680), T(1.10783), T(1.40586)
+    q = T(1.31564 * (np.sqrt(1 + 0.490811 * float(sigma) * float(sigma)) - 1))
+    ascale = (m0 + q) * (m1 * m1 + m2 * m2 + T(2) * m1 * q + q * q)
+    B = (m0 * (m1 * m1 + m2 * m2) / ascale) ** 2
+    a1 = q * (T(2) * m0 * m1 + m1 * m1 + m2 * m2 + (T(2) * m0 + T(4) * m1) * q + T(3) * q * q) / ascale
+    a2 = -q * q * (m0 + T(2) * m1 + T(3) * q) / ascale
+    a3 = q * q * q / ascale
+    a = [T(a1), T(a2), T(a3)]
+    return a, list(a), T(B), triggs_sdika_M(a)
+
+
+def imfilter_iir(img, factors, edge="pad", fill=0.0, arith="f64", c32=False):
+    """A cascade of Triggs-Sdika passes (src/imfilter.jl:961-1092): factors are
+    (axis, a, b, scale, M); edge "pad" takes the boundary values from the
+    lines' end elements (every Pad style, whose padding is empty for IIR
+    filters), "fill" uses `fill`.  arith: "f64" (Float64 arithmetic and
+    results), "f32" (Float32 arithmetic and results) or "f64/f32" (Float64
+    arithmetic, Float32 results); c32: Float32 coefficients.  `img` must hold
+    the values of the output eltype (Float32 values for the "f32" forms)."""
+    a = _f64(img)
+    nf = len(factors)
+    axis = np.array([f[0] for f in factors], dtype=np.int32)
+    ab = np.ascontiguousarray(np.concatenate([np.r_[np.asarray(f[1], np.float64), np.asarray(f[2], np.float64)]
+                                              for f in factors]) if nf else np.zeros(1))
+    sc = np.ascontiguousarray(np.array([float(f[3]) for f in factors] or [1.0]))
+    M = np.ascontiguousarray(np.concatenate([np.asarray(f[4], np.float64).reshape(-1) for f in factors])
+                             if nf else np.zeros(9))
+    out = np.zeros(a.shape, dtype=np.float64, order="F")
+    rc = lib().ora_imfilter_iir(a.ndim, _dims(a), a, nf, axis, ab, sc, M, 1 if edge == "fill" else 0,
+                                float(fill), {"f64": 0, "f32": 1, "f64/f32": 2}[arith], int(bool(c32)), out)
+    if rc == 2:
+        raise ValueError("DimensionMismatch")
+    _check(rc)
+    return out
+
+
 # ------------------------------------------------------------------- Algorithm.FFT()
 def nextprod23(n):
     """nextprod([2, 3], n): the smallest 2^a 3^b >= n."""
@@ -241,8 +298,9 @@ def naflag(img, na="isnan"):
 def imfilter_na(img, filt, seps, na="isnan"):
     """_imfilter_na! (src/imfilter.jl:280-318) in FP64.  `filt(a)` is the filter
     with a Fill(0) border; `seps` lists (first, weights) of factor d for axis d
-    when the kernel is separable with one factor per dimension (isseparable,
-    1218-1219), else None.  Separable and no NA element: the Fill(0) filter
+    -- or, for an IIR factor, a function that filters a vector of ones with it
+    and Fill(0) -- when the kernel is separable with one factor per dimension
+    (isseparable, 1218-1219), else None.  Separable and no NA element: the Fill(0) filter
     divided by the per-axis filters of ones, in axis order (normalize_dims!,
     1241-1250); otherwise the filter of the image with NA elements zeroed
     divided by the filter of the valid-pixel mask (imfilter_na_inseparable!,
@@ -256,9 +314,13 @@ def imfilter_na(img, filt, seps, na="isnan"):
 def _imfilter_na(img, filt, seps, flag):
     if seps is not None and not flag.any():
         out = np.asarray(filt(img), dtype=np.float64)
-        for d, (first, w) in enumerate(seps):
+        for d, sep in enumerate(seps):
             ones = np.asfortranarray(np.ones(img.shape[d]))
-            sd = imfilter_cascade(ones, [(0, first, np.asarray(w, np.float64))], "fill", 0.0)
+            if callable(sep):                      # an IIR factor: its filter of ones (1222-1228)
+                sd = sep(ones)
+            else:
+                first, w = sep
+                sd = imfilter_cascade(ones, [(0, first, np.asarray(w, np.float64))], "fill", 0.0)
             shape = [1] * img.ndim
             shape[d] = -1
             out = out / np.asarray(sd).reshape(shape)

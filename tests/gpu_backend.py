@@ -33,6 +33,31 @@ class GpuBackend:
         k = ifx.OffsetKernel(np.asarray(K, np.float64), tuple(kfirst))
         return np.asarray(ifx.imfilter(img, (k,), self._border(style, fill)), dtype=np.float64)
 
+    def _iir_kern(self, sigmas, nd):
+        ifx = self.ifx
+        return tuple(ifx.ReshapedOneD(ifx.KernelFactors.IIRGaussian(s), nd, ax) for ax, s in sigmas)
+
+    def iir(self, img, sigmas, style, fill=0.0):
+        ifx = self.ifx
+        img = self._img(img)
+        try:
+            out = ifx.imfilter(img, self._iir_kern(sigmas, img.ndim), self._border(style, fill))
+        except ifx.DimensionMismatch as e:
+            raise ValueError("DimensionMismatch: %s" % e)
+        return np.asarray(out, dtype=np.float64)
+
+    def iir_dim(self, img, sigma, dim, style):
+        ifx = self.ifx
+        img = self._img(img)
+        out = np.asfortranarray(np.zeros(img.shape))
+        ifx.imfilter_(out, img, ifx.KernelFactors.IIRGaussian(sigma), dim, style)
+        return out
+
+    def iir_na(self, img, sigmas, na="isnan"):
+        ifx = self.ifx
+        img = self._img(img)
+        return np.asarray(ifx.imfilter(img, self._iir_kern(sigmas, img.ndim), ifx.NA(na)), dtype=np.float64)
+
     def fft(self, img, K, kfirst, style, fill=0.0):
         ifx = self.ifx
         k = ifx.OffsetKernel(np.asarray(K, np.float64), tuple(kfirst))

@@ -87,6 +87,31 @@ class OracleBackend:
     def fft(self, img, K, kfirst, style, fill=0.0):
         return self.O.imfilter_fft(img, K, kfirst, style, fill)
 
+    def _iir_facs(self, sigmas):
+        facs = []
+        for ax, s in sigmas:
+            a, b, B, M = self.O.iir_gaussian(s)
+            if any(x != 0 for x in a) or B != 1:
+                facs.append((ax, a, b, B, M))
+        return facs
+
+    def iir(self, img, sigmas, style, fill=0.0):
+        """IIRGaussian factors (axis, σ) as a ReshapedOneD cascade."""
+        return self.O.imfilter_iir(img, self._iir_facs(sigmas), "fill" if style == "fill" else "pad", fill)
+
+    def iir_dim(self, img, sigma, dim, style):
+        return self.iir(img, [(dim - 1, sigma)], style)
+
+    def iir_na(self, img, sigmas, na="isnan"):
+        O = self.O
+        facs = self._iir_facs(sigmas)
+        filt = lambda a: O.imfilter_iir(a, facs, "fill", 0.0)
+        nd = np.asarray(img).ndim
+        seps = None
+        if len(sigmas) == nd and [ax for ax, _ in sigmas] == list(range(nd)):
+            seps = [(lambda v, f=self._iir_facs([(0, s)]): O.imfilter_iir(v, f, "fill", 0.0)) for _, s in sigmas]
+        return O.imfilter_na(img, filt, seps, na)
+
     def fft_cascade(self, img, factors, style, fill=0.0):
         nd = np.asarray(img).ndim
         K, first = cascade_kernel(factors, nd)
@@ -710,3 +735,67 @@ def check_fft_equals_fir(be, O, tol=1e-12):
             got = be.fft(a, K, first, style, 0.3)
             d = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
             assert d <= tol, (shape, ks, style, d)
+
+
+# ------------------------------------------------------------------- IIR (Triggs-Sdika)
+def check_iir_1d(be):
+    """test/triggs.jl:6-33: impulses at the ends and inside a 1000-vector,
+    IIRGaussian(σ) with Fill(0) stays within 10% (normwise) of the sampled
+    Gaussian; a 2-vector is a DimensionMismatch."""
+    l = 1000
+    xs = [1, 2, 3, 5, 10, 20, l >> 1, l - 19, l - 9, l - 4, l - 2, l - 1, l]
+    for sigma in [3.1, 5, 10.0, 20, 50.0, 100.0]:
+        for c in xs:
+            a = np.zeros(l)
+            a[c - 1] = 1
+            af = np.exp(-((np.arange(1, l + 1)) - c) ** 2 / (2 * sigma ** 2)) / (sigma * np.sqrt(2 * np.pi))
+            got = be.iir(F(a), [(0, sigma)], "fill", 0.0)
+            assert np.linalg.norm(got - af) < 0.1 * np.linalg.norm(af), (sigma, c)
+    try:
+        be.iir(F([1.0, 2.0]), [(0, 2.0)], "replicate")
+    except Exception as e:                         # DimensionMismatch on both backends
+        assert "DimensionMismatch" in type(e).__name__ + str(e)
+    else:
+        raise AssertionError("a 2-vector must be a DimensionMismatch")
+
+
+def check_iir_images(be):
+    """test/triggs.jl:45-82: the impulse of a 5x7 image filtered with
+    IIRGaussian((5,5)) and Fill(0) is within 20% (L2) of the sampled 2-D
+    Gaussian; (σ,0) and (0,σ) change the image; one pass along dimension 2
+    equals the (0,σ) cascade; with a NaN and NA() the result is the Fill(0)
+    filter of the zeroed image over the filter of the valid mask."""
+    sigma = 5
+    img = np.zeros((5, 7))
+    img[2, 3] = 1
+    img = F(img)
+    x = np.arange(-2, 3).reshape(-1, 1)
+    y = np.arange(-3, 4).reshape(1, -1)
+    cmp = np.exp(-(x ** 2 + y ** 2) / (2 * sigma ** 2)) / (sigma ** 2 * 2 * np.pi)
+    got = be.iir(img, [(0, sigma), (1, sigma)], "fill", 0.0)
+    assert np.sum((cmp - got) ** 2) < 0.2 ** 2 * np.sum(cmp ** 2)
+    r1 = be.iir(img, [(0, sigma), (1, 0)], "replicate")
+    r2 = be.iir(img, [(0, 0), (1, sigma)], "replicate")
+    assert not np.array_equal(r1, img) and not np.array_equal(r2, img)
+    np.testing.assert_array_equal(be.iir_dim(img, sigma, 2, "replicate"), r2)
+    nan = img.copy()
+    num = img.copy()
+    nan[0, 0] = np.nan
+    num[0, 0] = 0
+    den = np.ones(img.shape)
+    den[0, 0] = 0
+    rnum = be.iir(F(num), [(0, sigma), (1, sigma)], "fill", 0.0)
+    rden = be.iir(F(den), [(0, sigma), (1, sigma)], "fill", 0.0)
+    ret = be.iir_na(F(nan), [(0, sigma), (1, sigma)])
+    ret[0, 0] = rnum[0, 0] = 0
+    np.testing.assert_allclose(ret, rnum / rden, rtol=1e-10, atol=1e-14)
+
+
+def check_iir_na_ramp(be):
+    """test/triggs.jl:84-96: NA() on the 100x100 ramp 1:10000 (no NA element:
+    the separable normalisation) -- finite and close to the ramp itself away
+    from the edges (a Gaussian of a linear ramp is the ramp)."""
+    A = F(np.arange(1, 100 * 100 + 1, dtype=np.float64).reshape(100, 100, order="F"))
+    B = be.iir_na(A, [(0, 5.0), (1, 5.0)])
+    assert np.all(np.isfinite(B))
+    np.testing.assert_allclose(B[30:70, 30:70], A[30:70, 30:70], rtol=1e-3)

@@ -117,3 +117,15 @@ def test_fft_nopad(be):
 
 def test_fft_equals_fir(be, oracle):
     K.check_fft_equals_fir(be, oracle)
+
+
+def test_iir_1d(be):
+    K.check_iir_1d(be)
+
+
+def test_iir_images(be):
+    K.check_iir_images(be)
+
+
+def test_iir_na_ramp(be):
+    K.check_iir_na_ramp(be)

@@ -743,3 +743,100 @@ def test_dense_auto_takes_fft(gpu_ifx, oracle):
     fin = ~np.isnan(refb)
     assert np.isnan(refb).sum() == 31 * 31
     assert normwise(got[fin], refb[fin]) <= 1e-12
+
+
+# --------------------------------------------------------------------- IIR (Triggs-Sdika)
+def _iir_ref(oracle, vals, sigmas, style, fill, T=np.float64, arith="f64"):
+    facs = []
+    for ax, s in sigmas:
+        a, b, B, M = oracle.iir_gaussian(s, T)
+        facs.append((ax, a, b, B, M))
+    return oracle.imfilter_iir(vals, facs, "fill" if style == "fill" else "pad", fill, arith,
+                               T == np.float32)
+
+
+@pytest.mark.parametrize("kind", ["F32", "F64", "N0F8"])
+@pytest.mark.parametrize("style", ["replicate", "circular", "fill"])
+def test_iir_matches_oracle_bitwise(gpu_ifx, oracle, kind, style):
+    """IIRGaussian cascades (Float64 coefficients, Float64 results) on 1-D to
+    3-D arrays, both the contiguous and the strided axes, small and large σ:
+    the same bits as the oracle (same operation order, every product and sum
+    rounded once, results kept in the output eltype between steps)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("iir" + kind + style).encode()))
+    for shape, sig in [((1000,), (30.0,)), ((301, 257), (1.5, 4.0)), ((40, 33, 21), (2.0, 0.0, 3.5)),
+                       ((5, 7), (5.0, 5.0)), ((64, 4), (9.0, 1.2))]:
+        img = make_img(rng, shape, kind)
+        vals = values(ifx, img, kind)
+        kern = ifx.KernelFactors.IIRGaussian(sig) if len(sig) > 1 else \
+            (ifx.ReshapedOneD(ifx.KernelFactors.IIRGaussian(sig[0]), 1, 0),)
+        got = ifx.imfilter(wrap(ifx, img, kind), kern, border_of(ifx, style))
+        assert got.dtype == np.float64
+        ref = _iir_ref(oracle, vals, [(d, s) for d, s in enumerate(sig) if s != 0], style, 0.7)
+        assert np.array_equal(got, ref), (shape, sig, np.max(np.abs(got - ref)))
+
+
+def test_iir_float32_forms(gpu_ifx, oracle):
+    """Float32 coefficients on a Float32 image (Float32 arithmetic and
+    results) and Float64 coefficients into a Float32 output (Float64
+    arithmetic, Float32 results): the same bits as the oracle's Float32 forms;
+    bare TriggsSdika tuples take the axes in order and refuse other Pad styles;
+    in place on a vector; one pass along a dimension."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(606)
+    img = np.asfortranarray(rng.random((123, 77), dtype=np.float32))
+    s32 = (np.float32(2.5), np.float32(6.0))
+    got = ifx.imfilter(img, ifx.KernelFactors.IIRGaussian(s32), "replicate")
+    assert got.dtype == np.float32
+    ref = _iir_ref(oracle, img.astype(np.float64), [(0, s32[0]), (1, s32[1])], "replicate", 0.0,
+                   np.float32, "f32")
+    assert np.array_equal(got.astype(np.float64), ref)
+    out = np.asfortranarray(np.zeros(img.shape, np.float32))
+    ifx.imfilter_(out, img, ifx.KernelFactors.IIRGaussian((3.0, 7.0)), ifx.Fill(0.25))
+    ref = _iir_ref(oracle, img.astype(np.float64), [(0, 3.0), (1, 7.0)], "fill", 0.25, np.float64, "f64/f32")
+    assert np.array_equal(out.astype(np.float64), ref)
+    ts = ifx.KernelFactors.IIRGaussian(4.0)
+    bare = ifx.imfilter(img, (ts, ts), "replicate")
+    assert np.array_equal(bare, ifx.imfilter(img, ifx.KernelFactors.IIRGaussian((4.0, 4.0)), "replicate"))
+    with pytest.raises(ifx.ArgumentError):
+        ifx.imfilter(img, (ts, ts), "circular")
+    with pytest.raises(ifx.DimensionMismatch):
+        ifx.imfilter(img, (ts, ts, ts), "replicate")
+    v = np.asfortranarray(rng.random(500))
+    exp = _iir_ref(oracle, v, [(0, 4.0)], "fill", 0.0)
+    ifx.imfilter_(v, v, (ts,), ifx.Fill(0))
+    assert np.array_equal(v, exp)
+    o2 = np.asfortranarray(np.zeros(img.shape))
+    ifx.imfilter_(o2, img, ts, 2, "replicate")
+    assert np.array_equal(o2, _iir_ref(oracle, img.astype(np.float64), [(1, 4.0)], "replicate", 0.0))
+
+
+def test_iir_full_size_bitwise(gpu_ifx, oracle):
+    """A 2048x2048 Float32 image through IIRGaussian((3, 8)) with Fill(0):
+    bit-exact with the oracle at full size."""
+    ifx = gpu_ifx
+    img = np.asfortranarray(np.random.default_rng(2048).random((2048, 2048), dtype=np.float32))
+    got = ifx.imfilter(img, ifx.KernelFactors.IIRGaussian((3.0, 8.0)), ifx.Fill(0))
+    ref = _iir_ref(oracle, img.astype(np.float64), [(0, 3.0), (1, 8.0)], "fill", 0.0)
+    assert np.array_equal(got, ref)
+
+
+def test_iir_na_and_errors(gpu_ifx, oracle):
+    ifx = gpu_ifx
+    rng = np.random.default_rng(707)
+    img = np.asfortranarray(rng.random((60, 45)))
+    img[10, 7] = np.nan
+    img[33, 40] = np.nan
+    kern = ifx.KernelFactors.IIRGaussian((2.0, 3.0))
+    got = ifx.imfilter(img, kern, ifx.NA())
+    a1, b1, B1, M1 = oracle.iir_gaussian(2.0)
+    a2, b2, B2, M2 = oracle.iir_gaussian(3.0)
+    facs = [(0, a1, b1, B1, M1), (1, a2, b2, B2, M2)]
+    ref = oracle.imfilter_na(img, lambda a: oracle.imfilter_iir(a, facs, "fill", 0.0), None)
+    assert normwise(got, ref) <= 1e-12
+    with pytest.raises(ifx.DimensionMismatch):
+        ifx.imfilter(np.zeros((3, 10)), kern, "replicate")
+    with pytest.raises(ifx.ArgumentError):
+        ifx.imfilter(np.zeros((30, 10)), kern, ifx.Inner())
+    with pytest.raises(ifx.Unsupported):
+        ifx.imfilter(np.zeros((30, 10)), (kern[0], ifx.centered(np.ones(3) / 3)), "replicate")
