@@ -293,8 +293,7 @@ def _iir_factors(kernel, nd):
             if iscopy(k):
                 continue
             if not (isinstance(k, ReshapedOneD) and isinstance(k.data, TriggsSdika)):
-                raise _abi.Unsupported("cascades that mix IIR and FIR filters (Algorithm.Mixed) are not "
-                                       "part of the GB300 path")
+                return "mixed", False
             if k.axis >= nd:
                 raise _abi.DimensionMismatch("factor along axis %d of a %d-d image" % (k.axis + 1, nd))
             facs.append((k.axis, k.data))
@@ -327,6 +326,85 @@ def _imfilter_iir(out, img, facs, border, bare, kind, okind):
     ctx = _ctx()
     _abi.check(ctx.lib.ifx_imfilter_iir(ctx.handle, _desc(out, okind), _desc(img, kind), len(facs), arr, b,
                                         stream_for(img, out)))
+    return out
+
+
+def _colmajor(t):
+    """A dense column-major copy of a (strided) torch view."""
+    rev = list(reversed(range(t.dim())))
+    return t.permute(*rev).contiguous().permute(*rev)
+
+
+def _imfilter_mixed(out, img, kernel, border, alg, kind, okind):
+    """Algorithm.Mixed: a cascade of Triggs-Sdika and FIR filters
+    (src/imfilter.jl:385-457 with the padding of src/border.jl:614-662).  The
+    image is padded (in the output eltype) by twice the accumulated FIR
+    padding; stage k filters over indsstep_k -- the padded range shrunk by the
+    first filter, then by each next one (next_shrink) -- so an IIR stage has
+    its boundary values at the edges of its range; the image's indices are
+    kept.  Every stage is a GPU call: FIR stages are Inner() filters of the
+    stage's input box, IIR stages ifx_imfilter_iir passes over theirs."""
+    import torch
+    from .borders import padarray as _padarray
+    nd = img.ndim
+    if isinstance(border, (Inner, NoPad)):
+        raise _abi.ArgumentError("IIR filters take NA(), Pad or Fill borders, not %r" % (border,))
+    if okind not in ("F32", "F64"):
+        raise _abi.Unsupported("IIR filtering writes Float32 or Float64 outputs")
+    stages = []
+    for k in kernel:
+        if iscopy(k):
+            continue
+        if isinstance(k, TriggsSdika):
+            if nd != 1:
+                raise _abi.Unsupported("a bare TriggsSdika in a mixed cascade filters vectors only")
+            stages.append(("iir", 0, k, [(0, 0)]))
+        elif _is_iir(k):
+            stages.append(("iir", k.axis, k.data, [(0, 0)] * nd))
+        else:
+            lo, hi = kernel_support((k,), nd)
+            stages.append(("fir", k, None, list(zip(lo, hi))))
+    for st in stages:
+        if len(st[3]) < nd:
+            st[3].extend([(0, 0)] * (nd - len(st[3])))
+    pf, pl = kernel_support(kernel, nd)               # accumulate_padding (IIR filters 0:0)
+    pf = [2 * f if f < 0 else f for f in pf]          # doublepadding: IIR and FIR together
+    pl = [2 * l if l > 0 else l for l in pl]
+    lo = tuple(max(-f, 0) for f in pf)
+    hi = tuple(max(l, 0) for l in pl)
+    dimg = img if isinstance(img, DeviceArray) else DeviceArray.from_host(host_view(img, kind))
+    pb = Fill(border.value, lo, hi) if isinstance(border, Fill) else type(border)(border.style, lo, hi)
+    buf, _ = _padarray(dimg, pb, okind)               # image index i (0-based) at i + lo
+    R = [(f, n - 1 + l) for f, l, n in zip(pf, pl, img.shape)]
+
+    def shrink(R, st):
+        return [(r0 - f, r1 - l) for (r0, r1), (f, l) in zip(R, st[3])]
+
+    def sl(R):
+        return tuple(slice(r0 + o, r1 + o + 1) for (r0, r1), o in zip(R, lo))
+
+    R = shrink(R, stages[0])
+    for i, st in enumerate(stages):
+        nxt = DeviceArray(torch.empty_like(buf.tensor), okind)
+        if st[0] == "iir":
+            sub = DeviceArray(_colmajor(buf.tensor[sl(R)]), okind)
+            res = DeviceArray(_colmajor(torch.empty_like(sub.tensor)), okind)
+            _imfilter_iir(res, sub, [(st[1], st[2])], border, False, okind, okind)
+        else:
+            E = [(r0 + f, r1 + l) for (r0, r1), (f, l) in zip(R, st[3])]
+            sub = DeviceArray(_colmajor(buf.tensor[sl(E)]), okind)
+            res = imfilter(sub, (st[1],), Inner(), alg, okind)
+        nxt.tensor[sl(R)] = res.tensor.to(nxt.tensor.dtype)
+        buf = nxt
+        if i + 1 < len(stages):
+            R = shrink(R, stages[i + 1])
+    I = [(max(r0, 0), min(r1, n - 1)) for (r0, r1), n in zip(R, img.shape)]
+    region = tuple(slice(i0, i1 + 1) for i0, i1 in I)
+    vals = buf.tensor[sl(I)]
+    if isinstance(out, DeviceArray):
+        out.tensor[region] = vals.to(out.tensor.dtype)
+    else:
+        np.asarray(out).view(np.ndarray)[region] = vals.cpu().numpy()
     return out
 
 
@@ -459,6 +537,8 @@ def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
         raise _abi.ArgumentError("imfilter! with Inner(): allocate the interior with imfilter")
     iir = _iir_factors(kernel, nd)
     if iir is not None:
+        if iir[0] == "mixed":
+            return _imfilter_mixed(out, img, kernel, border, alg, kind, okind)
         return _imfilter_iir(out, img, iir[0], border, iir[1], kind, okind)
     b = border_struct(border, nd, kind)
     ai = _desc(img, kind)

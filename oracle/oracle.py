@@ -244,6 +244,64 @@ def imfilter_iir(img, factors, edge="pad", fill=0.0, arith="f64", c32=False):
     return out
 
 
+def imfilter_mixed(img, stages, style, fill=0.0):
+    """A cascade of Triggs-Sdika and FIR filters (Algorithm.Mixed), FP64:
+    src/imfilter.jl:385-457 over the padding of src/border.jl:614-662.  The
+    image is padded by twice the accumulated FIR padding (doublepadding);
+    stage k filters over indsstep_k, which starts as the padded range shrunk
+    by the first filter and shrinks by each next filter (next_shrink); an IIR
+    stage filters its whole range with its boundary values at the range's
+    edges; the image's indices are kept.  stages: ("fir", K, first) with an
+    N-d dense K, or ("iir", axis, (a, b, scale, M))."""
+    a = _f64(img)
+    nd = a.ndim
+
+    def kax(st):
+        if st[0] == "iir":
+            return [(0, 0)] * nd
+        K, first = np.asarray(st[1]), st[2]
+        return [(first[d], first[d] + K.shape[d] - 1) for d in range(nd)]
+
+    pf, pl = [0] * nd, [0] * nd
+    for st in stages:
+        for d, (f, l) in enumerate(kax(st)):
+            pf[d] += f
+            pl[d] += l
+    pf = [2 * f if f < 0 else f for f in pf]
+    pl = [2 * l if l > 0 else l for l in pl]
+    lo = [max(-f, 0) for f in pf]
+    hi = [max(l, 0) for l in pl]
+    buf = padarray(a, style, lo, hi, fill)            # image index i (0-based) at i + lo
+    R = [(f, n - 1 + l) for f, l, n in zip(pf, pl, a.shape)]      # expand(axes, padding), 0-based
+
+    def shrink(R, st):
+        return [(r0 - f, r1 - l) for (r0, r1), (f, l) in zip(R, kax(st))]
+
+    def sl(R):
+        return tuple(slice(r0 + o, r1 + o + 1) for (r0, r1), o in zip(R, lo))
+
+    R = shrink(R, stages[0])
+    for k, st in enumerate(stages):
+        nxt = np.full(buf.shape, np.nan, order="F")
+        if st[0] == "iir":
+            ax, (ca, cb, sc, M) = st[1], st[2]
+            nxt[sl(R)] = imfilter_iir(np.asfortranarray(buf[sl(R)]), [(ax, ca, cb, sc, M)],
+                                      "fill" if style == "fill" else "pad", fill)
+        else:
+            K, first = np.asarray(st[1], np.float64), st[2]
+            E = [(r0 + f, r1 + l) for (r0, r1), (f, l) in zip(R, kax(st))]
+            full = imfilter_dense(np.asfortranarray(buf[sl(E)]), K, first, "replicate")
+            inner = tuple(slice(-f, -f + (r1 - r0 + 1)) for (r0, r1), (f, l) in zip(R, kax(st)))
+            nxt[sl(R)] = full[inner]
+        buf = nxt
+        if k + 1 < len(stages):
+            R = shrink(R, stages[k + 1])
+    out = np.full(a.shape, np.nan, order="F")
+    I = [(max(r0, 0), min(r1, n - 1)) for (r0, r1), n in zip(R, a.shape)]
+    out[tuple(slice(i0, i1 + 1) for i0, i1 in I)] = buf[sl(I)]
+    return out
+
+
 # ------------------------------------------------------------------- Algorithm.FFT()
 def nextprod23(n):
     """nextprod([2, 3], n): the smallest 2^a 3^b >= n."""

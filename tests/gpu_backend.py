@@ -53,6 +53,21 @@ class GpuBackend:
         ifx.imfilter_(out, img, ifx.KernelFactors.IIRGaussian(sigma), dim, style)
         return out
 
+    def mixed(self, img, spec, style, fill=0.0):
+        ifx = self.ifx
+        img = self._img(img)
+        nd = img.ndim
+        ks = []
+        for st in spec:
+            if st[0] == "iir":
+                ts = ifx.KernelFactors.IIRGaussian(st[2])
+                ks.append(ts if nd == 1 else ifx.ReshapedOneD(ts, nd, st[1]))
+            elif st[0] == "lap":
+                ks.append(ifx.Kernel.Laplacian((True,) * nd))
+            else:
+                ks.append(ifx.OffsetKernel(np.asarray(st[1], np.float64), tuple(st[2])))
+        return np.asarray(ifx.imfilter(img, tuple(ks), self._border(style, fill)), dtype=np.float64)
+
     def iir_na(self, img, sigmas, na="isnan"):
         ifx = self.ifx
         img = self._img(img)

@@ -102,6 +102,26 @@ class OracleBackend:
     def iir_dim(self, img, sigma, dim, style):
         return self.iir(img, [(dim - 1, sigma)], style)
 
+    def mixed(self, img, spec, style, fill=0.0):
+        """spec: ("iir", axis, σ) | ("fir", K, first) | ("lap",) in cascade order."""
+        nd = np.asarray(img).ndim
+        stages = []
+        for st in spec:
+            if st[0] == "iir":
+                stages.append(("iir", st[1], self.O.iir_gaussian(st[2])))
+            elif st[0] == "lap":
+                L = np.zeros((3,) * nd)
+                for d in range(nd):
+                    idx = [1] * nd
+                    for e in (0, 2):
+                        idx[d] = e
+                        L[tuple(idx)] = 1
+                L[(1,) * nd] = -2 * nd
+                stages.append(("fir", L, (-1,) * nd))
+            else:
+                stages.append(("fir", np.asarray(st[1], np.float64), tuple(st[2])))
+        return self.O.imfilter_mixed(img, stages, style, fill)
+
     def iir_na(self, img, sigmas, na="isnan"):
         O = self.O
         facs = self._iir_facs(sigmas)
@@ -799,3 +819,39 @@ def check_iir_na_ramp(be):
     B = be.iir_na(A, [(0, 5.0), (1, 5.0)])
     assert np.all(np.isfinite(B))
     np.testing.assert_allclose(B[30:70, 30:70], A[30:70, 30:70], rtol=1e-3)
+
+
+def check_mixed(be):
+    """test/triggs.jl:35-43: IIR and FIR factors commute on 1:8 (Pad(:replicate)
+    and Fill(0)); test/specialty.jl:217-231: (IIRGaussian(σs)..., Laplacian())
+    correlates with the dense LoG (> 0.8) and the (Laplacian(), IIRGaussian...)
+    order trims its edges without reading unset values (no NaN)."""
+    img = F(np.arange(1, 9))
+    for style in ("replicate", "fill"):
+        a = be.mixed(img, [("iir", 0, 2.0), ("fir", np.ones(3) / 3, (-1,))], style, 0.0)
+        b = be.mixed(img, [("fir", np.ones(3) / 3, (-1,)), ("iir", 0, 2.0)], style, 0.0)
+        np.testing.assert_allclose(a, b, rtol=1e-10)
+    rng = np.random.default_rng(217)
+    im = F(rng.random((20, 21)))
+    K, first = LOG_2_5_3_2
+    f1 = be.dense(im, K, first, "replicate")
+    f2 = be.mixed(im, [("iir", 0, 2.5), ("iir", 1, 3.2), ("lap",)], "replicate")
+    assert np.corrcoef(f1.ravel(), f2.ravel())[0, 1] > 0.8
+    f3 = be.mixed(im, [("lap",), ("iir", 0, 2.5), ("iir", 1, 3.2)], "replicate")
+    assert not np.any(np.isnan(f3))
+
+
+def _log_kernel(sigmas):
+    """Kernel.LoG(σs) (src/kernel.jl:325-339), dense FP64, with its first indices."""
+    import math
+    N = len(sigmas)
+    ws = [int(math.ceil(8.5 * s)) >> 1 for s in sigmas]
+    s2 = np.array([float(s) ** 2 for s in sigmas])
+    Cn = 1.0 / (float(np.prod(sigmas)) * (2 * math.pi) ** (N / 2))
+    grids = np.meshgrid(*[np.arange(-w, w + 1, dtype=np.float64) for w in ws], indexing="ij")
+    xs = sum(g * g / s for g, s in zip(grids, s2))
+    xs4 = sum(g * g / (s * s) for g, s in zip(grids, s2))
+    return np.asfortranarray(Cn * (xs4 - float(np.sum(1.0 / s2))) * np.exp(-xs / 2)), tuple(-w for w in ws)
+
+
+LOG_2_5_3_2 = _log_kernel((2.5, 3.2))

@@ -838,5 +838,35 @@ def test_iir_na_and_errors(gpu_ifx, oracle):
         ifx.imfilter(np.zeros((3, 10)), kern, "replicate")
     with pytest.raises(ifx.ArgumentError):
         ifx.imfilter(np.zeros((30, 10)), kern, ifx.Inner())
-    with pytest.raises(ifx.Unsupported):
-        ifx.imfilter(np.zeros((30, 10)), (kern[0], ifx.centered(np.ones(3) / 3)), "replicate")
+    with pytest.raises(ifx.ArgumentError):
+        ifx.imfilter(np.zeros((30, 10)), (kern[0], ifx.Kernel.Laplacian()), ifx.Inner())
+
+
+@pytest.mark.parametrize("style", ["replicate", "reflect", "fill"])
+def test_mixed_cascades_match_oracle(gpu_ifx, oracle, style):
+    """Cascades of IIRGaussian factors with FIR filters (a Laplacian, a dense
+    kernel, a Gaussian factor) in several orders on 2-D and 3-D arrays: the
+    doubled padding, the shrinking stage ranges and the IIR boundary values at
+    each range's edges as the oracle's restatement, within 1e-12 (Float64
+    stages)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("mixed" + style).encode()))
+    lap2 = np.array([[0, 1, 0], [1, -4, 1], [0, 1, 0]], dtype=np.float64)
+    D = rng.standard_normal((3, 5))
+    g = np.asarray(ifx.KernelFactors.gaussian(1.5).data, np.float64)
+    for shape, kind in [((37, 29), "F64"), ((40, 33), "F32")]:
+        img = make_img(rng, shape, kind)
+        vals = values(ifx, img, kind)
+        a1, a2 = (oracle.iir_gaussian(s) for s in (2.5, 3.2))
+        I0 = ifx.ReshapedOneD(ifx.KernelFactors.IIRGaussian(2.5), 2, 0)
+        I1 = ifx.ReshapedOneD(ifx.KernelFactors.IIRGaussian(3.2), 2, 1)
+        G1 = ifx.ReshapedOneD(ifx.centered(g), 2, 1)
+        cases = [((I0, I1, ifx.Kernel.Laplacian()), [("iir", 0, a1), ("iir", 1, a2), ("fir", lap2, (-1, -1))]),
+                 ((ifx.Kernel.Laplacian(), I0, I1), [("fir", lap2, (-1, -1)), ("iir", 0, a1), ("iir", 1, a2)]),
+                 ((I0, ifx.OffsetKernel(D, (-1, -3)), G1),
+                  [("iir", 0, a1), ("fir", D, (-1, -3)), ("fir", g.reshape(1, -1), (0, -(g.size // 2)))])]
+        for ks, stages in cases:
+            got = ifx.imfilter(img, ks, border_of(ifx, style, 0.0))
+            ref = oracle.imfilter_mixed(vals, stages, style, 0.0)
+            assert not np.any(np.isnan(ref))
+            assert normwise(got, ref) <= 1e-12, (shape, style, len(stages))

@@ -170,3 +170,7 @@ def test_iir_images(be):
 
 def test_iir_na_ramp(be):
     K.check_iir_na_ramp(be)
+
+
+def test_mixed_cascades(be):
+    K.check_mixed(be)
