@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--no-dense", action="store_true")
     p.add_argument("--dense-ksizes", type=lambda t: [int(v) for v in t.split(",")], default=None,
                    help="dense section: kernel sizes to run (default 5,11,15,31)")
-    p.add_argument("--only", default=None, choices=[None, "dense", "sections"],
+    p.add_argument("--only", default=None, choices=[None, "dense", "sections", "next"],
                    help="run only one secondary section (small device footprint, for profiling)")
     return p.parse_args()
 
@@ -649,6 +649,64 @@ def run_sections(args, ifx, torch, hbm_peak):
     return out
 
 
+def run_next_rows(args, ifx, torch, hbm_peak):
+    """The callers and algorithms beside the FIR path, device-resident, through
+    the package's public API, CUDA-event timed with the L2 flushed: the FFT
+    algorithm on 4096^2 Float32 (45x45 and 101x101 kernels; the CUDA-core
+    direct kernel at 45x45 beside it), Triggs-Sdika IIRGaussian cascades
+    (4096^2 Float32 image with Float64 and Float32 coefficients; 16 x 1024^2),
+    NA() filtering (4096^2 Float32, 9-tap Gaussian, without and with NaNs) and
+    blob_LoG on a 1024^2 Float32 image (sigma 2, 4, 8)."""
+    out = {}
+    g = torch.Generator(device="cuda")
+    g.manual_seed(11)
+    n = 4096
+    img = ifx.DeviceArray(torch.rand((n, n), device="cuda", generator=g).t(), "F32")
+    o32 = ifx.DeviceArray.empty((n, n), "F32")
+    o64 = ifx.DeviceArray.empty((n, n), "F64")
+    rng = np.random.default_rng(12)
+    for k in (45, 101):
+        K = rng.standard_normal((k, k))
+        K /= K.sum()
+        ker = (ifx.OffsetKernel(K, (-(k // 2), -(k // 2))),)
+        ms = _time(torch, lambda: ifx.imfilter_(o32, img, ker, "reflect", ifx.Algorithm.FFT()))
+        row = {"ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6,
+               "achieved_gbs": n * n * 8 / (ms / 1e3) / 1e9}
+        if k == 45:
+            msd = _time(torch, lambda: ifx.imfilter_(o32, img, ker, "reflect", ifx.Algorithm.GB300("cuda_cores")),
+                        reps=2)
+            row["direct_cuda_cores_ms"] = round(msd, 4)
+        out["fft_4096_%dx%d" % (k, k)] = row
+    for T, o, name in ((np.float64, o64, "f64coef"), (np.float32, o32, "f32coef")):
+        kern = ifx.KernelFactors.IIRGaussian((T(3.0), T(3.0)))
+        ms = _time(torch, lambda: ifx.imfilter_(o, img, kern, "replicate"))
+        osz = 8 if o is o64 else 4
+        out["iir_4096_%s" % name] = {"ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6,
+                                     "achieved_gbs": 2 * n * n * (4 + osz) / (ms / 1e3) / 1e9}
+    vol = ifx.DeviceArray(torch.rand((16, 1024, 1024), device="cuda", generator=g).permute(2, 1, 0), "F32")
+    ov = ifx.DeviceArray.empty((1024, 1024, 16), "F64")
+    kv = ifx.KernelFactors.IIRGaussian((3.0, 3.0, 0.0))
+    ms = _time(torch, lambda: ifx.imfilter_(ov, vol, kv, "replicate"))
+    out["iir_16x1024_f64coef"] = {"ms": round(ms, 4), "mpix_s": 16 * 1024 * 1024 / (ms / 1e3) / 1e6}
+    del vol, ov
+    gk = ifx.KernelFactors.gaussian((2.0, 2.0))
+    ms = _time(torch, lambda: ifx.imfilter_(o64, img, gk, ifx.NA()))
+    out["na_4096_gauss9_nonan"] = {"ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6}
+    nan = ifx.DeviceArray(img.tensor.clone(), "F32")
+    nan.tensor[100, 200] = float("nan")
+    nan.tensor[3000, 17] = float("nan")
+    ms = _time(torch, lambda: ifx.imfilter_(o64, nan, gk, ifx.NA()))
+    out["na_4096_gauss9_nan"] = {"ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6}
+    del nan, o32, o64, img
+    m = 1024
+    bimg = ifx.DeviceArray(torch.rand((m, m), device="cuda", generator=g).t(), "F32")
+    ms = _time(torch, lambda: ifx.blob_LoG(bimg, [2.0, 4.0, 8.0]), reps=3)
+    out["blob_log_1024_3scales"] = {"ms": round(ms, 3), "mpix_s": m * m / (ms / 1e3) / 1e6,
+                                    "note": "multiLoG (LoG as sums of separable terms), local maxima, "
+                                            "threshold; includes the host readback of the blobs"}
+    return out
+
+
 def cpu_stream_baseline(args, seconds, threads):
     """The oracle port (restatement of the reference loops) on a bounded sample
     of the stream, all host threads for the separable passes."""
@@ -728,6 +786,9 @@ def main():
     if args.only == "sections":
         print(json.dumps({"configs": run_sections(args, ifx, torch, peaks()[0])}))
         return 0
+    if args.only == "next":
+        print(json.dumps({"next_rows": run_next_rows(args, ifx, torch, peaks()[0])}))
+        return 0
     res = run_stream(args, ifx, torch, rank)
     dev_ms = res["dev_ms"]
     if ws > 1:
@@ -743,6 +804,7 @@ def main():
     e2e = run_stream_e2e(args, ifx, torch, res["reqs"])
     dense = run_dense4096(args, ifx, torch) if not args.no_dense else None
     sections = run_sections(args, ifx, torch, hbm_peak) if not args.no_dense else None
+    nxt = run_next_rows(args, ifx, torch, hbm_peak) if not args.no_dense else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_stream_baseline(args, args.cpu_seconds, threads)
@@ -784,6 +846,7 @@ def main():
         "clocks": res["clocks"],
         "dense_4096": dense,
         "configs": sections,
+        "next_rows": nxt,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))

@@ -99,7 +99,8 @@ def multiLoG(img, sigmas, sigma_shape=None):
     return stack
 
 
-def _localextrema(img, window, edges, minima):
+def _localextrema_raw(img, window, edges, minima):
+    """(column-major linear indices, values) of the strict local extrema."""
     kind = kind_of(img)
     if not isinstance(img, DeviceArray):
         img = host_view(img, kind)
@@ -115,7 +116,8 @@ def _localextrema(img, window, edges, minima):
     win = (C.c_int32 * 4)(*[int(w) for w in window])
     edg = (C.c_int32 * 4)(*[int(bool(e)) for e in edges])
     ctx = _abi.context()
-    cap = 4096
+    total = int(np.prod(img.shape))
+    cap = max(1, min(total, 1 << 18))
     while True:
         idx = np.empty(cap, dtype=np.int64)
         val = np.empty(cap, dtype=np.float64)
@@ -128,8 +130,13 @@ def _localextrema(img, window, edges, minima):
             break
         cap = count.value
     n = count.value
-    coords = np.unravel_index(idx[:n], img.shape, order="F")
-    return [tuple(int(c[k]) + 1 for c in coords) for k in range(n)], val[:n]
+    return idx[:n], val[:n]
+
+
+def _localextrema(img, window, edges, minima):
+    idx, val = _localextrema_raw(img, window, edges, minima)
+    coords = np.unravel_index(idx, tuple(img.shape), order="F")
+    return [tuple(int(c[k]) + 1 for c in coords) for k in range(idx.size)], val
 
 
 def findlocalmaxima(img, window=None, edges=True):
@@ -158,19 +165,20 @@ def blob_LoG(img, sigmas, edges=None, sigma_shape=None, rthresh=0.001):
     shape = tuple(float(s) for s in (sigma_shape or (1,) * N))
     sig = sorted(float(s) for s in sigmas)
     stack = multiLoG(img, sig, shape)
-    locs, vals = _localextrema(stack, (3,) * (N + 1), tuple(edges), False)
-    out = []
+    idx, vals = _localextrema_raw(stack, (3,) * (N + 1), tuple(edges), False)
+    coords = np.unravel_index(idx, tuple(stack.shape), order="F")
     if rthresh != 0:
-        athresh = [rthresh / (s ** N * float(np.prod(shape))) for s in sig]
+        athresh = np.array([rthresh / (s ** N * float(np.prod(shape))) for s in sig])
         imgmax = C.c_double(0)
         ctx = _abi.context()
         _abi.check(ctx.lib.ifx_maxabs(ctx.handle, _desc(img, kind), C.byref(imgmax), stream_for(img)))
-        for loc, v in zip(locs, vals):
-            if v > athresh[loc[0] - 1] * imgmax.value:
-                out.append(BlobLoG(loc[1:], tuple(sig[loc[0] - 1] * f for f in shape), v))
+        # the same comparison per maximum, vectorised: v > athresh[scale] * maximum(abs, img)
+        keep = vals > athresh[coords[0]] * imgmax.value
     else:
-        out = [BlobLoG(loc[1:], tuple(sig[loc[0] - 1] * f for f in shape), v) for loc, v in zip(locs, vals)]
-    return out
+        keep = np.ones(vals.size, dtype=bool)
+    sel = np.nonzero(keep)[0]
+    return [BlobLoG(tuple(int(c[k]) + 1 for c in coords[1:]), tuple(sig[coords[0][k]] * f for f in shape),
+                    vals[k]) for k in sel]
 
 
 __all__ = ["BlobLoG", "blob_LoG", "multiLoG", "findlocalmaxima", "findlocalminima", "log_terms"]

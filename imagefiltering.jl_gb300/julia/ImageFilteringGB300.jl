@@ -199,6 +199,71 @@ function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::
     copyto!(out, CartesianIndices(axes(out)), full, CartesianIndices(axes(out)))
 end
 
+# ---------------------------------------------------------------- Algorithm.IIR()
+# Triggs-Sdika cascades (src/imfilter.jl:892-1092) -> ifx_imfilter_iir.  The
+# ReshapedOneD{...,TriggsSdika} tuples of IIRGaussian((σ...)) filter along their
+# own axes with any Pad style (their padding is empty) or Fill; a tuple of bare
+# TriggsSdika filters takes the axes in order and only :replicate or Fill.
+struct IfxIir
+    axis::Int32
+    coef_f32::Int32
+    a::NTuple{3,Float64}
+    b::NTuple{3,Float64}
+    scale::Float64
+    M::NTuple{9,Float64}                 # row-major
+    asum::Float64
+    bsum::Float64
+end
+const TS = ImageFiltering.KernelFactors.TriggsSdika
+ifxiir(k::TS{T}, axis) where {T} =
+    IfxIir(Int32(axis), Int32(T === Float32), Float64.(Tuple(k.a)), Float64.(Tuple(k.b)), Float64(k.scale),
+           ntuple(i -> Float64(k.M[(i - 1) ÷ 3 + 1, (i - 1) % 3 + 1]), 9), Float64(k.asum), Float64(k.bsum))
+
+function iir_call(out, img, facs::Vector{IfxIir}, b::IfxBorder)
+    GC.@preserve out img facs begin
+        check(ccall((:ifx_imfilter_iir, libifx), Cint,
+                    (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Int32, Ptr{IfxIir}, Ref{IfxBorder}, Ptr{Cvoid}),
+                    context(), Ref(ifxarray(out)), Ref(ifxarray(img)), Int32(length(facs)), facs, b, C_NULL))
+    end
+    out
+end
+
+function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
+                                  kernel::Tuple{ImageFiltering.ReshapedIIR,Vararg{ImageFiltering.ReshapedIIR}},
+                                  border::Union{Pad,Fill}) where {S,T,N}
+    facs = [ifxiir(k.data, npre(k)) for k in kernel if !iscopy(k)]
+    iir_call(out, img, facs, ifxborder(border, S))
+end
+
+function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
+                                  kernel::Tuple{TS,Vararg{TS}}, border::Union{Pad,Fill}) where {S,T,N}
+    isa(border, Pad) && border.style != :replicate && throw(ArgumentError("only \"replicate\" is supported"))
+    length(kernel) <= N || throw(DimensionMismatch("cannot have more kernels than dimensions"))
+    facs = [ifxiir(k, d - 1) for (d, k) in enumerate(kernel) if !iscopy(k)]
+    iir_call(out, img, facs, ifxborder(border, S))
+end
+
+# ---------------------------------------------------------------- Algorithm.FFT()
+# A second tag for the cuFFT path (src/imfilter.jl:776-884): the image padded
+# to the padfft sizes and correlated with the kernelconv composite.
+"Filter on a GB300 GPU through real FFTs (cuFFT)."
+struct GB300FFT <: Alg end
+export GB300FFT
+
+function ImageFiltering.imfilter!(r::CPU1{GB300FFT}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
+                                  kernel::ProcessedKernel, border::Union{Pad{0},Fill{<:Any,0}}) where {S,T,N}
+    K = ImageFiltering.samedims(out, ImageFiltering.kernelconv(kernel...))
+    Kd = collect(Float64, parent(K))
+    GC.@preserve out img Kd begin
+        check(ccall((:ifx_imfilter_fft, libifx), Cint,
+                    (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Ptr{Float64}, Ref{NTuple{4,Int64}},
+                     Ref{NTuple{4,Int64}}, Ref{IfxBorder}, Ptr{Cvoid}),
+                    context(), Ref(ifxarray(out)), Ref(ifxarray(img)), Kd, pad4(size(K), 1),
+                    pad4(map(first, axes(K)), 0), ifxborder(border, T), C_NULL))
+    end
+    out
+end
+
 # ---------------------------------------------------------------- mapwindow
 # mapwindow has no Alg hook; the entry points take the resource first.
 function ImageFiltering.mapwindow(::CPU1{GB300}, ::Union{typeof(median!),typeof(median)}, img::AbstractArray{T,N},
