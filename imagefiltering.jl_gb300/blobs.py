@@ -24,6 +24,12 @@ class BlobLoG:
         self.sigma = tuple(float(s) for s in sigma)
         self.amplitude = float(amplitude)
 
+    @classmethod
+    def _fast(cls, location, sigma, amplitude):
+        b = cls.__new__(cls)
+        b.location, b.sigma, b.amplitude = location, sigma, amplitude
+        return b
+
     def __eq__(self, other):
         return (isinstance(other, BlobLoG) and self.location == other.location and self.sigma == other.sigma
                 and self.amplitude == other.amplitude)
@@ -177,8 +183,10 @@ def blob_LoG(img, sigmas, edges=None, sigma_shape=None, rthresh=0.001):
     else:
         keep = np.ones(vals.size, dtype=bool)
     sel = np.nonzero(keep)[0]
-    return [BlobLoG(tuple(int(c[k]) + 1 for c in coords[1:]), tuple(sig[coords[0][k]] * f for f in shape),
-                    vals[k]) for k in sel]
+    locs = map(tuple, (np.stack([c[sel] for c in coords[1:]], axis=1) + 1).tolist())
+    sigt = [tuple(s * f for f in shape) for s in sig]
+    return [BlobLoG._fast(loc, sigt[k], v)
+            for loc, k, v in zip(locs, coords[0][sel].tolist(), vals[sel].tolist())]
 
 
 __all__ = ["BlobLoG", "blob_LoG", "multiLoG", "findlocalmaxima", "findlocalminima", "log_terms"]

@@ -7,7 +7,10 @@
 //      on a copy stream as soon as a request is admitted;
 //   2. while fewer than `max_inflight` batches run, packs admitted requests
 //      into one batched launch (the persistent tile work-queue kernel of
-//      ifx_batch.cu) on the compute stream, which waits for the uploads;
+//      ifx_batch.cu) on the compute stream, which waits for the uploads of
+//      that batch's requests only; after an idle period the first batches
+//      are smaller (1/8, 1/4, 1/2 of max_batch), so that results start
+//      flowing back over the link early;
 //   3. when a batch finishes, copies host outputs back on a download stream
 //      (the link's two directions overlap) and releases the request's device
 //      memory after those copies;
@@ -45,6 +48,7 @@ struct SReq {
     int status = IFX_OK;
     bool done = false;
     BatchItem item{};                      // validated form (fill values)
+    cudaEvent_t staged_ev = nullptr;       // after this request's allocations and upload (copy stream)
 };
 
 struct SBatch {
@@ -70,6 +74,7 @@ struct ifx_server {
     std::unordered_map<uint64_t, std::shared_ptr<ifx::SReq>> by_ticket;
     std::vector<double> latencies;
     uint64_t next_ticket = 1, submitted = 0, completed = 0, failed = 0, batches = 0;
+    int ramp = 0;                          // batches launched since the engine was last idle
     long long pixels = 0;
     int64_t hbm_in_use = 0, hbm_peak = 0;
     bool have_first = false;
@@ -158,8 +163,17 @@ static void admit(ifx_server *S)
             else r->d_out[o] = r->q.out[o].data;
         }
         S->queue.pop_front();
+        if (ok && (r->host_in || r->host_out[0] || r->host_out[1])) {
+            // the batch that takes this request waits for this point of the copy stream only
+            ok &= cudaEventCreateWithFlags(&r->staged_ev, cudaEventDisableTiming) == cudaSuccess;
+            if (ok) ok &= cudaEventRecord(r->staged_ev, S->copy) == cudaSuccess;
+        }
         if (!ok) {
             (void)cudaGetLastError();
+            if (r->staged_ev) {
+                cudaEventDestroy(r->staged_ev);
+                r->staged_ev = nullptr;
+            }
             r->status = IFX_ERR_NOMEM;
             r->done = true;
             ++S->failed;
@@ -176,15 +190,27 @@ static void admit(ifx_server *S)
 static void launch(ifx_server *S)
 {
     if (S->staged.empty() || (int)S->inflight.size() >= S->cfg.max_inflight) return;
-    const size_t n = std::min(S->staged.size(), (size_t)S->cfg.max_batch);
+    // Ramp: after an idle engine the first batches are 1/8, 1/4, 1/2 of max_batch, so
+    // that the first results reach the download stream early (a served stream is
+    // bound by the host link, and the link's download direction idles until then).
+    const size_t cap = std::max<size_t>(std::min<size_t>(16, (size_t)S->cfg.max_batch),
+                                        (size_t)S->cfg.max_batch >> std::max(0, 3 - S->ramp));
+    const size_t n = std::min(S->staged.size(), cap);
+    ++S->ramp;
     SBatch b;
     b.reqs.assign(S->staged.begin(), S->staged.begin() + n);
     S->staged.erase(S->staged.begin(), S->staged.begin() + n);
-    cudaEvent_t uploaded;
-    cudaEventCreateWithFlags(&uploaded, cudaEventDisableTiming);
-    cudaEventRecord(uploaded, S->copy);                     // every upload enqueued so far
-    cudaStreamWaitEvent(S->compute, uploaded, 0);
-    cudaEventDestroy(uploaded);
+    // wait for the copy-stream work of this batch's requests only: uploads are in
+    // admission order, so the last request's event covers the earlier ones
+    cudaEvent_t last = nullptr;
+    for (auto &r : b.reqs)
+        if (r->staged_ev) last = r->staged_ev;
+    if (last) cudaStreamWaitEvent(S->compute, last, 0);
+    for (auto &r : b.reqs)
+        if (r->staged_ev) {
+            cudaEventDestroy(r->staged_ev);                 // released once it has completed
+            r->staged_ev = nullptr;
+        }
     std::vector<BatchItem> items(n);
     for (size_t i = 0; i < n; ++i) {
         const SReq &r = *b.reqs[i];
@@ -237,6 +263,7 @@ static void engine_loop(ifx_server *S)
         launch(S);
         const bool idle = S->incoming.empty() && S->queue.empty() && S->staged.empty() &&
                           S->inflight.empty();
+        if (idle) S->ramp = 0;
         if (idle) S->cv_work.wait_for(lk, std::chrono::milliseconds(5));
         else {
             lk.unlock();
