@@ -73,13 +73,21 @@ __host__ __device__ inline int bt_tile_h(int op, int in_type)
     return op == BOP_FACTORED ? kFTY : kGTY;
 }
 
+// Thread roles of k_batch: warp 0 is the producer (it looks tiles up and
+// issues their copies); the other warps -- the consumers -- gather border
+// windows and run the tile routines, synchronising among themselves with
+// named barrier 1.
+__device__ __forceinline__ int ct_id() { return (int)threadIdx.x - 32; }
+__device__ __forceinline__ int ct_n() { return (int)blockDim.x - 32; }
+__device__ __forceinline__ void ct_sync() { asm volatile("bar.sync 1, %0;" ::"r"(ct_n()) : "memory"); }
+
 // Division-free 2-D gather of a tile whose element (r, c) is load(r, c): warps
 // take rows, lanes take columns; each thread issues up to 2 rows x 4 column
 // chunks of loads before storing them, so 8 global loads are in flight.
 template <class T, class F>
 __device__ __forceinline__ void gather2d(T *dst, int rows, int cols, int pitch, F load)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = ct_id() >> 5, nw = ct_n() >> 5;
     for (int r0 = warp; r0 < rows; r0 += 2 * nw) {
         T v[2][4];
 #pragma unroll
@@ -184,7 +192,7 @@ __device__ __forceinline__ void bt_issue_rows(const BReq &R, const TileGeo &g, u
 __device__ __forceinline__ void bt_gather_raw(const BReq &R, const TileGeo &g, unsigned char *st,
                                               unsigned char *lead)
 {
-    for (int r = threadIdx.x; r < g.rows; r += blockDim.x) lead[r] = 0;
+    for (int r = ct_id(); r < g.rows; r += ct_n()) lead[r] = 0;
     const int nx = R.nx, ny = R.ny, style = R.style;
     if (g.elt == 4) {
         const float *img = (const float *)R.in;
@@ -292,7 +300,7 @@ __device__ void bt_factored(const BReq &R, int tx0, int ty0, const Rows<Tin> &S,
 {
     constexpr int TX = kFTX, TY = kFTY, NB = 8;
     const int kx = R.kx, ky = R.ky, rows = TY + ky - 1;
-    const int tid = threadIdx.x, nth = blockDim.x;
+    const int tid = ct_id(), nth = ct_n();
     float acc[NB];
     // x pass over all rows (the y halo) -> I
     for (int it = tid; it < rows * (TX / NB); it += nth) {
@@ -302,7 +310,7 @@ __device__ void bt_factored(const BReq &R, int tx0, int ty0, const Rows<Tin> &S,
 #pragma unroll
         for (int i = 0; i < NB; ++i) I[r * kIPitch + c0 + i] = acc[i];
     }
-    __syncthreads();
+    ct_sync();
     // y pass down each column
     const OutTile<Tout> O(R, R.out0, tx0, ty0, TX, TY);
     for (int it = tid; it < TX * (TY / NB); it += nth) {
@@ -318,7 +326,7 @@ template <class Tin, class Tout>
 __device__ void bt_gradients(const BReq &R, int tx0, int ty0, const Rows<Tin> &S)
 {
     constexpr int TX = kGTX, TY = kGTY, NB = 8;
-    const int tid = threadIdx.x, nth = blockDim.x;
+    const int tid = ct_id(), nth = ct_n();
     const float d0 = R.wx[0], d1 = R.wx[1], d2 = R.wx[2];
     const float s0 = R.wy[0], s1 = R.wy[1], s2 = R.wy[2];
     const OutTile<Tout> O0(R, R.out0, tx0, ty0, TX, TY), O1(R, R.out1, tx0, ty0, TX, TY);
@@ -349,7 +357,7 @@ template <class Tin, class Tout>
 __device__ void bt_laplacian(const BReq &R, int tx0, int ty0, const Rows<Tin> &S)
 {
     constexpr int TX = kGTX, TY = kGTY, NB = 8;
-    const int tid = threadIdx.x, nth = blockDim.x;
+    const int tid = ct_id(), nth = ct_n();
     const OutTile<Tout> O(R, R.out0, tx0, ty0, TX, TY);
     for (int it = tid; it < TX * (TY / NB); it += nth) {
         const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
@@ -392,9 +400,9 @@ template <int W, class Tout>
 __device__ void bt_median_u8(const BReq &R, int tx0, int ty0, const Rows<uint8_t> &S)
 {
     constexpr int h = W / 2;
-    const int tid = threadIdx.x;
+    const int tid = ct_id();
     const OutTile<Tout> O(R, R.out0, tx0, ty0, kMUX, kMUY);
-    for (int step = tid >> 5; step < kMUY * (kMUX / 128); step += blockDim.x >> 5) {
+    for (int step = tid >> 5; step < kMUY * (kMUX / 128); step += ct_n() >> 5) {
         const int ly = step % kMUY, lx = (step / kMUY) * 128 + (tid & 31) * 4;
         const int x0 = tx0 + lx, y = ty0 + ly;
         if (x0 >= R.nx || y >= R.ny) continue;
@@ -438,13 +446,13 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Rows<float>
     using SK = SortKey<float>;
     constexpr int h = W / 2, N = W * W;
     // staged values -> order-preserving keys, in place, once per element
-    for (int e = threadIdx.x; e < (kMFY + W - 1) * (kMFX + W - 1); e += blockDim.x) {
+    for (int e = ct_id(); e < (kMFY + W - 1) * (kMFX + W - 1); e += ct_n()) {
         const int r = e / (kMFX + W - 1), c = e - r * (kMFX + W - 1);
         float *q = const_cast<float *>(S.row(r)) + c;
         *reinterpret_cast<uint32_t *>(q) = SK::key(*q);
     }
-    __syncthreads();
-    for (int p = threadIdx.x; p < kMFX * kMFY; p += blockDim.x) {
+    ct_sync();
+    for (int p = ct_id(); p < kMFX * kMFY; p += ct_n()) {
         const int lx = p % kMFX, ly = p / kMFX, x = tx0 + lx, y = ty0 + ly;
         if (x >= R.nx || y >= R.ny) continue;
         const bool edge = R.style == IFX_CIRCULAR && (x < h || x >= R.nx - h || y < h || y >= R.ny - h);
@@ -489,47 +497,56 @@ __device__ __forceinline__ void bt_dispatch(const BReq &R, int tx0, int ty0, con
 
 // ---------------------------------------------------------------- the kernel
 constexpr int kReqTable = 1024;      // requests whose first tiles are searched in shared memory
+// Pipeline shape: kBatchBufs staging buffers per CTA, so the windows of the
+// next kBatchBufs-1 tiles are in flight while a tile computes; kBatchThreads
+// threads (one producer warp, the rest consumers), kBatchCtas CTAs per SM
+// (registers and shared memory allow it).
+constexpr int kBatchBufs = 2, kBatchThreads = 288, kBatchCtas = 3;
 
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(kBatchThreads, kBatchCtas)
 k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int *err)
 {
+    constexpr int NB = kBatchBufs;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ long long s_tile[2];
+    __shared__ long long s_tile[NB];
     __shared__ int s_base[kReqTable];
-    __shared__ __align__(16) BReq s_req[2];
-    __shared__ __align__(8) uint64_t s_bar[2];
-    __shared__ unsigned char s_lead[2][kStageRows];
+    __shared__ __align__(16) BReq s_req[NB];
+    __shared__ __align__(8) uint64_t s_bar[NB];
+    __shared__ unsigned char s_lead[NB][kStageRows];
     const BHdr *hdr = reinterpret_cast<const BHdr *>(desc);
     const BReq *reqs = reinterpret_cast<const BReq *>(desc + sizeof(BHdr));
     const long long total = hdr->total_tiles;
     const int nreq = hdr->nreq;
     const int ntab = nreq < kReqTable ? nreq : kReqTable;
     const int tid = threadIdx.x, warp = tid >> 5;
-    float *I = reinterpret_cast<float *>(smem + 2 * kStageBytes);
+    float *I = reinterpret_cast<float *>(smem + NB * kStageBytes);
     for (int i = tid; i < ntab; i += blockDim.x) s_base[i] = (int)reqs[i].tile_base;
     s_n0f8[tid & 255] = __fdiv_rn((float)(tid & 255), 255.0f);
     s_u8f[tid & 255] = (float)(tid & 255);
-    long long ahead = 0;                 // thread 0: the tile after the next one
+    __shared__ int s_bulk[NB];           // buffer b's window arrives by bulk copies
+    long long ahead = 0;                 // thread 0: the next tile to hand out (already fetched)
     if (tid == 0) {
-        mbar_init(&s_bar[0], 1);
-        mbar_init(&s_bar[1], 1);
+        for (int i = 0; i < NB; ++i) mbar_init(&s_bar[i], 1);
         mbar_fence_init();
-        s_tile[0] = (long long)atomicAdd(counter, 1ULL);
+        for (int i = 0; i < NB - 1; ++i) s_tile[i] = (long long)atomicAdd(counter, 1ULL);
         ahead = (long long)atomicAdd(counter, 1ULL);
     }
     __syncthreads();
 
-    uint32_t bulk = 0, parity = 0;       // per buffer: copies in flight / phase awaited
-    bool have_req[2] = {false, false};   // s_req[b] holds a descriptor
-    // Looks tile t up, stages its descriptor in s_req[b] and, for an interior
-    // window, issues its row copies into buffer b.  Called by all threads.
-    // Consecutive tiles mostly belong to one request: then the descriptor is
-    // copied from the other buffer instead of searched for and fetched.
-    auto prepare = [&](int b, long long t) {
-        if (t >= total) return;
+    // Warp 0 only: looks tile t up, stages its descriptor in s_req[b] and, for an
+    // interior window, issues its row copies into buffer b.  Consecutive tiles
+    // mostly belong to one request: then the descriptor is copied from the
+    // previously prepared buffer `pb` instead of searched for and fetched.  The
+    // other warps meet the result after the next block barrier.
+    auto prepare = [&](int b, long long t, int pb) {
+        const int lane = tid & 31;
+        if (t >= total) {
+            if (lane == 0) s_bulk[b] = 0;
+            return;
+        }
         const int *src;
-        if (have_req[b ^ 1] && t >= s_req[b ^ 1].tile_base && t < s_req[b ^ 1].tile_end) {
-            src = reinterpret_cast<const int *>(&s_req[b ^ 1]);
+        if (pb >= 0 && t >= s_req[pb].tile_base && t < s_req[pb].tile_end) {
+            src = reinterpret_cast<const int *>(&s_req[pb]);
         } else {
             int lo = 0, hi = ntab - 1;
             while (lo < hi) {
@@ -548,68 +565,82 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
             src = reinterpret_cast<const int *>(reqs + lo);
         }
         int *dst = reinterpret_cast<int *>(&s_req[b]);
-        for (int i = tid; i < (int)(sizeof(BReq) / 4); i += blockDim.x) dst[i] = src[i];
-        have_req[b] = true;
-        __syncthreads();
+        for (int i = lane; i < (int)(sizeof(BReq) / 4); i += 32) dst[i] = src[i];
+        __syncwarp();
         const BReq &R = s_req[b];
         const int local = (int)(t - R.tile_base);
         const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
         const TileGeo g = bt_geo(R, bx * bt_tile_w(R.op, R.in_type), by * bt_tile_h(R.op, R.in_type));
-        if (bt_bulk_ok(R, g)) {
-            if (warp == 0) bt_issue_rows(R, g, smem + b * kStageBytes, s_lead[b], &s_bar[b]);
-            bulk |= 1u << b;
-        }
+        const bool bulk = bt_bulk_ok(R, g);
+        if (bulk) bt_issue_rows(R, g, smem + b * kStageBytes, s_lead[b], &s_bar[b]);
+        if (lane == 0) s_bulk[b] = bulk;
     };
 
-    prepare(0, s_tile[0]);
+    if (warp == 0)
+        for (int i = 0; i < NB - 1; ++i) prepare(i, s_tile[i], i - 1);
+    __syncthreads();
+
+    uint32_t parity = 0;                 // per buffer: the phase awaited next
     for (int k = 0;; ++k) {
-        const int b = k & 1;
+        const int b = k % NB;
         const long long t = s_tile[b];
         if (t >= total) break;
-        if (tid == 0) {                        // the counter's latency hides behind a tile
-            s_tile[b ^ 1] = ahead;
-            ahead = (long long)atomicAdd(counter, 1ULL);
-        }
-        __syncthreads();
-        prepare(b ^ 1, s_tile[b ^ 1]);         // its copies land while this tile runs
-
-        const BReq &R = s_req[b];
-        const int local = (int)(t - R.tile_base);
-        const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
-        const int tx0 = bx * bt_tile_w(R.op, R.in_type), ty0 = by * bt_tile_h(R.op, R.in_type);
-        unsigned char *st = smem + b * kStageBytes;
-        if (bulk & (1u << b)) {
-            const bool ok = mbar_wait_bounded(&s_bar[b], (parity >> b) & 1u);
-            parity ^= 1u << b;
-            bulk &= ~(1u << b);
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) {
-                    atomicExch(err, 1);
-                    if (bulk & (2u >> b)) mbar_wait_bounded(&s_bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
-                }
-                return;
+        bool ok = true;
+        if (warp == 0) {
+            // producer: tile k + NB - 1 into the buffer tile k - 1 used, while the
+            // consumers run tile k
+            const int nb = (k + NB - 1) % NB;
+            long long tn = 0;
+            if (tid == 0) {                    // the counter's latency hides behind a tile
+                tn = ahead;
+                ahead = (long long)atomicAdd(counter, 1ULL);
+                s_tile[nb] = tn;               // read by every thread in iteration k + NB - 1
             }
+            tn = __shfl_sync(0xffffffffu, tn, 0);
+            prepare(nb, tn, (k + NB - 2) % NB);
         } else {
-            bt_gather_raw(R, bt_geo(R, tx0, ty0), st, s_lead[b]);
-            __syncthreads();
+            const BReq &R = s_req[b];
+            const int local = (int)(t - R.tile_base);
+            const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
+            const int tx0 = bx * bt_tile_w(R.op, R.in_type), ty0 = by * bt_tile_h(R.op, R.in_type);
+            unsigned char *st = smem + b * kStageBytes;
+            if (s_bulk[b]) {
+                ok = mbar_wait_bounded(&s_bar[b], (parity >> b) & 1u);
+            } else {
+                bt_gather_raw(R, bt_geo(R, tx0, ty0), st, s_lead[b]);
+                ct_sync();
+            }
+            if (ok) {
+                const bool o64 = R.out_type == IFX_F64;
+                if (R.in_type == IFX_F32) {
+                    const Rows<float> S(st, s_lead[b], nullptr);
+                    if (o64) bt_dispatch<float, double>(R, tx0, ty0, S, I);
+                    else bt_dispatch<float, float>(R, tx0, ty0, S, I);
+                } else {
+                    const Rows<uint8_t> S(st, s_lead[b], R.in_type == IFX_N0F8 ? s_n0f8 : s_u8f);
+                    if (o64) bt_dispatch<uint8_t, double>(R, tx0, ty0, S, I);
+                    else bt_dispatch<uint8_t, float>(R, tx0, ty0, S, I);
+                }
+            }
+            // buffer b is refilled by the bulk copies of a later tile
+            fence_proxy_async();
         }
-        const bool o64 = R.out_type == IFX_F64;
-        if (R.in_type == IFX_F32) {
-            const Rows<float> S(st, s_lead[b], nullptr);
-            if (o64) bt_dispatch<float, double>(R, tx0, ty0, S, I);
-            else bt_dispatch<float, float>(R, tx0, ty0, S, I);
-        } else {
-            const Rows<uint8_t> S(st, s_lead[b], R.in_type == IFX_N0F8 ? s_n0f8 : s_u8f);
-            if (o64) bt_dispatch<uint8_t, double>(R, tx0, ty0, S, I);
-            else bt_dispatch<uint8_t, float>(R, tx0, ty0, S, I);
+        if (s_bulk[b]) parity ^= 1u << b;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+                // copies still in flight: wait (bounded) for them; buffer b's phase
+                // was counted as consumed above
+                const uint32_t ph = s_bulk[b] ? parity ^ (1u << b) : parity;
+                for (int i = 0; i < NB; ++i)
+                    if (s_bulk[i]) mbar_wait_bounded(&s_bar[i], (ph >> i) & 1u);
+            }
+            return;
         }
-        // buffer b is refilled by the bulk copies of a later tile
-        fence_proxy_async();
-        __syncthreads();
     }
 }
 
-constexpr size_t kBatchSmem = 2 * (size_t)kStageBytes + (size_t)kStageRows * kIPitch * sizeof(float);
+constexpr size_t kBatchSmem = kBatchBufs * (size_t)kStageBytes + (size_t)kStageRows * kIPitch * sizeof(float);
 
 // ---------------------------------------------------------------- host side
 struct BatchSlot {
@@ -656,7 +687,7 @@ static cudaError_t slot_build(BatchEngine &E, BatchSlot &S, size_t cap)
     if ((e = cudaStreamBeginCapture(E.capture, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
     cudaMemcpyAsync(S.dev, S.host, cap, cudaMemcpyHostToDevice, E.capture);
     cudaMemsetAsync(S.counter, 0, sizeof(unsigned long long), E.capture);
-    k_batch<<<E.grid, 256, kBatchSmem, E.capture>>>(S.dev, S.counter, err);
+    k_batch<<<E.grid, kBatchThreads, kBatchSmem, E.capture>>>(S.dev, S.counter, err);
     if ((e = cudaStreamEndCapture(E.capture, &S.graph)) != cudaSuccess) return e;
     size_t n = 0;
     if ((e = cudaGraphGetNodes(S.graph, nullptr, &n)) != cudaSuccess) return e;
@@ -685,7 +716,7 @@ static cudaError_t engine_for(int device, BatchEngine **out)
                                              (int)kBatchSmem);
         if (e != cudaSuccess) return e;
         int per_sm = 0, sms = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, kBatchSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kBatchThreads, kBatchSmem);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
         E->grid = (per_sm > 0 ? per_sm : 1) * sms;
         if ((e = cudaStreamCreateWithFlags(&E->capture, cudaStreamNonBlocking)) != cudaSuccess) return e;
@@ -825,7 +856,7 @@ cudaError_t plan_create(int device, const BatchItem *items, int n, void **out)
         return e;
     }
     cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), E->capture);
-    k_batch<<<E->grid, 256, kBatchSmem, E->capture>>>(P->dev, P->counter, err);
+    k_batch<<<E->grid, kBatchThreads, kBatchSmem, E->capture>>>(P->dev, P->counter, err);
     if ((e = cudaStreamEndCapture(E->capture, &P->graph)) != cudaSuccess ||
         (e = cudaGraphInstantiate(&P->exec, P->graph, 0)) != cudaSuccess) {
         plan_destroy(P);
