@@ -93,8 +93,17 @@ class Clocks:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
+            # the sampler is live before the timed region starts: wait (up to 3 s) for
+            # its first line, then keep only the samples taken from here on
+            t_end = time.time() + 3.0
+            while time.time() < t_end and self.proc.poll() is None:
+                self.f.flush()
+                if os.path.getsize(self.path) > 0:
+                    break
+                time.sleep(0.01)
+            self.skip = len(open(self.path).read().strip().splitlines()) if os.path.getsize(self.path) else 0
         except Exception:
             self.proc = None
         return self
@@ -108,6 +117,7 @@ class Clocks:
     def summary(self):
         try:
             rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+            rows = rows[getattr(self, "skip", 0):] or rows
         except Exception:
             rows = []
         sm, reasons, mx = [], set(), None
