@@ -18,7 +18,8 @@ from ._abi import (ArgumentError, DimensionMismatch, ErrorException, CudaError, 
 from .arrays import DeviceArray, N0f8Array, n0f8
 from .blobs import BlobLoG, blob_LoG, findlocalmaxima, findlocalminima, multiLoG
 from .borders import Fill, Inner, NA, NoPad, Pad, borderinstance, padarray
-from .filtering import Algorithm, factorkernel, filter_type, imfilter, imfilter_, imgradients
+from .filtering import (Algorithm, autotune, autotune_choice, factorkernel, filter_type, imfilter, imfilter_,
+                        imgradients)
 from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD, TriggsSdika,
                       centered, iscopy, kernelfactors)
 from .rank import extrema, mapwindow, mapwindow_, maximum, median, median_, minimum
@@ -35,6 +36,6 @@ __all__ = [
     "Inner", "NA", "NoPad", "BlobLoG", "blob_LoG", "multiLoG", "findlocalmaxima", "findlocalminima", "Kernel", "KernelFactors", "centered", "kernelfactors", "Algorithm",
     "OffsetArray", "OffsetKernel", "ReshapedOneD", "LaplacianKernel", "TriggsSdika", "DeviceArray", "N0f8Array",
     "n0f8", "median", "median_", "extrema", "minimum", "maximum", "filter_type", "factorkernel",
-    "iscopy", "borderinstance", "ArgumentError", "DimensionMismatch", "ErrorException",
+    "iscopy", "borderinstance", "autotune", "autotune_choice", "ArgumentError", "DimensionMismatch", "ErrorException",
     "CudaError", "OutOfMemory", "Unsupported", "launch_count", "library_path",
 ]

@@ -97,7 +97,7 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_server_destroy", "ifx_noalloc_scratch_bytes", "ifx_imfilter_factored_noalloc",
            "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable",
            "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs", "ifx_imfilter_fft",
-           "ifx_imfilter_iir"]
+           "ifx_imfilter_iir", "ifx_autotune", "ifx_autotune_choice"]
 
 _lib = None
 _lock = threading.Lock()
@@ -155,6 +155,9 @@ def load(path: str = LIB_PATH):
         lib.ifx_findlocalextrema.argtypes = [vp, P(IfxArray), P(C.c_int32), P(C.c_int32), C.c_int32,
                                              P(C.c_int64), P(C.c_double), C.c_int64, P(C.c_int64), vp]
         lib.ifx_maxabs.argtypes = [vp, P(IfxArray), P(C.c_double), vp]
+        lib.ifx_autotune.argtypes = [vp, C.c_int32, C.c_char_p]
+        lib.ifx_autotune_choice.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int64,
+                                            C.c_int64, P(C.c_int32), P(C.c_int32), P(C.c_double)]
         lib.ifx_imfilter_iir.argtypes = [vp, P(IfxArray), P(IfxArray), C.c_int32, P(IfxIir), P(IfxBorder), vp]
         lib.ifx_imfilter_fft.argtypes = [vp, P(IfxArray), P(IfxArray), P(C.c_double), P(C.c_int64),
                                          P(C.c_int64), P(IfxBorder), vp]

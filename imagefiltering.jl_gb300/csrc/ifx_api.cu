@@ -17,7 +17,6 @@ namespace ifx {
 static std::atomic<uint64_t> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 
-size_t sep2d_smem_bytes(int kx, int ky, int x_first, int f64);
 size_t dense2d_smem_bytes(int kw, int kh, int f64);
 
 static thread_local std::string t_err;
@@ -452,7 +451,7 @@ static int run_cascade(Call &c, const ifx_array_t &imgd, const void *img, const 
             Sep2dArgs a{img, imgd.eltype, out, outd.eltype, n[0], nd > 1 ? n[1] : 1,
                         fx.first, fx.len, fy.first, fy.len, fx.w, fy.w, x_first,
                         border->style, fill, ct == IFX_F64};
-            IFX_CUDA(launch_sep2d(a, c.s));
+            IFX_CUDA(launch_sep2d_tuned(a, c.s, !c.host));
             return IFX_OK;
         }
     }
@@ -1200,6 +1199,37 @@ int ifx_batch_plan_destroy(ifx_batch_plan_t *plan)
     cudaSetDevice(plan->device);
     plan_destroy(plan->impl);
     delete plan;
+    return IFX_OK;
+}
+
+// ---------------------------------------------------------------- autotuner
+int ifx_autotune(ifx_context_t *ctx, int32_t enable, const char *cache_path)
+{
+    (void)ctx;
+    autotune_set(enable != 0, cache_path);
+    return IFX_OK;
+}
+
+int ifx_autotune_choice(ifx_context_t *ctx, int32_t in_type, int32_t out_type, int32_t kx, int32_t ky,
+                        int32_t fill, int64_t nx, int64_t ny, int32_t *x_first, int32_t *variant, double *ms)
+{
+    (void)ctx;
+    if (!x_first || !variant) return fail(IFX_ERR_ARGUMENT, "NULL output");
+    Sep2dArgs a{};
+    a.in_type = in_type;
+    a.out_type = out_type;
+    a.kx = kx;
+    a.ky = ky;
+    a.style = fill ? IFX_FILL : IFX_REPLICATE;
+    a.nx = (int)nx;
+    a.ny = (int)ny;
+    a.compute_f64 = in_type == IFX_F64;
+    int xf, var;
+    float t = 0.0f;
+    if (!autotune_lookup(a, &xf, &var, &t)) return fail(IFX_ERR_ARGUMENT, "no tuned choice for this key");
+    *x_first = xf;
+    *variant = var;
+    if (ms) *ms = t;
     return IFX_OK;
 }
 

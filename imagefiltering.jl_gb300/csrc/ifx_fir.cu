@@ -591,11 +591,33 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     return true;
 }
 
+// Whether the TMA tile kernel takes these arguments (the checks of
+// sep2d_tma_t, without a launch).
+template <class Tin> static bool sep2d_tma_fits(const Sep2dArgs &a)
+{
+    if (a.kx > kCorrKmax || a.ky > kCorrKmax) return false;
+    const int RV = kStTY + a.ky - 1;
+    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin));
+    if (L.boxw > 256 || RV > 256 || L.total > 160 * 1024) return false;
+    CUtensorMap map;
+    return tma_encode_2d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, (long long)a.nx * (long long)sizeof(Tin),
+                         L.boxw, RV);
+}
+
+bool sep2d_tma_applies(const Sep2dArgs &a)
+{
+    if (a.compute_f64 || a.nx == 0 || a.ny == 0) return false;
+    if (a.in_type == IFX_F32 && (a.out_type == IFX_F32 || a.out_type == IFX_F64)) return sep2d_tma_fits<float>(a);
+    if (is8(a.in_type) && (a.out_type == IFX_F32 || a.out_type == IFX_F64)) return sep2d_tma_fits<uint8_t>(a);
+    return false;
+}
+
 // true when the TMA kernel took the call (its launch status in *e); false
-// when it does not apply and k_sep2d runs instead.
+// when it does not apply (or variant 2 asks for the gather kernel) and
+// k_sep2d runs instead.
 static bool launch_sep2d_tma(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
 {
-    if (a.compute_f64) return false;
+    if (a.compute_f64 || a.variant == 2) return false;
     const int it = a.in_type, ot = a.out_type;
     if (it == IFX_F32 && ot == IFX_F32) return sep2d_tma_t<float, float>(a, s, e);
     if (it == IFX_F32 && ot == IFX_F64) return sep2d_tma_t<float, double>(a, s, e);

@@ -48,8 +48,15 @@ struct Sep2dArgs {
     int x_first;                           // pass order
     int style; double fill;                // fill in value domain
     int compute_f64;
+    int variant;                           // 0: automatic, 1: TMA tile kernel where it applies, 2: gather kernel
 };
 cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s);
+bool sep2d_tma_applies(const Sep2dArgs &a);
+size_t sep2d_smem_bytes(int kx, int ky, int x_first, int f64);
+// the autotuner of the fused 2-D separable path (ifx_tune.cu)
+cudaError_t launch_sep2d_tuned(Sep2dArgs a, cudaStream_t s, bool device_arrays);
+void autotune_set(bool enable, const char *path);
+bool autotune_lookup(const Sep2dArgs &a, int *x_first, int *variant, float *ms);
 
 // Fused 3-D separable kernel (factors on axes 0, 1, 2 in that order; FP32) ---
 struct Sep3dArgs {

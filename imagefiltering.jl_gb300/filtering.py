@@ -598,6 +598,32 @@ def _imfilter_fft(ctx, out, ao, img, ai, ks, b, nd):
     return out
 
 
+def autotune(enable=True, cache=None):
+    """Enable (or disable) the autotuner of the fused 2-D separable path: the
+    first device-array call per (eltypes, taps, Fill/Pad, size class) times the
+    tile kernels and pass orders and keeps the fastest; `cache` is a text file
+    the choices persist in (loaded now, appended as keys are tuned)."""
+    ctx = _ctx()
+    _abi.check(ctx.lib.ifx_autotune(ctx.handle, int(bool(enable)),
+                                    None if cache is None else str(cache).encode()))
+
+
+_KIND_CODE = {"F32": 0, "F64": 1, "N0F8": 2, "U8": 3}
+
+
+def autotune_choice(in_kind, out_kind, kx, ky, fill, shape):
+    """The cached choice for a key: (x_first, variant, ms) with variant 1 the
+    TMA tile kernel and 2 the gather kernel; None when the key is not tuned."""
+    ctx = _ctx()
+    xf, var, ms = C.c_int32(), C.c_int32(), C.c_double()
+    rc = ctx.lib.ifx_autotune_choice(ctx.handle, _KIND_CODE[in_kind], _KIND_CODE[out_kind], int(kx), int(ky),
+                                     int(bool(fill)), int(shape[0]), int(shape[1]) if len(shape) > 1 else 1,
+                                     C.byref(xf), C.byref(var), C.byref(ms))
+    if rc:
+        return None
+    return xf.value, var.value, ms.value
+
+
 def imgradients(img, kernelfun=None, border="replicate"):
     """imgradients(img, kernelfun=KernelFactors.ando3, border="replicate")
     (src/specialty.jl:39-53): one output per dimension."""
@@ -652,5 +678,6 @@ def imgradients(img, kernelfun=None, border="replicate"):
     return tuple(outs)
 
 
-__all__ = ["Algorithm", "imfilter", "imfilter_", "imgradients", "filter_type", "factorkernel",
+__all__ = ["Algorithm", "imfilter", "imfilter_", "imgradients", "filter_type", "factorkernel", "autotune",
+           "autotune_choice",
            "Kernel", "KernelFactors"]

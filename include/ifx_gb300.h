@@ -178,6 +178,25 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
                           const int64_t *wfirst, const int64_t *wlen,
                           const ifx_border_t *border, int32_t which, void *stream);
 
+/* ---- autotuner --------------------------------------------------------------
+ * The fused 2-D separable path (ifx_imfilter_factored with at most one factor
+ * per axis of a 1-D or 2-D image) chooses between two tile kernels (TMA-fed or
+ * gather-based) and the order of its two passes.  With the tuner enabled, the
+ * first device-array call per key (input and output eltypes, x and y taps,
+ * Fill or Pad, floor(log2(pixels)), FP64 arithmetic) times every applicable
+ * candidate on its stream and keeps the fastest; choices are cached in memory
+ * and, when cache_path is given, in that text file (loaded here, appended as
+ * keys are tuned).  Cached choices apply whether or not the tuner is enabled.
+ * The tuner and its cache are process-wide.  (No reference counterpart: the
+ * reference sizes its FIRTiled tiles by a fixed rule, TiledIteration's
+ * padded_tilesize, src/imfilter.jl:1200-1206, 1273-1278.) */
+int ifx_autotune(ifx_context_t *ctx, int32_t enable, const char *cache_path);
+/* The cached choice for a key: x_first (1: the x pass first), variant (1: TMA
+ * tile kernel, 2: gather kernel) and its time in ms; IFX_ERR_ARGUMENT when the
+ * key has not been tuned. */
+int ifx_autotune_choice(ifx_context_t *ctx, int32_t in_type, int32_t out_type, int32_t kx, int32_t ky,
+                        int32_t fill, int64_t nx, int64_t ny, int32_t *x_first, int32_t *variant, double *ms);
+
 /* ---- Algorithm.IIR(): Triggs-Sdika recursive filters ---------------------------
  * One factor per pass, a KernelFactors.TriggsSdika (src/kernelfactors.jl:
  * 462-505): forward coefficients a, backward coefficients b, the right-edge
