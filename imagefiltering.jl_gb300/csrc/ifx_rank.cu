@@ -391,6 +391,120 @@ __global__ void k_extrema_pass(const T *__restrict__ smin, const T *__restrict__
     }
 }
 
+// =========================================================================
+// The same pass for 8-bit codes by van Herk / Gil-Werman: the line is cut
+// into segments of the window length w, aligned so that the lowest index lo
+// of a window lies in segment k = floor(lo / w); the window [lo, lo+w-1] is
+// then the suffix of segment k from lo joined with the prefix of segment k+1
+// up to lo+w-1.  One thread per (line, segment): a backward sweep over
+// segment k leaves the suffix minima/maxima in shared memory (per-thread
+// columns, conflict-free), a forward sweep over segment k+1 keeps the running
+// prefix and writes the w outputs whose windows start in segment k -- two
+// loads per output and source whatever w.  Positions outside the line are the
+// identity (255 for min, 0 for max), which is the truncation; the window
+// always holds its centre (a0 <= 0 <= a1), so it is never empty.  8-bit codes
+// order totally, so the result equals the direct scan's exactly.
+// =========================================================================
+constexpr int kVhgwThreads = 128;
+
+__global__ void __launch_bounds__(kVhgwThreads)
+k_extrema_vhgw_u8(const uint8_t *__restrict__ smin, const uint8_t *__restrict__ smax,
+                  uint8_t *__restrict__ dmin, uint8_t *__restrict__ dmax, int4 n4, int axis, int a0, int w,
+                  int use_fill, uint8_t fill, int interleaved, int want_min, int want_max, long long kmin,
+                  long long nseg, long long nlines)
+{
+    extern __shared__ uint8_t vh[];                     // [w][threads] suffix min, then suffix max
+    const int n[4] = {n4.x, n4.y, n4.z, n4.w};
+    long long st = 1;
+    for (int d = 0; d < axis; ++d) st *= n[d];
+    const long long na = n[axis];
+    const int a1 = a0 + w - 1;
+    const int tid = threadIdx.x, bt = blockDim.x;
+    uint8_t *hmn = vh, *hmx = vh + (size_t)w * bt;
+    const bool same = smin == smax;
+    const long long items = nseg * nlines;
+    for (long long it = blockIdx.x * (long long)bt + tid; it < items; it += (long long)gridDim.x * bt) {
+        // axis 0: neighbouring threads take neighbouring segments of a line (their
+        // ranges are contiguous); other axes: neighbouring lines (coalesced)
+        long long line, sg;
+        if (axis == 0) {
+            line = it / nseg;
+            sg = it - line * nseg;
+        } else {
+            sg = it / nlines;
+            line = it - sg * nlines;
+        }
+        const long long o = line / st, p = line - o * st;
+        const long long base = o * st * na + p;
+        const long long seg_lo = (kmin + sg) * w;
+        uint8_t vmn = 255, vmx = 0;
+        for (int j = w - 1; j >= 0; --j) {             // suffix of segment k
+            const long long pos = seg_lo + j;
+            if (pos >= 0 && pos < na) {
+                const long long off = base + pos * st;
+                const uint8_t x = smin[off];
+                const uint8_t y = same ? x : smax[off];
+                vmn = x < vmn ? x : vmn;
+                vmx = y > vmx ? y : vmx;
+            }
+            hmn[j * bt + tid] = vmn;
+            hmx[j * bt + tid] = vmx;
+        }
+        uint8_t gmn = 255, gmx = 0;                     // running prefix of segment k+1
+        for (int j = 0; j < w; ++j) {
+            if (j > 0) {
+                const long long pos = seg_lo + w + j - 1;
+                if (pos >= 0 && pos < na) {
+                    const long long off = base + pos * st;
+                    const uint8_t x = smin[off];
+                    const uint8_t y = same ? x : smax[off];
+                    gmn = x < gmn ? x : gmn;
+                    gmx = y > gmx ? y : gmx;
+                }
+            }
+            const long long c = seg_lo + j - a0;        // the output whose window starts here
+            if (c < 0 || c >= na) continue;
+            uint8_t mn = hmn[j * bt + tid], mx = hmx[j * bt + tid];
+            mn = gmn < mn ? gmn : mn;
+            mx = gmx > mx ? gmx : mx;
+            if (use_fill && (c + a0 < 0 || c + a1 > na - 1)) {
+                mn = fill < mn ? fill : mn;
+                mx = fill > mx ? fill : mx;
+            }
+            const long long q = base + c * st;
+            if (interleaved) {
+                dmin[2 * q] = mn;
+                dmin[2 * q + 1] = mx;
+            } else {
+                if (want_min) dmin[q] = mn;
+                if (want_max) dmax[q] = mx;
+            }
+        }
+    }
+}
+
+static bool extrema_vhgw_u8(const ExtremaPassArgs &a, cudaStream_t s, cudaError_t *e)
+{
+    const int w = a.a1 - a.a0 + 1;
+    if (a.a0 > 0 || a.a1 < 0 || w < 2 || 2 * (size_t)w * kVhgwThreads > 48 * 1024) return false;
+    int4 n = make_int4(a.n[0], a.nd > 1 ? a.n[1] : 1, a.nd > 2 ? a.n[2] : 1, a.nd > 3 ? a.n[3] : 1);
+    const int nn[4] = {n.x, n.y, n.z, n.w};
+    const long long total = (long long)n.x * n.y * n.z * n.w, na = nn[a.axis];
+    const long long nlines = total / na;
+    // segments holding the lowest window index of some output: lo = c + a0, c in [0, na)
+    const long long kmin = (a.a0 - (w - 1)) / w;        // floor(a0 / w) for a0 in (-w, 0]
+    const long long kmax = (na - 1 + a.a0) / w;
+    const long long nseg = kmax - kmin + 1;
+    const long long items = nseg * nlines;
+    k_extrema_vhgw_u8<<<grid1(items, kVhgwThreads), kVhgwThreads, 2 * (size_t)w * kVhgwThreads, s>>>(
+        (const uint8_t *)a.src_min, (const uint8_t *)a.src_max, (uint8_t *)a.dst_min, (uint8_t *)a.dst_max, n,
+        a.axis, a.a0, w, a.use_fill, (uint8_t)a.fill, a.dst_interleaved, a.want_min, a.want_max, kmin, nseg,
+        nlines);
+    note_launch();
+    *e = cudaGetLastError();
+    return true;
+}
+
 template <class T>
 static cudaError_t extrema_t(const ExtremaPassArgs &a, cudaStream_t s)
 {
@@ -410,7 +524,11 @@ cudaError_t launch_extrema_pass(const ExtremaPassArgs &a, cudaStream_t s)
     if (total == 0) return cudaSuccess;
     if (a.type == IFX_F32) return extrema_t<float>(a, s);
     if (a.type == IFX_F64) return extrema_t<double>(a, s);
-    if (a.type == IFX_N0F8 || a.type == IFX_U8) return extrema_t<uint8_t>(a, s);
+    if (a.type == IFX_N0F8 || a.type == IFX_U8) {
+        cudaError_t e;
+        if (extrema_vhgw_u8(a, s, &e)) return e;
+        return extrema_t<uint8_t>(a, s);
+    }
     return cudaErrorInvalidValue;
 }
 
