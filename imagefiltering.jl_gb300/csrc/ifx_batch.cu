@@ -58,7 +58,7 @@ enum { BOP_FACTORED = 1, BOP_GRADIENTS = 2, BOP_LAPLACIAN = 3, BOP_MEDIAN = 4 };
 // tile shapes (outputs per tile); each input window (tile + halo) fits one
 // staging buffer of 64 rows x 400 bytes
 constexpr int kFTX = 64, kFTY = 32;        // factored (halo up to 32 x 32)
-constexpr int kGTX = 64, kGTY = 56;        // gradients / laplacian (halo 2 x 2)
+constexpr int kGTX = 88, kGTY = 56;        // gradients / laplacian (halo 2 x 2); (88 + 2) * 4 + 15 <= kStagePitch
 constexpr int kMUX = 256, kMUY = 56;       // 8-bit median (4 pixels per thread and step)
 constexpr int kMFX = 64, kMFY = 56;        // float median
 
@@ -127,6 +127,7 @@ constexpr int kStageRows = kFTY + 32;                  // factored with 33 taps
 constexpr int kStagePitch = 400;                       // >= 15 + (64 + 32) * 4, multiple of 16
 constexpr int kStageBytes = kStageRows * kStagePitch;
 constexpr int kIPitch = kFTX + 4;                      // factored intermediate (floats)
+static_assert((kGTX + 2) * 4 + 15 <= kStagePitch && kGTY + 2 <= kStageRows, "gradient tiles fit a stage");
 
 struct TileGeo {
     int ox, oy, rows, cols, elt;
