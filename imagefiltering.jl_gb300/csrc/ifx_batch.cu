@@ -67,10 +67,16 @@ __host__ __device__ inline int bt_tile_w(int op, int in_type)
     if (op == BOP_MEDIAN) return (in_type == IFX_F32) ? kMFX : kMUX;
     return op == BOP_FACTORED ? kFTX : kGTX;
 }
-__host__ __device__ inline int bt_tile_h(int op, int in_type)
+// Factored tiles are as tall as the staging rows allow for the y factor's
+// taps, rounded down to a multiple of 8: 32 rows for 33 taps, 48 for 17, 56
+// for 9 or 5, 64 for 1.
+__host__ __device__ inline int bt_fact_h(int ky) { return (kFTY + 32 - (ky - 1)) & ~7; }
+
+__host__ __device__ inline int bt_tile_h(int op, int in_type, int ky)
 {
+    if (op == BOP_FACTORED) return bt_fact_h(ky);
     if (op == BOP_MEDIAN) return (in_type == IFX_F32) ? kMFY : kMUY;
-    return op == BOP_FACTORED ? kFTY : kGTY;
+    return kGTY;
 }
 
 // Thread roles of k_batch: warp 0 is the producer (it looks tiles up and
@@ -137,7 +143,7 @@ __device__ __forceinline__ TileGeo bt_geo(const BReq &R, int tx0, int ty0)
 {
     const int elt = R.in_type == IFX_F32 ? 4 : 1;
     switch (R.op) {
-    case BOP_FACTORED: return {tx0 + R.fx, ty0 + R.fy, kFTY + R.ky - 1, kFTX + R.kx - 1, elt};
+    case BOP_FACTORED: return {tx0 + R.fx, ty0 + R.fy, bt_fact_h(R.ky) + R.ky - 1, kFTX + R.kx - 1, elt};
     case BOP_GRADIENTS:
     case BOP_LAPLACIAN: return {tx0 - 1, ty0 - 1, kGTY + 2, kGTX + 2, elt};
     default: {
@@ -299,8 +305,8 @@ __device__ __forceinline__ void corr_fn(F at, const float *w, int k, float *acc)
 template <class Tin, class Tout>
 __device__ void bt_factored(const BReq &R, int tx0, int ty0, const Rows<Tin> &S, float *I)
 {
-    constexpr int TX = kFTX, TY = kFTY, NB = 8;
-    const int kx = R.kx, ky = R.ky, rows = TY + ky - 1;
+    constexpr int TX = kFTX, NB = 8;
+    const int kx = R.kx, ky = R.ky, TY = bt_fact_h(ky), rows = TY + ky - 1;
     const int tid = ct_id(), nth = ct_n();
     float acc[NB];
     // x pass over all rows (the y halo) -> I
@@ -571,7 +577,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
         const BReq &R = s_req[b];
         const int local = (int)(t - R.tile_base);
         const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
-        const TileGeo g = bt_geo(R, bx * bt_tile_w(R.op, R.in_type), by * bt_tile_h(R.op, R.in_type));
+        const TileGeo g = bt_geo(R, bx * bt_tile_w(R.op, R.in_type), by * bt_tile_h(R.op, R.in_type, R.ky));
         const bool bulk = bt_bulk_ok(R, g);
         if (bulk) bt_issue_rows(R, g, smem + b * kStageBytes, s_lead[b], &s_bar[b]);
         if (lane == 0) s_bulk[b] = bulk;
@@ -603,7 +609,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
             const BReq &R = s_req[b];
             const int local = (int)(t - R.tile_base);
             const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
-            const int tx0 = bx * bt_tile_w(R.op, R.in_type), ty0 = by * bt_tile_h(R.op, R.in_type);
+            const int tx0 = bx * bt_tile_w(R.op, R.in_type), ty0 = by * bt_tile_h(R.op, R.in_type, R.ky);
             unsigned char *st = smem + b * kStageBytes;
             if (s_bulk[b]) {
                 ok = mbar_wait_bounded(&s_bar[b], (parity >> b) & 1u);
@@ -772,7 +778,7 @@ long long batch_describe(const BatchItem *items, int n, std::vector<BReq> &out)
         R.fy = it.fy;
         for (int t = 0; t < it.kx && t < kBatchMaxTaps; ++t) R.wx[t] = (float)it.wx[t];
         for (int t = 0; t < it.ky && t < kBatchMaxTaps; ++t) R.wy[t] = (float)it.wy[t];
-        const int tw = bt_tile_w(R.op, R.in_type), th = bt_tile_h(R.op, R.in_type);
+        const int tw = bt_tile_w(R.op, R.in_type), th = bt_tile_h(R.op, R.in_type, R.ky);
         R.tiles_x = (R.nx + tw - 1) / tw;
         const long long tiles = (long long)R.tiles_x * ((R.ny + th - 1) / th);
         R.tile_base = base;
