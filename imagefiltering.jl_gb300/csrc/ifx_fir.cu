@@ -485,6 +485,8 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         if (sizeof(Tin) == 1) prefetch(tn);        // the codes are converted: raw is free
 
         const int tx0 = px - fx, ty0 = py - fy;
+        // interior output tiles store without bounds tests, by pointer steps
+        const bool full = tx0 >= 0 && tx0 + TX <= nx && ty0 + TY <= ny;
         float acc[NB];
         if (x_first) {
             // x pass over all RV rows -> I (pitch si)
@@ -506,7 +508,11 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
                 corr_col<NB>(I + (size_t)r0 * L.si + c, L.si, wy, ky, acc);
                 const int x = tx0 + c;
-                if (x >= 0 && x < nx) {
+                if (full) {
+                    Tout *o = out + (long long)(ty0 + r0) * nx + x;
+#pragma unroll
+                    for (int i = 0; i < NB; ++i, o += nx) *o = out_cvt<Tout>(acc[i]);
+                } else if (x >= 0 && x < nx) {
 #pragma unroll
                     for (int i = 0; i < NB; ++i) {
                         const int y = ty0 + r0 + i;
@@ -531,7 +537,11 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 row_item(it, r, c0);
                 corr_row4<NB>(I + (size_t)r * L.si + c0, wx, kx, acc);
                 const int y = ty0 + r;
-                if (y < ny) {
+                if (full) {
+                    Tout *o = out + (long long)y * nx + tx0 + c0;
+#pragma unroll
+                    for (int i = 0; i < NB; ++i) o[i] = out_cvt<Tout>(acc[i]);
+                } else if (y < ny) {
 #pragma unroll
                     for (int i = 0; i < NB; ++i) {
                         const int x = tx0 + c0 + i;
