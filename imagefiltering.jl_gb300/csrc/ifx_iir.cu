@@ -513,12 +513,11 @@ template <class Tin, class S, class C> static cudaError_t iir_run(const IirArgs 
             const long long warps = (a.lines + 31) / 32;
             const int wpb = warps < 4LL * 152 ? 1 : 2;
             const size_t smem = wpb * iir_row_smem_per_warp<Tin, S>();
-            static bool attr = false;                     // the opt-in above 48 KB, once per instantiation
-            if (!attr) {
-                cudaFuncSetAttribute(k_iir_rows_async<Tin, S, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(2 * iir_row_smem_per_warp<Tin, S>()));
-                attr = true;
-            }
+            // the opt-in above 48 KB, once per instantiation (thread-safe static initialisation)
+            static const cudaError_t attr = cudaFuncSetAttribute(
+                k_iir_rows_async<Tin, S, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                (int)(2 * iir_row_smem_per_warp<Tin, S>()));
+            if (attr != cudaSuccess) return attr;
             k_iir_rows_async<Tin, S, C><<<(unsigned)((warps + wpb - 1) / wpb), 32 * wpb, smem, s>>>(a);
         } else {
             const int tpb = a.lines < 128LL * 152 ? 32 : 128;
