@@ -95,21 +95,18 @@ __global__ void k_fft_mulconj(C *a, const C *b, long long n)
     }
 }
 
-// out[i] = R0[i] * scale for the image's indices (R0 has the padded sizes)
+// out[i] = R0[i] * scale for the image's indices (R0 has the padded sizes):
+// one output row (axis 0) per block row, the row index split once per row
 template <class Tc, class Tout>
-__global__ void k_fft_crop(const Tc *R, Tout *out, int4 n, int4 P, long long total, Tc scale)
+__global__ void k_fft_crop(const Tc *R, Tout *out, int4 n, int4 P, long long rows, Tc scale)
 {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int na[4] = {n.x, n.y, n.z, n.w}, Pa[4] = {P.x, P.y, P.z, P.w};
-        long long rem = i, o = 0, st = 1;
-        for (int d = 0; d < 4; ++d) {
-            const long long c = rem % na[d];
-            rem /= na[d];
-            o += c * st;
-            st *= Pa[d];
-        }
-        out[i] = out_cvt<Tout>(R[o] * scale);
+    for (long long row = blockIdx.y * (long long)blockDim.y + threadIdx.y; row < rows;
+         row += (long long)gridDim.y * blockDim.y) {
+        const long long y = row % n.y, zw = row / n.y, z = zw % n.z, w = zw / n.z;
+        const Tc *src = R + ((w * P.z + z) * P.y + y) * (long long)P.x;
+        Tout *dst = out + row * (long long)n.x;
+        for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < n.x; x += gridDim.x * blockDim.x)
+            dst[x] = out_cvt<Tout>(src[x] * scale);
     }
 }
 
@@ -197,8 +194,14 @@ static int fft_run_t(const FftArgs &f, cudaStream_t s)
     else r = api.c2r(inv, (cufftComplex *)A, (cufftReal *)R);
     if (r != CUFFT_SUCCESS) return -1;
     int4 n4 = make_int4((int)f.n[0], (int)f.n[1], (int)f.n[2], (int)f.n[3]);
-    k_fft_crop<Tc, Tout><<<grid_of(f.total), 256, 0, s>>>(R, (Tout *)f.out, n4, P4, f.total,
-                                                           (Tc)(1.0 / (double)f.Ptotal));
+    {
+        const long long rows = f.total / f.n[0];
+        const dim3 blk(128, 2);
+        const unsigned gx = (unsigned)((f.n[0] + 127) / 128);
+        const long long gy = (rows + 1) / 2 < 65535 ? (rows + 1) / 2 : 65535;
+        k_fft_crop<Tc, Tout><<<dim3(gx, (unsigned)gy), blk, 0, s>>>(R, (Tout *)f.out, n4, P4, rows,
+                                                                    (Tc)(1.0 / (double)f.Ptotal));
+    }
     note_launch(4);
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }

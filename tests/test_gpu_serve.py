@@ -110,3 +110,33 @@ def test_server_bounded_wait_and_oversize(gpu_ifx):
         except TimeoutError:
             srv.wait(t, timeout=30)
         assert np.all(so[0] == 1.0)
+
+
+def test_server_concurrent_submitters(gpu_ifx):
+    """Four host threads submit and wait at once (the C calls release the
+    GIL): every result equals the single-request API, the ramp of batch sizes
+    after idle periods included."""
+    import threading
+    ifx = gpu_ifx
+    from imagefiltering_gb300.serve import Server
+    items = mixed_requests(ifx, seed=11, n=64)
+    outs = [host_outputs(ifx, img, op) for img, op, _ in items]
+    errors = []
+    with Server(hbm_cap_bytes=1 << 30, max_batch=8, max_inflight=3) as srv:
+        def worker(k):
+            try:
+                for i in range(k, len(items), 4):
+                    img, op, border = items[i]
+                    t = srv.submit(op, img, outs[i], border)
+                    srv.wait(t, timeout=60.0)
+            except Exception as e:            # reported on the main thread
+                errors.append(e)
+        threads = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        m = srv.metrics()
+    assert not errors, errors
+    assert m["completed"] >= len(items)
+    check_outputs(ifx, items, outs)
