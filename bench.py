@@ -187,7 +187,7 @@ def stream_calls(ifx, reqs, dev_inputs, out_arena, torch):
 
 # dram__bytes_read.sum + dram__bytes_write.sum over algorithmic bytes for one k_batch
 # launch on a 60-request wave of the same stream (206.356 + 884.533 MB / 1147.791 MB)
-K_BATCH_TRAFFIC_RATIO = (206.356224 + 884.532736) / 1147.791071
+K_BATCH_TRAFFIC_RATIO = (208.952320 + 885.413376) / 1147.791071
 
 
 def alg_bytes(r):
