@@ -138,4 +138,52 @@ template <int N> __device__ __forceinline__ uint32_t median_u8x4(const uint32_t 
     return __byte_perm(a[(N - 1) / 2], b[(N - 1) / 2], 0x6420);
 }
 
+// 3 x 3 medians of four horizontally adjacent windows, sharing the sorting of
+// their columns.  A[j] holds columns 0..3 of window row j, the low two bytes
+// of B[j] columns 4 and 5; output q's window is columns q..q+2.  Each column
+// of three is sorted once (in 16-bit lanes, two columns per word) and the
+// median of the nine is med3(max of the column minima, med3 of the column
+// middles, min of the column maxima) -- a min/max identity that holds for
+// all 0-1 inputs, hence for all inputs.  Columns 0..5 serve the four windows:
+// 3 x 3 compare-exchanges for the six columns plus 12 lane operations per
+// pair of outputs, against 24 compare-exchanges per pair in the pruned
+// nine-input network.
+__device__ __forceinline__ void cs_u16x2(uint32_t &a, uint32_t &b)
+{
+    const uint32_t lo = __vminu2(a, b);
+    b = __vmaxu2(a, b);
+    a = lo;
+}
+__device__ __forceinline__ uint32_t med3_u16x2(uint32_t a, uint32_t b, uint32_t c)
+{
+    return __vmaxu2(__vminu2(a, b), __vminu2(__vmaxu2(a, b), c));
+}
+__device__ __forceinline__ uint32_t median3x3_u8x4(const uint32_t (&A)[3], const uint32_t (&B)[3])
+{
+    uint32_t p[3][3];                            // [column pair 01, 23, 45][sorted rank]
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        p[0][j] = __byte_perm(A[j], 0u, 0x4140);
+        p[1][j] = __byte_perm(A[j], 0u, 0x4342);
+        p[2][j] = __byte_perm(B[j], 0u, 0x4140);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        cs_u16x2(p[k][0], p[k][1]);
+        cs_u16x2(p[k][1], p[k][2]);
+        cs_u16x2(p[k][0], p[k][1]);
+    }
+    // columns (c+1, c+2) from the pairs (c, c+1) and (c+2, c+3)
+    auto mid = [](uint32_t x, uint32_t y) { return __byte_perm(x, y, 0x5432); };
+    uint32_t r[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {                // outputs (0, 1), then (2, 3)
+        const uint32_t lo = __vmaxu2(__vmaxu2(p[h][0], mid(p[h][0], p[h + 1][0])), p[h + 1][0]);
+        const uint32_t hi = __vminu2(__vminu2(p[h][2], mid(p[h][2], p[h + 1][2])), p[h + 1][2]);
+        const uint32_t md = med3_u16x2(p[h][1], mid(p[h][1], p[h + 1][1]), p[h + 1][1]);
+        r[h] = med3_u16x2(lo, md, hi);
+    }
+    return __byte_perm(r[0], r[1], 0x6420);
+}
+
 } // namespace ifx
