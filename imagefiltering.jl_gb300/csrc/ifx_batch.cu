@@ -416,21 +416,25 @@ __device__ void bt_median_u8(const BReq &R, int tx0, int ty0, const Rows<uint8_t
         uint32_t w[W * W];
         const bool edge = R.style == IFX_CIRCULAR &&
                           (x0 < h || x0 + 3 >= R.nx - h || y < h || y >= R.ny - h);
-        if (W == 3 && !edge) {                       // shared column sorts
-            uint32_t A[3], B[3];
+        // 3 x 3: shared column sorts.  (The 5 x 5 form of the standalone kernel
+        // measured slower here: under this kernel's 72-register budget it spills.)
+        if constexpr (W == 3) {
+            if (!edge) {
+                uint32_t A[3], B[3];
 #pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const unsigned char *base = S.st + (ly + j) * kStagePitch;
-                const int l = S.lead[ly + j];
-                A[j] = load_word(base, l + lx);
-                B[j] = load_word(base, l + lx + 4);
+                for (int j = 0; j < 3; ++j) {
+                    const unsigned char *base = S.st + (ly + j) * kStagePitch;
+                    const int l = S.lead[ly + j];
+                    A[j] = load_word(base, l + lx);
+                    B[j] = load_word(base, l + lx + 4);
+                }
+                const uint32_t res = median3x3_u8x4(A, B);
+                float v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) v[q] = S.lut[(res >> (8 * q)) & 0xFF];
+                O.template row<4>(lx, ly, v);
+                continue;
             }
-            const uint32_t res = median3x3_u8x4(A, B);
-            float v[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) v[q] = S.lut[(res >> (8 * q)) & 0xFF];
-            O.template row<4>(lx, ly, v);
-            continue;
         }
         if (!edge) {
 #pragma unroll

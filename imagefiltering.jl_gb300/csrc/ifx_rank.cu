@@ -203,22 +203,23 @@ k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, in
         return wd;
     };
     uint32_t res = 0;
-    if constexpr (W0 == 3 && W1 == 3) {
+    if constexpr ((W0 == 3 && W1 == 3) || (W0 == 5 && W1 == 5)) {
         if (!edge) {                                   // shared column sorts
-            uint32_t A[3], B[3];
+            uint32_t A[W0], B[W0];
 #pragma unroll
-            for (int j = 0; j < 3; ++j) {
+            for (int j = 0; j < W0; ++j) {
                 A[j] = word(j, 0);
                 B[j] = load_word(tile + (size_t)(ly + j) * CT, lx + 4);
             }
-            res = median3x3_u8x4(A, B);
+            if constexpr (W0 == 3) res = median3x3_u8x4(A, B);
+            else res = median5x5_u8x4(A, B);
         } else {
-            uint32_t w[9];
+            uint32_t w[W0 * W1];
 #pragma unroll
-            for (int j = 0; j < 3; ++j)
+            for (int j = 0; j < W1; ++j)
 #pragma unroll
-                for (int i = 0; i < 3; ++i) w[j * 3 + i] = word(j, i);
-            res = median_u8x4<9>(w);
+                for (int i = 0; i < W0; ++i) w[j * W0 + i] = word(j, i);
+            res = median_u8x4<W0 * W1>(w);
         }
     } else if constexpr (W0 > 0 && W1 > 0) {
         // fixed window: byte-wise selection network (four windows per word)

@@ -186,4 +186,66 @@ __device__ __forceinline__ uint32_t median3x3_u8x4(const uint32_t (&A)[3], const
     return __byte_perm(r[0], r[1], 0x6420);
 }
 
+// 5 x 5 medians of four horizontally adjacent windows.  A[j] / B[j] hold
+// columns 0..3 / 4..7 of window row j; output q's window is columns q..q+4.
+// Every column's five values are sorted once (Batcher's network for five, in
+// 16-bit lanes, shared by the windows that contain the column); the median of
+// a window is then selected from its five sorted columns by a 63-comparator
+// network.  That network was derived offline for this purpose: sorting the
+// ranks across the columns and taking the median of the 13 elements of a
+// rows-and-columns-sorted 5 x 5 array that can hold rank 13 (those with
+// (c+1)(r+1) <= 13 and (5-c)(5-r) <= 13) is exact, and greedy removal of
+// comparators from that composite, checked after each removal against all
+// 6^5 column-sorted 0-1 inputs (0-1 principle), left these 63 (102 live
+// min/max operations against 202 for the pruned 25-input Batcher network).
+// Wire c*5 + r is column c, rank r (0 = smallest); the median is wire 12.
+struct Med25 {
+    static constexpr int n = 63;
+    static constexpr unsigned char a[63] = {0, 10, 0, 5, 5, 10, 15, 1, 1, 6, 1, 11, 6, 16, 2, 12, 2, 7, 7, 2, 12, 7, 17, 3, 13, 3, 8, 8, 3, 13, 8, 4, 14, 4, 9, 14, 9, 9, 15, 17, 3, 4, 9, 11, 4, 11, 4, 7, 8, 7, 8, 8, 11, 16, 20, 4, 8, 9, 11, 12, 8, 12, 11};
+    static constexpr unsigned char b[63] = {5, 15, 10, 15, 10, 20, 20, 6, 11, 16, 21, 21, 11, 21, 7, 17, 12, 17, 12, 22, 22, 12, 22, 8, 18, 13, 18, 13, 23, 23, 13, 9, 19, 14, 19, 24, 14, 11, 16, 20, 7, 8, 12, 13, 7, 12, 11, 12, 13, 9, 11, 9, 12, 17, 21, 16, 20, 15, 16, 17, 11, 15, 12};
+};
+
+template <int I> __device__ __forceinline__ void med25_cx(uint32_t (&v)[25])
+{
+    constexpr int x = Med25::a[I];
+    constexpr int y = Med25::b[I];
+    const uint32_t lo = __vminu2(v[x], v[y]);
+    const uint32_t hi = __vmaxu2(v[x], v[y]);
+    v[x] = lo;
+    v[y] = hi;
+}
+
+template <size_t... I> __device__ __forceinline__ void med25_apply(uint32_t (&v)[25], std::index_sequence<I...>)
+{
+    (med25_cx<(int)I>(v), ...);
+}
+
+__device__ __forceinline__ uint32_t median5x5_u8x4(const uint32_t (&A)[5], const uint32_t (&B)[5])
+{
+    uint32_t p[4][5];                            // [column pair 01, 23, 45, 67][sorted rank]
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        p[0][j] = __byte_perm(A[j], 0u, 0x4140);
+        p[1][j] = __byte_perm(A[j], 0u, 0x4342);
+        p[2][j] = __byte_perm(B[j], 0u, 0x4140);
+        p[3][j] = __byte_perm(B[j], 0u, 0x4342);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) net_apply_u16x2<5>(p[k], std::make_index_sequence<NetOf<5>::net.n>{});
+    auto mid = [](uint32_t x, uint32_t y) { return __byte_perm(x, y, 0x5432); };
+    uint32_t r[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {                // outputs (0, 1), then (2, 3)
+        uint32_t v[25];
+#pragma unroll
+        for (int i = 0; i < 5; ++i)              // window column slot i: columns (2h+i, 2h+i+1)
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                v[i * 5 + k] = (i & 1) ? mid(p[h + (i - 1) / 2][k], p[h + (i + 1) / 2][k]) : p[h + i / 2][k];
+        med25_apply(v, std::make_index_sequence<Med25::n>{});
+        r[h] = v[12];
+    }
+    return __byte_perm(r[0], r[1], 0x6420);
+}
+
 } // namespace ifx
