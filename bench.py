@@ -68,6 +68,22 @@ def dist_init():
     return rank, ws, dist
 
 
+def job_throughput(ms, pixels, dist=None, device="cpu"):
+    """Whole-job Mpixel/s over the ranks: the slowest rank's time (max) and the
+    pixels of all ranks (sum); (value, max_ms, total_pixels).  `dist` is the
+    initialised torch.distributed module (None for one process); the tensors
+    live on `device` ("cuda" under NCCL, "cpu" under gloo)."""
+    if dist is None:
+        return pixels / (ms / 1e3) / 1e6, ms, pixels
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([float(pixels)], dtype=torch.float64, device=device)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    ms_max, px = float(t.item()), float(n.item())
+    return px / (ms_max / 1e3) / 1e6, ms_max, px
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -411,6 +427,7 @@ def run_stream_e2e(args, ifx, torch, reqs_all):
         m = srv.metrics()
         px = sum(r.pixels for r in reqs)
         res["value"] = px / wall / 1e6
+        res["pixels"] = px
         res["throughput_p50_ms"] = m["p50_latency_s"] * 1e3
         res["throughput_p99_ms"] = m["p99_latency_s"] * 1e3
         res["hbm_peak_gb"] = m["hbm_peak"] / 2 ** 30
@@ -818,18 +835,14 @@ def main():
         print(json.dumps({"next_rows": run_next_rows(args, ifx, torch, peaks()[0])}))
         return 0
     res = run_stream(args, ifx, torch, rank)
-    dev_ms = res["dev_ms"]
-    if ws > 1:
-        t = torch.tensor([dev_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms = float(t.item())
-    pixels_all = res["pixels"] * ws
-    value = pixels_all / (dev_ms / 1e3) / 1e6
+    value, dev_ms, _ = job_throughput(res["dev_ms"], res["pixels"], dist if ws > 1 else None, "cuda")
     per_op = res["per_op"]
     bk_ms, bk_bytes, bk_n = res["batch_kernel"]
     achieved = bk_bytes / (bk_ms / 1e3) / 1e9
-    plain_value = res["pixels"] * ws / (res["plain_ms"] / 1e3) / 1e6
+    plain_value, _, _ = job_throughput(res["plain_ms"], res["pixels"], dist if ws > 1 else None, "cuda")
     e2e = run_stream_e2e(args, ifx, torch, res["reqs"])
+    if ws > 1:                                   # the served stream of every rank, slowest wall time
+        e2e["value"], _, _ = job_throughput(e2e["pixels"] / e2e["value"] / 1e3, e2e["pixels"], dist, "cuda")
     dense = run_dense4096(args, ifx, torch) if not args.no_dense else None
     sections = run_sections(args, ifx, torch, hbm_peak) if not args.no_dense else None
     nxt = run_next_rows(args, ifx, torch, hbm_peak) if not args.no_dense else None
