@@ -13,7 +13,7 @@ CUDA kernels of ``_build/libifx_gb300.so``; there is no CPU fallback, and the
 functions raise if the library is missing.
 """
 from . import _abi
-from ._abi import (ArgumentError, DimensionMismatch, ErrorException, CudaError, OutOfMemory,
+from ._abi import (ArgumentError, Cancelled, DimensionMismatch, ErrorException, CudaError, OutOfMemory,
                    Unsupported, launch_count)
 from .arrays import DeviceArray, N0f8Array, n0f8
 from .blobs import BlobLoG, blob_LoG, findlocalmaxima, findlocalminima, multiLoG
@@ -37,5 +37,5 @@ __all__ = [
     "OffsetArray", "OffsetKernel", "ReshapedOneD", "LaplacianKernel", "TriggsSdika", "DeviceArray", "N0f8Array",
     "n0f8", "median", "median_", "extrema", "minimum", "maximum", "filter_type", "factorkernel",
     "iscopy", "borderinstance", "autotune", "autotune_choice", "ArgumentError", "DimensionMismatch", "ErrorException",
-    "CudaError", "OutOfMemory", "Unsupported", "launch_count", "library_path",
+    "CudaError", "OutOfMemory", "Unsupported", "Cancelled", "launch_count", "library_path",
 ]

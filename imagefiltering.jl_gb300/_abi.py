@@ -45,8 +45,12 @@ class Unsupported(NotImplementedError):
     """A case the GB300 path does not implement (no CPU fallback exists)."""
 
 
+class Cancelled(RuntimeError):
+    """A served request cancelled before it ran."""
+
+
 _EXC = {1: ArgumentError, 2: DimensionMismatch, 3: ErrorException, 4: CudaError, 5: OutOfMemory,
-        6: TimeoutError, 7: Unsupported}
+        6: TimeoutError, 7: Unsupported, 8: Cancelled}
 
 
 class IfxArray(C.Structure):
@@ -97,7 +101,8 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_server_destroy", "ifx_noalloc_scratch_bytes", "ifx_imfilter_factored_noalloc",
            "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable",
            "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs", "ifx_imfilter_fft",
-           "ifx_imfilter_iir", "ifx_autotune", "ifx_autotune_choice"]
+           "ifx_imfilter_iir", "ifx_autotune", "ifx_autotune_choice", "ifx_server_cancel",
+           "ifx_server_inject_launch_error", "ifx_server_pause"]
 
 _lib = None
 _lock = threading.Lock()
@@ -143,6 +148,9 @@ def load(path: str = LIB_PATH):
         lib.ifx_server_submit.argtypes = [vp, P(IfxRequest), P(C.c_uint64)]
         lib.ifx_server_wait.argtypes = [vp, C.c_uint64, C.c_double, P(C.c_int32)]
         lib.ifx_server_drain.argtypes = [vp, C.c_double]
+        lib.ifx_server_cancel.argtypes = [vp, C.c_uint64]
+        lib.ifx_server_inject_launch_error.argtypes = [vp, C.c_int32]
+        lib.ifx_server_pause.argtypes = [vp, C.c_int32]
         lib.ifx_server_metrics.argtypes = [vp, P(IfxServerMetrics)]
         lib.ifx_server_reset_metrics.argtypes = [vp]
         lib.ifx_server_destroy.argtypes = [vp]

@@ -75,6 +75,8 @@ struct ifx_server {
     std::vector<double> latencies;
     uint64_t next_ticket = 1, submitted = 0, completed = 0, failed = 0, batches = 0;
     int ramp = 0;                          // batches launched since the engine was last idle
+    int inject_fail = 0;                   // launches still to report as failed (host-side injection)
+    bool paused = false;                   // admission goes on, no new batches launch
     long long pixels = 0;
     int64_t hbm_in_use = 0, hbm_peak = 0;
     bool have_first = false;
@@ -115,7 +117,7 @@ static void finish_batches(ifx_server *S)
             if (cudaEventQuery(b.compute_done) == cudaErrorNotReady) return;
             cudaStreamWaitEvent(S->down, b.compute_done, 0);
             for (auto &r : b.reqs)
-                for (int o = 0; o < nouts(r->q); ++o)
+                for (int o = 0; o < nouts(r->q) && r->status == IFX_OK; ++o)
                     if (r->host_out[o])
                         cudaMemcpyAsync(r->q.out[o].data, r->d_out[o], r->out_bytes[o],
                                         cudaMemcpyDeviceToHost, S->down);
@@ -132,6 +134,10 @@ static void finish_batches(ifx_server *S)
         for (auto &r : b.reqs) {
             r->done = true;
             S->hbm_in_use -= r->need;
+            if (r->status != IFX_OK) {            // a failed launch: no outputs, no latency sample
+                ++S->failed;
+                continue;
+            }
             S->latencies.push_back(std::chrono::duration<double>(now - r->t_submit).count());
             S->pixels += r->pixels;
             ++S->completed;
@@ -189,7 +195,7 @@ static void admit(ifx_server *S)
 // Launch one batch of staged requests (srv->mu held).
 static void launch(ifx_server *S)
 {
-    if (S->staged.empty() || (int)S->inflight.size() >= S->cfg.max_inflight) return;
+    if (S->paused || S->staged.empty() || (int)S->inflight.size() >= S->cfg.max_inflight) return;
     // Ramp: after an idle engine the first batches are 1/8, 1/4, 1/2 of max_batch, so
     // that the first results reach the download stream early (a served stream is
     // bound by the host link, and the link's download direction idles until then).
@@ -239,7 +245,13 @@ static void launch(ifx_server *S)
     cudaEventCreateWithFlags(&b.compute_done, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&b.copy_done, cudaEventDisableTiming);
     long long tiles = 0;
-    cudaError_t e = launch_batch(S->device, items.data(), (int)n, S->compute, &tiles);
+    cudaError_t e;
+    if (S->inject_fail > 0) {                     // injected on the host: the kernel never runs
+        --S->inject_fail;
+        e = cudaErrorLaunchFailure;
+    } else {
+        e = launch_batch(S->device, items.data(), (int)n, S->compute, &tiles);
+    }
     if (e != cudaSuccess) {
         S->engine_error = cudaGetErrorString(e);
         for (auto &r : b.reqs) r->status = IFX_ERR_CUDA;
@@ -364,6 +376,60 @@ int ifx_server_wait(ifx_server_t *S, uint64_t ticket, double timeout_s, int32_t 
     }
     if (status) *status = r->status;
     S->by_ticket.erase(ticket);
+    return IFX_OK;
+}
+
+int ifx_server_cancel(ifx_server_t *S, uint64_t ticket)
+{
+    if (!S) return IFX_ERR_ARGUMENT;
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->by_ticket.find(ticket);
+    if (it == S->by_ticket.end()) return set_error(IFX_ERR_ARGUMENT, "unknown ticket");
+    auto r = it->second;
+    if (r->done) return set_error(IFX_ERR_ARGUMENT, "the request is done");
+    auto drop = [&](auto &seq) {
+        for (auto q = seq.begin(); q != seq.end(); ++q)
+            if (q->get() == r.get()) {
+                seq.erase(q);
+                return true;
+            }
+        return false;
+    };
+    if (!drop(S->incoming) && !drop(S->queue)) {
+        if (!drop(S->staged)) return set_error(IFX_ERR_ARGUMENT, "the request is already in a launched batch");
+        // admitted: its device memory goes back once the copy stream has passed its uploads
+        if (r->host_in && r->d_in) cudaFreeAsync(r->d_in, S->copy);
+        for (int o = 0; o < 2; ++o)
+            if (r->host_out[o] && r->d_out[o]) cudaFreeAsync(r->d_out[o], S->copy);
+        if (r->staged_ev) {
+            cudaEventDestroy(r->staged_ev);
+            r->staged_ev = nullptr;
+        }
+        S->hbm_in_use -= r->need;
+    }
+    r->status = IFX_ERR_CANCELLED;
+    r->done = true;
+    ++S->failed;
+    S->cv_done.notify_all();
+    return IFX_OK;
+}
+
+int ifx_server_pause(ifx_server_t *S, int32_t paused)
+{
+    if (!S) return IFX_ERR_ARGUMENT;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->paused = paused != 0;
+    }
+    S->cv_work.notify_one();
+    return IFX_OK;
+}
+
+int ifx_server_inject_launch_error(ifx_server_t *S, int32_t count)
+{
+    if (!S || count < 0) return IFX_ERR_ARGUMENT;
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->inject_fail = count;
     return IFX_OK;
 }
 

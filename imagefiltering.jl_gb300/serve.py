@@ -50,6 +50,22 @@ class Server:
         if st.value:
             raise _abi._EXC.get(st.value, RuntimeError)("request %d failed (status %d)" % (ticket, st.value))
 
+    def cancel(self, ticket):
+        """Cancel a request that has not joined a launched batch (its wait then
+        raises Cancelled); ArgumentError when it is done or already running."""
+        _abi.check(self.ctx.lib.ifx_server_cancel(self.handle, C.c_uint64(ticket)))
+        self._pending.pop(ticket, None)
+
+    def pause(self, paused=True):
+        """Stop launching new batches (admission and uploads go on) or resume."""
+        _abi.check(self.ctx.lib.ifx_server_pause(self.handle, int(bool(paused))))
+
+    def inject_launch_error(self, count=1):
+        """Failure injection on the host, for tests: the next `count` batched
+        launches are reported as failed without running; their requests fail
+        with CudaError and the server keeps serving."""
+        _abi.check(self.ctx.lib.ifx_server_inject_launch_error(self.handle, int(count)))
+
     def drain(self, timeout=600.0):
         rc = self.ctx.lib.ifx_server_drain(self.handle, float(timeout))
         if rc == 6:

@@ -45,7 +45,8 @@ typedef enum {
     IFX_ERR_CUDA = 4,              /* a CUDA runtime call failed                        */
     IFX_ERR_NOMEM = 5,             /* device or host allocation failed / over the cap   */
     IFX_ERR_TIMEOUT = 6,           /* a bounded wait ran out                            */
-    IFX_ERR_UNSUPPORTED = 7        /* a case this path does not implement               */
+    IFX_ERR_UNSUPPORTED = 7,       /* a case this path does not implement               */
+    IFX_ERR_CANCELLED = 8          /* a served request cancelled before it ran          */
 } ifx_status;
 
 typedef enum {                     /* element types of arrays crossing the ABI          */
@@ -378,6 +379,18 @@ int ifx_server_submit(ifx_server_t *srv, const ifx_request_t *req, uint64_t *tic
  * the request's own status when it is. */
 int ifx_server_wait(ifx_server_t *srv, uint64_t ticket, double timeout_s, int32_t *status);
 int ifx_server_drain(ifx_server_t *srv, double timeout_s);
+/* Cancels a request that has not joined a launched batch: it completes with
+ * IFX_ERR_CANCELLED (counted as failed) and its device memory is released;
+ * IFX_ERR_ARGUMENT when the ticket is unknown, done or already launched. */
+int ifx_server_cancel(ifx_server_t *srv, uint64_t ticket);
+/* paused != 0: requests are still admitted (and uploaded) but no new batch
+ * launches until the server is resumed (paused = 0); batches already launched
+ * finish.  For maintenance windows and for tests that need requests to wait. */
+int ifx_server_pause(ifx_server_t *srv, int32_t paused);
+/* Failure injection on the host, for tests: the next `count` batched launches
+ * are reported as failed launches without running their kernel; their
+ * requests complete with IFX_ERR_CUDA and the server keeps serving. */
+int ifx_server_inject_launch_error(ifx_server_t *srv, int32_t count);
 int ifx_server_metrics(ifx_server_t *srv, ifx_server_metrics_t *m);
 int ifx_server_reset_metrics(ifx_server_t *srv);
 int ifx_server_destroy(ifx_server_t *srv);

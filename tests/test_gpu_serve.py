@@ -140,3 +140,63 @@ def test_server_concurrent_submitters(gpu_ifx):
     assert not errors, errors
     assert m["completed"] >= len(items)
     check_outputs(ifx, items, outs)
+
+
+def test_server_cancel_before_launch(gpu_ifx):
+    """Requests cancelled while queued or admitted complete as Cancelled and
+    give their device memory back; the others complete correctly."""
+    ifx = gpu_ifx
+    from imagefiltering_gb300.serve import Server
+    items = mixed_requests(ifx, seed=21, n=40)
+    outs = [host_outputs(ifx, img, op) for img, op, _ in items]
+    with Server(hbm_cap_bytes=1 << 30, max_batch=4, max_inflight=1) as srv:
+        srv.pause(True)                          # requests are admitted but wait for launch
+        tickets = [srv.submit(op, img, o, border) for (img, op, border), o in zip(items, outs)]
+        cancelled = set()
+        for i in range(30, 40):
+            srv.cancel(tickets[i])
+            cancelled.add(i)
+        srv.pause(False)
+        img0, op0, border0 = items[0]
+        done = srv.submit(op0, img0, host_outputs(ifx, img0, op0), border0)
+        srv.wait(done, timeout=60)
+        with pytest.raises(ifx.ArgumentError):  # waited for: unknown to the server now
+            srv.cancel(done)
+        for i, t in enumerate(tickets):
+            if i in cancelled:
+                with pytest.raises(ifx.Cancelled):
+                    srv.wait(t, timeout=60)
+            else:
+                srv.wait(t, timeout=60)
+        srv.drain()
+        m = srv.metrics()
+    assert len(cancelled) == 10
+    assert m["completed"] == len(items) + 1 - len(cancelled) and m["failed"] == len(cancelled)
+    assert m["hbm_in_use"] == 0
+    keep = [i for i in range(len(items)) if i not in cancelled]
+    check_outputs(ifx, [items[i] for i in keep], [outs[i] for i in keep])
+
+
+def test_server_injected_launch_failure(gpu_ifx):
+    """A batched launch reported failed (injected on the host, no GPU fault):
+    its requests fail with CudaError, their memory is released, and the
+    server goes on serving correct results."""
+    ifx = gpu_ifx
+    from imagefiltering_gb300.serve import Server
+    items = mixed_requests(ifx, seed=22, n=16)
+    outs = [host_outputs(ifx, img, op) for img, op, _ in items]
+    with Server(hbm_cap_bytes=1 << 30, max_batch=8, max_inflight=1) as srv:
+        srv.pause(True)                          # all eight join the one failing launch
+        srv.inject_launch_error(1)
+        first = [srv.submit(op, img, o, border) for (img, op, border), o in zip(items[:8], outs[:8])]
+        srv.pause(False)
+        for t in first:
+            with pytest.raises(ifx.CudaError):
+                srv.wait(t, timeout=60)
+        second = [srv.submit(op, img, o, border) for (img, op, border), o in zip(items[8:], outs[8:])]
+        for t in second:
+            srv.wait(t, timeout=60)
+        srv.drain()
+        m = srv.metrics()
+    assert m["failed"] == 8 and m["completed"] == 8 and m["hbm_in_use"] == 0
+    check_outputs(ifx, items[8:], outs[8:])
