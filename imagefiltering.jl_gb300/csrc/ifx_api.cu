@@ -627,6 +627,7 @@ uint64_t ifx_launch_count(void) { return g_launches.load(); }
 
 int ifx_create(ifx_context_t **ctx, int device)
 {
+    IFX_RANGE("ifx_abi_version");
     if (!ctx) return fail(IFX_ERR_ARGUMENT, "ctx is NULL");
     *ctx = nullptr;
     int ndev = 0;
@@ -646,6 +647,7 @@ int ifx_create(ifx_context_t **ctx, int device)
 
 int ifx_destroy(ifx_context_t *ctx)
 {
+    IFX_RANGE("ifx_destroy");
     if (!ctx) return IFX_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
@@ -658,6 +660,7 @@ int ifx_destroy(ifx_context_t *ctx)
 
 int ifx_synchronize(ifx_context_t *ctx, void *stream)
 {
+    IFX_RANGE("ifx_synchronize");
     if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
     IFX_CUDA(cudaSetDevice(ctx->device));
     IFX_CUDA(cudaStreamSynchronize(stream ? (cudaStream_t)stream : ctx->stream));
@@ -669,6 +672,7 @@ int ifx_synchronize(ifx_context_t *ctx, void *stream)
 int ifx_padarray(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
                  const ifx_border_t *border, void *stream)
 {
+    IFX_RANGE("ifx_padarray");
     int rc;
     if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
         return rc;
@@ -715,6 +719,7 @@ int ifx_imfilter_factored(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
                           int32_t nfactors, const ifx_factor_t *factors,
                           const ifx_border_t *border, void *stream)
 {
+    IFX_RANGE("ifx_imfilter_factored");
     std::vector<Fac> facs;
     double fill;
     bool nothing;
@@ -741,6 +746,7 @@ int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *
                        const double *kernel, const int64_t *ksize, const int64_t *kfirst,
                        const ifx_border_t *border, int32_t method, void *stream)
 {
+    IFX_RANGE("ifx_imfilter_dense");
     int rc;
     if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
         return rc;
@@ -854,6 +860,7 @@ int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *
 int ifx_imfilter_laplacian(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
                            const int32_t *flags, const ifx_border_t *border, void *stream)
 {
+    IFX_RANGE("ifx_imfilter_laplacian");
     int rc;
     if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
         return rc;
@@ -905,6 +912,7 @@ int ifx_imgradients(ifx_context_t *ctx, ifx_array_t *outs, const ifx_array_t *im
                     const double *deriv, const double *smooth, int32_t length, int64_t first,
                     const int32_t *extended, const ifx_border_t *border, void *stream)
 {
+    IFX_RANGE("ifx_imgradients");
     int rc;
     if ((rc = check_array(img, "img")) || (rc = check_border(border))) return rc;
     if (!outs || !deriv || !smooth || !extended) return fail(IFX_ERR_ARGUMENT, "NULL argument");
@@ -1007,6 +1015,7 @@ int ifx_mapwindow_median(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t
                          const int64_t *wfirst, const int64_t *wlen, const ifx_border_t *border,
                          void *stream)
 {
+    IFX_RANGE("ifx_mapwindow_median");
     int rc;
     if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
         return rc;
@@ -1060,6 +1069,7 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
                           const int64_t *wfirst, const int64_t *wlen, const ifx_border_t *border,
                           int32_t which, void *stream)
 {
+    IFX_RANGE("ifx_mapwindow_extrema");
     int rc;
     if ((rc = check_array(img, "img")) || (rc = check_array(out, "out"))) return rc;
     if (border && (rc = check_border(border))) return rc;
@@ -1141,6 +1151,7 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
 int ifx_batch_run(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n, int64_t *tiles,
                   void *stream)
 {
+    IFX_RANGE("ifx_batch_run");
     if (n < 0 || (n > 0 && !reqs)) return fail(IFX_ERR_ARGUMENT, "bad request list");
     if (tiles) *tiles = 0;
     std::vector<BatchItem> items((size_t)n);
@@ -1166,6 +1177,7 @@ struct ifx_batch_plan {
 int ifx_batch_plan_create(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t n,
                           ifx_batch_plan_t **plan)
 {
+    IFX_RANGE("ifx_batch_plan_create");
     if (!plan) return fail(IFX_ERR_ARGUMENT, "plan is NULL");
     *plan = nullptr;
     if (n < 0 || (n > 0 && !reqs)) return fail(IFX_ERR_ARGUMENT, "bad request list");
@@ -1186,6 +1198,7 @@ int ifx_batch_plan_create(ifx_context_t *ctx, const ifx_request_t *reqs, int32_t
 
 int ifx_batch_plan_launch(ifx_batch_plan_t *plan, int64_t *tiles, void *stream)
 {
+    IFX_RANGE("ifx_batch_plan_launch");
     if (!plan) return fail(IFX_ERR_ARGUMENT, "plan is NULL");
     long long t = 0;
     IFX_CUDA(plan_launch(plan->impl, (cudaStream_t)stream, &t));
@@ -1195,6 +1208,7 @@ int ifx_batch_plan_launch(ifx_batch_plan_t *plan, int64_t *tiles, void *stream)
 
 int ifx_batch_plan_destroy(ifx_batch_plan_t *plan)
 {
+    IFX_RANGE("ifx_batch_plan_destroy");
     if (!plan) return IFX_OK;
     cudaSetDevice(plan->device);
     plan_destroy(plan->impl);
@@ -1205,6 +1219,7 @@ int ifx_batch_plan_destroy(ifx_batch_plan_t *plan)
 // ---------------------------------------------------------------- autotuner
 int ifx_autotune(ifx_context_t *ctx, int32_t enable, const char *cache_path)
 {
+    IFX_RANGE("ifx_autotune");
     (void)ctx;
     autotune_set(enable != 0, cache_path);
     return IFX_OK;
@@ -1213,6 +1228,7 @@ int ifx_autotune(ifx_context_t *ctx, int32_t enable, const char *cache_path)
 int ifx_autotune_choice(ifx_context_t *ctx, int32_t in_type, int32_t out_type, int32_t kx, int32_t ky,
                         int32_t fill, int64_t nx, int64_t ny, int32_t *x_first, int32_t *variant, double *ms)
 {
+    IFX_RANGE("ifx_autotune_choice");
     (void)ctx;
     if (!x_first || !variant) return fail(IFX_ERR_ARGUMENT, "NULL output");
     Sep2dArgs a{};
@@ -1237,6 +1253,7 @@ int ifx_autotune_choice(ifx_context_t *ctx, int32_t in_type, int32_t out_type, i
 int ifx_imfilter_iir(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, int32_t nfactors,
                      const ifx_iir_t *factors, const ifx_border_t *border, void *stream)
 {
+    IFX_RANGE("ifx_imfilter_iir");
     int rc;
     if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
         return rc;
@@ -1397,6 +1414,7 @@ static bool fft_cheaper(const ifx_array_t &img, const ifx_array_t &out, const in
 int ifx_imfilter_fft(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, const double *kernel,
                      const int64_t *ksize, const int64_t *kfirst, const ifx_border_t *border, void *stream)
 {
+    IFX_RANGE("ifx_imfilter_fft");
     int rc;
     if ((rc = check_array(img, "img")) || (rc = check_array(out, "out")) || (rc = check_border(border)))
         return rc;
@@ -1427,6 +1445,7 @@ int ifx_imfilter_factored_sum(ifx_context_t *ctx, ifx_array_t *out, const ifx_ar
                               int32_t nfactors, const ifx_factor_t *factors, double scale,
                               const ifx_border_t *border, void *stream)
 {
+    IFX_RANGE("ifx_imfilter_factored_sum");
     int rc;
     if (nterms < 1 || nfactors < 1 || !factors) return fail(IFX_ERR_ARGUMENT, "no terms");
     if ((rc = check_array(out, "out"))) return rc;
@@ -1469,6 +1488,7 @@ int ifx_findlocalextrema(ifx_context_t *ctx, const ifx_array_t *img, const int32
                          int32_t minima, int64_t *indices, double *values, int64_t capacity, int64_t *count,
                          void *stream)
 {
+    IFX_RANGE("ifx_findlocalextrema");
     int rc;
     if ((rc = check_array(img, "img"))) return rc;
     if (!window || !edges || !count || (capacity > 0 && (!indices || !values)))
@@ -1518,6 +1538,7 @@ int ifx_findlocalextrema(ifx_context_t *ctx, const ifx_array_t *img, const int32
 
 int ifx_maxabs(ifx_context_t *ctx, const ifx_array_t *img, double *result, void *stream)
 {
+    IFX_RANGE("ifx_maxabs");
     int rc;
     if ((rc = check_array(img, "img"))) return rc;
     if (!result) return fail(IFX_ERR_ARGUMENT, "result is NULL");
@@ -1547,6 +1568,7 @@ int ifx_maxabs(ifx_context_t *ctx, const ifx_array_t *img, double *result, void 
 int ifx_na_prepare(ifx_context_t *ctx, ifx_array_t *zeroed, ifx_array_t *valid, const ifx_array_t *img,
                    int32_t na, int32_t *has_na, void *stream)
 {
+    IFX_RANGE("ifx_na_prepare");
     int rc;
     if ((rc = check_array(img, "img")) || (rc = check_array(zeroed, "zeroed")) ||
         (rc = check_array(valid, "valid")))
@@ -1579,6 +1601,7 @@ int ifx_na_prepare(ifx_context_t *ctx, ifx_array_t *zeroed, ifx_array_t *valid, 
 
 int ifx_na_divide(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *den, void *stream)
 {
+    IFX_RANGE("ifx_na_divide");
     int rc;
     if ((rc = check_array(out, "out")) || (rc = check_array(den, "den")) || (rc = check_same_axes(*out, *den)))
         return rc;
@@ -1599,6 +1622,7 @@ int ifx_na_divide(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *den, 
 
 int ifx_na_normalize_separable(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *sums, void *stream)
 {
+    IFX_RANGE("ifx_na_normalize_separable");
     int rc;
     if ((rc = check_array(out, "out"))) return rc;
     if (!sums) return fail(IFX_ERR_ARGUMENT, "sums is NULL");

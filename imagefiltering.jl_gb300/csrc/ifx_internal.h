@@ -6,7 +6,18 @@
 #include <vector>
 #include "ifx_common.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace ifx {
+
+// NVTX range around a public entry point (a no-op unless a profiler attaches)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+#define IFX_RANGE(name) ::ifx::NvtxRange ifx_nvtx_range_(name)
 
 constexpr int kMaxDenseTaps = 3600;      // dense kernels passed by value (60x60)
 

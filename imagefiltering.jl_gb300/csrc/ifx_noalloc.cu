@@ -74,6 +74,7 @@ int ifx_imfilter_factored_noalloc(ifx_array_t *out, const ifx_array_t *img, int3
                                   const ifx_factor_t *factors, const ifx_border_t *border,
                                   void *stream)
 {
+    IFX_RANGE("ifx_imfilter_factored_noalloc");
     std::vector<Fac> facs;
     double fill;
     bool nothing;

@@ -196,6 +196,7 @@ static void admit(ifx_server *S)
 static void launch(ifx_server *S)
 {
     if (S->paused || S->staged.empty() || (int)S->inflight.size() >= S->cfg.max_inflight) return;
+    IFX_RANGE("ifx_server_launch_batch");
     // Ramp: after an idle engine the first batches are 1/8, 1/4, 1/2 of max_batch, so
     // that the first results reach the download stream early (a served stream is
     // bound by the host link, and the link's download direction idles until then).
@@ -293,6 +294,7 @@ extern "C" {
 
 int ifx_server_create(ifx_context_t *ctx, const ifx_server_config_t *cfg, ifx_server_t **out)
 {
+    IFX_RANGE("ifx_server_create");
     if (!ctx || !cfg || !out) return set_error(IFX_ERR_ARGUMENT, "NULL argument");
     if (cfg->hbm_cap_bytes <= 0 || cfg->max_batch < 1 || cfg->max_inflight < 1)
         return set_error(IFX_ERR_ARGUMENT, "server config: cap, max_batch and max_inflight must be positive");
@@ -318,6 +320,7 @@ int ifx_server_create(ifx_context_t *ctx, const ifx_server_config_t *cfg, ifx_se
 
 int ifx_server_submit(ifx_server_t *S, const ifx_request_t *q, uint64_t *ticket)
 {
+    IFX_RANGE("ifx_server_submit");
     if (!S || !q || !ticket) return IFX_ERR_ARGUMENT;
     // validate exactly as a batch would, then keep an owned copy
     BatchItem it;
@@ -363,6 +366,7 @@ int ifx_server_submit(ifx_server_t *S, const ifx_request_t *q, uint64_t *ticket)
 
 int ifx_server_wait(ifx_server_t *S, uint64_t ticket, double timeout_s, int32_t *status)
 {
+    IFX_RANGE("ifx_server_wait");
     if (!S) return IFX_ERR_ARGUMENT;
     std::unique_lock<std::mutex> lk(S->mu);
     auto it = S->by_ticket.find(ticket);
@@ -381,6 +385,7 @@ int ifx_server_wait(ifx_server_t *S, uint64_t ticket, double timeout_s, int32_t 
 
 int ifx_server_cancel(ifx_server_t *S, uint64_t ticket)
 {
+    IFX_RANGE("ifx_server_cancel");
     if (!S) return IFX_ERR_ARGUMENT;
     std::lock_guard<std::mutex> lk(S->mu);
     auto it = S->by_ticket.find(ticket);
@@ -416,6 +421,7 @@ int ifx_server_cancel(ifx_server_t *S, uint64_t ticket)
 
 int ifx_server_pause(ifx_server_t *S, int32_t paused)
 {
+    IFX_RANGE("ifx_server_pause");
     if (!S) return IFX_ERR_ARGUMENT;
     {
         std::lock_guard<std::mutex> lk(S->mu);
@@ -427,6 +433,7 @@ int ifx_server_pause(ifx_server_t *S, int32_t paused)
 
 int ifx_server_inject_launch_error(ifx_server_t *S, int32_t count)
 {
+    IFX_RANGE("ifx_server_inject_launch_error");
     if (!S || count < 0) return IFX_ERR_ARGUMENT;
     std::lock_guard<std::mutex> lk(S->mu);
     S->inject_fail = count;
@@ -435,6 +442,7 @@ int ifx_server_inject_launch_error(ifx_server_t *S, int32_t count)
 
 int ifx_server_drain(ifx_server_t *S, double timeout_s)
 {
+    IFX_RANGE("ifx_server_drain");
     if (!S) return IFX_ERR_ARGUMENT;
     std::unique_lock<std::mutex> lk(S->mu);
     const auto until = Clock::now() + std::chrono::duration_cast<Clock::duration>(
@@ -449,6 +457,7 @@ int ifx_server_drain(ifx_server_t *S, double timeout_s)
 
 int ifx_server_metrics(ifx_server_t *S, ifx_server_metrics_t *m)
 {
+    IFX_RANGE("ifx_server_metrics");
     if (!S || !m) return IFX_ERR_ARGUMENT;
     std::lock_guard<std::mutex> lk(S->mu);
     memset(m, 0, sizeof *m);
@@ -475,6 +484,7 @@ int ifx_server_metrics(ifx_server_t *S, ifx_server_metrics_t *m)
 
 int ifx_server_reset_metrics(ifx_server_t *S)
 {
+    IFX_RANGE("ifx_server_reset_metrics");
     if (!S) return IFX_ERR_ARGUMENT;
     std::lock_guard<std::mutex> lk(S->mu);
     if (S->completed + S->failed != S->submitted) return IFX_ERR_ARGUMENT;
@@ -488,6 +498,7 @@ int ifx_server_reset_metrics(ifx_server_t *S)
 
 int ifx_server_destroy(ifx_server_t *S)
 {
+    IFX_RANGE("ifx_server_destroy");
     if (!S) return IFX_OK;
     ifx_server_drain(S, 60.0);
     S->stop.store(true);
