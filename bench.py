@@ -552,16 +552,21 @@ _FLUSH = []
 
 
 def _time(torch, fn, reps=5):
-    """Mean CUDA-event time of fn() over `reps` runs; L2 is flushed (a 256 MB
-    buffer is overwritten) before every timed run, outside the events."""
+    """Mean CUDA-event time of fn() over `reps` runs; L2 is flushed before
+    every timed run, outside the events: a 256 MB buffer is overwritten, then a
+    second 256 MB buffer is read, so that L2 holds clean lines of neither the
+    inputs nor the outputs and the timed kernels pay for no write-back of the
+    flush's own dirty lines."""
     if not _FLUSH:
         _FLUSH.append(torch.empty(256 << 20, dtype=torch.uint8, device="cuda"))
+        _FLUSH.append(torch.zeros(64 << 20, dtype=torch.float32, device="cuda"))
     for _ in range(2):
         fn()
     torch.cuda.synchronize()
     total = 0.0
     for _ in range(reps):
         _FLUSH[0].zero_()
+        _FLUSH[1].sum()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()

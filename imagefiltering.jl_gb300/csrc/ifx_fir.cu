@@ -323,20 +323,37 @@ static cudaError_t sep2d_t(const Sep2dArgs &a, cudaStream_t s)
 // Fused 2-D separable kernel, persistent and fed by the Tensor Memory
 // Accelerator (FP32 compute; Float32 or 8-bit images whose rows meet the copy
 // engine's 16-byte rules; factors of at most kCorrKmax taps).  Each CTA walks
-// tiles blockIdx.x, +gridDim.x, ...  The input buffer of a tile is free once
-// its first pass (or, for 8-bit codes, their conversion to values) has read
-// it: the bulk copy of the next tile (TX+kx-1 by TY+ky-1 inputs) is issued
-// then and lands while the second pass runs.  Tiles whose input window leaves
-// the image are gathered through the border map instead (same index
-// arithmetic as k_sep2d).
+// tiles blockIdx.x, +gridDim.x, ...  Two input buffers alternate: when a
+// tile starts, the bulk copy of the CTA's next tile (TX+kx-1 by TY+ky-1
+// inputs) is issued into the other buffer, so it lands while both passes of
+// this tile run.  Every tile arrives by the copy engine, whose cells outside
+// the image are zeros; for tiles whose window leaves the image those cells
+// then take the border's values in shared memory (rows, then columns, from
+// in-image cells of the tile, or of the image where the window does not hold
+// them), so only the halo strips cost index arithmetic.
 //
 // Shared-memory layout keeps the row passes free of bank conflicts: the tile
 // grid is shifted so that every window starts on a 16-byte boundary,
 // row pitches are 4 mod 8 floats, and each 8-lane phase of a warp reads 4 rows
-// x 2 window starts with 16-byte loads.  The passes are those of k_sep2d
-// (cascade order, pass ranges); outputs of FP32 results widen exactly.
+// x 2 window starts with 16-byte loads.  Both passes run on the packed FP32x2
+// pipe: the row pass on pairs of outputs, the column pass on pairs of
+// columns (whose outputs store as one 8- or 16-byte word).  The passes are
+// those of k_sep2d (cascade order, pass ranges); outputs of FP32 results
+// widen exactly.
 // =========================================================================
-constexpr int kStTX = 64, kStTY = 64, kStNB = 16;
+constexpr int kStTX = 64, kStTY = 64, kStNB = 16, kStNBY = 8;
+
+// Two adjacent outputs of an FP32 result (8-byte store for Float32, 16-byte
+// for Float64; the caller checks the alignment).
+template <class To> __device__ __forceinline__ void store_pair(To *o, float2 v);
+template <> __device__ __forceinline__ void store_pair<float>(float *o, float2 v)
+{
+    *reinterpret_cast<float2 *>(o) = v;
+}
+template <> __device__ __forceinline__ void store_pair<double>(double *o, float2 v)
+{
+    *reinterpret_cast<double2 *>(o) = make_double2(f32_to_f64(v.x), f32_to_f64(v.y));
+}
 
 __host__ __device__ inline size_t st_round128(size_t b) { return (b + 127) & ~(size_t)127; }
 // smallest pitch >= n floats that is 4 mod 8
@@ -358,10 +375,10 @@ __host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int x_first, 
     L.st = st_pitch(CV + 3);
     L.si = x_first ? st_pitch(kStTX) : st_pitch(CV + 3);
     L.raw = st_round128((size_t)L.boxw * RV * elt_bytes);
-    L.w = st_round128(2 * (IFX_MAX_TAPS + 3) * sizeof(float) + 256 * sizeof(float));
+    L.w = st_round128(2 * (IFX_MAX_TAPS + 3) * sizeof(float2) + 256 * sizeof(float));
     L.t = elt_bytes == 1 ? st_round128((size_t)RV * L.st * sizeof(float)) : 0;
     L.i = st_round128((size_t)(x_first ? RV : kStTY) * L.si * sizeof(float));
-    L.total = L.raw + L.w + L.t + L.i;
+    L.total = 2 * L.raw + L.w + L.t + L.i;       // two input buffers: the next tile loads during this one
     return L;
 }
 
@@ -369,29 +386,31 @@ template <class Tin, class Tout>
 __global__ void __launch_bounds__(256)
 k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img, Tout *__restrict__ out,
             int nx, int ny, int fx, int kx, int fy, int ky, int x_first, int style, float fill, bool norm,
-            int shift, int tiles_x, int tiles, int *err, const __grid_constant__ Sep2dW<float> W)
+            int shift, int tiles_x, int tiles, int pair_store, int *err, const __grid_constant__ Sep2dW<float> W)
 {
-    constexpr int TX = kStTX, TY = kStTY, NB = kStNB;
+    constexpr int TX = kStTX, TY = kStTY, NB = kStNB, NBY = kStNBY;
     constexpr int ALIGN = 16 / (int)sizeof(Tin);          // x granularity of a box start
     extern __shared__ __align__(128) unsigned char st_smem[];
-    __shared__ __align__(8) uint64_t bar;
+    __shared__ __align__(8) uint64_t bar[2];
     const int RV = TY + ky - 1, CV = TX + kx - 1;
     const SepTmaSmem L = sep_tma_smem(kx, ky, x_first, (int)sizeof(Tin));
     const int boxw = L.boxw;
-    Tin *raw = reinterpret_cast<Tin *>(st_smem);
-    float *wx = reinterpret_cast<float *>(st_smem + L.raw);
-    float *wy = wx + (IFX_MAX_TAPS + 3);
-    float *lut = wy + (IFX_MAX_TAPS + 3);                   // 8-bit code -> value
-    float *T = reinterpret_cast<float *>(st_smem + L.raw + L.w);
-    float *I = reinterpret_cast<float *>(st_smem + L.raw + L.w + L.t);
+    auto raw_buf = [&](int b) { return reinterpret_cast<Tin *>(st_smem + (size_t)b * L.raw); };
+    unsigned char *rest = st_smem + 2 * L.raw;
+    float2 *wx = reinterpret_cast<float2 *>(rest);   // (w, w) pairs
+    float2 *wy = wx + (IFX_MAX_TAPS + 3);
+    float *lut = reinterpret_cast<float *>(wy + (IFX_MAX_TAPS + 3));   // 8-bit code -> value
+    float *T = reinterpret_cast<float *>(rest + L.w);
+    float *I = reinterpret_cast<float *>(rest + L.w + L.t);
     const int tid = threadIdx.x, nth = blockDim.x;
     const uint32_t box_bytes = (uint32_t)(boxw * RV * (int)sizeof(Tin));
-    for (int t = tid; t < kx; t += nth) wx[t] = W.wx[t];
-    for (int t = tid; t < ky; t += nth) wy[t] = W.wy[t];
+    for (int t = tid; t < kx; t += nth) wx[t] = make_float2(W.wx[t], W.wx[t]);
+    for (int t = tid; t < ky; t += nth) wy[t] = make_float2(W.wy[t], W.wy[t]);
     if (sizeof(Tin) == 1)
         for (int c = tid; c < 256; c += nth) lut[c] = to_c<float>((uint8_t)c, norm);
     if (tid == 0) {
-        mbar_init(&bar, 1);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
         mbar_fence_init();
         tma_prefetch_map(&map);
     }
@@ -408,18 +427,20 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         origin(t, px, py);
         return px >= 0 && px + CV <= nx && py >= 0 && py + RV <= ny;
     };
-    // all threads call it (uniform); thread 0 issues the copy of tile t
-    uint32_t parity = 0;
-    bool pending = false;
-    auto prefetch = [&](int t) {
-        if (t < tiles && interior(t)) {
+    // all threads call it (uniform); thread 0 issues the copy of tile t into
+    // buffer b.  The buffer's previous readers finished before the block
+    // barrier that ended the previous tile (after a proxy fence).
+    uint32_t parity = 0;              // bit b: phase of bar[b] to wait for
+    uint32_t pending = 0;             // bit b: a copy into buffer b is in flight
+    auto prefetch = [&](int t, int b) {
+        if (t < tiles) {
             if (tid == 0) {
                 int px, py;
                 origin(t, px, py);
-                mbar_expect_tx(&bar, box_bytes);
-                tma_load_2d(raw, &map, px & ~(ALIGN - 1), py, &bar);
+                mbar_expect_tx(&bar[b], box_bytes);
+                tma_load_2d(raw_buf(b), &map, px & ~(ALIGN - 1), py, &bar[b]);
             }
-            pending = true;
+            pending |= 1u << b;
         }
     };
     // row-pass item -> (row, window start): a warp covers 16 rows x 2 starts and
@@ -431,121 +452,160 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     };
 
     int t = blockIdx.x;
-    prefetch(t);
-    for (; t < tiles; t += gridDim.x) {
-        const int tn = t + gridDim.x;
+    prefetch(t, 0);
+    for (int n = 0; t < tiles; t += gridDim.x, ++n) {
+        const int b = n & 1;
+        Tin *raw = raw_buf(b);
+        // the next tile loads into the other buffer while this one computes
+        prefetch(t + gridDim.x, b ^ 1);
         int px, py;
         origin(t, px, py);
-        const float *P;
+        // every tile arrives by the copy engine (cells outside the image as zeros)
+        const uint32_t ph = (parity >> b) & 1u;
+        const bool ok = mbar_wait_sleep(&bar[b], ph);
+        parity ^= 1u << b;
+        pending &= ~(1u << b);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+                // copies may still land: give them time before the block exits
+                mbar_wait_sleep(&bar[b], ph);
+                if (pending & (1u << (b ^ 1))) mbar_wait_sleep(&bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
+            }
+            return;
+        }
+        float *P;
         int SP;
-        if (pending) {
-            const uint32_t ph = parity;
-            const bool ok = mbar_wait_bounded(&bar, ph);
-            parity ^= 1u;
-            pending = false;
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) {
-                    atomicExch(err, 1);
-                    mbar_wait_bounded(&bar, ph);   // the copy may still land: give it time
-                }
-                return;
-            }
-            if (sizeof(Tin) == 4) {
-                P = reinterpret_cast<const float *>(raw);       // window starts aligned
-                SP = boxw;
-            } else {
-                // codes -> values, four per thread (the box starts at the window)
-                const int q4 = (CV + 3) >> 2;
-                for (int idx = tid; idx < RV * q4; idx += nth) {
-                    const int r = idx / q4, c = 4 * (idx - r * q4);
-                    const uint32_t w4 = *reinterpret_cast<const uint32_t *>(
-                        reinterpret_cast<const uint8_t *>(raw) + r * boxw + c);
-                    *reinterpret_cast<float4 *>(T + r * L.st + c) =
-                        make_float4(lut[w4 & 0xFF], lut[(w4 >> 8) & 0xFF], lut[(w4 >> 16) & 0xFF], lut[w4 >> 24]);
-                }
-                P = T;
-                SP = L.st;
-            }
+        if (sizeof(Tin) == 4) {
+            P = reinterpret_cast<float *>(raw);       // window starts aligned
+            SP = boxw;
         } else {
-            // border tile: gather through the border map
-            float *G = sizeof(Tin) == 4 ? reinterpret_cast<float *>(raw) : T;
-            const int SG = sizeof(Tin) == 4 ? boxw : L.st;
-            gather_tile<8>(G, RV * SG, [&](int idx) -> float {
-                const int r = idx / SG, c = idx - r * SG;
-                if (c >= CV) return 0.0f;
-                const int mx = map_index(px + c, nx, style);
+            // codes -> values, four per thread (the box starts at the window)
+            const int q4 = (CV + 3) >> 2;
+            for (int idx = tid; idx < RV * q4; idx += nth) {
+                const int r = idx / q4, c = 4 * (idx - r * q4);
+                const uint32_t w4 = *reinterpret_cast<const uint32_t *>(
+                    reinterpret_cast<const uint8_t *>(raw) + r * boxw + c);
+                *reinterpret_cast<float4 *>(T + r * L.st + c) =
+                    make_float4(lut[w4 & 0xFF], lut[(w4 >> 8) & 0xFF], lut[(w4 >> 16) & 0xFF], lut[w4 >> 24]);
+            }
+            P = T;
+            SP = L.st;
+        }
+        if (!interior(t)) {
+            // border tile: the cells of the window outside the image take the
+            // border's values, rows first (in-image columns), then columns (all
+            // rows, corners included).  Sources are in-image cells: read from
+            // the tile when the window holds them, from the image otherwise.
+            if (sizeof(Tin) == 1) __syncthreads();        // the converted tile is complete
+            const int top = min(max(-py, 0), RV), bot = min(max(RV - (ny - py), 0), RV - top);
+            const int lft = min(max(-px, 0), CV), rgt = min(max(CV - (nx - px), 0), CV - lft);
+            const int ncin = CV - lft - rgt;
+            for (int idx = tid; idx < (top + bot) * ncin; idx += nth) {
+                const int rr = idx / ncin, c = lft + (idx - rr * ncin);
+                const int r = rr < top ? rr : RV - bot + (rr - top);
+                float v = fill;
                 const int my = map_index(py + r, ny, style);
-                return (mx < 0 || my < 0) ? fill : cvt<float, Tin>(img[(long long)my * nx + mx], norm);
-            });
-            P = G;
-            SP = SG;
+                if (my >= 0) {
+                    const int sr = my - py;
+                    v = (sr >= 0 && sr < RV) ? P[sr * SP + c]
+                                             : cvt<float, Tin>(img[(long long)my * nx + px + c], norm);
+                }
+                P[r * SP + c] = v;
+            }
+            __syncthreads();
+            const int nco = lft + rgt;
+            for (int idx = tid; idx < RV * nco; idx += nth) {
+                const int r = idx / nco, cc = idx - r * nco;
+                const int c = cc < lft ? cc : CV - rgt + (cc - lft);
+                float v = fill;
+                const int mx = map_index(px + c, nx, style);
+                if (mx >= 0) {
+                    const int sc = mx - px;
+                    if (sc >= 0 && sc < CV) {
+                        v = P[r * SP + sc];
+                    } else {
+                        const int my = map_index(py + r, ny, style);
+                        v = my < 0 ? fill : cvt<float, Tin>(img[(long long)my * nx + mx], norm);
+                    }
+                }
+                P[r * SP + c] = v;
+            }
         }
         fence_proxy_async();
         __syncthreads();
-        if (sizeof(Tin) == 1) prefetch(tn);        // the codes are converted: raw is free
 
         const int tx0 = px - fx, ty0 = py - fy;
         // interior output tiles store without bounds tests, by pointer steps
         const bool full = tx0 >= 0 && tx0 + TX <= nx && ty0 + TY <= ny;
-        float acc[NB];
+        float2 acc[NB / 2];
         if (x_first) {
             // x pass over all RV rows -> I (pitch si)
             for (int it = tid; it < ((RV + 15) & ~15) * (TX / NB); it += nth) {
                 int r, c0;
                 row_item(it, r, c0);
                 if (r >= RV) continue;
-                corr_row4<NB>(P + (size_t)r * SP + c0, wx, kx, acc);
+                corr_row4_x2<NB>(P + (size_t)r * SP + c0, wx, kx, acc);
                 float4 *d = reinterpret_cast<float4 *>(I + (size_t)r * L.si + c0);
 #pragma unroll
                 for (int q = 0; q < NB / 4; ++q)
-                    d[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+                    d[q] = make_float4(acc[2 * q].x, acc[2 * q].y, acc[2 * q + 1].x, acc[2 * q + 1].y);
             }
             fence_proxy_async();
             __syncthreads();
-            if (sizeof(Tin) == 4) prefetch(tn);    // the first pass has read raw
-            // y pass down each column, NB rows per item
-            for (int it = tid; it < TX * (TY / NB); it += nth) {
-                const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
-                corr_col<NB>(I + (size_t)r0 * L.si + c, L.si, wy, ky, acc);
+            // y pass down each column pair, NBY rows per item: a warp covers one
+            // 64-wide row block (256 contiguous bytes of I per load)
+            float2 ya[NBY];
+            for (int it = tid; it < (TX / 2) * (TY / NBY); it += nth) {
+                const int rs = it / (TX / 2), c = 2 * (it - rs * (TX / 2)), r0 = rs * NBY;
+                corr_col_x2<NBY>(I + (size_t)r0 * L.si + c, L.si, wy, ky, ya);
                 const int x = tx0 + c;
-                if (full) {
+                if (full && pair_store) {
                     Tout *o = out + (long long)(ty0 + r0) * nx + x;
 #pragma unroll
-                    for (int i = 0; i < NB; ++i, o += nx) *o = out_cvt<Tout>(acc[i]);
-                } else if (x >= 0 && x < nx) {
+                    for (int i = 0; i < NBY; ++i, o += nx) store_pair<Tout>(o, ya[i]);
+                } else {
 #pragma unroll
-                    for (int i = 0; i < NB; ++i) {
+                    for (int i = 0; i < NBY; ++i) {
                         const int y = ty0 + r0 + i;
-                        if (y < ny) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
+                        if (y >= ny) break;
+                        Tout *o = out + (long long)y * nx + x;
+                        if (x >= 0 && x < nx) o[0] = out_cvt<Tout>(ya[i].x);
+                        if (x + 1 >= 0 && x + 1 < nx) o[1] = out_cvt<Tout>(ya[i].y);
                     }
                 }
             }
         } else {
-            // y pass down each of the CV columns -> I (TY rows, pitch si)
-            for (int it = tid; it < CV * (TY / NB); it += nth) {
-                const int rs = it / CV, c = it - rs * CV, r0 = rs * NB;
-                corr_col<NB>(P + (size_t)r0 * SP + c, SP, wy, ky, acc);
+            // y pass down column pairs of the CV columns -> I (TY rows, pitch si);
+            // the pair at CV-1 (CV odd) also fills column CV, inside the pitch
+            float2 ya[NBY];
+            for (int it = tid; it < ((CV + 1) >> 1) * (TY / NBY); it += nth) {
+                const int cp = (CV + 1) >> 1, rs = it / cp, c = 2 * (it - rs * cp), r0 = rs * NBY;
+                corr_col_x2<NBY>(P + (size_t)r0 * SP + c, SP, wy, ky, ya);
 #pragma unroll
-                for (int i = 0; i < NB; ++i) I[(size_t)(r0 + i) * L.si + c] = acc[i];
+                for (int i = 0; i < NBY; ++i) *reinterpret_cast<float2 *>(I + (size_t)(r0 + i) * L.si + c) = ya[i];
             }
             fence_proxy_async();
             __syncthreads();
-            if (sizeof(Tin) == 4) prefetch(tn);    // the first pass has read raw
             // x pass along the TY rows
             for (int it = tid; it < TY * (TX / NB); it += nth) {
                 int r, c0;
                 row_item(it, r, c0);
-                corr_row4<NB>(I + (size_t)r * L.si + c0, wx, kx, acc);
+                corr_row4_x2<NB>(I + (size_t)r * L.si + c0, wx, kx, acc);
                 const int y = ty0 + r;
                 if (full) {
                     Tout *o = out + (long long)y * nx + tx0 + c0;
 #pragma unroll
-                    for (int i = 0; i < NB; ++i) o[i] = out_cvt<Tout>(acc[i]);
+                    for (int m = 0; m < NB / 2; ++m) {
+                        o[2 * m] = out_cvt<Tout>(acc[m].x);
+                        o[2 * m + 1] = out_cvt<Tout>(acc[m].y);
+                    }
                 } else if (y < ny) {
 #pragma unroll
                     for (int i = 0; i < NB; ++i) {
                         const int x = tx0 + c0 + i;
-                        if (x >= 0 && x < nx) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
+                        const float v = (i & 1) ? acc[i >> 1].y : acc[i >> 1].x;
+                        if (x >= 0 && x < nx) out[(long long)y * nx + x] = out_cvt<Tout>(v);
                     }
                 }
             }
@@ -593,9 +653,13 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     if (tiles > (1ll << 30)) return false;
     const long long slots = (long long)sms * per_sm;
     const int grid = (int)(tiles < slots ? tiles : slots);
+    // interior output pairs (x even relative to the row start) store as one
+    // 8- or 16-byte word when rows and the tile grid keep them aligned
+    const int pair_store = (a.nx % 2 == 0) && (shift % 2 == 0) &&
+                           ((uintptr_t)a.out % (2 * sizeof(Tout)) == 0);
     kern<<<grid, 256, L.total, s>>>(map, (const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.fx, a.kx, a.fy,
                                     a.ky, a.x_first, a.style, (float)a.fill, a.in_type == IFX_N0F8, shift,
-                                    tiles_x, (int)tiles, err, W);
+                                    tiles_x, (int)tiles, pair_store, err, W);
     note_launch();
     *e = cudaGetLastError();
     return true;

@@ -63,6 +63,23 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     return false;
 }
 
+// Waits for phase `parity` of *bar with the suspend-time hint of try_wait
+// (the thread sleeps until the phase completes or about `ns` nanoseconds
+// pass) instead of polling: waiting warps issue almost nothing.  Gives up
+// after `tries` waits (a few seconds at most).
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity, uint32_t tries = 4096u,
+                                                uint32_t ns = 1000000u)
+{
+    for (uint32_t i = 0; i < tries; ++i) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity), "r"(ns) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
 // Box (x, y) of `map` -> shared memory at `dst` (128-byte aligned), completing
 // `bytes` of transaction count on *bar.  x * element size must be a multiple
 // of 16 bytes.

@@ -86,12 +86,15 @@ def test_separable_2d_random(gpu_ifx, oracle, kind, style):
 @pytest.mark.parametrize("style", STYLES)
 def test_separable_2d_tma_tiles(gpu_ifx, oracle, kind, style):
     """Images whose rows meet the bulk-copy rules (width a multiple of 16), so
-    that the persistent kernel copies interior tiles by TMA and gathers the
-    border tiles: random factor lengths/offsets, both pass orders, Float32 and
-    Float64 outputs, several tiles per CTA on the largest image."""
+    that the persistent kernel copies every tile by TMA and gives the window
+    cells outside the image their border values in shared memory (from the
+    tile, or from the image where the window does not hold the source):
+    random factor lengths/offsets, both pass orders, Float32 and Float64
+    outputs, images smaller than one tile, several tiles per CTA on the
+    largest image."""
     ifx = gpu_ifx
     rng = np.random.default_rng(zlib.crc32(("tma" + kind + style).encode()))
-    for shape in [(256, 200), (1040, 333), (4096, 1100)]:
+    for shape in [(32, 7), (48, 70), (256, 200), (1040, 333), (4096, 1100)]:
         img = make_img(rng, shape, kind)
         for _ in range(2 if shape[0] < 4096 else 1):
             lx, ly = int(rng.integers(1, 34)), int(rng.integers(1, 34))
