@@ -556,7 +556,10 @@ def _time(torch, fn, reps=5):
     every timed run, outside the events: a 256 MB buffer is overwritten, then a
     second 256 MB buffer is read, so that L2 holds clean lines of neither the
     inputs nor the outputs and the timed kernels pay for no write-back of the
-    flush's own dirty lines."""
+    flush's own dirty lines.  A GPU sleep of about half a millisecond is
+    queued before the start event, so that the host's own work of the call
+    (argument checks, descriptors, the launch) overlaps it and the events
+    time the device work alone."""
     if not _FLUSH:
         _FLUSH.append(torch.empty(256 << 20, dtype=torch.uint8, device="cuda"))
         _FLUSH.append(torch.zeros(64 << 20, dtype=torch.float32, device="cuda"))
@@ -567,6 +570,7 @@ def _time(torch, fn, reps=5):
     for _ in range(reps):
         _FLUSH[0].zero_()
         _FLUSH[1].sum()
+        torch.cuda._sleep(1_000_000)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()

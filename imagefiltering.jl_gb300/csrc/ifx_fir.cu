@@ -365,10 +365,10 @@ struct SepTmaSmem {
     size_t raw, w, t, i, total;
 };
 
-__host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int x_first, int elt_bytes)
+__host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int x_first, int elt_bytes, int ty)
 {
     SepTmaSmem L;
-    const int RV = kStTY + ky - 1, CV = kStTX + kx - 1;
+    const int RV = ty + ky - 1, CV = kStTX + kx - 1;
     // Windows start on 16-byte boundaries.  Float32: 3 floats of slack for
     // the 16-byte loads; 8-bit: codes are converted four at a time.
     L.boxw = elt_bytes == 4 ? st_pitch(CV + 3) : (CV + 3 + 15) / 16 * 16;
@@ -377,7 +377,7 @@ __host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int x_first, 
     L.raw = st_round128((size_t)L.boxw * RV * elt_bytes);
     L.w = st_round128(2 * (IFX_MAX_TAPS + 3) * sizeof(float2) + 256 * sizeof(float));
     L.t = elt_bytes == 1 ? st_round128((size_t)RV * L.st * sizeof(float)) : 0;
-    L.i = st_round128((size_t)(x_first ? RV : kStTY) * L.si * sizeof(float));
+    L.i = st_round128((size_t)(x_first ? RV : ty) * L.si * sizeof(float));
     L.total = 2 * L.raw + L.w + L.t + L.i;       // two input buffers: the next tile loads during this one
     return L;
 }
@@ -386,14 +386,16 @@ template <class Tin, class Tout>
 __global__ void __launch_bounds__(256)
 k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img, Tout *__restrict__ out,
             int nx, int ny, int fx, int kx, int fy, int ky, int x_first, int style, float fill, bool norm,
-            int shift, int tiles_x, int tiles, int pair_store, int *err, const __grid_constant__ Sep2dW<float> W)
+            int shift, int ty, int tiles_x, int tiles, int pair_store, int *err,
+            const __grid_constant__ Sep2dW<float> W)
 {
-    constexpr int TX = kStTX, TY = kStTY, NB = kStNB, NBY = kStNBY;
+    constexpr int TX = kStTX, NB = kStNB, NBY = kStNBY;
+    const int TY = ty;                                      // a multiple of NBY, at most 64
     constexpr int ALIGN = 16 / (int)sizeof(Tin);          // x granularity of a box start
     extern __shared__ __align__(128) unsigned char st_smem[];
     __shared__ __align__(8) uint64_t bar[2];
     const int RV = TY + ky - 1, CV = TX + kx - 1;
-    const SepTmaSmem L = sep_tma_smem(kx, ky, x_first, (int)sizeof(Tin));
+    const SepTmaSmem L = sep_tma_smem(kx, ky, x_first, (int)sizeof(Tin), TY);
     const int boxw = L.boxw;
     auto raw_buf = [&](int b) { return reinterpret_cast<Tin *>(st_smem + (size_t)b * L.raw); };
     unsigned char *rest = st_smem + 2 * L.raw;
@@ -416,11 +418,11 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     }
     __syncthreads();
 
-    // tile t covers outputs x in [tx*TX - shift, +TX), y in [ty*TY, +TY)
+    // tile t covers outputs x in [tx*TX - shift, +TX), y in [yt*TY, +TY)
     auto origin = [&](int t, int &px, int &py) {
-        const int ty = t / tiles_x, tx = t - ty * tiles_x;
+        const int yt = t / tiles_x, tx = t - yt * tiles_x;
         px = tx * TX - shift + fx;
-        py = ty * TY + fy;
+        py = yt * TY + fy;
     };
     auto interior = [&](int t) {
         int px, py;
@@ -587,10 +589,12 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             }
             fence_proxy_async();
             __syncthreads();
-            // x pass along the TY rows
-            for (int it = tid; it < TY * (TX / NB); it += nth) {
+            // x pass along the TY rows (items cover whole 16-row groups: TY
+            // may be 8 mod 16)
+            for (int it = tid; it < ((TY + 15) & ~15) * (TX / NB); it += nth) {
                 int r, c0;
                 row_item(it, r, c0);
+                if (r >= TY) continue;
                 corr_row4_x2<NB>(I + (size_t)r * L.si + c0, wx, kx, acc);
                 const int y = ty0 + r;
                 if (full) {
@@ -615,12 +619,22 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     }
 }
 
+// Tile height: 64 rows, lowered in steps of 8 (to 32 at most) until three
+// CTAs share an SM (the largest factors would otherwise leave two).
+static int sep_tma_ty(int kx, int ky, int x_first, int elt_bytes)
+{
+    int ty = kStTY;
+    while (ty > 32 && sep_tma_smem(kx, ky, x_first, elt_bytes, ty).total > 74 * 1024) ty -= kStNBY;
+    return ty;
+}
+
 template <class Tin, class Tout>
 static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
 {
     if (a.kx > kCorrKmax || a.ky > kCorrKmax) return false;
-    const int RV = kStTY + a.ky - 1;
-    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin));
+    const int ty = sep_tma_ty(a.kx, a.ky, a.x_first, (int)sizeof(Tin));
+    const int RV = ty + a.ky - 1;
+    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin), ty);
     if (L.boxw > 256 || RV > 256 || L.total > 160 * 1024) return false;
     CUtensorMap map;
     if (!tma_encode_2d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, (long long)a.nx * (long long)sizeof(Tin),
@@ -649,7 +663,7 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     constexpr int ALIGN = 16 / (int)sizeof(Tin);
     const int shift = ((a.fx % ALIGN) + ALIGN) % ALIGN;
     const int tiles_x = (a.nx + shift + kStTX - 1) / kStTX;
-    const long long tiles = (long long)tiles_x * ((a.ny + kStTY - 1) / kStTY);
+    const long long tiles = (long long)tiles_x * ((a.ny + ty - 1) / ty);
     if (tiles > (1ll << 30)) return false;
     const long long slots = (long long)sms * per_sm;
     const int grid = (int)(tiles < slots ? tiles : slots);
@@ -658,7 +672,7 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     const int pair_store = (a.nx % 2 == 0) && (shift % 2 == 0) &&
                            ((uintptr_t)a.out % (2 * sizeof(Tout)) == 0);
     kern<<<grid, 256, L.total, s>>>(map, (const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.fx, a.kx, a.fy,
-                                    a.ky, a.x_first, a.style, (float)a.fill, a.in_type == IFX_N0F8, shift,
+                                    a.ky, a.x_first, a.style, (float)a.fill, a.in_type == IFX_N0F8, shift, ty,
                                     tiles_x, (int)tiles, pair_store, err, W);
     note_launch();
     *e = cudaGetLastError();
@@ -670,8 +684,9 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
 template <class Tin> static bool sep2d_tma_fits(const Sep2dArgs &a)
 {
     if (a.kx > kCorrKmax || a.ky > kCorrKmax) return false;
-    const int RV = kStTY + a.ky - 1;
-    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin));
+    const int ty = sep_tma_ty(a.kx, a.ky, a.x_first, (int)sizeof(Tin));
+    const int RV = ty + a.ky - 1;
+    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin), ty);
     if (L.boxw > 256 || RV > 256 || L.total > 160 * 1024) return false;
     CUtensorMap map;
     return tma_encode_2d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, (long long)a.nx * (long long)sizeof(Tin),

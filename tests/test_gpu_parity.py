@@ -114,6 +114,25 @@ def test_separable_2d_tma_tiles(gpu_ifx, oracle, kind, style):
             assert normwise(got, ref) <= RTOL[kind], (shape, order, style)
 
 
+@pytest.mark.parametrize("kind", ["F32", "N0F8"])
+def test_separable_2d_tma_tile_heights(gpu_ifx, oracle, kind):
+    """Long factors lower the TMA kernel's tile height below 64 rows (to 56,
+    48, 40: not all multiples of 16); both pass orders, every tile row of the
+    image, including a partial last one."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("tma-heights" + kind).encode()))
+    img = make_img(rng, (320, 203), kind)
+    for taps in (17, 25, 33, 36):
+        wx, wy = rng.standard_normal(taps), rng.standard_normal(taps)
+        fx, fy = -(taps // 2), -(taps // 2) + 1
+        for x_first in (True, False):
+            order = [(0, fx, wx), (1, fy, wy)] if x_first else [(1, fy, wy), (0, fx, wx)]
+            ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(w, (f,)), 2, ax) for ax, f, w in order)
+            got = ifx.imfilter(wrap(ifx, img, kind), ks, ifx.Pad("symmetric"))
+            ref = oracle.imfilter_cascade(values(ifx, img, kind), order, "symmetric", 0.0)
+            assert normwise(got, ref) <= RTOL[kind], (taps, x_first)
+
+
 def test_float64_widening_exact(gpu_ifx):
     """Float64 outputs of FP32 arithmetic are widened exactly: zeros,
     subnormals, the extremes of the normal range, Inf and NaN."""
