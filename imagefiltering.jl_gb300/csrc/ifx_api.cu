@@ -456,15 +456,25 @@ static int run_cascade(Call &c, const ifx_array_t &imgd, const void *img, const 
         }
     }
 
-    // 3-D with one factor per axis in axis order: the fused z-marching kernel
+    // 3-D with one factor per axis in axis order: the z sweep into an FP32
+    // volume and the x/y TMA sweep over its planes, or (rows off the copy
+    // engine's rules, long z factors) the fused z-marching kernel
     if (nd == 3 && ct == IFX_F32 && facs.size() == 3 && facs[0].axis == 0 && facs[1].axis == 1 &&
-        facs[2].axis == 2 &&
-        sep3d_supported(facs[0].len, facs[1].len, facs[2].len, n[0], n[1], n[2], 1)) {
+        facs[2].axis == 2) {
         Sep3dArgs a{img, imgd.eltype, out, outd.eltype, n[0], n[1], n[2], 1,
                     facs[0].first, facs[0].len, facs[1].first, facs[1].len, facs[2].first, facs[2].len,
                     facs[0].w, facs[1].w, facs[2].w, border->style, fill};
-        IFX_CUDA(launch_sep3d(a, c.s));
-        return IFX_OK;
+        if (sep3d_split_applies(a)) {
+            void *vol = nullptr;
+            rc = slot_get(c.ctx, tmp_slot_base, (size_t)n[0] * n[1] * n[2] * sizeof(float), &vol);
+            if (rc) return rc;
+            IFX_CUDA(launch_sep3d_split(a, static_cast<float *>(vol), c.s));
+            return IFX_OK;
+        }
+        if (sep3d_supported(facs[0].len, facs[1].len, facs[2].len, n[0], n[1], n[2], 1)) {
+            IFX_CUDA(launch_sep3d(a, c.s));
+            return IFX_OK;
+        }
     }
     // generic: materialise the padded box in the compute type, then passes
     size_t need_a = 0, need_b = 0;

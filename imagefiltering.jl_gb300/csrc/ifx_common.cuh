@@ -77,13 +77,12 @@ template <class To> __device__ __forceinline__ To from_c(double v) { return (To)
 __device__ __forceinline__ double f32_to_f64(float f)
 {
     const uint32_t b = __float_as_uint(f);
-    const uint32_t e = (b >> 23) & 0xFFu;
-    if (e == 0u || e == 0xFFu) {
-        if ((b & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
-        return (double)f;
-    }
-    const uint32_t hi = (b & 0x80000000u) | (((b >> 3) & 0x0FFFFFFFu) + (896u << 20));
-    return __hiloint2double((int)hi, (int)(b << 29));
+    const uint32_t a = b & 0x7FFFFFFFu;
+    // one unsigned compare: the magnitude lies in [2^-126, 2^128), exponent 1..254
+    if (a - 0x00800000u < 0x7F000000u)
+        return __hiloint2double((int)((b & 0x80000000u) | ((a >> 3) + (896u << 20))), (int)(b << 29));
+    if (a == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+    return (double)f;
 }
 
 // Output store conversion from an FP32 result.

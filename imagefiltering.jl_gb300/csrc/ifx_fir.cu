@@ -14,6 +14,7 @@
 //    671-739); dense kernels sum over all taps (src/imfilter.jl:624-669).
 #include "ifx_internal.h"
 #include "ifx_tma.cuh"
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -386,7 +387,7 @@ template <class Tin, class Tout>
 __global__ void __launch_bounds__(256)
 k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img, Tout *__restrict__ out,
             int nx, int ny, int fx, int kx, int fy, int ky, int x_first, int style, float fill, bool norm,
-            int shift, int ty, int tiles_x, int tiles, int pair_store, int *err,
+            int shift, int ty, int tiles_x, int tiles_per_slice, int tiles, int pair_store, int *err,
             const __grid_constant__ Sep2dW<float> W)
 {
     constexpr int TX = kStTX, NB = kStNB, NBY = kStNBY;
@@ -418,17 +419,20 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     }
     __syncthreads();
 
-    // tile t covers outputs x in [tx*TX - shift, +TX), y in [yt*TY, +TY)
-    auto origin = [&](int t, int &px, int &py) {
-        const int yt = t / tiles_x, tx = t - yt * tiles_x;
+    // tile t covers outputs x in [tx*TX - shift, +TX), y in [yt*TY, +TY) of
+    // plane sl (a stack of planes of nx x ny, filtered each on its own)
+    auto origin = [&](int t, int &px, int &py, int &sl) {
+        sl = t / tiles_per_slice;
+        const int u = t - sl * tiles_per_slice, yt = u / tiles_x, tx = u - yt * tiles_x;
         px = tx * TX - shift + fx;
         py = yt * TY + fy;
     };
     auto interior = [&](int t) {
-        int px, py;
-        origin(t, px, py);
+        int px, py, sl;
+        origin(t, px, py, sl);
         return px >= 0 && px + CV <= nx && py >= 0 && py + RV <= ny;
     };
+    const long long plane = (long long)nx * ny;
     // all threads call it (uniform); thread 0 issues the copy of tile t into
     // buffer b.  The buffer's previous readers finished before the block
     // barrier that ended the previous tile (after a proxy fence).
@@ -437,10 +441,10 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     auto prefetch = [&](int t, int b) {
         if (t < tiles) {
             if (tid == 0) {
-                int px, py;
-                origin(t, px, py);
+                int px, py, sl;
+                origin(t, px, py, sl);
                 mbar_expect_tx(&bar[b], box_bytes);
-                tma_load_2d(raw_buf(b), &map, px & ~(ALIGN - 1), py, &bar[b]);
+                tma_load_3d(raw_buf(b), &map, px & ~(ALIGN - 1), py, sl, &bar[b]);
             }
             pending |= 1u << b;
         }
@@ -460,8 +464,10 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         Tin *raw = raw_buf(b);
         // the next tile loads into the other buffer while this one computes
         prefetch(t + gridDim.x, b ^ 1);
-        int px, py;
-        origin(t, px, py);
+        int px, py, sl;
+        origin(t, px, py, sl);
+        const Tin *img_s = img + sl * plane;
+        Tout *out_s = out + sl * plane;
         // every tile arrives by the copy engine (cells outside the image as zeros)
         const uint32_t ph = (parity >> b) & 1u;
         const bool ok = mbar_wait_sleep(&bar[b], ph);
@@ -511,7 +517,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 if (my >= 0) {
                     const int sr = my - py;
                     v = (sr >= 0 && sr < RV) ? P[sr * SP + c]
-                                             : cvt<float, Tin>(img[(long long)my * nx + px + c], norm);
+                                             : cvt<float, Tin>(img_s[(long long)my * nx + px + c], norm);
                 }
                 P[r * SP + c] = v;
             }
@@ -528,7 +534,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                         v = P[r * SP + sc];
                     } else {
                         const int my = map_index(py + r, ny, style);
-                        v = my < 0 ? fill : cvt<float, Tin>(img[(long long)my * nx + mx], norm);
+                        v = my < 0 ? fill : cvt<float, Tin>(img_s[(long long)my * nx + mx], norm);
                     }
                 }
                 P[r * SP + c] = v;
@@ -563,7 +569,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 corr_col_x2<NBY>(I + (size_t)r0 * L.si + c, L.si, wy, ky, ya);
                 const int x = tx0 + c;
                 if (full && pair_store) {
-                    Tout *o = out + (long long)(ty0 + r0) * nx + x;
+                    Tout *o = out_s + (long long)(ty0 + r0) * nx + x;
 #pragma unroll
                     for (int i = 0; i < NBY; ++i, o += nx) store_pair<Tout>(o, ya[i]);
                 } else {
@@ -571,7 +577,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                     for (int i = 0; i < NBY; ++i) {
                         const int y = ty0 + r0 + i;
                         if (y >= ny) break;
-                        Tout *o = out + (long long)y * nx + x;
+                        Tout *o = out_s + (long long)y * nx + x;
                         if (x >= 0 && x < nx) o[0] = out_cvt<Tout>(ya[i].x);
                         if (x + 1 >= 0 && x + 1 < nx) o[1] = out_cvt<Tout>(ya[i].y);
                     }
@@ -598,7 +604,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 corr_row4_x2<NB>(I + (size_t)r * L.si + c0, wx, kx, acc);
                 const int y = ty0 + r;
                 if (full) {
-                    Tout *o = out + (long long)y * nx + tx0 + c0;
+                    Tout *o = out_s + (long long)y * nx + tx0 + c0;
 #pragma unroll
                     for (int m = 0; m < NB / 2; ++m) {
                         o[2 * m] = out_cvt<Tout>(acc[m].x);
@@ -609,7 +615,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                     for (int i = 0; i < NB; ++i) {
                         const int x = tx0 + c0 + i;
                         const float v = (i & 1) ? acc[i >> 1].y : acc[i >> 1].x;
-                        if (x >= 0 && x < nx) out[(long long)y * nx + x] = out_cvt<Tout>(v);
+                        if (x >= 0 && x < nx) out_s[(long long)y * nx + x] = out_cvt<Tout>(v);
                     }
                 }
             }
@@ -636,9 +642,10 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     const int RV = ty + a.ky - 1;
     const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin), ty);
     if (L.boxw > 256 || RV > 256 || L.total > 160 * 1024) return false;
+    const int nsl = a.nsl > 1 ? a.nsl : 1;
     CUtensorMap map;
-    if (!tma_encode_2d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, (long long)a.nx * (long long)sizeof(Tin),
-                       L.boxw, RV))
+    const long long pitch = (long long)a.nx * (long long)sizeof(Tin);
+    if (!tma_encode_3d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, nsl, pitch, pitch * a.ny, L.boxw, RV))
         return false;
     int dev = 0;
     if ((*e = cudaGetDevice(&dev)) != cudaSuccess) return true;
@@ -663,7 +670,8 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     constexpr int ALIGN = 16 / (int)sizeof(Tin);
     const int shift = ((a.fx % ALIGN) + ALIGN) % ALIGN;
     const int tiles_x = (a.nx + shift + kStTX - 1) / kStTX;
-    const long long tiles = (long long)tiles_x * ((a.ny + ty - 1) / ty);
+    const long long per_slice = (long long)tiles_x * ((a.ny + ty - 1) / ty);
+    const long long tiles = per_slice * nsl;
     if (tiles > (1ll << 30)) return false;
     const long long slots = (long long)sms * per_sm;
     const int grid = (int)(tiles < slots ? tiles : slots);
@@ -673,7 +681,7 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
                            ((uintptr_t)a.out % (2 * sizeof(Tout)) == 0);
     kern<<<grid, 256, L.total, s>>>(map, (const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.fx, a.kx, a.fy,
                                     a.ky, a.x_first, a.style, (float)a.fill, a.in_type == IFX_N0F8, shift, ty,
-                                    tiles_x, (int)tiles, pair_store, err, W);
+                                    tiles_x, (int)per_slice, (int)tiles, pair_store, err, W);
     note_launch();
     *e = cudaGetLastError();
     return true;
@@ -688,9 +696,12 @@ template <class Tin> static bool sep2d_tma_fits(const Sep2dArgs &a)
     const int RV = ty + a.ky - 1;
     const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin), ty);
     if (L.boxw > 256 || RV > 256 || L.total > 160 * 1024) return false;
+    const int nsl = a.nsl > 1 ? a.nsl : 1;
+    const long long tiles = (long long)((a.nx + 16 + kStTX - 1) / kStTX) * ((a.ny + ty - 1) / ty) * nsl;
     CUtensorMap map;
-    return tma_encode_2d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, (long long)a.nx * (long long)sizeof(Tin),
-                         L.boxw, RV);
+    const long long pitch = (long long)a.nx * (long long)sizeof(Tin);
+    return tiles <= (1ll << 30) &&
+           tma_encode_3d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, nsl, pitch, pitch * a.ny, L.boxw, RV);
 }
 
 bool sep2d_tma_applies(const Sep2dArgs &a)
@@ -725,6 +736,7 @@ cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s)
     if (a.nx == 0 || a.ny == 0) return cudaSuccess;
     cudaError_t e = cudaSuccess;
     if (launch_sep2d_tma(a, s, &e)) return e;
+    if (a.nsl > 1) return cudaErrorInvalidValue;     // stacks of planes: TMA tile kernel only
     const int it = a.in_type, ot = a.out_type;
     if (!a.compute_f64) {
         if (it == IFX_F32 && ot == IFX_F32) return sep2d_t<float, float, float>(a, s);
@@ -908,6 +920,145 @@ cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s)
 }
 
 // =========================================================================
+// 3-D separable path in two sweeps (the default where it applies): the z
+// factor first, from the image into an FP32 volume, then the x and y factors
+// of every z plane by the TMA tile kernel over the stack of planes, into the
+// output.  Pad-then-cascade filters one fixed padded array, so the order of
+// the factors only moves FP32 rounding; a Fill border becomes, for the x/y
+// sweep, the z-filtered fill value fill * sum(wz).  Traffic: the image once,
+// the FP32 volume twice, the output once.
+//
+// k_zpass: a thread computes kZNB consecutive z outputs of two adjacent x
+// (FP32x2 pairs), a warp 64 consecutive x of one row, a CTA 8 rows; the z
+// window goes through the border map (one map per plane, warp-uniform).
+// =========================================================================
+constexpr int kZNB = 8;
+
+struct ZpassW { float wz[kCorrKmax]; };
+
+template <class Tin, bool PAIR>
+__global__ void __launch_bounds__(256)
+k_zpass(const Tin *__restrict__ img, float *__restrict__ out, int nx, int ny, int nz, int zblocks, int fz, int kz,
+        int style, float fill, bool norm, const __grid_constant__ ZpassW W)
+{
+    constexpr int NB = kZNB;
+    __shared__ float2 w2[kCorrKmax];
+    const int tid = threadIdx.x;
+    for (int t = tid; t < kz; t += blockDim.x) w2[t] = make_float2(W.wz[t], W.wz[t]);
+    __syncthreads();
+    const int lane = tid & 31, warp = tid >> 5;
+    const int x = 2 * (blockIdx.x * 32 + lane), y = blockIdx.y * 8 + warp;
+    const int zb = blockIdx.z % zblocks, vol = blockIdx.z / zblocks, z0 = zb * NB;
+    if (x >= nx || y >= ny) return;
+    const long long plane = (long long)nx * ny;
+    const long long base = (long long)vol * plane * nz + (long long)y * nx + x;
+    const bool two = x + 1 < nx;
+    auto at = [&](int j) -> float2 {
+        const int ms = map_index(z0 + fz + j, nz, style);
+        if (ms < 0) return make_float2(fill, fill);
+        const Tin *p = img + base + (long long)ms * plane;
+        if constexpr (PAIR && sizeof(Tin) == 4) {
+            return *reinterpret_cast<const float2 *>(p);
+        } else if constexpr (PAIR) {
+            const uchar2 u = *reinterpret_cast<const uchar2 *>(p);
+            return make_float2(cvt<float, Tin>(u.x, norm), cvt<float, Tin>(u.y, norm));
+        } else {
+            return make_float2(cvt<float, Tin>(p[0], norm), two ? cvt<float, Tin>(p[1], norm) : 0.0f);
+        }
+    };
+    float2 v[NB + kCorrKmax - 1], acc[NB];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        v[i] = at(i);
+        acc[i] = make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int t = 0; t < kCorrKmax; ++t) {
+        if (t >= kz) break;
+        if (t > 0) v[NB - 1 + t] = at(NB - 1 + t);
+        const float2 w = w2[t];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) acc[i] = __ffma2_rn(w, v[i + t], acc[i]);
+    }
+    float *o = out + base + (long long)z0 * plane;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        if (z0 + i >= nz) break;
+        if constexpr (PAIR) {
+            *reinterpret_cast<float2 *>(o + i * plane) = acc[i];
+        } else {
+            o[i * plane] = acc[i].x;
+            if (two) o[i * plane + 1] = acc[i].y;
+        }
+    }
+}
+
+template <class Tin>
+static cudaError_t zpass_t(const Sep3dArgs &a, float *tmp, cudaStream_t s)
+{
+    ZpassW W;
+    memset(&W, 0, sizeof W);
+    for (int t = 0; t < a.kz; ++t) W.wz[t] = (float)a.wz[t];
+    const int zblocks = (a.nz + kZNB - 1) / kZNB;
+    dim3 grid((a.nx + 63) / 64, (a.ny + 7) / 8, zblocks * a.nvol);
+    const bool pair = a.nx % 2 == 0 && (uintptr_t)a.img % (2 * sizeof(Tin)) == 0;
+    if (pair)
+        k_zpass<Tin, true><<<grid, 256, 0, s>>>((const Tin *)a.img, tmp, a.nx, a.ny, a.nz, zblocks, a.fz, a.kz,
+                                                a.style, (float)a.fill, a.in_type == IFX_N0F8, W);
+    else
+        k_zpass<Tin, false><<<grid, 256, 0, s>>>((const Tin *)a.img, tmp, a.nx, a.ny, a.nz, zblocks, a.fz,
+                                                 a.kz, a.style, (float)a.fill, a.in_type == IFX_N0F8, W);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// The x/y sweep of the split path over the FP32 volume at `tmp`.
+static Sep2dArgs sep3d_xy_args(const Sep3dArgs &a, const float *tmp)
+{
+    double wsum = 0.0;
+    for (int t = 0; t < a.kz; ++t) wsum += a.wz[t];
+    Sep2dArgs b{};
+    b.img = tmp;
+    b.in_type = IFX_F32;
+    b.out = a.out;
+    b.out_type = a.out_type;
+    b.nx = a.nx;
+    b.ny = a.ny;
+    b.fx = a.fx;
+    b.kx = a.kx;
+    b.fy = a.fy;
+    b.ky = a.ky;
+    b.wx = a.wx;
+    b.wy = a.wy;
+    b.x_first = 1;
+    b.style = a.style;
+    b.fill = a.fill * wsum;
+    b.compute_f64 = 0;
+    b.variant = 1;
+    b.nsl = a.nz * a.nvol;
+    return b;
+}
+
+bool sep3d_split_applies(const Sep3dArgs &a)
+{
+    if (!(a.in_type == IFX_F32 || is8(a.in_type)) || !(a.out_type == IFX_F32 || a.out_type == IFX_F64)) return false;
+    if (a.kz > kCorrKmax || a.kx > kCorrKmax || a.ky > kCorrKmax || a.nx % 4 != 0) return false;
+    if ((long long)a.nx * a.ny * a.nz * a.nvol >= (1ll << 40)) return false;
+    if ((long long)((a.nz + kZNB - 1) / kZNB) * a.nvol > 65535 || (a.ny + 7) / 8 > 65535) return false;
+    // the FP32 volume of cudaMalloc is 256-byte aligned: probe the x/y sweep with such a base
+    Sep2dArgs b = sep3d_xy_args(a, reinterpret_cast<const float *>(uintptr_t(256)));
+    return sep2d_tma_applies(b);
+}
+
+cudaError_t launch_sep3d_split(const Sep3dArgs &a, float *tmp, cudaStream_t s)
+{
+    if ((long long)a.nx * a.ny * a.nz == 0 || a.nvol == 0) return cudaSuccess;
+    cudaError_t e = is8(a.in_type) ? zpass_t<uint8_t>(a, tmp, s) : zpass_t<float>(a, tmp, s);
+    if (e != cudaSuccess) return e;
+    return launch_sep2d(sep3d_xy_args(a, tmp), s);
+}
+
+// =========================================================================
 // Fused 3-D gradients (imgradients with a 3-tap (derivative, smoothing) pair
 // on all three axes, src/specialty.jl:39-53): gradient d is the cascade of
 // the derivative along axis d and the smoothing along the other axes, in axis
@@ -929,10 +1080,33 @@ __device__ __forceinline__ Tc tap3(const Tc *w, Tc a, Tc b, Tc c)
     return fma(w[2], c, fma(w[1], b, w[0] * a));
 }
 
-template <class Tin, class Tc, class Tout>
+// Sobel-structured pairs (derivative (-h, 0, h), smoothing (q, 2q, q), h and
+// q powers of two, as KernelFactors.sobel's [-1,0,1]/2 and [1,2,1]/4): the
+// passes sum unscaled, D = c - a (one addition) and S = (a + c) + 2b (an
+// addition and an exact-doubling fma), and every gradient takes the common
+// power-of-two factor h q^2 once at the end.  Scaling by a power of two is
+// exact, so this reorders the reference's sums only (FP64 rounding,
+// differences far inside the Float64 tolerance) and needs 14 instead of 26
+// FP64 operations per voxel, the bound on this part's narrow FP64 pipe.
+template <class Tc> __device__ __forceinline__ Tc sob_d(Tc a, Tc, Tc c) { return c - a; }
+template <class Tc> __device__ __forceinline__ Tc sob_s(Tc a, Tc b, Tc c) { return fma(Tc(2), b, a + c); }
+
+// v * 2^e for a power-of-two factor f = 2^e: exponent arithmetic when v and
+// the result are normal numbers, the multiplication otherwise.
+__device__ __forceinline__ double scale_pow2(double v, int e, double f)
+{
+    const long long b = __double_as_longlong(v);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    if (ex > 0 && ex < 2047 && ex + e > 0 && ex + e < 2047) return __longlong_as_double(b + ((long long)e << 52));
+    return v * f;
+}
+__device__ __forceinline__ float scale_pow2(float v, int, float f) { return v * f; }
+
+template <class Tin, class Tc, class Tout, bool SOB>
 __global__ void __launch_bounds__(256)
 k_grad3d(const Tin *__restrict__ img, Tout *__restrict__ gx, Tout *__restrict__ gy, Tout *__restrict__ gz,
-         int nx, int ny, int nz, Tc d0, Tc d1, Tc d2, Tc s0, Tc s1, Tc s2, int style, Tc fill, bool norm)
+         int nx, int ny, int nz, Tc d0, Tc d1, Tc d2, Tc s0, Tc s1, Tc s2, int style, Tc fill, bool norm,
+         int scale_exp, Tc scale)
 {
     constexpr int TX = kG3TX, TY = g3ty<Tc>(), RT = TY + 2, CT = TX + 2;
     __shared__ Tc T[RT * CT];                   // input slice tile with x/y halo
@@ -957,17 +1131,28 @@ k_grad3d(const Tin *__restrict__ img, Tout *__restrict__ gx, Tout *__restrict__ 
         for (int e = tid; e < RT * TX; e += nth) {
             const int r = e / TX, c = e - r * TX;
             const Tc *p = T + r * CT + c;
-            Dx[e] = tap3(dw, p[0], p[1], p[2]);
-            Sx[e] = tap3(sw, p[0], p[1], p[2]);
+            if constexpr (SOB) {
+                Dx[e] = sob_d(p[0], p[1], p[2]);
+                Sx[e] = sob_s(p[0], p[1], p[2]);
+            } else {
+                Dx[e] = tap3(dw, p[0], p[1], p[2]);
+                Sx[e] = tap3(sw, p[0], p[1], p[2]);
+            }
         }
         __syncthreads();
         const int slot = (sl - (z0 - 1)) % 3;
         for (int e = tid; e < TY * TX; e += nth) {
             const int r = e / TX, c = e - r * TX;
             const int i0 = r * TX + c, i1 = i0 + TX, i2 = i1 + TX;
-            ring[slot][0][e] = tap3(sw, Dx[i0], Dx[i1], Dx[i2]);
-            ring[slot][1][e] = tap3(dw, Sx[i0], Sx[i1], Sx[i2]);
-            ring[slot][2][e] = tap3(sw, Sx[i0], Sx[i1], Sx[i2]);
+            if constexpr (SOB) {
+                ring[slot][0][e] = sob_s(Dx[i0], Dx[i1], Dx[i2]);
+                ring[slot][1][e] = sob_d(Sx[i0], Sx[i1], Sx[i2]);
+                ring[slot][2][e] = sob_s(Sx[i0], Sx[i1], Sx[i2]);
+            } else {
+                ring[slot][0][e] = tap3(sw, Dx[i0], Dx[i1], Dx[i2]);
+                ring[slot][1][e] = tap3(dw, Sx[i0], Sx[i1], Sx[i2]);
+                ring[slot][2][e] = tap3(sw, Sx[i0], Sx[i1], Sx[i2]);
+            }
         }
         __syncthreads();
         const int z = sl - 1;                   // output slice completed by this input slice
@@ -978,22 +1163,61 @@ k_grad3d(const Tin *__restrict__ img, Tout *__restrict__ gx, Tout *__restrict__ 
                 const int x = tx0 + c, y = ty0 + r;
                 if (x >= nx || y >= ny) continue;
                 const long long o = (long long)z * plane + (long long)y * nx + x;
-                gx[o] = out_cvt<Tout>(tap3(sw, ring[a][0][e], ring[b][0][e], ring[c3][0][e]));
-                gy[o] = out_cvt<Tout>(tap3(sw, ring[a][1][e], ring[b][1][e], ring[c3][1][e]));
-                gz[o] = out_cvt<Tout>(tap3(dw, ring[a][2][e], ring[b][2][e], ring[c3][2][e]));
+                if constexpr (SOB) {
+                    gx[o] = out_cvt<Tout>(scale_pow2(sob_s(ring[a][0][e], ring[b][0][e], ring[c3][0][e]),
+                                                     scale_exp, scale));
+                    gy[o] = out_cvt<Tout>(scale_pow2(sob_s(ring[a][1][e], ring[b][1][e], ring[c3][1][e]),
+                                                     scale_exp, scale));
+                    gz[o] = out_cvt<Tout>(scale_pow2(sob_d(ring[a][2][e], ring[b][2][e], ring[c3][2][e]),
+                                                     scale_exp, scale));
+                } else {
+                    gx[o] = out_cvt<Tout>(tap3(sw, ring[a][0][e], ring[b][0][e], ring[c3][0][e]));
+                    gy[o] = out_cvt<Tout>(tap3(sw, ring[a][1][e], ring[b][1][e], ring[c3][1][e]));
+                    gz[o] = out_cvt<Tout>(tap3(dw, ring[a][2][e], ring[b][2][e], ring[c3][2][e]));
+                }
             }
         }
     }
+}
+
+// Power of two 2^e with |e| < 64 (returns false otherwise).
+static bool pow2_exp(double v, int *e)
+{
+    int ex = 0;
+    const double m = std::frexp(std::fabs(v), &ex);
+    if (m != 0.5 || ex - 1 < -63 || ex - 1 > 63) return false;
+    *e = ex - 1;
+    return true;
+}
+
+// Whether (d, s) are Sobel-structured, and the exponent of the common factor
+// h q^2 (negative h folds its sign into the factor).
+static bool sobel_structured(const Grad3dArgs &a, int *scale_exp, double *scale)
+{
+    int eh = 0, eq = 0;
+    if (a.d[1] != 0.0 || a.d[0] != -a.d[2] || !pow2_exp(a.d[2], &eh)) return false;
+    if (a.s[0] != a.s[2] || a.s[1] != 2.0 * a.s[0] || a.s[0] <= 0.0 || !pow2_exp(a.s[0], &eq)) return false;
+    *scale_exp = eh + 2 * eq;
+    *scale = a.d[2] * a.s[0] * a.s[0];
+    return a.d[2] > 0.0;       // a negative factor would flip signs in the exponent path
 }
 
 template <class Tin, class Tc, class Tout>
 static cudaError_t grad3d_t(const Grad3dArgs &a, cudaStream_t s)
 {
     dim3 grid((a.nx + kG3TX - 1) / kG3TX, (a.ny + g3ty<Tc>() - 1) / g3ty<Tc>(), (a.nz + kG3ZC - 1) / kG3ZC);
-    k_grad3d<Tin, Tc, Tout><<<grid, 256, 0, s>>>(
-        (const Tin *)a.img, (Tout *)a.out[0], (Tout *)a.out[1], (Tout *)a.out[2], a.nx, a.ny, a.nz,
-        (Tc)a.d[0], (Tc)a.d[1], (Tc)a.d[2], (Tc)a.s[0], (Tc)a.s[1], (Tc)a.s[2], a.style, (Tc)a.fill,
-        a.in_type == IFX_N0F8);
+    int se = 0;
+    double sc = 1.0;
+    if (sizeof(Tc) == 8 && sobel_structured(a, &se, &sc))
+        k_grad3d<Tin, Tc, Tout, true><<<grid, 256, 0, s>>>(
+            (const Tin *)a.img, (Tout *)a.out[0], (Tout *)a.out[1], (Tout *)a.out[2], a.nx, a.ny, a.nz,
+            (Tc)a.d[0], (Tc)a.d[1], (Tc)a.d[2], (Tc)a.s[0], (Tc)a.s[1], (Tc)a.s[2], a.style, (Tc)a.fill,
+            a.in_type == IFX_N0F8, se, (Tc)sc);
+    else
+        k_grad3d<Tin, Tc, Tout, false><<<grid, 256, 0, s>>>(
+            (const Tin *)a.img, (Tout *)a.out[0], (Tout *)a.out[1], (Tout *)a.out[2], a.nx, a.ny, a.nz,
+            (Tc)a.d[0], (Tc)a.d[1], (Tc)a.d[2], (Tc)a.s[0], (Tc)a.s[1], (Tc)a.s[2], a.style, (Tc)a.fill,
+            a.in_type == IFX_N0F8, 0, (Tc)1);
     note_launch();
     return cudaGetLastError();
 }

@@ -60,6 +60,8 @@ struct Sep2dArgs {
     int style; double fill;                // fill in value domain
     int compute_f64;
     int variant;                           // 0: automatic, 1: TMA tile kernel where it applies, 2: gather kernel
+    int nsl;                               // planes of nx x ny stacked at img/out, filtered each on its own
+                                           // (0 or 1: one; more: TMA tile kernel only)
 };
 cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s);
 bool sep2d_tma_applies(const Sep2dArgs &a);
@@ -80,6 +82,10 @@ struct Sep3dArgs {
 };
 bool sep3d_supported(int kx, int ky, int kz, int nx, int ny, int nz, int nvol);
 cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s);
+// the split 3-D path (z sweep into an FP32 volume of nx*ny*nz*nvol floats at
+// tmp, then the x/y TMA sweep over its planes); applies needs no device memory
+bool sep3d_split_applies(const Sep3dArgs &a);
+cudaError_t launch_sep3d_split(const Sep3dArgs &a, float *tmp, cudaStream_t s);
 
 // Fused 3-D gradients (3-tap derivative / smoothing pair, all axes extended):
 // the three imgradients outputs from one sweep -----------------------------

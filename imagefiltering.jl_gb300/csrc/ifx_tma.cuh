@@ -20,6 +20,11 @@ namespace ifx {
 bool tma_encode_2d(CUtensorMap *map, const void *base, int elt_bytes, long long nx, long long ny,
                    long long pitch_bytes, int box_w, int box_h);
 
+// The same over a stack of nz planes of ny rows (plane pitch `plane_bytes`),
+// box box_w x box_h x 1.
+bool tma_encode_3d(CUtensorMap *map, const void *base, int elt_bytes, long long nx, long long ny, long long nz,
+                   long long pitch_bytes, long long plane_bytes, int box_w, int box_h);
+
 // Per-device error word for kernels whose bounded waits ran out (0 = none);
 // allocated on first use.  tma_error_take reads and clears it.
 int *tma_error_word(int device);
@@ -88,6 +93,15 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
     asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
                  "[%0], [%1, {%2, %3}], [%4];"
                  :: "r"(smem_addr(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Box (x, y, z) of a 3-D `map` (box depth 1), as tma_load_2d.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+                 "[%0], [%1, {%2, %3, %4}], [%5];"
+                 :: "r"(smem_addr(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
                  : "memory");
 }
 

@@ -206,6 +206,33 @@ def test_separable_3d_volume(gpu_ifx, oracle):
     assert normwise(got, ref) <= 1e-5
 
 
+@pytest.mark.parametrize("kind", ["F32", "N0F8", "U8"])
+@pytest.mark.parametrize("style", STYLES)
+def test_separable_3d_split(gpu_ifx, oracle, kind, style):
+    """3-D cascades with one factor per axis: volumes whose rows meet the
+    bulk-copy rules take the z sweep into an FP32 volume and the x/y TMA
+    sweep over its planes (Fill becomes the z-filtered fill value there);
+    others (width 37) the fused z-marching kernel.  Random lengths and
+    offsets, Float64 and Float32 outputs."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("3dsplit" + kind + style).encode()))
+    for shape in [(16, 9, 13), (64, 33, 40), (37, 20, 11)]:
+        img = make_img(rng, shape, kind)
+        lens = [int(rng.integers(1, 20)) for _ in range(3)]
+        facs = [(ax, int(rng.integers(-lens[ax], 2)), rng.standard_normal(lens[ax])) for ax in range(3)]
+        f32w = rng.random() < 0.5
+        ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(w.astype(np.float32) if f32w else w, (f,)), 3, ax)
+                   for ax, f, w in facs)
+        fill = 0.7 if kind != "U8" else 3.0
+        b = ifx.Fill(fill) if style == "fill" else ifx.Pad(style)
+        got = ifx.imfilter(wrap(ifx, img, kind), ks, b)
+        fv = fill_value(kind, fill) if kind != "U8" else 3.0
+        ref_facs = [(ax, f, w.astype(np.float32).astype(np.float64) if f32w else w) for ax, f, w in facs]
+        ref = oracle.imfilter_cascade(values(ifx, img, kind), ref_facs, style, fv)
+        assert got.dtype == (np.float32 if f32w else np.float64)
+        assert normwise(got, ref) <= RTOL[kind], (shape, style, lens)
+
+
 # --------------------------------------------------------------------- dense
 @pytest.mark.parametrize("ksz,seed", [(5, 20), (15, 21), (31, 22)])
 @pytest.mark.parametrize("style", ["reflect", "fill", "replicate", "circular", "symmetric"])
