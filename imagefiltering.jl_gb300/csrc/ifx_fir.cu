@@ -449,12 +449,20 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             pending |= 1u << b;
         }
     };
-    // row-pass item -> (row, window start): a warp covers 16 rows x 2 starts and
-    // each 8-lane phase 4 rows x 2 starts (conflict-free for pitches 4 mod 8)
-    auto row_item = [](int it, int &r, int &c0) {
-        const int lane = it & 31, grp = it >> 5;
-        r = 16 * (grp >> 1) + 4 * (lane >> 3) + ((lane >> 1) & 3);
-        c0 = NB * (2 * (grp & 1) + (lane & 1));
+    // row-pass item -> (row, window start) over `rows` rows: two warps cover 16
+    // rows x 4 starts, each 8-lane phase 4 rows x 2 starts; the last rows go in
+    // groups of 8 rows x 4 starts per warp, each phase 8 rows x 1 start (both
+    // conflict-free for pitches 4 mod 8).  row_items(rows) items, whole warps.
+    auto row_items = [](int rows) { return 64 * (rows >> 4) + 32 * (((rows & 15) + 7) >> 3); };
+    auto row_item = [](int it, int rows, int &r, int &c0) {
+        const int lane = it & 31, grp = it >> 5, full = 2 * (rows >> 4);
+        if (grp < full) {
+            r = 16 * (grp >> 1) + 4 * (lane >> 3) + ((lane >> 1) & 3);
+            c0 = NB * (2 * (grp & 1) + (lane & 1));
+        } else {
+            r = 8 * grp + (lane & 7);              // rows 8*full onwards, 8 per warp
+            c0 = NB * (lane >> 3);
+        }
     };
 
     int t = blockIdx.x;
@@ -549,9 +557,9 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         float2 acc[NB / 2];
         if (x_first) {
             // x pass over all RV rows -> I (pitch si)
-            for (int it = tid; it < ((RV + 15) & ~15) * (TX / NB); it += nth) {
+            for (int it = tid; it < row_items(RV); it += nth) {
                 int r, c0;
-                row_item(it, r, c0);
+                row_item(it, RV, r, c0);
                 if (r >= RV) continue;
                 corr_row4_x2<NB>(P + (size_t)r * SP + c0, wx, kx, acc);
                 float4 *d = reinterpret_cast<float4 *>(I + (size_t)r * L.si + c0);
@@ -597,9 +605,9 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             __syncthreads();
             // x pass along the TY rows (items cover whole 16-row groups: TY
             // may be 8 mod 16)
-            for (int it = tid; it < ((TY + 15) & ~15) * (TX / NB); it += nth) {
+            for (int it = tid; it < row_items(TY); it += nth) {
                 int r, c0;
-                row_item(it, r, c0);
+                row_item(it, TY, r, c0);
                 if (r >= TY) continue;
                 corr_row4_x2<NB>(I + (size_t)r * L.si + c0, wx, kx, acc);
                 const int y = ty0 + r;
@@ -662,9 +670,13 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     if ((*e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total)) !=
         cudaSuccess)
         return true;
+    // 8 warps; the row pass's last groups take a second round (blocks with a
+    // warp for every group, 288-320 threads, measured slower)
+    const int nthreads = 256;
     int sms = 0, per_sm = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, L.total) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nthreads, L.total) != cudaSuccess ||
+        per_sm < 1)
         per_sm = 1;
     // tiles shift left so that tile windows start on 16-byte boundaries
     constexpr int ALIGN = 16 / (int)sizeof(Tin);
@@ -679,7 +691,7 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     // 8- or 16-byte word when rows and the tile grid keep them aligned
     const int pair_store = (a.nx % 2 == 0) && (shift % 2 == 0) &&
                            ((uintptr_t)a.out % (2 * sizeof(Tout)) == 0);
-    kern<<<grid, 256, L.total, s>>>(map, (const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.fx, a.kx, a.fy,
+    kern<<<grid, nthreads, L.total, s>>>(map, (const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.fx, a.kx, a.fy,
                                     a.ky, a.x_first, a.style, (float)a.fill, a.in_type == IFX_N0F8, shift, ty,
                                     tiles_x, (int)per_slice, (int)tiles, pair_store, err, W);
     note_launch();
