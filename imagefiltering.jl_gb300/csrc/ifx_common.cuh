@@ -221,57 +221,10 @@ __device__ __forceinline__ void corr_row4(const float *p, const float *w, int k,
     }
 }
 
-// Packed forms on the FP32x2 pipe (__ffma2_rn: two lanes of one FMA
+// Packed form on the FP32x2 pipe (__ffma2_rn: two lanes of one FMA
 // instruction, each rounded as fmaf).  Per output the taps accumulate in the
-// order of corr_row4 / corr_col, so the results are bit-identical to them.
-// Weights come as (w, w) pairs.
-
-// Row form: acc[m] = (out[2m], out[2m+1]) with out[i] = sum_{t<k} w[t] p[i+t],
-// i < NB (NB a multiple of 4), p 16-byte aligned.  Even taps use the aligned
-// value pairs (v[2j], v[2j+1]); odd taps the pairs (v[2j+1], v[2j+2]), built
-// once from two aligned ones.  Reads p[0 .. 4*ceil((NB+k-1)/4) - 1].
-template <int NB>
-__device__ __forceinline__ void corr_row4_x2(const float *p, const float2 *w2, int k, float2 *acc)
-{
-    constexpr int NP = (NB + kCorrKmax + 3) / 2 + 1;
-    float2 E[NP], O[NP];
-    const float4 *q = reinterpret_cast<const float4 *>(p);
-#pragma unroll
-    for (int c = 0; c < NB / 4; ++c) {
-        const float4 f = q[c];
-        E[2 * c] = make_float2(f.x, f.y);
-        E[2 * c + 1] = make_float2(f.z, f.w);
-    }
-#pragma unroll
-    for (int m = 0; m < NB / 2; ++m) acc[m] = make_float2(0.0f, 0.0f);
-#pragma unroll
-    for (int t = 0; t < kCorrKmax; ++t) {
-        if (t >= k) break;
-        // tap t reads v[t .. NB-1+t]: the quad holding v[NB-1+t] arrives when it starts
-        if (t > 0 && ((NB - 1 + t) & 3) == 0) {
-            const float4 f = q[(NB - 1 + t) >> 2];
-            E[(NB - 1 + t) >> 1] = make_float2(f.x, f.y);
-            E[((NB - 1 + t) >> 1) + 1] = make_float2(f.z, f.w);
-        }
-        const float2 w = w2[t];
-        const int s = t >> 1;
-        if ((t & 1) == 0) {
-#pragma unroll
-            for (int m = 0; m < NB / 2; ++m) acc[m] = __ffma2_rn(w, E[m + s], acc[m]);
-        } else {
-            // O[j] = (v[2j+1], v[2j+2]); this tap is the first to need O[NB/2-1+s]
-            if (t == 1) {
-#pragma unroll
-                for (int j = 0; j < NB / 2; ++j) O[j] = make_float2(E[j].y, E[j + 1].x);
-            } else {
-                O[NB / 2 - 1 + s] = make_float2(E[NB / 2 - 1 + s].y, E[NB / 2 + s].x);
-            }
-#pragma unroll
-            for (int m = 0; m < NB / 2; ++m) acc[m] = __ffma2_rn(w, O[m + s], acc[m]);
-        }
-    }
-}
-
+// order of corr_col, so the results are bit-identical to it.  Weights come as
+// (w, w) pairs.
 // Column-pair form: acc[i] = (out(i, 0), out(i, 1)) with
 // out(i, j) = sum_{t<k} w[t] p[(i+t)*step + j], i < NB; p and step*4 bytes
 // 8-byte aligned.  Reads rows 0 .. NB+k-2 of the two columns.

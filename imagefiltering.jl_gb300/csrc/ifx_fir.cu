@@ -336,9 +336,10 @@ static cudaError_t sep2d_t(const Sep2dArgs &a, cudaStream_t s)
 // Shared-memory layout keeps the row passes free of bank conflicts: the tile
 // grid is shifted so that every window starts on a 16-byte boundary,
 // row pitches are 4 mod 8 floats, and each 8-lane phase of a warp reads 4 rows
-// x 2 window starts with 16-byte loads.  Both passes run on the packed FP32x2
-// pipe: the row pass on pairs of outputs, the column pass on pairs of
-// columns (whose outputs store as one 8- or 16-byte word).  The passes are
+// x 2 window starts with 16-byte loads.  The column pass runs on the packed
+// FP32x2 pipe, on pairs of columns whose outputs store as one 8- or 16-byte
+// word; the row pass stays scalar (packed output pairs need the shifted
+// value pairs built by moves, which measured slower).  The passes are
 // those of k_sep2d (cascade order, pass ranges); outputs of FP32 results
 // widen exactly.
 // =========================================================================
@@ -400,14 +401,14 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     const int boxw = L.boxw;
     auto raw_buf = [&](int b) { return reinterpret_cast<Tin *>(st_smem + (size_t)b * L.raw); };
     unsigned char *rest = st_smem + 2 * L.raw;
-    float2 *wx = reinterpret_cast<float2 *>(rest);   // (w, w) pairs
-    float2 *wy = wx + (IFX_MAX_TAPS + 3);
+    float *wxs = reinterpret_cast<float *>(rest);     // row-pass weights
+    float2 *wy = reinterpret_cast<float2 *>(rest) + (IFX_MAX_TAPS + 3);   // column-pass (w, w) pairs
     float *lut = reinterpret_cast<float *>(wy + (IFX_MAX_TAPS + 3));   // 8-bit code -> value
     float *T = reinterpret_cast<float *>(rest + L.w);
     float *I = reinterpret_cast<float *>(rest + L.w + L.t);
     const int tid = threadIdx.x, nth = blockDim.x;
     const uint32_t box_bytes = (uint32_t)(boxw * RV * (int)sizeof(Tin));
-    for (int t = tid; t < kx; t += nth) wx[t] = make_float2(W.wx[t], W.wx[t]);
+    for (int t = tid; t < kx; t += nth) wxs[t] = W.wx[t];
     for (int t = tid; t < ky; t += nth) wy[t] = make_float2(W.wy[t], W.wy[t]);
     if (sizeof(Tin) == 1)
         for (int c = tid; c < 256; c += nth) lut[c] = to_c<float>((uint8_t)c, norm);
@@ -554,18 +555,18 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         const int tx0 = px - fx, ty0 = py - fy;
         // interior output tiles store without bounds tests, by pointer steps
         const bool full = tx0 >= 0 && tx0 + TX <= nx && ty0 + TY <= ny;
-        float2 acc[NB / 2];
+        float acc[NB];
         if (x_first) {
             // x pass over all RV rows -> I (pitch si)
             for (int it = tid; it < row_items(RV); it += nth) {
                 int r, c0;
                 row_item(it, RV, r, c0);
                 if (r >= RV) continue;
-                corr_row4_x2<NB>(P + (size_t)r * SP + c0, wx, kx, acc);
+                corr_row4<NB>(P + (size_t)r * SP + c0, wxs, kx, acc);
                 float4 *d = reinterpret_cast<float4 *>(I + (size_t)r * L.si + c0);
 #pragma unroll
                 for (int q = 0; q < NB / 4; ++q)
-                    d[q] = make_float4(acc[2 * q].x, acc[2 * q].y, acc[2 * q + 1].x, acc[2 * q + 1].y);
+                    d[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
             }
             fence_proxy_async();
             __syncthreads();
@@ -609,21 +610,17 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 int r, c0;
                 row_item(it, TY, r, c0);
                 if (r >= TY) continue;
-                corr_row4_x2<NB>(I + (size_t)r * L.si + c0, wx, kx, acc);
+                corr_row4<NB>(I + (size_t)r * L.si + c0, wxs, kx, acc);
                 const int y = ty0 + r;
                 if (full) {
                     Tout *o = out_s + (long long)y * nx + tx0 + c0;
 #pragma unroll
-                    for (int m = 0; m < NB / 2; ++m) {
-                        o[2 * m] = out_cvt<Tout>(acc[m].x);
-                        o[2 * m + 1] = out_cvt<Tout>(acc[m].y);
-                    }
+                    for (int i = 0; i < NB; ++i) o[i] = out_cvt<Tout>(acc[i]);
                 } else if (y < ny) {
 #pragma unroll
                     for (int i = 0; i < NB; ++i) {
                         const int x = tx0 + c0 + i;
-                        const float v = (i & 1) ? acc[i >> 1].y : acc[i >> 1].x;
-                        if (x >= 0 && x < nx) out_s[(long long)y * nx + x] = out_cvt<Tout>(v);
+                        if (x >= 0 && x < nx) out_s[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
                     }
                 }
             }
