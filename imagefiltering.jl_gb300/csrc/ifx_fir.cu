@@ -396,6 +396,8 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     constexpr int ALIGN = 16 / (int)sizeof(Tin);          // x granularity of a box start
     extern __shared__ __align__(128) unsigned char st_smem[];
     __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int src_row[64 + kCorrKmax], src_col[kStTX + kCorrKmax];   // border tiles' source maps
+    constexpr int kSrcFill = -1;
     const int RV = TY + ky - 1, CV = TX + kx - 1;
     const SepTmaSmem L = sep_tma_smem(kx, ky, x_first, (int)sizeof(Tin), TY);
     const int boxw = L.boxw;
@@ -477,6 +479,18 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         origin(t, px, py, sl);
         const Tin *img_s = img + sl * plane;
         Tout *out_s = out + sl * plane;
+        // a border tile's source maps (see below), while its copy is in flight;
+        // the barrier after the wait publishes them
+        const bool border = !interior(t);
+        if (border) {
+            for (int i = tid; i < RV + CV; i += nth) {
+                const bool row = i < RV;
+                const int w = row ? RV : CV, o = row ? py : px, j = row ? i : i - RV;
+                const int m = map_index(o + j, row ? ny : nx, style);
+                const int code = m < 0 ? kSrcFill : (m - o >= 0 && m - o < w ? m - o : -2 - m);
+                (row ? src_row : src_col)[j] = code;
+            }
+        }
         // every tile arrives by the copy engine (cells outside the image as zeros)
         const uint32_t ph = (parity >> b) & 1u;
         const bool ok = mbar_wait_sleep(&bar[b], ph);
@@ -509,44 +523,41 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             P = T;
             SP = L.st;
         }
-        if (!interior(t)) {
+        if (border) {
             // border tile: the cells of the window outside the image take the
             // border's values, rows first (in-image columns), then columns (all
             // rows, corners included).  Sources are in-image cells: read from
             // the tile when the window holds them, from the image otherwise.
-            if (sizeof(Tin) == 1) __syncthreads();        // the converted tile is complete
+            // The border map runs once per window row and column, into
+            // src_row / src_col: >= 0 the source's row (column) in the tile,
+            // kSrcFill the fill value, <= -2 the image row (column) -2 - code.
             const int top = min(max(-py, 0), RV), bot = min(max(RV - (ny - py), 0), RV - top);
             const int lft = min(max(-px, 0), CV), rgt = min(max(CV - (nx - px), 0), CV - lft);
+            if (sizeof(Tin) == 1) __syncthreads();        // the converted tile is complete
             const int ncin = CV - lft - rgt;
-            for (int idx = tid; idx < (top + bot) * ncin; idx += nth) {
-                const int rr = idx / ncin, c = lft + (idx - rr * ncin);
-                const int r = rr < top ? rr : RV - bot + (rr - top);
-                float v = fill;
-                const int my = map_index(py + r, ny, style);
-                if (my >= 0) {
-                    const int sr = my - py;
-                    v = (sr >= 0 && sr < RV) ? P[sr * SP + c]
-                                             : cvt<float, Tin>(img_s[(long long)my * nx + px + c], norm);
-                }
-                P[r * SP + c] = v;
+            for (int rr = tid >> 5; rr < top + bot; rr += nth >> 5) {
+                const int r = rr < top ? rr : RV - bot + (rr - top), code = src_row[r];
+                for (int c = lft + (tid & 31); c < lft + ncin; c += 32)
+                    P[r * SP + c] = code >= 0          ? P[code * SP + c]
+                                    : code == kSrcFill ? fill
+                                                       : cvt<float, Tin>(img_s[(long long)(-2 - code) * nx + px + c], norm);
             }
             __syncthreads();
+            // outside columns: 16 threads per row, rows in steps of nth / 16
             const int nco = lft + rgt;
-            for (int idx = tid; idx < RV * nco; idx += nth) {
-                const int r = idx / nco, cc = idx - r * nco;
-                const int c = cc < lft ? cc : CV - rgt + (cc - lft);
-                float v = fill;
-                const int mx = map_index(px + c, nx, style);
-                if (mx >= 0) {
-                    const int sc = mx - px;
-                    if (sc >= 0 && sc < CV) {
-                        v = P[r * SP + sc];
-                    } else {
-                        const int my = map_index(py + r, ny, style);
-                        v = my < 0 ? fill : cvt<float, Tin>(img_s[(long long)my * nx + mx], norm);
+            for (int r = tid >> 4; r < RV; r += nth >> 4) {
+                for (int cc = tid & 15; cc < nco; cc += 16) {
+                    const int c = cc < lft ? cc : CV - rgt + (cc - lft), code = src_col[c];
+                    float v = fill;
+                    if (code >= 0) {
+                        v = P[r * SP + code];
+                    } else if (code != kSrcFill) {
+                        const int rc = src_row[r];
+                        const int my = rc >= 0 ? py + rc : -2 - rc;
+                        if (rc != kSrcFill) v = cvt<float, Tin>(img_s[(long long)my * nx + (-2 - code)], norm);
                     }
+                    P[r * SP + c] = v;
                 }
-                P[r * SP + c] = v;
             }
         }
         fence_proxy_async();
@@ -555,13 +566,16 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         const int tx0 = px - fx, ty0 = py - fy;
         // interior output tiles store without bounds tests, by pointer steps
         const bool full = tx0 >= 0 && tx0 + TX <= nx && ty0 + TY <= ny;
+        // a tile at the right or bottom edge skips the items whose outputs all
+        // fall outside the image (the last tile column may hold 1-3 columns)
+        const int need_x = nx - tx0, need_y = ny - ty0;
         float acc[NB];
         if (x_first) {
-            // x pass over all RV rows -> I (pitch si)
+            // x pass over the RV rows -> I (pitch si)
             for (int it = tid; it < row_items(RV); it += nth) {
                 int r, c0;
                 row_item(it, RV, r, c0);
-                if (r >= RV) continue;
+                if (r >= RV || c0 >= need_x || r >= need_y + ky - 1) continue;
                 corr_row4<NB>(P + (size_t)r * SP + c0, wxs, kx, acc);
                 float4 *d = reinterpret_cast<float4 *>(I + (size_t)r * L.si + c0);
 #pragma unroll
@@ -575,6 +589,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             float2 ya[NBY];
             for (int it = tid; it < (TX / 2) * (TY / NBY); it += nth) {
                 const int rs = it / (TX / 2), c = 2 * (it - rs * (TX / 2)), r0 = rs * NBY;
+                if (c >= need_x || r0 >= need_y) continue;
                 corr_col_x2<NBY>(I + (size_t)r0 * L.si + c, L.si, wy, ky, ya);
                 const int x = tx0 + c;
                 if (full && pair_store) {
@@ -598,6 +613,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             float2 ya[NBY];
             for (int it = tid; it < ((CV + 1) >> 1) * (TY / NBY); it += nth) {
                 const int cp = (CV + 1) >> 1, rs = it / cp, c = 2 * (it - rs * cp), r0 = rs * NBY;
+                if (c >= need_x + kx - 1 || r0 >= need_y) continue;
                 corr_col_x2<NBY>(P + (size_t)r0 * SP + c, SP, wy, ky, ya);
 #pragma unroll
                 for (int i = 0; i < NBY; ++i) *reinterpret_cast<float2 *>(I + (size_t)(r0 + i) * L.si + c) = ya[i];
@@ -609,7 +625,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             for (int it = tid; it < row_items(TY); it += nth) {
                 int r, c0;
                 row_item(it, TY, r, c0);
-                if (r >= TY) continue;
+                if (r >= TY || r >= need_y || c0 >= need_x) continue;
                 corr_row4<NB>(I + (size_t)r * L.si + c0, wxs, kx, acc);
                 const int y = ty0 + r;
                 if (full) {
