@@ -204,6 +204,20 @@ static size_t sep2d_smem(int kx, int ky, int x_first)
     return (t + i + 2 * (IFX_MAX_TAPS + 3)) * sizeof(Tc);
 }
 
+// FP32 taps up to kCorrKmax: the unrolled chain with a fixed register per
+// window value; otherwise (FP64, longer factors) the sliding window.
+template <class Tc, int NB>
+__device__ __forceinline__ void corr_tc(const Tc *p, int step, const Tc *w, int k, Tc *acc)
+{
+    if constexpr (sizeof(Tc) == 4) {
+        if (k <= kCorrKmax) {
+            corr_col<NB>(p, step, w, k, acc);
+            return;
+        }
+    }
+    corr_run<Tc, NB>(p, step, w, k, acc);
+}
+
 template <class Tin, class Tc, class Tout>
 __global__ void __launch_bounds__(256)
 k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
@@ -228,14 +242,36 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
     const int RV = TY + ky - 1, CV = TX + kx - 1;   // valid (image-backed) part
     Tc *I = T + (size_t)RT * CT;
 
-    // 1. gather through the border map
-    gather_tile<8>(T, RT * CT, [&](int idx) -> Tc {
-        const int r = idx / CT, c = idx - r * CT;
-        if (r >= RV || c >= CV) return Tc(0);
-        const int mx = map_index(tx0 + fx + c, nx, style);
-        const int my = map_index(ty0 + fy + r, ny, style);
-        return (mx < 0 || my < 0) ? fill : cvt<Tc, Tin>(img[(long long)my * nx + mx], norm);
-    });
+    // 1. the input window: rows straight from the image when it lies inside
+    //    (a warp per row, four loads in flight per lane), else gathered
+    //    through the border map
+    if (tx0 + fx >= 0 && tx0 + fx + CV <= nx && ty0 + fy >= 0 && ty0 + fy + RV <= ny) {
+        const int lane = tid & 31, nw = nth >> 5;
+        for (int r = tid >> 5; r < RT; r += nw) {
+            const Tin *rp = img + (long long)(ty0 + fy + r) * nx + tx0 + fx;
+            for (int c0 = 0; c0 < CT; c0 += 128) {
+                Tc v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = c0 + lane + 32 * q;
+                    v[q] = (r < RV && c < CV) ? cvt<Tc, Tin>(rp[c], norm) : Tc(0);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = c0 + lane + 32 * q;
+                    if (c < CT) T[(size_t)r * CT + c] = v[q];
+                }
+            }
+        }
+    } else {
+        gather_tile<8>(T, RT * CT, [&](int idx) -> Tc {
+            const int r = idx / CT, c = idx - r * CT;
+            if (r >= RV || c >= CV) return Tc(0);
+            const int mx = map_index(tx0 + fx + c, nx, style);
+            const int my = map_index(ty0 + fy + r, ny, style);
+            return (mx < 0 || my < 0) ? fill : cvt<Tc, Tin>(img[(long long)my * nx + mx], norm);
+        });
+    }
     __syncthreads();
 
     Tc acc[NB];
@@ -245,7 +281,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         for (int it = tid; it < (TY + ky4) * segs; it += nth) {
             const int r = it / segs, c0 = (it - r * segs) * NB;
             if (r < RT) {
-                corr_run<Tc, NB>(T + (size_t)r * CT + c0, 1, wx, kx, acc);
+                corr_tc<Tc, NB>(T + (size_t)r * CT + c0, 1, wx, kx, acc);
 #pragma unroll
                 for (int i = 0; i < NB; ++i) I[(size_t)r * TX + c0 + i] = acc[i];
             } else {
@@ -258,7 +294,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         const int rsegs = TY / NB;
         for (int it = tid; it < TX * rsegs; it += nth) {
             const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
-            corr_run<Tc, NB>(I + (size_t)r0 * TX + c, TX, wy, ky, acc);
+            corr_tc<Tc, NB>(I + (size_t)r0 * TX + c, TX, wy, ky, acc);
             const int x = tx0 + c;
             if (x < nx) {
 #pragma unroll
@@ -275,7 +311,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         for (int it = tid; it < CI * rsegs; it += nth) {
             const int rs = it / CI, c = it - rs * CI, r0 = rs * NB;
             if (c < CT) {
-                corr_run<Tc, NB>(T + (size_t)r0 * CT + c, CT, wy, ky, acc);
+                corr_tc<Tc, NB>(T + (size_t)r0 * CT + c, CT, wy, ky, acc);
 #pragma unroll
                 for (int i = 0; i < NB; ++i) I[(size_t)(r0 + i) * CI + c] = acc[i];
             } else {
@@ -288,7 +324,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         const int segs = TX / NB;
         for (int it = tid; it < TY * segs; it += nth) {
             const int r = it / segs, c0 = (it - r * segs) * NB;
-            corr_run<Tc, NB>(I + (size_t)r * CI + c0, 1, wx, kx, acc);
+            corr_tc<Tc, NB>(I + (size_t)r * CI + c0, 1, wx, kx, acc);
             const int y = ty0 + r;
             if (y < ny) {
 #pragma unroll

@@ -65,7 +65,7 @@ def fill_value(kind, fill=0.7):
 def test_separable_2d_random(gpu_ifx, oracle, kind, style):
     ifx = gpu_ifx
     rng = np.random.default_rng(zlib.crc32((kind + style).encode()))
-    for shape in [(67, 45), (130, 7), (3, 200), (64, 64)]:
+    for shape in [(67, 45), (130, 7), (3, 200), (64, 64), (203, 301)]:   # 203: rows off the copy rules
         img = make_img(rng, shape, kind)
         for _ in range(3):
             lx, ly = int(rng.integers(1, 34)), int(rng.integers(1, 34))
