@@ -258,11 +258,11 @@ template <class Tout> struct OutTile {
         Tout *p = base + (long long)(ty0 + r0) * nx + x;
         if (full) {
 #pragma unroll
-            for (int i = 0; i < NB; ++i) p[(long long)i * nx] = out_cvt<Tout>(v[i]);
+            for (int i = 0; i < NB; ++i) p[(long long)i * nx] = out_cvt_alt<Tout>(v[i], i);
         } else if (x < nx) {
 #pragma unroll
             for (int i = 0; i < NB; ++i)
-                if (ty0 + r0 + i < ny) p[(long long)i * nx] = out_cvt<Tout>(v[i]);
+                if (ty0 + r0 + i < ny) p[(long long)i * nx] = out_cvt_alt<Tout>(v[i], i);
         }
     }
     // N outputs along row r from column c0
@@ -272,11 +272,11 @@ template <class Tout> struct OutTile {
         Tout *p = base + (long long)y * nx + tx0 + c0;
         if (full) {
 #pragma unroll
-            for (int i = 0; i < N; ++i) p[i] = out_cvt<Tout>(v[i]);
+            for (int i = 0; i < N; ++i) p[i] = out_cvt_alt<Tout>(v[i], i);
         } else if (y < ny) {
 #pragma unroll
             for (int i = 0; i < N; ++i)
-                if (tx0 + c0 + i < nx) p[i] = out_cvt<Tout>(v[i]);
+                if (tx0 + c0 + i < nx) p[i] = out_cvt_alt<Tout>(v[i], i);
         }
     }
 };

