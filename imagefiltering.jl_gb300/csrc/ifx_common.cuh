@@ -98,6 +98,7 @@ template <class To> __device__ __forceinline__ To out_cvt_alt(float v, int i)
     if constexpr (sizeof(To) == 8) return (i & 1) ? f32_to_f64(v) : (double)v;
     else return out_cvt<To>(v);
 }
+template <class To> __device__ __forceinline__ To out_cvt_alt(double v, int) { return (To)v; }
 
 __host__ __device__ __forceinline__ int up4(int k) { return (k + 3) & ~3; }
 

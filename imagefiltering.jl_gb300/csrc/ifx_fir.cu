@@ -300,7 +300,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
 #pragma unroll
                 for (int i = 0; i < NB; ++i) {
                     const int y = ty0 + r0 + i;
-                    if (y < ny) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
+                    if (y < ny) out[(long long)y * nx + x] = out_cvt_alt<Tout>(acc[i], i);
                 }
             }
         }
@@ -330,7 +330,7 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
 #pragma unroll
                 for (int i = 0; i < NB; ++i) {
                     const int x = tx0 + c0 + i;
-                    if (x < nx) out[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
+                    if (x < nx) out[(long long)y * nx + x] = out_cvt_alt<Tout>(acc[i], i);
                 }
             }
         }
@@ -670,12 +670,12 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 if (full) {
                     Tout *o = out_s + (long long)y * nx + tx0 + c0;
 #pragma unroll
-                    for (int i = 0; i < NB; ++i) o[i] = out_cvt<Tout>(acc[i]);
+                    for (int i = 0; i < NB; ++i) o[i] = out_cvt_alt<Tout>(acc[i], i);
                 } else if (y < ny) {
 #pragma unroll
                     for (int i = 0; i < NB; ++i) {
                         const int x = tx0 + c0 + i;
-                        if (x >= 0 && x < nx) out_s[(long long)y * nx + x] = out_cvt<Tout>(acc[i]);
+                        if (x >= 0 && x < nx) out_s[(long long)y * nx + x] = out_cvt_alt<Tout>(acc[i], i);
                     }
                 }
             }
