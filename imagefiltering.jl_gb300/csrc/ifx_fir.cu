@@ -680,7 +680,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 }
             }
         }
-        // I and T are rewritten by the next round
+        // I and T are rewritten by the next tile
         __syncthreads();
     }
 }

@@ -114,7 +114,7 @@ def test_borderinstance(ifx):
 def test_filter_type(ifx):
     kf = ifx.KernelFactors.gaussian((2, 2))
     kf32 = ifx.KernelFactors.gaussian((np.float32(2), np.float32(2)))
-    assert ifx.filter_type("F32", kf) == "F64"        # src/imfilter.jl:1133 (survey item 5)
+    assert ifx.filter_type("F32", kf) == "F64"        # src/imfilter.jl:1133
     assert ifx.filter_type("F32", kf32) == "F32"
     assert ifx.filter_type("N0F8", kf) == "F64"
     assert ifx.filter_type("U8", kf) == "F64"
@@ -134,7 +134,7 @@ def test_gaussian_weights(ifx):
     np.testing.assert_allclose(g.data, cmp(2, range(-4, 5)), rtol=1e-14)
     k = ifx.KernelFactors.gaussian((2, 3), (9, 7))
     np.testing.assert_allclose(k[1].data.data, cmp(3, range(-3, 4)), rtol=1e-14)
-    assert len(ifx.KernelFactors.gaussian(2).data) == 9        # 4*ceil(σ)+1 (survey item 4)
+    assert len(ifx.KernelFactors.gaussian(2).data) == 9        # 4*ceil(σ)+1, src/kernelfactors.jl:438-459
     assert abs(ifx.KernelFactors.gaussian(5).data.sum() - 1) < 1e-14
     k = ifx.KernelFactors.gaussian((3, 3, 0))
     assert list(k[2].data.data) == [1.0] and k[2].data.first == (0,)
