@@ -996,9 +996,9 @@ cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s)
 // (FP32x2 pairs), a warp 64 consecutive x of one row, a CTA 8 rows; the z
 // window goes through the border map (one map per plane, warp-uniform).
 // =========================================================================
-constexpr int kZNB = 8;
+constexpr int kZNB = 8, kZMax = 17;      // outputs per thread, longest z factor
 
-struct ZpassW { float wz[kCorrKmax]; };
+struct ZpassW { float wz[kZMax]; };
 
 template <class Tin, bool PAIR>
 __global__ void __launch_bounds__(256)
@@ -1006,7 +1006,7 @@ k_zpass(const Tin *__restrict__ img, float *__restrict__ out, int nx, int ny, in
         int style, float fill, bool norm, const __grid_constant__ ZpassW W)
 {
     constexpr int NB = kZNB;
-    __shared__ float2 w2[kCorrKmax];
+    __shared__ float2 w2[kZMax];
     const int tid = threadIdx.x;
     for (int t = tid; t < kz; t += blockDim.x) w2[t] = make_float2(W.wz[t], W.wz[t]);
     __syncthreads();
@@ -1030,16 +1030,17 @@ k_zpass(const Tin *__restrict__ img, float *__restrict__ out, int nx, int ny, in
             return make_float2(cvt<float, Tin>(p[0], norm), two ? cvt<float, Tin>(p[1], norm) : 0.0f);
         }
     };
-    float2 v[NB + kCorrKmax - 1], acc[NB];
+    // the whole window is loaded before any arithmetic: every load of the
+    // thread is in flight at once (the sweep is bound by their latency)
+    float2 v[NB + kZMax - 1], acc[NB];
 #pragma unroll
-    for (int i = 0; i < NB; ++i) {
-        v[i] = at(i);
-        acc[i] = make_float2(0.0f, 0.0f);
-    }
+    for (int j = 0; j < NB + kZMax - 1; ++j)
+        if (j < NB + kz - 1) v[j] = at(j);
 #pragma unroll
-    for (int t = 0; t < kCorrKmax; ++t) {
+    for (int i = 0; i < NB; ++i) acc[i] = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int t = 0; t < kZMax; ++t) {
         if (t >= kz) break;
-        if (t > 0) v[NB - 1 + t] = at(NB - 1 + t);
         const float2 w = w2[t];
 #pragma unroll
         for (int i = 0; i < NB; ++i) acc[i] = __ffma2_rn(w, v[i + t], acc[i]);
@@ -1106,7 +1107,7 @@ static Sep2dArgs sep3d_xy_args(const Sep3dArgs &a, const float *tmp)
 bool sep3d_split_applies(const Sep3dArgs &a)
 {
     if (!(a.in_type == IFX_F32 || is8(a.in_type)) || !(a.out_type == IFX_F32 || a.out_type == IFX_F64)) return false;
-    if (a.kz > kCorrKmax || a.kx > kCorrKmax || a.ky > kCorrKmax || a.nx % 4 != 0) return false;
+    if (a.kz > kZMax || a.kx > kCorrKmax || a.ky > kCorrKmax || a.nx % 4 != 0) return false;
     if ((long long)a.nx * a.ny * a.nz * a.nvol >= (1ll << 40)) return false;
     if ((long long)((a.nz + kZNB - 1) / kZNB) * a.nvol > 65535 || (a.ny + 7) / 8 > 65535) return false;
     // the FP32 volume of cudaMalloc is 256-byte aligned: probe the x/y sweep with such a base
