@@ -23,25 +23,6 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-bool tma_encode_2d(CUtensorMap *map, const void *base, int elt_bytes, long long nx, long long ny,
-                   long long pitch_bytes, int box_w, int box_h)
-{
-    if (elt_bytes != 1 && elt_bytes != 4) return false;
-    if (((uintptr_t)base & 15) || (pitch_bytes & 15) || pitch_bytes <= 0) return false;
-    if (nx <= 0 || ny <= 0 || nx > (1ll << 31) || ny > (1ll << 31)) return false;
-    if (box_w < 1 || box_w > 256 || box_h < 1 || box_h > 256 || (box_w * elt_bytes) % 16) return false;
-    auto fn = encode_fn();
-    if (!fn) return false;
-    cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
-    cuuint64_t strides[1] = {(cuuint64_t)pitch_bytes};
-    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
-    cuuint32_t estr[2] = {1, 1};
-    const CUtensorMapDataType dt = elt_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT8;
-    return fn(map, dt, 2, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 bool tma_encode_3d(CUtensorMap *map, const void *base, int elt_bytes, long long nx, long long ny, long long nz,
                    long long pitch_bytes, long long plane_bytes, int box_w, int box_h)
 {

@@ -1,27 +1,23 @@
-// ifx_tma.cuh -- Tensor Memory Accelerator helpers for sm_103a: 2-D tiled
-// bulk copies global -> shared completing on an mbarrier, with bounded waits.
+// ifx_tma.cuh -- Tensor Memory Accelerator helpers for sm_103a: tiled bulk
+// copies of 2-D boxes out of 3-D stacks of planes, global -> shared, completing
+// on an mbarrier, with bounded waits.
 //
 // A tiled copy's innermost coordinate times the element size must be a
-// multiple of 16 bytes; callers round the x coordinate down to that boundary,
-// copy a box wide enough to cover the rounding, and index from the remainder.
-// Only loads are issued (never a store or reduce), and a load box may reach
-// past the image on any side: those elements arrive as zeros and are never
-// read by the kernels.
+// multiple of 16 bytes; callers start every box on that boundary.  Only loads
+// are issued (never a store or reduce), and a load box may reach past the
+// image on any side: those elements arrive as zeros, and the kernels give the
+// ones their windows use the border's values before reading them.
 #pragma once
 #include <cuda.h>
 #include <cstdint>
 
 namespace ifx {
 
-// Encodes a 2-D row-major tensor map (x contiguous) over an image of nx x ny
-// elements of `elt_bytes` (1 or 4) with row pitch `pitch_bytes`, box
-// box_w x box_h.  Returns false when the image does not meet the copy engine's
-// rules (16-byte base and pitch, box limits) or the driver refuses.
-bool tma_encode_2d(CUtensorMap *map, const void *base, int elt_bytes, long long nx, long long ny,
-                   long long pitch_bytes, int box_w, int box_h);
-
-// The same over a stack of nz planes of ny rows (plane pitch `plane_bytes`),
-// box box_w x box_h x 1.
+// Encodes a 3-D tensor map over a stack of nz planes of ny rows of nx
+// elements of `elt_bytes` (1 or 4), row pitch `pitch_bytes`, plane pitch
+// `plane_bytes`, box box_w x box_h x 1.  Returns false when the image does not
+// meet the copy engine's rules (16-byte base and pitches, box limits) or the
+// driver refuses.
 bool tma_encode_3d(CUtensorMap *map, const void *base, int elt_bytes, long long nx, long long ny, long long nz,
                    long long pitch_bytes, long long plane_bytes, int box_w, int box_h);
 
@@ -85,18 +81,9 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity, 
     return false;
 }
 
-// Box (x, y) of `map` -> shared memory at `dst` (128-byte aligned), completing
-// `bytes` of transaction count on *bar.  x * element size must be a multiple
-// of 16 bytes.
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
-{
-    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
-                 "[%0], [%1, {%2, %3}], [%4];"
-                 :: "r"(smem_addr(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_addr(bar))
-                 : "memory");
-}
-
-// Box (x, y, z) of a 3-D `map` (box depth 1), as tma_load_2d.
+// Box (x, y, z) of a 3-D `map` (box depth 1) -> shared memory at `dst`
+// (128-byte aligned), completing the box's bytes of transaction count on
+// *bar.  x * element size must be a multiple of 16 bytes.
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar)
 {
     asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
