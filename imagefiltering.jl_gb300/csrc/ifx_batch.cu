@@ -59,7 +59,7 @@ enum { BOP_FACTORED = 1, BOP_GRADIENTS = 2, BOP_LAPLACIAN = 3, BOP_MEDIAN = 4 };
 // staging buffer of 64 rows x 400 bytes
 constexpr int kFTX = 64, kFTY = 32;        // factored (halo up to 32 x 32)
 constexpr int kGTX = 88, kGTY = 56;        // gradients / laplacian (halo 2 x 2); (88 + 2) * 4 + 15 <= kStagePitch
-constexpr int kMUX = 256, kMUY = 56;       // 8-bit median (4 pixels per thread and step)
+constexpr int kMUX = 256, kMUY = 56;       // 8-bit median
 constexpr int kMFX = 64, kMFY = 56;        // float median
 
 __host__ __device__ inline int bt_tile_w(int op, int in_type)
@@ -403,68 +403,108 @@ __device__ __forceinline__ int bt_win_index(const BReq &R, int x, int y, int i, 
     return my * R.nx + mx;
 }
 
+// Value of an 8-bit median code in the output eltype's domain: N0f8 -> c/255
+// (Float32), UInt8 -> c.
+__device__ __forceinline__ float code_value(uint32_t c, bool norm)
+{
+    return norm ? n0f8_to_f32(c) : (float)c;
+}
+
+// Median of the W x W window of output (x, y) read from the image through the
+// window-relative map (circular windows at the edges).
+template <int W>
+__device__ __forceinline__ uint32_t bt_median_u8_at(const BReq &R, int x, int y)
+{
+    const uint8_t *img = (const uint8_t *)R.in;
+    uint32_t v[W * W];
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+#pragma unroll
+        for (int i = 0; i < W; ++i) v[j * W + i] = img[bt_win_index(R, x, y, i, j, W / 2)];
+    net_sort<W * W, uint32_t>(v);
+    return v[(W * W - 1) / 2];
+}
+
+// Circular images: outputs of the tile whose windows leave the image wrap
+// inside window-intersect-image (copy_win!), not through the whole-image map
+// the tile was staged with.  After the tile's blocks are stored, the consumer
+// threads recompute those outputs one per thread, from the image (a per-block
+// test instead would stall every warp that holds one such block).
+template <class F>
+__device__ __forceinline__ void bt_circular_edges(const BReq &R, int tx0, int ty0, int tw, int th, int h, F one)
+{
+    if (R.style != IFX_CIRCULAR) return;
+    const EdgeRects E(tx0, ty0, tw, th, R.nx, R.ny, h, h, h, h);
+    if (E.count == 0) return;
+    ct_sync();                      // the blocks' stores of these outputs come first
+    for (int e = ct_id(); e < E.count; e += ct_n()) {
+        int x, y;
+        E.at(e, x, y);
+        one(x, y);
+    }
+}
+
 template <int W, class Tout>
 __device__ void bt_median_u8(const BReq &R, int tx0, int ty0, const Rows<uint8_t> &S)
 {
-    constexpr int h = W / 2;
     const int tid = ct_id();
+    const int nx = R.nx, ny = R.ny;
+    const bool norm = R.in_type == IFX_N0F8;
     const OutTile<Tout> O(R, R.out0, tx0, ty0, kMUX, kMUY);
-    for (int step = tid >> 5; step < kMUY * (kMUX / 128); step += ct_n() >> 5) {
-        const int ly = step % kMUY, lx = (step / kMUY) * 128 + (tid & 31) * 4;
-        const int x0 = tx0 + lx, y = ty0 + ly;
-        if (x0 >= R.nx || y >= R.ny) continue;
-        uint32_t w[W * W];
-        const bool edge = R.style == IFX_CIRCULAR &&
-                          (x0 < h || x0 + 3 >= R.nx - h || y < h || y >= R.ny - h);
-        // 3 x 3: shared column sorts.  (The 5 x 5 form of the standalone kernel
-        // measured slower here: under this kernel's 72-register budget it spills.)
-        if constexpr (W == 3) {
-            if (!edge) {
-                uint32_t A[3], B[3];
+    if constexpr (W == 5) {
+        // Blocks of 8 x BH outputs per thread: two 4 x BH blocks side by side,
+        // one in each 16-bit lane, through the generated 5 x 5 block network.
+        constexpr int BH = MedBlock<5>::BH, BX = kMUX / 8, NBLK = BX * (kMUY / BH);
+        for (int b = tid; b < NBLK; b += ct_n()) {
+            const int lx = (b % BX) * 8, ly = (b / BX) * BH;
+            if (tx0 + lx >= nx || ty0 + ly >= ny) continue;
+            uint32_t in[BH + 4][8], out[BH][4];
 #pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    const unsigned char *base = S.st + (ly + j) * kStagePitch;
-                    const int l = S.lead[ly + j];
-                    A[j] = load_word(base, l + lx);
-                    B[j] = load_word(base, l + lx + 4);
+            for (int r = 0; r < BH + 4; ++r) {
+                const int off = S.lead[ly + r] + lx, a = off & ~3;
+                const uint32_t *w = reinterpret_cast<const uint32_t *>(S.st + (ly + r) * kStagePitch + a);
+                const uint32_t w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
+                const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)(off & 3);
+                const uint32_t bytes[3] = {__byte_perm(w0, w1, sel), __byte_perm(w1, w2, sel),
+                                           __byte_perm(w2, w3, sel)};
+#pragma unroll
+                for (int c = 0; c < 8; ++c) in[r][c] = lanes_c_c4(bytes, c);
+            }
+            median_block4<5, CxU16x2>(in, out);
+#pragma unroll
+            for (int j = 0; j < BH; ++j) {
+                float v[8];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    v[q] = code_value(out[j][q] & 0xFFFFu, norm);
+                    v[q + 4] = code_value(out[j][q] >> 16, norm);
                 }
-                const uint32_t res = median3x3_u8x4(A, B);
-                float v[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) v[q] = S.lut[(res >> (8 * q)) & 0xFF];
-                O.template row<4>(lx, ly, v);
-                continue;
+                O.template row<8>(lx, ly + j, v);
             }
         }
-        if (!edge) {
+    } else {
+        for (int step = tid >> 5; step < kMUY * (kMUX / 128); step += ct_n() >> 5) {
+            const int ly = step % kMUY, lx = (step / kMUY) * 128 + (tid & 31) * 4;
+            if (tx0 + lx >= nx || ty0 + ly >= ny) continue;
+            // 3 x 3: shared column sorts
+            uint32_t A[3], B[3];
 #pragma unroll
-            for (int j = 0; j < W; ++j) {
+            for (int j = 0; j < 3; ++j) {
                 const unsigned char *base = S.st + (ly + j) * kStagePitch;
                 const int l = S.lead[ly + j];
-#pragma unroll
-                for (int i = 0; i < W; ++i) w[j * W + i] = load_word(base, l + lx + i);
+                A[j] = load_word(base, l + lx);
+                B[j] = load_word(base, l + lx + 4);
             }
-        } else {
-            const uint8_t *img = (const uint8_t *)R.in;
+            const uint32_t res = median3x3_u8x4(A, B);
+            float v[4];
 #pragma unroll
-            for (int j = 0; j < W; ++j)
-#pragma unroll
-                for (int i = 0; i < W; ++i) {
-                    uint32_t word = 0;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int x = x0 + q < R.nx ? x0 + q : R.nx - 1;
-                        word |= (uint32_t)img[bt_win_index(R, x, y, i, j, h)] << (8 * q);
-                    }
-                    w[j * W + i] = word;
-                }
+            for (int q = 0; q < 4; ++q) v[q] = code_value((res >> (8 * q)) & 0xFFu, norm);
+            O.template row<4>(lx, ly, v);
         }
-        const uint32_t res = median_u8x4<W * W>(w);
-        float v[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] = S.lut[(res >> (8 * q)) & 0xFF];
-        O.template row<4>(lx, ly, v);
     }
+    bt_circular_edges(R, tx0, ty0, kMUX, kMUY, W / 2, [&](int x, int y) {
+        ((Tout *)R.out0)[(long long)y * nx + x] = out_cvt<Tout>(code_value(bt_median_u8_at<W>(R, x, y), norm));
+    });
 }
 
 template <int W, class Tout>
@@ -472,6 +512,7 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Rows<float>
 {
     using SK = SortKey<float>;
     constexpr int h = W / 2, N = W * W;
+    const int nx = R.nx, ny = R.ny;
     // staged values -> order-preserving keys, in place, once per element
     for (int e = ct_id(); e < (kMFY + W - 1) * (kMFX + W - 1); e += ct_n()) {
         const int r = e / (kMFX + W - 1), c = e - r * (kMFX + W - 1);
@@ -479,28 +520,39 @@ __device__ void bt_median_f32(const BReq &R, int tx0, int ty0, const Rows<float>
         *reinterpret_cast<uint32_t *>(q) = SK::key(*q);
     }
     ct_sync();
-    for (int p = ct_id(); p < kMFX * kMFY; p += ct_n()) {
-        const int lx = p % kMFX, ly = p / kMFX, x = tx0 + lx, y = ty0 + ly;
-        if (x >= R.nx || y >= R.ny) continue;
-        const bool edge = R.style == IFX_CIRCULAR && (x < h || x >= R.nx - h || y < h || y >= R.ny - h);
-        uint32_t v[N];
-        if (!edge) {
+    // blocks of 4 x BH outputs per thread through the generated block network
+    constexpr int BH = MedBlock<W>::BH, BX = kMFX / 4, NBLK = BX * (kMFY / BH);
+    static_assert(kMFY % BH == 0, "whole blocks per tile");
+    const OutTile<Tout> O(R, R.out0, tx0, ty0, kMFX, kMFY);
+    for (int b = ct_id(); b < NBLK; b += ct_n()) {
+        const int lx = (b % BX) * 4, ly = (b / BX) * BH;
+        if (tx0 + lx >= nx || ty0 + ly >= ny) continue;
+        uint32_t in[BH + W - 1][W + 3], out[BH][4];
 #pragma unroll
-            for (int j = 0; j < W; ++j) {
-                const uint32_t *rowk = reinterpret_cast<const uint32_t *>(S.row(ly + j));
+        for (int r = 0; r < BH + W - 1; ++r) {
+            const uint32_t *rowk = reinterpret_cast<const uint32_t *>(S.row(ly + r)) + lx;
 #pragma unroll
-                for (int i = 0; i < W; ++i) v[j * W + i] = rowk[lx + i];
-            }
-        } else {
-            const float *img = (const float *)R.in;
-#pragma unroll
-            for (int j = 0; j < W; ++j)
-#pragma unroll
-                for (int i = 0; i < W; ++i) v[j * W + i] = SK::key(img[bt_win_index(R, x, y, i, j, h)]);
+            for (int c = 0; c < W + 3; ++c) in[r][c] = rowk[c];
         }
-        net_sort<N, uint32_t>(v);
-        ((Tout *)R.out0)[(long long)y * R.nx + x] = out_cvt<Tout>(SK::val(v[(N - 1) / 2]));
+        median_block4<W, CxKey32>(in, out);
+#pragma unroll
+        for (int j = 0; j < BH; ++j) {
+            float v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = SK::val(out[j][q]);
+            O.template row<4>(lx, ly + j, v);
+        }
     }
+    bt_circular_edges(R, tx0, ty0, kMFX, kMFY, h, [&](int x, int y) {
+        const float *img = (const float *)R.in;
+        uint32_t k[N];
+#pragma unroll
+        for (int jj = 0; jj < W; ++jj)
+#pragma unroll
+            for (int ii = 0; ii < W; ++ii) k[jj * W + ii] = SK::key(img[bt_win_index(R, x, y, ii, jj, h)]);
+        net_sort<N, uint32_t>(k);
+        ((Tout *)R.out0)[(long long)y * nx + x] = out_cvt<Tout>(SK::val(k[(N - 1) / 2]));
+    });
 }
 
 // Tile routine for the (element type, output type) pair of the request.

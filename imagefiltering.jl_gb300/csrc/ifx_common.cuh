@@ -65,6 +65,20 @@ template <class Tc> __device__ __forceinline__ Tc to_c(uint8_t v, bool norm)
     return norm ? (Tc)v / (Tc)255 : (Tc)v;
 }
 
+// N0f8 code c as Float32, c/255 correctly rounded, without a table or a
+// division: c is made exact from the mantissa bits of 2^23 + c, q = c * r
+// with r = fl(1/255), and one correction step q + (c - 255 q) r (Markstein's
+// correction of a quotient from a reciprocal; the residual c - 255 q is exact
+// in one fused multiply-add).  Checked against the correctly rounded quotient
+// for all 256 codes.
+__device__ __forceinline__ float n0f8_to_f32(uint32_t c)
+{
+    const float f = __fsub_rn(__uint_as_float(0x4B000000u | c), 8388608.0f);
+    const float r = 1.0f / 255.0f;
+    const float q = __fmul_rn(f, r);
+    return __fmaf_rn(__fmaf_rn(-q, 255.0f, f), r, q);
+}
+
 template <class To> __device__ __forceinline__ To from_c(float v) { return (To)v; }
 template <class To> __device__ __forceinline__ To from_c(double v) { return (To)v; }
 

@@ -22,6 +22,7 @@
 #include "ifx_internal.h"
 #include "ifx_select.cuh"
 #include <cstring>
+#include <type_traits>
 #include <utility>
 
 namespace ifx {
@@ -40,7 +41,7 @@ template <> __device__ __forceinline__ void store_sel<uint8_t>(void *out, int ou
                                                                uint8_t v, bool norm)
 {
     if (out_type == IFX_F32)
-        ((float *)out)[i] = norm ? __fdiv_rn((float)v, 255.0f) : (float)v;
+        ((float *)out)[i] = norm ? n0f8_to_f32(v) : (float)v;
     else if (out_type == IFX_F64)
         ((double *)out)[i] = norm ? __ddiv_rn((double)v, 255.0) : (double)v;
     else
@@ -88,6 +89,43 @@ __device__ __forceinline__ long long win_index2(int x, int y, int i, int j, int 
 __device__ __forceinline__ bool win_leaves(int x, int y, int f0, int f1, int w0, int w1, int nx, int ny)
 {
     return x + f0 < 0 || x + f0 + w0 > nx || y + f1 < 0 || y + f1 + w1 > ny;
+}
+
+// 8-bit median of the window of output (x, y) read from the image through
+// the window-relative map: the largest code v with #{window codes < v} < rank,
+// found bit by bit from the most significant.
+__device__ __forceinline__ uint32_t median_u8_direct(const uint8_t *img, int x, int y, int f0, int f1, int w0,
+                                                     int w1, int nx, int ny, int style)
+{
+    const int rank = (w0 * w1 + 1) / 2;
+    uint32_t res = 0;
+    for (int b = 7; b >= 0; --b) {
+        const uint32_t trial = res | (1u << b);
+        int cnt = 0;
+        for (int j = 0; j < w1; ++j)
+            for (int i = 0; i < w0; ++i) cnt += img[win_index2(x, y, i, j, f0, f1, w0, w1, nx, ny, style)] < trial;
+        if (cnt < rank) res = trial;
+    }
+    return res;
+}
+
+// Circular images: after a tile's outputs are stored, the outputs whose
+// windows leave the image (they wrap inside window-intersect-image, which the
+// tile gathered through the whole-image map does not hold) are recomputed,
+// shared evenly by the CTA's threads.  The condition is uniform in the CTA.
+template <class F>
+__device__ __forceinline__ void circular_edges(int style, int tx0, int ty0, int tw, int th, int nx, int ny, int f0,
+                                               int f1, int w0, int w1, F one)
+{
+    if (style != IFX_CIRCULAR) return;
+    const EdgeRects E(tx0, ty0, tw, th, nx, ny, -f0, f0 + w0 - 1, -f1, f1 + w1 - 1);
+    if (E.count == 0) return;
+    __syncthreads();
+    for (int e = threadIdx.x; e < E.count; e += blockDim.x) {
+        int x, y;
+        E.at(e, x, y);
+        one(x, y);
+    }
 }
 
 // =========================================================================
@@ -187,40 +225,16 @@ k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, in
     const int lx = (threadIdx.x & 31) * 4, ly = threadIdx.x >> 5;
     const int m = w0 * w1;
     const uint32_t rank4 = 0x01010101u * (uint32_t)((m + 1) / 2);
-    // circular windows that leave the image are read through the window-relative map
-    const int xw = tx0 + lx, yw = ty0 + ly;
-    const bool edge = style == IFX_CIRCULAR && yw < ny && xw < nx &&
-                      (win_leaves(xw, yw, f0, f1, w0, w1, nx, ny) ||
-                       win_leaves(min(xw + 3, nx - 1), yw, f0, f1, w0, w1, nx, ny));
-    auto word = [&](int j, int i) -> uint32_t {
-        if (!edge) return load_word(tile + (size_t)(ly + j) * CT, lx + i);
-        uint32_t wd = 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int x = min(xw + q, nx - 1);
-            wd |= (uint32_t)img[win_index2(x, yw, i, j, f0, f1, w0, w1, nx, ny, style)] << (8 * q);
-        }
-        return wd;
-    };
+    auto word = [&](int j, int i) -> uint32_t { return load_word(tile + (size_t)(ly + j) * CT, lx + i); };
     uint32_t res = 0;
-    if constexpr ((W0 == 3 && W1 == 3) || (W0 == 5 && W1 == 5)) {
-        if (!edge) {                                   // shared column sorts
-            uint32_t A[W0], B[W0];
+    if constexpr (W0 == 3 && W1 == 3) {               // shared column sorts
+        uint32_t A[W0], B[W0];
 #pragma unroll
-            for (int j = 0; j < W0; ++j) {
-                A[j] = word(j, 0);
-                B[j] = load_word(tile + (size_t)(ly + j) * CT, lx + 4);
-            }
-            if constexpr (W0 == 3) res = median3x3_u8x4(A, B);
-            else res = median5x5_u8x4(A, B);
-        } else {
-            uint32_t w[W0 * W1];
-#pragma unroll
-            for (int j = 0; j < W1; ++j)
-#pragma unroll
-                for (int i = 0; i < W0; ++i) w[j * W0 + i] = word(j, i);
-            res = median_u8x4<W0 * W1>(w);
+        for (int j = 0; j < W0; ++j) {
+            A[j] = word(j, 0);
+            B[j] = word(j, 4);
         }
+        res = median3x3_u8x4(A, B);
     } else if constexpr (W0 > 0 && W1 > 0) {
         // fixed window: byte-wise selection network (four windows per word)
         uint32_t w[W0 * W1];
@@ -248,6 +262,10 @@ k_median_u8(const uint8_t *__restrict__ img, void *out, int out_type, int nx, in
                                            (uint8_t)(res >> (8 * q)), norm);
         }
     }
+    circular_edges(style, tx0, ty0, kMedTX, kMedTY, nx, ny, f0, f1, w0, w1, [&](int xe, int ye) {
+        store_sel<uint8_t>(out, out_type, (long long)ye * nx + xe,
+                           (uint8_t)median_u8_direct(img, xe, ye, f0, f1, w0, w1, nx, ny, style), norm);
+    });
 }
 
 constexpr int kFmTX = 32, kFmTY = 8;
@@ -271,17 +289,144 @@ k_median_float(const T *__restrict__ img, void *out, int out_type, int nx, int n
     __syncthreads();
     const int lx = threadIdx.x % kFmTX, ly = threadIdx.x / kFmTX;
     const int x = tx0 + lx, y = ty0 + ly;
-    const bool edge = style == IFX_CIRCULAR && x < nx && y < ny &&
-                      win_leaves(x, y, f0, f1, W0, W1, nx, ny);
     K v[N];
 #pragma unroll
     for (int j = 0; j < W1; ++j)
 #pragma unroll
-        for (int i = 0; i < W0; ++i)
-            v[j * W0 + i] = edge ? SK::key(img[win_index2(x, y, i, j, f0, f1, W0, W1, nx, ny, style)])
-                                 : tile[(ly + j) * CT + lx + i];
+        for (int i = 0; i < W0; ++i) v[j * W0 + i] = tile[(ly + j) * CT + lx + i];
     net_sort<N, K>(v);
     if (x < nx && y < ny) store_sel<T>(out, out_type, (long long)y * nx + x, SK::val(v[(N - 1) / 2]), false);
+    circular_edges(style, tx0, ty0, kFmTX, kFmTY, nx, ny, f0, f1, W0, W1, [&](int xe, int ye) {
+        K u[N];
+#pragma unroll
+        for (int j = 0; j < W1; ++j)
+#pragma unroll
+            for (int i = 0; i < W0; ++i) u[j * W0 + i] = SK::key(img[win_index2(xe, ye, i, j, f0, f1, W0, W1, nx, ny, style)]);
+        net_sort<N, K>(u);
+        store_sel<T>(out, out_type, (long long)ye * nx + xe, SK::val(u[(N - 1) / 2]), false);
+    });
+}
+
+// =========================================================================
+// Square 3 x 3 and 5 x 5 medians, 2-D, through the generated block networks
+// (ifx_median_nets.cuh): each thread computes a block of 4 x BH adjacent
+// outputs from their shared footprint, sharing the column sorts and merges
+// between the block's windows.  Floats run on order-preserving integer keys
+// (Julia's isless order), 8-bit codes in the two 16-bit lanes of a word (two
+// blocks per thread).  Circular windows that leave the image are recomputed
+// afterwards through the window-relative map (circular_edges).
+// =========================================================================
+constexpr int kMbTX = 64, kMbTY = 32, kMbThreads = 128;
+
+template <class T, int W>
+__global__ void __launch_bounds__(kMbThreads)
+k_median_block(const T *__restrict__ img, void *out, int out_type, int nx, int ny, int f0, int f1, int style,
+               T fill)
+{
+    using SK = SortKey<T>;
+    using K = typename SK::K;
+    using CX = std::conditional_t<sizeof(K) == 4, CxKey32, CxKey64>;
+    constexpr int BH = MedBlock<W>::BH, CT = kMbTX + W - 1, RT = kMbTY + W - 1, N = W * W;
+    __shared__ K tile[RT * CT];
+    const int tx0 = blockIdx.x * kMbTX, ty0 = blockIdx.y * kMbTY;
+    gather_tile<8>(tile, RT * CT, [&](int idx) -> K {
+        const int r = idx / CT, c = idx - r * CT;
+        const int mx = map_index(tx0 + f0 + c, nx, style);
+        const int my = map_index(ty0 + f1 + r, ny, style);
+        return SK::key((mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx]);
+    });
+    __syncthreads();
+    constexpr int BX = kMbTX / 4, NBLK = BX * (kMbTY / BH);
+    for (int b = threadIdx.x; b < NBLK; b += kMbThreads) {
+        const int lx = (b % BX) * 4, ly = (b / BX) * BH;
+        const int x0 = tx0 + lx, y = ty0 + ly;
+        if (x0 >= nx || y >= ny) continue;
+        K in[BH + W - 1][W + 3], res[BH][4];
+#pragma unroll
+        for (int r = 0; r < BH + W - 1; ++r)
+#pragma unroll
+            for (int c = 0; c < W + 3; ++c) in[r][c] = tile[(ly + r) * CT + lx + c];
+        median_block4<W, CX>(in, res);
+#pragma unroll
+        for (int j = 0; j < BH; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (x0 + q < nx && y + j < ny)
+                    store_sel<T>(out, out_type, (long long)(y + j) * nx + x0 + q, SK::val(res[j][q]), false);
+    }
+    circular_edges(style, tx0, ty0, kMbTX, kMbTY, nx, ny, f0, f1, W, W, [&](int x, int ye) {
+        K v[N];
+#pragma unroll
+        for (int jj = 0; jj < W; ++jj)
+#pragma unroll
+            for (int ii = 0; ii < W; ++ii) v[jj * W + ii] = SK::key(img[win_index2(x, ye, ii, jj, f0, f1, W, W, nx, ny, style)]);
+        net_sort<N, K>(v);
+        store_sel<T>(out, out_type, (long long)ye * nx + x, SK::val(v[(N - 1) / 2]), false);
+    });
+}
+
+template <class T, int W>
+static cudaError_t median_block_t(const MedianArgs &a, cudaStream_t s)
+{
+    const int nx = a.n[0], ny = a.nd > 1 ? a.n[1] : 1;
+    dim3 grid((nx + kMbTX - 1) / kMbTX, (ny + kMbTY - 1) / kMbTY);
+    k_median_block<T, W><<<grid, kMbThreads, 0, s>>>((const T *)a.img, a.out, a.out_type, nx, ny, a.wfirst[0],
+                                                     a.nd > 1 ? a.wfirst[1] : 0, a.style, (T)a.fill);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// 8-bit 5 x 5: a CTA tile of 128 x 16 outputs, each thread two 4 x 1 blocks
+// side by side (outputs x0 .. x0+7 of one row), one per 16-bit lane.
+constexpr int kM5TX = 128, kM5TY = 16, kM5CT = kM5TX + 8, kM5RT = kM5TY + 4;
+
+__global__ void __launch_bounds__(256)
+k_median_u8_5x5(const uint8_t *__restrict__ img, void *out, int out_type, int nx, int ny, int f0, int f1,
+                int style, uint8_t fill, bool norm)
+{
+    __shared__ __align__(16) uint8_t tile[kM5RT * kM5CT];
+    const int tx0 = blockIdx.x * kM5TX, ty0 = blockIdx.y * kM5TY;
+    gather_tile<8>(tile, kM5RT * kM5CT, [&](int idx) -> uint8_t {
+        const int r = idx / kM5CT, c = idx - r * kM5CT;
+        if (c >= kM5TX + 4) return 0;
+        const int mx = map_index(tx0 + f0 + c, nx, style);
+        const int my = map_index(ty0 + f1 + r, ny, style);
+        return (mx < 0 || my < 0) ? fill : img[(long long)my * nx + mx];
+    });
+    __syncthreads();
+    const int lx = (threadIdx.x % (kM5TX / 8)) * 8, ly = threadIdx.x / (kM5TX / 8);
+    const int x0 = tx0 + lx, y = ty0 + ly;
+    if (x0 < nx && y < ny) {
+        uint32_t in[5][8], o[1][4];
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+            const uint32_t *w = reinterpret_cast<const uint32_t *>(tile + (ly + r) * kM5CT + lx);
+            const uint32_t bytes[3] = {w[0], w[1], w[2]};
+#pragma unroll
+            for (int c = 0; c < 8; ++c) in[r][c] = lanes_c_c4(bytes, c);
+        }
+        median_block4<5, CxU16x2>(in, o);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const uint32_t code = q < 4 ? (o[0][q] & 0xFFFFu) : (o[0][q - 4] >> 16);
+            if (x0 + q < nx) store_sel<uint8_t>(out, out_type, (long long)y * nx + x0 + q, (uint8_t)code, norm);
+        }
+    }
+    circular_edges(style, tx0, ty0, kM5TX, kM5TY, nx, ny, f0, f1, 5, 5, [&](int x, int yy) {
+        store_sel<uint8_t>(out, out_type, (long long)yy * nx + x,
+                           (uint8_t)median_u8_direct(img, x, yy, f0, f1, 5, 5, nx, ny, style), norm);
+    });
+}
+
+static cudaError_t median_u8_5x5_t(const MedianArgs &a, cudaStream_t s)
+{
+    const int nx = a.n[0], ny = a.nd > 1 ? a.n[1] : 1;
+    dim3 grid((nx + kM5TX - 1) / kM5TX, (ny + kM5TY - 1) / kM5TY);
+    k_median_u8_5x5<<<grid, 256, 0, s>>>((const uint8_t *)a.img, a.out, a.out_type, nx, ny, a.wfirst[0],
+                                         a.nd > 1 ? a.wfirst[1] : 0, a.style, (uint8_t)a.fill,
+                                         a.in_type == IFX_N0F8);
+    note_launch();
+    return cudaGetLastError();
 }
 
 template <class T, int W0, int W1>
@@ -340,7 +485,7 @@ cudaError_t launch_median(const MedianArgs &a, cudaStream_t s)
     if (u8 && a.nd <= 2 && m <= 255) {
         const int w0 = a.wlen[0], w1 = a.nd > 1 ? a.wlen[1] : 1;
         if (w0 == 3 && w1 == 3) return median_u8_t<3, 3>(a, s);
-        if (w0 == 5 && w1 == 5) return median_u8_t<5, 5>(a, s);
+        if (w0 == 5 && w1 == 5) return median_u8_5x5_t(a, s);
         if (w0 == 7 && w1 == 7) return median_u8_t<7, 7>(a, s);
         return median_u8_t<0, 0>(a, s);
     }
@@ -349,8 +494,8 @@ cudaError_t launch_median(const MedianArgs &a, cudaStream_t s)
     if (fast2d && (a.in_type == IFX_F32 || a.in_type == IFX_F64)) {
         const int w0 = a.wlen[0], w1 = a.nd > 1 ? a.wlen[1] : 1;
         const bool f32 = a.in_type == IFX_F32;
-        if (w0 == 3 && w1 == 3) return f32 ? median_float_t<float, 3, 3>(a, s) : median_float_t<double, 3, 3>(a, s);
-        if (w0 == 5 && w1 == 5) return f32 ? median_float_t<float, 5, 5>(a, s) : median_float_t<double, 5, 5>(a, s);
+        if (w0 == 3 && w1 == 3) return f32 ? median_block_t<float, 3>(a, s) : median_block_t<double, 3>(a, s);
+        if (w0 == 5 && w1 == 5) return f32 ? median_block_t<float, 5>(a, s) : median_block_t<double, 5>(a, s);
         if (w0 == 7 && w1 == 7) return f32 ? median_float_t<float, 7, 7>(a, s) : median_float_t<double, 7, 7>(a, s);
     }
     if (a.in_type == IFX_F32) return median_px_t<float>(a, s);

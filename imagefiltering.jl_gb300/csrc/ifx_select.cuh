@@ -5,8 +5,100 @@
 #include <cstdint>
 #include <utility>
 #include "ifx_common.cuh"
+#include "ifx_median_nets.cuh"
 
 namespace ifx {
+
+// Compare-exchange halves for the generated block networks: order-preserving
+// 32/64-bit keys, and 8-bit codes zero-extended into the two 16-bit lanes of a
+// word (two independent blocks per word, one lane-wise min or max each).
+struct CxKey32 {
+    using T = uint32_t;
+    static __device__ __forceinline__ T lo(T a, T b) { return min(a, b); }
+    static __device__ __forceinline__ T hi(T a, T b) { return max(a, b); }
+};
+struct CxKey64 {
+    using T = unsigned long long;
+    static __device__ __forceinline__ T lo(T a, T b) { return min(a, b); }
+    static __device__ __forceinline__ T hi(T a, T b) { return max(a, b); }
+};
+struct CxU16x2 {
+    using T = uint32_t;
+    static __device__ __forceinline__ T lo(T a, T b) { return __vminu2(a, b); }
+    static __device__ __forceinline__ T hi(T a, T b) { return __vmaxu2(a, b); }
+};
+
+// Rows of a 4-wide block of W x W medians: two for 3 x 3 windows, one for
+// 5 x 5 (whose two-row block needs more registers than the kernels that use
+// it can hold).
+template <int W> struct MedBlock {
+    static constexpr int BH = W == 3 ? 2 : 1;
+};
+
+// The W x W medians of a 4 x BH block of outputs from its (BH+W-1) x (W+3) footprint.
+template <int W, class CX>
+__device__ __forceinline__ void median_block4(const typename CX::T (&in)[MedBlock<W>::BH + W - 1][W + 3],
+                                              typename CX::T (&out)[MedBlock<W>::BH][4])
+{
+    static_assert(W == 3 || W == 5, "generated blocks: 3 x 3 and 5 x 5 windows");
+    if constexpr (W == 3) median3_block4x2<CX>(in, out);
+    else median5_block4x1<CX>(in, out);
+}
+
+// Outputs of a tile whose windows leave the image -- the tile's part of the
+// image minus the interior [hx0, nx-hx1) x [hy0, ny-hy1) -- as up to four
+// rectangles (rows above and below the interior, then columns left and right
+// of it), enumerated by one index so that the threads of a CTA share them
+// evenly.  Median windows that leave a circular image wrap inside
+// window-intersect-image (copy_win!), which a tile gathered through the
+// whole-image map does not hold: the tile kernels compute every output from
+// their tile and then recompute these few, one per thread.
+struct EdgeRects {
+    int x0[4], x1[4], y0[4], y1[4];
+    int count;
+
+    __device__ __forceinline__ EdgeRects(int tx0, int ty0, int tw, int th, int nx, int ny, int hx0, int hx1,
+                                         int hy0, int hy1)
+    {
+        const int X1 = min(tx0 + tw, nx), Y1 = min(ty0 + th, ny);
+        const int ym0 = max(ty0, hy0), ym1 = min(Y1, ny - hy1);
+        set(0, tx0, X1, ty0, min(Y1, hy0));                       // above
+        set(1, tx0, X1, max(max(ty0, ny - hy1), hy0), Y1);        // below
+        set(2, tx0, min(X1, hx0), ym0, ym1);                      // left
+        set(3, max(max(tx0, nx - hx1), hx0), X1, ym0, ym1);       // right
+        count = 0;
+        for (int k = 0; k < 4; ++k) count += (x1[k] - x0[k]) * (y1[k] - y0[k]);
+    }
+    __device__ __forceinline__ void set(int k, int a, int b, int c, int d)
+    {
+        const bool e = b <= a || d <= c;
+        x0[k] = a;
+        x1[k] = e ? a : b;
+        y0[k] = c;
+        y1[k] = e ? c : d;
+    }
+    // output e of the set (e < count)
+    __device__ __forceinline__ void at(int e, int &x, int &y) const
+    {
+        int k = 0;
+        for (; k < 3; ++k) {
+            const int n = (x1[k] - x0[k]) * (y1[k] - y0[k]);
+            if (e < n) break;
+            e -= n;
+        }
+        const int w = x1[k] - x0[k];
+        y = y0[k] + e / w;
+        x = x0[k] + e - (e / w) * w;
+    }
+};
+
+// Bytes c and c+4 of the 12 bytes b[0..2] as the two 16-bit lanes of a word.
+__device__ __forceinline__ uint32_t lanes_c_c4(const uint32_t (&b)[3], int c)
+{
+    const uint32_t lo = c < 4 ? b[0] : b[1], hi = c < 4 ? b[1] : b[2];
+    const int q = c & 3;
+    return __byte_perm(lo, hi, (uint32_t)(q | ((4 + q) << 8))) & 0x00FF00FFu;
+}
 
 __device__ __forceinline__ uint32_t load_word(const uint8_t *row, int col)
 {
@@ -182,68 +274,6 @@ __device__ __forceinline__ uint32_t median3x3_u8x4(const uint32_t (&A)[3], const
         const uint32_t hi = __vminu2(__vminu2(p[h][2], mid(p[h][2], p[h + 1][2])), p[h + 1][2]);
         const uint32_t md = med3_u16x2(p[h][1], mid(p[h][1], p[h + 1][1]), p[h + 1][1]);
         r[h] = med3_u16x2(lo, md, hi);
-    }
-    return __byte_perm(r[0], r[1], 0x6420);
-}
-
-// 5 x 5 medians of four horizontally adjacent windows.  A[j] / B[j] hold
-// columns 0..3 / 4..7 of window row j; output q's window is columns q..q+4.
-// Every column's five values are sorted once (Batcher's network for five, in
-// 16-bit lanes, shared by the windows that contain the column); the median of
-// a window is then selected from its five sorted columns by a 63-comparator
-// network.  That network was derived offline for this purpose: sorting the
-// ranks across the columns and taking the median of the 13 elements of a
-// rows-and-columns-sorted 5 x 5 array that can hold rank 13 (those with
-// (c+1)(r+1) <= 13 and (5-c)(5-r) <= 13) is exact, and greedy removal of
-// comparators from that composite, checked after each removal against all
-// 6^5 column-sorted 0-1 inputs (0-1 principle), left these 63 (102 live
-// min/max operations against 202 for the pruned 25-input Batcher network).
-// Wire c*5 + r is column c, rank r (0 = smallest); the median is wire 12.
-struct Med25 {
-    static constexpr int n = 63;
-    static constexpr unsigned char a[63] = {0, 10, 0, 5, 5, 10, 15, 1, 1, 6, 1, 11, 6, 16, 2, 12, 2, 7, 7, 2, 12, 7, 17, 3, 13, 3, 8, 8, 3, 13, 8, 4, 14, 4, 9, 14, 9, 9, 15, 17, 3, 4, 9, 11, 4, 11, 4, 7, 8, 7, 8, 8, 11, 16, 20, 4, 8, 9, 11, 12, 8, 12, 11};
-    static constexpr unsigned char b[63] = {5, 15, 10, 15, 10, 20, 20, 6, 11, 16, 21, 21, 11, 21, 7, 17, 12, 17, 12, 22, 22, 12, 22, 8, 18, 13, 18, 13, 23, 23, 13, 9, 19, 14, 19, 24, 14, 11, 16, 20, 7, 8, 12, 13, 7, 12, 11, 12, 13, 9, 11, 9, 12, 17, 21, 16, 20, 15, 16, 17, 11, 15, 12};
-};
-
-template <int I> __device__ __forceinline__ void med25_cx(uint32_t (&v)[25])
-{
-    constexpr int x = Med25::a[I];
-    constexpr int y = Med25::b[I];
-    const uint32_t lo = __vminu2(v[x], v[y]);
-    const uint32_t hi = __vmaxu2(v[x], v[y]);
-    v[x] = lo;
-    v[y] = hi;
-}
-
-template <size_t... I> __device__ __forceinline__ void med25_apply(uint32_t (&v)[25], std::index_sequence<I...>)
-{
-    (med25_cx<(int)I>(v), ...);
-}
-
-__device__ __forceinline__ uint32_t median5x5_u8x4(const uint32_t (&A)[5], const uint32_t (&B)[5])
-{
-    uint32_t p[4][5];                            // [column pair 01, 23, 45, 67][sorted rank]
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-        p[0][j] = __byte_perm(A[j], 0u, 0x4140);
-        p[1][j] = __byte_perm(A[j], 0u, 0x4342);
-        p[2][j] = __byte_perm(B[j], 0u, 0x4140);
-        p[3][j] = __byte_perm(B[j], 0u, 0x4342);
-    }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) net_apply_u16x2<5>(p[k], std::make_index_sequence<NetOf<5>::net.n>{});
-    auto mid = [](uint32_t x, uint32_t y) { return __byte_perm(x, y, 0x5432); };
-    uint32_t r[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {                // outputs (0, 1), then (2, 3)
-        uint32_t v[25];
-#pragma unroll
-        for (int i = 0; i < 5; ++i)              // window column slot i: columns (2h+i, 2h+i+1)
-#pragma unroll
-            for (int k = 0; k < 5; ++k)
-                v[i * 5 + k] = (i & 1) ? mid(p[h + (i - 1) / 2][k], p[h + (i + 1) / 2][k]) : p[h + i / 2][k];
-        med25_apply(v, std::make_index_sequence<Med25::n>{});
-        r[h] = v[12];
     }
     return __byte_perm(r[0], r[1], 0x6420);
 }

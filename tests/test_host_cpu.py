@@ -235,45 +235,6 @@ def test_median_network_49_random():
         assert v == sorted(v)
 
 
-def _med25_table():
-    """The Med25 comparator table of csrc/ifx_select.cuh."""
-    import os
-    import re
-    src = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "imagefiltering.jl_gb300", "csrc",
-                            "ifx_select.cuh")).read()
-    body = src[src.index("struct Med25"):]
-    a = [int(x) for x in re.search(r"a\[63\] = \{([^}]*)\}", body).group(1).split(",")]
-    b = [int(x) for x in re.search(r"b\[63\] = \{([^}]*)\}", body).group(1).split(",")]
-    return list(zip(a, b))
-
-
-def test_median5x5_network_on_sorted_columns():
-    """The 5x5 selection network takes five sorted columns (wire c*5 + r, r = 0
-    the smallest) and leaves the median on wire 12: exhaustive over every
-    column-sorted 0-1 input (0-1 principle), then random integer windows."""
-    import itertools
-    net = _med25_table()
-    assert len(net) == 63
-    cases = list(itertools.product(range(6), repeat=5))
-    wires = [np.zeros(len(cases), dtype=bool) for _ in range(25)]
-    for n, ts in enumerate(cases):
-        for c, t in enumerate(ts):
-            for r in range(5):
-                wires[c * 5 + r][n] = r >= 5 - t
-    ones = sum(w.astype(int) for w in wires)
-    for a, b in net:
-        wires[a], wires[b] = wires[a] & wires[b], wires[a] | wires[b]
-    assert np.array_equal(wires[12], ones >= 13)
-    rng = np.random.default_rng(5)
-    for _ in range(3000):
-        win = rng.integers(0, 12, (5, 5))
-        v = [int(x) for c in range(5) for x in sorted(win[:, c])]
-        for a, b in net:
-            if v[a] > v[b]:
-                v[a], v[b] = v[b], v[a]
-        assert v[12] == sorted(win.ravel())[12]
-
-
 def test_median3x3_sorted_column_identity():
     """med3(max of column minima, med3 of column middles, min of column
     maxima) is the median of a 3x3 window: all 0-1 windows, then random."""
