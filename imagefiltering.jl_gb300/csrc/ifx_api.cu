@@ -620,6 +620,27 @@ int factored_prepare(const ifx_array_t *out, const ifx_array_t *img, int32_t nfa
 
 bool is_device_array(const void *p) { return is_device_ptr(p); }
 
+int check_device_array(const ifx_array_t &a, int device, const char *name)
+{
+    const void *p = a.data;
+    const size_t bytes = (size_t)numel(a) * elsize(a.eltype);
+    cudaPointerAttributes attr;
+    if (!p || cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(IFX_ERR_ARGUMENT, "%s: device arrays only (host arrays would need staging buffers)", name);
+    }
+    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+        return fail(IFX_ERR_ARGUMENT, "%s: device arrays only (host arrays would need staging buffers)", name);
+    if (attr.type == cudaMemoryTypeDevice && attr.device != device)
+        return fail(IFX_ERR_ARGUMENT, "%s lives on device %d but device %d is current: make the array's "
+                    "device current before the call", name, attr.device, device);
+    DevRanges r;
+    if (!r.holds(p, bytes))
+        return fail(IFX_ERR_ARGUMENT, "%s: the array's %zu bytes run past the end of its device allocation",
+                    name, bytes);
+    return IFX_OK;
+}
+
 } // namespace ifx
 
 using namespace ifx;

@@ -225,6 +225,9 @@ int generic_cascade_run(cudaStream_t s, const ifx_array_t &imgd, const void *img
                         const ifx_array_t &outd, void *out, const std::vector<Fac> &facs, int style,
                         double fill, void *bufA, void *bufB);
 bool is_device_array(const void *p);
+// IFX_OK when the array's bytes are device (or managed) memory inside one
+// allocation and, for device memory, on `device`; IFX_ERR_ARGUMENT otherwise.
+int check_device_array(const ifx_array_t &a, int device, const char *name);
 
 // Batched engine -------------------------------------------------------------
 struct BatchItem {                         // one validated 2-D request, device pointers

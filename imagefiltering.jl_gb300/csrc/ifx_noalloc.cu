@@ -14,8 +14,10 @@
 // buffers).
 //
 // Set-up: the first call on a device, with that device current, looks up the
-// array's device address once (cudaGetSymbolAddress) and keeps it; make that
-// first call before any stream capture starts.  All calls on a device share
+// array's device address (cudaGetSymbolAddress) and keeps it; make that first
+// call before any stream capture starts.  A failed look-up is not kept: the
+// next call tries again.  The arrays (and the stream, if one is given) must
+// belong to the current device, since the scratch used is that device's.  All calls on a device share
 // the one array and leave the last call's contents in it.  Nothing needs to
 // start at zero: the pipeline writes every scratch element before reading it.
 // Calls whose work overlaps on the GPU (different streams, or the same array
@@ -31,32 +33,27 @@ constexpr size_t kNoAllocScratchBytes = 32u << 20;     // 32 MiB per device
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 constexpr int kMaxDevices = 64;
-static std::once_flag g_setup_once[kMaxDevices];
+static std::mutex g_setup_mu;
 static void *g_scratch_addr[kMaxDevices];
-static cudaError_t g_setup_err[kMaxDevices];
 
-// Device address of g_noalloc_scratch on the current device.  In host code
-// the symbol's name only stands for the array; the kernels need this address.
-static int scratch_address(void **addr)
+// Device address of g_noalloc_scratch on device `dev` (the current device).
+// In host code the symbol's name only stands for the array; the kernels need
+// this address.  Only a successful look-up is kept.
+static int scratch_address(int dev, void **addr)
 {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        char m[160];
-        snprintf(m, sizeof m, "cudaGetDevice failed: %s", cudaGetErrorString(e));
-        return set_error(IFX_ERR_CUDA, m);
-    }
     if (dev < 0 || dev >= kMaxDevices) return set_error(IFX_ERR_UNSUPPORTED, "device ordinal out of range");
-    std::call_once(g_setup_once[dev], [dev] {
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    if (!g_scratch_addr[dev]) {
         void *p = nullptr;
-        g_setup_err[dev] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            (void)cudaGetLastError();
+            char m[260];
+            snprintf(m, sizeof m, "cudaGetSymbolAddress of the fixed scratch failed on device %d: %s (make "
+                     "the first call on a device outside stream capture)", dev, cudaGetErrorString(e));
+            return set_error(IFX_ERR_CUDA, m);
+        }
         g_scratch_addr[dev] = p;
-    });
-    if (g_setup_err[dev] != cudaSuccess || !g_scratch_addr[dev]) {
-        char m[200];
-        snprintf(m, sizeof m, "cudaGetSymbolAddress of the fixed scratch failed on device %d: %s", dev,
-                 cudaGetErrorString(g_setup_err[dev]));
-        return set_error(IFX_ERR_CUDA, m);
     }
     *addr = g_scratch_addr[dev];
     return IFX_OK;
@@ -84,10 +81,28 @@ int ifx_imfilter_factored_noalloc(ifx_array_t *out, const ifx_array_t *img, int3
         if (f.len > IFX_MAX_TAPS)           // longer factors need a device weight buffer
             return set_error(IFX_ERR_UNSUPPORTED, "the allocation-free entry point takes factors of up to "
                                                   "129 taps (IFX_MAX_TAPS)");
-    if (!is_device_array(img->data) || !is_device_array(out->data))
-        return set_error(IFX_ERR_ARGUMENT, "the allocation-free entry point takes device arrays only "
-                                           "(host arrays would need staging buffers)");
+    int dev = -1;
+    cudaError_t ge = cudaGetDevice(&dev);
+    if (ge != cudaSuccess) {
+        char m[160];
+        snprintf(m, sizeof m, "cudaGetDevice failed: %s", cudaGetErrorString(ge));
+        return set_error(IFX_ERR_CUDA, m);
+    }
+    if ((rc = check_device_array(*img, dev, "img")) || (rc = check_device_array(*out, dev, "out")))
+        return rc;
     const cudaStream_t s = (cudaStream_t)stream;
+    if (s) {
+        int sdev = -1;
+        if (cudaStreamGetDevice(s, &sdev) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return set_error(IFX_ERR_ARGUMENT, "stream: not a valid CUDA stream");
+        }
+        if (sdev != dev) {
+            char m[160];
+            snprintf(m, sizeof m, "the stream belongs to device %d but device %d is current", sdev, dev);
+            return set_error(IFX_ERR_ARGUMENT, m);
+        }
+    }
     if (facs.empty()) {                          // copy kernels only: a conversion, no scratch
         PadBoxArgs pa;
         pa.img = img->data;
@@ -117,7 +132,7 @@ int ifx_imfilter_factored_noalloc(ifx_array_t *out, const ifx_array_t *img, int3
         return set_error(IFX_ERR_NOMEM, m);
     }
     void *base = nullptr;
-    if ((rc = scratch_address(&base))) return rc;
+    if ((rc = scratch_address(dev, &base))) return rc;
     unsigned char *bufA = (unsigned char *)base;
     unsigned char *bufB = need_b ? bufA + a_bytes : nullptr;
     return generic_cascade_run(s, *img, img->data, *out, out->data, facs, border->style, fill, bufA, bufB);
