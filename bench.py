@@ -23,6 +23,7 @@ import argparse
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -99,7 +100,7 @@ class Clocks:
     def __init__(self, dev):
         self.dev = dev
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        self.path = os.path.join(tempfile.gettempdir(), "ifx_clocks_bench_%d.csv" % os.getpid())
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)

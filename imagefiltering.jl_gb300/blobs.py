@@ -5,6 +5,7 @@ and formats the results as the reference does.
 """
 import ctypes as C
 import math
+from collections.abc import Sequence
 
 import numpy as np
 
@@ -37,6 +38,37 @@ class BlobLoG:
     def __repr__(self):
         return "BlobLoG(location=CartesianIndex%s, σ=%s, amplitude=%r)" % (
             self.location if len(self.location) > 1 else "(%d,)" % self.location[0], self.sigma, self.amplitude)
+
+
+class BlobList(Sequence):
+    """The blobs of one blob_LoG call, kept as arrays (1-based locations, scale
+    indices, amplitudes); a BlobLoG is built only when an element is read, so
+    finding thousands of blobs costs no per-blob host objects."""
+
+    def __init__(self, locations, scales, amplitudes, sigmas):
+        self.locations = locations              # (n, N) int64, 1-based
+        self.scales = scales                    # (n,) index into sigmas
+        self.amplitudes = amplitudes            # (n,) float64
+        self.sigmas = sigmas                    # per-scale sigma tuples
+
+    def __len__(self):
+        return int(self.amplitudes.size)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self[j] for j in range(*i.indices(len(self)))]
+        if i < 0:
+            i += len(self)
+        if not 0 <= i < len(self):
+            raise IndexError(i)
+        return BlobLoG._fast(tuple(int(v) for v in self.locations[i]), self.sigmas[int(self.scales[i])],
+                             float(self.amplitudes[i]))
+
+    def __eq__(self, other):
+        return list(self) == list(other)
+
+    def __repr__(self):
+        return "BlobList(%d blobs)" % len(self)
 
 
 def _desc(a, kind):
@@ -183,10 +215,9 @@ def blob_LoG(img, sigmas, edges=None, sigma_shape=None, rthresh=0.001):
     else:
         keep = np.ones(vals.size, dtype=bool)
     sel = np.nonzero(keep)[0]
-    locs = map(tuple, (np.stack([c[sel] for c in coords[1:]], axis=1) + 1).tolist())
+    locs = np.stack([c[sel] for c in coords[1:]], axis=1).astype(np.int64) + 1
     sigt = [tuple(s * f for f in shape) for s in sig]
-    return [BlobLoG._fast(loc, sigt[k], v)
-            for loc, k, v in zip(locs, coords[0][sel].tolist(), vals[sel].tolist())]
+    return BlobList(locs, coords[0][sel], vals[sel].astype(np.float64), sigt)
 
 
-__all__ = ["BlobLoG", "blob_LoG", "multiLoG", "findlocalmaxima", "findlocalminima", "log_terms"]
+__all__ = ["BlobLoG", "BlobList", "blob_LoG", "multiLoG", "findlocalmaxima", "findlocalminima", "log_terms"]

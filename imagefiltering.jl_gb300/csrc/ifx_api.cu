@@ -658,7 +658,7 @@ uint64_t ifx_launch_count(void) { return g_launches.load(); }
 
 int ifx_create(ifx_context_t **ctx, int device)
 {
-    IFX_RANGE("ifx_abi_version");
+    IFX_RANGE("ifx_create");
     if (!ctx) return fail(IFX_ERR_ARGUMENT, "ctx is NULL");
     *ctx = nullptr;
     int ndev = 0;

@@ -4,8 +4,8 @@
 The reference is Julia and cannot run here, so its golden tables are read as
 text from its test files and parsed with a small Julia-literal reader.  The
 JSON this writes is committed; this script is the record of how it was made
-and needs the reference source tree (default: /root/reference; override with
-the first command-line argument).  Tests never read the reference tree.
+and needs the reference source tree, whose path is its one command-line
+argument.  Tests never read the reference tree.
 
 Tables extracted (paths relative to the reference tree):
   * test/border.jl   -- every ``padarray(A, <border>) == OffsetArray([...], offs)``
@@ -23,7 +23,9 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: extract_reference_kats.py <ImageFiltering.jl source tree>")
+REF = sys.argv[1]
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
 
 
