@@ -71,9 +71,13 @@ template <class Tc> __device__ __forceinline__ Tc to_c(uint8_t v, bool norm)
 // correction of a quotient from a reciprocal; the residual c - 255 q is exact
 // in one fused multiply-add).  Checked against the correctly rounded quotient
 // for all 256 codes.
+__device__ __forceinline__ float u8_to_f32(uint32_t c)
+{
+    return __fsub_rn(__uint_as_float(0x4B000000u | c), 8388608.0f);     // (2^23 + c) - 2^23
+}
 __device__ __forceinline__ float n0f8_to_f32(uint32_t c)
 {
-    const float f = __fsub_rn(__uint_as_float(0x4B000000u | c), 8388608.0f);
+    const float f = u8_to_f32(c);
     const float r = 1.0f / 255.0f;
     const float q = __fmul_rn(f, r);
     return __fmaf_rn(__fmaf_rn(-q, 255.0f, f), r, q);
