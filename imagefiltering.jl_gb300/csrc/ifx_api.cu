@@ -1142,6 +1142,14 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
     void *dout;
     if ((rc = c.input(*img, &din)) || (rc = c.output(*out, &dout, which == 0 ? 2 * N * es : 0)))
         return rc;
+    if (nd == 2 && (img->eltype == IFX_N0F8 || img->eltype == IFX_U8) && wl[0] == wl[1] && a0[0] == a0[1]) {
+        cudaError_t e;
+        if (launch_extrema2d_u8(din, dout, (int)img->size[0], (int)img->size[1], wl[0], a0[0], use_fill, fill,
+                                which, c.s, &e)) {
+            IFX_CUDA(e);
+            return c.finish();
+        }
+    }
     void *planes[4] = {nullptr, nullptr, nullptr, nullptr};
     if (nd > 1)
         for (int i = 0; i < (nd > 2 ? 4 : 2); ++i)

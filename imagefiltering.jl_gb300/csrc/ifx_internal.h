@@ -214,6 +214,11 @@ struct ExtremaPassArgs {                   // one separable min/max pass along `
     int want_min, want_max;
 };
 cudaError_t launch_extrema_pass(const ExtremaPassArgs &a, cudaStream_t s);
+// 8-bit 2-D extrema of square w x w windows (first offset a0 on both axes) in
+// one launch; false when w has no compiled tile kernel.  which: 0 interleaved
+// (min, max), 1 min, 2 max.
+bool launch_extrema2d_u8(const void *img, void *out, int nx, int ny, int w, int a0, int use_fill, double fill,
+                         int which, cudaStream_t s, cudaError_t *e);
 
 // Separable cascade, generic pipeline (shared with the fixed-scratch entry) ---
 struct Fac { int axis, first, len; const double *w; };

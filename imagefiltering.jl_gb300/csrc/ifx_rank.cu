@@ -668,6 +668,211 @@ static bool extrema_vhgw_u8(const ExtremaPassArgs &a, cudaStream_t s, cudaError_
     return true;
 }
 
+// =========================================================================
+// 8-bit running min and max of square W x W windows, 2-D, both axes in one
+// launch.  A CTA stages its tile plus halo in shared memory with coordinates
+// clamped to the image: a window truncated at an edge holds the edge value
+// whenever it would reach past it (windows contain their output), so
+// clamping gives exactly the truncated-window extrema (and with them every
+// Pad style, see the pass kernel above).  The x pass runs van Herk /
+// Gil-Werman on runs of W outputs (one segment: suffix extrema of the run's
+// W inputs, prefix extrema of the next W-1, one combine per output) with two
+// rows in the 16-bit lanes of a word; the y pass does the same down column
+// pairs.  A Fill value joins the outputs whose window leaves the image along
+// the pass's axis.  Outputs: interleaved (min, max) codes, or one of them.
+// =========================================================================
+template <int W> struct ExTile {
+    static constexpr int NRX = ((128 + W - 1) / W + 1) & ~1;   // runs per row (even: even tile width)
+    static constexpr int NRY = (32 + W / 2) / W;               // runs per column (tiles about 32 tall)
+    static constexpr int TX = W * NRX, TY = W * NRY;
+    static constexpr int R = TY + W - 1, C = TX + W - 1;
+    static constexpr int RP = (R + 1) & ~1;                    // rows staged (even: row pairs)
+    static constexpr int CP = (C + 3) & ~3;
+};
+
+// Van Herk / Gil-Werman over a run: out[i] = op over v[i .. i+W-1], i < W,
+// from v[0 .. 2W-2] (two independent 16-bit lanes per word).
+template <int W, bool MAX>
+__device__ __forceinline__ void vhgw_run(const uint32_t (&v)[2 * W - 1], uint32_t (&out)[W])
+{
+    auto op = [](uint32_t a, uint32_t b) { return MAX ? __vmaxu2(a, b) : __vminu2(a, b); };
+    out[W - 1] = v[W - 1];
+#pragma unroll
+    for (int j = W - 2; j >= 0; --j) out[j] = op(v[j], out[j + 1]);   // suffix extrema of the run
+    uint32_t g = v[W];
+#pragma unroll
+    for (int i = 1; i < W; ++i) {                                       // prefix extrema of the next W-1
+        out[i] = op(out[i], g);
+        if (i + 1 < W) g = op(g, v[W + i]);
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(256, W <= 9 ? 6 : 4)
+k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int nx, int ny, int a0, int use_fill,
+               uint32_t fill, int which)
+{
+    using G = ExTile<W>;
+    __shared__ __align__(16) uint8_t xin[G::RP * G::CP];
+    __shared__ __align__(16) uint8_t xmn[G::RP * G::TX];
+    __shared__ __align__(16) uint8_t xmx[G::RP * G::TX];
+    const int tx0 = blockIdx.x * G::TX, ty0 = blockIdx.y * G::TY;
+    {   // a warp per staged row, four columns per lane (one 32-bit shared store);
+        // a warp's loads for up to four rows are in flight before it stores
+        constexpr int kChunks = (G::CP + 127) / 128;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int r0 = warp; r0 < G::RP; r0 += 4 * nw) {
+            uint32_t word[4][kChunks];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int r = r0 + q * nw;
+                const uint8_t *row = img + (long long)min(max(ty0 + a0 + r, 0), ny - 1) * nx;
+#pragma unroll
+                for (int k = 0; k < kChunks; ++k) {
+                    const int c = 4 * lane + 128 * k, x = tx0 + a0 + c;
+                    uint32_t wv = 0;
+                    if (r < G::RP && c < G::CP) {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) wv |= (uint32_t)__ldg(row + min(max(x + j, 0), nx - 1)) << (8 * j);
+                    }
+                    word[q][k] = wv;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int k = 0; k < kChunks; ++k) {
+                    const int r = r0 + q * nw, c = 4 * lane + 128 * k;
+                    if (r < G::RP && c < G::CP) *reinterpret_cast<uint32_t *>(xin + r * G::CP + c) = word[q][k];
+                }
+        }
+    }
+    __syncthreads();
+    const uint32_t fill2 = fill * 0x00010001u;
+    // x pass: row pairs (r, r+1) x runs of W outputs
+    for (int it = threadIdx.x; it < (G::RP / 2) * G::NRX; it += blockDim.x) {
+        const int rp = it / G::NRX, run = it - rp * G::NRX, r = 2 * rp, c0 = run * W;
+        // bytes c0 .. c0+2W-2 of rows r and r+1, read as aligned words
+        constexpr int NWD = (2 * W - 1 + 3) / 4 + 1;
+        const int a = c0 & ~3, sh = c0 & 3;
+        uint32_t ra[NWD], rb[NWD];
+#pragma unroll
+        for (int q = 0; q < NWD; ++q) {
+            ra[q] = a + 4 * q < G::CP ? *reinterpret_cast<const uint32_t *>(xin + r * G::CP + a + 4 * q) : 0u;
+            rb[q] = a + 4 * q < G::CP ? *reinterpret_cast<const uint32_t *>(xin + (r + 1) * G::CP + a + 4 * q) : 0u;
+        }
+        // realigned so that byte j is byte j % 4 of word j / 4 (compile-time indices)
+        uint32_t al[NWD - 1], bl[NWD - 1];
+#pragma unroll
+        for (int q = 0; q < NWD - 1; ++q) {
+            al[q] = __funnelshift_r(ra[q], ra[q + 1], 8 * sh);
+            bl[q] = __funnelshift_r(rb[q], rb[q + 1], 8 * sh);
+        }
+        uint32_t v[2 * W - 1];
+#pragma unroll
+        for (int j = 0; j < 2 * W - 1; ++j)
+            v[j] = __byte_perm(al[j >> 2], bl[j >> 2], (uint32_t)((j & 3) | (4 + (j & 3)) << 8)) & 0x00FF00FFu;
+        uint32_t mn[W], mx[W];
+        vhgw_run<W, false>(v, mn);
+        vhgw_run<W, true>(v, mx);
+#pragma unroll
+        for (int i = 0; i < W; ++i) {
+            if (use_fill) {
+                const int x = tx0 + c0 + i;
+                if (x + a0 < 0 || x + a0 + W - 1 > nx - 1) {
+                    mn[i] = __vminu2(mn[i], fill2);
+                    mx[i] = __vmaxu2(mx[i], fill2);
+                }
+            }
+            xmn[r * G::TX + c0 + i] = (uint8_t)mn[i];
+            xmn[(r + 1) * G::TX + c0 + i] = (uint8_t)(mn[i] >> 16);
+            xmx[r * G::TX + c0 + i] = (uint8_t)mx[i];
+            xmx[(r + 1) * G::TX + c0 + i] = (uint8_t)(mx[i] >> 16);
+        }
+    }
+    __syncthreads();
+    // y pass: column pairs (c, c+1) x runs of W outputs down
+    for (int it = threadIdx.x; it < (G::TX / 2) * G::NRY; it += blockDim.x) {
+        const int run = it / (G::TX / 2), c = 2 * (it - run * (G::TX / 2)), r0 = run * W;
+        const int x = tx0 + c;
+        if (x >= nx || ty0 + r0 >= ny) continue;
+        uint32_t v[2 * W - 1], mn[W], mx[W];
+#pragma unroll
+        for (int j = 0; j < 2 * W - 1; ++j) {
+            const uint16_t q = *reinterpret_cast<const uint16_t *>(xmn + (r0 + j) * G::TX + c);
+            v[j] = __byte_perm((uint32_t)q, 0u, 0x4140);
+        }
+        vhgw_run<W, false>(v, mn);
+#pragma unroll
+        for (int j = 0; j < 2 * W - 1; ++j) {
+            const uint16_t q = *reinterpret_cast<const uint16_t *>(xmx + (r0 + j) * G::TX + c);
+            v[j] = __byte_perm((uint32_t)q, 0u, 0x4140);
+        }
+        vhgw_run<W, true>(v, mx);
+        const bool two = x + 1 < nx;
+#pragma unroll
+        for (int i = 0; i < W; ++i) {
+            const int y = ty0 + r0 + i;
+            if (y >= ny) break;
+            uint32_t m = mn[i], M = mx[i];
+            if (use_fill && (y + a0 < 0 || y + a0 + W - 1 > ny - 1)) {
+                m = __vminu2(m, fill2);
+                M = __vmaxu2(M, fill2);
+            }
+            const long long p = (long long)y * nx + x;
+            if (which == 0) {
+                // (min, max) of x, then of x+1
+                const uint32_t word = __byte_perm(m, M, 0x6240);
+                uint8_t *q = out + 2 * p;
+                if (two && ((uintptr_t)q & 3) == 0) {
+                    *reinterpret_cast<uint32_t *>(q) = word;
+                } else {
+                    *reinterpret_cast<uint16_t *>(q) = (uint16_t)word;
+                    if (two) *reinterpret_cast<uint16_t *>(q + 2) = (uint16_t)(word >> 16);
+                }
+            } else {
+                const uint32_t sel = which == 1 ? m : M;
+                out[p] = (uint8_t)sel;
+                if (two) out[p + 1] = (uint8_t)(sel >> 16);
+            }
+        }
+    }
+}
+
+template <int W>
+static cudaError_t extrema2d_u8_t(const uint8_t *img, uint8_t *out, int nx, int ny, int a0, int use_fill, int fill,
+                                  int which, cudaStream_t s)
+{
+    using G = ExTile<W>;
+    dim3 grid((nx + G::TX - 1) / G::TX, (ny + G::TY - 1) / G::TY);
+    k_extrema2d_u8<W><<<grid, 256, 0, s>>>(img, out, nx, ny, a0, use_fill, (uint32_t)fill & 0xFFu, which);
+    note_launch();
+    return cudaGetLastError();
+}
+
+bool launch_extrema2d_u8(const void *img, void *out, int nx, int ny, int w, int a0, int use_fill, double fill,
+                         int which, cudaStream_t s, cudaError_t *e)
+{
+    const uint8_t *i = (const uint8_t *)img;
+    uint8_t *o = (uint8_t *)out;
+    const int f = (int)fill;
+    switch (w) {
+    case 3: *e = extrema2d_u8_t<3>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 5: *e = extrema2d_u8_t<5>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 7: *e = extrema2d_u8_t<7>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 9: *e = extrema2d_u8_t<9>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 11: *e = extrema2d_u8_t<11>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 13: *e = extrema2d_u8_t<13>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 15: *e = extrema2d_u8_t<15>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 17: *e = extrema2d_u8_t<17>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 21: *e = extrema2d_u8_t<21>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 25: *e = extrema2d_u8_t<25>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 31: *e = extrema2d_u8_t<31>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    case 33: *e = extrema2d_u8_t<33>(i, o, nx, ny, a0, use_fill, f, which, s); return true;
+    default: return false;
+    }
+}
+
 template <class T>
 static cudaError_t extrema_t(const ExtremaPassArgs &a, cudaStream_t s)
 {

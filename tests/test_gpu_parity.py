@@ -431,6 +431,32 @@ def test_extrema_exact(gpu_ifx, oracle, kind):
             assert np.array_equal(np.asarray(hi, np.float64), mx)
 
 
+@pytest.mark.parametrize("w", [3, 5, 7, 9, 11, 13, 15, 17, 21, 25, 31, 33])
+def test_extrema_2d_tile_kernel(gpu_ifx, oracle, w):
+    """8-bit square windows take the one-launch 2-D tile kernel: against the
+    oracle for images smaller than a window, odd widths and several tiles per
+    axis, every Pad style and Fill, and min, max or both."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(1000 + w)
+    for shape in [(5, 3), (w + 2, 2 * w + 1), (301, 157)]:
+        img = np.asfortranarray(rng.integers(0, 256, shape, dtype=np.uint8))
+        mm = ifx.mapwindow(ifx.extrema, ifx.n0f8(img), (w, w))
+        mn, mx = oracle.extrema_trunc(img.astype(np.float64), [w, w])
+        assert np.array_equal(np.asarray(mm[0], np.float64), mn), shape       # N0f8 codes
+        assert np.array_equal(np.asarray(mm[1], np.float64), mx), shape
+        for style in STYLES:
+            b = ifx.Fill(91) if style == "fill" else ifx.Pad(style)
+            if style == "reflect" and min(shape) < 2:
+                continue
+            mn, mx = oracle.mapwindow_extrema(img.astype(np.float64), [-(w // 2)] * 2, [w, w], style, 91.0)
+            mm = ifx.mapwindow(ifx.extrema, img, (w, w), border=b)
+            assert np.array_equal(np.asarray(mm[0], np.float64), mn), (shape, style)
+            assert np.array_equal(np.asarray(mm[1], np.float64), mx), (shape, style)
+            lo = ifx.mapwindow(ifx.minimum, img, (w, w), border=b)
+            hi = ifx.mapwindow(ifx.maximum, img, (w, w), border=b)
+            assert np.array_equal(np.asarray(lo, np.float64), mn) and np.array_equal(np.asarray(hi, np.float64), mx)
+
+
 def test_config_2048_rank_filters(gpu_ifx, oracle):
     """2048x2048 Gray{N0f8} with 5% salt-and-pepper, median 3x3/5x5 and extrema
     7x7/15x15, Pad(:symmetric): bit-exact on sampled rows and on all edges."""
