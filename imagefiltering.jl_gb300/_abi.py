@@ -102,7 +102,7 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable",
            "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs", "ifx_imfilter_fft",
            "ifx_imfilter_iir", "ifx_autotune", "ifx_autotune_choice", "ifx_server_cancel",
-           "ifx_server_inject_launch_error", "ifx_server_pause"]
+           "ifx_server_inject_launch_error", "ifx_server_pause", "ifx_debug_force_wait_timeout"]
 
 _lib = None
 _lock = threading.Lock()
@@ -126,6 +126,7 @@ def load(path: str = LIB_PATH):
         lib.ifx_last_error.restype = C.c_char_p
         lib.ifx_launch_count.restype = C.c_uint64
         lib.ifx_synchronize.argtypes = [vp, vp]
+        lib.ifx_debug_force_wait_timeout.argtypes = [vp, C.c_int32]
         lib.ifx_padarray.argtypes = [vp, P(IfxArray), P(IfxArray), P(IfxBorder), vp]
         lib.ifx_imfilter_factored.argtypes = [vp, P(IfxArray), P(IfxArray), C.c_int32,
                                               P(IfxFactor), P(IfxBorder), vp]

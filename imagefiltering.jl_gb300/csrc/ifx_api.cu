@@ -3,6 +3,7 @@
 // dispatch to the sm_103a kernels.  No CPU compute path exists: every result
 // is produced by a kernel of this library.
 #include "ifx_internal.h"
+#include "ifx_tma.cuh"
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -697,6 +698,17 @@ int ifx_synchronize(ifx_context_t *ctx, void *stream)
     IFX_CUDA(cudaStreamSynchronize(stream ? (cudaStream_t)stream : ctx->stream));
     if (kernel_timeout_take(ctx->device))
         return fail(IFX_ERR_TIMEOUT, "a kernel's bounded wait for its copies or tensor-core work ran out");
+    return IFX_OK;
+}
+
+int ifx_debug_force_wait_timeout(ifx_context_t *ctx, int32_t on)
+{
+    IFX_RANGE("ifx_debug_force_wait_timeout");
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    IFX_CUDA(cudaSetDevice(ctx->device));
+    IFX_CUDA(cudaDeviceSynchronize());
+    IFX_CUDA(set_first_wait_tma(on != 0));
+    IFX_CUDA(set_first_wait_batch(on != 0));
     return IFX_OK;
 }
 

@@ -582,6 +582,17 @@ constexpr int kReqTable = 1024;      // requests whose first tiles are searched 
 // (registers and shared memory allow it).
 constexpr int kBatchBufs = 2, kBatchThreads = 288, kBatchCtas = 3;
 
+// Poll budget of each tile's first wait for its copies; a testing setting
+// (ifx_debug_force_wait_timeout) sets it to 0 so that the timeout path runs.
+// The drain waits of that path keep their full budget.
+static __device__ unsigned g_first_wait_batch = kFirstWaitBatch;
+
+cudaError_t set_first_wait_batch(bool force_timeout)
+{
+    const unsigned v = force_timeout ? 0u : kFirstWaitBatch;
+    return cudaMemcpyToSymbol(g_first_wait_batch, &v, sizeof v);
+}
+
 __global__ void __launch_bounds__(kBatchThreads, kBatchCtas)
 k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int *err)
 {
@@ -598,6 +609,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
     const int nreq = hdr->nreq;
     const int ntab = nreq < kReqTable ? nreq : kReqTable;
     const int tid = threadIdx.x, warp = tid >> 5;
+    const unsigned first_tries = g_first_wait_batch;
     float *I = reinterpret_cast<float *>(smem + NB * kStageBytes);
     for (int i = tid; i < ntab; i += blockDim.x) s_base[i] = (int)reqs[i].tile_base;
     s_n0f8[tid & 255] = __fdiv_rn((float)(tid & 255), 255.0f);
@@ -684,7 +696,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
             const int tx0 = bx * bt_tile_w(R.op, R.in_type), ty0 = by * bt_tile_h(R.op, R.in_type, R.ky);
             unsigned char *st = smem + b * kStageBytes;
             if (s_bulk[b]) {
-                ok = mbar_wait_bounded(&s_bar[b], (parity >> b) & 1u);
+                ok = mbar_wait_bounded(&s_bar[b], (parity >> b) & 1u, first_tries);
             } else {
                 bt_gather_raw(R, bt_geo(R, tx0, ty0), st, s_lead[b]);
                 ct_sync();

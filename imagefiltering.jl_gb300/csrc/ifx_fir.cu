@@ -423,6 +423,18 @@ __host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int x_first, 
     return L;
 }
 
+// Poll budget of each tile's first wait for its copy.  A testing setting
+// (ifx_debug_force_wait_timeout) sets it to 0, so that the wait gives up at
+// once and the kernel takes its timeout path; the waits for copies still in
+// flight on that path keep their full budget.
+static __device__ unsigned g_first_wait_tma = kFirstWaitTma;
+
+cudaError_t set_first_wait_tma(bool force_timeout)
+{
+    const unsigned v = force_timeout ? 0u : kFirstWaitTma;
+    return cudaMemcpyToSymbol(g_first_wait_tma, &v, sizeof v);
+}
+
 template <class Tin, class Tout>
 __global__ void __launch_bounds__(256)
 k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img, Tout *__restrict__ out,
@@ -440,6 +452,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     const int RV = TY + ky - 1, CV = TX + kx - 1;
     const SepTmaSmem L = sep_tma_smem(kx, ky, x_first, (int)sizeof(Tin), TY);
     const int boxw = L.boxw;
+    const unsigned first_tries = g_first_wait_tma;
     auto raw_buf = [&](int b) { return reinterpret_cast<Tin *>(st_smem + (size_t)b * L.raw); };
     unsigned char *rest = st_smem + 2 * L.raw;
     float *wxs = reinterpret_cast<float *>(rest);     // row-pass weights
@@ -532,7 +545,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         }
         // every tile arrives by the copy engine (cells outside the image as zeros)
         const uint32_t ph = (parity >> b) & 1u;
-        const bool ok = mbar_wait_sleep(&bar[b], ph);
+        const bool ok = mbar_wait_sleep(&bar[b], ph, first_tries);
         parity ^= 1u << b;
         pending &= ~(1u << b);
         if (__syncthreads_or(!ok)) {

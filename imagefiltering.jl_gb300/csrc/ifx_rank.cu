@@ -708,7 +708,7 @@ __device__ __forceinline__ void vhgw_run(const uint32_t (&v)[2 * W - 1], uint32_
 }
 
 template <int W>
-__global__ void __launch_bounds__(256, W <= 9 ? 6 : 4)
+__global__ void __launch_bounds__(256, W <= 9 ? 5 : (W <= 17 ? 4 : 2))
 k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int nx, int ny, int a0, int use_fill,
                uint32_t fill, int which)
 {

@@ -57,6 +57,12 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity)
 }
 
 // Waits for phase `parity` of *bar, giving up after `tries` polls.
+// Default poll budgets of the kernels' first wait for a tile's copies.
+constexpr unsigned kFirstWaitBatch = 1u << 22, kFirstWaitTma = 4096u;
+// Testing: every first wait gives up at once (true) or takes its default budget.
+cudaError_t set_first_wait_tma(bool force_timeout);
+cudaError_t set_first_wait_batch(bool force_timeout);
+
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t tries = 1u << 22)
 {
     for (uint32_t i = 0; i < tries; ++i)

@@ -103,6 +103,14 @@ const char *ifx_last_error(void);
 /* Number of this library's kernel launches made by the calling process so far. */
 uint64_t ifx_launch_count(void);
 int ifx_synchronize(ifx_context_t *ctx, void *stream);
+/* Testing aid, no counterpart in the reference: on != 0 makes the first wait
+ * of every tile of the copy-fed kernels (the TMA-fed separable kernel and the
+ * batched engine) on the context's device give up at once, so that the
+ * kernels take their timeout path (they wait, with their full bound, for the
+ * copies still in flight, record the timeout and return) and the next
+ * ifx_synchronize reports IFX_ERR_TIMEOUT; on == 0 restores the default
+ * bounds.  No GPU fault is involved. */
+int ifx_debug_force_wait_timeout(ifx_context_t *ctx, int32_t on);
 
 /* ---- a1: border index maps ------------------------------------------------
  * padarray(T, img, border) (src/border.jl:324-331 -> borderarray.jl:179-196,
