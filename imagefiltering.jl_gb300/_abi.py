@@ -90,7 +90,8 @@ class IfxServerMetrics(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("batches", C.c_uint64), ("pixels", C.c_uint64), ("p50_latency_s", C.c_double),
                 ("p99_latency_s", C.c_double), ("max_latency_s", C.c_double), ("busy_s", C.c_double),
-                ("hbm_in_use", C.c_int64), ("hbm_peak", C.c_int64), ("queue_depth", C.c_int32)]
+                ("hbm_in_use", C.c_int64), ("hbm_peak", C.c_int64), ("queue_depth", C.c_int32),
+                ("deferred_free", C.c_uint64)]
 
 SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "ifx_launch_count",
            "ifx_synchronize", "ifx_padarray", "ifx_imfilter_factored", "ifx_imfilter_dense",

@@ -2,7 +2,9 @@
 //
 // Requests arrive through ifx_server_submit at any time.  One engine thread
 //   1. admits queued requests in arrival order while the device bytes they
-//      need (staged input, outputs) fit under the HBM cap; device memory
+//      need (staged input, outputs) fit under the HBM cap and in the device's
+//      available memory (free memory plus the pool's unused part, less a
+//      reserve: a shared device may have less than the cap); device memory
 //      comes from the stream-ordered allocator and host images are uploaded
 //      on a copy stream as soon as a request is admitted;
 //   2. while fewer than `max_inflight` batches run, packs admitted requests
@@ -65,6 +67,7 @@ struct ifx_server {
     ifx_server_config_t cfg{};
     cudaStream_t copy = nullptr, compute = nullptr;   // copy: uploads; compute: batches
     cudaStream_t down = nullptr;                        // downloads and releases
+    uint64_t deferred_free = 0;                         // admissions held back by free device memory
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<std::shared_ptr<ifx::SReq>> incoming;           // submitted, not seen by the engine
@@ -150,12 +153,51 @@ static void finish_batches(ifx_server *S)
     }
 }
 
-// Admission in arrival order under the HBM cap (srv->mu held).
+// Device memory the server can still take: the device's free memory plus what
+// its stream-ordered pool holds but does not use, less a reserve kept for
+// other users of the device and for the library's own buffers.
+constexpr size_t kFreeReserve = 256ull << 20;
+
+static size_t device_available(const ifx_server *S)
+{
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return SIZE_MAX;                     // no answer: the cap alone decides
+    }
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, S->device) == cudaSuccess) {
+        uint64_t reserved = 0, used = 0;
+        if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+            free_b += (size_t)(reserved - used);
+    }
+    (void)cudaGetLastError();
+    return free_b > kFreeReserve ? free_b - kFreeReserve : 0;
+}
+
+// Admission in arrival order while a request fits both the HBM cap and the
+// device's available memory (srv->mu held).  With nothing admitted a request
+// is admitted anyway: waiting could not free any memory of this server, and
+// an allocation failure then fails that request alone.
 static void admit(ifx_server *S)
 {
+    size_t avail = 0;
+    bool have_avail = false;
     while (!S->queue.empty()) {
         auto r = S->queue.front();
-        if (S->hbm_in_use + r->need > S->cfg.hbm_cap_bytes && S->hbm_in_use > 0) return;
+        if (S->hbm_in_use > 0) {
+            if (S->hbm_in_use + r->need > S->cfg.hbm_cap_bytes) return;
+            if (!have_avail) {
+                avail = device_available(S);
+                have_avail = true;
+            }
+            if (r->need > avail) {
+                ++S->deferred_free;
+                return;
+            }
+            avail -= r->need;
+        }
         bool ok = true;
         if (r->host_in) {
             ok &= cudaMallocAsync(&r->d_in, r->in_bytes, S->copy) == cudaSuccess;
@@ -469,6 +511,7 @@ int ifx_server_metrics(ifx_server_t *S, ifx_server_metrics_t *m)
     m->hbm_in_use = S->hbm_in_use;
     m->hbm_peak = S->hbm_peak;
     m->queue_depth = (int32_t)(S->incoming.size() + S->queue.size());
+    m->deferred_free = S->deferred_free;
     if (!S->latencies.empty()) {
         std::vector<double> v = S->latencies;
         std::sort(v.begin(), v.end());
@@ -510,6 +553,15 @@ int ifx_server_destroy(ifx_server_t *S)
     cudaStreamDestroy(S->copy);
     cudaStreamDestroy(S->down);
     cudaStreamDestroy(S->compute);
+    // the pool kept freed request memory (up to the cap) for the next
+    // admissions; with the server gone it goes back to the device
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, S->device) == cudaSuccess) {
+        const uint64_t zero = 0;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, (void *)&zero);
+        cudaMemPoolTrimTo(pool, 0);
+    }
+    (void)cudaGetLastError();
     delete S;
     return IFX_OK;
 }

@@ -379,6 +379,8 @@ typedef struct ifx_server_metrics {
     double busy_s;                 /* first submit -> last completion */
     int64_t hbm_in_use, hbm_peak;
     int32_t queue_depth;           /* submitted, not yet admitted */
+    uint64_t deferred_free;        /* admissions held back because the device's free
+                                      memory (less a 256 MiB reserve) was short */
 } ifx_server_metrics_t;
 
 int ifx_server_create(ifx_context_t *ctx, const ifx_server_config_t *cfg, ifx_server_t **srv);

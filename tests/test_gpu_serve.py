@@ -200,3 +200,38 @@ def test_server_injected_launch_failure(gpu_ifx):
         m = srv.metrics()
     assert m["failed"] == 8 and m["completed"] == 8 and m["hbm_in_use"] == 0
     check_outputs(ifx, items[8:], outs[8:])
+
+
+def test_server_admission_by_free_device_memory(gpu_ifx):
+    """A cap far above what the device has free (another user holds most of
+    it): admission follows the device's free memory, so requests wait instead
+    of failing their allocations, and all complete with correct results."""
+    ifx = gpu_ifx
+    import torch
+    from imagefiltering_gb300.serve import Server
+    torch.cuda.synchronize()
+    free, _ = torch.cuda.mem_get_info()
+    keep = 640 << 20                                   # what the other user leaves free
+    hog = torch.empty(max(free - keep, 0), dtype=torch.uint8, device="cuda")
+    try:
+        rng = np.random.default_rng(12)
+        items = []
+        for i in range(12):                            # 4096^2 Float32 -> Float64: 192 MiB each on the device
+            img = np.asfortranarray(rng.random((4096, 4096), dtype=np.float32))
+            items.append((img, ("gaussian", 1.0 + (i % 3)), ifx.Pad("reflect")))
+        with Server(hbm_cap_bytes=100 << 30, max_batch=2, max_inflight=2) as srv:
+            outs, tickets = [], []
+            for img, op, border in items:
+                o = host_outputs(ifx, img, op)
+                outs.append(o)
+                tickets.append(srv.submit(op, img, o, border))
+            for t in tickets:
+                srv.wait(t, timeout=120)
+            m = srv.metrics()
+        assert m["completed"] == len(items) and m["failed"] == 0, m
+        assert m["deferred_free"] > 0, m               # admissions waited for memory
+        assert m["hbm_peak"] <= keep, m
+    finally:
+        del hog
+        torch.cuda.empty_cache()
+    check_outputs(ifx, items[:3], outs[:3])
