@@ -691,7 +691,7 @@ def run_sections(args, ifx, torch, hbm_peak):
     def crop(t, h):
         return np.asfortranarray(t[c0 - h[0]:c0 + cn + h[0], c0 - h[1]:c0 + cn + h[1],
                                    c0 - h[2]:c0 + cn + h[2]].cpu().numpy().astype(np.float64))
-    hv = [f.data.size // 2 for f in kf]
+    hv = [-int(f.data.first[0]) for f in kf]
     facs_g = [(f.axis, f.data.first[0], np.asarray(f.data.data)) for f in kf]
     ref_g = O.imfilter_cascade(crop(vols[7].tensor, hv), facs_g, "symmetric")
     es_g = err_stats(crop(gau[1].tensor, [0, 0, 0]), ref_g[hv[0]:hv[0] + cn, hv[1]:hv[1] + cn, hv[2]:hv[2] + cn])
@@ -813,14 +813,13 @@ def run_next_rows(args, ifx, torch, hbm_peak):
 
 def reference_sample(args):
     """The fixed request sample the CPU legs time: every 10th request of the
-    first timed wave of the stream (the same requests on every step and in
-    every run; sizes, ops, eltypes and borders in the stream's proportions)."""
+    stream's first wave (the same requests on every step and in every run,
+    whatever the warm-up count; sizes, ops, eltypes and borders in the
+    stream's proportions)."""
     import __graft_entry__ as g
     g.load_package()
     from imagefiltering_gb300 import synthetic as S
-    reqs = S.stream_requests(args.per_step * (args.warmup + 1), seed=5)
-    wave = reqs[args.per_step * args.warmup: args.per_step * (args.warmup + 1)]
-    return wave[::10]
+    return S.stream_requests(args.per_step, seed=5)[::10]
 
 
 def cpu_stream_baseline(args, threads, reqs=None, images=None):
@@ -852,7 +851,7 @@ def cpu_stream_baseline(args, threads, reqs=None, images=None):
         px += r.pixels
     dt = time.perf_counter() - t0
     return {"value": px / dt / 1e6, "unit": "Mpixel/s", "cores": threads, "kind": "port",
-            "sample": "fixed sample of the stream: every 10th request of the first timed wave (%d requests, "
+            "sample": "fixed sample of the stream: every 10th request of its first wave (%d requests, "
                       "%.1f Mpixel), oracle port of the reference loops; separable passes threaded over %d "
                       "threads, median/Laplacian single-threaded as in the reference" % (len(reqs), px / 1e6, threads)}
 
@@ -941,9 +940,9 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        from imagefiltering_gb300 import synthetic as S
         import __graft_entry__ as g
         g.load_package()
+        from imagefiltering_gb300 import synthetic as S
         sample = reference_sample(args)
         images = [S.image_for(r) for r in sample]
         vals = []
@@ -958,7 +957,7 @@ def main():
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "requests_per_step": len(sample),
                            "mode": "the reference loops (oracle port) on the host cores; every step runs the same "
-                                   "fixed sample of the GPU arm's first timed wave (every 10th of its %d requests)"
+                                   "fixed sample of the stream's first wave (every 10th of its %d requests)"
                                    % args.per_step},
                 "cpu_baseline": {"value": v, "unit": "Mpixel/s", "cores": threads, "kind": "port",
                                  "sample": r["sample"]},
