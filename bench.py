@@ -203,8 +203,8 @@ def stream_calls(ifx, reqs, dev_inputs, out_arena, torch):
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum over algorithmic bytes for one k_batch
-# launch on a 60-request wave of the same stream (206.356 + 884.533 MB / 1147.791 MB)
-K_BATCH_TRAFFIC_RATIO = (208.952320 + 885.413376) / 1147.791071
+# launch on a 60-request wave of the same stream (206.723 + 895.578 MB / 1147.791 MB)
+K_BATCH_TRAFFIC_RATIO = (206.722560 + 895.578368) / 1147.791071
 
 
 def alg_bytes(r):
