@@ -616,6 +616,25 @@ def run_sections(args, ifx, torch, hbm_peak):
             arr[i].axis, arr[i].length, arr[i].first, arr[i].weights = ax, w.size, -(w.size // 2), A.dptr(w)
         return arr, keep
 
+    # C1: one 512^2 Float32 image, KernelFactors.gaussian((2,2)) (9 taps) and the
+    # 17-tap form, Pad(:replicate), Float64 output; error against the oracle on the whole image
+    n1 = 512
+    img1 = ifx.DeviceArray(torch.rand((n1, n1), device="cuda", generator=g).t(), "F32")
+    host1 = img1.numpy().astype(np.float64)
+    for taps in (9, 17):
+        gk = np.asarray(ifx.KernelFactors.gaussian(2.0, taps).data)
+        arr, keep = factors([(0, gk), (1, gk)])
+        o1 = ifx.DeviceArray.empty((n1, n1), "F64")
+        b = A.border_struct("replicate")
+        ms = _time(torch, lambda: A.check(ctx.lib.ifx_imfilter_factored(
+            ctx.handle, desc(o1), desc(img1), 2, arr, C.byref(b), stream)))
+        ref = O.imfilter_cascade(np.asfortranarray(host1), [(0, -(taps // 2), gk), (1, -(taps // 2), gk)],
+                                 "replicate")
+        es = err_stats(o1.numpy(), ref)
+        out["C1_512_gaussian_%dtap_F32_F64" % taps] = {
+            "ms": round(ms, 4), "mpix_s": n1 * n1 / (ms / 1e3) / 1e6, "normwise_err": es["normwise"],
+            "max_abs_err": es["max_abs"], "max_rel_err": es["max_rel"],
+            "note": "1 MiB image: latency-bound (one launch), judged on its error, not its roofline"}
     n = 4096
     ifx.autotune(True)            # the separable cases below are tuned on their first (warm-up) call
     imgs = {"F32": ifx.DeviceArray(torch.rand((n, n), device="cuda", generator=g).t(), "F32"),
