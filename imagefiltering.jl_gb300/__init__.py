@@ -13,13 +13,13 @@ CUDA kernels of ``_build/libifx_gb300.so``; there is no CPU fallback, and the
 functions raise if the library is missing.
 """
 from . import _abi
-from ._abi import (ArgumentError, Cancelled, DimensionMismatch, ErrorException, CudaError, OutOfMemory,
-                   Unsupported, launch_count)
-from .arrays import DeviceArray, N0f8Array, n0f8
+from ._abi import (ArgumentError, Cancelled, DimensionMismatch, ErrorException, CudaError, InexactError,
+                   OutOfMemory, Unsupported, launch_count)
+from .arrays import RGB, DeviceArray, N0f8Array, N0f16Array, n0f8, n0f16, rgb
 from .blobs import BlobLoG, blob_LoG, findlocalmaxima, findlocalminima, multiLoG
 from .borders import Fill, Inner, NA, NoPad, Pad, borderinstance, padarray
-from .filtering import (Algorithm, autotune, autotune_choice, factorkernel, filter_type, imfilter, imfilter_,
-                        imgradients)
+from .filtering import (Algorithm, autotune, autotune_choice, convert_, factorkernel, filter_type, imfilter,
+                        imfilter_, imgradients, maxabs)
 from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD, TriggsSdika,
                       centered, iscopy, kernelfactors)
 from .rank import extrema, mapwindow, mapwindow_, maximum, median, median_, minimum
@@ -35,7 +35,7 @@ __all__ = [
     "imfilter", "imfilter_", "imgradients", "mapwindow", "mapwindow_", "padarray", "Pad", "Fill",
     "Inner", "NA", "NoPad", "BlobLoG", "blob_LoG", "multiLoG", "findlocalmaxima", "findlocalminima", "Kernel", "KernelFactors", "centered", "kernelfactors", "Algorithm",
     "OffsetArray", "OffsetKernel", "ReshapedOneD", "LaplacianKernel", "TriggsSdika", "DeviceArray", "N0f8Array",
-    "n0f8", "median", "median_", "extrema", "minimum", "maximum", "filter_type", "factorkernel",
+    "n0f8", "N0f16Array", "n0f16", "RGB", "rgb", "convert_", "maxabs", "InexactError", "median", "median_", "extrema", "minimum", "maximum", "filter_type", "factorkernel",
     "iscopy", "borderinstance", "autotune", "autotune_choice", "ArgumentError", "DimensionMismatch", "ErrorException",
     "CudaError", "OutOfMemory", "Unsupported", "Cancelled", "launch_count", "library_path",
 ]

@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libifx_gb300.so")
 
 # ifx_eltype
 F32, F64, N0F8, U8, I16 = 0, 1, 2, 3, 4
+I8, U16, I32, I64, N0F16 = 5, 6, 7, 8, 9
 # ifx_style
 STYLES = {"replicate": 0, "circular": 1, "symmetric": 2, "reflect": 3, "fill": 4}
 MAX_DIMS = 4
@@ -47,6 +48,10 @@ class Unsupported(NotImplementedError):
 
 class Cancelled(RuntimeError):
     """A served request cancelled before it ran."""
+
+
+class InexactError(ValueError):
+    """Julia's InexactError: a value does not fit the target eltype."""
 
 
 _EXC = {1: ArgumentError, 2: DimensionMismatch, 3: ErrorException, 4: CudaError, 5: OutOfMemory,
@@ -103,7 +108,7 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable",
            "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs", "ifx_imfilter_fft",
            "ifx_imfilter_iir", "ifx_autotune", "ifx_autotune_choice", "ifx_server_cancel",
-           "ifx_server_inject_launch_error", "ifx_server_pause", "ifx_debug_force_wait_timeout"]
+           "ifx_server_inject_launch_error", "ifx_server_pause", "ifx_debug_force_wait_timeout", "ifx_convert"]
 
 _lib = None
 _lock = threading.Lock()
@@ -128,6 +133,7 @@ def load(path: str = LIB_PATH):
         lib.ifx_launch_count.restype = C.c_uint64
         lib.ifx_synchronize.argtypes = [vp, vp]
         lib.ifx_debug_force_wait_timeout.argtypes = [vp, C.c_int32]
+        lib.ifx_convert.argtypes = [vp, P(IfxArray), P(IfxArray), vp]
         lib.ifx_padarray.argtypes = [vp, P(IfxArray), P(IfxArray), P(IfxBorder), vp]
         lib.ifx_imfilter_factored.argtypes = [vp, P(IfxArray), P(IfxArray), C.c_int32,
                                               P(IfxFactor), P(IfxBorder), vp]
@@ -221,7 +227,8 @@ def launch_count() -> int:
 
 # ----------------------------------------------------------------- descriptors
 def eltype_code(kind: str) -> int:
-    return {"F32": F32, "F64": F64, "N0F8": N0F8, "U8": U8, "I16": I16}[kind]
+    return {"F32": F32, "F64": F64, "N0F8": N0F8, "U8": U8, "I16": I16, "I8": I8, "U16": U16, "I32": I32,
+            "I64": I64, "N0F16": N0F16}[kind]
 
 
 def describe(data_ptr: int, kind: str, shape, strides=None, first=None) -> IfxArray:

@@ -18,14 +18,64 @@ class N0f8Array(np.ndarray):
     """uint8 codes interpreted as N0f8 (c/255)."""
 
 
+class N0f16Array(np.ndarray):
+    """uint16 codes interpreted as N0f16 (c/65535), the Gray{N0f16} of the reference."""
+
+
 def n0f8(a) -> "N0f8Array":
     return np.asfortranarray(np.asarray(a, dtype=np.uint8)).view(N0f8Array)
 
 
+def n0f16(a) -> "N0f16Array":
+    return np.asfortranarray(np.asarray(a, dtype=np.uint16)).view(N0f16Array)
+
+
 _NP_KIND = {np.dtype(np.float32): "F32", np.dtype(np.float64): "F64", np.dtype(np.uint8): "U8",
-            np.dtype(np.int16): "I16"}
+            np.dtype(np.int16): "I16", np.dtype(np.int8): "I8", np.dtype(np.uint16): "U16",
+            np.dtype(np.int32): "I32", np.dtype(np.int64): "I64"}
 _KIND_NP = {"F32": np.float32, "F64": np.float64, "U8": np.uint8, "N0F8": np.uint8,
-            "I16": np.int16}
+            "I16": np.int16, "I8": np.int8, "U16": np.uint16, "N0F16": np.uint16, "I32": np.int32,
+            "I64": np.int64}
+# kinds the filters take directly; the others go through ifx_convert
+NATIVE_KINDS = ("F32", "F64", "N0F8", "U8")
+INT_KINDS = ("U8", "I8", "I16", "U16", "I32", "I64")
+
+
+def _torch_dtype(kind):
+    import torch
+    # 16-bit unsigned kinds are stored as int16 (the same bits)
+    return {"F32": torch.float32, "F64": torch.float64, "U8": torch.uint8, "N0F8": torch.uint8,
+            "I16": torch.int16, "I8": torch.int8, "U16": torch.int16, "N0F16": torch.int16,
+            "I32": torch.int32, "I64": torch.int64}[kind]
+
+
+class RGB:
+    """An RGB image (Array{RGB{T}}) as its channel planes in Julia's memory
+    order: ``data`` has shape (3,) + image shape and axis 0 is the channel --
+    reinterpret(T, img) of the reference's array, T N0f8, Float32 or Float64
+    (host array or DeviceArray).  Linear filters act on the image axes of each
+    channel; filter_type gives RGB of the promoted eltype
+    (src/imfilter.jl:1133)."""
+
+    def __init__(self, data):
+        if data.shape[0] != 3:
+            raise ValueError("RGB data needs the channel axis (length 3) first")
+        self.data = data
+
+    @property
+    def shape(self):
+        return tuple(self.data.shape[1:])
+
+    @property
+    def ndim(self):
+        return len(self.data.shape) - 1
+
+    def channel(self, i):
+        return self.data[i] if not isinstance(self.data, DeviceArray) else DeviceArray(self.data.tensor[i], self.data.kind)
+
+
+def rgb(data):
+    return RGB(data)
 
 
 class DeviceArray:
@@ -36,7 +86,7 @@ class DeviceArray:
         self.tensor = tensor
         if kind is None:
             kind = {torch.float32: "F32", torch.float64: "F64", torch.uint8: "U8",
-                    torch.int16: "I16"}[tensor.dtype]
+                    torch.int16: "I16", torch.int8: "I8", torch.int32: "I32", torch.int64: "I64"}[tensor.dtype]
         self.kind = kind
         self.first = first
 
@@ -57,14 +107,17 @@ class DeviceArray:
     def numpy(self):
         a = self.tensor.detach().cpu().numpy()
         a = np.asfortranarray(a)
+        if self.kind in ("U16", "N0F16"):
+            a = a.view(np.uint16)
+        if self.kind == "N0F16":
+            return a.view(N0f16Array)
         return a.view(N0f8Array) if self.kind == "N0F8" else a
 
     @staticmethod
     def empty(shape, kind, device="cuda"):
         """A column-major tensor of Julia shape `shape`."""
         import torch
-        dt = {"F32": torch.float32, "F64": torch.float64, "U8": torch.uint8,
-              "N0F8": torch.uint8, "I16": torch.int16}[kind]
+        dt = _torch_dtype(kind)
         rev = tuple(reversed(shape))
         t = torch.empty(rev, dtype=dt, device=device)
         t = t.permute(*reversed(range(len(shape)))) if len(shape) > 1 else t
@@ -76,7 +129,10 @@ class DeviceArray:
         k = kind_of(a)
         a = np.asfortranarray(a)
         d = DeviceArray.empty(a.shape, k, device)
-        src = torch.from_numpy(np.ascontiguousarray(a.view(np.ndarray).T))
+        host = a.view(np.ndarray)
+        if k in ("U16", "N0F16"):
+            host = host.view(np.int16)
+        src = torch.from_numpy(np.ascontiguousarray(host.T))
         d.tensor.copy_(src.permute(*reversed(range(a.ndim))) if a.ndim > 1 else src)
         return d
 
@@ -86,6 +142,8 @@ def kind_of(a) -> str:
         return a.kind
     if isinstance(a, N0f8Array):
         return "N0F8"
+    if isinstance(a, N0f16Array):
+        return "N0F16"
     dt = np.asarray(a).dtype
     if dt not in _NP_KIND:
         raise NotImplementedError("eltype %s is not supported by the GB300 path" % dt)
@@ -96,6 +154,8 @@ def host_view(a, kind=None):
     """Fortran-ordered numpy array (keeps the N0f8 marker)."""
     if kind == "N0F8" or isinstance(a, N0f8Array):
         return n0f8(a)
+    if kind == "N0F16" or isinstance(a, N0f16Array):
+        return n0f16(a)
     return np.asfortranarray(a)
 
 
@@ -104,6 +164,8 @@ def alloc_like(img, shape, kind):
     if isinstance(img, DeviceArray):
         return DeviceArray.empty(shape, kind, img.tensor.device)
     out = np.empty(shape, dtype=_KIND_NP[kind], order="F")
+    if kind == "N0F16":
+        return out.view(N0f16Array)
     return out.view(N0f8Array) if kind == "N0F8" else out
 
 

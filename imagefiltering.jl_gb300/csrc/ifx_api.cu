@@ -54,6 +54,19 @@ static size_t elsize(int t)
     }
 }
 static bool is8(int t) { return t == IFX_N0F8 || t == IFX_U8; }
+// Element sizes of every eltype ifx_convert takes (the filters take the ones
+// elsize knows).
+static size_t conv_elsize(int t)
+{
+    switch (t) {
+    case IFX_I8: return 1;
+    case IFX_U16:
+    case IFX_N0F16: return 2;
+    case IFX_I32: return 4;
+    case IFX_I64: return 8;
+    default: return elsize(t);
+    }
+}
 
 // ------------------------------------------------------------------ context
 struct Slot {
@@ -67,7 +80,7 @@ struct ifx_context {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::mutex mu;
-    ifx::Slot slots[24];
+    ifx::Slot slots[32];
 };
 
 namespace ifx {
@@ -105,12 +118,14 @@ static long long numel(const ifx_array_t &a)
     return n;
 }
 
-static int check_array(const ifx_array_t *a, const char *name, int values_per_elem = 1)
+static int check_array(const ifx_array_t *a, const char *name, int values_per_elem = 1, bool any_eltype = false)
 {
     if (!a) return fail(IFX_ERR_ARGUMENT, "%s is NULL", name);
     if (a->ndim < 1 || a->ndim > IFX_MAX_DIMS)
         return fail(IFX_ERR_ARGUMENT, "%s: ndims %d not in 1..%d", name, a->ndim, IFX_MAX_DIMS);
-    if (elsize(a->eltype) == 0) return fail(IFX_ERR_ARGUMENT, "%s: unknown eltype %d", name, a->eltype);
+    if ((any_eltype ? conv_elsize(a->eltype) : elsize(a->eltype)) == 0)
+        return fail(IFX_ERR_ARGUMENT, "%s: eltype %d is not taken here%s", name, a->eltype,
+                    conv_elsize(a->eltype) ? " (convert it with ifx_convert first)" : "");
     long long s = 1;
     for (int d = 0; d < a->ndim; ++d) {
         if (a->size[d] < 0) return fail(IFX_ERR_ARGUMENT, "%s: negative size", name);
@@ -1584,6 +1599,47 @@ int ifx_findlocalextrema(ifx_context_t *ctx, const ifx_array_t *img, const int32
     }
     if ((rc = c.finish())) return rc;
     IFX_CUDA(cudaStreamSynchronize(c.s));
+    return IFX_OK;
+}
+
+int ifx_convert(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, void *stream)
+{
+    IFX_RANGE("ifx_convert");
+    int rc;
+    if ((rc = check_array(img, "img", 1, true)) || (rc = check_array(out, "out", 1, true))) return rc;
+    if ((rc = check_same_axes(*out, *img))) return rc;
+    const int st = img->eltype, dt = out->eltype;
+    const bool to_int = dt == IFX_U8 || dt == IFX_I8 || dt == IFX_I16 || dt == IFX_U16 || dt == IFX_I32 ||
+                        dt == IFX_I64;
+    if (!(to_int || dt == IFX_F32 || dt == IFX_F64) && dt != st)
+        return fail(IFX_ERR_UNSUPPORTED, "conversion to N0f8/N0f16 is not supported (from eltype %d)", st);
+    const long long n = numel(*img);
+    if (n == 0) return IFX_OK;
+    if (!ctx) return fail(IFX_ERR_ARGUMENT, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Call c;
+    if ((rc = begin(ctx, stream, c))) return rc;
+    const void *din;
+    void *dout, *flag;
+    if ((rc = c.input(*img, &din, (size_t)n * conv_elsize(st))) ||
+        (rc = c.output(*out, &dout, (size_t)n * conv_elsize(dt))))
+        return rc;
+    if (dt == st) {
+        if (dout != din) IFX_CUDA(cudaMemcpyAsync(dout, din, (size_t)n * conv_elsize(st), cudaMemcpyDeviceToDevice, c.s));
+        return c.finish();
+    }
+    if ((rc = slot_get(ctx, 24, 16, &flag))) return rc;
+    if (to_int) IFX_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), c.s));
+    IFX_CUDA(launch_convert(din, st, dout, dt, n, (int *)flag, c.s));
+    int bad = 0;
+    if (to_int) IFX_CUDA(cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+    if ((rc = c.finish())) return rc;
+    if (to_int) {
+        IFX_CUDA(cudaStreamSynchronize(c.s));
+        if (bad)
+            return fail(IFX_ERR_ARGUMENT, "InexactError: a value is not an integer inside the range of "
+                        "the output's eltype");
+    }
     return IFX_OK;
 }
 

@@ -214,6 +214,8 @@ struct ExtremaPassArgs {                   // one separable min/max pass along `
     int want_min, want_max;
 };
 cudaError_t launch_extrema_pass(const ExtremaPassArgs &a, cudaStream_t s);
+// Element conversion (ifx_convert): *bad set when an integer target cannot hold a value.
+cudaError_t launch_convert(const void *src, int st, void *dst, int dt, long long n, int *bad, cudaStream_t s);
 // 8-bit 2-D extrema of square w x w windows (first offset a0 on both axes) in
 // one launch; false when w has no compiled tile kernel.  which: 0 interleaved
 // (min, max), 1 min, 2 max.

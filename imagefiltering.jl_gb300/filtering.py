@@ -13,7 +13,8 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from .arrays import DeviceArray, alloc_like, host_view, kind_of, ptr_strides, stream_for
+from .arrays import (INT_KINDS, NATIVE_KINDS, RGB, DeviceArray, alloc_like, host_view, kind_of, ptr_strides,
+                     stream_for)
 from .borders import Fill, Inner, NA, NoPad, border_struct, borderinstance
 from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD, TriggsSdika,
                       iscopy)
@@ -62,30 +63,64 @@ def _kernel_dtype(k):
     return np.dtype(k.dtype)
 
 
+_INT_OF_DTYPE = {np.dtype(np.int8): "I8", np.dtype(np.uint8): "U8", np.dtype(np.int16): "I16",
+                 np.dtype(np.uint16): "U16", np.dtype(np.int32): "I32", np.dtype(np.int64): "I64"}
+_INT_BITS = {"I8": (8, True), "U8": (8, False), "I16": (16, True), "U16": (16, False), "I32": (32, True),
+             "I64": (64, True)}
+
+
+def _promote_int(a, b):
+    """Julia's promote_type of two integer eltypes: the wider one; between a
+    signed and an unsigned type of the same width (or a wider unsigned one),
+    the unsigned one."""
+    (na, sa), (nb, sb) = _INT_BITS[a], _INT_BITS[b]
+    if sa == sb:
+        return a if na >= nb else b
+    s_, u_ = (a, b) if sa else (b, a)
+    return s_ if _INT_BITS[s_][0] > _INT_BITS[u_][0] else u_
+
+
 def _promote_one(img_kind, kdt):
-    """typeof(zero(S)*zero(T) + ...) for the supported (S, T) pairs."""
+    """typeof(zero(S)*zero(T) + ...) for the supported (S, T) pairs
+    (src/imfilter.jl:1133; Float32 for Normed and Int, Float64 wins)."""
     if kdt is None:
         return None
     if img_kind == "F64" or kdt == np.float64:
         return "F64"
     if kdt == np.float32:
         return "F32"
-    if np.issubdtype(kdt, np.integer) or kdt == np.bool_:
-        if img_kind in ("F32", "N0F8"):
+    if kdt == np.bool_:
+        kdt = np.dtype(np.int8) if img_kind in INT_KINDS else kdt
+        if kdt == np.bool_:
             return "F32"
-        raise _abi.Unsupported("integer kernels on integer images (integer arithmetic) are not "
-                               "part of the GB300 path")
+    if np.issubdtype(kdt, np.integer):
+        if img_kind in ("F32", "N0F8", "N0F16"):
+            return "F32"
+        if img_kind in INT_KINDS:
+            kk = _INT_OF_DTYPE.get(np.dtype(kdt))
+            if kk is None:
+                raise _abi.Unsupported("kernel eltype %s" % kdt)
+            return img_kind if np.dtype(kdt) == np.bool_ else _promote_int(img_kind, kk)
     raise _abi.Unsupported("kernel eltype %s" % kdt)
 
 
 def filter_type(img_kind, kernel):
     """src/imfilter.jl:1131-1154."""
     if isinstance(kernel, LaplacianKernel):
-        return {"F32": "F32", "F64": "F64", "N0F8": "F32", "U8": "I16"}[img_kind]
+        # float32 for Normed, the type itself for signed integers, signed_type for unsigned
+        return {"F32": "F32", "F64": "F64", "N0F8": "F32", "N0F16": "F32", "U8": "I16", "U16": "I32",
+                "I8": "I8", "I16": "I16", "I32": "I32", "I64": "I64"}[img_kind]
     if isinstance(kernel, tuple):
         kinds = [filter_type(img_kind, k) for k in kernel]
         if "F64" in kinds:
             return "F64"
+        if kinds and all(k in INT_KINDS for k in kinds):
+            r = kinds[0]
+            for k in kinds[1:]:
+                r = _promote_int(r, k)
+            return r
+        if "F32" in kinds:
+            return "F32"
         return kinds[0] if kinds else {"F64": "F64"}.get(img_kind, "F32")
     return _promote_one(img_kind, _kernel_dtype(kernel))
 
@@ -471,9 +506,140 @@ def _imfilter_na(out, img, kernel, border, alg, kind, okind):
     return out
 
 
+def convert_(out, img):
+    """out .= convert.(eltype(out), img) on the GPU (ifx_convert): integer,
+    N0f16 and other eltypes to Float32/Float64, and Float64 to integers (a value
+    that is not an integer of the target's range raises InexactError, as the
+    reference does when it stores a result)."""
+    kind, okind = kind_of(img), kind_of(out)
+    if not isinstance(img, DeviceArray):
+        img = host_view(img, kind)
+    ctx = _ctx()
+    try:
+        _abi.check(ctx.lib.ifx_convert(ctx.handle, _desc(out, okind), _desc(img, kind), stream_for(img, out)))
+    except _abi.ArgumentError as e:
+        if "InexactError" in str(e):
+            raise _abi.InexactError(str(e))
+        raise
+    return out
+
+
+def _fill_in_eltype(border, kind):
+    """Fill(v) holds v converted to the image eltype (src/borderarray.jl:11-20):
+    an integer for integer images (InexactError otherwise), the nearest code
+    for N0f16."""
+    v = float(border.value)
+    if kind in INT_KINDS:
+        if v != int(v):
+            raise _abi.InexactError("Fill value %r for an integer image" % (border.value,))
+        return float(int(v))
+    if kind == "N0F16":
+        return round(v * 65535) / 65535.0
+    return v
+
+
+def _bound_sum_abs(kernel):
+    """An upper bound of sum |weights| over the (cascaded) kernel."""
+    b = 1.0
+    for k in kernel:
+        if iscopy(k):
+            continue
+        if isinstance(k, LaplacianKernel):
+            b *= 4.0 * sum(1 for f in k.flags if f)
+        elif isinstance(k, ReshapedOneD):
+            b *= float(np.sum(np.abs(np.asarray(k.data.data, np.float64))))
+        else:
+            b *= float(np.sum(np.abs(np.asarray(getattr(k, "data", k), np.float64))))
+    return b
+
+
+def _imfilter_converted(out, img, kernel, border, alg, kind, okind):
+    """Images the filters do not take directly (Int8..Int64, UInt16, N0f16) and
+    integer results: the image is converted on the GPU to a compute eltype that
+    holds its values exactly -- Float32 for 8- and 16-bit values, Float64 for
+    32- and 64-bit integers and whenever the result is an integer (integer
+    kernels on integer images accumulate exactly in Float64 while every partial
+    sum stays below 2^53, checked from max|img| and sum |k|) -- filtered there,
+    and an integer result is converted back (InexactError when it does not fit,
+    as the reference's store would raise)."""
+    int_out = okind in INT_KINDS
+    ct = "F64" if (int_out or kind in ("I32", "I64")) else "F32"
+    if kind in ("F32", "F64") and not int_out:
+        ct = kind
+    tmp = alloc_like(img, img.shape, ct)
+    convert_(tmp, img)
+    if int_out:
+        m = maxabs(tmp)
+        if not m * _bound_sum_abs(kernel) < 2.0 ** 53:
+            raise _abi.Unsupported("integer filtering whose partial sums may exceed 2^53")
+    if isinstance(border, Fill):
+        border = Fill(_fill_in_eltype(border, kind), border.lo, border.hi) if border.lo is not None \
+            else Fill(_fill_in_eltype(border, kind))
+    res = alloc_like(img, img.shape, "F64") if int_out else out
+    imfilter_(res, tmp, kernel, border, alg)
+    if int_out:
+        convert_(out, res)
+    return out
+
+
+def maxabs(img):
+    """maximum(abs, img) on the GPU (ifx_maxabs)."""
+    kind = kind_of(img)
+    if not isinstance(img, DeviceArray):
+        img = host_view(img, kind)
+    r = C.c_double(0)
+    ctx = _ctx()
+    _abi.check(ctx.lib.ifx_maxabs(ctx.handle, _desc(img, kind), C.byref(r), stream_for(img)))
+    return r.value
+
+
+def _shift_kernel(kernel):
+    """A processed kernel of the image axes as a kernel of the (channel, image
+    axes...) array: nothing along the channel axis."""
+    out = []
+    for k in kernel:
+        if isinstance(k, ReshapedOneD):
+            out.append(ReshapedOneD(k.data, k.N + 1, k.axis + 1))
+        elif isinstance(k, LaplacianKernel):
+            out.append(LaplacianKernel((False,) + k.flags))
+        elif isinstance(k, OffsetKernel):
+            out.append(OffsetKernel(np.asarray(k.data)[None], (0,) + tuple(k.first)))
+        else:
+            raise _abi.Unsupported("kernel %r on an RGB image" % (k,))
+    return tuple(out)
+
+
+def _shift_border(border):
+    if isinstance(border, (NA, Inner, NoPad)):
+        raise _abi.Unsupported("%r borders of RGB images" % (border,))
+    if getattr(border, "lo", None) is not None:
+        lo, hi = (0,) + tuple(border.lo), (0,) + tuple(border.hi)
+        return Fill(border.value, lo, hi) if isinstance(border, Fill) else type(border)(border.style, lo, hi)
+    return border
+
+
+def _imfilter_rgb(img, kernel, border, alg, T, out=None):
+    """imfilter of an RGB image: the channel planes as one array with the
+    channel axis first, filtered along the image axes only."""
+    kind = kind_of(img.data)
+    kernel = factorkernel(kernel)
+    if T is None:
+        T = filter_type(kind, kernel)
+    if T in INT_KINDS:
+        raise _abi.Unsupported("RGB images with integer results")
+    k3 = _shift_kernel(kernel)
+    b3 = _shift_border(borderinstance(border))
+    if out is None:
+        out = RGB(alloc_like(img.data, img.data.shape, T))
+    imfilter_(out.data, img.data, k3, b3, alg)
+    return out
+
+
 def imfilter(img, kernel, border="replicate", alg=None, T=None):
     """imfilter([T], img, kernel, [border="replicate"], [alg]) (src/imfilter.jl:1-27).
     With Inner() the result covers only the interior and carries `first`."""
+    if isinstance(img, RGB):
+        return _imfilter_rgb(img, kernel, border, alg, T)
     kind = kind_of(img)
     if not isinstance(img, DeviceArray):
         img = host_view(img, kind)
@@ -492,6 +658,10 @@ def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
     """imfilter!(out, img, kernel, [border], [alg]) (src/imfilter.jl:204-254);
     imfilter!(out, img, kernel, NoPad(), inds) computes only out[inds] (1-based
     (first, last) per axis), reading only inside img (src/imfilter.jl:367-404)."""
+    if isinstance(img, RGB):
+        if not isinstance(out, RGB):
+            raise _abi.ArgumentError("an RGB image needs an RGB output")
+        return _imfilter_rgb(img, kernel, border, alg, kind_of(out.data), out)
     kind = kind_of(img)
     if not isinstance(img, DeviceArray):
         img = host_view(img, kind)
@@ -508,6 +678,11 @@ def imfilter_(out, img, kernel, border="replicate", alg=None, inds=None):
     kernel = factorkernel(kernel)
     nd = img.ndim
     border = borderinstance(border)
+    lap_u8 = kind == "U8" and okind == "I16" and all(isinstance(k, LaplacianKernel) or iscopy(k) for k in kernel)
+    if kind not in NATIVE_KINDS or (okind in INT_KINDS and not lap_u8):
+        if isinstance(border, (NA, Inner)) or inds is not None or isinstance(border, NoPad):
+            raise _abi.Unsupported("NA/Inner/NoPad filtering of %s images" % kind)
+        return _imfilter_converted(out, img, kernel, border, alg, kind, okind)
     if isinstance(alg, Algorithm.FFT) and inds is None and isinstance(border, NoPad):
         # _imfilter_fft! with NoPad (src/imfilter.jl:819-841): the circular
         # correlation over the unpadded image, which is what a circular

@@ -15,7 +15,8 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from .arrays import DeviceArray, N0f8Array, alloc_like, host_view, kind_of, ptr_strides, stream_for
+from .arrays import (INT_KINDS, NATIVE_KINDS, DeviceArray, N0f8Array, N0f16Array, alloc_like, host_view,
+                     kind_of, ptr_strides, stream_for)
 from .borders import Inner, border_struct, borderinstance
 
 
@@ -89,7 +90,93 @@ def resolve_window(window, nd, allow_even=False):
     return wf, wl
 
 
-_MEDIAN_OUT = {"N0F8": "F32", "U8": "F64", "F32": "F32", "F64": "F64"}
+# eltype of Statistics.middle of one value: Float64 for integers, Float32 for
+# the 8/16-bit Normed types (taken as Float32, like Float32(::N0f8)), the float itself
+_MEDIAN_OUT = {"N0F8": "F32", "N0F16": "F32", "U8": "F64", "F32": "F32", "F64": "F64", "I8": "F64",
+               "I16": "F64", "U16": "F64", "I32": "F64", "I64": "F64"}
+
+
+def _index_sel(indices, shape):
+    """Julia index ranges per axis (1-based values: range(1, 11, 2) is 1:2:10,
+    or a list of indices) -> numpy/torch selectors and the result's shape."""
+    if not isinstance(indices, (tuple, list)) or (len(indices) and isinstance(indices[0], (int, np.integer))):
+        indices = (indices,)
+    if len(indices) != len(shape):
+        raise _abi.DimensionMismatch("indices need one range per axis")
+    sel, out_shape = [], []
+    for r, n in zip(indices, shape):
+        vals = list(r) if not isinstance(r, (int, np.integer)) else [int(r)]
+        if any(v < 1 or v > n for v in vals):
+            raise _abi.DimensionMismatch("indices outside the image's axes")
+        if len(vals) >= 2 and all(b - a == vals[1] - vals[0] for a, b in zip(vals, vals[1:])) and vals[1] > vals[0]:
+            sel.append(slice(vals[0] - 1, vals[-1], vals[1] - vals[0]))
+        elif len(vals) == 1:
+            sel.append(slice(vals[0] - 1, vals[0]))
+        else:
+            sel.append(np.asarray(vals, dtype=np.int64) - 1)
+        out_shape.append(len(vals))
+    return tuple(sel), tuple(out_shape)
+
+
+def _take(full, sel, lead):
+    """full[lead + sel] as a new array on the same side."""
+    if isinstance(full, DeviceArray):
+        t = full.tensor
+        for ax, s_ in enumerate(lead + sel):
+            if isinstance(s_, slice):
+                idx = [slice(None)] * t.dim()
+                idx[ax] = s_
+                t = t[tuple(idx)]
+            else:
+                import torch
+                t = t.index_select(ax, torch.as_tensor(s_, device=t.device))
+        r = DeviceArray.empty(tuple(t.shape), full.kind, t.device)
+        r.tensor.copy_(t)
+        return r
+    a = full
+    for ax, s_ in enumerate(lead + sel):
+        idx = [slice(None)] * a.ndim
+        idx[ax] = s_
+        a = a[tuple(idx)]
+    return np.asfortranarray(a).view(type(full)) if isinstance(full, np.ndarray) else a
+
+
+def _converted_rank(f, img, window, border, kind, name):
+    """Rank filters of Int8..Int64, UInt16 and N0f16 images: the values (for
+    N0f16 the codes, whose order is the values') are converted exactly to
+    Float64 on the GPU, filtered there, and converted to the result's eltype
+    (the image's for extrema / minimum / maximum)."""
+    from .filtering import convert_, maxabs
+    codes = img
+    if kind == "N0F16":                      # the codes, as UInt16
+        codes = DeviceArray(img.tensor, "U16") if isinstance(img, DeviceArray) else np.asarray(img).view(np.uint16)
+    tmp = alloc_like(img, img.shape, "F64")
+    convert_(tmp, codes)
+    if kind == "I64" and not maxabs(tmp) < 2.0 ** 53:
+        raise _abi.Unsupported("Int64 rank filters with values beyond 2^53")
+    b = border
+    if b is not None:
+        from .filtering import _fill_in_eltype
+        from .borders import Fill
+        bi = borderinstance(b)
+        if isinstance(bi, Fill):
+            v = _fill_in_eltype(bi, kind)
+            b = Fill(round(v * 65535) if kind == "N0F16" else v, bi.lo, bi.hi) if bi.lo is not None \
+                else Fill(round(v * 65535) if kind == "N0F16" else v)
+    res = mapwindow(f, tmp, window, border=b)
+    if name == "median":
+        if kind != "N0F16":
+            return res                        # Float64 (middle of an integer)
+        c16 = alloc_like(img, res.shape, "U16")
+        convert_(c16, res)
+        out = alloc_like(img, res.shape, "F32")
+        convert_(out, DeviceArray(c16.tensor, "N0F16") if isinstance(c16, DeviceArray) else c16.view(N0f16Array))
+        return out
+    back = alloc_like(img, res.shape, "U16" if kind == "N0F16" else kind)
+    convert_(back, res)
+    if kind == "N0F16":
+        return DeviceArray(back.tensor, "N0F16") if isinstance(back, DeviceArray) else back.view(N0f16Array)
+    return back
 
 
 def mapwindow(f, img, window, border=None, indices=None):
@@ -101,8 +188,16 @@ def mapwindow(f, img, window, border=None, indices=None):
     if not isinstance(img, DeviceArray):
         img = host_view(img, kind)
     name = _fname(f)
+    if indices is not None:
+        # mapwindow(f, img, window; indices) == mapwindow(f, img, window)[indices...]
+        # (src/mapwindow.jl:95-121, test/mapwindow.jl:131-150)
+        full = mapwindow(f, img, window, border=border)
+        sel, _ = _index_sel(indices, img.shape)
+        return _take(full, sel, (slice(None),) if name == "extrema" else ())
     if isinstance(border, Inner):
         return _mapwindow_inner(f, img, window, name)
+    if kind not in NATIVE_KINDS:
+        return _converted_rank(f, img, window, border, kind, name)
     if name == "extrema":
         shape = (2,) + tuple(img.shape)
         if isinstance(img, DeviceArray):
@@ -142,9 +237,15 @@ def _mapwindow_inner(f, img, window, name):
 
 
 def mapwindow_(f, out, img, window, border=None, indices=None):
-    """mapwindow!(f, out, img, window; border) (src/mapwindow.jl:113-121)."""
-    if indices is not None:
-        raise _abi.Unsupported("mapwindow indices= is not part of the GB300 path")
+    """mapwindow!(f, out, img, window; border, indices) (src/mapwindow.jl:113-121)."""
+    if indices is not None or kind_of(img) not in NATIVE_KINDS:
+        res = mapwindow(f, img, window, border=border, indices=indices)
+        if isinstance(out, DeviceArray):
+            out.tensor.copy_(res.tensor)
+        else:
+            out[...] = np.asarray(res).view(np.asarray(out).dtype) if np.asarray(res).dtype == np.asarray(out).dtype \
+                else np.asarray(res)
+        return out
     kind = kind_of(img)
     if not isinstance(img, DeviceArray):
         img = host_view(img, kind)

@@ -54,7 +54,13 @@ typedef enum {                     /* element types of arrays crossing the ABI  
     IFX_F64 = 1,                   /* Float64 / Gray{Float64}                           */
     IFX_N0F8 = 2,                  /* N0f8 / Gray{N0f8}: 8-bit code c means c/255       */
     IFX_U8 = 3,                    /* UInt8: 8-bit code c means c                       */
-    IFX_I16 = 4                    /* Int16 (Laplacian of UInt8, src/imfilter.jl:1139)  */
+    IFX_I16 = 4,                   /* Int16 (Laplacian of UInt8, src/imfilter.jl:1139)  */
+    /* element types that only ifx_convert takes (the filters take the types above) */
+    IFX_I8 = 5,                    /* Int8                                               */
+    IFX_U16 = 6,                   /* UInt16                                             */
+    IFX_I32 = 7,                   /* Int32                                              */
+    IFX_I64 = 8,                   /* Int64 / Int                                        */
+    IFX_N0F16 = 9                  /* N0f16 / Gray{N0f16}: 16-bit code c means c/65535   */
 } ifx_eltype;
 
 typedef enum {                     /* border styles (src/border.jl:136-248, 465-555)    */
@@ -267,6 +273,18 @@ int ifx_findlocalextrema(ifx_context_t *ctx, const ifx_array_t *img, const int32
                          int32_t minima, int64_t *indices, double *values, int64_t capacity, int64_t *count,
                          void *stream);
 int ifx_maxabs(ifx_context_t *ctx, const ifx_array_t *img, double *result, void *stream);
+
+/* ---- element conversion -----------------------------------------------------
+ * out .= convert.(eltype(out), img) (the eltype conversions around the
+ * reference's imfilter!: its padded copy in the filter type,
+ * src/border.jl:324-331, and the store of each result, src/imfilter.jl:
+ * 660-666).  Any pair of the eltypes above, same axes.  To Float32/Float64: the
+ * value (N0f8 c/255 and N0f16 c/65535 correctly rounded; integers exactly, or
+ * rounded to nearest for Float32 beyond 2^24).  To an integer type: every
+ * value must be an integer in the type's range, else IFX_ERR_ARGUMENT
+ * (Julia's InexactError); such calls are synchronous (the check is read
+ * back).  To N0f8/N0f16: the value must be a code/255 (code/65535) exactly. */
+int ifx_convert(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, void *stream);
 
 /* ---- NA() borders ---------------------------------------------------------
  * The non-filter steps of NA filtering (_imfilter_na!, src/imfilter.jl:280-318;
