@@ -18,8 +18,8 @@ from ._abi import (ArgumentError, Cancelled, DimensionMismatch, ErrorException, 
 from .arrays import RGB, DeviceArray, N0f8Array, N0f16Array, n0f8, n0f16, rgb
 from .blobs import BlobLoG, blob_LoG, findlocalmaxima, findlocalminima, multiLoG
 from .borders import Fill, Inner, NA, NoPad, Pad, borderinstance, padarray
-from .filtering import (Algorithm, autotune, autotune_choice, convert_, factorkernel, filter_type, imfilter,
-                        imfilter_, imgradients, maxabs)
+from .filtering import (Algorithm, autotune, autotune_choice, autotune_clear, autotune_lookup, autotune_pin,
+                        convert_, factorkernel, filter_type, imfilter, imfilter_, imgradients, maxabs)
 from .kernels import (Kernel, KernelFactors, LaplacianKernel, OffsetKernel, ReshapedOneD, TriggsSdika,
                       centered, iscopy, kernelfactors)
 from .rank import extrema, mapwindow, mapwindow_, maximum, median, median_, minimum
@@ -36,6 +36,6 @@ __all__ = [
     "Inner", "NA", "NoPad", "BlobLoG", "blob_LoG", "multiLoG", "findlocalmaxima", "findlocalminima", "Kernel", "KernelFactors", "centered", "kernelfactors", "Algorithm",
     "OffsetArray", "OffsetKernel", "ReshapedOneD", "LaplacianKernel", "TriggsSdika", "DeviceArray", "N0f8Array",
     "n0f8", "N0f16Array", "n0f16", "RGB", "rgb", "convert_", "maxabs", "InexactError", "median", "median_", "extrema", "minimum", "maximum", "filter_type", "factorkernel",
-    "iscopy", "borderinstance", "autotune", "autotune_choice", "ArgumentError", "DimensionMismatch", "ErrorException",
+    "iscopy", "borderinstance", "autotune", "autotune_choice", "autotune_lookup", "autotune_pin", "autotune_clear", "ArgumentError", "DimensionMismatch", "ErrorException",
     "CudaError", "OutOfMemory", "Unsupported", "Cancelled", "launch_count", "library_path",
 ]

@@ -87,6 +87,14 @@ class IfxRequest(C.Structure):
 OP_FACTORED2D, OP_GRADIENTS2D, OP_LAPLACIAN2D, OP_MEDIAN2D = 1, 2, 3, 4
 
 
+class IfxTuneChoice(C.Structure):
+    _fields_ = [("variant", C.c_int32), ("x_first", C.c_int32), ("tile_w", C.c_int32), ("tile_h", C.c_int32),
+                ("depth", C.c_int32), ("ms", C.c_double)]
+
+
+TUNE_SEP2D, TUNE_SEP3D = 0, 1
+
+
 class IfxServerConfig(C.Structure):
     _fields_ = [("hbm_cap_bytes", C.c_int64), ("max_batch", C.c_int32), ("max_inflight", C.c_int32)]
 
@@ -108,7 +116,8 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_na_prepare", "ifx_na_divide", "ifx_na_normalize_separable",
            "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs", "ifx_imfilter_fft",
            "ifx_imfilter_iir", "ifx_autotune", "ifx_autotune_choice", "ifx_server_cancel",
-           "ifx_server_inject_launch_error", "ifx_server_pause", "ifx_debug_force_wait_timeout", "ifx_convert"]
+           "ifx_server_inject_launch_error", "ifx_server_pause", "ifx_debug_force_wait_timeout", "ifx_convert",
+           "ifx_autotune_lookup", "ifx_autotune_pin", "ifx_autotune_clear"]
 
 _lib = None
 _lock = threading.Lock()
@@ -174,6 +183,11 @@ def load(path: str = LIB_PATH):
         lib.ifx_autotune.argtypes = [vp, C.c_int32, C.c_char_p]
         lib.ifx_autotune_choice.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int64,
                                             C.c_int64, P(C.c_int32), P(C.c_int32), P(C.c_double)]
+        lib.ifx_autotune_lookup.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, P(C.c_int32), C.c_int32,
+                                            P(C.c_int64), P(IfxTuneChoice)]
+        lib.ifx_autotune_pin.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, P(C.c_int32), C.c_int32,
+                                         P(C.c_int64), P(IfxTuneChoice)]
+        lib.ifx_autotune_clear.argtypes = [vp]
         lib.ifx_imfilter_iir.argtypes = [vp, P(IfxArray), P(IfxArray), C.c_int32, P(IfxIir), P(IfxBorder), vp]
         lib.ifx_imfilter_fft.argtypes = [vp, P(IfxArray), P(IfxArray), P(C.c_double), P(C.c_int64),
                                          P(C.c_int64), P(IfxBorder), vp]

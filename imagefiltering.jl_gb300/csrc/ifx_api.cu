@@ -473,22 +473,27 @@ static int run_cascade(Call &c, const ifx_array_t &imgd, const void *img, const 
     }
 
     // 3-D with one factor per axis in axis order: the z sweep into an FP32
-    // volume and the x/y TMA sweep over its planes, or (rows off the copy
-    // engine's rules, long z factors) the fused z-marching kernel
+    // volume and the x/y TMA sweep over its planes (the default), or the fused
+    // z-marching kernel (rows off the copy engine's rules, long z factors, or
+    // the autotuner's choice)
     if (nd == 3 && ct == IFX_F32 && facs.size() == 3 && facs[0].axis == 0 && facs[1].axis == 1 &&
         facs[2].axis == 2) {
         Sep3dArgs a{img, imgd.eltype, out, outd.eltype, n[0], n[1], n[2], 1,
                     facs[0].first, facs[0].len, facs[1].first, facs[1].len, facs[2].first, facs[2].len,
                     facs[0].w, facs[1].w, facs[2].w, border->style, fill};
-        if (sep3d_split_applies(a)) {
+        const bool split = sep3d_split_applies(a);
+        const bool fused = sep3d_supported(facs[0].len, facs[1].len, facs[2].len, n[0], n[1], n[2], 1);
+        if (split || fused) {
+            // the FP32 volume only when the split sweeps may run: no cached
+            // choice of the fused kernel
+            TuneChoice ch;
+            const bool fused_cached = fused && autotune_lookup3(a, &ch) && ch.variant == 2;
             void *vol = nullptr;
-            rc = slot_get(c.ctx, tmp_slot_base, (size_t)n[0] * n[1] * n[2] * sizeof(float), &vol);
-            if (rc) return rc;
-            IFX_CUDA(launch_sep3d_split(a, static_cast<float *>(vol), c.s));
-            return IFX_OK;
-        }
-        if (sep3d_supported(facs[0].len, facs[1].len, facs[2].len, n[0], n[1], n[2], 1)) {
-            IFX_CUDA(launch_sep3d(a, c.s));
+            if (split && !fused_cached) {
+                rc = slot_get(c.ctx, tmp_slot_base, (size_t)n[0] * n[1] * n[2] * sizeof(float), &vol);
+                if (rc) return rc;
+            }
+            IFX_CUDA(launch_sep3d_tuned(a, static_cast<float *>(vol), c.s, !c.host));
             return IFX_OK;
         }
     }
@@ -1297,21 +1302,67 @@ int ifx_autotune_choice(ifx_context_t *ctx, int32_t in_type, int32_t out_type, i
     IFX_RANGE("ifx_autotune_choice");
     (void)ctx;
     if (!x_first || !variant) return fail(IFX_ERR_ARGUMENT, "NULL output");
-    Sep2dArgs a{};
-    a.in_type = in_type;
-    a.out_type = out_type;
-    a.kx = kx;
-    a.ky = ky;
-    a.style = fill ? IFX_FILL : IFX_REPLICATE;
-    a.nx = (int)nx;
-    a.ny = (int)ny;
-    a.compute_f64 = in_type == IFX_F64;
-    int xf, var;
-    float t = 0.0f;
-    if (!autotune_lookup(a, &xf, &var, &t)) return fail(IFX_ERR_ARGUMENT, "no tuned choice for this key");
-    *x_first = xf;
-    *variant = var;
-    if (ms) *ms = t;
+    TuneChoice ch;
+    if (!autotune_lookup_key(TUNE_SEP2D, in_type, out_type, kx, ky, 1, fill, nx, ny, 1, &ch))
+        return fail(IFX_ERR_ARGUMENT, "no tuned choice for this key");
+    *x_first = ch.x_first;
+    *variant = ch.variant;
+    if (ms) *ms = ch.ms;
+    return IFX_OK;
+}
+
+static int check_tune_key(int32_t path, const int32_t *taps, const int64_t *size)
+{
+    if (path != IFX_TUNE_SEP2D && path != IFX_TUNE_SEP3D) return fail(IFX_ERR_ARGUMENT, "unknown tuner path");
+    if (!taps || !size) return fail(IFX_ERR_ARGUMENT, "NULL key");
+    for (int d = 0; d < 3; ++d)
+        if (taps[d] < 1 || size[d] < 0) return fail(IFX_ERR_ARGUMENT, "bad key: taps >= 1, sizes >= 0");
+    return IFX_OK;
+}
+
+int ifx_autotune_lookup(ifx_context_t *ctx, int32_t path, int32_t in_type, int32_t out_type, const int32_t *taps,
+                        int32_t fill, const int64_t *size, ifx_tune_choice_t *choice)
+{
+    IFX_RANGE("ifx_autotune_lookup");
+    (void)ctx;
+    int rc;
+    if ((rc = check_tune_key(path, taps, size))) return rc;
+    if (!choice) return fail(IFX_ERR_ARGUMENT, "NULL output");
+    TuneChoice ch;
+    if (!autotune_lookup_key(path, in_type, out_type, taps[0], taps[1], taps[2], fill, size[0], size[1], size[2],
+                             &ch))
+        return fail(IFX_ERR_ARGUMENT, "no tuned choice for this key");
+    choice->variant = ch.variant;
+    choice->x_first = ch.x_first;
+    choice->tile_w = ch.tile_w;
+    choice->tile_h = ch.tile_h;
+    choice->depth = ch.depth;
+    choice->ms = ch.ms;
+    return IFX_OK;
+}
+
+int ifx_autotune_pin(ifx_context_t *ctx, int32_t path, int32_t in_type, int32_t out_type, const int32_t *taps,
+                     int32_t fill, const int64_t *size, const ifx_tune_choice_t *choice)
+{
+    IFX_RANGE("ifx_autotune_pin");
+    (void)ctx;
+    int rc;
+    if ((rc = check_tune_key(path, taps, size))) return rc;
+    if (!choice) return fail(IFX_ERR_ARGUMENT, "NULL choice");
+    const ifx_tune_choice_t &c = *choice;
+    if (c.variant != 1 && c.variant != 2) return fail(IFX_ERR_ARGUMENT, "variant must be 1 or 2");
+    if (c.x_first != 0 && c.x_first != 1) return fail(IFX_ERR_ARGUMENT, "x_first must be 0 or 1");
+    if (c.tile_w < 0 || c.tile_h < 0 || c.depth < 0) return fail(IFX_ERR_ARGUMENT, "negative tile or depth");
+    autotune_pin_key(path, in_type, out_type, taps[0], taps[1], taps[2], fill, size[0], size[1], size[2],
+                     TuneChoice{c.variant, c.x_first, c.tile_w, c.tile_h, c.depth, (float)c.ms});
+    return IFX_OK;
+}
+
+int ifx_autotune_clear(ifx_context_t *ctx)
+{
+    IFX_RANGE("ifx_autotune_clear");
+    (void)ctx;
+    autotune_clear();
     return IFX_OK;
 }
 

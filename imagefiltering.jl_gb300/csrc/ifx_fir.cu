@@ -180,6 +180,9 @@ cudaError_t launch_pass_box(const PassBoxArgs &a, cudaStream_t s)
 //  2. first pass over the whole tile height (or width), i.e. over the halo
 //     the second pass needs -- the reference's cascade ranges;
 //  3. second pass, store in the output eltype.
+// The tile is TX = 64 or 128 wide for FP32, 32 or 64 for FP64 (a template
+// parameter) and TY = 8..128 rows (a multiple of 8); the default is 64 x 64
+// for FP32 and 32 x 32 for FP64, the autotuner may pick another.
 // =========================================================================
 template <class Tc> struct Sep2dTile;
 template <> struct Sep2dTile<float> { static constexpr int TX = 64, TY = 64; };
@@ -190,9 +193,8 @@ template <class Tc> struct Sep2dW { Tc wx[IFX_MAX_TAPS + 3]; Tc wy[IFX_MAX_TAPS 
 
 
 template <class Tc>
-static size_t sep2d_smem(int kx, int ky, int x_first)
+static size_t sep2d_smem(int kx, int ky, int x_first, int TX = Sep2dTile<Tc>::TX, int TY = Sep2dTile<Tc>::TY)
 {
-    const int TX = Sep2dTile<Tc>::TX, TY = Sep2dTile<Tc>::TY;
     size_t t, i;
     if (x_first) {
         t = (size_t)(TY + ky - 1) * (TX + up4(kx));
@@ -218,13 +220,13 @@ __device__ __forceinline__ void corr_tc(const Tc *p, int step, const Tc *w, int 
     corr_run<Tc, NB>(p, step, w, k, acc);
 }
 
-template <class Tin, class Tc, class Tout>
+template <class Tin, class Tc, class Tout, int TX>
 __global__ void __launch_bounds__(256)
 k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
-        int fx, int kx, int fy, int ky, int x_first, int style, Tc fill, bool norm,
+        int fx, int kx, int fy, int ky, int x_first, int style, Tc fill, bool norm, int TY,
         const __grid_constant__ Sep2dW<Tc> W)
 {
-    constexpr int TX = Sep2dTile<Tc>::TX, TY = Sep2dTile<Tc>::TY, NB = kSepNB;
+    constexpr int NB = kSepNB, lx = TX == 32 ? 5 : (TX == 64 ? 6 : 7), ls = lx - 3;   // log2 TX, log2 segments
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tc *sm = reinterpret_cast<Tc *>(smem_raw);
     const int kx4 = up4(kx), ky4 = up4(ky);
@@ -277,9 +279,8 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
     Tc acc[NB];
     if (x_first) {
         // 2. x pass over RT rows -> I (RT rows valid, pad rows zero), row stride TX
-        const int segs = TX / NB;
-        for (int it = tid; it < (TY + ky4) * segs; it += nth) {
-            const int r = it / segs, c0 = (it - r * segs) * NB;
+        for (int it = tid; it < ((TY + ky4) << ls); it += nth) {
+            const int r = it >> ls, c0 = (it & ((1 << ls) - 1)) * NB;
             if (r < RT) {
                 corr_tc<Tc, NB>(T + (size_t)r * CT + c0, 1, wx, kx, acc);
 #pragma unroll
@@ -292,8 +293,8 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         __syncthreads();
         // 3. y pass down each column, 8 rows per item
         const int rsegs = TY / NB;
-        for (int it = tid; it < TX * rsegs; it += nth) {
-            const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
+        for (int it = tid; it < (rsegs << lx); it += nth) {
+            const int rs = it >> lx, c = it & (TX - 1), r0 = rs * NB;
             corr_tc<Tc, NB>(I + (size_t)r0 * TX + c, TX, wy, ky, acc);
             const int x = tx0 + c;
             if (x < nx) {
@@ -321,9 +322,8 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
         }
         __syncthreads();
         // 3. x pass along rows
-        const int segs = TX / NB;
-        for (int it = tid; it < TY * segs; it += nth) {
-            const int r = it / segs, c0 = (it - r * segs) * NB;
+        for (int it = tid; it < (TY << ls); it += nth) {
+            const int r = it >> ls, c0 = (it & ((1 << ls) - 1)) * NB;
             corr_tc<Tc, NB>(I + (size_t)r * CI + c0, 1, wx, kx, acc);
             const int y = ty0 + r;
             if (y < ny) {
@@ -337,21 +337,40 @@ k_sep2d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny,
     }
 }
 
+// The gather kernel's tile for `a`: the requested one when the kernel takes
+// it (width 32, 64 or 128; height a multiple of 8 up to 128; shared memory
+// within 200 KB), else the default.
+template <class Tc> static void sep2d_gather_tile(const Sep2dArgs &a, int *tw, int *th)
+{
+    const int w = a.tile_w, h = a.tile_h;
+    const bool wide_ok = sizeof(Tc) == 4 ? (w == 64 || w == 128) : (w == 32 || w == 64);
+    if (wide_ok && h >= 8 && h <= 128 && h % 8 == 0 &&
+        sep2d_smem<Tc>(a.kx, a.ky, a.x_first, w, h) <= 200 * 1024 && (a.ny + h - 1) / h <= 65535) {
+        *tw = w;
+        *th = h;
+    } else {
+        *tw = Sep2dTile<Tc>::TX;
+        *th = Sep2dTile<Tc>::TY;
+    }
+}
+
 template <class Tin, class Tc, class Tout>
 static cudaError_t sep2d_t(const Sep2dArgs &a, cudaStream_t s)
 {
-    constexpr int TX = Sep2dTile<Tc>::TX, TY = Sep2dTile<Tc>::TY;
+    int TX, TY;
+    sep2d_gather_tile<Tc>(a, &TX, &TY);
     Sep2dW<Tc> W;
     memset(&W, 0, sizeof W);
     for (int t = 0; t < a.kx; ++t) W.wx[t] = (Tc)a.wx[t];
     for (int t = 0; t < a.ky; ++t) W.wy[t] = (Tc)a.wy[t];
-    const size_t smem = sep2d_smem<Tc>(a.kx, a.ky, a.x_first);
-    auto kern = k_sep2d<Tin, Tc, Tout>;
+    const size_t smem = sep2d_smem<Tc>(a.kx, a.ky, a.x_first, TX, TY);
+    constexpr int TW0 = Sep2dTile<Tc>::TX;          // the two widths: the default and twice it
+    auto kern = TX == TW0 ? k_sep2d<Tin, Tc, Tout, TW0> : k_sep2d<Tin, Tc, Tout, 2 * TW0>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY);
     kern<<<grid, 256, smem, s>>>((const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.fx, a.kx, a.fy,
-                                 a.ky, a.x_first, a.style, (Tc)a.fill, a.in_type == IFX_N0F8, W);
+                                 a.ky, a.x_first, a.style, (Tc)a.fill, a.in_type == IFX_N0F8, TY, W);
     note_launch();
     return cudaGetLastError();
 }
@@ -378,8 +397,13 @@ static cudaError_t sep2d_t(const Sep2dArgs &a, cudaStream_t s)
 // value pairs built by moves, which measured slower).  The passes are
 // those of k_sep2d (cascade order, pass ranges); outputs of FP32 results
 // widen exactly.
+//
+// Tiles are TX = 64 or 128 outputs wide (a 128-wide tile runs the 64-wide
+// row-pass layout on each half, halves on alternate warps) and TY = 8..128
+// rows (a multiple of 8).  The default is 64 wide and as tall as keeps three
+// CTAs on an SM; the autotuner may pick another shape.
 // =========================================================================
-constexpr int kStTX = 64, kStTY = 64, kStNB = 16, kStNBY = 8;
+constexpr int kStTX = 64, kStTY = 64, kStNB = 16, kStNBY = 8, kStMaxTX = 128, kStMaxTY = 128;
 
 // Two adjacent outputs of an FP32 result (8-byte store for Float32, 16-byte
 // for Float64; the caller checks the alignment).  Float64: one value widens
@@ -406,15 +430,16 @@ struct SepTmaSmem {
     size_t raw, w, t, i, total;
 };
 
-__host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int x_first, int elt_bytes, int ty)
+__host__ __device__ inline SepTmaSmem sep_tma_smem(int kx, int ky, int x_first, int elt_bytes, int ty,
+                                                   int tx = kStTX)
 {
     SepTmaSmem L;
-    const int RV = ty + ky - 1, CV = kStTX + kx - 1;
+    const int RV = ty + ky - 1, CV = tx + kx - 1;
     // Windows start on 16-byte boundaries.  Float32: 3 floats of slack for
     // the 16-byte loads; 8-bit: codes are converted four at a time.
     L.boxw = elt_bytes == 4 ? st_pitch(CV + 3) : (CV + 3 + 15) / 16 * 16;
     L.st = st_pitch(CV + 3);
-    L.si = x_first ? st_pitch(kStTX) : st_pitch(CV + 3);
+    L.si = x_first ? st_pitch(tx) : st_pitch(CV + 3);
     L.raw = st_round128((size_t)L.boxw * RV * elt_bytes);
     L.w = st_round128(2 * (IFX_MAX_TAPS + 3) * sizeof(float2) + 256 * sizeof(float));
     L.t = elt_bytes == 1 ? st_round128((size_t)RV * L.st * sizeof(float)) : 0;
@@ -435,22 +460,23 @@ cudaError_t set_first_wait_tma(bool force_timeout)
     return cudaMemcpyToSymbol(g_first_wait_tma, &v, sizeof v);
 }
 
-template <class Tin, class Tout>
+template <class Tin, class Tout, int WSH>
 __global__ void __launch_bounds__(256)
 k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img, Tout *__restrict__ out,
             int nx, int ny, int fx, int kx, int fy, int ky, int x_first, int style, float fill, bool norm,
             int shift, int ty, int tiles_x, int tiles_per_slice, int tiles, int pair_store, int *err,
             const __grid_constant__ Sep2dW<float> W)
 {
-    constexpr int TX = kStTX, NB = kStNB, NBY = kStNBY;
-    const int TY = ty;                                      // a multiple of NBY, at most 64
+    constexpr int NB = kStNB, NBY = kStNBY, wsh = WSH;
+    constexpr int TX = kStTX << WSH;                        // 64 or 128
+    const int TY = ty;                                      // a multiple of NBY, at most kStMaxTY
     constexpr int ALIGN = 16 / (int)sizeof(Tin);          // x granularity of a box start
     extern __shared__ __align__(128) unsigned char st_smem[];
     __shared__ __align__(8) uint64_t bar[2];
-    __shared__ int src_row[64 + kCorrKmax], src_col[kStTX + kCorrKmax];   // border tiles' source maps
+    __shared__ int src_row[kStMaxTY + kCorrKmax], src_col[kStMaxTX + kCorrKmax];   // border tiles' source maps
     constexpr int kSrcFill = -1;
     const int RV = TY + ky - 1, CV = TX + kx - 1;
-    const SepTmaSmem L = sep_tma_smem(kx, ky, x_first, (int)sizeof(Tin), TY);
+    const SepTmaSmem L = sep_tma_smem(kx, ky, x_first, (int)sizeof(Tin), TY, TX);
     const int boxw = L.boxw;
     const unsigned first_tries = g_first_wait_tma;
     auto raw_buf = [&](int b) { return reinterpret_cast<Tin *>(st_smem + (size_t)b * L.raw); };
@@ -507,10 +533,11 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     // row-pass item -> (row, window start) over `rows` rows: two warps cover 16
     // rows x 4 starts, each 8-lane phase 4 rows x 2 starts; the last rows go in
     // groups of 8 rows x 4 starts per warp, each phase 8 rows x 1 start (both
-    // conflict-free for pitches 4 mod 8).  row_items(rows) items, whole warps.
-    auto row_items = [](int rows) { return 64 * (rows >> 4) + 32 * (((rows & 15) + 7) >> 3); };
-    auto row_item = [](int it, int rows, int &r, int &c0) {
-        const int lane = it & 31, grp = it >> 5, full = 2 * (rows >> 4);
+    // conflict-free for pitches 4 mod 8).  row_items(rows) items, whole warps,
+    // per 64 columns; a 128-wide tile gives its halves to alternate warps.
+    auto row_items = [&](int rows) { return (64 * (rows >> 4) + 32 * (((rows & 15) + 7) >> 3)) << wsh; };
+    auto row_item = [&](int it, int rows, int &r, int &c0) {
+        const int lane = it & 31, half = (it >> 5) & wsh, grp = it >> (5 + wsh), full = 2 * (rows >> 4);
         if (grp < full) {
             r = 16 * (grp >> 1) + 4 * (lane >> 3) + ((lane >> 1) & 3);
             c0 = NB * (2 * (grp & 1) + (lane & 1));
@@ -518,6 +545,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             r = 8 * grp + (lane & 7);              // rows 8*full onwards, 8 per warp
             c0 = NB * (lane >> 3);
         }
+        c0 += 64 * half;
     };
 
     int t = blockIdx.x;
@@ -639,8 +667,8 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             // y pass down each column pair, NBY rows per item: a warp covers one
             // 64-wide row block (256 contiguous bytes of I per load)
             float2 ya[NBY];
-            for (int it = tid; it < (TX / 2) * (TY / NBY); it += nth) {
-                const int rs = it / (TX / 2), c = 2 * (it - rs * (TX / 2)), r0 = rs * NBY;
+            for (int it = tid; it < (TY / NBY) << (5 + wsh); it += nth) {
+                const int rs = it >> (5 + wsh), c = 2 * (it & ((TX >> 1) - 1)), r0 = rs * NBY;
                 if (c >= need_x || r0 >= need_y) continue;
                 corr_col_x2<NBY>(I + (size_t)r0 * L.si + c, L.si, wy, ky, ya);
                 const int x = tx0 + c;
@@ -707,14 +735,35 @@ static int sep_tma_ty(int kx, int ky, int x_first, int elt_bytes)
     return ty;
 }
 
+// The TMA kernel's tile for `a`: the requested shape when the kernel takes it
+// (64 or 128 wide, a multiple of 8 rows up to 128, the box within the copy
+// engine's 256 x 256 limit, shared memory within 200 KB), else the default
+// (64 wide, sep_tma_ty rows, within 160 KB); false when neither fits.
+template <class Tin> static bool sep_tma_tile(const Sep2dArgs &a, int *tx, int *ty, SepTmaSmem *L)
+{
+    if (a.kx > kCorrKmax || a.ky > kCorrKmax) return false;
+    auto fits = [&](int w, int h, size_t cap) {
+        *L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin), h, w);
+        return L->boxw <= 256 && h + a.ky - 1 <= 256 && L->total <= cap;
+    };
+    const int w = a.tile_w, h = a.tile_h;
+    if ((w == kStTX || w == kStMaxTX) && h >= kStNBY && h <= kStMaxTY && h % kStNBY == 0 && fits(w, h, 200 * 1024)) {
+        *tx = w;
+        *ty = h;
+        return true;
+    }
+    *tx = kStTX;
+    *ty = sep_tma_ty(a.kx, a.ky, a.x_first, (int)sizeof(Tin));
+    return fits(*tx, *ty, 160 * 1024);
+}
+
 template <class Tin, class Tout>
 static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
 {
-    if (a.kx > kCorrKmax || a.ky > kCorrKmax) return false;
-    const int ty = sep_tma_ty(a.kx, a.ky, a.x_first, (int)sizeof(Tin));
+    int TX, ty;
+    SepTmaSmem L;
+    if (!sep_tma_tile<Tin>(a, &TX, &ty, &L)) return false;
     const int RV = ty + a.ky - 1;
-    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin), ty);
-    if (L.boxw > 256 || RV > 256 || L.total > 160 * 1024) return false;
     const int nsl = a.nsl > 1 ? a.nsl : 1;
     CUtensorMap map;
     const long long pitch = (long long)a.nx * (long long)sizeof(Tin);
@@ -731,7 +780,7 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     memset(&W, 0, sizeof W);
     for (int t = 0; t < a.kx; ++t) W.wx[t] = (float)a.wx[t];
     for (int t = 0; t < a.ky; ++t) W.wy[t] = (float)a.wy[t];
-    auto kern = k_sep2d_tma<Tin, Tout>;
+    auto kern = TX == kStMaxTX ? k_sep2d_tma<Tin, Tout, 1> : k_sep2d_tma<Tin, Tout, 0>;
     if ((*e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total)) !=
         cudaSuccess)
         return true;
@@ -746,7 +795,7 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     // tiles shift left so that tile windows start on 16-byte boundaries
     constexpr int ALIGN = 16 / (int)sizeof(Tin);
     const int shift = ((a.fx % ALIGN) + ALIGN) % ALIGN;
-    const int tiles_x = (a.nx + shift + kStTX - 1) / kStTX;
+    const int tiles_x = (a.nx + shift + TX - 1) / TX;
     const long long per_slice = (long long)tiles_x * ((a.ny + ty - 1) / ty);
     const long long tiles = per_slice * nsl;
     if (tiles > (1ll << 30)) return false;
@@ -768,13 +817,12 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
 // sep2d_tma_t, without a launch).
 template <class Tin> static bool sep2d_tma_fits(const Sep2dArgs &a)
 {
-    if (a.kx > kCorrKmax || a.ky > kCorrKmax) return false;
-    const int ty = sep_tma_ty(a.kx, a.ky, a.x_first, (int)sizeof(Tin));
+    int TX, ty;
+    SepTmaSmem L;
+    if (!sep_tma_tile<Tin>(a, &TX, &ty, &L)) return false;
     const int RV = ty + a.ky - 1;
-    const SepTmaSmem L = sep_tma_smem(a.kx, a.ky, a.x_first, (int)sizeof(Tin), ty);
-    if (L.boxw > 256 || RV > 256 || L.total > 160 * 1024) return false;
     const int nsl = a.nsl > 1 ? a.nsl : 1;
-    const long long tiles = (long long)((a.nx + 16 + kStTX - 1) / kStTX) * ((a.ny + ty - 1) / ty) * nsl;
+    const long long tiles = (long long)((a.nx + 16 + TX - 1) / TX) * ((a.ny + ty - 1) / ty) * nsl;
     CUtensorMap map;
     const long long pitch = (long long)a.nx * (long long)sizeof(Tin);
     return tiles <= (1ll << 30) &&
@@ -806,6 +854,19 @@ static bool launch_sep2d_tma(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
 size_t sep2d_smem_bytes(int kx, int ky, int x_first, int f64)
 {
     return f64 ? sep2d_smem<double>(kx, ky, x_first) : sep2d_smem<float>(kx, ky, x_first);
+}
+
+bool sep2d_tile_shape(const Sep2dArgs &a, int variant, int *tw, int *th)
+{
+    if (variant == 1) {
+        if (!sep2d_tma_applies(a)) return false;
+        SepTmaSmem L;
+        return is8(a.in_type) ? sep_tma_tile<uint8_t>(a, tw, th, &L) : sep_tma_tile<float>(a, tw, th, &L);
+    }
+    if (a.nsl > 1) return false;
+    if (a.compute_f64) sep2d_gather_tile<double>(a, tw, th);
+    else sep2d_gather_tile<float>(a, tw, th);
+    return true;
 }
 
 cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s)
@@ -858,7 +919,7 @@ __host__ __device__ inline size_t sep3d_smem_floats(int kx, int ky, int kz)
 template <class Tin, class Tout>
 __global__ void __launch_bounds__(256)
 k_sep3d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny, int nz, int fx, int kx,
-        int fy, int ky, int fz, int kz, int style, float fill, bool norm,
+        int fy, int ky, int fz, int kz, int style, float fill, bool norm, int zcd,
         const __grid_constant__ Sep3dW W)
 {
     constexpr int TX = k3TX, TY = k3TY, NB = 8;
@@ -874,8 +935,9 @@ k_sep3d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny, int
     for (int t = tid; t < ky; t += nth) wy[t] = W.wy[t];
     for (int t = tid; t < kz; t += nth) wz[t] = W.wz[t];
     const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
-    const int zc = blockIdx.z % ((nz + k3ZC - 1) / k3ZC), vol = blockIdx.z / ((nz + k3ZC - 1) / k3ZC);
-    const int z0 = zc * k3ZC, z1 = min(nz, z0 + k3ZC);
+    const int zchunks = (nz + zcd - 1) / zcd;               // zcd output slices per chunk
+    const int zc = blockIdx.z % zchunks, vol = blockIdx.z / zchunks;
+    const int z0 = zc * zcd, z1 = min(nz, z0 + zcd);
     const long long vstride = (long long)nx * ny * nz;
     const Tin *src = img + vol * vstride;
     Tout *dst = out + vol * vstride;
@@ -958,7 +1020,7 @@ k_sep3d(const Tin *__restrict__ img, Tout *__restrict__ out, int nx, int ny, int
 }
 
 template <class Tin, class Tout>
-static cudaError_t sep3d_t(const Sep3dArgs &a, cudaStream_t s)
+static cudaError_t sep3d_t(const Sep3dArgs &a, cudaStream_t s, int zcd)
 {
     Sep3dW W;
     memset(&W, 0, sizeof W);
@@ -969,10 +1031,10 @@ static cudaError_t sep3d_t(const Sep3dArgs &a, cudaStream_t s)
     auto kern = k_sep3d<Tin, Tout>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int zchunks = (a.nz + k3ZC - 1) / k3ZC;
+    const int zchunks = (a.nz + zcd - 1) / zcd;
     dim3 grid((a.nx + k3TX - 1) / k3TX, (a.ny + k3TY - 1) / k3TY, zchunks * a.nvol);
     kern<<<grid, 256, smem, s>>>((const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.nz, a.fx, a.kx, a.fy,
-                                 a.ky, a.fz, a.kz, a.style, (float)a.fill, a.in_type == IFX_N0F8, W);
+                                 a.ky, a.fz, a.kz, a.style, (float)a.fill, a.in_type == IFX_N0F8, zcd, W);
     note_launch();
     return cudaGetLastError();
 }
@@ -985,14 +1047,17 @@ bool sep3d_supported(int kx, int ky, int kz, int nx, int ny, int nz, int nvol)
            sep3d_smem_floats(kx, ky, kz) * sizeof(float) <= 200 * 1024;
 }
 
-cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s)
+cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s, int zdepth)
 {
     if ((long long)a.nx * a.ny * a.nz == 0 || a.nvol == 0) return cudaSuccess;
+    // chunk depths from 4 to 256 slices whose chunk count fits the grid, else the default
+    int zcd = k3ZC;
+    if (zdepth >= 4 && zdepth <= 256 && (long long)((a.nz + zdepth - 1) / zdepth) * a.nvol <= 65535) zcd = zdepth;
     const int it = a.in_type, ot = a.out_type;
-    if (it == IFX_F32 && ot == IFX_F32) return sep3d_t<float, float>(a, s);
-    if (it == IFX_F32 && ot == IFX_F64) return sep3d_t<float, double>(a, s);
-    if (is8(it) && ot == IFX_F32) return sep3d_t<uint8_t, float>(a, s);
-    if (is8(it) && ot == IFX_F64) return sep3d_t<uint8_t, double>(a, s);
+    if (it == IFX_F32 && ot == IFX_F32) return sep3d_t<float, float>(a, s, zcd);
+    if (it == IFX_F32 && ot == IFX_F64) return sep3d_t<float, double>(a, s, zcd);
+    if (is8(it) && ot == IFX_F32) return sep3d_t<uint8_t, float>(a, s, zcd);
+    if (is8(it) && ot == IFX_F64) return sep3d_t<uint8_t, double>(a, s, zcd);
     return cudaErrorInvalidValue;
 }
 
@@ -1128,12 +1193,15 @@ bool sep3d_split_applies(const Sep3dArgs &a)
     return sep2d_tma_applies(b);
 }
 
-cudaError_t launch_sep3d_split(const Sep3dArgs &a, float *tmp, cudaStream_t s)
+cudaError_t launch_sep3d_split(const Sep3dArgs &a, float *tmp, cudaStream_t s, int tw, int th)
 {
     if ((long long)a.nx * a.ny * a.nz == 0 || a.nvol == 0) return cudaSuccess;
     cudaError_t e = is8(a.in_type) ? zpass_t<uint8_t>(a, tmp, s) : zpass_t<float>(a, tmp, s);
     if (e != cudaSuccess) return e;
-    return launch_sep2d(sep3d_xy_args(a, tmp), s);
+    Sep2dArgs b = sep3d_xy_args(a, tmp);
+    b.tile_w = tw;
+    b.tile_h = th;
+    return launch_sep2d(b, s);
 }
 
 // =========================================================================

@@ -62,14 +62,15 @@ struct Sep2dArgs {
     int variant;                           // 0: automatic, 1: TMA tile kernel where it applies, 2: gather kernel
     int nsl;                               // planes of nx x ny stacked at img/out, filtered each on its own
                                            // (0 or 1: one; more: TMA tile kernel only)
+    int tile_w, tile_h;                    // output tile (0: the kernel's default); shapes a kernel
+                                           // cannot take fall back to its default
 };
 cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s);
 bool sep2d_tma_applies(const Sep2dArgs &a);
 size_t sep2d_smem_bytes(int kx, int ky, int x_first, int f64);
-// the autotuner of the fused 2-D separable path (ifx_tune.cu)
-cudaError_t launch_sep2d_tuned(Sep2dArgs a, cudaStream_t s, bool device_arrays);
-void autotune_set(bool enable, const char *path);
-bool autotune_lookup(const Sep2dArgs &a, int *x_first, int *variant, float *ms);
+// the tile shape each kernel of the fused 2-D path would run for `a`
+// (variant 1: TMA tile kernel, 2: gather kernel); false when it cannot run it
+bool sep2d_tile_shape(const Sep2dArgs &a, int variant, int *tw, int *th);
 
 // Fused 3-D separable kernel (factors on axes 0, 1, 2 in that order; FP32) ---
 struct Sep3dArgs {
@@ -81,11 +82,40 @@ struct Sep3dArgs {
     int style; double fill;
 };
 bool sep3d_supported(int kx, int ky, int kz, int nx, int ny, int nz, int nvol);
-cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s);
+// zdepth: output slices per z chunk of the fused kernel (0: default; the z
+// halo of kz - 1 input slices is filtered once per chunk)
+cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s, int zdepth = 0);
 // the split 3-D path (z sweep into an FP32 volume of nx*ny*nz*nvol floats at
-// tmp, then the x/y TMA sweep over its planes); applies needs no device memory
+// tmp, then the x/y TMA sweep over its planes, in tiles of tw x th when
+// given); applies needs no device memory
 bool sep3d_split_applies(const Sep3dArgs &a);
-cudaError_t launch_sep3d_split(const Sep3dArgs &a, float *tmp, cudaStream_t s);
+cudaError_t launch_sep3d_split(const Sep3dArgs &a, float *tmp, cudaStream_t s, int tw = 0, int th = 0);
+
+// The autotuner (ifx_tune.cu) -------------------------------------------------
+// A tuned choice: variant (2-D: 1 TMA tile kernel, 2 gather kernel; 3-D: 1
+// split sweeps, 2 fused z-marching kernel), pass order, output tile shape,
+// z chunk depth, and the time it was tuned at.
+struct TuneChoice {
+    int variant, x_first, tile_w, tile_h, depth;
+    float ms;
+};
+enum { TUNE_SEP2D = 0, TUNE_SEP3D = 1 };
+void autotune_set(bool enable, const char *path);
+bool autotune_enabled();
+bool autotune_lookup(const Sep2dArgs &a, TuneChoice *c);
+bool autotune_lookup3(const Sep3dArgs &a, TuneChoice *c);
+// key fields as the public API gives them (path, eltypes, taps, Fill, extents)
+bool autotune_lookup_key(int path, int in_type, int out_type, int kx, int ky, int kz, int fill, long long nx,
+                         long long ny, long long nz, TuneChoice *c);
+void autotune_pin_key(int path, int in_type, int out_type, int kx, int ky, int kz, int fill, long long nx,
+                      long long ny, long long nz, const TuneChoice &c);
+void autotune_clear();
+// the fused 2-D separable filter of `a`, tuned (device_arrays: tuning allowed)
+cudaError_t launch_sep2d_tuned(Sep2dArgs a, cudaStream_t s, bool device_arrays);
+// the 3-D separable filter of `a`: the cached choice, or (tuner enabled,
+// device arrays) every candidate timed; tmp: the split path's FP32 volume
+// (nullptr when the split path does not apply)
+cudaError_t launch_sep3d_tuned(const Sep3dArgs &a, float *tmp, cudaStream_t s, bool device_arrays);
 
 // Fused 3-D gradients (3-tap derivative / smoothing pair, all axes extended):
 // the three imgradients outputs from one sweep -----------------------------

@@ -774,10 +774,13 @@ def _imfilter_fft(ctx, out, ao, img, ai, ks, b, nd):
 
 
 def autotune(enable=True, cache=None):
-    """Enable (or disable) the autotuner of the fused 2-D separable path: the
-    first device-array call per (eltypes, taps, Fill/Pad, size class) times the
-    tile kernels and pass orders and keeps the fastest; `cache` is a text file
-    the choices persist in (loaded now, appended as keys are tuned)."""
+    """Enable (or disable) the autotuner of the separable paths: the first
+    device-array call per (eltypes, taps, Fill/Pad, size class) times the
+    candidates -- for 2-D filters the tile kernel, pass order and output tile
+    width and height; for 3-D filters the split sweeps (with their x/y tile)
+    or the fused z-marching kernel (with its z chunk depth) -- and keeps the
+    fastest; `cache` is a text file the choices persist in (loaded now,
+    appended as keys are tuned)."""
     ctx = _ctx()
     _abi.check(ctx.lib.ifx_autotune(ctx.handle, int(bool(enable)),
                                     None if cache is None else str(cache).encode()))
@@ -797,6 +800,53 @@ def autotune_choice(in_kind, out_kind, kx, ky, fill, shape):
     if rc:
         return None
     return xf.value, var.value, ms.value
+
+
+_TUNE_FIELDS = ("variant", "x_first", "tile_w", "tile_h", "depth", "ms")
+
+
+def _tune_key(in_kind, out_kind, taps, shape):
+    taps = tuple(int(t) for t in taps) + (1,) * (3 - len(taps))
+    shape = tuple(int(n) for n in shape) + (1,) * (3 - len(shape))
+    path = _abi.TUNE_SEP3D if len(shape) == 3 and shape[2] > 1 and taps[2] > 0 else _abi.TUNE_SEP2D
+    return path, (C.c_int32 * 3)(*taps), (C.c_int64 * 3)(*shape)
+
+
+def autotune_lookup(in_kind, out_kind, taps, fill, shape, path=None):
+    """The cached choice for a key as a dict (variant, x_first, tile_w,
+    tile_h, depth, ms), or None.  `taps` and `shape` are per axis (2 for the
+    2-D path, 3 for the 3-D path); `path` defaults to 3-D for 3-D shapes."""
+    ctx = _ctx()
+    p, t, n = _tune_key(in_kind, out_kind, taps, shape)
+    if path is not None:
+        p = path
+    ch = _abi.IfxTuneChoice()
+    rc = ctx.lib.ifx_autotune_lookup(ctx.handle, p, _KIND_CODE[in_kind], _KIND_CODE[out_kind], t,
+                                     int(bool(fill)), n, C.byref(ch))
+    if rc:
+        return None
+    return {f: getattr(ch, f) for f in _TUNE_FIELDS}
+
+
+def autotune_pin(in_kind, out_kind, taps, fill, shape, path=None, **choice):
+    """Pin the choice for a key (fields as autotune_lookup returns them; the
+    ones not given are 0 / the defaults): the next calls with the key run it."""
+    ctx = _ctx()
+    p, t, n = _tune_key(in_kind, out_kind, taps, shape)
+    if path is not None:
+        p = path
+    unknown = set(choice) - set(_TUNE_FIELDS)
+    if unknown:
+        raise ArgumentError(f"unknown tuner fields {sorted(unknown)}")
+    ch = _abi.IfxTuneChoice(**{"variant": 1, "x_first": 1, **choice})
+    _abi.check(ctx.lib.ifx_autotune_pin(ctx.handle, p, _KIND_CODE[in_kind], _KIND_CODE[out_kind], t,
+                                        int(bool(fill)), n, C.byref(ch)))
+
+
+def autotune_clear():
+    """Forget every cached and pinned choice (the cache file stays)."""
+    ctx = _ctx()
+    _abi.check(ctx.lib.ifx_autotune_clear(ctx.handle))
 
 
 def imgradients(img, kernelfun=None, border="replicate"):
@@ -854,5 +904,5 @@ def imgradients(img, kernelfun=None, border="replicate"):
 
 
 __all__ = ["Algorithm", "imfilter", "imfilter_", "imgradients", "filter_type", "factorkernel", "autotune",
-           "autotune_choice",
+           "autotune_choice", "autotune_lookup", "autotune_pin", "autotune_clear",
            "Kernel", "KernelFactors"]

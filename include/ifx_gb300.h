@@ -194,23 +194,53 @@ int ifx_mapwindow_extrema(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
                           const ifx_border_t *border, int32_t which, void *stream);
 
 /* ---- autotuner --------------------------------------------------------------
- * The fused 2-D separable path (ifx_imfilter_factored with at most one factor
- * per axis of a 1-D or 2-D image) chooses between two tile kernels (TMA-fed or
- * gather-based) and the order of its two passes.  With the tuner enabled, the
- * first device-array call per key (input and output eltypes, x and y taps,
- * Fill or Pad, floor(log2(pixels)), FP64 arithmetic) times every applicable
- * candidate on its stream and keeps the fastest; choices are cached in memory
- * and, when cache_path is given, in that text file (loaded here, appended as
- * keys are tuned).  Cached choices apply whether or not the tuner is enabled.
- * The tuner and its cache are process-wide.  (No reference counterpart: the
- * reference sizes its FIRTiled tiles by a fixed rule, TiledIteration's
- * padded_tilesize, src/imfilter.jl:1200-1206, 1273-1278.) */
+ * Two paths of ifx_imfilter_factored are tuned.
+ *  IFX_TUNE_SEP2D, the fused 2-D separable path (at most one factor per axis
+ *  of a 1-D or 2-D image): the tile kernel (variant 1: TMA-fed, 2: gather),
+ *  the pass order (x_first), and the output tile's width and height (tile_w x
+ *  tile_h outputs; the staged window adds the kx - 1 / ky - 1 halo, so the
+ *  shape sets the halo's share of every copy and pass).  TMA tiles: 64 or 128
+ *  wide, 8-128 rows; gather tiles: 32, 64 or 128 wide, 8-128 rows.
+ *  IFX_TUNE_SEP3D, one factor per axis of a volume: variant 1 the split
+ *  sweeps (z factor into an FP32 volume, then the x/y TMA sweep with its
+ *  tile shape), variant 2 the fused z-marching kernel, whose `depth` output
+ *  slices per chunk amortise the kz - 1 halo slices each chunk re-filters.
+ * With the tuner enabled, the first device-array call per key (path, input
+ * and output eltypes, taps, Fill or Pad, floor(log2(elements)), FP64
+ * arithmetic) times every applicable candidate on its stream and keeps the
+ * fastest; choices are cached in memory and, when cache_path is given, in
+ * that text file (loaded here, appended as keys are tuned).  Cached choices
+ * apply whether or not the tuner is enabled; a cached shape a kernel cannot
+ * take runs as the kernel's default.  The tuner and its cache are
+ * process-wide.  (No reference counterpart: the reference sizes its FIRTiled
+ * tiles by a fixed rule, TiledIteration's padded_tilesize,
+ * src/imfilter.jl:1200-1206, 1273-1278.) */
+#define IFX_TUNE_SEP2D 0
+#define IFX_TUNE_SEP3D 1
+typedef struct ifx_tune_choice {
+    int32_t variant;               /* see above                                          */
+    int32_t x_first;               /* 2-D: 1 the x pass first                            */
+    int32_t tile_w, tile_h;        /* output tile (0: the kernel's default)             */
+    int32_t depth;                 /* 3-D fused: output slices per chunk (0: default)    */
+    double ms;                     /* time per call when tuned (pinned: as given)        */
+} ifx_tune_choice_t;
 int ifx_autotune(ifx_context_t *ctx, int32_t enable, const char *cache_path);
-/* The cached choice for a key: x_first (1: the x pass first), variant (1: TMA
- * tile kernel, 2: gather kernel) and its time in ms; IFX_ERR_ARGUMENT when the
- * key has not been tuned. */
+/* The cached 2-D choice for a key: x_first (1: the x pass first), variant (1:
+ * TMA tile kernel, 2: gather kernel) and its time in ms; IFX_ERR_ARGUMENT when
+ * the key has not been tuned. */
 int ifx_autotune_choice(ifx_context_t *ctx, int32_t in_type, int32_t out_type, int32_t kx, int32_t ky,
                         int32_t fill, int64_t nx, int64_t ny, int32_t *x_first, int32_t *variant, double *ms);
+/* The cached choice of either path: taps[3] = x, y, z taps (1 for absent
+ * axes), size[3] = the array's extents (1 for absent axes); IFX_ERR_ARGUMENT
+ * when the key has not been tuned. */
+int ifx_autotune_lookup(ifx_context_t *ctx, int32_t path, int32_t in_type, int32_t out_type, const int32_t *taps,
+                        int32_t fill, const int64_t *size, ifx_tune_choice_t *choice);
+/* Sets the choice for a key (replacing a cached one; not written to the cache
+ * file): the next calls with that key run it. */
+int ifx_autotune_pin(ifx_context_t *ctx, int32_t path, int32_t in_type, int32_t out_type, const int32_t *taps,
+                     int32_t fill, const int64_t *size, const ifx_tune_choice_t *choice);
+/* Forgets every cached and pinned choice (the cache file is left as it is). */
+int ifx_autotune_clear(ifx_context_t *ctx);
 
 /* ---- Algorithm.IIR(): Triggs-Sdika recursive filters ---------------------------
  * One factor per pass, a KernelFactors.TriggsSdika (src/kernelfactors.jl:

@@ -221,10 +221,15 @@ def test_server_admission_by_free_device_memory(gpu_ifx):
             items.append((img, ("gaussian", 1.0 + (i % 3)), ifx.Pad("reflect")))
         with Server(hbm_cap_bytes=100 << 30, max_batch=2, max_inflight=2) as srv:
             outs, tickets = [], []
+            # paused: admission goes on but no batch launches, so the admitted
+            # requests hold their memory until every request is queued (else
+            # a fast device finishes each one before the next arrives)
+            srv.pause(True)
             for img, op, border in items:
                 o = host_outputs(ifx, img, op)
                 outs.append(o)
                 tickets.append(srv.submit(op, img, o, border))
+            srv.pause(False)
             for t in tickets:
                 srv.wait(t, timeout=120)
             m = srv.metrics()

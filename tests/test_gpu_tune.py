@@ -1,6 +1,9 @@
-"""The autotuner of the fused 2-D separable path: it times the candidates on
-the first device-array call per key, keeps the fastest, caches the choice in
-a file, and the tuned call stays within the FP32 tolerance of the oracle."""
+"""The autotuner of the separable paths: it times the candidates on the
+first device-array call per key, keeps the fastest, caches the choice in a
+file, and the tuned call stays within the FP32 tolerance of the oracle; every
+value of every tuned parameter, pinned, stays within it too."""
+import zlib
+
 import numpy as np
 import pytest
 
@@ -23,6 +26,7 @@ def test_autotune_separable(gpu_ifx, oracle, tmp_path):
     facs = [(f.axis, f.data.first[0], np.asarray(f.data.data, np.float64)) for f in k]
     kx, ky = (len(f.data) for f in k)
     try:
+        ifx.autotune_clear()
         ifx.autotune(True, cache)
         for style, border, okind in [("replicate", "replicate", "F32"), ("fill", ifx.Fill(0.25), "F64")]:
             assert ifx.autotune_choice("F32", okind, kx, ky, style == "fill", host.shape) is None
@@ -36,7 +40,7 @@ def test_autotune_separable(gpu_ifx, oracle, tmp_path):
             ifx.imfilter_(out, img, k, border)               # cached: same candidate, same bits
             assert np.array_equal(out.numpy(), first)
         lines = cache.read_text().strip().splitlines()
-        assert len(lines) == 2 and all(len(line.split()) == 10 for line in lines)
+        assert len(lines) == 2 and all(line.split()[0] == "t2" and len(line.split()) == 16 for line in lines)
         # host arrays are not tuned
         h = np.asfortranarray(rng.random((300, 200), dtype=np.float32))
         ifx.imfilter(h, ifx.KernelFactors.gaussian((1.0, 1.0)), "reflect")
@@ -46,3 +50,142 @@ def test_autotune_separable(gpu_ifx, oracle, tmp_path):
         assert ifx.autotune_choice("F32", "F32", kx, ky, False, host.shape) is not None
     finally:
         ifx.autotune(False, None)
+        ifx.autotune_clear()
+
+
+# ---------------------------------------------------------------- every tuned parameter
+STYLES = ["replicate", "circular", "symmetric", "reflect", "fill"]
+
+
+def _img(rng, shape, kind):
+    if kind == "F32":
+        return np.asfortranarray(rng.random(shape, dtype=np.float32))
+    if kind == "F64":
+        return np.asfortranarray(rng.random(shape))
+    return np.asfortranarray(rng.integers(0, 256, shape, dtype=np.uint8))
+
+
+def _values(img, kind):
+    return img.astype(np.float64) / 255.0 if kind == "N0F8" else img.astype(np.float64)
+
+
+# (variant, tile widths, tile heights) per compute type: the TMA kernel takes
+# 64 / 128 wide tiles, the gather kernel 64 / 128 (FP32) or 32 / 64 (FP64)
+TILES_2D = {"tma": (1, (64, 128), (8, 16, 24, 48, 96, 128)),
+            "gather32": (2, (64, 128), (8, 16, 40, 64, 128)),
+            "gather64": (2, (32, 64), (8, 24, 32, 64))}
+
+
+@pytest.mark.parametrize("kind", ["F32", "N0F8", "F64"])
+@pytest.mark.parametrize("style", STYLES)
+def test_pinned_2d_choices(gpu_ifx, oracle, kind, style):
+    """Every value of every tuned 2-D parameter -- kernel, pass order, tile
+    width, tile height -- pinned in turn, on images with partial edge tiles:
+    each result within the tolerance of the oracle, and the tile shape does
+    not change a single output's arithmetic (the same bits for every shape of
+    one kernel and pass order)."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("pin2d" + kind + style).encode()))
+    shape = (336, 203)                         # rows meet the 16-byte rule: the TMA kernel applies
+    img = _img(rng, shape, kind)
+    src = ifx.n0f8(img) if kind == "N0F8" else img
+    kx, ky = 13, 21
+    wx, wy = rng.standard_normal(kx), rng.standard_normal(ky)
+    facs = [(0, -6, wx), (1, -11, wy)]
+    ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(w, (f,)), 2, ax) for ax, f, w in facs)
+    border = ifx.Fill(0.7) if style == "fill" else ifx.Pad(style)
+    fv = {"F32": float(np.float32(0.7)), "F64": 0.7, "N0F8": round(0.7 * 255) / 255.0}[kind]
+    ref = oracle.imfilter_cascade(_values(img, kind), facs, style, fv)
+    tol = 1e-12 if kind == "F64" else 1e-5
+    groups = ["gather64"] if kind == "F64" else ["tma", "gather32"]
+    try:
+        for g in groups:
+            variant, widths, heights = TILES_2D[g]
+            for x_first in (1, 0):
+                first = None
+                for tw in widths:
+                    for th in heights:
+                        ifx.autotune_pin(kind, "F64", (kx, ky), style == "fill", shape, variant=variant,
+                                         x_first=x_first, tile_w=tw, tile_h=th)
+                        got = ifx.imfilter(src, ks, border)
+                        assert got.dtype == np.float64
+                        assert normwise(got, ref) <= tol, (g, x_first, tw, th)
+                        if first is None:
+                            first = got
+                        else:
+                            assert np.array_equal(got, first), (g, x_first, tw, th)
+    finally:
+        ifx.autotune_clear()
+
+
+@pytest.mark.parametrize("kind", ["F32", "N0F8"])
+@pytest.mark.parametrize("style", ["symmetric", "fill", "circular"])
+def test_pinned_3d_choices(gpu_ifx, oracle, kind, style):
+    """3-D: the split sweeps with every x/y tile shape, and the fused
+    z-marching kernel with every z chunk depth (chunks shorter than, equal
+    to and longer than the z factor's halo), pinned in turn."""
+    ifx = gpu_ifx
+    rng = np.random.default_rng(zlib.crc32(("pin3d" + kind + style).encode()))
+    shape = (68, 45, 37)
+    img = _img(rng, shape, kind)
+    src = ifx.n0f8(img) if kind == "N0F8" else img
+    taps = (9, 7, 11)
+    facs = [(ax, -(taps[ax] // 2), rng.standard_normal(taps[ax])) for ax in range(3)]
+    ks = tuple(ifx.ReshapedOneD(ifx.OffsetKernel(w, (f,)), 3, ax) for ax, f, w in facs)
+    border = ifx.Fill(0.7) if style == "fill" else ifx.Pad(style)
+    fv = {"F32": float(np.float32(0.7)), "N0F8": round(0.7 * 255) / 255.0}[kind]
+    ref = oracle.imfilter_cascade(_values(img, kind), facs, style, fv)
+    try:
+        split = [dict(variant=1, tile_w=tw, tile_h=th) for tw, th in [(0, 0), (64, 16), (64, 64), (128, 32),
+                                                                      (128, 96)]]
+        fused = [dict(variant=2, depth=d) for d in (4, 5, 8, 16, 37, 64)]
+        for ch in split + fused:
+            ifx.autotune_pin(kind, "F64", taps, style == "fill", shape, **ch)
+            got = ifx.imfilter(src, ks, border)
+            assert normwise(got, ref) <= 1e-5, ch
+    finally:
+        ifx.autotune_clear()
+
+
+def test_autotune_widened(gpu_ifx, oracle, tmp_path):
+    """The tuner picks a tile shape for the 2-D path and a z strategy (with a
+    tile shape or a chunk depth) for the 3-D path, stores them in the cache
+    file, and a fresh load restores them."""
+    ifx = gpu_ifx
+    cache = tmp_path / "tune2.txt"
+    rng = np.random.default_rng(404)
+    try:
+        ifx.autotune_clear()
+        ifx.autotune(True, cache)
+        h2 = np.asfortranarray(rng.random((1024, 600), dtype=np.float32))
+        k2 = ifx.KernelFactors.gaussian((2.0, 3.0))
+        taps2 = tuple(len(f.data) for f in k2)
+        out2 = ifx.DeviceArray.empty(h2.shape, "F64")
+        ifx.imfilter_(out2, ifx.DeviceArray.from_host(h2), k2, "reflect")
+        c2 = ifx.autotune_lookup("F32", "F64", taps2, False, h2.shape)
+        assert c2 is not None and c2["variant"] in (1, 2) and c2["tile_w"] in (64, 128) and c2["tile_h"] >= 8
+        facs2 = [(f.axis, f.data.first[0], np.asarray(f.data.data, np.float64)) for f in k2]
+        assert normwise(out2.numpy(), oracle.imfilter_cascade(h2.astype(np.float64), facs2, "reflect")) <= 1e-5
+
+        h3 = np.asfortranarray(rng.random((96, 80, 64), dtype=np.float32))
+        k3 = ifx.KernelFactors.gaussian((1.5, 1.5, 1.0))
+        taps3 = tuple(len(f.data) for f in k3)
+        out3 = ifx.DeviceArray.empty(h3.shape, "F64")
+        ifx.imfilter_(out3, ifx.DeviceArray.from_host(h3), k3, "symmetric")
+        c3 = ifx.autotune_lookup("F32", "F64", taps3, False, h3.shape)
+        assert c3 is not None and c3["variant"] in (1, 2)
+        assert (c3["variant"] == 2 and c3["depth"] >= 4) or c3["variant"] == 1
+        facs3 = [(f.axis, f.data.first[0], np.asarray(f.data.data, np.float64)) for f in k3]
+        assert normwise(out3.numpy(), oracle.imfilter_cascade(h3.astype(np.float64), facs3, "symmetric")) <= 1e-5
+
+        lines = [ln.split() for ln in cache.read_text().strip().splitlines()]
+        assert len(lines) == 2 and all(ln[0] == "t2" and len(ln) == 16 for ln in lines)
+        ifx.autotune_clear()
+        assert ifx.autotune_lookup("F32", "F64", taps2, False, h2.shape) is None
+        ifx.autotune(True, cache)
+        for taps, shape, c in ((taps2, h2.shape, c2), (taps3, h3.shape, c3)):
+            got = ifx.autotune_lookup("F32", "F64", taps, False, shape)
+            assert got is not None and abs(got.pop("ms") - c.pop("ms")) < 1e-5 and got == c   # ms: 6 decimals
+    finally:
+        ifx.autotune(False, None)
+        ifx.autotune_clear()
