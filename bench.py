@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--e2e-requests", type=int, default=1000)
     p.add_argument("--hbm-cap-gb", type=int, default=150)
     p.add_argument("--no-dense", action="store_true")
+    p.add_argument("--no-tune", dest="tune", action="store_false",
+                   help="no autotuning in the warm-up waves (default tiles everywhere)")
     p.add_argument("--dense-ksizes", type=lambda t: [int(v) for v in t.split(",")], default=None,
                    help="dense section: kernel sizes to run (default 5,11,15,31)")
     p.add_argument("--only", default=None, choices=[None, "dense", "sections", "next"],
@@ -269,9 +271,18 @@ def run_stream(args, ifx, torch, rank):
         ins = make_inputs(w)
         calls, keep, _ = stream_calls(ifx, w, ins, out_arena, torch)
         bt, arr = batch_for_wave(ifx, w, ins, out_arena)
-        prepared.append((w, ins, calls, keep, bt, arr, B.Plan(bt)))
+        prepared.append([w, ins, calls, keep, bt, arr, None])
     torch.cuda.synchronize()
     warm_p, timed_p = prepared[:args.warmup], prepared[args.warmup:]
+    # The autotuner runs during the warm-up waves only: their plans' first
+    # launches time the batched engine's tile candidates per key, their plain
+    # calls the 2-D path's.  The timed waves' plans are described after that,
+    # with the cached tiles (keys no warm-up wave held keep the defaults); the
+    # tuner is off in the timed region.
+    if args.tune:
+        ifx.autotune(True)
+    for p in warm_p:
+        p[6] = B.Plan(p[4])
     stream = ifx.arrays.torch_stream()
     tiles = C.c_int64()
 
@@ -322,9 +333,24 @@ def run_stream(args, ifx, torch, rank):
     for w, ins, calls, keep, bt, arr, plan in warm_p:
         for op, fn, a in calls:
             A.check(fn(*a))
-        A.check(ctx.lib.ifx_batch_run(ctx.handle, arr, len(w), C.byref(tiles), stream))
         A.check(ctx.lib.ifx_batch_plan_launch(plan.handle, C.byref(tiles), stream))
+        A.check(ctx.lib.ifx_batch_run(ctx.handle, arr, len(w), C.byref(tiles), stream))
     torch.cuda.synchronize()
+    ifx.autotune(False)                  # cached choices still apply
+    for p in timed_p:
+        p[6] = B.Plan(p[4])
+    tuned_tiles = {}
+    for r in timed:
+        okind = r.out_kinds()[0]
+        if r.op == "gaussian":
+            key, c = "factored/%s/%d" % (r.kind, r.taps()), B.autotune_lookup("factored", r.kind, okind, r.taps(),
+                                                                            r.taps())
+        elif r.op in ("sobel", "laplacian"):
+            name = "gradients" if r.op == "sobel" else "laplacian"
+            key, c = "%s/%s" % (name, r.kind), B.autotune_lookup(name, r.kind, okind, 3, 3)
+        else:
+            continue
+        tuned_tiles[key] = None if c is None else [c["tile_w"], c["tile_h"]]
     plain_ms, _, plain_ev, _ = timed_region("plain", True)
     run_ms, _, _, _ = timed_region("batch_run", False)
     batch_ms, launches, batch_ev, clocks = timed_region("batched", False)
@@ -359,7 +385,8 @@ def run_stream(args, ifx, torch, rank):
             "per_op_batched": per_op_batched,
             "launches": launches,
             "host_ms_per_step": {k: v * 1e3 / max(len(timed_p), 1) for k, v in host_s.items()},
-            "per_op": per_op, "batch_kernel": bk, "clocks": clocks, "reqs": timed}
+            "per_op": per_op, "batch_kernel": bk, "clocks": clocks, "reqs": timed,
+            "tuned_batch_tiles": tuned_tiles}
 
 
 def run_stream_e2e(args, ifx, torch, reqs_all):
@@ -636,7 +663,12 @@ def run_sections(args, ifx, torch, hbm_peak):
             "max_abs_err": es["max_abs"], "max_rel_err": es["max_rel"],
             "note": "1 MiB image: latency-bound (one launch), judged on its error, not its roofline"}
     n = 4096
-    ifx.autotune(True)            # the separable cases below are tuned on their first (warm-up) call
+
+    def tuned_desc(c):
+        if c is None:
+            return None
+        return {"kernel": "tma" if c["variant"] == 1 else "gather", "x_first": c["x_first"],
+                "tile": [c["tile_w"], c["tile_h"]]}
     imgs = {"F32": ifx.DeviceArray(torch.rand((n, n), device="cuda", generator=g).t(), "F32"),
             "N0F8": ifx.DeviceArray(torch.randint(0, 256, (n, n), device="cuda", generator=g,
                                                   dtype=torch.uint8).t(), "N0F8")}
@@ -648,10 +680,17 @@ def run_sections(args, ifx, torch, hbm_peak):
             for okind, osz in (("F64", 8), ("F32", 4)):
                 o = ifx.DeviceArray.empty((n, n), okind)
                 b = A.border_struct("replicate")
+                # the default choice (tuner off, nothing cached), then the tuned
+                # one (tuned on the first, warm-up, call)
+                ifx.autotune_clear()
+                ms_default = _time(torch, lambda: A.check(ctx.lib.ifx_imfilter_factored(
+                    ctx.handle, desc(o), desc(img), 2, arr, C.byref(b), stream)))
+                ifx.autotune(True)
                 ms = _time(torch, lambda: A.check(ctx.lib.ifx_imfilter_factored(
                     ctx.handle, desc(o), desc(img), 2, arr, C.byref(b), stream)))
+                ifx.autotune(False)
                 gbs = n * n * (isz + osz) / (ms / 1e3) / 1e9
-                ch = ifx.autotune_choice(ikind, okind, taps, taps, False, (n, n))
+                ch = ifx.autotune_lookup(ikind, okind, (taps, taps), False, (n, n))
                 # error on a 384^2 crop against the oracle run on the crop plus its halo
                 h, c0, cn = taps // 2, 1000, 384
                 host = img.numpy()[c0 - h:c0 + cn + h, c0 - h:c0 + cn + h].astype(np.float64)
@@ -662,11 +701,10 @@ def run_sections(args, ifx, torch, hbm_peak):
                 out["separable_4096_%s_%dtap_%s" % (ikind, taps, okind)] = {
                     "ms": round(ms, 4), "mpix_s": n * n / (ms / 1e3) / 1e6, "achieved_gbs": gbs,
                     "hbm_frac": gbs / hbm_peak, "normwise_err": es["normwise"], "max_abs_err": es["max_abs"],
-                    "max_rel_err": es["max_rel"],
-                    "tuned": None if ch is None else {"x_first": ch[0],
-                                                      "kernel": "tma" if ch[1] == 1 else "gather"}}
+                    "max_rel_err": es["max_rel"], "default_ms": round(ms_default, 4),
+                    "tuned": tuned_desc(ch)}
                 del o
-    ifx.autotune(False)
+    ifx.autotune_clear()
     del imgs, img
     # 256^3 x 8 volumes: Gaussian (3,3,1.5) -> Float64, then Sobel gradients of that
     nv = 256
@@ -698,9 +736,14 @@ def run_sections(args, ifx, torch, hbm_peak):
         for i in range(len(vols)):
             A.check(ctx.lib.ifx_imgradients(ctx.handle, gdesc, desc(gau[i % 2]), A.dptr(d), A.dptr(sm), 3, -1,
                                             ext, C.byref(b), stream))
+    ms_g_default = _time(torch, volume_gauss, reps=2)        # tuner off, nothing cached
+    ifx.autotune(True)                                       # tuned on the first (warm-up) call
     ms = _time(torch, volume_step, reps=2)
+    ifx.autotune(False)
     ms_g = _time(torch, volume_gauss, reps=2)
     ms_d = _time(torch, volume_grad, reps=2)
+    ch3 = ifx.autotune_lookup("F32", "F64", [len(f.data) for f in kf], False, (nv, nv, nv))
+    ifx.autotune_clear()
     vox = 8 * nv ** 3
     alg = vox * ((4 + 8) + (8 + 3 * 8))
     # errors on a 40^3 interior crop of the last volume: its Gaussian against the
@@ -725,6 +768,10 @@ def run_sections(args, ifx, torch, hbm_peak):
         "ms": round(ms, 3), "mvox_s": vox / (ms / 1e3) / 1e6, "achieved_gbs": alg / (ms / 1e3) / 1e9,
         "hbm_frac": alg / (ms / 1e3) / 1e9 / hbm_peak,
         "gaussian_ms": round(ms_g, 3), "gradients_ms": round(ms_d, 3),
+        "gaussian_default_ms": round(ms_g_default, 3),
+        "gaussian_tuned": None if ch3 is None else {
+            "method": "split" if ch3["variant"] == 1 else "fused", "tile": [ch3["tile_w"], ch3["tile_h"]],
+            "z_depth": ch3["depth"]},
         "note": "Gaussian sigma (3,3,1.5) on Float32 volumes (Float64 out, FP32 arithmetic), then "
                 "imgradients of the Float64 result (FP64 arithmetic, the three gradients in one sweep)"}
     del vols, gau, grads
@@ -1027,7 +1074,10 @@ def main():
                            "replayed from a validated plan (CUDA graph), device-resident inputs",
                    "l2": "inputs larger than L2 (each step ~%.1f GB)" %
                    (sum(alg_bytes(r) for r in res["reqs"]) / args.steps / 1e9),
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "autotune": "tile shapes tuned in the warm-up waves, tuner off in the timed region"
+                   if args.tune else "off (default tiles)"},
+        "tuned_batch_tiles": res["tuned_batch_tiles"],
         "plain_gpu": {"value": plain_value, "unit": "Mpixel/s",
                       "mode": "one C-ABI call per request (device-resident)",
                       "per_op_ms": {k: round(v[0], 3) for k, v in per_op.items()}},

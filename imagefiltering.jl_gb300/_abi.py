@@ -117,7 +117,8 @@ SYMBOLS = ["ifx_abi_version", "ifx_create", "ifx_destroy", "ifx_last_error", "if
            "ifx_imfilter_factored_sum", "ifx_findlocalextrema", "ifx_maxabs", "ifx_imfilter_fft",
            "ifx_imfilter_iir", "ifx_autotune", "ifx_autotune_choice", "ifx_server_cancel",
            "ifx_server_inject_launch_error", "ifx_server_pause", "ifx_debug_force_wait_timeout", "ifx_convert",
-           "ifx_autotune_lookup", "ifx_autotune_pin", "ifx_autotune_clear"]
+           "ifx_autotune_lookup", "ifx_autotune_pin", "ifx_autotune_clear", "ifx_batch_autotune_lookup",
+           "ifx_batch_autotune_pin"]
 
 _lib = None
 _lock = threading.Lock()
@@ -188,6 +189,8 @@ def load(path: str = LIB_PATH):
         lib.ifx_autotune_pin.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, P(C.c_int32), C.c_int32,
                                          P(C.c_int64), P(IfxTuneChoice)]
         lib.ifx_autotune_clear.argtypes = [vp]
+        lib.ifx_batch_autotune_lookup.argtypes = [vp] + [C.c_int32] * 6 + [P(IfxTuneChoice)]
+        lib.ifx_batch_autotune_pin.argtypes = [vp] + [C.c_int32] * 6 + [P(IfxTuneChoice)]
         lib.ifx_imfilter_iir.argtypes = [vp, P(IfxArray), P(IfxArray), C.c_int32, P(IfxIir), P(IfxBorder), vp]
         lib.ifx_imfilter_fft.argtypes = [vp, P(IfxArray), P(IfxArray), P(C.c_double), P(C.c_int64),
                                          P(C.c_int64), P(IfxBorder), vp]

@@ -135,3 +135,29 @@ def outputs_for(op, img):
     if op[0] == "median":
         kinds = [MEDIAN_OUT[kind_of(img)]]
     return [DeviceArray.empty(img.shape, k, img.tensor.device) for k in kinds]
+
+
+_KIND_CODE = {"F32": 0, "F64": 1, "N0F8": 2, "U8": 3}
+_OP_CODE = {"factored": 1, "gradients": 2, "laplacian": 3, "median": 4}
+
+
+def autotune_lookup(op, in_kind, out_kind, kx=0, ky=0, window=0):
+    """The batched engine's cached tile for a key, {"tile_w", "tile_h", "ms"},
+    or None.  op: "factored" (kx, ky = the factors' taps), "gradients",
+    "laplacian" or "median" (window 3 or 5)."""
+    ctx = _abi.context()
+    ch = _abi.IfxTuneChoice()
+    rc = ctx.lib.ifx_batch_autotune_lookup(ctx.handle, _OP_CODE[op], _KIND_CODE[in_kind], _KIND_CODE[out_kind],
+                                           int(kx), int(ky), int(window), C.byref(ch))
+    if rc:
+        return None
+    return {"tile_w": ch.tile_w, "tile_h": ch.tile_h, "ms": ch.ms}
+
+
+def autotune_pin(op, in_kind, out_kind, tile_w, tile_h, kx=0, ky=0, window=0):
+    """Pin the batched engine's tile for a key (batches described after this
+    use it; a tile the engine cannot take runs as the default)."""
+    ctx = _abi.context()
+    ch = _abi.IfxTuneChoice(0, 0, int(tile_w), int(tile_h), 0, 0.0)
+    _abi.check(ctx.lib.ifx_batch_autotune_pin(ctx.handle, _OP_CODE[op], _KIND_CODE[in_kind], _KIND_CODE[out_kind],
+                                              int(kx), int(ky), int(window), C.byref(ch)))

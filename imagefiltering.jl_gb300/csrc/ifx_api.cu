@@ -1358,6 +1358,48 @@ int ifx_autotune_pin(ifx_context_t *ctx, int32_t path, int32_t in_type, int32_t 
     return IFX_OK;
 }
 
+// The batched engine's key as its requests hold it: factored (taps x, taps y),
+// gradients (3, 3), Laplacian and median no taps, the window for medians only.
+static int batch_tune_key(int32_t op, int32_t in_type, int32_t out_type, int32_t *kx, int32_t *ky, int32_t *win)
+{
+    if (op < IFX_OP_FACTORED2D || op > IFX_OP_MEDIAN2D) return fail(IFX_ERR_ARGUMENT, "unknown op %d", op);
+    if (in_type != IFX_F32 && !is8(in_type)) return fail(IFX_ERR_ARGUMENT, "batched images are Float32 or 8-bit");
+    if (out_type != IFX_F32 && out_type != IFX_F64) return fail(IFX_ERR_ARGUMENT, "outputs are Float32 or Float64");
+    if (op == IFX_OP_GRADIENTS2D) *kx = *ky = 3;
+    else if (op != IFX_OP_FACTORED2D) *kx = *ky = 0;
+    if (op != IFX_OP_MEDIAN2D) *win = 0;
+    return IFX_OK;
+}
+
+int ifx_batch_autotune_lookup(ifx_context_t *ctx, int32_t op, int32_t in_type, int32_t out_type, int32_t kx,
+                              int32_t ky, int32_t window, ifx_tune_choice_t *choice)
+{
+    IFX_RANGE("ifx_batch_autotune_lookup");
+    (void)ctx;
+    int rc;
+    if ((rc = batch_tune_key(op, in_type, out_type, &kx, &ky, &window))) return rc;
+    if (!choice) return fail(IFX_ERR_ARGUMENT, "NULL output");
+    TuneChoice ch;
+    if (!autotune_lookup_batch(op, in_type, out_type, kx, ky, window, &ch))
+        return fail(IFX_ERR_ARGUMENT, "no tuned choice for this key");
+    *choice = ifx_tune_choice_t{ch.variant, ch.x_first, ch.tile_w, ch.tile_h, ch.depth, ch.ms};
+    return IFX_OK;
+}
+
+int ifx_batch_autotune_pin(ifx_context_t *ctx, int32_t op, int32_t in_type, int32_t out_type, int32_t kx,
+                           int32_t ky, int32_t window, const ifx_tune_choice_t *choice)
+{
+    IFX_RANGE("ifx_batch_autotune_pin");
+    (void)ctx;
+    int rc;
+    if ((rc = batch_tune_key(op, in_type, out_type, &kx, &ky, &window))) return rc;
+    if (!choice) return fail(IFX_ERR_ARGUMENT, "NULL choice");
+    if (choice->tile_w < 0 || choice->tile_h < 0) return fail(IFX_ERR_ARGUMENT, "negative tile");
+    autotune_store_batch(op, in_type, out_type, kx, ky, window,
+                         TuneChoice{0, 0, choice->tile_w, choice->tile_h, 0, (float)choice->ms}, false);
+    return IFX_OK;
+}
+
 int ifx_autotune_clear(ifx_context_t *ctx)
 {
     IFX_RANGE("ifx_autotune_clear");

@@ -36,6 +36,7 @@ constexpr int kBatchMaxTaps = 36;     // factor taps (<= 33) rounded up to 4
 struct BReq {
     int op, in_type, out_type, style;
     int nx, ny, tiles_x, win;
+    int tw, th;                       // output tile of this request (see bt_tile_ok)
     long long tile_base, tile_end;    // this request's tiles: [tile_base, tile_end)
     const void *in;
     void *out0;
@@ -43,8 +44,8 @@ struct BReq {
     float fill;                       // value domain (N0f8: c/255)
     int fill_code;                    // 8-bit images: the fill code
     int kx, ky, fx, fy;
-    float wx[kBatchMaxTaps];
-    float wy[kBatchMaxTaps];
+    float2 wx[kBatchMaxTaps];         // weights as (w, w) pairs: operands of the packed FP32x2 FMA
+    float2 wy[kBatchMaxTaps];
 };
 
 struct BHdr {
@@ -55,12 +56,13 @@ struct BHdr {
 
 enum { BOP_FACTORED = 1, BOP_GRADIENTS = 2, BOP_LAPLACIAN = 3, BOP_MEDIAN = 4 };
 
-// tile shapes (outputs per tile); each input window (tile + halo) fits one
-// staging buffer of 64 rows x 400 bytes
+// Default tile shapes (outputs per tile); each input window (tile + halo)
+// fits one staging buffer of 64 rows x 400 bytes
 constexpr int kFTX = 64, kFTY = 32;        // factored (halo up to 32 x 32)
 constexpr int kGTX = 88, kGTY = 56;        // gradients / laplacian (halo 2 x 2); (88 + 2) * 4 + 15 <= kStagePitch
 constexpr int kMUX = 256, kMUY = 56;       // 8-bit median
 constexpr int kMFX = 64, kMFY = 56;        // float median
+constexpr int kStageRowsMax = kFTY + 32, kStagePitchBytes = 400;
 
 __host__ __device__ inline int bt_tile_w(int op, int in_type)
 {
@@ -77,6 +79,26 @@ __host__ __device__ inline int bt_tile_h(int op, int in_type, int ky)
     if (op == BOP_FACTORED) return bt_fact_h(ky);
     if (op == BOP_MEDIAN) return (in_type == IFX_F32) ? kMFY : kMUY;
     return kGTY;
+}
+
+// Tile shapes the routines take besides the defaults: factored tiles a
+// multiple of 64 wide (the routine runs 64-column blocks through its
+// intermediate) and a multiple of 8 tall; gradient / Laplacian tiles a
+// multiple of 88 wide and 56 tall; median tiles the defaults only.  The
+// window (tile + halo, plus up to 15 bytes of row lead) must fit the staging
+// buffer.
+inline bool bt_tile_ok(int op, int in_type, int kx, int ky, int tw, int th)
+{
+    const int elt = in_type == IFX_F32 ? 4 : 1;
+    if (tw <= 0 || th <= 0) return false;
+    switch (op) {
+    case BOP_FACTORED:
+        return tw % kFTX == 0 && th % 8 == 0 && th + ky - 1 <= kStageRowsMax &&
+               (tw + kx - 1) * elt + 15 <= kStagePitchBytes;
+    case BOP_GRADIENTS:
+    case BOP_LAPLACIAN: return tw % kGTX == 0 && th == kGTY && (tw + 2) * elt + 15 <= kStagePitchBytes;
+    default: return tw == bt_tile_w(op, in_type) && th == bt_tile_h(op, in_type, ky);
+    }
 }
 
 // Thread roles of k_batch: warp 0 is the producer (it looks tiles up and
@@ -129,8 +151,8 @@ __shared__ float s_n0f8[256];
 // aligned superset; lead[r] is the row start's offset in it), issued one tile
 // ahead so the copies land while the previous tile computes.  Windows that
 // leave the image are gathered through the border map (lead 0).
-constexpr int kStageRows = kFTY + 32;                  // factored with 33 taps
-constexpr int kStagePitch = 400;                       // >= 15 + (64 + 32) * 4, multiple of 16
+constexpr int kStageRows = kStageRowsMax;              // factored with 33 taps
+constexpr int kStagePitch = kStagePitchBytes;          // >= 15 + (64 + 32) * 4, multiple of 16
 constexpr int kStageBytes = kStageRows * kStagePitch;
 constexpr int kIPitch = kFTX + 4;                      // factored intermediate (floats)
 static_assert((kGTX + 2) * 4 + 15 <= kStagePitch && kGTY + 2 <= kStageRows, "gradient tiles fit a stage");
@@ -143,9 +165,9 @@ __device__ __forceinline__ TileGeo bt_geo(const BReq &R, int tx0, int ty0)
 {
     const int elt = R.in_type == IFX_F32 ? 4 : 1;
     switch (R.op) {
-    case BOP_FACTORED: return {tx0 + R.fx, ty0 + R.fy, bt_fact_h(R.ky) + R.ky - 1, kFTX + R.kx - 1, elt};
+    case BOP_FACTORED: return {tx0 + R.fx, ty0 + R.fy, R.th + R.ky - 1, R.tw + R.kx - 1, elt};
     case BOP_GRADIENTS:
-    case BOP_LAPLACIAN: return {tx0 - 1, ty0 - 1, kGTY + 2, kGTX + 2, elt};
+    case BOP_LAPLACIAN: return {tx0 - 1, ty0 - 1, R.th + 2, R.tw + 2, elt};
     default: {
         const int h = R.win / 2;
         if (elt == 4) return {tx0 - h, ty0 - h, kMFY + R.win - 1, kMFX + R.win - 1, 4};
@@ -282,9 +304,10 @@ template <class Tout> struct OutTile {
 };
 
 // ---------------------------------------------------------------- factored
-// acc[i] = sum_{t<k} w[t] src(i+t), i < NB, the window read through `at`.
+// acc[i] = sum_{t<k} w[t] src(i+t), i < NB, the window read through `at`
+// (weights as (w, w) pairs; the first lane is used).
 template <int NB, class F>
-__device__ __forceinline__ void corr_fn(F at, const float *w, int k, float *acc)
+__device__ __forceinline__ void corr_fn(F at, const float2 *w, int k, float *acc)
 {
     float v[NB + kCorrKmax - 1];
 #pragma unroll
@@ -296,49 +319,103 @@ __device__ __forceinline__ void corr_fn(F at, const float *w, int k, float *acc)
     for (int t = 0; t < kCorrKmax; ++t) {
         if (t >= k) break;
         if (t > 0) v[NB - 1 + t] = at(NB - 1 + t);
-        const float wt = w[t];
+        const float wt = w[t].x;
 #pragma unroll
         for (int i = 0; i < NB; ++i) acc[i] = fmaf(wt, v[i + t], acc[i]);
     }
 }
 
+// The same for two sources at once on the
+// packed FP32x2 pipe: at(j) returns element j of both; each lane computes
+// the fmaf chain of the scalar form, in the same order (the same bits).
+template <int NB, class F>
+__device__ __forceinline__ void corr_fn2(F at, const float2 *w, int k, float2 *acc)
+{
+    float2 v[NB + kCorrKmax - 1];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        v[i] = at(i);
+        acc[i] = make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int t = 0; t < kCorrKmax; ++t) {
+        if (t >= k) break;
+        if (t > 0) v[NB - 1 + t] = at(NB - 1 + t);
+        const float2 wt = w[t];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) acc[i] = __ffma2_rn(wt, v[i + t], acc[i]);
+    }
+}
+
+// Factored tiles: the x pass over all rows of the window (the y halo) into
+// the intermediate I, then the y pass down each column of I.  8-bit images
+// run the x pass on row pairs on the packed FP32x2 pipe (each value is two
+// shared loads, code and table, either way); Float32 images run it one row
+// per item (row pairs read rows 8 words apart, which share banks in this
+// layout, and measured slower).  A window with an odd row count pairs its
+// last row with itself (the copy lands in intermediate row `rows`, which is
+// never read).  Every output is the fmaf chain of the reference's cascade
+// order in both forms.
 template <class Tin, class Tout>
 __device__ void bt_factored(const BReq &R, int tx0, int ty0, const Rows<Tin> &S, float *I)
 {
-    constexpr int TX = kFTX, NB = 8;
-    const int kx = R.kx, ky = R.ky, TY = bt_fact_h(ky), rows = TY + ky - 1;
+    constexpr int BW = kFTX, NB = 8;                 // 64-column blocks through the intermediate
+    const int kx = R.kx, ky = R.ky, TY = R.th, rows = TY + ky - 1;
     const int tid = ct_id(), nth = ct_n();
-    float acc[NB];
-    // x pass over all rows (the y halo) -> I
-    for (int it = tid; it < rows * (TX / NB); it += nth) {
-        const int r = it >> 3, c0 = (it & 7) * NB;
-        const auto *p = S.row(r) + c0;
-        corr_fn<NB>([&](int j) { return S.val(p, j); }, R.wx, kx, acc);
+    for (int cb = 0; cb < R.tw && tx0 + cb < R.nx; cb += BW) {
+        if (cb > 0) ct_sync();                       // the previous block's y pass has read I
+        if constexpr (sizeof(Tin) == 1) {
+            const int pairs = (rows + 1) >> 1;
+            float2 acc[NB];
+            for (int it = tid; it < pairs * (BW / NB); it += nth) {
+                const int r = 2 * (it >> 3), c0 = (it & 7) * NB;
+                const auto *p0 = S.row(r) + cb + c0, *p1 = S.row(r + 1 < rows ? r + 1 : r) + cb + c0;
+                corr_fn2<NB>([&](int j) { return make_float2(S.val(p0, j), S.val(p1, j)); }, R.wx, kx, acc);
+                float4 *d0 = reinterpret_cast<float4 *>(I + r * kIPitch + c0);
+                float4 *d1 = reinterpret_cast<float4 *>(I + (r + 1) * kIPitch + c0);
 #pragma unroll
-        for (int i = 0; i < NB; ++i) I[r * kIPitch + c0 + i] = acc[i];
-    }
-    ct_sync();
-    // y pass down each column
-    const OutTile<Tout> O(R, R.out0, tx0, ty0, TX, TY);
-    for (int it = tid; it < TX * (TY / NB); it += nth) {
-        const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
-        corr_col<NB>(I + r0 * kIPitch + c, kIPitch, R.wy, ky, acc);
-        O.template col<NB>(c, r0, acc);
+                for (int q = 0; q < NB / 4; ++q) {
+                    d0[q] = make_float4(acc[4 * q].x, acc[4 * q + 1].x, acc[4 * q + 2].x, acc[4 * q + 3].x);
+                    d1[q] = make_float4(acc[4 * q].y, acc[4 * q + 1].y, acc[4 * q + 2].y, acc[4 * q + 3].y);
+                }
+            }
+        } else {
+            float acc[NB];
+            for (int it = tid; it < rows * (BW / NB); it += nth) {
+                const int r = it >> 3, c0 = (it & 7) * NB;
+                const float *p = S.row(r) + cb + c0;
+                corr_fn<NB>([&](int j) { return p[j]; }, R.wx, kx, acc);
+#pragma unroll
+                for (int i = 0; i < NB; ++i) I[r * kIPitch + c0 + i] = acc[i];
+            }
+        }
+        ct_sync();
+        // y pass down each column
+        float acc[NB];
+        const OutTile<Tout> O(R, R.out0, tx0 + cb, ty0, BW, TY);
+        for (int it = tid; it < BW * (TY / NB); it += nth) {
+            const int rs = it / BW, c = it - rs * BW, r0 = rs * NB;
+            corr_fn<NB>([&](int j) { return I[(r0 + j) * kIPitch + c]; }, R.wy, ky, acc);
+            O.template col<NB>(c, r0, acc);
+        }
     }
 }
 
 // ---------------------------------------------------------------- gradients
 // out0 = smooth_y(deriv_x), out1 = deriv_y(smooth_x) over a halo-1 window.
+// Gradient and Laplacian tiles are R.tw wide: blocks of kGTX columns, items
+// numbered across the blocks.
 template <class Tin, class Tout>
 __device__ void bt_gradients(const BReq &R, int tx0, int ty0, const Rows<Tin> &S)
 {
-    constexpr int TX = kGTX, TY = kGTY, NB = 8;
+    constexpr int TX = kGTX, TY = kGTY, NB = 8, PER = TX * (TY / NB);
     const int tid = ct_id(), nth = ct_n();
-    const float d0 = R.wx[0], d1 = R.wx[1], d2 = R.wx[2];
-    const float s0 = R.wy[0], s1 = R.wy[1], s2 = R.wy[2];
-    const OutTile<Tout> O0(R, R.out0, tx0, ty0, TX, TY), O1(R, R.out1, tx0, ty0, TX, TY);
-    for (int it = tid; it < TX * (TY / NB); it += nth) {
-        const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
+    const float d0 = R.wx[0].x, d1 = R.wx[1].x, d2 = R.wx[2].x;
+    const float s0 = R.wy[0].x, s1 = R.wy[1].x, s2 = R.wy[2].x;
+    const OutTile<Tout> O0(R, R.out0, tx0, ty0, R.tw, TY), O1(R, R.out1, tx0, ty0, R.tw, TY);
+    for (int it = tid; it < (R.tw / TX) * PER; it += nth) {
+        const int cb = it / PER, rem = it - cb * PER;
+        const int rs = rem / TX, c = cb * TX + rem - rs * TX, r0 = rs * NB;
         float D[NB + 2], Sm[NB + 2];
 #pragma unroll
         for (int j = 0; j < NB + 2; ++j) {
@@ -363,11 +440,12 @@ __device__ void bt_gradients(const BReq &R, int tx0, int ty0, const Rows<Tin> &S
 template <class Tin, class Tout>
 __device__ void bt_laplacian(const BReq &R, int tx0, int ty0, const Rows<Tin> &S)
 {
-    constexpr int TX = kGTX, TY = kGTY, NB = 8;
+    constexpr int TX = kGTX, TY = kGTY, NB = 8, PER = TX * (TY / NB);
     const int tid = ct_id(), nth = ct_n();
-    const OutTile<Tout> O(R, R.out0, tx0, ty0, TX, TY);
-    for (int it = tid; it < TX * (TY / NB); it += nth) {
-        const int rs = it / TX, c = it - rs * TX, r0 = rs * NB;
+    const OutTile<Tout> O(R, R.out0, tx0, ty0, R.tw, TY);
+    for (int it = tid; it < (R.tw / TX) * PER; it += nth) {
+        const int cb = it / PER, rem = it - cb * PER;
+        const int rs = rem / TX, c = cb * TX + rem - rs * TX, r0 = rs * NB;
         float col[NB + 2], lft[NB], rgt[NB], res[NB];
 #pragma unroll
         for (int j = 0; j < NB + 2; ++j) {
@@ -661,7 +739,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
         const BReq &R = s_req[b];
         const int local = (int)(t - R.tile_base);
         const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
-        const TileGeo g = bt_geo(R, bx * bt_tile_w(R.op, R.in_type), by * bt_tile_h(R.op, R.in_type, R.ky));
+        const TileGeo g = bt_geo(R, bx * R.tw, by * R.th);
         const bool bulk = bt_bulk_ok(R, g);
         if (bulk) bt_issue_rows(R, g, smem + b * kStageBytes, s_lead[b], &s_bar[b]);
         if (lane == 0) s_bulk[b] = bulk;
@@ -693,7 +771,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
             const BReq &R = s_req[b];
             const int local = (int)(t - R.tile_base);
             const int by = local / R.tiles_x, bx = local - by * R.tiles_x;
-            const int tx0 = bx * bt_tile_w(R.op, R.in_type), ty0 = by * bt_tile_h(R.op, R.in_type, R.ky);
+            const int tx0 = bx * R.tw, ty0 = by * R.th;
             unsigned char *st = smem + b * kStageBytes;
             if (s_bulk[b]) {
                 ok = mbar_wait_bounded(&s_bar[b], (parity >> b) & 1u, first_tries);
@@ -823,6 +901,42 @@ int batch_grid(int device)
     return engine_for(device, &E) == cudaSuccess ? E->grid : 0;
 }
 
+// The tile of a request: `force` when given, else the cached (tuned or
+// pinned) choice of its key, when the routine takes it; else the default.
+static int bt_key_win(const BReq &R) { return R.op == BOP_MEDIAN ? R.win : 0; }
+
+static void bt_choose_tile(BReq &R, const TuneChoice *force)
+{
+    R.tw = bt_tile_w(R.op, R.in_type);
+    R.th = bt_tile_h(R.op, R.in_type, R.ky);
+    TuneChoice c;
+    if (force) c = *force;
+    else if (!autotune_lookup_batch(R.op, R.in_type, R.out_type, R.kx, R.ky, bt_key_win(R), &c)) return;
+    if (bt_tile_ok(R.op, R.in_type, R.kx, R.ky, c.tile_w, c.tile_h)) {
+        R.tw = c.tile_w;
+        R.th = c.tile_h;
+    }
+}
+
+// The tile shapes the tuner tries for a request's key: factored tiles 64,
+// 128 or 256 wide (8-bit images: the staging rows hold them) at the tallest
+// height and half of it; gradient / Laplacian tiles 88, 176 or 352 wide;
+// median tiles are not tuned (their block networks fix the shape).
+static std::vector<TuneChoice> bt_candidates(const BReq &R)
+{
+    std::vector<TuneChoice> out;
+    if (R.op == BOP_FACTORED) {
+        const int h0 = bt_fact_h(R.ky), hs[2] = {h0, (h0 / 2) & ~7};
+        for (int w = kFTX; w <= 4 * kFTX; w *= 2)
+            for (int h : hs)
+                if (bt_tile_ok(R.op, R.in_type, R.kx, R.ky, w, h)) out.push_back(TuneChoice{0, 0, w, h, 0, 0.0f});
+    } else if (R.op == BOP_GRADIENTS || R.op == BOP_LAPLACIAN) {
+        for (int w = kGTX; w <= 4 * kGTX; w *= 2)
+            if (bt_tile_ok(R.op, R.in_type, R.kx, R.ky, w, kGTY)) out.push_back(TuneChoice{0, 0, w, kGTY, 0, 0.0f});
+    }
+    return out;
+}
+
 // Fill `out` from a validated request list; returns the total tile count.
 // The descriptor lists the requests grouped by tile routine (op, element
 // type, window): tiles are handed out in descriptor order, so the CTAs that
@@ -860,13 +974,26 @@ long long batch_describe(const BatchItem *items, int n, std::vector<BReq> &out)
         R.ky = it.ky;
         R.fx = it.fx;
         R.fy = it.fy;
-        for (int t = 0; t < it.kx && t < kBatchMaxTaps; ++t) R.wx[t] = (float)it.wx[t];
-        for (int t = 0; t < it.ky && t < kBatchMaxTaps; ++t) R.wy[t] = (float)it.wy[t];
-        const int tw = bt_tile_w(R.op, R.in_type), th = bt_tile_h(R.op, R.in_type, R.ky);
-        R.tiles_x = (R.nx + tw - 1) / tw;
-        const long long tiles = (long long)R.tiles_x * ((R.ny + th - 1) / th);
+        for (int t = 0; t < it.kx && t < kBatchMaxTaps; ++t) R.wx[t] = make_float2((float)it.wx[t], (float)it.wx[t]);
+        for (int t = 0; t < it.ky && t < kBatchMaxTaps; ++t) R.wy[t] = make_float2((float)it.wy[t], (float)it.wy[t]);
+        bt_choose_tile(R, nullptr);
+        R.tiles_x = (R.nx + R.tw - 1) / R.tw;
+        const long long tiles = (long long)R.tiles_x * ((R.ny + R.th - 1) / R.th);
         R.tile_base = base;
         base += tiles;
+        R.tile_end = base;
+    }
+    return base;
+}
+
+// Re-cuts the requests into tiles after their tile shapes changed.
+static long long bt_assign(std::vector<BReq> &reqs)
+{
+    long long base = 0;
+    for (BReq &R : reqs) {
+        R.tiles_x = (R.nx + R.tw - 1) / R.tw;
+        R.tile_base = base;
+        base += (long long)R.tiles_x * ((R.ny + R.th - 1) / R.th);
         R.tile_end = base;
     }
     return base;
@@ -913,7 +1040,106 @@ struct BatchPlanImpl {
     cudaGraphExec_t exec = nullptr;
     long long tiles = 0;
     int n = 0;
+    std::vector<BReq> reqs;           // the descriptors (host copy), for re-cutting after tuning
+    bool tuned = false;               // the tuner ran (or had nothing to tune) for this plan
 };
+
+// Uploads header + descriptors of `reqs` to `dev` (synchronous).
+static cudaError_t bt_upload(unsigned char *dev, const std::vector<BReq> &reqs, long long tiles)
+{
+    const size_t bytes = sizeof(BHdr) + reqs.size() * sizeof(BReq);
+    std::vector<unsigned char> host(bytes);
+    BHdr h{(int)reqs.size(), 0, tiles};
+    memcpy(host.data(), &h, sizeof h);
+    if (!reqs.empty()) memcpy(host.data() + sizeof(BHdr), reqs.data(), reqs.size() * sizeof(BReq));
+    return cudaMemcpy(dev, host.data(), bytes, cudaMemcpyHostToDevice);
+}
+
+// The tuner on a plan's first launch (stream s): every key of the plan that
+// has several candidate tiles and no cached choice is timed on the plan's
+// own requests of that key -- a batch of just those, one warm-up and three
+// timed launches per candidate -- and the fastest tile is cached.  Then the
+// plan is re-cut with the cached tiles.  The timed batches write the
+// requests' outputs, which the plan's launch then rewrites.
+static cudaError_t plan_tune(BatchPlanImpl *P, cudaStream_t s)
+{
+    BatchEngine *E;
+    cudaError_t e = engine_for(P->device, &E);
+    if (e != cudaSuccess) return e;
+    int *err = tma_error_word(P->device);
+    if (!err) return cudaErrorMemoryAllocation;
+    // keys in plan order, each with the indices of its requests
+    std::vector<std::vector<int>> groups;
+    for (int i = 0; i < P->n; ++i) {
+        const BReq &R = P->reqs[i];
+        bool found = false;
+        for (auto &g : groups) {
+            const BReq &Q = P->reqs[g[0]];
+            if (Q.op == R.op && Q.in_type == R.in_type && Q.out_type == R.out_type && Q.kx == R.kx &&
+                Q.ky == R.ky && bt_key_win(Q) == bt_key_win(R)) {
+                g.push_back(i);
+                found = true;
+                break;
+            }
+        }
+        if (!found) groups.push_back({i});
+    }
+    unsigned char *dev = nullptr;
+    unsigned long long *counter = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const size_t cap = sizeof(BHdr) + (size_t)P->n * sizeof(BReq);
+    if ((e = cudaMalloc(&dev, cap)) == cudaSuccess && (e = cudaMalloc(&counter, sizeof *counter)) == cudaSuccess &&
+        (e = cudaEventCreate(&e0)) == cudaSuccess && (e = cudaEventCreate(&e1)) == cudaSuccess &&
+        (e = cudaStreamSynchronize(s)) == cudaSuccess) {
+        for (const auto &g : groups) {
+            const BReq &R0 = P->reqs[g[0]];
+            TuneChoice have;
+            if (autotune_lookup_batch(R0.op, R0.in_type, R0.out_type, R0.kx, R0.ky, bt_key_win(R0), &have))
+                continue;
+            const std::vector<TuneChoice> cands = bt_candidates(R0);
+            if (cands.size() < 2) continue;
+            TuneChoice best{0, 0, 0, 0, 0, 1e30f};
+            for (const TuneChoice &c : cands) {
+                std::vector<BReq> sub;
+                for (int i : g) {
+                    sub.push_back(P->reqs[i]);
+                    bt_choose_tile(sub.back(), &c);
+                }
+                const long long tiles = bt_assign(sub);
+                if ((e = bt_upload(dev, sub, tiles)) != cudaSuccess) break;
+                auto run = [&]() {
+                    cudaMemsetAsync(counter, 0, sizeof *counter, s);
+                    k_batch<<<E->grid, kBatchThreads, kBatchSmem, s>>>(dev, counter, err);
+                    note_launch();
+                    return cudaGetLastError();
+                };
+                if ((e = run()) != cudaSuccess || (e = cudaEventRecord(e0, s)) != cudaSuccess) break;
+                for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = run();
+                if (e != cudaSuccess || (e = cudaEventRecord(e1, s)) != cudaSuccess ||
+                    (e = cudaEventSynchronize(e1)) != cudaSuccess)
+                    break;
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms /= 3.0f;
+                if (ms < best.ms) {
+                    best = c;
+                    best.ms = ms;
+                }
+            }
+            if (e != cudaSuccess) break;
+            if (best.ms < 1e30f)
+                autotune_store_batch(R0.op, R0.in_type, R0.out_type, R0.kx, R0.ky, bt_key_win(R0), best, true);
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (dev) cudaFree(dev);
+    if (counter) cudaFree(counter);
+    if (e != cudaSuccess) return e;
+    for (BReq &R : P->reqs) bt_choose_tile(R, nullptr);
+    P->tiles = bt_assign(P->reqs);
+    return bt_upload(P->dev, P->reqs, P->tiles);
+}
 
 cudaError_t plan_create(int device, const BatchItem *items, int n, void **out)
 {
@@ -923,16 +1149,11 @@ cudaError_t plan_create(int device, const BatchItem *items, int n, void **out)
     auto *P = new BatchPlanImpl();
     P->device = device;
     P->n = n;
-    std::vector<BReq> reqs;
-    P->tiles = batch_describe(items, n, reqs);
+    P->tiles = batch_describe(items, n, P->reqs);
     const size_t bytes = sizeof(BHdr) + (size_t)n * sizeof(BReq);
-    std::vector<unsigned char> host(bytes);
-    BHdr h{n, 0, P->tiles};
-    memcpy(host.data(), &h, sizeof h);
-    if (n) memcpy(host.data() + sizeof(BHdr), reqs.data(), (size_t)n * sizeof(BReq));
     if ((e = cudaMalloc(&P->dev, bytes)) != cudaSuccess ||
         (e = cudaMalloc(&P->counter, sizeof(unsigned long long))) != cudaSuccess ||
-        (e = cudaMemcpy(P->dev, host.data(), bytes, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        (e = bt_upload(P->dev, P->reqs, P->tiles)) != cudaSuccess) {
         plan_destroy(P);
         return e;
     }
@@ -960,6 +1181,11 @@ cudaError_t plan_create(int device, const BatchItem *items, int n, void **out)
 cudaError_t plan_launch(void *plan, cudaStream_t s, long long *tiles)
 {
     auto *P = (BatchPlanImpl *)plan;
+    if (!P->tuned && P->tiles > 0 && autotune_enabled()) {
+        cudaError_t e = plan_tune(P, s);
+        if (e != cudaSuccess) return e;
+        P->tuned = true;
+    }
     if (tiles) *tiles = P->tiles;
     if (P->tiles == 0) return cudaSuccess;
     cudaError_t e = cudaGraphLaunch(P->exec, s);

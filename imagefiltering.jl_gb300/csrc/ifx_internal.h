@@ -99,7 +99,7 @@ struct TuneChoice {
     int variant, x_first, tile_w, tile_h, depth;
     float ms;
 };
-enum { TUNE_SEP2D = 0, TUNE_SEP3D = 1 };
+enum { TUNE_SEP2D = 0, TUNE_SEP3D = 1, TUNE_BATCH = 2 };
 void autotune_set(bool enable, const char *path);
 bool autotune_enabled();
 bool autotune_lookup(const Sep2dArgs &a, TuneChoice *c);
@@ -110,6 +110,11 @@ bool autotune_lookup_key(int path, int in_type, int out_type, int kx, int ky, in
 void autotune_pin_key(int path, int in_type, int out_type, int kx, int ky, int kz, int fill, long long nx,
                       long long ny, long long nz, const TuneChoice &c);
 void autotune_clear();
+// the batched engine's tile per (op, eltypes, taps, median window): a cached
+// choice (tile_w, tile_h) and storing one (persist: written to the cache file)
+bool autotune_lookup_batch(int op, int in_type, int out_type, int kx, int ky, int win, TuneChoice *c);
+void autotune_store_batch(int op, int in_type, int out_type, int kx, int ky, int win, const TuneChoice &c,
+                          bool persist);
 // the fused 2-D separable filter of `a`, tuned (device_arrays: tuning allowed)
 cudaError_t launch_sep2d_tuned(Sep2dArgs a, cudaStream_t s, bool device_arrays);
 // the 3-D separable filter of `a`: the cached choice, or (tuner enabled,

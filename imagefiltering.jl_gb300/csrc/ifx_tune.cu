@@ -15,6 +15,9 @@
 //  z-marching kernel with its chunk depth -- the output slices a CTA walks,
 //  over which the kz - 1 halo slices, filtered along x and y once per chunk,
 //  are amortised.
+//  Batched engine (ifx_batch.cu tunes it, on a plan's first launch): the tile
+//  shape of each (op, eltypes, taps) group of requests, stored here under the
+//  key (TUNE_BATCH, eltypes, kx, ky, median window, op).
 //
 // With the tuner enabled, the first device-array call for a key
 //   (path, input eltype, output eltype, x / y / z taps, Fill or Pad,
@@ -216,6 +219,24 @@ void autotune_clear()
     Tuner &T = tuner();
     std::lock_guard<std::mutex> lk(T.mu);
     T.cache.clear();
+}
+
+bool autotune_lookup_batch(int op, int in_type, int out_type, int kx, int ky, int win, TuneChoice *c)
+{
+    return lookup(TuneKey{TUNE_BATCH, in_type, out_type, kx, ky, win, op, 0, 0}, c);
+}
+
+void autotune_store_batch(int op, int in_type, int out_type, int kx, int ky, int win, const TuneChoice &c,
+                          bool persist)
+{
+    const TuneKey k{TUNE_BATCH, in_type, out_type, kx, ky, win, op, 0, 0};
+    if (persist) {
+        store(k, c);
+        return;
+    }
+    Tuner &T = tuner();
+    std::lock_guard<std::mutex> lk(T.mu);
+    T.cache[k] = c;
 }
 
 bool autotune_lookup(const Sep2dArgs &a, TuneChoice *c) { return lookup(key_of(a), c); }

@@ -241,6 +241,21 @@ int ifx_autotune_pin(ifx_context_t *ctx, int32_t path, int32_t in_type, int32_t 
                      int32_t fill, const int64_t *size, const ifx_tune_choice_t *choice);
 /* Forgets every cached and pinned choice (the cache file is left as it is). */
 int ifx_autotune_clear(ifx_context_t *ctx);
+/* The batched engine (ifx_batch_plan_launch): with the tuner enabled, a
+ * plan's first launch times, for every key of its requests without a cached
+ * choice (op, image and output eltypes, taps -- factored: the two factors'
+ * taps, gradients: 3, 3, others ignored -- and the median window), the
+ * candidate output tiles on the plan's own requests of that key, and caches
+ * the fastest; later plans and ifx_batch_run / the server use cached tiles.
+ * Candidates: factored tiles 64, 128 or 256 wide (8-bit images; Float32
+ * rows hold 64) at the tallest height the staging rows allow for the y
+ * factor and half of it; gradient and Laplacian tiles 88, 176 or 352 wide
+ * (8-bit images).  Median tiles are fixed.  tile_w / tile_h of the choice;
+ * a tile the engine cannot take runs as the default. */
+int ifx_batch_autotune_lookup(ifx_context_t *ctx, int32_t op, int32_t in_type, int32_t out_type, int32_t kx,
+                              int32_t ky, int32_t window, ifx_tune_choice_t *choice);
+int ifx_batch_autotune_pin(ifx_context_t *ctx, int32_t op, int32_t in_type, int32_t out_type, int32_t kx,
+                           int32_t ky, int32_t window, const ifx_tune_choice_t *choice);
 
 /* ---- Algorithm.IIR(): Triggs-Sdika recursive filters ---------------------------
  * One factor per pass, a KernelFactors.TriggsSdika (src/kernelfactors.jl:

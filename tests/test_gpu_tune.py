@@ -189,3 +189,125 @@ def test_autotune_widened(gpu_ifx, oracle, tmp_path):
     finally:
         ifx.autotune(False, None)
         ifx.autotune_clear()
+
+
+# ---------------------------------------------------------------- the batched engine's tiles
+def _batch_items(ifx, rng, op, kind, n=10):
+    items = []
+    for i in range(n):
+        h, w = int(rng.integers(1, 420)), int(rng.integers(2, 700))
+        style = STYLES[int(rng.integers(0, 5))]
+        if style == "reflect" and (h == 1 or w == 1):
+            style = "symmetric"
+        fill = {"F32": 0.3, "N0F8": 0.6, "U8": 17}[kind]
+        border = ifx.Fill(fill) if style == "fill" else ifx.Pad(style)
+        img = _img(rng, (h, w), kind)
+        items.append((ifx.n0f8(img) if kind == "N0F8" else img, op, border))
+    return items
+
+
+def _batch_oracle(ifx, oracle, img, op, border):
+    kind = "N0F8" if isinstance(img, ifx.N0f8Array) else ("U8" if img.dtype == np.uint8 else "F32")
+    vals = img.astype(np.float64) / 255.0 if kind == "N0F8" else img.astype(np.float64)
+    style = "fill" if isinstance(border, ifx.Fill) else border.style
+    fv = {"F32": float(np.float32(0.3)), "N0F8": round(0.6 * 255) / 255.0, "U8": 17.0}[kind] if style == "fill" \
+        else 0.0
+    if op[0] == "gaussian":
+        k = np.asarray(ifx.KernelFactors.gaussian(op[1]).data)
+        return [oracle.imfilter_cascade(vals, [(0, -(k.size // 2), k), (1, -(k.size // 2), k)], style, fv)]
+    if op[0] == "sobel":
+        d, s = ifx.KernelFactors.sobel.gradient_pair
+        return [oracle.imfilter_cascade(vals, [(0, -1, d if ax == 0 else s), (1, -1, s if ax == 0 else d)], style,
+                                        fv) for ax in range(2)]
+    vals32 = (img.astype(np.float32) / np.float32(255)).astype(np.float64) if kind == "N0F8" else vals
+    fv32 = float(np.float32(round(0.6 * 255)) / np.float32(255)) if kind == "N0F8" else float(np.float32(fv))
+    return [oracle.laplacian(vals32, [1, 1], style, fv32 if style == "fill" else 0.0, "f32")]
+
+
+@pytest.mark.parametrize("op,kind,tiles", [
+    (("gaussian", 2.0), "N0F8", [(64, 56), (64, 24), (128, 56), (128, 24), (256, 56), (256, 24)]),
+    (("gaussian", 7.5), "U8", [(64, 32), (128, 16), (256, 32)]),
+    (("gaussian", 1.2), "F32", [(64, 56), (64, 24)]),
+    (("sobel",), "N0F8", [(88, 56), (176, 56), (352, 56)]),
+    (("laplacian",), "N0F8", [(88, 56), (176, 56), (352, 56)]),
+])
+def test_batch_pinned_tiles(gpu_ifx, oracle, op, kind, tiles):
+    """Every tile the batched engine's tuner may pick, pinned in turn: the
+    batch's results against the oracle (Laplacian exact), and the same bits
+    for every tile (the tile does not change an output's arithmetic)."""
+    ifx = gpu_ifx
+    import torch
+    from imagefiltering_gb300 import batch as B
+    rng = np.random.default_rng(zlib.crc32(repr((op, kind)).encode()))
+    items = _batch_items(ifx, rng, op, kind)
+    name = {"gaussian": "factored", "sobel": "gradients", "laplacian": "laplacian"}[op[0]]
+    taps = len(ifx.KernelFactors.gaussian(op[1]).data) if op[0] == "gaussian" else 3
+    refs = [_batch_oracle(ifx, oracle, img, o, b) for img, o, b in items]
+    first = None
+    try:
+        for tw, th in tiles:
+            B.autotune_pin(name, kind, B.out_kinds(op)[0] if op[0] != "laplacian" else "F32", tw, th, taps, taps)
+            bt = B.Batch()
+            outs = []
+            for img, o, border in items:
+                d = ifx.DeviceArray.from_host(img)
+                oo = B.outputs_for(o, d)
+                bt.add(o, d, oo, border)
+                outs.append(oo)
+            bt.run()
+            torch.cuda.synchronize()
+            got = [[x.numpy() for x in oo] for oo in outs]
+            for g, r, (img, _, border) in zip(got, refs, items):
+                for a, b in zip(g, r):
+                    if op[0] == "laplacian":
+                        assert np.array_equal(np.asarray(a, np.float64), b), (tw, th, img.shape, border)
+                    else:
+                        assert normwise(a, b) <= 1e-5 or np.max(np.abs(a - b)) < 1e-6, (tw, th, img.shape)
+            if first is None:
+                first = got
+            else:
+                for u, v in zip(first, got):
+                    for a, b in zip(u, v):
+                        assert np.array_equal(a, b), (tw, th)
+    finally:
+        ifx.autotune_clear()
+
+
+def test_batch_plan_tuned_on_first_launch(gpu_ifx, oracle):
+    """With the tuner enabled, a plan's first launch times the candidate tiles
+    of its keys, caches the fastest, and its results match the untuned run."""
+    ifx = gpu_ifx
+    import torch
+    from imagefiltering_gb300 import batch as B
+    rng = np.random.default_rng(77)
+    items = _batch_items(ifx, rng, ("gaussian", 3.0), "N0F8", n=12) + \
+        _batch_items(ifx, rng, ("laplacian",), "N0F8", n=6)
+    bt = B.Batch()
+    outs = []
+    for img, o, border in items:
+        d = ifx.DeviceArray.from_host(img)
+        oo = B.outputs_for(o, d)
+        bt.add(o, d, oo, border)
+        outs.append(oo)
+    try:
+        ifx.autotune_clear()
+        bt.run()
+        torch.cuda.synchronize()
+        base = [[x.numpy() for x in oo] for oo in outs]
+        plan = B.Plan(bt)
+        ifx.autotune(True, None)
+        plan.launch()
+        torch.cuda.synchronize()
+        taps = len(ifx.KernelFactors.gaussian(3.0).data)
+        cf = B.autotune_lookup("factored", "N0F8", "F64", taps, taps)
+        cl = B.autotune_lookup("laplacian", "N0F8", "F32")
+        assert cf is not None and cf["tile_w"] in (64, 128, 256) and cf["ms"] > 0
+        assert cl is not None and cl["tile_w"] in (88, 176, 352)
+        again = [[x.numpy() for x in oo] for oo in outs]
+        for u, v in zip(base, again):
+            for a, b in zip(u, v):
+                assert np.array_equal(a, b)
+        plan.close()
+    finally:
+        ifx.autotune(False, None)
+        ifx.autotune_clear()
