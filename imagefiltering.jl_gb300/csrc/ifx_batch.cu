@@ -1055,10 +1055,14 @@ static cudaError_t bt_upload(unsigned char *dev, const std::vector<BReq> &reqs, 
     return cudaMemcpy(dev, host.data(), bytes, cudaMemcpyHostToDevice);
 }
 
+// A tile replaces the default only when it is at least this much faster.
+constexpr float kBatchTuneMargin = 0.97f;
+
 // The tuner on a plan's first launch (stream s): every key of the plan that
 // has several candidate tiles and no cached choice is timed on the plan's
 // own requests of that key -- a batch of just those, one warm-up and three
-// timed launches per candidate -- and the fastest tile is cached.  Then the
+// timed launches per candidate, L2 overwritten before each -- and the
+// fastest tile is cached (the default unless another is clearly faster).  Then the
 // plan is re-cut with the cached tiles.  The timed batches write the
 // requests' outputs, which the plan's launch then rewrites.
 static cudaError_t plan_tune(BatchPlanImpl *P, cudaStream_t s)
@@ -1086,11 +1090,10 @@ static cudaError_t plan_tune(BatchPlanImpl *P, cudaStream_t s)
     }
     unsigned char *dev = nullptr;
     unsigned long long *counter = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TuneTimer tt;
     const size_t cap = sizeof(BHdr) + (size_t)P->n * sizeof(BReq);
     if ((e = cudaMalloc(&dev, cap)) == cudaSuccess && (e = cudaMalloc(&counter, sizeof *counter)) == cudaSuccess &&
-        (e = cudaEventCreate(&e0)) == cudaSuccess && (e = cudaEventCreate(&e1)) == cudaSuccess &&
-        (e = cudaStreamSynchronize(s)) == cudaSuccess) {
+        (e = tt.init()) == cudaSuccess && (e = cudaStreamSynchronize(s)) == cudaSuccess) {
         for (const auto &g : groups) {
             const BReq &R0 = P->reqs[g[0]];
             TuneChoice have;
@@ -1098,8 +1101,13 @@ static cudaError_t plan_tune(BatchPlanImpl *P, cudaStream_t s)
                 continue;
             const std::vector<TuneChoice> cands = bt_candidates(R0);
             if (cands.size() < 2) continue;
-            TuneChoice best{0, 0, 0, 0, 0, 1e30f};
-            for (const TuneChoice &c : cands) {
+            // the default tile first; another replaces it only when clearly faster
+            BReq D = R0;
+            bt_choose_tile(D, nullptr);
+            TuneChoice def{0, 0, D.tw, D.th, 0, 0.0f}, best{0, 0, 0, 0, 0, 1e30f};
+            for (int ci = -1; ci < (int)cands.size() && e == cudaSuccess; ++ci) {
+                const TuneChoice c = ci < 0 ? def : cands[ci];
+                if (ci >= 0 && c.tile_w == def.tile_w && c.tile_h == def.tile_h) continue;
                 std::vector<BReq> sub;
                 for (int i : g) {
                     sub.push_back(P->reqs[i]);
@@ -1107,32 +1115,27 @@ static cudaError_t plan_tune(BatchPlanImpl *P, cudaStream_t s)
                 }
                 const long long tiles = bt_assign(sub);
                 if ((e = bt_upload(dev, sub, tiles)) != cudaSuccess) break;
-                auto run = [&]() {
-                    cudaMemsetAsync(counter, 0, sizeof *counter, s);
-                    k_batch<<<E->grid, kBatchThreads, kBatchSmem, s>>>(dev, counter, err);
-                    note_launch();
-                    return cudaGetLastError();
-                };
-                if ((e = run()) != cudaSuccess || (e = cudaEventRecord(e0, s)) != cudaSuccess) break;
-                for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = run();
-                if (e != cudaSuccess || (e = cudaEventRecord(e1, s)) != cudaSuccess ||
-                    (e = cudaEventSynchronize(e1)) != cudaSuccess)
-                    break;
                 float ms = 0.0f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                ms /= 3.0f;
+                e = tt.time(
+                    [&]() {
+                        cudaMemsetAsync(counter, 0, sizeof *counter, s);
+                        k_batch<<<E->grid, kBatchThreads, kBatchSmem, s>>>(dev, counter, err);
+                        note_launch();
+                        return cudaGetLastError();
+                    },
+                    s, &ms);
+                if (e != cudaSuccess) break;
+                if (ci < 0) def.ms = ms;
                 if (ms < best.ms) {
                     best = c;
                     best.ms = ms;
                 }
             }
             if (e != cudaSuccess) break;
-            if (best.ms < 1e30f)
-                autotune_store_batch(R0.op, R0.in_type, R0.out_type, R0.kx, R0.ky, bt_key_win(R0), best, true);
+            if (best.ms > kBatchTuneMargin * def.ms) best = def;
+            autotune_store_batch(R0.op, R0.in_type, R0.out_type, R0.kx, R0.ky, bt_key_win(R0), best, true);
         }
     }
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
     if (dev) cudaFree(dev);
     if (counter) cudaFree(counter);
     if (e != cudaSuccess) return e;

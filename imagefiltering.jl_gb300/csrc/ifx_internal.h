@@ -3,6 +3,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <functional>
 #include <vector>
 #include "ifx_common.cuh"
 
@@ -100,6 +101,15 @@ struct TuneChoice {
     float ms;
 };
 enum { TUNE_SEP2D = 0, TUNE_SEP3D = 1, TUNE_BATCH = 2 };
+// Times tuner candidates with L2 overwritten before each timed launch.
+struct TuneTimer {
+    void *flush = nullptr;
+    size_t flush_bytes = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t init();
+    ~TuneTimer();
+    cudaError_t time(const std::function<cudaError_t()> &run, cudaStream_t s, float *ms);
+};
 void autotune_set(bool enable, const char *path);
 bool autotune_enabled();
 bool autotune_lookup(const Sep2dArgs &a, TuneChoice *c);

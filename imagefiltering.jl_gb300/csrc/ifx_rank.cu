@@ -682,12 +682,18 @@ static bool extrema_vhgw_u8(const ExtremaPassArgs &a, cudaStream_t s, cudaError_
 // the pass's axis.  Outputs: interleaved (min, max) codes, or one of them.
 // =========================================================================
 template <int W> struct ExTile {
-    static constexpr int NRX = ((128 + W - 1) / W + 1) & ~1;   // runs per row (even: even tile width)
-    static constexpr int NRY = (32 + W / 2) / W;               // runs per column (tiles about 32 tall)
+    // runs per row: a multiple of 4, so that the tile width is (the y pass
+    // takes four columns per word, and their stores align)
+    static constexpr int NRX = ((128 + W - 1) / W + 1) & ~1;
+    // runs per column: tiles about 64 tall (about 32 for W > 17, whose
+    // staging would pass the 48 KB of static shared memory)
+    static constexpr int NRY = ((W <= 17 ? 64 : 32) + W / 2) / W;
     static constexpr int TX = W * NRX, TY = W * NRY;
     static constexpr int R = TY + W - 1, C = TX + W - 1;
     static constexpr int RP = (R + 1) & ~1;                    // rows staged (even: row pairs)
     static constexpr int CP = (C + 3) & ~3;
+    static constexpr int NV = (C + 30) / 16;                   // 16-byte vectors of a row's aligned superset
+    static constexpr int CV = 16 * NV;                         // staged row pitch (bytes)
 };
 
 // Van Herk / Gil-Werman over a run: out[i] = op over v[i .. i+W-1], i < W,
@@ -713,11 +719,45 @@ k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int n
                uint32_t fill, int which)
 {
     using G = ExTile<W>;
-    __shared__ __align__(16) uint8_t xin[G::RP * G::CP];
+    __shared__ __align__(16) uint8_t xin[G::RP * G::CV];
     __shared__ __align__(16) uint8_t xmn[G::RP * G::TX];
     __shared__ __align__(16) uint8_t xmx[G::RP * G::TX];
     const int tx0 = blockIdx.x * G::TX, ty0 = blockIdx.y * G::TY;
-    {   // a warp per staged row, four columns per lane (one 32-bit shared store);
+    // The staged window: rows ty0 + a0 .. + RP - 1, columns from tx0 + a0,
+    // coordinates clamped to the image (equal to the truncated windows).  A
+    // window inside the image, in an image whose rows start on 16-byte
+    // boundaries, is staged by 16-byte loads of each row's aligned superset
+    // (its first `lead` bytes precede the window); others byte by byte
+    // through the clamp (lead 0).
+    const int gx0 = tx0 + a0, gy0 = ty0 + a0, ax = gx0 & ~15;
+    const bool vec = ((uintptr_t)img & 15) == 0 && (nx & 15) == 0 && gx0 >= 0 && gy0 >= 0 &&
+                     gy0 + G::RP <= ny && ax + G::CV <= nx;
+    const int lead = vec ? gx0 - ax : 0;
+    if (vec) {
+        // (row, vector) items, four loads in flight per thread before the stores
+        constexpr int TOT = G::RP * G::NV;
+        const uint4 *src = reinterpret_cast<const uint4 *>(img + (long long)gy0 * nx + ax);
+        const int rowv = nx >> 4;
+        for (int base = threadIdx.x; base < TOT; base += 4 * blockDim.x) {
+            uint4 v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int it = base + q * blockDim.x;
+                if (it < TOT) {
+                    const int r = it / G::NV, k = it - r * G::NV;
+                    v[q] = __ldg(src + (long long)r * rowv + k);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int it = base + q * blockDim.x;
+                if (it < TOT) {
+                    const int r = it / G::NV, k = it - r * G::NV;
+                    *reinterpret_cast<uint4 *>(xin + r * G::CV + 16 * k) = v[q];
+                }
+            }
+        }
+    } else {   // a warp per staged row, four columns per lane (one 32-bit shared store);
         // a warp's loads for up to four rows are in flight before it stores
         constexpr int kChunks = (G::CP + 127) / 128;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -743,7 +783,7 @@ k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int n
 #pragma unroll
                 for (int k = 0; k < kChunks; ++k) {
                     const int r = r0 + q * nw, c = 4 * lane + 128 * k;
-                    if (r < G::RP && c < G::CP) *reinterpret_cast<uint32_t *>(xin + r * G::CP + c) = word[q][k];
+                    if (r < G::RP && c < G::CP) *reinterpret_cast<uint32_t *>(xin + r * G::CV + c) = word[q][k];
                 }
         }
     }
@@ -752,14 +792,14 @@ k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int n
     // x pass: row pairs (r, r+1) x runs of W outputs
     for (int it = threadIdx.x; it < (G::RP / 2) * G::NRX; it += blockDim.x) {
         const int rp = it / G::NRX, run = it - rp * G::NRX, r = 2 * rp, c0 = run * W;
-        // bytes c0 .. c0+2W-2 of rows r and r+1, read as aligned words
+        // bytes c0 .. c0+2W-2 of the window's rows r and r+1, read as aligned words
         constexpr int NWD = (2 * W - 1 + 3) / 4 + 1;
-        const int a = c0 & ~3, sh = c0 & 3;
+        const int a = (lead + c0) & ~3, sh = (lead + c0) & 3;
         uint32_t ra[NWD], rb[NWD];
 #pragma unroll
         for (int q = 0; q < NWD; ++q) {
-            ra[q] = a + 4 * q < G::CP ? *reinterpret_cast<const uint32_t *>(xin + r * G::CP + a + 4 * q) : 0u;
-            rb[q] = a + 4 * q < G::CP ? *reinterpret_cast<const uint32_t *>(xin + (r + 1) * G::CP + a + 4 * q) : 0u;
+            ra[q] = a + 4 * q < G::CV ? *reinterpret_cast<const uint32_t *>(xin + r * G::CV + a + 4 * q) : 0u;
+            rb[q] = a + 4 * q < G::CV ? *reinterpret_cast<const uint32_t *>(xin + (r + 1) * G::CV + a + 4 * q) : 0u;
         }
         // realigned so that byte j is byte j % 4 of word j / 4 (compile-time indices)
         uint32_t al[NWD - 1], bl[NWD - 1];

@@ -22,9 +22,11 @@
 // With the tuner enabled, the first device-array call for a key
 //   (path, input eltype, output eltype, x / y / z taps, Fill or Pad,
 //    size class = floor(log2(elements)), FP64 arithmetic)
-// times every applicable candidate on the call's stream (one warm-up and
-// three timed launches each, CUDA events), keeps the fastest and runs it;
-// later calls with the key take the cached choice without timing.  Choices
+// times the default and every applicable candidate on the call's stream (one
+// warm-up and three timed launches each, CUDA events, L2 overwritten before
+// each timed launch), keeps the fastest -- the default unless another is at
+// least 3 % faster -- and runs it; later calls with the key take the cached
+// choice without timing.  Choices
 // persist in a text cache file, one line per key, loaded when the tuner is
 // enabled and appended as keys are tuned.  Host arrays are never tuned
 // (their time is the copies'); with the tuner disabled cached choices still
@@ -32,6 +34,7 @@
 #include "ifx_internal.h"
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -135,34 +138,50 @@ void store(const TuneKey &k, const TuneChoice &c)
     append_file(T, k, c);
 }
 
-// Times `run` (one warm-up, three timed launches) on stream s; ms per launch.
-template <class F> cudaError_t time_candidate(F run, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, float *ms)
+} // namespace
+
+// Candidate timing: one warm-up launch, then three timed launches, each
+// after L2 is overwritten (a device buffer twice the L2 size is cleared), so
+// that every timed launch reads its inputs from HBM as a call on fresh data
+// does; the mean of the three, in ms.
+cudaError_t TuneTimer::init()
+{
+    cudaError_t e;
+    int dev = 0, l2 = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+    flush_bytes = 2 * (size_t)(l2 > 0 ? l2 : (64 << 20));
+    if ((e = cudaMalloc(&flush, flush_bytes)) != cudaSuccess) return e;
+    if ((e = cudaEventCreate(&e0)) != cudaSuccess) return e;
+    return cudaEventCreate(&e1);
+}
+
+TuneTimer::~TuneTimer()
+{
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (flush) cudaFree(flush);
+}
+
+cudaError_t TuneTimer::time(const std::function<cudaError_t()> &run, cudaStream_t s, float *ms)
 {
     cudaError_t e;
     if ((e = run()) != cudaSuccess) return e;
-    if ((e = cudaEventRecord(e0, s)) != cudaSuccess) return e;
-    for (int r = 0; r < 3; ++r)
+    float total = 0.0f;
+    for (int r = 0; r < 3; ++r) {
+        if ((e = cudaMemsetAsync(flush, r, flush_bytes, s)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(e0, s)) != cudaSuccess) return e;
         if ((e = run()) != cudaSuccess) return e;
-    if ((e = cudaEventRecord(e1, s)) != cudaSuccess || (e = cudaEventSynchronize(e1)) != cudaSuccess) return e;
-    float t = 0.0f;
-    if ((e = cudaEventElapsedTime(&t, e0, e1)) != cudaSuccess) return e;
-    *ms = t / 3.0f;
+        if ((e = cudaEventRecord(e1, s)) != cudaSuccess || (e = cudaEventSynchronize(e1)) != cudaSuccess) return e;
+        float t = 0.0f;
+        if ((e = cudaEventElapsedTime(&t, e0, e1)) != cudaSuccess) return e;
+        total += t;
+    }
+    *ms = total / 3.0f;
     return cudaSuccess;
 }
 
-struct Events {
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    cudaError_t init()
-    {
-        cudaError_t e = cudaEventCreate(&e0);
-        return e != cudaSuccess ? e : cudaEventCreate(&e1);
-    }
-    ~Events()
-    {
-        if (e0) cudaEventDestroy(e0);
-        if (e1) cudaEventDestroy(e1);
-    }
-};
+namespace {
 
 // The 2-D candidates: per kernel and pass order, the distinct tile shapes the
 // kernel takes (a requested shape it cannot take runs as its default, so
@@ -269,29 +288,39 @@ static Sep2dArgs with_choice(Sep2dArgs a, const TuneChoice &c)
     return a;
 }
 
+// A candidate replaces the default only when it is at least this much faster
+// (timing noise does not move a key off the default).
+constexpr float kTuneMargin = 0.97f;
+
 cudaError_t launch_sep2d_tuned(Sep2dArgs a, cudaStream_t s, bool device_arrays)
 {
     TuneChoice ch;
     if (autotune_lookup(a, &ch)) return launch_sep2d(with_choice(a, ch), s);
     if (!autotune_enabled() || !device_arrays) return launch_sep2d(a, s);
-    Events ev;
+    TuneTimer tt;
     cudaError_t e;
-    if ((e = ev.init()) != cudaSuccess) return e;
-    TuneChoice best{0, a.x_first, 0, 0, 0, 1e30f};
+    if ((e = tt.init()) != cudaSuccess) return e;
+    // the default first (the kernel and tile an untuned call runs, written out)
+    TuneChoice def{sep2d_tma_applies(a) ? 1 : 2, a.x_first, 0, 0, 0, 0.0f};
+    {
+        Sep2dArgs d = a;
+        d.variant = def.variant;
+        if (!sep2d_tile_shape(d, def.variant, &def.tile_w, &def.tile_h)) def.tile_w = def.tile_h = 0;
+    }
+    if ((e = tt.time([&] { return launch_sep2d(with_choice(a, def), s); }, s, &def.ms)) != cudaSuccess) return e;
+    TuneChoice best = def;
     for (const TuneChoice &c : sep2d_candidates(a)) {
         const Sep2dArgs ca = with_choice(a, c);
         float ms;
-        if ((e = time_candidate([&] { return launch_sep2d(ca, s); }, s, ev.e0, ev.e1, &ms)) != cudaSuccess) return e;
+        if ((e = tt.time([&] { return launch_sep2d(ca, s); }, s, &ms)) != cudaSuccess) return e;
         if (ms < best.ms) {
             best = c;
             best.ms = ms;
         }
     }
-    if (best.ms < 1e30f) {
-        store(key_of(a), best);
-        a = with_choice(a, best);
-    }
-    return launch_sep2d(a, s);           // the result of the chosen candidate is the call's
+    if (best.ms > kTuneMargin * def.ms) best = def;
+    store(key_of(a), best);
+    return launch_sep2d(with_choice(a, best), s);    // the result of the chosen candidate is the call's
 }
 
 cudaError_t launch_sep3d_tuned(const Sep3dArgs &a, float *tmp, cudaStream_t s, bool device_arrays)
@@ -316,21 +345,23 @@ cudaError_t launch_sep3d_tuned(const Sep3dArgs &a, float *tmp, cudaStream_t s, b
         for (int d : zd)
             if (d < 2 * a.nz || d == 8) cands.push_back(TuneChoice{2, 1, 0, 0, d, 0.0f});
     }
-    Events ev;
+    TuneTimer tt;
     cudaError_t e;
-    if ((e = ev.init()) != cudaSuccess) return e;
-    TuneChoice best = ch;
-    best.ms = 1e30f;
+    if ((e = tt.init()) != cudaSuccess) return e;
+    TuneChoice def = ch;                                // the default: split where it applies
+    if ((e = tt.time([&] { return run(def); }, s, &def.ms)) != cudaSuccess) return e;
+    TuneChoice best = def;
     for (const TuneChoice &c : cands) {
         float ms;
-        if ((e = time_candidate([&] { return run(c); }, s, ev.e0, ev.e1, &ms)) != cudaSuccess) return e;
+        if ((e = tt.time([&] { return run(c); }, s, &ms)) != cudaSuccess) return e;
         if (ms < best.ms) {
             best = c;
             best.ms = ms;
         }
     }
-    if (best.ms < 1e30f) store(key_of(a), best);
-    return run(best.ms < 1e30f ? best : ch);
+    if (best.ms > kTuneMargin * def.ms) best = def;
+    store(key_of(a), best);
+    return run(best);
 }
 
 } // namespace ifx

@@ -435,10 +435,11 @@ def test_extrema_exact(gpu_ifx, oracle, kind):
 def test_extrema_2d_tile_kernel(gpu_ifx, oracle, w):
     """8-bit square windows take the one-launch 2-D tile kernel: against the
     oracle for images smaller than a window, odd widths and several tiles per
-    axis, every Pad style and Fill, and min, max or both."""
+    axis, widths a multiple of 16 (interior tiles staged by 16-byte loads),
+    every Pad style and Fill, and min, max or both."""
     ifx = gpu_ifx
     rng = np.random.default_rng(1000 + w)
-    for shape in [(5, 3), (w + 2, 2 * w + 1), (301, 157)]:
+    for shape in [(5, 3), (w + 2, 2 * w + 1), (301, 157), (512, 203)]:
         img = np.asfortranarray(rng.integers(0, 256, shape, dtype=np.uint8))
         mm = ifx.mapwindow(ifx.extrema, ifx.n0f8(img), (w, w))
         mn, mx = oracle.extrema_trunc(img.astype(np.float64), [w, w])
