@@ -213,6 +213,37 @@ def alg_bytes(r):
     return r.in_bytes() + r.out_bytes()
 
 
+# Per-pixel arithmetic of each request kind, as lane operations on the pipe it
+# runs on: FMA pipe (128 lanes per SM and clock) for the linear filters, the
+# integer ALU (64 lanes per SM and clock) for the median networks' min/max.
+#   Gaussian: taps x + taps y multiply-adds (no halo); Sobel: two 3-tap passes
+#   per output, two outputs; Laplacian: one multiply and four adds; median:
+#   the generated block networks' min/max per output (3x3 18.5, 5x5 83.5), two
+#   outputs per operation for 8-bit codes (16-bit lanes).
+def alg_ops(r):
+    if r.op == "gaussian":
+        return 2 * r.taps() * r.pixels, 0
+    if r.op == "sobel":
+        return 12 * r.pixels, 0
+    if r.op == "laplacian":
+        return 5 * r.pixels, 0
+    per = 18.5 if r.win == 3 else 83.5
+    return 0, per * r.pixels / (2 if r.kind != "F32" else 1)
+
+
+def mixed_floor_ms(reqs, hbm_gbs, sm_mhz, sms=152):
+    """Lower bound of a wave's device time: per request the larger of its HBM
+    time (algorithmic bytes at the measured copy rate) and its arithmetic time
+    (alg_ops at full pipe rate and the sampled SM clock), summed."""
+    fma_rate = sms * 128 * sm_mhz * 1e6
+    alu_rate = sms * 64 * sm_mhz * 1e6
+    t = 0.0
+    for r in reqs:
+        fma, alu = alg_ops(r)
+        t += max(alg_bytes(r) / (hbm_gbs * 1e9), fma / fma_rate, alu / alu_rate)
+    return t * 1e3
+
+
 BATCH_OP = {"gaussian": lambda r: ("gaussian", r.sigma), "sobel": lambda r: ("sobel",),
             "laplacian": lambda r: ("laplacian",), "median": lambda r: ("median", r.win)}
 
@@ -1050,6 +1081,11 @@ def main():
     per_op = res["per_op"]
     bk_ms, bk_bytes, bk_n = res["batch_kernel"]
     achieved = bk_bytes / (bk_ms / 1e3) / 1e9
+    sm_mhz = (res["clocks"] or {}).get("sm_mhz") or 2070.0
+    floor = mixed_floor_ms(res["reqs"], hbm_peak, sm_mhz)
+    mixed = {"ms": floor, "frac": floor / bk_ms, "sm_mhz": sm_mhz,
+             "note": "per request max(HBM time, FMA- or ALU-pipe time of its arithmetic) summed over the "
+                     "timed waves; frac = floor / the k_batch launches' device time"}
     plain_value, _, _ = job_throughput(res["plain_ms"], res["pixels"], dist if ws > 1 else None, "cuda")
     e2e = run_stream_e2e(args, ifx, torch, res["reqs"])
     if ws > 1:                                   # the served stream of every rank, slowest wall time
@@ -1097,7 +1133,8 @@ def main():
                      "traffic_source": "DRAM read+write bytes of one k_batch launch in an ncu capture "
                                        "of a 60-request wave of the same stream: %.4f x the algorithmic "
                                        "bytes, scaled to this launch's" % K_BATCH_TRAFFIC_RATIO,
-                     "launches": bk_n, "alg_bytes_per_launch": bk_bytes / max(bk_n, 1)},
+                     "launches": bk_n, "alg_bytes_per_launch": bk_bytes / max(bk_n, 1),
+                     "mixed_floor": mixed},
         "clocks": res["clocks"],
         "dense_4096": dense,
         "configs": sections,

@@ -140,8 +140,6 @@ __device__ __forceinline__ void gather2d(T *dst, int rows, int cols, int pitch, 
     }
 }
 
-// N0f8 codes as Float32 (c/255 correctly rounded), one table per CTA.
-__shared__ float s_n0f8[256];
 
 // ---------------------------------------------------------------- staging
 // A tile's input window (rows x cols elements from image position (ox, oy))
@@ -240,9 +238,10 @@ __device__ __forceinline__ void bt_gather_raw(const BReq &R, const TileGeo &g, u
 }
 
 // Value of staged element (r, c) in the compute domain (the element type is a
-// compile-time parameter of the tile routines; 8-bit codes go through the
-// CTA's code -> value table).
-__shared__ float s_u8f[256];                           // UInt8 code c as Float32
+// compile-time parameter of the tile routines).  8-bit codes convert in
+// arithmetic -- N0f8 c/255 correctly rounded, UInt8 c -- rather than through
+// a shared table, whose lookups by 32 lanes at random codes conflict on the
+// banks; row pairs convert on the packed FP32x2 pipe.
 
 template <class Tin> struct Rows;
 template <> struct Rows<float> {
@@ -258,11 +257,25 @@ template <> struct Rows<float> {
 template <> struct Rows<uint8_t> {
     const unsigned char *st;
     const unsigned char *lead;
-    const float *lut;
-    __device__ __forceinline__ Rows(const unsigned char *s, const unsigned char *l, const float *t)
-        : st(s), lead(l), lut(t) {}
+    bool norm;                        // N0f8 (c/255) or UInt8 (c)
+    __device__ __forceinline__ Rows(const unsigned char *s, const unsigned char *l, bool n)
+        : st(s), lead(l), norm(n) {}
     __device__ __forceinline__ const uint8_t *row(int r) const { return st + r * kStagePitch + lead[r]; }
-    __device__ __forceinline__ float val(const uint8_t *p, int c) const { return lut[p[c]]; }
+    __device__ __forceinline__ float val(const uint8_t *p, int c) const
+    {
+        return norm ? n0f8_to_f32(p[c]) : u8_to_f32(p[c]);
+    }
+    // elements c of two rows, as a pair
+    __device__ __forceinline__ float2 val2(const uint8_t *p0, const uint8_t *p1, int c) const
+    {
+        const float2 f = __fadd2_rn(make_float2(__uint_as_float(0x4B000000u | p0[c]),
+                                                __uint_as_float(0x4B000000u | p1[c])),
+                                    make_float2(-8388608.0f, -8388608.0f));      // (2^23 + c) - 2^23
+        if (!norm) return f;
+        const float2 r = make_float2(1.0f / 255.0f, 1.0f / 255.0f);
+        const float2 q = __fmul2_rn(f, r);                                        // as n0f8_to_f32, per lane
+        return __ffma2_rn(__ffma2_rn(q, make_float2(-255.0f, -255.0f), f), r, q);
+    }
 };
 
 // Output rows of a tile: element (x, y) of `out`; `full` tiles skip the bounds tests.
@@ -349,8 +362,8 @@ __device__ __forceinline__ void corr_fn2(F at, const float2 *w, int k, float2 *a
 
 // Factored tiles: the x pass over all rows of the window (the y halo) into
 // the intermediate I, then the y pass down each column of I.  8-bit images
-// run the x pass on row pairs on the packed FP32x2 pipe (each value is two
-// shared loads, code and table, either way); Float32 images run it one row
+// run the x pass on row pairs on the packed FP32x2 pipe (codes convert two at
+// a time there too); Float32 images run it one row
 // per item (row pairs read rows 8 words apart, which share banks in this
 // layout, and measured slower).  A window with an odd row count pairs its
 // last row with itself (the copy lands in intermediate row `rows`, which is
@@ -370,7 +383,7 @@ __device__ void bt_factored(const BReq &R, int tx0, int ty0, const Rows<Tin> &S,
             for (int it = tid; it < pairs * (BW / NB); it += nth) {
                 const int r = 2 * (it >> 3), c0 = (it & 7) * NB;
                 const auto *p0 = S.row(r) + cb + c0, *p1 = S.row(r + 1 < rows ? r + 1 : r) + cb + c0;
-                corr_fn2<NB>([&](int j) { return make_float2(S.val(p0, j), S.val(p1, j)); }, R.wx, kx, acc);
+                corr_fn2<NB>([&](int j) { return S.val2(p0, p1, j); }, R.wx, kx, acc);
                 float4 *d0 = reinterpret_cast<float4 *>(I + r * kIPitch + c0);
                 float4 *d1 = reinterpret_cast<float4 *>(I + (r + 1) * kIPitch + c0);
 #pragma unroll
@@ -690,8 +703,6 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
     const unsigned first_tries = g_first_wait_batch;
     float *I = reinterpret_cast<float *>(smem + NB * kStageBytes);
     for (int i = tid; i < ntab; i += blockDim.x) s_base[i] = (int)reqs[i].tile_base;
-    s_n0f8[tid & 255] = __fdiv_rn((float)(tid & 255), 255.0f);
-    s_u8f[tid & 255] = (float)(tid & 255);
     __shared__ int s_bulk[NB];           // buffer b's window arrives by bulk copies
     long long ahead = 0;                 // thread 0: the next tile to hand out (already fetched)
     if (tid == 0) {
@@ -786,7 +797,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
                     if (o64) bt_dispatch<float, double>(R, tx0, ty0, S, I);
                     else bt_dispatch<float, float>(R, tx0, ty0, S, I);
                 } else {
-                    const Rows<uint8_t> S(st, s_lead[b], R.in_type == IFX_N0F8 ? s_n0f8 : s_u8f);
+                    const Rows<uint8_t> S(st, s_lead[b], R.in_type == IFX_N0F8);
                     if (o64) bt_dispatch<uint8_t, double>(R, tx0, ty0, S, I);
                     else bt_dispatch<uint8_t, float>(R, tx0, ty0, S, I);
                 }
