@@ -52,8 +52,10 @@ def parse():
                    help="no autotuning in the warm-up waves (default tiles everywhere)")
     p.add_argument("--dense-ksizes", type=lambda t: [int(v) for v in t.split(",")], default=None,
                    help="dense section: kernel sizes to run (default 5,11,15,31)")
-    p.add_argument("--only", default=None, choices=[None, "dense", "sections", "next"],
+    p.add_argument("--only", default=None, choices=[None, "dense", "sections", "next", "batchgroup"],
                    help="run only one secondary section (small device footprint, for profiling)")
+    p.add_argument("--group", default="laplacian/N0F8",
+                   help="--only batchgroup: OP/KIND of the first timed wave's requests to run as one plan")
     return p.parse_args()
 
 
@@ -418,6 +420,43 @@ def run_stream(args, ifx, torch, rank):
             "host_ms_per_step": {k: v * 1e3 / max(len(timed_p), 1) for k, v in host_s.items()},
             "per_op": per_op, "batch_kernel": bk, "clocks": clocks, "reqs": timed,
             "tuned_batch_tiles": tuned_tiles}
+
+
+def run_batch_group(args, ifx, torch, hbm_peak):
+    """One request group (--group OP/KIND) of the first timed wave as its own
+    batch plan, with inputs for that group only (a small device footprint for
+    profiling k_batch on one tile routine): 3 warm-up launches, then 5 timed
+    launches (CUDA events, L2 flushed before each)."""
+    import ctypes as C
+    from imagefiltering_gb300 import synthetic as S, batch as B
+    op, kind = args.group.split("/")
+    per = args.per_step
+    reqs = [r for r in S.stream_requests(per * (args.warmup + 1), seed=5)[per * args.warmup:]
+            if r.op == op and r.kind == kind]
+    dev = torch.device("cuda")
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5)
+    ins = [torch.rand((r.w, r.h), device=dev, generator=gen) if r.kind == "F32" else
+           torch.randint(0, 256, (r.w, r.h), device=dev, dtype=torch.uint8, generator=gen) for r in reqs]
+    arena = torch.empty(sum(r.out_bytes() + 256 * len(r.out_kinds()) for r in reqs) + 4096, dtype=torch.uint8,
+                        device=dev)
+    bt, _ = batch_for_wave(ifx, reqs, ins, arena)
+    plan = B.Plan(bt)
+    A = ifx._abi
+    ctx = A.context()
+    stream = ifx.arrays.torch_stream()
+    tiles = C.c_int64()
+    launch = lambda: A.check(ctx.lib.ifx_batch_plan_launch(plan.handle, C.byref(tiles), stream))
+    for _ in range(3):
+        launch()
+    torch.cuda.synchronize()
+    ms = _time(torch, launch, reps=5)
+    by = sum(alg_bytes(r) for r in reqs)
+    out = {"group": args.group, "requests": len(reqs), "tiles": tiles.value, "ms": ms,
+           "mpix": sum(r.pixels for r in reqs) / 1e6, "alg_bytes": by, "hbm_frac": by / (ms / 1e3) / 1e9 / hbm_peak,
+           "mixed_floor_ms": mixed_floor_ms(reqs, hbm_peak, 2070.0)}
+    plan.close()
+    return out
 
 
 def run_stream_e2e(args, ifx, torch, reqs_all):
@@ -1075,6 +1114,9 @@ def main():
         return 0
     if args.only == "next":
         print(json.dumps({"next_rows": run_next_rows(args, ifx, torch, peaks()[0])}))
+        return 0
+    if args.only == "batchgroup":
+        print(json.dumps({"batch_group": run_batch_group(args, ifx, torch, peaks()[0])}))
         return 0
     res = run_stream(args, ifx, torch, rank)
     value, dev_ms, _ = job_throughput(res["dev_ms"], res["pixels"], dist if ws > 1 else None, "cuda")

@@ -490,7 +490,7 @@ static int run_cascade(Call &c, const ifx_array_t &imgd, const void *img, const 
             const bool fused_cached = fused && autotune_lookup3(a, &ch) && ch.variant == 2;
             void *vol = nullptr;
             if (split && !fused_cached) {
-                rc = slot_get(c.ctx, tmp_slot_base, (size_t)n[0] * n[1] * n[2] * sizeof(float), &vol);
+                rc = slot_get(c.ctx, tmp_slot_base, sep3d_split_tmp_bytes(a), &vol);
                 if (rc) return rc;
             }
             IFX_CUDA(launch_sep3d_tuned(a, static_cast<float *>(vol), c.s, !c.host));

@@ -463,8 +463,8 @@ cudaError_t set_first_wait_tma(bool force_timeout)
 template <class Tin, class Tout, int WSH>
 __global__ void __launch_bounds__(256)
 k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img, Tout *__restrict__ out,
-            int nx, int ny, int fx, int kx, int fy, int ky, int x_first, int style, float fill, bool norm,
-            int shift, int ty, int tiles_x, int tiles_per_slice, int tiles, int pair_store, int *err,
+            int nx, int ny, int inx, int iny, int fx, int kx, int fy, int ky, int x_first, int style, float fill,
+            bool norm, int shift, int ty, int tiles_x, int tiles_per_slice, int tiles, int pair_store, int *err,
             const __grid_constant__ Sep2dW<float> W)
 {
     constexpr int NB = kStNB, NBY = kStNBY, wsh = WSH;
@@ -511,9 +511,11 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
     auto interior = [&](int t) {
         int px, py, sl;
         origin(t, px, py, sl);
-        return px >= 0 && px + CV <= nx && py >= 0 && py + RV <= ny;
+        return px >= 0 && px + CV <= inx && py >= 0 && py + RV <= iny;
     };
-    const long long plane = (long long)nx * ny;
+    // input planes are inx x iny (the output's nx x ny, or a padded copy of
+    // the input whose windows all lie inside)
+    const long long plane_in = (long long)inx * iny, plane_out = (long long)nx * ny;
     // all threads call it (uniform); thread 0 issues the copy of tile t into
     // buffer b.  The buffer's previous readers finished before the block
     // barrier that ended the previous tile (after a proxy fence).
@@ -557,8 +559,8 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
         prefetch(t + gridDim.x, b ^ 1);
         int px, py, sl;
         origin(t, px, py, sl);
-        const Tin *img_s = img + sl * plane;
-        Tout *out_s = out + sl * plane;
+        const Tin *img_s = img + sl * plane_in;
+        Tout *out_s = out + sl * plane_out;
         // a border tile's source maps (see below), while its copy is in flight;
         // the barrier after the wait publishes them
         const bool border = !interior(t);
@@ -566,7 +568,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             for (int i = tid; i < RV + CV; i += nth) {
                 const bool row = i < RV;
                 const int w = row ? RV : CV, o = row ? py : px, j = row ? i : i - RV;
-                const int m = map_index(o + j, row ? ny : nx, style);
+                const int m = map_index(o + j, row ? iny : inx, style);
                 const int code = m < 0 ? kSrcFill : (m - o >= 0 && m - o < w ? m - o : -2 - m);
                 (row ? src_row : src_col)[j] = code;
             }
@@ -611,8 +613,8 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
             // The border map runs once per window row and column, into
             // src_row / src_col: >= 0 the source's row (column) in the tile,
             // kSrcFill the fill value, <= -2 the image row (column) -2 - code.
-            const int top = min(max(-py, 0), RV), bot = min(max(RV - (ny - py), 0), RV - top);
-            const int lft = min(max(-px, 0), CV), rgt = min(max(CV - (nx - px), 0), CV - lft);
+            const int top = min(max(-py, 0), RV), bot = min(max(RV - (iny - py), 0), RV - top);
+            const int lft = min(max(-px, 0), CV), rgt = min(max(CV - (inx - px), 0), CV - lft);
             if (sizeof(Tin) == 1) __syncthreads();        // the converted tile is complete
             const int ncin = CV - lft - rgt;
             for (int rr = tid >> 5; rr < top + bot; rr += nth >> 5) {
@@ -620,7 +622,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                 for (int c = lft + (tid & 31); c < lft + ncin; c += 32)
                     P[r * SP + c] = code >= 0          ? P[code * SP + c]
                                     : code == kSrcFill ? fill
-                                                       : cvt<float, Tin>(img_s[(long long)(-2 - code) * nx + px + c], norm);
+                                                       : cvt<float, Tin>(img_s[(long long)(-2 - code) * inx + px + c], norm);
             }
             __syncthreads();
             // outside columns: 16 threads per row, rows in steps of nth / 16
@@ -634,7 +636,7 @@ k_sep2d_tma(const __grid_constant__ CUtensorMap map, const Tin *__restrict__ img
                     } else if (code != kSrcFill) {
                         const int rc = src_row[r];
                         const int my = rc >= 0 ? py + rc : -2 - rc;
-                        if (rc != kSrcFill) v = cvt<float, Tin>(img_s[(long long)my * nx + (-2 - code)], norm);
+                        if (rc != kSrcFill) v = cvt<float, Tin>(img_s[(long long)my * inx + (-2 - code)], norm);
                     }
                     P[r * SP + c] = v;
                 }
@@ -765,9 +767,10 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     if (!sep_tma_tile<Tin>(a, &TX, &ty, &L)) return false;
     const int RV = ty + a.ky - 1;
     const int nsl = a.nsl > 1 ? a.nsl : 1;
+    const int inx = a.in_nx > 0 ? a.in_nx : a.nx, iny = a.in_ny > 0 ? a.in_ny : a.ny;
     CUtensorMap map;
-    const long long pitch = (long long)a.nx * (long long)sizeof(Tin);
-    if (!tma_encode_3d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, nsl, pitch, pitch * a.ny, L.boxw, RV))
+    const long long pitch = (long long)inx * (long long)sizeof(Tin);
+    if (!tma_encode_3d(&map, a.img, (int)sizeof(Tin), inx, iny, nsl, pitch, pitch * iny, L.boxw, RV))
         return false;
     int dev = 0;
     if ((*e = cudaGetDevice(&dev)) != cudaSuccess) return true;
@@ -805,7 +808,7 @@ static bool sep2d_tma_t(const Sep2dArgs &a, cudaStream_t s, cudaError_t *e)
     // 8- or 16-byte word when rows and the tile grid keep them aligned
     const int pair_store = (a.nx % 2 == 0) && (shift % 2 == 0) &&
                            ((uintptr_t)a.out % (2 * sizeof(Tout)) == 0);
-    kern<<<grid, nthreads, L.total, s>>>(map, (const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, a.fx, a.kx, a.fy,
+    kern<<<grid, nthreads, L.total, s>>>(map, (const Tin *)a.img, (Tout *)a.out, a.nx, a.ny, inx, iny, a.fx, a.kx, a.fy,
                                     a.ky, a.x_first, a.style, (float)a.fill, a.in_type == IFX_N0F8, shift, ty,
                                     tiles_x, (int)per_slice, (int)tiles, pair_store, err, W);
     note_launch();
@@ -823,10 +826,11 @@ template <class Tin> static bool sep2d_tma_fits(const Sep2dArgs &a)
     const int RV = ty + a.ky - 1;
     const int nsl = a.nsl > 1 ? a.nsl : 1;
     const long long tiles = (long long)((a.nx + 16 + TX - 1) / TX) * ((a.ny + ty - 1) / ty) * nsl;
+    const int inx = a.in_nx > 0 ? a.in_nx : a.nx, iny = a.in_ny > 0 ? a.in_ny : a.ny;
     CUtensorMap map;
-    const long long pitch = (long long)a.nx * (long long)sizeof(Tin);
+    const long long pitch = (long long)inx * (long long)sizeof(Tin);
     return tiles <= (1ll << 30) &&
-           tma_encode_3d(&map, a.img, (int)sizeof(Tin), a.nx, a.ny, nsl, pitch, pitch * a.ny, L.boxw, RV);
+           tma_encode_3d(&map, a.img, (int)sizeof(Tin), inx, iny, nsl, pitch, pitch * iny, L.boxw, RV);
 }
 
 bool sep2d_tma_applies(const Sep2dArgs &a)
@@ -874,7 +878,8 @@ cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s)
     if (a.nx == 0 || a.ny == 0) return cudaSuccess;
     cudaError_t e = cudaSuccess;
     if (launch_sep2d_tma(a, s, &e)) return e;
-    if (a.nsl > 1) return cudaErrorInvalidValue;     // stacks of planes: TMA tile kernel only
+    // stacks of planes and padded inputs: TMA tile kernel only
+    if (a.nsl > 1 || (a.in_nx > 0 && a.in_nx != a.nx) || (a.in_ny > 0 && a.in_ny != a.ny)) return cudaErrorInvalidValue;
     const int it = a.in_type, ot = a.out_type;
     if (!a.compute_f64) {
         if (it == IFX_F32 && ot == IFX_F32) return sep2d_t<float, float, float>(a, s);
@@ -1066,22 +1071,54 @@ cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s, int zdepth)
 // factor first, from the image into an FP32 volume, then the x and y factors
 // of every z plane by the TMA tile kernel over the stack of planes, into the
 // output.  Pad-then-cascade filters one fixed padded array, so the order of
-// the factors only moves FP32 rounding; a Fill border becomes, for the x/y
-// sweep, the z-filtered fill value fill * sum(wz).  Traffic: the image once,
-// the FP32 volume twice, the output once.
+// the factors only moves FP32 rounding.  The FP32 volume is the z-filtered
+// PADDED array: its planes carry the x/y border (lx columns left, ly rows on
+// top, and what the x/y windows reach past the far edges, the width rounded
+// up to a multiple of 4), each halo cell the z filter of the column the
+// border maps it to (Fill: of fill values).  The x/y sweep then reads every
+// window inside a plane -- no border work in its tiles -- with window starts
+// on 16-byte boundaries (lx makes fx + lx a multiple of 4).  Traffic: the
+// image once, the padded FP32 volume twice, the output once.
 //
-// k_zpass: a thread computes kZNB consecutive z outputs of two adjacent x
-// (FP32x2 pairs), a warp 64 consecutive x of one row, a CTA 8 rows; the z
-// window goes through the border map (one map per plane, warp-uniform).
+// k_zpass: a thread computes kZNB consecutive z outputs of two adjacent
+// padded x (FP32x2 pairs), a warp 64 consecutive x of one row, a CTA 8 rows;
+// the z window goes through the border map (one map per plane,
+// warp-uniform), x and y through the border map once per thread.
 // =========================================================================
 constexpr int kZNB = 8, kZMax = 17;      // outputs per thread, longest z factor
 
 struct ZpassW { float wz[kZMax]; };
 
+// Geometry of the padded FP32 volume of the split path.
+struct SplitGeo {
+    int lx, ly;                           // left / top border columns and rows
+    int nxp, nyp;                         // padded plane
+    int fxp, fyp;                         // x / y window offsets in padded coordinates (>= 0)
+};
+
+static SplitGeo split_geo(const Sep3dArgs &a)
+{
+    SplitGeo g;
+    g.lx = a.fx < 0 ? -a.fx : 0;
+    g.lx += ((-(a.fx + g.lx)) % 4 + 4) % 4;              // fx + lx a multiple of 4
+    g.fxp = a.fx + g.lx;
+    g.nxp = (a.nx + g.fxp + a.kx - 1 + 3) & ~3;
+    g.ly = a.fy < 0 ? -a.fy : 0;
+    g.fyp = a.fy + g.ly;
+    g.nyp = a.ny + g.fyp + a.ky - 1;
+    return g;
+}
+
+size_t sep3d_split_tmp_bytes(const Sep3dArgs &a)
+{
+    const SplitGeo g = split_geo(a);
+    return (size_t)g.nxp * g.nyp * a.nz * a.nvol * sizeof(float);
+}
+
 template <class Tin, bool PAIR>
 __global__ void __launch_bounds__(256)
 k_zpass(const Tin *__restrict__ img, float *__restrict__ out, int nx, int ny, int nz, int zblocks, int fz, int kz,
-        int style, float fill, bool norm, const __grid_constant__ ZpassW W)
+        int style, float fill, bool norm, int lx, int ly, int nxp, int nyp, const __grid_constant__ ZpassW W)
 {
     constexpr int NB = kZNB;
     __shared__ float2 w2[kZMax];
@@ -1089,24 +1126,30 @@ k_zpass(const Tin *__restrict__ img, float *__restrict__ out, int nx, int ny, in
     for (int t = tid; t < kz; t += blockDim.x) w2[t] = make_float2(W.wz[t], W.wz[t]);
     __syncthreads();
     const int lane = tid & 31, warp = tid >> 5;
-    const int x = 2 * (blockIdx.x * 32 + lane), y = blockIdx.y * 8 + warp;
+    const int xp = 2 * (blockIdx.x * 32 + lane), yp = blockIdx.y * 8 + warp;
     const int zb = blockIdx.z % zblocks, vol = blockIdx.z / zblocks, z0 = zb * NB;
-    if (x >= nx || y >= ny) return;
+    if (xp >= nxp || yp >= nyp) return;
+    // the source columns of padded (xp, yp) and (xp + 1, yp); negative: fill
+    const int my = map_index(yp - ly, ny, style);
+    const int mx0 = map_index(xp - lx, nx, style), mx1 = map_index(xp + 1 - lx, nx, style);
+    const bool in0 = my >= 0 && mx0 >= 0, in1 = my >= 0 && mx1 >= 0;
+    // one 8-byte load for both when they are adjacent and the pair is aligned
+    const bool pair = PAIR && in0 && in1 && mx1 == mx0 + 1 && (mx0 & 1) == 0;
     const long long plane = (long long)nx * ny;
-    const long long base = (long long)vol * plane * nz + (long long)y * nx + x;
-    const bool two = x + 1 < nx;
+    const long long base = (long long)vol * plane * nz + (long long)(in0 || in1 ? my : 0) * nx;
     auto at = [&](int j) -> float2 {
         const int ms = map_index(z0 + fz + j, nz, style);
         if (ms < 0) return make_float2(fill, fill);
         const Tin *p = img + base + (long long)ms * plane;
         if constexpr (PAIR && sizeof(Tin) == 4) {
-            return *reinterpret_cast<const float2 *>(p);
+            if (pair) return *reinterpret_cast<const float2 *>(p + mx0);
         } else if constexpr (PAIR) {
-            const uchar2 u = *reinterpret_cast<const uchar2 *>(p);
-            return make_float2(cvt<float, Tin>(u.x, norm), cvt<float, Tin>(u.y, norm));
-        } else {
-            return make_float2(cvt<float, Tin>(p[0], norm), two ? cvt<float, Tin>(p[1], norm) : 0.0f);
+            if (pair) {
+                const uchar2 u = *reinterpret_cast<const uchar2 *>(p + mx0);
+                return make_float2(cvt<float, Tin>(u.x, norm), cvt<float, Tin>(u.y, norm));
+            }
         }
+        return make_float2(in0 ? cvt<float, Tin>(p[mx0], norm) : fill, in1 ? cvt<float, Tin>(p[mx1], norm) : fill);
     };
     // the whole window is loaded before any arithmetic: every load of the
     // thread is in flight at once (the sweep is bound by their latency)
@@ -1123,16 +1166,12 @@ k_zpass(const Tin *__restrict__ img, float *__restrict__ out, int nx, int ny, in
 #pragma unroll
         for (int i = 0; i < NB; ++i) acc[i] = __ffma2_rn(w, v[i + t], acc[i]);
     }
-    float *o = out + base + (long long)z0 * plane;
+    const long long pplane = (long long)nxp * nyp;
+    float *o = out + (long long)vol * pplane * nz + (long long)z0 * pplane + (long long)yp * nxp + xp;
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
         if (z0 + i >= nz) break;
-        if constexpr (PAIR) {
-            *reinterpret_cast<float2 *>(o + i * plane) = acc[i];
-        } else {
-            o[i * plane] = acc[i].x;
-            if (two) o[i * plane + 1] = acc[i].y;
-        }
+        *reinterpret_cast<float2 *>(o + i * pplane) = acc[i];
     }
 }
 
@@ -1142,24 +1181,28 @@ static cudaError_t zpass_t(const Sep3dArgs &a, float *tmp, cudaStream_t s)
     ZpassW W;
     memset(&W, 0, sizeof W);
     for (int t = 0; t < a.kz; ++t) W.wz[t] = (float)a.wz[t];
+    const SplitGeo g = split_geo(a);
     const int zblocks = (a.nz + kZNB - 1) / kZNB;
-    dim3 grid((a.nx + 63) / 64, (a.ny + 7) / 8, zblocks * a.nvol);
+    dim3 grid((g.nxp + 63) / 64, (g.nyp + 7) / 8, zblocks * a.nvol);
     const bool pair = a.nx % 2 == 0 && (uintptr_t)a.img % (2 * sizeof(Tin)) == 0;
     if (pair)
         k_zpass<Tin, true><<<grid, 256, 0, s>>>((const Tin *)a.img, tmp, a.nx, a.ny, a.nz, zblocks, a.fz, a.kz,
-                                                a.style, (float)a.fill, a.in_type == IFX_N0F8, W);
+                                                a.style, (float)a.fill, a.in_type == IFX_N0F8, g.lx, g.ly, g.nxp,
+                                                g.nyp, W);
     else
         k_zpass<Tin, false><<<grid, 256, 0, s>>>((const Tin *)a.img, tmp, a.nx, a.ny, a.nz, zblocks, a.fz,
-                                                 a.kz, a.style, (float)a.fill, a.in_type == IFX_N0F8, W);
+                                                 a.kz, a.style, (float)a.fill, a.in_type == IFX_N0F8, g.lx, g.ly,
+                                                 g.nxp, g.nyp, W);
     note_launch();
     return cudaGetLastError();
 }
 
-// The x/y sweep of the split path over the FP32 volume at `tmp`.
+// The x/y sweep of the split path over the padded FP32 volume at `tmp`:
+// every window needed lies inside its plane, so the border style of the sweep
+// only touches cells that feed no output (Fill(0)).
 static Sep2dArgs sep3d_xy_args(const Sep3dArgs &a, const float *tmp)
 {
-    double wsum = 0.0;
-    for (int t = 0; t < a.kz; ++t) wsum += a.wz[t];
+    const SplitGeo g = split_geo(a);
     Sep2dArgs b{};
     b.img = tmp;
     b.in_type = IFX_F32;
@@ -1167,15 +1210,17 @@ static Sep2dArgs sep3d_xy_args(const Sep3dArgs &a, const float *tmp)
     b.out_type = a.out_type;
     b.nx = a.nx;
     b.ny = a.ny;
-    b.fx = a.fx;
+    b.in_nx = g.nxp;
+    b.in_ny = g.nyp;
+    b.fx = g.fxp;
     b.kx = a.kx;
-    b.fy = a.fy;
+    b.fy = g.fyp;
     b.ky = a.ky;
     b.wx = a.wx;
     b.wy = a.wy;
     b.x_first = 1;
-    b.style = a.style;
-    b.fill = a.fill * wsum;
+    b.style = IFX_FILL;
+    b.fill = 0.0;
     b.compute_f64 = 0;
     b.variant = 1;
     b.nsl = a.nz * a.nvol;
@@ -1185,9 +1230,10 @@ static Sep2dArgs sep3d_xy_args(const Sep3dArgs &a, const float *tmp)
 bool sep3d_split_applies(const Sep3dArgs &a)
 {
     if (!(a.in_type == IFX_F32 || is8(a.in_type)) || !(a.out_type == IFX_F32 || a.out_type == IFX_F64)) return false;
-    if (a.kz > kZMax || a.kx > kCorrKmax || a.ky > kCorrKmax || a.nx % 4 != 0) return false;
-    if ((long long)a.nx * a.ny * a.nz * a.nvol >= (1ll << 40)) return false;
-    if ((long long)((a.nz + kZNB - 1) / kZNB) * a.nvol > 65535 || (a.ny + 7) / 8 > 65535) return false;
+    if (a.kz > kZMax || a.kx > kCorrKmax || a.ky > kCorrKmax) return false;
+    const SplitGeo g = split_geo(a);
+    if ((long long)g.nxp * g.nyp * a.nz * a.nvol >= (1ll << 40)) return false;
+    if ((long long)((a.nz + kZNB - 1) / kZNB) * a.nvol > 65535 || (g.nyp + 7) / 8 > 65535) return false;
     // the FP32 volume of cudaMalloc is 256-byte aligned: probe the x/y sweep with such a base
     Sep2dArgs b = sep3d_xy_args(a, reinterpret_cast<const float *>(uintptr_t(256)));
     return sep2d_tma_applies(b);

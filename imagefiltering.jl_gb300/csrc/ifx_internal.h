@@ -65,6 +65,8 @@ struct Sep2dArgs {
                                            // (0 or 1: one; more: TMA tile kernel only)
     int tile_w, tile_h;                    // output tile (0: the kernel's default); shapes a kernel
                                            // cannot take fall back to its default
+    int in_nx, in_ny;                      // input planes (0: nx x ny); larger: a padded input whose
+                                           // windows (offsets fx, fy) lie inside (TMA tile kernel only)
 };
 cudaError_t launch_sep2d(const Sep2dArgs &a, cudaStream_t s);
 bool sep2d_tma_applies(const Sep2dArgs &a);
@@ -86,10 +88,11 @@ bool sep3d_supported(int kx, int ky, int kz, int nx, int ny, int nz, int nvol);
 // zdepth: output slices per z chunk of the fused kernel (0: default; the z
 // halo of kz - 1 input slices is filtered once per chunk)
 cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s, int zdepth = 0);
-// the split 3-D path (z sweep into an FP32 volume of nx*ny*nz*nvol floats at
-// tmp, then the x/y TMA sweep over its planes, in tiles of tw x th when
-// given); applies needs no device memory
+// the split 3-D path (z sweep into a padded FP32 volume of
+// sep3d_split_tmp_bytes at tmp, then the x/y TMA sweep over its planes, in
+// tiles of tw x th when given); applies needs no device memory
 bool sep3d_split_applies(const Sep3dArgs &a);
+size_t sep3d_split_tmp_bytes(const Sep3dArgs &a);       // the split path's padded FP32 volume
 cudaError_t launch_sep3d_split(const Sep3dArgs &a, float *tmp, cudaStream_t s, int tw = 0, int th = 0);
 
 // The autotuner (ifx_tune.cu) -------------------------------------------------

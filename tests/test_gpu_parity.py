@@ -209,11 +209,12 @@ def test_separable_3d_volume(gpu_ifx, oracle):
 @pytest.mark.parametrize("kind", ["F32", "N0F8", "U8"])
 @pytest.mark.parametrize("style", STYLES)
 def test_separable_3d_split(gpu_ifx, oracle, kind, style):
-    """3-D cascades with one factor per axis: volumes whose rows meet the
-    bulk-copy rules take the z sweep into an FP32 volume and the x/y TMA
-    sweep over its planes (Fill becomes the z-filtered fill value there);
-    others (width 37) the fused z-marching kernel.  Random lengths and
-    offsets, Float64 and Float32 outputs."""
+    """3-D cascades with one factor per axis take the z sweep into a padded
+    FP32 volume (its halo cells the z filter of the columns the border maps
+    them to; Fill: of fill values) and the x/y TMA sweep over its planes,
+    for any width (37 included: the padded rows meet the bulk-copy rules).
+    Random lengths and offsets (positive ones too), Float64 and Float32
+    outputs."""
     ifx = gpu_ifx
     rng = np.random.default_rng(zlib.crc32(("3dsplit" + kind + style).encode()))
     for shape in [(16, 9, 13), (64, 33, 40), (37, 20, 11)]:
