@@ -108,6 +108,18 @@ inline bool bt_tile_ok(int op, int in_type, int kx, int ky, int tw, int th)
 __device__ __forceinline__ int ct_id() { return (int)threadIdx.x - 32; }
 __device__ __forceinline__ int ct_n() { return (int)blockDim.x - 32; }
 __device__ __forceinline__ void ct_sync() { asm volatile("bar.sync 1, %0;" ::"r"(ct_n()) : "memory"); }
+// Named barrier 1 with an AND over the consumers' predicates: every consumer
+// gets the same answer (a per-thread result, such as a bounded wait that one
+// thread gave up on, would otherwise split the consumers at the next barrier
+// inside a tile routine).
+__device__ __forceinline__ bool ct_all(bool v)
+{
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, 1, %2, p;\n\t"
+                 "selp.u32 %0, 1, 0, q;\n\t}\n"
+                 : "=r"(r) : "r"((uint32_t)v), "r"(ct_n()) : "memory");
+    return r != 0;
+}
 
 // Division-free 2-D gather of a tile whose element (r, c) is load(r, c): warps
 // take rows, lanes take columns; each thread issues up to 2 rows x 4 column
@@ -785,7 +797,7 @@ k_batch(const unsigned char *__restrict__ desc, unsigned long long *counter, int
             const int tx0 = bx * R.tw, ty0 = by * R.th;
             unsigned char *st = smem + b * kStageBytes;
             if (s_bulk[b]) {
-                ok = mbar_wait_bounded(&s_bar[b], (parity >> b) & 1u, first_tries);
+                ok = ct_all(mbar_wait_bounded(&s_bar[b], (parity >> b) & 1u, first_tries));
             } else {
                 bt_gather_raw(R, bt_geo(R, tx0, ty0), st, s_lead[b]);
                 ct_sync();
