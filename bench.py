@@ -2,17 +2,21 @@
 """Benchmark of the GB300 FIR / rank-filter path.  Prints ONE JSON line.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload stream|dense4096|volume256x8|rank2048|gauss512]
+                    [--only dense|sections|next|batchgroup]
 
-Default workload ("stream"): the mixed serving stream -- 2-D images with one
+The workload: the mixed serving stream -- 2-D images with one
 side log-uniform in 64..4096 (aspect 1:4..4:1), Float32 or N0f8, op drawn from
 {Gaussian σ~U[0.5,8], Sobel gradient, Laplacian 3x3, median 3x3/5x5}, border
 drawn from the Pad styles (seed 5).  A step is one wave of `--per-step`
 requests of that stream, in stream order; K steps cover K*per_step requests.
 
   value  Mpixel/s (output pixels of all requests / device time), inputs
-         resident in HBM, through the batched engine when built, else one
-         C-ABI call per request ("plain").
+         resident in HBM, through the batched engine (one persistent launch
+         per wave); `plain_gpu` is the same stream as one C-ABI call per
+         request.
+The line also carries the other configurations (`configs`: 512^2 and 4096^2
+separable, the 256^3 x 8 volume, the 2048^2 rank filters; `dense_4096`) and
+the CPU baselines; `--only` runs one of those sections alone.
   e2e    the same metric through the public API with pinned HOST buffers:
          host->device copies of each request's image and device->host copies
          of its outputs inside the timed region.
@@ -40,8 +44,6 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="stream",
-                   choices=["stream", "dense4096", "volume256x8", "rank2048", "gauss512"])
     p.add_argument("--per-step", type=int, default=500)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
