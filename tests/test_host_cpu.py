@@ -253,3 +253,58 @@ def test_median3x3_sorted_column_identity():
     for _ in range(3000):
         v = list(rng.integers(0, 9, 9))
         assert fast([v[0:3], v[3:6], v[6:9]]) == sorted(v)[4]
+
+
+def test_tuner_cache_and_pins_without_a_gpu(lib, ifx, tmp_path):
+    """The tuner's host side: a cache file of 't2' lines loads into choices the
+    lookup returns (other lines are skipped), pins replace them and validate
+    their fields, the batched engine's keys normalise their taps, and clear
+    forgets everything -- none of it touches the device."""
+    import ctypes as C
+    A = ifx._abi
+    cache = tmp_path / "tune.txt"
+    # key: path in out kx ky kz fill sizeclass f64 | variant x_first tile_w tile_h depth ms
+    cache.write_text("an old line that is not a choice\n"
+                     "t2 0 0 1 9 9 0 0 24 0 1 1 128 48 0 0.041\n"
+                     "t2 1 0 1 13 13 9 0 24 0 2 1 0 0 64 0.800\n"
+                     "t2 2 2 1 17 17 0 1 0 0 0 0 128 48 0 0.090\n")
+    taps2, size2 = (C.c_int32 * 3)(9, 9, 1), (C.c_int64 * 3)(4096, 4096, 1)      # 2^24 pixels
+    taps3, size3 = (C.c_int32 * 3)(13, 13, 9), (C.c_int64 * 3)(256, 256, 256)
+    ch = A.IfxTuneChoice()
+    try:
+        assert lib.ifx_autotune(None, 0, str(cache).encode()) == 0
+        assert lib.ifx_autotune_lookup(None, A.TUNE_SEP2D, 0, 1, taps2, 0, size2, C.byref(ch)) == 0
+        assert (ch.variant, ch.x_first, ch.tile_w, ch.tile_h) == (1, 1, 128, 48) and abs(ch.ms - 0.041) < 1e-6
+        assert lib.ifx_autotune_lookup(None, A.TUNE_SEP3D, 0, 1, taps3, 0, size3, C.byref(ch)) == 0
+        assert (ch.variant, ch.depth) == (2, 64)
+        xf, var, ms = C.c_int32(), C.c_int32(), C.c_double()
+        assert lib.ifx_autotune_choice(None, 0, 1, 9, 9, 0, 4096, 4096, C.byref(xf), C.byref(var), C.byref(ms)) == 0
+        assert (xf.value, var.value) == (1, 1)
+        # the batched engine's key: factored N0f8 -> Float64, 17 x 17 taps (the file's op field is 1)
+        assert lib.ifx_batch_autotune_lookup(None, 1, 2, 1, 17, 17, 5, C.byref(ch)) == 0      # window ignored
+        assert (ch.tile_w, ch.tile_h) == (128, 48)
+        # another size class is another key
+        size_small = (C.c_int64 * 3)(512, 512, 1)
+        assert lib.ifx_autotune_lookup(None, A.TUNE_SEP2D, 0, 1, taps2, 0, size_small, C.byref(ch)) == 1
+        # pins: validated, then returned by the lookup; gradients' taps are always 3 x 3
+        bad = A.IfxTuneChoice(3, 1, 0, 0, 0, 0.0)
+        assert lib.ifx_autotune_pin(None, A.TUNE_SEP2D, 0, 1, taps2, 0, size_small, C.byref(bad)) == 1
+        assert "variant" in lib.ifx_last_error().decode()
+        good = A.IfxTuneChoice(2, 0, 64, 32, 0, 0.0)
+        assert lib.ifx_autotune_pin(None, A.TUNE_SEP2D, 0, 1, taps2, 0, size_small, C.byref(good)) == 0
+        assert lib.ifx_autotune_lookup(None, A.TUNE_SEP2D, 0, 1, taps2, 0, size_small, C.byref(ch)) == 0
+        assert (ch.variant, ch.x_first, ch.tile_w, ch.tile_h) == (2, 0, 64, 32)
+        assert lib.ifx_autotune_pin(None, 7, 0, 1, taps2, 0, size_small, C.byref(good)) == 1
+        gpin = A.IfxTuneChoice(0, 0, 176, 56, 0, 0.0)
+        assert lib.ifx_batch_autotune_pin(None, 2, 2, 1, 1, 1, 0, C.byref(gpin)) == 0
+        assert lib.ifx_batch_autotune_lookup(None, 2, 2, 1, 3, 3, 0, C.byref(ch)) == 0
+        assert (ch.tile_w, ch.tile_h) == (176, 56)
+        assert lib.ifx_batch_autotune_lookup(None, 9, 2, 1, 3, 3, 0, C.byref(ch)) == 1      # unknown op
+        # pins are not written to the file; clear forgets cached and pinned choices
+        assert len(cache.read_text().splitlines()) == 4
+        assert lib.ifx_autotune_clear(None) == 0
+        assert lib.ifx_autotune_lookup(None, A.TUNE_SEP2D, 0, 1, taps2, 0, size2, C.byref(ch)) == 1
+        assert lib.ifx_batch_autotune_lookup(None, 2, 2, 1, 3, 3, 0, C.byref(ch)) == 1
+    finally:
+        lib.ifx_autotune(None, 0, None)
+        lib.ifx_autotune_clear(None)
