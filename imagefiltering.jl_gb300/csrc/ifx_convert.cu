@@ -9,7 +9,8 @@
 // checked for every code); to Float64: integers rounded to nearest (exact
 // below 2^53), codes divided correctly rounded.  To an integer type: the
 // value must be an integer inside the type's range, as Julia's convert
-// demands (InexactError); offending elements set *bad and are written as 0.
+// demands (InexactError; N0f8/N0f16 values are integers at 0 and 1 only);
+// offending elements set *bad and are written as 0.
 #include "ifx_internal.h"
 
 namespace ifx {
@@ -78,7 +79,11 @@ __global__ void k_convert(const void *__restrict__ src, int st, void *__restrict
             ok = fabs(x) < 9.2233720368547758e18 && trunc(x) == x;
             v = ok ? (long long)x : 0;
         } else {
-            ok = false;                               // N0f8 / N0f16 codes as integers: not a conversion Julia does
+            // N0f8 / N0f16: the value c/255 (c/65535) is an integer only at 0 and 1
+            const uint32_t c = st == IFX_N0F8 ? ((const uint8_t *)src)[i] : ((const uint16_t *)src)[i];
+            const uint32_t one = st == IFX_N0F8 ? 255u : 65535u;
+            ok = c == 0 || c == one;
+            v = c == one ? 1 : 0;
         }
         long long lo, hi;
         switch (dt) {

@@ -17,7 +17,7 @@ module ImageFilteringGB300
 using ImageFiltering, ComputationalResources, OffsetArrays, Statistics
 using ImageFiltering: ProcessedKernel, ReshapedOneD, Pad, Fill, NoPad, Inner, NA, BorderSpecAny, iscopy
 using ImageFiltering.Algorithm: Alg
-using ImageCore: N0f8, Gray, Normed
+using ImageCore: N0f8, N0f16, Gray, Normed
 
 export GB300
 
@@ -58,6 +58,15 @@ eltcode(::Type{<:Union{N0f8,Gray{N0f8}}}) = Int32(2)
 eltcode(::Type{UInt8}) = Int32(3)
 eltcode(::Type{Int16}) = Int32(4)
 eltcode(::Type{Gray{T}}) where {T<:Union{Float32,Float64}} = eltcode(T)
+eltcode(::Type{Int8}) = Int32(5)
+eltcode(::Type{UInt16}) = Int32(6)
+eltcode(::Type{Int32}) = Int32(7)
+eltcode(::Type{Int64}) = Int32(8)
+eltcode(::Type{<:Union{N0f16,Gray{N0f16}}}) = Int32(9)
+
+# Eltypes the filters read directly; the others (Int8 .. Int64, UInt16,
+# Gray{N0f16}) go through ifx_convert (filter_converted! below).
+native(::Type{T}) where {T} = T <: Union{Float32,Float64,N0f8,Gray{N0f8},UInt8,Gray{Float32},Gray{Float64}}
 
 npre(::ReshapedOneD{T,N,Npre}) where {T,N,Npre} = Npre     # the axis a factor filters (0-based)
 
@@ -100,11 +109,39 @@ function check(rc)
     error(msg)
 end
 
+# ---------------------------------------------------------------- eltypes
+"`out .= convert.(eltype(out), img)` on the GPU (ifx_convert), with Julia's InexactError."
+function ifxconvert!(out::AbstractArray, img::AbstractArray)
+    GC.@preserve out img begin
+        rc = ccall((:ifx_convert, libifx), Cint, (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Ptr{Cvoid}),
+                   context(), Ref(ifxarray(out)), Ref(ifxarray(img)), C_NULL)
+        if rc == 1 && occursin("InexactError", unsafe_string(ccall((:ifx_last_error, libifx), Cstring, ())))
+            throw(InexactError(:convert, eltype(out), img))
+        end
+        check(rc)
+    end
+    out
+end
+
+# An image of an eltype the filters do not read: converted on the GPU to the
+# compute type (the output's float type, Float64 for integer outputs) and
+# filtered; integer results (accumfilter's promotion, src/utils.jl:124-129)
+# convert back, raising InexactError as Julia's convert does.  A Fill value
+# is first converted to the image's eltype (src/borderarray.jl:11-20).
+function filter_converted!(r, out::AbstractArray{S,N}, img::AbstractArray{T,N}, kernel, border) where {S,T,N}
+    Tc = S <: AbstractFloat ? S : Float64
+    imgc = ifxconvert!(similar(img, Tc), img)
+    b = border isa Fill ? Fill(Tc(convert(T, border.value)), border.lo, border.hi) : border
+    S <: AbstractFloat && return imfilter!(r, out, imgc, kernel, b)
+    ifxconvert!(out, imfilter!(r, similar(out, Float64), imgc, kernel, b))
+end
+
 # ---------------------------------------------------------------- imfilter!
 # Separable kernels: a tuple of ReshapedOneD (KernelFactors.*) -> ifx_imfilter_factored
 function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
                                   kernel::Tuple{ReshapedOneD,Vararg{ReshapedOneD}},
                                   border::Union{Pad,Fill}) where {S,T,N}
+    native(T) || return filter_converted!(r, out, img, kernel, border)
     ws = [collect(Float64, parent(k.data)) for k in kernel]
     facs = [IfxFactor(Int32(npre(k)), Int32(length(k.data)),
                       Int64(first(axes(k.data, 1))), pointer(w)) for (k, w) in zip(kernel, ws)]
@@ -122,6 +159,7 @@ end
 function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
                                   kernel::Tuple{AbstractArray,Vararg{AbstractArray}},
                                   border::Union{Pad,Fill}) where {S,T,N}
+    native(T) || return filter_converted!(r, out, img, kernel, border)
     ks = filter(k -> !iscopy(k), collect(kernel))
     length(ks) == 1 || throw(ArgumentError("GB300: one dense kernel per call"))
     K = ImageFiltering.samedims(out, ks[1])
@@ -142,6 +180,7 @@ end
 function ImageFiltering.imfilter!(r::CPU1{GB300}, out::AbstractArray{S,N}, img::AbstractArray{T,N},
                                   kernel::Tuple{ImageFiltering.Kernel.Laplacian},
                                   border::Union{Pad,Fill}) where {S,T,N}
+    native(T) || return filter_converted!(r, out, img, kernel, border)
     flags = pad4(map(Int32, kernel[1].flags), 0)
     GC.@preserve out img begin
         check(ccall((:ifx_imfilter_laplacian, libifx), Cint,
@@ -266,8 +305,15 @@ end
 
 # ---------------------------------------------------------------- mapwindow
 # mapwindow has no Alg hook; the entry points take the resource first.
-function ImageFiltering.mapwindow(::CPU1{GB300}, ::Union{typeof(median!),typeof(median)}, img::AbstractArray{T,N},
+function ImageFiltering.mapwindow(r::CPU1{GB300}, f::Union{typeof(median!),typeof(median)}, img::AbstractArray{T,N},
                                   window::Dims{N}; border="replicate") where {T,N}
+    # other eltypes: the median of the values converted to middle's eltype
+    # (an order-preserving conversion), through ifx_convert
+    if !native(T)
+        M = typeof(Statistics.middle(first(img)))
+        b = border isa Fill ? Fill(M(convert(T, border.value)), border.lo, border.hi) : border
+        return mapwindow(r, f, ifxconvert!(similar(img, M), img), window; border=b)
+    end
     wf = pad4(map(w -> -(w >> 1), window), 0)
     wl = pad4(window, 1)
     out = similar(img, typeof(Statistics.middle(first(img))))

@@ -323,12 +323,13 @@ int ifx_maxabs(ifx_context_t *ctx, const ifx_array_t *img, double *result, void 
  * out .= convert.(eltype(out), img) (the eltype conversions around the
  * reference's imfilter!: its padded copy in the filter type,
  * src/border.jl:324-331, and the store of each result, src/imfilter.jl:
- * 660-666).  Any pair of the eltypes above, same axes.  To Float32/Float64: the
- * value (N0f8 c/255 and N0f16 c/65535 correctly rounded; integers exactly, or
+ * 660-666), same axes.  To Float32/Float64 from any eltype above: the value
+ * (N0f8 c/255 and N0f16 c/65535 correctly rounded; integers exactly, or
  * rounded to nearest for Float32 beyond 2^24).  To an integer type: every
- * value must be an integer in the type's range, else IFX_ERR_ARGUMENT
- * (Julia's InexactError); such calls are synchronous (the check is read
- * back).  To N0f8/N0f16: the value must be a code/255 (code/65535) exactly. */
+ * value must be an integer in the type's range (N0f8/N0f16 values are at 0
+ * and 1 only), else IFX_ERR_ARGUMENT (Julia's InexactError); such calls are
+ * synchronous (the check is read back).  To N0f8/N0f16: from the same eltype
+ * only (a copy); other conversions to them return IFX_ERR_UNSUPPORTED. */
 int ifx_convert(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img, void *stream);
 
 /* ---- NA() borders ---------------------------------------------------------

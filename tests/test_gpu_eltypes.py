@@ -52,6 +52,15 @@ def test_convert_to_integer_and_inexact(gpu_ifx):
         ifx.convert_(out, np.asfortranarray(np.array([[1.5, 0.0], [0.0, 0.0]])))
     with pytest.raises(ifx.InexactError):
         ifx.convert_(out, np.asfortranarray(np.array([[128.0, 0.0], [0.0, 0.0]])))
+    # N0f8 / N0f16 values are integers at 0 and 1 only (convert(Int, N0f8(1)) == 1)
+    for codes, src in [(np.array([[0, 255], [255, 0]], np.uint8), ifx.n0f8),
+                       (np.array([[65535, 0], [0, 65535]], np.uint16), ifx.n0f16)]:
+        ifx.convert_(out, src(np.asfortranarray(codes)))
+        assert np.array_equal(out, (codes > 0).astype(np.int8))
+        bad = codes.copy()
+        bad[0, 0] = 128
+        with pytest.raises(ifx.InexactError):
+            ifx.convert_(out, src(np.asfortranarray(bad)))
 
 
 @pytest.mark.parametrize("dt", [np.int8, np.int16, np.uint16, np.int32, np.int64])
