@@ -458,7 +458,12 @@ static int run_cascade(Call &c, const ifx_array_t &imgd, const void *img, const 
         Fac fx{0, 0, 1, &one}, fy{1, 0, 1, &one};
         int x_first = 1;
         for (size_t i = 0; i < facs.size(); ++i) (facs[i].axis == 0 ? fx : fy) = facs[i];
-        if (facs.size() == 2) x_first = facs[0].axis == 0;
+        // Two factors: pad-then-cascade commutes (only FP32 rounding moves), and
+        // the FP32 kernels run the x pass first whatever the factor order -- their
+        // last pass then stores down columns, coalesced (the y pass first measured
+        // 2-2.5x slower in the TMA kernel: its last pass stores along rows, a
+        // row per lane).  FP64 keeps the kernel order; the autotuner may choose.
+        if (facs.size() == 2) x_first = ct == IFX_F64 ? facs[0].axis == 0 : 1;
         else x_first = facs[0].axis == 0 ? 1 : 0;
         if (fx.len > IFX_MAX_TAPS || fy.len > IFX_MAX_TAPS ||
             sep2d_smem_bytes(fx.len, fy.len, x_first, ct == IFX_F64) > 200 * 1024)

@@ -89,9 +89,10 @@ def test_separable_2d_tma_tiles(gpu_ifx, oracle, kind, style):
     that the persistent kernel copies every tile by TMA and gives the window
     cells outside the image their border values in shared memory (from the
     tile, or from the image where the window does not hold the source):
-    random factor lengths/offsets, both pass orders, Float32 and Float64
-    outputs, images smaller than one tile, several tiles per CTA on the
-    largest image."""
+    random factor lengths/offsets, both factor orders (the FP32 kernels run
+    the x pass first either way; the y-first pass order is pinned in
+    test_gpu_tune.py), Float32 and Float64 outputs, images smaller than one
+    tile, several tiles per CTA on the largest image."""
     ifx = gpu_ifx
     rng = np.random.default_rng(zlib.crc32(("tma" + kind + style).encode()))
     for shape in [(32, 7), (48, 70), (256, 200), (1040, 333), (4096, 1100)]:
@@ -117,7 +118,7 @@ def test_separable_2d_tma_tiles(gpu_ifx, oracle, kind, style):
 @pytest.mark.parametrize("kind", ["F32", "N0F8"])
 def test_separable_2d_tma_tile_heights(gpu_ifx, oracle, kind):
     """Long factors lower the TMA kernel's tile height below 64 rows (to 56,
-    48, 40: not all multiples of 16); both pass orders, every tile row of the
+    48, 40: not all multiples of 16); both factor orders, every tile row of the
     image, including a partial last one."""
     ifx = gpu_ifx
     rng = np.random.default_rng(zlib.crc32(("tma-heights" + kind).encode()))
