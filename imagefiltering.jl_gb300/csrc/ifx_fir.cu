@@ -1081,9 +1081,10 @@ cudaError_t launch_sep3d(const Sep3dArgs &a, cudaStream_t s, int zdepth)
 // image once, the padded FP32 volume twice, the output once.
 //
 // k_zpass: a thread computes kZNB consecutive z outputs of two adjacent
-// padded x (FP32x2 pairs), a warp 64 consecutive x of one row, a CTA 8 rows;
-// the z window goes through the border map (one map per plane,
-// warp-uniform), x and y through the border map once per thread.
+// padded x (FP32x2 pairs); threads take the padded plane's pairs in linear
+// order (rows back to back: no partial blocks at the row ends); the z window
+// goes through the border map (one map per plane, uniform), x and y through
+// the border map once per thread.
 // =========================================================================
 constexpr int kZNB = 8, kZMax = 17;      // outputs per thread, longest z factor
 
@@ -1125,10 +1126,10 @@ k_zpass(const Tin *__restrict__ img, float *__restrict__ out, int nx, int ny, in
     const int tid = threadIdx.x;
     for (int t = tid; t < kz; t += blockDim.x) w2[t] = make_float2(W.wz[t], W.wz[t]);
     __syncthreads();
-    const int lane = tid & 31, warp = tid >> 5;
-    const int xp = 2 * (blockIdx.x * 32 + lane), yp = blockIdx.y * 8 + warp;
-    const int zb = blockIdx.z % zblocks, vol = blockIdx.z / zblocks, z0 = zb * NB;
-    if (xp >= nxp || yp >= nyp) return;
+    const long long lin = 2ll * ((long long)blockIdx.x * blockDim.x + tid);     // nxp is even
+    if (lin >= (long long)nxp * nyp) return;
+    const int yp = (int)(lin / nxp), xp = (int)(lin - (long long)yp * nxp);
+    const int zb = blockIdx.y % zblocks, vol = blockIdx.y / zblocks, z0 = zb * NB;
     // the source columns of padded (xp, yp) and (xp + 1, yp); negative: fill
     const int my = map_index(yp - ly, ny, style);
     const int mx0 = map_index(xp - lx, nx, style), mx1 = map_index(xp + 1 - lx, nx, style);
@@ -1183,7 +1184,7 @@ static cudaError_t zpass_t(const Sep3dArgs &a, float *tmp, cudaStream_t s)
     for (int t = 0; t < a.kz; ++t) W.wz[t] = (float)a.wz[t];
     const SplitGeo g = split_geo(a);
     const int zblocks = (a.nz + kZNB - 1) / kZNB;
-    dim3 grid((g.nxp + 63) / 64, (g.nyp + 7) / 8, zblocks * a.nvol);
+    dim3 grid((unsigned)(((long long)g.nxp * g.nyp / 2 + 255) / 256), zblocks * a.nvol);
     const bool pair = a.nx % 2 == 0 && (uintptr_t)a.img % (2 * sizeof(Tin)) == 0;
     if (pair)
         k_zpass<Tin, true><<<grid, 256, 0, s>>>((const Tin *)a.img, tmp, a.nx, a.ny, a.nz, zblocks, a.fz, a.kz,
@@ -1233,7 +1234,8 @@ bool sep3d_split_applies(const Sep3dArgs &a)
     if (a.kz > kZMax || a.kx > kCorrKmax || a.ky > kCorrKmax) return false;
     const SplitGeo g = split_geo(a);
     if ((long long)g.nxp * g.nyp * a.nz * a.nvol >= (1ll << 40)) return false;
-    if ((long long)((a.nz + kZNB - 1) / kZNB) * a.nvol > 65535 || (g.nyp + 7) / 8 > 65535) return false;
+    if ((long long)((a.nz + kZNB - 1) / kZNB) * a.nvol > 65535 || (long long)g.nxp * g.nyp / 2 / 256 >= (1ll << 31))
+        return false;
     // the FP32 volume of cudaMalloc is 256-byte aligned: probe the x/y sweep with such a base
     Sep2dArgs b = sep3d_xy_args(a, reinterpret_cast<const float *>(uintptr_t(256)));
     return sep2d_tma_applies(b);
