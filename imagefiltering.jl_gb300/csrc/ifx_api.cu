@@ -835,6 +835,23 @@ int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *
     if (numel(*img) == 0) return IFX_OK;
     if ((rc = check_reflect(border, *img))) return rc;
     const bool tc_ok = nd <= 2 && dense_tc_supported(img->eltype, (int)ksize[0], nd > 1 ? (int)ksize[1] : 1);
+    // The automatic method takes the tensor cores only for sign-definite
+    // kernels (smoothing kernels: every weight >= 0, or every weight <= 0).
+    // Their BF16 hi/lo products carry errors of about 2^-17 of each term; with
+    // weights of one sign these average out, while kernels of mixed signs whose
+    // sum nearly cancels reached 1.2e-5 normwise at 31 x 31 (two of twelve
+    // N(0,1) kernels normalised to sum 1), above the 1e-5 bound: those take the
+    // CUDA cores (reference precision) unless the tensor cores are asked for.
+    bool sign_definite = true;
+    if (method == 0 && tc_ok) {
+        bool pos = false, neg = false;
+        for (long long i = 0; i < kn; ++i) {
+            pos |= kernel[i] > 0.0;
+            neg |= kernel[i] < 0.0;
+        }
+        sign_definite = !(pos && neg);
+    }
+    const bool tc_auto = tc_ok && sign_definite;
     if (method == 2 && !tc_ok)
         return fail(IFX_ERR_UNSUPPORTED, "the tensor-core path takes 2-D Float32/8-bit images and "
                     "kernels up to 33 wide and 40 tall");
@@ -848,7 +865,7 @@ int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *
     // automatic: the FFT when it is estimated well below the direct kernels
     // and every element is finite (the reference's filter_algorithm,
     // src/imfilter.jl:1200-1206, also falls back to FIR for non-finite images)
-    if (method == 0 && !border->explicit_pad && (kn > kMaxDenseTaps || fft_cheaper(*img, *out, ksize, tc_ok)) &&
+    if (method == 0 && !border->explicit_pad && (kn > kMaxDenseTaps || fft_cheaper(*img, *out, ksize, tc_auto)) &&
         fft_available()) {
         FftArgs f;
         int lo[IFX_MAXD], sz[IFX_MAXD];
@@ -876,9 +893,9 @@ int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *
     if ((rc = image_fill(border, img->eltype, ct, &fill))) return rc;
     int n[IFX_MAXD];
     for (int d = 0; d < IFX_MAXD; ++d) n[d] = d < nd ? (int)img->size[d] : 1;
-    // automatic: tensor cores for 2-D kernels of 11 x 11 and larger (faster than the
-    // CUDA-core kernel there, within the 1e-5 normwise bound)
-    const bool use_tc = method == 2 || (method == 0 && tc_ok && ksize[0] >= 11 && nd > 1 && ksize[1] >= 11);
+    // automatic: tensor cores for sign-definite 2-D kernels of 11 x 11 and larger
+    // (faster than the CUDA-core kernel there)
+    const bool use_tc = method == 2 || (method == 0 && tc_auto && ksize[0] >= 11 && nd > 1 && ksize[1] >= 11);
     if (use_tc) {
         Dense2dArgs a{din, img->eltype, dout, out->eltype, n[0], nd > 1 ? n[1] : 1,
                       (int)kfirst[0], (int)ksize[0], nd > 1 ? (int)kfirst[1] : 0,

@@ -564,9 +564,15 @@ def test_dense_tensor_cores(gpu_ifx, oracle, ksz, seed, style):
     ref = oracle.imfilter_dense(img.astype(np.float64), K, kern.first, style, 0.0)
     assert got.dtype == np.float64
     assert normwise(got, ref) <= 1e-5
-    # the automatic method takes the tensor cores from 11 x 11 up: the same kernel
+    # the automatic method: these kernels have weights of both signs, so the
+    # CUDA-core kernel (reference precision); a sign-definite kernel of the
+    # same size takes the tensor cores
     auto = ifx.imfilter(img, kern, b, ifx.Algorithm.GB300())
-    assert np.array_equal(auto, got)
+    assert np.array_equal(auto, ifx.imfilter(img, kern, b, ifx.Algorithm.GB300("cuda_cores")))
+    Kp = np.abs(K) / np.abs(K).sum()
+    kp = ifx.centered(Kp)
+    assert np.array_equal(ifx.imfilter(img, kp, b, ifx.Algorithm.GB300()),
+                          ifx.imfilter(img, kp, b, ifx.Algorithm.GB300("tensor_cores")))
 
 
 def test_dense_tensor_cores_shapes(gpu_ifx, oracle):
@@ -974,3 +980,39 @@ def test_fft_full_size_against_direct(gpu_ifx):
         ifx.imfilter_(b, img, ker, "reflect", ifx.Algorithm.GB300("cuda_cores"))
         d = (a.tensor.double() - b.tensor.double()).abs().max() / b.tensor.double().abs().max()
         assert float(d) <= tol, (kind, float(d))
+
+
+def test_dense_tensor_cores_31x31_twelve_seeds(gpu_ifx, oracle):
+    """The tensor-core error at 31 x 31 over twelve kernel seeds, normwise,
+    max_abs and max_rel against the FP64 oracle.  Kernels of both signs
+    (N(0,1) normalised to sum 1, |sum| >= 0.1) stay within 1.5e-5 on the
+    tensor cores -- above 1e-5 for some seeds, so the automatic method gives
+    them the CUDA cores, within 1e-5 for every seed; sign-definite kernels
+    (|N(0,1)| normalised) stay within 1e-5 on the tensor cores, which the
+    automatic method takes for them."""
+    ifx = gpu_ifx
+    img = np.asfortranarray(np.random.default_rng(3).random((320, 288), dtype=np.float32))
+
+    def err(got, ref):
+        d = np.abs(np.asarray(got, np.float64) - ref)
+        big = np.abs(ref) >= 1e-3 * np.max(np.abs(ref))
+        return normwise(got, ref), float(d.max()), float(np.max(d[big] / np.abs(ref[big])))
+
+    mixed, definite = [], []
+    for seed in range(100, 112):
+        rng = np.random.default_rng(seed)
+        while True:
+            K = rng.standard_normal((31, 31))
+            if abs(K.sum()) >= 0.1:
+                break
+        for kind, Kk, out in (("mixed", K / K.sum(), mixed), ("definite", np.abs(K) / np.abs(K).sum(), definite)):
+            kern = ifx.centered(Kk)
+            ref = oracle.imfilter_dense(img.astype(np.float64), Kk, kern.first, "reflect", 0.0)
+            tc = err(ifx.imfilter(img, kern, "reflect", ifx.Algorithm.GB300("tensor_cores")), ref)
+            auto = err(ifx.imfilter(img, kern, "reflect", ifx.Algorithm.GB300()), ref)
+            out.append((seed, tc, auto))
+            print("seed %d %s: tensor cores normwise %.3g max_abs %.3g max_rel %.3g; automatic normwise %.3g"
+                  % (seed, kind, tc[0], tc[1], tc[2], auto[0]))
+    assert max(t[0] for _, t, _ in mixed) <= 1.5e-5
+    assert max(a[0] for _, _, a in mixed + definite) <= 1e-5
+    assert max(t[0] for _, t, _ in definite) <= 1e-5
