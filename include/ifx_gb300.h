@@ -139,15 +139,17 @@ int ifx_imfilter_factored(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_
  * imfilter! with a single dense (non-separable) kernel, the `(dummy, K)` case
  * after factorkernel (src/imfilter.jl:1159-1184) -> __imfilter_inbounds!
  * (src/imfilter.jl:624-669).  K is column-major with sizes ksize and first
- * indices kfirst (host memory).  method: 0 = automatic (tensor cores for 2-D
- * kernels of 11 x 11 and larger that they take, CUDA cores otherwise, and the
+ * indices kfirst (host memory).  method: 0 = automatic (tensor cores for
+ * sign-definite 2-D kernels -- every weight >= 0, or every weight <= 0 -- of
+ * 11 x 11 and larger that they take, CUDA cores otherwise, and the
  * FFT path of ifx_imfilter_fft when its estimated time is under half the
  * direct one -- large kernels, Float64 images -- or the kernel has more than
  * 3600 taps, provided every image element is finite; that check reads one
  * flag back, so the call waits for its stream then),
  * 1 = FP32/FP64 CUDA cores, 2 = tcgen05 tensor cores (BF16 hi/lo split, three
  * products, FP32 accumulation; 2-D Float32 and 8-bit images, kernels up to
- * 33 wide and 40 tall). */
+ * 33 wide and 40 tall; up to about 1.5e-5 normwise for kernels of mixed
+ * signs whose sum nearly cancels, which the automatic method keeps off them). */
 int ifx_imfilter_dense(ifx_context_t *ctx, ifx_array_t *out, const ifx_array_t *img,
                        const double *kernel, const int64_t *ksize, const int64_t *kfirst,
                        const ifx_border_t *border, int32_t method, void *stream);
