@@ -464,9 +464,11 @@ def run_batch_group(args, ifx, torch, hbm_peak):
 def run_stream_e2e(args, ifx, torch, reqs_all):
     """Through the serving loop with pinned HOST buffers: every request's image
     is copied host->device and its outputs device->host inside the timed
-    region.  Throughput: all requests submitted at once.  Latency: Poisson
-    arrivals at half the measured throughput, p50/p99 of submit -> outputs in
-    host memory."""
+    region.  Throughput: all requests submitted at once, nine passes, the
+    median is the value; after each pass the same uploads and downloads run
+    alone on the link (`link`), which gives the link's floor and its own spread
+    in the same minute.  Latency: Poisson arrivals at half the measured
+    throughput, p50/p99 of submit -> outputs in host memory."""
     from imagefiltering_gb300.serve import Server
     reqs = reqs_all[: min(len(reqs_all), args.e2e_requests)]
     A = ifx._abi
@@ -489,6 +491,7 @@ def run_stream_e2e(args, ifx, torch, reqs_all):
     in_np = in_arena.numpy()
     out_np = out_arena.numpy()
     items = []
+    up, dn = [], []                         # (offset, bytes) of every upload and download
     io = oo = 0
     from imagefiltering_gb300 import batch as B
     for r in reqs:
@@ -497,12 +500,14 @@ def run_stream_e2e(args, ifx, torch, reqs_all):
             img = in_np[io:io + nb].view(np.float32).reshape((r.h, r.w), order="F")
         else:
             img = ifx.n0f8(in_np[io:io + nb].reshape((r.h, r.w), order="F"))
+        up.append((io, nb))
         io += sz(nb)
         outs = []
         for k in r.out_kinds():
             ob = r.pixels * (8 if k == "F64" else 4)
             outs.append(out_np[oo:oo + ob].view(np.float64 if k == "F64" else np.float32)
                         .reshape((r.h, r.w), order="F"))
+            dn.append((oo, ob))
             oo += sz(ob)
         bt = B.Batch()
         q = bt.add(BATCH_OP[r.op](r), img, outs, r.style)
@@ -519,8 +524,11 @@ def run_stream_e2e(args, ifx, torch, reqs_all):
             srv.submit_struct(q)
         srv.drain()
         px = sum(r.pixels for r in reqs)
-        runs = []
-        for _ in range(5):                  # five timed passes: the median one is the value
+        link_in = torch.empty(in_total, dtype=torch.uint8, device="cuda")
+        link_out = torch.empty(out_total, dtype=torch.uint8, device="cuda")
+        link_streams = (torch.cuda.Stream(), torch.cuda.Stream())
+        runs, link_ms = [], []
+        for _ in range(9):                  # nine timed passes: the median one is the value
             srv.reset_metrics()
             t0 = time.perf_counter()
             for r, q, bt in items:
@@ -528,10 +536,23 @@ def run_stream_e2e(args, ifx, torch, reqs_all):
             srv.drain()
             wall = time.perf_counter() - t0
             runs.append((px / wall / 1e6, wall, srv.metrics()))
+            link_ms.append(link_pass(torch, in_arena, out_arena, link_in, link_out, link_streams, up, dn) * 1e3)
+        del link_in, link_out
+        torch.cuda.empty_cache()
         value, wall, m = sorted(runs, key=lambda x: x[0])[len(runs) // 2]
         res["value"] = value
         res["runs"] = [round(v, 1) for v, _, _ in runs]
         res["spread"] = (max(v for v, _, _ in runs) - min(v for v, _, _ in runs)) / value
+        served_ms = sorted(w * 1e3 for _, w, _ in runs)
+        link_sorted = sorted(link_ms)
+        res["link"] = {"ms": [round(t, 1) for t in link_ms], "median_ms": link_sorted[len(link_ms) // 2],
+                       "min_ms": link_sorted[0],
+                       "gbs_median": (h2d + d2h) / (link_sorted[len(link_ms) // 2] / 1e3) / 1e9,
+                       "served_median_ms": served_ms[len(runs) // 2],
+                       "served_over_link": served_ms[len(runs) // 2] / link_sorted[len(link_ms) // 2],
+                       "mode": "the same uploads and downloads (same bytes, same chunks, two streams) with no "
+                               "server and no kernel, timed after each served pass: the link's floor for the "
+                               "served stream and the link's own pass-to-pass spread"}
         res["pixels"] = px
         res["throughput_p50_ms"] = m["p50_latency_s"] * 1e3
         res["throughput_p99_ms"] = m["p99_latency_s"] * 1e3
@@ -557,10 +578,7 @@ def run_stream_e2e(args, ifx, torch, reqs_all):
                 "d2h_bytes_per_step": int(d2h * args.per_step / n), "requests": n,
                 "mode": "served: ifx_server (continuous batching, HBM cap %d GB, batches of up to %d "
                         "requests, %d in flight) with pinned host buffers" % (args.hbm_cap_gb, max_batch,
-                                                                             max_inflight),
-                "link_bound": {"d2h_gbs_measured": 193.5, "h2d_gbs_measured": 211.3, "both_gbs_measured": 343.1,
-                               "d2h_only_ms_per_1000": round(d2h / 193.5e9 * 1e3, 1),
-                               "note": "the device->host copies of the outputs alone bound the served stream"}})
+                                                                             max_inflight)})
     # plain per-request blocking calls with the same host buffers, for comparison
     plain = reqs[: min(n, 200)]
     t0 = time.perf_counter()
@@ -571,6 +589,26 @@ def run_stream_e2e(args, ifx, torch, reqs_all):
                              "requests": len(plain),
                              "mode": "one blocking C-ABI call per request with host buffers"}
     return res
+
+
+def link_pass(torch, in_arena, out_arena, dev_in, dev_out, streams, up, dn):
+    """The host link alone: the uploads `up` and downloads `dn` ((offset, bytes)
+    into the pinned arenas and the device buffers of their sizes) issued in turn
+    on the two `streams`.  Returns the wall time in seconds."""
+    s_up, s_dn = streams
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(max(len(up), len(dn))):
+        if i < len(up):
+            o, nb = up[i]
+            with torch.cuda.stream(s_up):
+                dev_in[o:o + nb].copy_(in_arena[o:o + nb], non_blocking=True)
+        if i < len(dn):
+            o, nb = dn[i]
+            with torch.cuda.stream(s_dn):
+                out_arena[o:o + nb].copy_(dev_out[o:o + nb], non_blocking=True)
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0
 
 
 def call_single(ifx, r, q):

@@ -13,9 +13,9 @@
 //      that batch's requests only; after an idle period the first batches
 //      are smaller (1/8, 1/4, 1/2 of max_batch), so that results start
 //      flowing back over the link early;
-//   3. when a batch finishes, copies host outputs back on a download stream
-//      (the link's two directions overlap) and releases the request's device
-//      memory after those copies;
+//   3. queues, with each batch, the copies of its host outputs on a download
+//      stream behind the batch's kernel (the link's two directions overlap)
+//      and the release of its requests' device memory after those copies;
 //   4. records submit -> done latency of every request.
 // Requests admitted while other batches run overlap with them on the device:
 // uploads of batch k+1 run on the copy stream during batch k.
@@ -56,7 +56,6 @@ struct SReq {
 struct SBatch {
     std::vector<std::shared_ptr<SReq>> reqs;
     cudaEvent_t compute_done = nullptr, copy_done = nullptr;
-    bool copies_enqueued = false;
 };
 
 } // namespace ifx
@@ -111,27 +110,30 @@ static bool dev_ptr(const void *p)
 
 static int nouts(const ifx_request_t &q) { return q.op == IFX_OP_GRADIENTS2D ? 2 : 1; }
 
-// Called with srv->mu held: move finished batches to done, free memory.
+// Queues a launched batch's downloads and releases on the download stream,
+// behind the batch's kernel (srv->mu held).  They are queued when the batch is
+// launched, so the copies start as soon as the kernel ends, whatever the
+// engine thread is doing then.
+static void enqueue_downloads(ifx_server *S, SBatch &b)
+{
+    cudaStreamWaitEvent(S->down, b.compute_done, 0);
+    for (auto &r : b.reqs)
+        for (int o = 0; o < nouts(r->q) && r->status == IFX_OK; ++o)
+            if (r->host_out[o])
+                cudaMemcpyAsync(r->q.out[o].data, r->d_out[o], r->out_bytes[o], cudaMemcpyDeviceToHost, S->down);
+    for (auto &r : b.reqs) {
+        if (r->host_in && r->d_in) cudaFreeAsync(r->d_in, S->down);
+        for (int o = 0; o < 2; ++o)
+            if (r->host_out[o] && r->d_out[o]) cudaFreeAsync(r->d_out[o], S->down);
+    }
+    cudaEventRecord(b.copy_done, S->down);
+}
+
+// Called with srv->mu held: move batches whose downloads have finished to done.
 static void finish_batches(ifx_server *S)
 {
     while (!S->inflight.empty()) {
         SBatch &b = S->inflight.front();
-        if (!b.copies_enqueued) {
-            if (cudaEventQuery(b.compute_done) == cudaErrorNotReady) return;
-            cudaStreamWaitEvent(S->down, b.compute_done, 0);
-            for (auto &r : b.reqs)
-                for (int o = 0; o < nouts(r->q) && r->status == IFX_OK; ++o)
-                    if (r->host_out[o])
-                        cudaMemcpyAsync(r->q.out[o].data, r->d_out[o], r->out_bytes[o],
-                                        cudaMemcpyDeviceToHost, S->down);
-            for (auto &r : b.reqs) {
-                if (r->host_in && r->d_in) cudaFreeAsync(r->d_in, S->down);
-                for (int o = 0; o < 2; ++o)
-                    if (r->host_out[o] && r->d_out[o]) cudaFreeAsync(r->d_out[o], S->down);
-            }
-            cudaEventRecord(b.copy_done, S->down);
-            b.copies_enqueued = true;
-        }
         if (cudaEventQuery(b.copy_done) == cudaErrorNotReady) return;
         const auto now = Clock::now();
         for (auto &r : b.reqs) {
@@ -300,6 +302,7 @@ static void launch(ifx_server *S)
         for (auto &r : b.reqs) r->status = IFX_ERR_CUDA;
     }
     cudaEventRecord(b.compute_done, S->compute);
+    enqueue_downloads(S, b);
     ++S->batches;
     S->inflight.push_back(std::move(b));
 }
