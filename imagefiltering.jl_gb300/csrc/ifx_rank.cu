@@ -678,8 +678,12 @@ static bool extrema_vhgw_u8(const ExtremaPassArgs &a, cudaStream_t s, cudaError_
 // Gil-Werman on runs of W outputs (one segment: suffix extrema of the run's
 // W inputs, prefix extrema of the next W-1, one combine per output) with two
 // rows in the 16-bit lanes of a word; the y pass does the same down column
-// pairs.  A Fill value joins the outputs whose window leaves the image along
-// the pass's axis.  Outputs: interleaved (min, max) codes, or one of them.
+// pairs.  The x pass writes its results by row pairs (a 32-bit word holds two
+// rows of two columns), so that its stores and the y pass's loads move four
+// bytes each: byte-wise stores and 16-bit loads made the shared-memory queue
+// the kernel's first stall.  A Fill value joins the outputs whose window
+// leaves the image along the pass's axis.  Outputs: interleaved (min, max)
+// codes, or one of them.
 // =========================================================================
 template <int W> struct ExTile {
     // runs per row: a multiple of 4, so that the tile width is (the y pass
@@ -713,15 +717,54 @@ __device__ __forceinline__ void vhgw_run(const uint32_t (&v)[2 * W - 1], uint32_
     }
 }
 
+// Stores W x-pass results of a row pair (row 2p in byte 0, row 2p + 1 in byte
+// 2 of each word) at columns c0 .. c0 + W - 1 of the pair layout: two columns
+// per 32-bit store on even columns, the odd one out (the last column for an
+// even c0, the first for an odd one) as 16 bits.  Neighbouring lanes hold
+// runs of both parities, so the words of both cases are formed and selected
+// rather than branched on (`odd`: c0 is odd).
 template <int W>
-__global__ void __launch_bounds__(256, W <= 9 ? 5 : (W <= 17 ? 4 : 2))
+__device__ __forceinline__ void ex_put_pairs(uint8_t *p, const uint32_t (&v)[W], int odd)
+{
+#pragma unroll
+    for (int i = 0; i + 1 < W; i += 2) {
+        const uint32_t even_w = __byte_perm(v[i], v[i + 1], 0x6420);
+        const uint32_t odd_w = __byte_perm(v[i + 1], v[i + 2], 0x6420);
+        *reinterpret_cast<uint32_t *>(p + 2 * (i + odd)) = odd ? odd_w : even_w;
+    }
+    const uint32_t lone = odd ? v[0] : v[W - 1];
+    *reinterpret_cast<uint16_t *>(p + (odd ? 0 : 2 * (W - 1))) = (uint16_t)__byte_perm(lone, 0u, 0x0020);
+}
+
+// Rows r0 .. r0 + 2W - 2 of columns (c, c + 1) from the pair layout, column c
+// in the low 16-bit lane: W word loads, each giving two rows (S = r0 & 1;
+// `p` addresses pair r0 / 2 at column c, PITCH bytes per pair).
+template <int W, int S, int PITCH>
+__device__ __forceinline__ void ex_get_column(const uint8_t *p, uint32_t (&v)[2 * W - 1])
+{
+    uint32_t w[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) w[k] = *reinterpret_cast<const uint32_t *>(p + k * PITCH);
+#pragma unroll
+    for (int j = 0; j < 2 * W - 1; ++j)
+        v[j] = __byte_perm(w[(j + S) >> 1], 0u, ((j + S) & 1) ? 0x4341 : 0x4240);
+}
+
+// Four CTAs per SM up to W = 17 (64 registers: at five CTAs and 48 registers
+// the small windows spilled, and a 2048^2 image puts at most four CTAs on an
+// SM either way); W > 17 needs more registers for its runs.
+template <int W>
+__global__ void __launch_bounds__(256, W <= 17 ? 4 : 2)
 k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int nx, int ny, int a0, int use_fill,
                uint32_t fill, int which)
 {
     using G = ExTile<W>;
     __shared__ __align__(16) uint8_t xin[G::RP * G::CV];
-    __shared__ __align__(16) uint8_t xmn[G::RP * G::TX];
-    __shared__ __align__(16) uint8_t xmx[G::RP * G::TX];
+    // x-pass results by row pairs: byte 2c + h of pair p is column c of row
+    // 2p + h, so one 32-bit word holds two rows of two columns (one pair row
+    // beyond the staged rows: a y run may load the word of its last row's pair)
+    __shared__ __align__(16) uint8_t xmn[(G::RP + 2) * G::TX];
+    __shared__ __align__(16) uint8_t xmx[(G::RP + 2) * G::TX];
     const int tx0 = blockIdx.x * G::TX, ty0 = blockIdx.y * G::TY;
     // The staged window: rows ty0 + a0 .. + RP - 1, columns from tx0 + a0,
     // coordinates clamped to the image (equal to the truncated windows).  A
@@ -815,20 +858,19 @@ k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int n
         uint32_t mn[W], mx[W];
         vhgw_run<W, false>(v, mn);
         vhgw_run<W, true>(v, mx);
+        if (use_fill) {
 #pragma unroll
-        for (int i = 0; i < W; ++i) {
-            if (use_fill) {
+            for (int i = 0; i < W; ++i) {
                 const int x = tx0 + c0 + i;
                 if (x + a0 < 0 || x + a0 + W - 1 > nx - 1) {
                     mn[i] = __vminu2(mn[i], fill2);
                     mx[i] = __vmaxu2(mx[i], fill2);
                 }
             }
-            xmn[r * G::TX + c0 + i] = (uint8_t)mn[i];
-            xmn[(r + 1) * G::TX + c0 + i] = (uint8_t)(mn[i] >> 16);
-            xmx[r * G::TX + c0 + i] = (uint8_t)mx[i];
-            xmx[(r + 1) * G::TX + c0 + i] = (uint8_t)(mx[i] >> 16);
         }
+        const int at = rp * 2 * G::TX + 2 * c0;          // column c0 of the pair (even: TX is)
+        ex_put_pairs<W>(xmn + at, mn, c0 & 1);
+        ex_put_pairs<W>(xmx + at, mx, c0 & 1);
     }
     __syncthreads();
     // y pass: column pairs (c, c+1) x runs of W outputs down
@@ -837,17 +879,12 @@ k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int n
         const int x = tx0 + c;
         if (x >= nx || ty0 + r0 >= ny) continue;
         uint32_t v[2 * W - 1], mn[W], mx[W];
-#pragma unroll
-        for (int j = 0; j < 2 * W - 1; ++j) {
-            const uint16_t q = *reinterpret_cast<const uint16_t *>(xmn + (r0 + j) * G::TX + c);
-            v[j] = __byte_perm((uint32_t)q, 0u, 0x4140);
-        }
+        const int at = (r0 >> 1) * 2 * G::TX + 2 * c;       // 4-byte aligned: c is even
+        if (r0 & 1) ex_get_column<W, 1, 2 * G::TX>(xmn + at, v);
+        else ex_get_column<W, 0, 2 * G::TX>(xmn + at, v);
         vhgw_run<W, false>(v, mn);
-#pragma unroll
-        for (int j = 0; j < 2 * W - 1; ++j) {
-            const uint16_t q = *reinterpret_cast<const uint16_t *>(xmx + (r0 + j) * G::TX + c);
-            v[j] = __byte_perm((uint32_t)q, 0u, 0x4140);
-        }
+        if (r0 & 1) ex_get_column<W, 1, 2 * G::TX>(xmx + at, v);
+        else ex_get_column<W, 0, 2 * G::TX>(xmx + at, v);
         vhgw_run<W, true>(v, mx);
         const bool two = x + 1 < nx;
 #pragma unroll
