@@ -689,15 +689,19 @@ template <int W> struct ExTile {
     // runs per row: a multiple of 4, so that the tile width is (the y pass
     // takes four columns per word, and their stores align)
     static constexpr int NRX = ((128 + W - 1) / W + 1) & ~1;
-    // runs per column: tiles about 64 tall (about 32 for W > 17, whose
-    // staging would pass the 48 KB of static shared memory)
-    static constexpr int NRY = ((W <= 17 ? 64 : 32) + W / 2) / W;
+    // runs per column: tiles about 32 tall (2048^2, 15 x 15: 18.4 us with
+    // 60-row tiles, 16.8-17.3 with 30-row ones, whose 966 CTAs spread more
+    // evenly over the SMs than 490 do; 80-row tiles were slower still)
+    static constexpr int NRY = (32 + W / 2) / W;
     static constexpr int TX = W * NRX, TY = W * NRY;
     static constexpr int R = TY + W - 1, C = TX + W - 1;
     static constexpr int RP = (R + 1) & ~1;                    // rows staged (even: row pairs)
     static constexpr int CP = (C + 3) & ~3;
     static constexpr int NV = (C + 30) / 16;                   // 16-byte vectors of a row's aligned superset
-    static constexpr int CV = 16 * NV;                         // staged row pitch (bytes)
+    static constexpr int CV = 16 * NV;                         // bytes staged per row
+    // staged row pitch: an odd number of 16-byte vectors, so that the rows of
+    // the four row pairs one warp reads in the x pass fall in different banks
+    static constexpr int XP = 16 * (NV | 1);
 };
 
 // Van Herk / Gil-Werman over a run: out[i] = op over v[i .. i+W-1], i < W,
@@ -751,15 +755,15 @@ __device__ __forceinline__ void ex_get_column(const uint8_t *p, uint32_t (&v)[2 
 }
 
 // Four CTAs per SM up to W = 17 (64 registers: at five CTAs and 48 registers
-// the small windows spilled, and a 2048^2 image puts at most four CTAs on an
-// SM either way); W > 17 needs more registers for its runs.
+// the small windows spilled and ran slower); W > 17 needs more registers for
+// its runs.
 template <int W>
 __global__ void __launch_bounds__(256, W <= 17 ? 4 : 2)
 k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int nx, int ny, int a0, int use_fill,
                uint32_t fill, int which)
 {
     using G = ExTile<W>;
-    __shared__ __align__(16) uint8_t xin[G::RP * G::CV];
+    __shared__ __align__(16) uint8_t xin[G::RP * G::XP];
     // x-pass results by row pairs: byte 2c + h of pair p is column c of row
     // 2p + h, so one 32-bit word holds two rows of two columns (one pair row
     // beyond the staged rows: a y run may load the word of its last row's pair)
@@ -796,7 +800,7 @@ k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int n
                 const int it = base + q * blockDim.x;
                 if (it < TOT) {
                     const int r = it / G::NV, k = it - r * G::NV;
-                    *reinterpret_cast<uint4 *>(xin + r * G::CV + 16 * k) = v[q];
+                    *reinterpret_cast<uint4 *>(xin + r * G::XP + 16 * k) = v[q];
                 }
             }
         }
@@ -826,7 +830,7 @@ k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int n
 #pragma unroll
                 for (int k = 0; k < kChunks; ++k) {
                     const int r = r0 + q * nw, c = 4 * lane + 128 * k;
-                    if (r < G::RP && c < G::CP) *reinterpret_cast<uint32_t *>(xin + r * G::CV + c) = word[q][k];
+                    if (r < G::RP && c < G::CP) *reinterpret_cast<uint32_t *>(xin + r * G::XP + c) = word[q][k];
                 }
         }
     }
@@ -841,8 +845,8 @@ k_extrema2d_u8(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int n
         uint32_t ra[NWD], rb[NWD];
 #pragma unroll
         for (int q = 0; q < NWD; ++q) {
-            ra[q] = a + 4 * q < G::CV ? *reinterpret_cast<const uint32_t *>(xin + r * G::CV + a + 4 * q) : 0u;
-            rb[q] = a + 4 * q < G::CV ? *reinterpret_cast<const uint32_t *>(xin + (r + 1) * G::CV + a + 4 * q) : 0u;
+            ra[q] = a + 4 * q < G::CV ? *reinterpret_cast<const uint32_t *>(xin + r * G::XP + a + 4 * q) : 0u;
+            rb[q] = a + 4 * q < G::CV ? *reinterpret_cast<const uint32_t *>(xin + (r + 1) * G::XP + a + 4 * q) : 0u;
         }
         // realigned so that byte j is byte j % 4 of word j / 4 (compile-time indices)
         uint32_t al[NWD - 1], bl[NWD - 1];
