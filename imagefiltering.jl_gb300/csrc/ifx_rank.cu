@@ -702,6 +702,12 @@ template <int W> struct ExTile {
     // staged row pitch: an odd number of 16-byte vectors, so that the rows of
     // the four row pairs one warp reads in the x pass fall in different banks
     static constexpr int XP = 16 * (NV | 1);
+    // the pair layout's 32-bit accesses are 4-byte aligned when a pair row is
+    static_assert(TX % 2 == 0, "tile width must be even");
+    // the y pass's last run loads pairs up to (r0 >> 1) + W - 1; RP / 2 + 1 pairs are allocated
+    static_assert(((NRY - 1) * W) / 2 + W - 1 < RP / 2 + 1, "y runs stay inside the pair rows");
+    // staging and both pair arrays are static shared memory (48 KB at most)
+    static_assert(RP * XP + 2 * (RP + 2) * TX <= 48 * 1024, "tile exceeds static shared memory");
 };
 
 // Van Herk / Gil-Werman over a run: out[i] = op over v[i .. i+W-1], i < W,
