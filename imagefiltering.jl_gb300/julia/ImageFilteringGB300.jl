@@ -327,4 +327,112 @@ function ImageFiltering.mapwindow(r::CPU1{GB300}, f::Union{typeof(median!),typeo
     out
 end
 
+ifxborder(b, ::Type) = throw(ArgumentError("GB300: borders of type $(typeof(b)) are not taken here"))
+
+# An array of Tuple{E,E} (min, max) pairs as ifx_mapwindow_extrema writes it:
+# eltype E, strides counted in pairs.
+function pairout(A::AbstractArray{<:Tuple,N}, ::Type{E}) where {N,E}
+    P = parent(A)
+    IfxArray(Ptr{Cvoid}(pointer(P)), eltcode(E), Int32(N), pad4(size(A), 1), pad4(strides(P), 0),
+             pad4(map(first, axes(A)), 1))
+end
+# The same pairs as the (2, size...) array of their values, element type C.
+function pairvalues(A::AbstractArray{<:Tuple,N}, ::Type{C}) where {N,C}
+    N <= 3 || throw(ArgumentError("GB300: at most 3 dimensions here"))
+    P = parent(A)
+    IfxArray(Ptr{Cvoid}(pointer(P)), eltcode(C), Int32(N + 1), pad4((2, size(A)...), 1),
+             pad4((1, map(s -> 2s, strides(P))...), 0), pad4((1, map(first, axes(A))...), 1))
+end
+
+codetype(::Type{T}) where {T} = T
+codetype(::Type{<:Union{N0f16,Gray{N0f16}}}) = UInt16
+
+# mapwindow(extrema / minimum / maximum, img, window; border) ->
+# ifx_mapwindow_extrema.  Without a border keyword extrema is the reference's
+# Lemire filter (src/mapwindow.jl:337-338: truncated windows, even lengths
+# allowed); with one, or for minimum / maximum, the generic window path
+# (src/mapwindow.jl:270-333, default border "replicate").
+function ImageFiltering.mapwindow(r::CPU1{GB300}, f::Union{typeof(extrema),typeof(minimum),typeof(maximum)},
+                                  img::AbstractArray{T,N}, window::Dims{N}; border=nothing) where {T,N}
+    which = f === extrema ? Int32(0) : f === minimum ? Int32(1) : Int32(2)
+    native(T) || return extrema_converted(r, f, img, window, border, which)
+    lemire = which == 0 && border === nothing
+    lemire || all(isodd, window) || error("entries in window must be odd, got $window")
+    b = border === nothing ? ImageFiltering.borderinstance("replicate") :
+        border isa AbstractString ? ImageFiltering.borderinstance(border) : border
+    bref = Ref(ifxborder(b, T))
+    out = similar(img, which == 0 ? Tuple{T,T} : T)
+    o = which == 0 ? pairout(out, T) : ifxarray(out)
+    GC.@preserve out img bref begin
+        bp = lemire ? Ptr{IfxBorder}(C_NULL) : Base.unsafe_convert(Ptr{IfxBorder}, bref)
+        check(ccall((:ifx_mapwindow_extrema, libifx), Cint,
+                    (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Ref{NTuple{4,Int64}}, Ref{NTuple{4,Int64}},
+                     Ptr{IfxBorder}, Int32, Ptr{Cvoid}),
+                    context(), Ref(o), Ref(ifxarray(img)), pad4(map(w -> -(w >> 1), window), 0), pad4(window, 1),
+                    bp, which, C_NULL))
+    end
+    out
+end
+
+# Extrema of eltypes the kernels do not read: the values (N0f16: the codes,
+# whose order is the values') converted exactly to Float64 on the GPU,
+# filtered there, and converted back to the image's eltype.
+function extrema_converted(r, f, img::AbstractArray{T,N}, window, border, which) where {T,N}
+    C = codetype(T)
+    T === Int64 && any(x -> abs(x) >= 2^53, img) &&
+        throw(ArgumentError("GB300: Int64 rank filters with values beyond 2^53"))
+    tmp = ifxconvert!(similar(img, Float64), C === T ? img : reinterpret(C, img))
+    res = if border === nothing
+        mapwindow(r, f, tmp, window)
+    else
+        bi = border isa AbstractString ? ImageFiltering.borderinstance(border) : border
+        b = bi isa Fill ? Fill(Float64(reinterpret(C, convert(T, bi.value))), bi.lo, bi.hi) : bi
+        mapwindow(r, f, tmp, window; border=b)
+    end
+    out = similar(img, which == 0 ? Tuple{T,T} : T)
+    if which == 0
+        GC.@preserve out res begin
+            check(ccall((:ifx_convert, libifx), Cint, (Ptr{Cvoid}, Ref{IfxArray}, Ref{IfxArray}, Ptr{Cvoid}),
+                        context(), Ref(pairvalues(out, C)), Ref(pairvalues(res, Float64)), C_NULL))
+        end
+    else
+        ifxconvert!(C === T ? out : reinterpret(C, out), res)
+    end
+    out
+end
+
+# ---------------------------------------------------------------- imgradients
+# imgradients has no Alg hook; this method takes the resource first.  When the
+# kernel function's derivative and smoothing factors share their length and
+# first index (sobel, prewitt, ando3/4/5, scharr, bickley), every gradient
+# comes from one sweep (ifx_imgradients); otherwise each gradient is one
+# GB300 imfilter, as the reference computes them (src/specialty.jl:39-53).
+function ImageFiltering.imgradients(r::CPU1{GB300}, img::AbstractArray{T,N}, kernelfun::Function,
+                                    border="replicate") where {T,N}
+    extended = map(ImageFiltering.isextended, axes(img))
+    kerns = ntuple(d -> kernelfun(extended, d), N)
+    ax = findall(collect(extended))
+    b = border isa AbstractString ? ImageFiltering.borderinstance(border) : border
+    fused = native(T) && !isempty(ax) && b isa Union{Pad,Fill}
+    if fused
+        d1 = ax[1]
+        e = length(ax) > 1 ? ax[2] : d1
+        kd, ks = kerns[d1][d1].data, kerns[d1][e].data
+        deriv, smooth = collect(Float64, parent(kd)), collect(Float64, parent(ks))
+        f1 = first(axes(kd, 1))
+        fused = length(smooth) == length(deriv) && first(axes(ks, 1)) == f1
+    end
+    fused || return ntuple(d -> imfilter(r, img, kerns[d], border), N)
+    outs = ntuple(d -> similar(img, ImageFiltering.filter_type(img, kerns[d])), N)
+    descs = [ifxarray(o) for o in outs]
+    GC.@preserve outs img deriv smooth descs begin
+        check(ccall((:ifx_imgradients, libifx), Cint,
+                    (Ptr{Cvoid}, Ptr{IfxArray}, Ref{IfxArray}, Ptr{Float64}, Ptr{Float64}, Int32, Int64,
+                     Ref{NTuple{4,Int32}}, Ref{IfxBorder}, Ptr{Cvoid}),
+                    context(), descs, Ref(ifxarray(img)), deriv, smooth, Int32(length(deriv)), Int64(f1),
+                    map(Int32, pad4(map(Int, extended), 0)), ifxborder(b, T), C_NULL))
+    end
+    outs
+end
+
 end # module
