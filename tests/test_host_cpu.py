@@ -118,6 +118,50 @@ def test_julia_binding_matches_the_c_abi(lib):
             assert _jl_kind(a) == _c_kind(c), (name, a, c)
 
 
+def _c_fields(hdr, tag):
+    """(kind, count) of each field of `typedef struct tag { ... }`."""
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    body = re.search(r"typedef struct " + tag + r"\s*\{(.*?)\}", hdr, re.S).group(1)
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        m = re.match(r"((?:const\s+)?\w+\s*\**)\s*(.*)", decl)
+        ctype, names = m.group(1), m.group(2)
+        for nm in _split_top(names):
+            n = re.search(r"\[(\w+)\]", nm)
+            count = {"IFX_MAX_DIMS": 4}.get(n.group(1), None) if n else 1
+            if n and count is None:
+                count = int(n.group(1))
+            kind = "ptr" if "*" in ctype + nm.split("[")[0] else _c_kind(ctype + " ")
+            out.append((kind, count))
+    return out
+
+
+def _jl_fields(jl, name):
+    body = re.search(r"struct " + name + r"\n(.*?)\nend", jl, re.S).group(1)
+    out = []
+    for line in body.splitlines():
+        line = line.split("#")[0].strip()
+        if not line:
+            continue
+        t = line.split("::", 1)[1].strip()
+        m = re.match(r"NTuple\{(\d+),\s*(\w+)\}", t)
+        out.append((_jl_kind(m.group(2)), int(m.group(1))) if m else (_jl_kind(t), 1))
+    return out
+
+
+def test_julia_binding_structs_match_the_c_abi():
+    """The Julia mirrors of the C structs have the C fields in order: the same
+    kinds and array lengths (so the same layout under C alignment rules)."""
+    jl = open(os.path.join(ROOT, "imagefiltering.jl_gb300", "julia", "ImageFilteringGB300.jl")).read()
+    hdr = open(os.path.join(ROOT, "include", "ifx_gb300.h")).read()
+    for jname, ctag in (("IfxArray", "ifx_array"), ("IfxBorder", "ifx_border"), ("IfxFactor", "ifx_factor"),
+                        ("IfxIir", "ifx_iir")):
+        assert _jl_fields(jl, jname) == _c_fields(hdr, ctag), jname
+
+
 def _arr(ifx, a, kind):
     p = a.ctypes.data
     return ifx._abi.describe(p, kind, a.shape, [s // a.itemsize for s in a.strides])
